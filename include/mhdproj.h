@@ -1,0 +1,218 @@
+/*
+ * mhdproj.h -- C ABI of the GB300 MAC pressure projection.
+ *
+ * Drop-in replacement for the projection of sdfgeoff/mhd-simulator's fluid
+ * solver: FluidState::project(warm_start) -> Result<(u32, f32), String>
+ * (src/fluid/mod.rs:1015-1115) together with the coefficient cache it builds
+ * (pressure_coefficients, src/fluid/solver.wgsl:93-103), the gauge selection
+ * (configure_pressure_projection and anchors, src/fluid/mod.rs:978-1002 and
+ * :1447-1493) and the pressure written by `fields` (p = rho_l * phi / dt,
+ * src/fluid/solver.wgsl:269-270).  The reference's method is private Rust on
+ * wgpu buffers; this header is the FFI boundary a Rust crate would bind
+ * instead.
+ *
+ * Conventions
+ *  - Cells are indexed x-fastest: i = x + nx*(y + ny*z) (src/simulation.rs:319-323).
+ *  - Face velocities are three SoA arrays of FP32 with shapes
+ *      u: (nx+1) x ny x nz,  v: nx x (ny+1) x nz,  w: nx x ny x (nz+1)
+ *    (x-fastest).  The reference packs the three components into one vec4
+ *    per (n+1)^3 face-cell (solver.wgsl:33-36); only the parity tests convert.
+ *    On a periodic axis the last face duplicates face 0: inputs are read at
+ *    face 0, outputs are written to both.
+ *  - Every pointer argument of the compute entry points is a DEVICE pointer
+ *    unless the function name ends in _host.  The context owns its workspace.
+ *  - Return value 0 is success; otherwise an mhdproj_status code, with a
+ *    message from mhdproj_last_error().  A context is used by one host thread
+ *    at a time and issues all work on its own CUDA stream.
+ */
+#ifndef MHDPROJ_H
+#define MHDPROJ_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mhdproj_ctx mhdproj_ctx;
+
+typedef enum {
+    MHDPROJ_OK = 0,
+    MHDPROJ_ERR_INVALID = 1,        /* bad argument or configuration */
+    MHDPROJ_ERR_CUDA = 2,           /* CUDA runtime error */
+    MHDPROJ_ERR_NOT_CONVERGED = 3,  /* "Fluid pressure solve did not converge after N iterations" */
+    MHDPROJ_ERR_NONFINITE = 4,      /* "Nonfinite fluid pressure residual" */
+    MHDPROJ_ERR_NO_PROGRESS = 5,    /* "Fluid pressure iteration made no progress" */
+    MHDPROJ_ERR_STATE = 6,          /* call order (e.g. project before set_coefficients) */
+    MHDPROJ_ERR_OUT_OF_MEMORY = 7,  /* workspace does not fit */
+    MHDPROJ_ERR_TIMEOUT = 8         /* a bounded host wait on the device expired */
+} mhdproj_status;
+
+typedef enum {
+    /* Closed domain as in the reference: walls and solid faces are closed,
+       the constant null space is fixed by a pinned cell per component or by
+       mean-free residuals for a single component (src/fluid/mod.rs:978-1002). */
+    MHDPROJ_BOUNDARY_REFERENCE_CLOSED = 0,
+    /* Dirichlet p = 0 on the top z-face (a GB300-path extension). */
+    MHDPROJ_BOUNDARY_OUTLET_TOP = 1
+} mhdproj_boundary;
+
+typedef enum {
+    MHDPROJ_PRECISION_FP32 = 0,     /* multigrid level fields in FP32 */
+    MHDPROJ_PRECISION_FP16 = 1,     /* multigrid level fields in FP16, FP32 accumulation */
+    MHDPROJ_PRECISION_BF16 = 2      /* multigrid level fields in BF16, FP32 accumulation */
+} mhdproj_precision;
+
+typedef enum {
+    /* The reference algorithm, FP32 throughout: Jacobi-CG below 96^3 cells,
+       aggregation-multigrid CG at or above (src/fluid/mod.rs:1030-1096,
+       src/fluid/multigrid.rs), with the reference's convergence tests. */
+    MHDPROJ_SOLVER_REFERENCE = 0,
+    /* The GB300 path: CG preconditioned by a red-black Gauss-Seidel
+       aggregation V-cycle with exact coarse solve, FP64 reductions, FP64
+       refinement residual on the finest level. */
+    MHDPROJ_SOLVER_GB300 = 1
+} mhdproj_solver;
+
+typedef enum {
+    MHDPROJ_PRECOND_AUTO = -1,      /* reference: by the 96^3 rule; GB300: RBGS multigrid */
+    MHDPROJ_PRECOND_JACOBI = 0,
+    MHDPROJ_PRECOND_MULTIGRID = 1
+} mhdproj_preconditioner;
+
+typedef struct {
+    uint32_t nx, ny, nz;
+    float h;                /* cell size in metres (GridSi::cell_m) */
+    uint32_t periodic;      /* bit a set: axis a is periodic (FluidConfig::periodic) */
+    int32_t boundary;       /* mhdproj_boundary */
+} mhdproj_grid;
+
+typedef struct {
+    int32_t solver;         /* mhdproj_solver */
+    int32_t precision;      /* mhdproj_precision (GB300 solver) */
+    int32_t preconditioner; /* mhdproj_preconditioner */
+    float rel_tol;          /* FluidConfig::relative_tolerance */
+    float abs_div_tol;      /* FluidConfig::absolute_divergence_tolerance, 1/s */
+    uint32_t max_iterations;/* FluidConfig::max_iterations (all refinement passes) */
+    int32_t max_refinements;/* GB300 solver: FP64 refinement passes (>= 1) */
+    int32_t two_phase;      /* reference solver: SurfaceConfig::enabled (density from the liquid fraction) */
+    int32_t gauge;          /* reference solver: -1 automatic, 0 pinned cells, 1 mean-free if connected */
+    int32_t compute_divergence; /* fill max/RMS divergence of the projected velocity in the stats */
+} mhdproj_options;
+
+typedef struct {
+    uint32_t iterations;        /* CG iterations, all passes */
+    uint32_t refinements;       /* FP64 residual evaluations after the first (GB300 solver) */
+    float relative_residual;    /* reference: sqrt(s[1]/s[2]) of the final check; GB300: FP64 true residual */
+    double true_relative_residual; /* ||b - A phi|| / ||b|| evaluated in FP64 */
+    double max_divergence;      /* max |div u| over active cells, 1/s (if requested) */
+    double rms_divergence;
+    float elapsed_ms;           /* device time of the call */
+    int32_t meanfree;           /* reference solver: gauge mode used */
+    int32_t multigrid;          /* preconditioner used */
+    uint32_t levels;            /* multigrid levels */
+    uint64_t coarse_cells;      /* cells on levels >= 1 */
+} mhdproj_stats;
+
+/* Defaults: GB300 solver, FP16 levels, rel_tol 1e-6, abs floor 0, 20000 iterations. */
+void mhdproj_default_options(mhdproj_options *options);
+
+/* FluidState::new's projection set-up (src/fluid/mod.rs:199-330).  Validates the
+ * grid and options and allocates the workspace. */
+int mhdproj_create(const mhdproj_grid *grid, const mhdproj_options *options, mhdproj_ctx **out);
+
+/* Release the context and its device memory. */
+void mhdproj_destroy(mhdproj_ctx *ctx);
+
+/* Message of the last failing call on ctx ("" if none).  ctx may be NULL for
+ * errors of mhdproj_create. */
+const char *mhdproj_last_error(const mhdproj_ctx *ctx);
+
+/* Issue all work on this cudaStream_t (default: a stream the context owns). */
+int mhdproj_set_stream(mhdproj_ctx *ctx, void *stream);
+
+/* Mobility inputs (pressure_coefficients, solver.wgsl:93-103, with mobility()
+ * :43-51): liquid fraction per cell (FluidCell.reserved.z) and a solid mask
+ * (nonzero = wall cell), plus the liquid and ambient densities.  The fluid
+ * mask is every non-solid cell.  The connected components and gauges
+ * (anchors(), src/fluid/mod.rs:1447-1493) are recomputed only when the solid
+ * mask differs from the previous call, as FluidState::update_cells does. */
+int mhdproj_set_coefficients(mhdproj_ctx *ctx, const float *alpha, const uint8_t *solid, float rho_liquid,
+                             float rho_air);
+
+/* Reference solver only: the thermal phase-fraction drag of mobility()
+ * (solver.wgsl:46-50), beta / (1 + dt * rate (1-f)^2 / (f^3 + 1e-3)) with f the
+ * smaller phase fraction (FluidCell.reserved.y) of the two cells.  Pass
+ * phase = NULL to disable.  Takes effect at the next mhdproj_set_coefficients. */
+int mhdproj_set_phase_drag(mhdproj_ctx *ctx, const float *phase, float drag_rate, float dt);
+
+/* FluidState::project + correct (src/fluid/mod.rs:1015-1115, solver.wgsl:245-250):
+ * project the candidate face velocities u_star onto discretely divergence-free
+ * fields.  u_out may alias u_star.  p_out (may be NULL) receives the pressure
+ * rho_l * phi / dt per cell (0 in solid cells).  warm_start reuses the previous
+ * call's pressure: the reference's pressure_warm/pressure_commit (:164-184) in
+ * the reference solver, the previous potential as the initial guess in the
+ * GB300 solver.  On failure the outputs are not written. */
+int mhdproj_project(mhdproj_ctx *ctx, const float *u_star_x, const float *u_star_y, const float *u_star_z,
+                    float *u_out_x, float *u_out_y, float *u_out_z, float *p_out, float dt, int warm_start,
+                    mhdproj_stats *stats);
+
+/* The same call on HOST buffers: copies alpha, solid and u_star to the device,
+ * sets the coefficients, projects, and copies u_out and p_out back. */
+int mhdproj_project_host(mhdproj_ctx *ctx, const float *alpha, const uint8_t *solid, float rho_liquid,
+                         float rho_air, const float *u_star_x, const float *u_star_y, const float *u_star_z,
+                         float *u_out_x, float *u_out_y, float *u_out_z, float *p_out, float dt, int warm_start,
+                         mhdproj_stats *stats);
+
+/* Vector-Jacobian product of the projection with the current coefficients
+ * (GB300 solver): given dL/du_out (faces) and dL/dp_out (cells, may be NULL)
+ * return dL/du_star.  One adjoint CG solve with the same symmetric operator,
+ * then the transposed divergence.  torch.autograd.Function.backward contract. */
+int mhdproj_project_vjp(mhdproj_ctx *ctx, const float *grad_u_x, const float *grad_u_y, const float *grad_u_z,
+                        const float *grad_p, float dt, float *grad_us_x, float *grad_us_y, float *grad_us_z,
+                        mhdproj_stats *stats);
+
+/* Chain u_{k+1} = P(u_k + dt f / rho_face) for `steps` steps from u0 with a
+ * fixed face force f (N/m^3); objective J = sum of w^2 over the outlet faces of
+ * the final state.  States are checkpointed every `checkpoint_every` steps.
+ * The final state is written to u_final (device).  */
+int mhdproj_chain_forward(mhdproj_ctx *ctx, const float *u0_x, const float *u0_y, const float *u0_z,
+                          const float *f_x, const float *f_y, const float *f_z, float dt, int steps,
+                          int checkpoint_every, float *uf_x, float *uf_y, float *uf_z, double *objective,
+                          mhdproj_stats *stats);
+/* dJ/df of the last mhdproj_chain_forward, by the adjoint chain. */
+int mhdproj_chain_backward(mhdproj_ctx *ctx, float *grad_f_x, float *grad_f_y, float *grad_f_z,
+                           mhdproj_stats *stats);
+
+/* Probes used by the tests.  y = A x with the solver's operator (reference:
+ * apply() of solver.wgsl:78-92 on the cached coefficients, pinned cells as
+ * identity rows); z = M r with the solver's preconditioner (reference: the
+ * fixed V-cycle of multigrid.wgsl, or r/diag for Jacobi).  x, y, r, z are
+ * FP32 device arrays of nx*ny*nz cells. */
+int mhdproj_apply_operator(mhdproj_ctx *ctx, const float *x, float *y);
+int mhdproj_apply_preconditioner(mhdproj_ctx *ctx, const float *r, float *z);
+/* Copy the fine coefficient cache, 4 floats per cell (device pointer):
+ * reference solver (beta_x, beta_y, beta_z of the low faces, diagonal) as in
+ * velocity[i] of pressure_coefficients; GB300 solver (beta_x, beta_y, beta_z,
+ * reaction of outlet and pinned-cell edges). */
+int mhdproj_copy_coefficients(mhdproj_ctx *ctx, float *coef4);
+/* Copy the last solution potential phi (FP64 device array of nx*ny*nz). */
+int mhdproj_copy_potential(mhdproj_ctx *ctx, double *phi);
+/* Cell classes after the last topology change (host array of nx*ny*nz):
+ * reference solver: the encoded mask of anchors(); GB300 solver: 0 solid,
+ * 1 active, 2 pinned gauge cell.  Returns the number of components. */
+int mhdproj_copy_topology(mhdproj_ctx *ctx, uint32_t *mask_host, uint32_t *components);
+
+/* Host utilities, mirroring src/fluid/multigrid.rs:25-65 and src/fluid/mod.rs:1447-1493. */
+/* Aggregation hierarchy: halve (ceil) until every dimension is <= 4.  Returns
+ * 0 and the level count / coarse-cell total, or MHDPROJ_ERR_INVALID for zero,
+ * overflowing or out-of-range dimensions. */
+int mhdproj_hierarchy(const uint32_t dims[4], uint32_t *levels, uint64_t *coarse_cells);
+/* Connected components of a 0/1 fluid mask with one root per component;
+ * encodes mask[i] = class | root << 2 (class 1 member, 2 root).  Returns the
+ * component count. */
+uint32_t mhdproj_anchors(uint32_t *mask, const uint32_t dims[3], uint32_t periodic);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

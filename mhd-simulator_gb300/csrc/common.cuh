@@ -1,0 +1,181 @@
+// common.cuh -- shared device helpers for the GB300 projection kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace mhdproj {
+
+// Tiles: 32 x 8 threads over (x, y); each thread walks a run of z.
+constexpr int TX = 32;
+constexpr int TY = 8;
+constexpr int TILE_THREADS = TX * TY;
+// Upper bound on blocks of a reduction launch (the partials arrays are sized by it).
+constexpr int MAX_REDUCE_BLOCKS = 8192;
+
+struct Grid3 {
+    int nx, ny, nz;
+    int periodic;  // bit a: axis a periodic
+    int zper;      // z cells per block (tile launches)
+    __host__ __device__ long long n() const { return (long long)nx * ny * nz; }
+};
+
+// Device scalar block of the CG solver.  Written only by last-block
+// reductions (single writer) and read by every kernel of the iteration.
+struct Scalars {
+    double bb;          // ||b||^2 (FP64)
+    double rr_true;     // ||b - A phi||^2 of the last refinement residual
+    double rr;          // inner ||r||^2
+    double rr_target;   // inner stop threshold on ||r||^2
+    double rz;          // r . z (preconditioned)
+    double pq;          // p . A p
+    double alpha, beta; // CG scalars
+    double abs_floor;   // absolute floor on ||r||^2 (reference abs_div_tol term)
+    double tol2;        // relative tolerance squared
+    double inner_floor2;// minimum inner relative reduction squared
+    double objective;   // chain objective / misc reductions
+    double divmax, div2;// divergence statistics
+    float alpha_f, beta_f, sigma, inv_sigma;
+    int converged;      // inner solve finished
+    int outer_done;     // true residual meets the target
+    int iterations;     // inner iterations of this solve
+    int total_iterations;
+    int nonfinite;      // a reduction produced NaN/Inf
+    int breakdown;      // p.Ap <= 0
+    unsigned int ticket[8];
+};
+
+// ------------------------------------------------------------ indexing
+__device__ __forceinline__ int wrap_or_neg(int c, int n, bool periodic) {
+    if (c < 0) return periodic ? c + n : -1;
+    if (c >= n) return periodic ? c - n : -1;
+    return c;
+}
+
+// ------------------------------------------------ rounding-explicit FP32
+// The mobility is computed with an operation order shared with the CPU
+// oracle; explicit intrinsics stop the compiler from fusing multiply-adds.
+__device__ __forceinline__ float rho_of(float a, float rho_l, float rho_air) {
+    return __fadd_rn(__fmul_rn(rho_air, __fsub_rn(1.0f, a)), __fmul_rn(rho_l, a));
+}
+__device__ __forceinline__ float beta_of(float aL, float aR, float rho_l, float rho_air) {
+    return __fdiv_rn(rho_l, __fmul_rn(0.5f, __fadd_rn(rho_of(aL, rho_l, rho_air), rho_of(aR, rho_l, rho_air))));
+}
+__device__ __forceinline__ float outlet_conductance(float a, float rho_l, float rho_air) {
+    return __fmul_rn(2.0f, __fdiv_rn(rho_l, rho_of(a, rho_l, rho_air)));
+}
+
+// ------------------------------------------------------ storage types
+struct CoefF32 { using store = float4; };
+struct CoefF16 { using store = uint2; };
+struct CoefBF16 { using store = uint2; };
+
+__device__ __forceinline__ float4 load_coef(const float4* p, long long i) { return __ldg(p + i); }
+__device__ __forceinline__ float4 load_coef_h(const uint2* p, long long i) {
+    uint2 u = __ldg(p + i);
+    __half2 a = *reinterpret_cast<__half2*>(&u.x), b = *reinterpret_cast<__half2*>(&u.y);
+    float2 fa = __half22float2(a), fb = __half22float2(b);
+    return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+__device__ __forceinline__ float4 load_coef_b(const uint2* p, long long i) {
+    uint2 u = __ldg(p + i);
+    __nv_bfloat162 a = *reinterpret_cast<__nv_bfloat162*>(&u.x), b = *reinterpret_cast<__nv_bfloat162*>(&u.y);
+    float2 fa = __bfloat1622float2(a), fb = __bfloat1622float2(b);
+    return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+__device__ __forceinline__ uint2 pack_coef_h(float4 c) {
+    __half2 a = __floats2half2_rn(c.x, c.y), b = __floats2half2_rn(c.z, c.w);
+    uint2 u;
+    u.x = *reinterpret_cast<unsigned*>(&a);
+    u.y = *reinterpret_cast<unsigned*>(&b);
+    return u;
+}
+__device__ __forceinline__ uint2 pack_coef_b(float4 c) {
+    __nv_bfloat162 a = __floats2bfloat162_rn(c.x, c.y), b = __floats2bfloat162_rn(c.z, c.w);
+    uint2 u;
+    u.x = *reinterpret_cast<unsigned*>(&a);
+    u.y = *reinterpret_cast<unsigned*>(&b);
+    return u;
+}
+
+// Scalar vector element types.
+__device__ __forceinline__ float to_f(float v) { return v; }
+__device__ __forceinline__ float to_f(__half v) { return __half2float(v); }
+__device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
+template <class T> __device__ __forceinline__ T from_f(float v);
+template <> __device__ __forceinline__ float from_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ __half from_f<__half>(float v) { return __float2half_rn(v); }
+template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+
+// ------------------------------------------------------- reductions
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide sum of K doubles (blockDim.x*y*z == 256); the result is valid in
+// thread 0.  Uses the caller's shared buffer of 8*K doubles.
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K], double* sh) {
+    const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int lane = t & 31, warp = t >> 5;
+#pragma unroll
+    for (int k = 0; k < K; k++) v[k] = warp_sum(v[k]);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < K; k++) sh[warp * K + k] = v[k];
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x * blockDim.y * blockDim.z) >> 5;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            double s = lane < nw ? sh[lane * K + k] : 0.0;
+            v[k] = warp_sum(s);
+        }
+    }
+    __syncthreads();
+}
+
+// Store this block's K partial sums; returns true in the block that arrives
+// last (threadFenceReduction pattern).  `partials` is laid out [K][nblocks].
+template <int K>
+__device__ __forceinline__ bool store_partials_is_last(const double (&v)[K], double* partials, int nblocks,
+                                                       unsigned int* ticket) {
+    __shared__ bool last;
+    const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    if (t == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) partials[k * nblocks + b] = v[k];
+        __threadfence();
+        unsigned int arrived = atomicAdd(ticket, 1u);
+        last = arrived == (unsigned)(nblocks - 1);
+    }
+    __syncthreads();
+    return last;
+}
+
+// In the last block: sum the partials in a fixed order (deterministic), the
+// total is returned in thread 0; resets the ticket for the next launch.
+template <int K>
+__device__ __forceinline__ void finish_partials(double (&tot)[K], const double* partials, int nblocks, double* sh,
+                                                unsigned int* ticket) {
+    __threadfence();
+    const int t = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nt = blockDim.x * blockDim.y * blockDim.z;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        double s = 0.0;
+        for (int b = t; b < nblocks; b += nt) s += ((volatile const double*)partials)[k * nblocks + b];
+        tot[k] = s;
+    }
+    block_sum<K>(tot, sh);
+    if (t == 0) *ticket = 0u;
+}
+
+}  // namespace mhdproj

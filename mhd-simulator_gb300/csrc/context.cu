@@ -1,0 +1,894 @@
+// context.cu -- the C ABI of mhdproj.h: context lifetime, topology, the GB300
+// solver's CG/refinement driver, the adjoint and the chained projection.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/mhdproj.h"
+#include "kernels.h"
+#include "reference.h"
+#include "topology.h"
+
+using namespace mhdproj;
+
+static thread_local std::string g_create_error;
+
+struct mhdproj_ctx {
+    mhdproj_grid grid{};
+    mhdproj_options opt{};
+    std::string err;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    long long n = 0;
+    long long nfx = 0, nfy = 0, nfz = 0;
+    int outlet = 0;
+    Launch L{};
+    std::vector<void*> allocs;
+    // topology and coefficients
+    uint8_t* d_solid_prev = nullptr;
+    uint8_t* d_cls = nullptr;
+    int* d_flag = nullptr;
+    int* h_flag = nullptr;
+    std::vector<uint8_t> h_solid;
+    std::vector<uint8_t> h_cls;
+    std::vector<uint32_t> h_mask;
+    uint32_t components = 0, pinned = 0;
+    long long n_active = 0;
+    bool have_topology = false, have_coef = false;
+    float* alpha = nullptr;
+    float4* coef = nullptr;
+    void* coef_lo = nullptr;
+    float* gtop = nullptr;
+    float rho_l = 0.f, rho_air = 0.f;
+    // solver state
+    double *b64 = nullptr, *phi64 = nullptr, *psi64 = nullptr;
+    float *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *e = nullptr, *ztmp = nullptr;
+    Scalars* sc = nullptr;
+    Scalars* h_sc = nullptr;
+    double* partials = nullptr;
+    MGPlan mg{};
+    bool use_mg = false;
+    cudaGraphExec_t it_graph = nullptr;
+    bool graph_failed = false;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_sync = nullptr;
+    bool have_solution = false;
+    // host-buffer staging
+    float *s_alpha = nullptr, *s_u = nullptr, *s_v = nullptr, *s_w = nullptr, *s_p = nullptr;
+    uint8_t* s_solid = nullptr;
+    // chain
+    float *c_cur[3] = {nullptr, nullptr, nullptr}, *c_star[3] = {nullptr, nullptr, nullptr};
+    float *c_lam[3] = {nullptr, nullptr, nullptr}, *c_lam2[3] = {nullptr, nullptr, nullptr};
+    double* c_grad[3] = {nullptr, nullptr, nullptr};
+    std::vector<float*> c_checkpoints;
+    int c_steps = 0, c_every = 0;
+    float c_dt = 0.f;
+    bool c_ready = false;
+    // reference solver
+    RefState* ref = nullptr;
+};
+
+static int fail(mhdproj_ctx* c, int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    else g_create_error = buf;
+    return code;
+}
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t _e = (call);                                                                   \
+        if (_e != cudaSuccess)                                                                     \
+            return fail(ctx, _e == cudaErrorMemoryAllocation ? MHDPROJ_ERR_OUT_OF_MEMORY : MHDPROJ_ERR_CUDA, \
+                        "%s: %s", #call, cudaGetErrorString(_e));                                  \
+    } while (0)
+
+template <class T>
+static cudaError_t dalloc(mhdproj_ctx* ctx, T** p, size_t bytes) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes ? bytes : 16);
+    if (e != cudaSuccess) return e;
+    ctx->allocs.push_back(q);
+    *p = (T*)q;
+    return cudaMemsetAsync(q, 0, bytes ? bytes : 16, ctx->stream);
+}
+
+static Fields fields(mhdproj_ctx* c) {
+    Fields F{};
+    F.cls = c->d_cls;
+    F.alpha = c->alpha;
+    F.coef = c->coef;
+    F.coef_lo = c->coef_lo;
+    F.coef_lo_kind = c->opt.precision;
+    F.gtop = c->gtop;
+    F.b64 = c->b64;
+    F.phi64 = c->phi64;
+    F.r = c->r;
+    F.z = c->z;
+    F.p = c->p;
+    F.q = c->q;
+    F.e = c->e;
+    F.sc = c->sc;
+    F.partials = c->partials;
+    F.outlet = c->outlet;
+    F.h = c->grid.h;
+    F.rho_l = c->rho_l;
+    F.rho_air = c->rho_air;
+    F.n_active = c->n_active;
+    return F;
+}
+
+// Bounded host wait on the context stream (no unbounded spin).
+static int wait_stream(mhdproj_ctx* ctx, double timeout_s = 600.0) {
+    CK(cudaEventRecord(ctx->ev_sync, ctx->stream));
+    auto t0 = std::chrono::steady_clock::now();
+    int spins = 0;
+    for (;;) {
+        cudaError_t e = cudaEventQuery(ctx->ev_sync);
+        if (e == cudaSuccess) return 0;
+        if (e != cudaErrorNotReady) return fail(ctx, MHDPROJ_ERR_CUDA, "stream wait: %s", cudaGetErrorString(e));
+        if (++spins > 2000) std::this_thread::sleep_for(std::chrono::microseconds(50));
+        else std::this_thread::yield();
+        double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (el > timeout_s) return fail(ctx, MHDPROJ_ERR_TIMEOUT, "device work did not finish within %.0f s", timeout_s);
+    }
+}
+static int read_scalars(mhdproj_ctx* ctx) {
+    CK(cudaMemcpyAsync(ctx->h_sc, ctx->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, ctx->stream));
+    return wait_stream(ctx);
+}
+
+// ------------------------------------------------------------ options
+extern "C" void mhdproj_default_options(mhdproj_options* o) {
+    memset(o, 0, sizeof *o);
+    o->solver = MHDPROJ_SOLVER_GB300;
+    o->precision = MHDPROJ_PRECISION_FP16;
+    o->preconditioner = MHDPROJ_PRECOND_AUTO;
+    o->rel_tol = 1e-6f;
+    o->abs_div_tol = 0.0f;
+    o->max_iterations = 20000;
+    o->max_refinements = 4;
+    o->two_phase = 1;
+    o->gauge = -1;
+    o->compute_divergence = 0;
+}
+
+extern "C" const char* mhdproj_last_error(const mhdproj_ctx* ctx) {
+    return ctx ? ctx->err.c_str() : g_create_error.c_str();
+}
+
+// ----------------------------------------------------------- hierarchy
+static int build_levels(mhdproj_ctx* ctx) {
+    MGPlan& P = ctx->mg;
+    P.precision = ctx->opt.precision;
+    P.sc = ctx->sc;
+    P.prolong = 2.0f;
+    int d[3] = {(int)ctx->grid.nx, (int)ctx->grid.ny, (int)ctx->grid.nz};
+    const int per = (int)ctx->grid.periodic;
+    const size_t vbytes = P.precision == 0 ? 4 : 2;
+    P.nlevels = 0;
+    for (;;) {
+        MGLevel& L = P.lv[P.nlevels];
+        L.L = tile_launch(d[0], d[1], d[2], per, 152 * 8);
+        L.odd_periodic = false;
+        for (int a = 0; a < 3; a++)
+            if ((per & (1 << a)) && (d[a] & 1) && d[a] >= 3) L.odd_periodic = true;
+        const long long n = (long long)d[0] * d[1] * d[2];
+        if (P.nlevels == 0) {
+            L.coef32 = ctx->coef;
+            L.coef_lo = ctx->coef_lo;
+            L.r = ctx->r;
+            L.e = ctx->z;
+            L.tmp = nullptr;
+            if (L.odd_periodic) CK(dalloc(ctx, (float**)&L.tmp, n * 4));
+        } else {
+            CK(dalloc(ctx, &L.coef32, n * sizeof(float4)));
+            L.coef_lo = nullptr;
+            if (P.precision != 0) CK(dalloc(ctx, (uint2**)&L.coef_lo, n * sizeof(uint2)));
+            CK(dalloc(ctx, (char**)&L.r, n * vbytes));
+            CK(dalloc(ctx, (char**)&L.e, n * vbytes));
+            L.tmp = nullptr;
+            if (L.odd_periodic) CK(dalloc(ctx, (char**)&L.tmp, n * vbytes));
+        }
+        P.nlevels++;
+        if (d[0] <= 4 && d[1] <= 4 && d[2] <= 4) break;
+        if (P.nlevels >= 31) return fail(ctx, MHDPROJ_ERR_INVALID, "multigrid hierarchy too deep");
+        for (int a = 0; a < 3; a++) d[a] = (d[a] + 1) / 2;
+    }
+    P.m = d[0] * d[1] * d[2];
+    CK(dalloc(ctx, &P.ainv, (size_t)P.m * P.m * sizeof(float)));
+    return 0;
+}
+
+// --------------------------------------------------------- create/destroy
+extern "C" int mhdproj_create(const mhdproj_grid* grid, const mhdproj_options* options, mhdproj_ctx** out) {
+    mhdproj_ctx* ctx = nullptr;
+    if (!grid || !out) return fail(nullptr, MHDPROJ_ERR_INVALID, "grid and out must not be NULL");
+    *out = nullptr;
+    mhdproj_options o;
+    if (options) o = *options;
+    else mhdproj_default_options(&o);
+    const long long n = (long long)grid->nx * grid->ny * grid->nz;
+    if (grid->nx == 0 || grid->ny == 0 || grid->nz == 0) return fail(nullptr, MHDPROJ_ERR_INVALID, "Invalid pressure grid dimensions");
+    if (n >= (1ll << 31) - 1 || (long long)(grid->nx + 1) * grid->ny * grid->nz >= (1ll << 31) ||
+        (long long)grid->nx * grid->ny * (grid->nz + 1) >= (1ll << 31))
+        return fail(nullptr, MHDPROJ_ERR_INVALID, "Fluid allocation exceeds 32-bit cell indexing");
+    if (!(grid->h > 0.0f) || !std::isfinite(grid->h)) return fail(nullptr, MHDPROJ_ERR_INVALID, "cell size must be positive");
+    if (grid->boundary != MHDPROJ_BOUNDARY_REFERENCE_CLOSED && grid->boundary != MHDPROJ_BOUNDARY_OUTLET_TOP)
+        return fail(nullptr, MHDPROJ_ERR_INVALID, "unknown boundary mode");
+    if (grid->boundary == MHDPROJ_BOUNDARY_OUTLET_TOP && (grid->periodic & 4u))
+        return fail(nullptr, MHDPROJ_ERR_INVALID, "a top outlet needs a non-periodic z axis");
+    if (o.solver != MHDPROJ_SOLVER_REFERENCE && o.solver != MHDPROJ_SOLVER_GB300)
+        return fail(nullptr, MHDPROJ_ERR_INVALID, "unknown solver");
+    if (o.precision < 0 || o.precision > 2) return fail(nullptr, MHDPROJ_ERR_INVALID, "unknown precision");
+    // FluidConfig::validate (src/fluid/mod.rs:56-80) limits; the GB300 solver
+    // also accepts tolerances below 1e-7 because it refines in FP64.
+    if (!std::isfinite(o.abs_div_tol) || o.abs_div_tol < 0.f || o.max_iterations < 1 || o.max_iterations > 1000000)
+        return fail(nullptr, MHDPROJ_ERR_INVALID, "Invalid fluid timestep, initial condition or solver limits/tolerances");
+    if (o.solver == MHDPROJ_SOLVER_REFERENCE) {
+        if (!(o.rel_tol >= 1e-7f && o.rel_tol <= 1e-2f) || o.max_iterations > 20000)
+            return fail(nullptr, MHDPROJ_ERR_INVALID, "Invalid fluid timestep, initial condition or solver limits/tolerances");
+        if (grid->boundary != MHDPROJ_BOUNDARY_REFERENCE_CLOSED)
+            return fail(nullptr, MHDPROJ_ERR_INVALID, "the reference solver has closed boundaries only");
+    } else {
+        if (!(o.rel_tol >= 1e-12f && o.rel_tol <= 1e-2f))
+            return fail(nullptr, MHDPROJ_ERR_INVALID, "relative tolerance must lie in [1e-12, 1e-2]");
+        if (o.max_refinements < 1 || o.max_refinements > 64)
+            return fail(nullptr, MHDPROJ_ERR_INVALID, "max_refinements must lie in [1, 64]");
+    }
+    ctx = new mhdproj_ctx();
+    ctx->grid = *grid;
+    ctx->opt = o;
+    ctx->n = n;
+    ctx->nfx = (long long)(grid->nx + 1) * grid->ny * grid->nz;
+    ctx->nfy = (long long)grid->nx * (grid->ny + 1) * grid->nz;
+    ctx->nfz = (long long)grid->nx * grid->ny * (grid->nz + 1);
+    ctx->outlet = grid->boundary == MHDPROJ_BOUNDARY_OUTLET_TOP;
+    int rc = 0;
+    auto bad = [&](int code) {
+        g_create_error = ctx->err;
+        mhdproj_destroy(ctx);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        fail(ctx, MHDPROJ_ERR_CUDA, "cudaStreamCreate failed (is a GPU visible?)");
+        return bad(MHDPROJ_ERR_CUDA);
+    }
+    ctx->own_stream = true;
+    if (cudaEventCreate(&ctx->ev_a) != cudaSuccess || cudaEventCreate(&ctx->ev_b) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_sync, cudaEventDisableTiming) != cudaSuccess) {
+        fail(ctx, MHDPROJ_ERR_CUDA, "cudaEventCreate failed");
+        return bad(MHDPROJ_ERR_CUDA);
+    }
+    if (cudaMallocHost(&ctx->h_sc, sizeof(Scalars)) != cudaSuccess || cudaMallocHost(&ctx->h_flag, sizeof(int)) != cudaSuccess) {
+        fail(ctx, MHDPROJ_ERR_CUDA, "cudaMallocHost failed");
+        return bad(MHDPROJ_ERR_CUDA);
+    }
+    ctx->L = tile_launch(grid->nx, grid->ny, grid->nz, grid->periodic, 152 * 8);
+    if ((rc = [&]() -> int {
+             CK(dalloc(ctx, &ctx->d_solid_prev, n));
+             CK(dalloc(ctx, &ctx->d_cls, n));
+             CK(dalloc(ctx, &ctx->d_flag, sizeof(int)));
+             CK(dalloc(ctx, &ctx->sc, sizeof(Scalars)));
+             CK(dalloc(ctx, &ctx->partials, sizeof(double) * 4 * MAX_REDUCE_BLOCKS));
+             if (ctx->opt.solver == MHDPROJ_SOLVER_REFERENCE) {
+                 int r = ref_create(&ctx->ref, grid, &ctx->opt, ctx->stream, ctx->err);
+                 return r;
+             }
+             CK(dalloc(ctx, &ctx->alpha, n * 4));
+             CK(dalloc(ctx, &ctx->coef, n * sizeof(float4)));
+             if (ctx->opt.precision != 0) CK(dalloc(ctx, (uint2**)&ctx->coef_lo, n * sizeof(uint2)));
+             CK(dalloc(ctx, &ctx->gtop, (size_t)grid->nx * grid->ny * 4));
+             CK(dalloc(ctx, &ctx->b64, n * 8));
+             CK(dalloc(ctx, &ctx->phi64, n * 8));
+             CK(dalloc(ctx, &ctx->psi64, n * 8));
+             CK(dalloc(ctx, &ctx->r, n * 4));
+             CK(dalloc(ctx, &ctx->z, n * 4));
+             CK(dalloc(ctx, &ctx->p, n * 4));
+             CK(dalloc(ctx, &ctx->q, n * 4));
+             CK(dalloc(ctx, &ctx->e, n * 4));
+             ctx->use_mg = ctx->opt.preconditioner != MHDPROJ_PRECOND_JACOBI;
+             if (ctx->use_mg) {
+                 int r = build_levels(ctx);
+                 if (r) return r;
+                 CK(mg_prepare_attributes());
+             }
+             CK(cudaStreamSynchronize(ctx->stream));
+             return 0;
+         }()) != 0)
+        return bad(rc);
+    *out = ctx;
+    return 0;
+}
+
+extern "C" void mhdproj_destroy(mhdproj_ctx* ctx) {
+    if (!ctx) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->it_graph) cudaGraphExecDestroy(ctx->it_graph);
+    if (ctx->ref) ref_destroy(ctx->ref);
+    for (void* p : ctx->allocs) cudaFree(p);
+    for (float* p : ctx->c_checkpoints) cudaFree(p);
+    if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
+    if (ctx->h_flag) cudaFreeHost(ctx->h_flag);
+    if (ctx->ev_a) cudaEventDestroy(ctx->ev_a);
+    if (ctx->ev_b) cudaEventDestroy(ctx->ev_b);
+    if (ctx->ev_sync) cudaEventDestroy(ctx->ev_sync);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" int mhdproj_set_stream(mhdproj_ctx* ctx, void* stream) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    ctx->own_stream = false;
+    ctx->stream = (cudaStream_t)stream;
+    if (ctx->ref) ref_set_stream(ctx->ref, ctx->stream);
+    return 0;
+}
+
+// -------------------------------------------------------- coefficients
+__global__ void k_compare_u8(const uint8_t* a, const uint8_t* b, long long n, int* flag) {
+    long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    int diff = 0;
+    for (; i < n; i += stride) diff |= ((a[i] != 0) != (b[i] != 0));
+    if (__syncthreads_or(diff) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+static int update_topology(mhdproj_ctx* ctx, const uint8_t* solid, bool* changed) {
+    *changed = !ctx->have_topology;
+    if (ctx->have_topology) {
+        CK(cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+        k_compare_u8<<<152 * 4, 256, 0, ctx->stream>>>(solid, ctx->d_solid_prev, ctx->n, ctx->d_flag);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(ctx->h_flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        int rc = wait_stream(ctx);
+        if (rc) return rc;
+        *changed = *ctx->h_flag != 0;
+    }
+    if (!*changed) return 0;
+    CK(cudaMemcpyAsync(ctx->d_solid_prev, solid, ctx->n, cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->h_solid.resize(ctx->n);
+    CK(cudaMemcpyAsync(ctx->h_solid.data(), solid, ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+    int rc = wait_stream(ctx);
+    if (rc) return rc;
+    const uint32_t dims[3] = {ctx->grid.nx, ctx->grid.ny, ctx->grid.nz};
+    if (ctx->opt.solver == MHDPROJ_SOLVER_REFERENCE) {
+        ctx->h_mask.resize(ctx->n);
+        for (long long i = 0; i < ctx->n; i++) ctx->h_mask[i] = ctx->h_solid[i] ? 0u : 1u;
+        ctx->components = host_anchors(ctx->h_mask.data(), dims, ctx->grid.periodic);
+        long long nf = 0;
+        for (long long i = 0; i < ctx->n; i++) nf += ctx->h_mask[i] != 0;
+        ctx->n_active = nf;
+        rc = ref_set_topology(ctx->ref, ctx->h_mask.data(), ctx->components, ctx->err);
+        if (rc) return rc;
+    } else {
+        ctx->h_cls.resize(ctx->n);
+        ctx->pinned = host_classify(ctx->h_solid.data(), dims, ctx->grid.periodic, ctx->outlet, ctx->h_cls.data(),
+                                    &ctx->components);
+        long long na = 0;
+        for (long long i = 0; i < ctx->n; i++) na += ctx->h_cls[i] == 1;
+        ctx->n_active = na;
+        CK(cudaMemcpyAsync(ctx->d_cls, ctx->h_cls.data(), ctx->n, cudaMemcpyHostToDevice, ctx->stream));
+        rc = wait_stream(ctx);
+        if (rc) return rc;
+    }
+    ctx->have_topology = true;
+    return 0;
+}
+
+extern "C" int mhdproj_set_coefficients(mhdproj_ctx* ctx, const float* alpha, const uint8_t* solid, float rho_liquid,
+                                        float rho_air) {
+    if (!ctx || !alpha || !solid) return ctx ? fail(ctx, MHDPROJ_ERR_INVALID, "alpha and solid must not be NULL") : MHDPROJ_ERR_INVALID;
+    if (!(rho_liquid > 0.f) || !std::isfinite(rho_liquid) || !(rho_air > 0.f) || !std::isfinite(rho_air))
+        return fail(ctx, MHDPROJ_ERR_INVALID, "Fluid material needs a positive density");
+    bool changed = false;
+    int rc = update_topology(ctx, solid, &changed);
+    if (rc) return rc;
+    ctx->rho_l = rho_liquid;
+    ctx->rho_air = rho_air;
+    if (ctx->ref) {
+        rc = ref_set_coefficients(ctx->ref, alpha, rho_liquid, rho_air, ctx->err);
+        if (rc) return rc;
+        ctx->have_coef = true;
+        return 0;
+    }
+    CK(cudaMemcpyAsync(ctx->alpha, alpha, ctx->n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    Fields F = fields(ctx);
+    launch_coefficients(ctx->L, F, ctx->stream);
+    CK(cudaGetLastError());
+    if (ctx->use_mg) {
+        mg_build(ctx->mg, ctx->stream);
+        CK(cudaGetLastError());
+    }
+    ctx->have_coef = true;
+    return 0;
+}
+
+extern "C" int mhdproj_set_phase_drag(mhdproj_ctx* ctx, const float* phase, float drag_rate, float dt) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (!ctx->ref) return fail(ctx, MHDPROJ_ERR_INVALID, "phase drag is a reference-solver mobility term");
+    return ref_set_phase_drag(ctx->ref, phase, drag_rate, dt, ctx->err);
+}
+
+// ------------------------------------------------------------- solver
+__global__ void k_jacobi(Grid3 g, const float4* __restrict__ coef, const float* __restrict__ r, float* __restrict__ z,
+                         const Scalars* sc) {
+    if (sc->converged) return;
+    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
+    if (x >= g.nx || y >= g.ny) return;
+    const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
+    for (int zz = z0; zz < z1; zz++) {
+        const int i = x + g.nx * (y + g.ny * zz);
+        const float4 c = coef[i];
+        float d = c.x + c.y + c.z + c.w;
+        int xp = x + 1 < g.nx ? i + 1 : ((g.periodic & 1) ? i + 1 - g.nx : -1);
+        int yp = y + 1 < g.ny ? i + g.nx : ((g.periodic & 2) ? i + g.nx - g.nx * g.ny : -1);
+        int zp = zz + 1 < g.nz ? i + g.nx * g.ny : ((g.periodic & 4) ? i + g.nx * g.ny - g.nx * g.ny * g.nz : -1);
+        if (xp >= 0) d += coef[xp].x;
+        if (yp >= 0) d += coef[yp].y;
+        if (zp >= 0) d += coef[zp].z;
+        z[i] = d > 0.f ? sc->sigma * r[i] / d : 0.f;
+    }
+}
+static void enqueue_precondition(mhdproj_ctx* ctx) {
+    if (ctx->use_mg) mg_vcycle(ctx->mg, ctx->stream);
+    else k_jacobi<<<ctx->L.grid, ctx->L.block, 0, ctx->stream>>>(ctx->L.g, ctx->coef, ctx->r, ctx->z, ctx->sc);
+}
+static void enqueue_iteration_body(mhdproj_ctx* ctx) {
+    Fields F = fields(ctx);
+    launch_spmv_pq(ctx->L, F, ctx->stream);
+    launch_update(ctx->L, F, ctx->stream);
+    enqueue_precondition(ctx);
+    launch_dot_rz(ctx->L, F, 0, ctx->stream);
+    launch_search(ctx->L, F, ctx->stream);
+}
+
+static int launch_iterations(mhdproj_ctx* ctx, int count) {
+    if (!ctx->it_graph && !ctx->graph_failed) {
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamSynchronize(ctx->stream));
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            enqueue_iteration_body(ctx);
+            e = cudaStreamEndCapture(ctx->stream, &graph);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->it_graph, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            ctx->graph_failed = true;
+            ctx->it_graph = nullptr;
+        }
+    }
+    for (int k = 0; k < count; k++) {
+        if (ctx->it_graph) CK(cudaGraphLaunch(ctx->it_graph, ctx->stream));
+        else enqueue_iteration_body(ctx);
+    }
+    CK(cudaGetLastError());
+    return 0;
+}
+
+// Solve A x = b64 (already in ctx->b64 with ||b||^2 in sc->bb) by CG with
+// FP64 refinement.  x64 holds the initial guess.  Returns 0 or an error.
+static int solve(mhdproj_ctx* ctx, double* x64, mhdproj_stats* st) {
+    Fields F = fields(ctx);
+    const double tol2 = (double)ctx->opt.rel_tol * ctx->opt.rel_tol;
+    (void)tol2;
+    int passes = 0;
+    launch_residual64(ctx->L, F, x64, ctx->stream);
+    enqueue_precondition(ctx);
+    launch_dot_rz(ctx->L, F, 1, ctx->stream);
+    CK(cudaGetLastError());
+    int rc = read_scalars(ctx);
+    if (rc) return rc;
+    const uint32_t max_it = ctx->opt.max_iterations;
+    for (;;) {
+        Scalars& S = *ctx->h_sc;
+        if (S.nonfinite) return fail(ctx, MHDPROJ_ERR_NONFINITE, "Nonfinite fluid pressure residual");
+        if (S.outer_done) break;
+        if (passes > ctx->opt.max_refinements || (uint32_t)S.total_iterations >= max_it) {
+            const double rel = S.bb > 0 ? std::sqrt(S.rr_true / S.bb) : 0.0;
+            const double floor_ = ctx->opt.abs_div_tol;
+            return fail(ctx, MHDPROJ_ERR_NOT_CONVERGED,
+                        "Fluid pressure solve did not converge after %d iterations (true relative residual %.3e, "
+                        "requested %.3e, RMS divergence floor %.3e s\xe2\x81\xbb\xc2\xb9)",
+                        S.total_iterations, rel, (double)ctx->opt.rel_tol, floor_);
+        }
+        // inner CG on A e = r
+        int batch = 4;
+        double rr_prev = S.rr;
+        int it_prev = S.iterations;
+        while (!ctx->h_sc->converged && (uint32_t)ctx->h_sc->total_iterations < max_it) {
+            int room = (int)(max_it - (uint32_t)ctx->h_sc->total_iterations);
+            int b = std::min(batch, room);
+            rc = launch_iterations(ctx, b);
+            if (rc) return rc;
+            rc = read_scalars(ctx);
+            if (rc) return rc;
+            Scalars& T = *ctx->h_sc;
+            if (T.nonfinite) return fail(ctx, MHDPROJ_ERR_NONFINITE, "Nonfinite fluid pressure residual");
+            if (T.converged) break;
+            if (T.iterations <= it_prev) return fail(ctx, MHDPROJ_ERR_NO_PROGRESS, "Fluid pressure iteration made no progress");
+            // predict the remaining iterations from the observed contraction
+            const int done = T.iterations - it_prev;
+            double rate = (rr_prev > 0 && T.rr > 0) ? std::pow(T.rr / rr_prev, 1.0 / done) : 0.5;
+            int need = 16;
+            if (rate > 0 && rate < 1 && T.rr > T.rr_target) need = (int)std::ceil(std::log(T.rr_target / T.rr) / std::log(rate));
+            batch = std::max(1, std::min(16, need));
+            rr_prev = T.rr;
+            it_prev = T.iterations;
+        }
+        launch_accumulate(ctx->L, F, x64, ctx->stream);
+        passes++;
+        launch_residual64(ctx->L, F, x64, ctx->stream);
+        enqueue_precondition(ctx);
+        launch_dot_rz(ctx->L, F, 1, ctx->stream);
+        CK(cudaGetLastError());
+        rc = read_scalars(ctx);
+        if (rc) return rc;
+    }
+    if (st) {
+        const Scalars& S = *ctx->h_sc;
+        st->iterations = (uint32_t)S.total_iterations;
+        st->refinements = (uint32_t)(passes > 0 ? passes - 1 : 0);
+        st->true_relative_residual = S.bb > 0 ? std::sqrt(S.rr_true / S.bb) : 0.0;
+        st->relative_residual = (float)st->true_relative_residual;
+        st->multigrid = ctx->use_mg;
+        st->levels = ctx->use_mg ? (uint32_t)ctx->mg.nlevels : 0;
+        long long cc = 0;
+        if (ctx->use_mg)
+            for (int l = 1; l < ctx->mg.nlevels; l++) cc += ctx->mg.lv[l].L.g.n();
+        st->coarse_cells = (uint64_t)cc;
+    }
+    return 0;
+}
+
+static void begin_scalars(mhdproj_ctx* ctx) {
+    const double tol2 = (double)ctx->opt.rel_tol * ctx->opt.rel_tol;
+    const double h = ctx->grid.h;
+    const double abs_floor = (double)ctx->opt.abs_div_tol * ctx->opt.abs_div_tol * h * h * h * h * (double)ctx->n_active;
+    // FP32 CG reduces its own residual by about 1e-5 reliably; refine beyond.
+    launch_init_scalars(ctx->sc, tol2, abs_floor, 1e-10, ctx->stream);
+}
+
+static int project_gb300(mhdproj_ctx* ctx, const float* us, const float* vs, const float* ws, float* uo, float* vo,
+                         float* wo, float* po, float dt, int warm, mhdproj_stats* st) {
+    if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients before projecting");
+    CK(cudaEventRecord(ctx->ev_a, ctx->stream));
+    begin_scalars(ctx);
+    Fields F = fields(ctx);
+    launch_rhs(ctx->L, F, us, vs, ws, ctx->stream);
+    if (!warm || !ctx->have_solution) CK(cudaMemsetAsync(ctx->phi64, 0, ctx->n * 8, ctx->stream));
+    mhdproj_stats local{};
+    int rc = solve(ctx, ctx->phi64, &local);
+    if (rc) return rc;
+    launch_correct(ctx->L, F, ctx->phi64, us, vs, ws, uo, vo, wo, po, dt, ctx->stream);
+    if (ctx->opt.compute_divergence) launch_divergence(ctx->L, F, uo, vo, wo, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev_b, ctx->stream));
+    if (ctx->opt.compute_divergence) {
+        rc = read_scalars(ctx);
+        if (rc) return rc;
+        local.max_divergence = ctx->h_sc->divmax;
+        local.rms_divergence = ctx->n_active ? std::sqrt(ctx->h_sc->div2 / (double)ctx->n_active) : 0.0;
+    } else {
+        rc = wait_stream(ctx);
+        if (rc) return rc;
+    }
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev_a, ctx->ev_b));
+    local.elapsed_ms = ms;
+    local.meanfree = 0;
+    ctx->have_solution = true;
+    if (st) *st = local;
+    return 0;
+}
+
+extern "C" int mhdproj_project(mhdproj_ctx* ctx, const float* usx, const float* usy, const float* usz, float* uox,
+                               float* uoy, float* uoz, float* p_out, float dt, int warm_start, mhdproj_stats* stats) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (!usx || !usy || !usz || !uox || !uoy || !uoz) return fail(ctx, MHDPROJ_ERR_INVALID, "face arrays must not be NULL");
+    if (!(dt > 0.f) || !std::isfinite(dt)) return fail(ctx, MHDPROJ_ERR_INVALID, "Invalid fluid timestep, initial condition or solver limits/tolerances");
+    if (ctx->ref) {
+        if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients before projecting");
+        mhdproj_stats local{};
+        CK(cudaEventRecord(ctx->ev_a, ctx->stream));
+        int rc = ref_project(ctx->ref, usx, usy, usz, uox, uoy, uoz, p_out, dt, warm_start, &local, ctx->err);
+        if (rc) return rc;
+        CK(cudaEventRecord(ctx->ev_b, ctx->stream));
+        rc = wait_stream(ctx);
+        if (rc) return rc;
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ctx->ev_a, ctx->ev_b));
+        local.elapsed_ms = ms;
+        if (stats) *stats = local;
+        return 0;
+    }
+    return project_gb300(ctx, usx, usy, usz, uox, uoy, uoz, p_out, dt, warm_start, stats);
+}
+
+extern "C" int mhdproj_project_host(mhdproj_ctx* ctx, const float* alpha, const uint8_t* solid, float rho_liquid,
+                                    float rho_air, const float* usx, const float* usy, const float* usz, float* uox,
+                                    float* uoy, float* uoz, float* p_out, float dt, int warm_start,
+                                    mhdproj_stats* stats) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (!alpha || !solid || !usx || !usy || !usz || !uox || !uoy || !uoz)
+        return fail(ctx, MHDPROJ_ERR_INVALID, "host arrays must not be NULL");
+    if (!ctx->s_alpha) {
+        CK(dalloc(ctx, &ctx->s_alpha, ctx->n * 4));
+        CK(dalloc(ctx, &ctx->s_solid, ctx->n));
+        CK(dalloc(ctx, &ctx->s_u, ctx->nfx * 4));
+        CK(dalloc(ctx, &ctx->s_v, ctx->nfy * 4));
+        CK(dalloc(ctx, &ctx->s_w, ctx->nfz * 4));
+        CK(dalloc(ctx, &ctx->s_p, ctx->n * 4));
+    }
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(ctx->s_alpha, alpha, ctx->n * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->s_solid, solid, ctx->n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->s_u, usx, ctx->nfx * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->s_v, usy, ctx->nfy * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(ctx->s_w, usz, ctx->nfz * 4, cudaMemcpyHostToDevice, s));
+    int rc = mhdproj_set_coefficients(ctx, ctx->s_alpha, ctx->s_solid, rho_liquid, rho_air);
+    if (rc) return rc;
+    rc = mhdproj_project(ctx, ctx->s_u, ctx->s_v, ctx->s_w, ctx->s_u, ctx->s_v, ctx->s_w, ctx->s_p, dt, warm_start,
+                         stats);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(uox, ctx->s_u, ctx->nfx * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(uoy, ctx->s_v, ctx->nfy * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(uoz, ctx->s_w, ctx->nfz * 4, cudaMemcpyDeviceToHost, s));
+    if (p_out) CK(cudaMemcpyAsync(p_out, ctx->s_p, ctx->n * 4, cudaMemcpyDeviceToHost, s));
+    return wait_stream(ctx);
+}
+
+// -------------------------------------------------------------- adjoint
+static int vjp_gb300(mhdproj_ctx* ctx, const float* gu, const float* gv, const float* gw, const float* gp, float dt,
+                     float* ou, float* ov, float* ow, mhdproj_stats* st) {
+    begin_scalars(ctx);
+    Fields F = fields(ctx);
+    launch_adj_rhs(ctx->L, F, gu, gv, gw, gp, dt, ctx->stream);
+    CK(cudaMemsetAsync(ctx->psi64, 0, ctx->n * 8, ctx->stream));
+    int rc = solve(ctx, ctx->psi64, st);
+    if (rc) return rc;
+    launch_adj_correct(ctx->L, F, ctx->psi64, gu, gv, gw, ou, ov, ow, ctx->stream);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+extern "C" int mhdproj_project_vjp(mhdproj_ctx* ctx, const float* gux, const float* guy, const float* guz,
+                                   const float* gp, float dt, float* ogx, float* ogy, float* ogz,
+                                   mhdproj_stats* stats) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (ctx->ref) return fail(ctx, MHDPROJ_ERR_INVALID, "the adjoint is part of the GB300 solver");
+    if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients before the adjoint");
+    if (!gux || !guy || !guz || !ogx || !ogy || !ogz) return fail(ctx, MHDPROJ_ERR_INVALID, "face arrays must not be NULL");
+    if (!(dt > 0.f)) return fail(ctx, MHDPROJ_ERR_INVALID, "dt must be positive");
+    CK(cudaEventRecord(ctx->ev_a, ctx->stream));
+    mhdproj_stats local{};
+    int rc = vjp_gb300(ctx, gux, guy, guz, gp, dt, ogx, ogy, ogz, &local);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->ev_b, ctx->stream));
+    rc = wait_stream(ctx);
+    if (rc) return rc;
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev_a, ctx->ev_b));
+    local.elapsed_ms = ms;
+    if (stats) *stats = local;
+    return 0;
+}
+
+// ---------------------------------------------------------------- chain
+__global__ void k_d2f(const double* a, float* b, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+static int chain_alloc(mhdproj_ctx* ctx) {
+    if (ctx->c_ready) return 0;
+    const long long m[3] = {ctx->nfx, ctx->nfy, ctx->nfz};
+    for (int a = 0; a < 3; a++) {
+        CK(dalloc(ctx, &ctx->c_cur[a], m[a] * 4));
+        CK(dalloc(ctx, &ctx->c_star[a], m[a] * 4));
+        CK(dalloc(ctx, &ctx->c_lam[a], m[a] * 4));
+        CK(dalloc(ctx, &ctx->c_lam2[a], m[a] * 4));
+        CK(dalloc(ctx, &ctx->c_grad[a], m[a] * 8));
+    }
+    ctx->c_ready = true;
+    return 0;
+}
+
+extern "C" int mhdproj_chain_forward(mhdproj_ctx* ctx, const float* u0x, const float* u0y, const float* u0z,
+                                     const float* fx, const float* fy, const float* fz, float dt, int steps,
+                                     int checkpoint_every, float* ufx, float* ufy, float* ufz, double* objective,
+                                     mhdproj_stats* stats) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (ctx->ref) return fail(ctx, MHDPROJ_ERR_INVALID, "the chained adjoint is part of the GB300 solver");
+    if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients before the chain");
+    if (steps < 1 || checkpoint_every < 1 || !(dt > 0.f)) return fail(ctx, MHDPROJ_ERR_INVALID, "steps, checkpoint_every and dt must be positive");
+    int rc = chain_alloc(ctx);
+    if (rc) return rc;
+    const long long m[3] = {ctx->nfx, ctx->nfy, ctx->nfz};
+    const float* u0[3] = {u0x, u0y, u0z};
+    cudaStream_t s = ctx->stream;
+    for (int a = 0; a < 3; a++) CK(cudaMemcpyAsync(ctx->c_cur[a], u0[a], m[a] * 4, cudaMemcpyDeviceToDevice, s));
+    // checkpoints: the state entering every checkpoint_every-th step
+    const int nck = (steps + checkpoint_every - 1) / checkpoint_every;
+    while ((int)ctx->c_checkpoints.size() < 3 * nck) {
+        float* p = nullptr;
+        const int a = (int)ctx->c_checkpoints.size() % 3;
+        CK(cudaMalloc(&p, m[a] * 4));
+        ctx->c_checkpoints.push_back(p);
+    }
+    CK(cudaEventRecord(ctx->ev_a, s));
+    Fields F = fields(ctx);
+    mhdproj_stats total{};
+    for (int k = 0; k < steps; k++) {
+        if (k % checkpoint_every == 0) {
+            const int c = k / checkpoint_every;
+            for (int a = 0; a < 3; a++)
+                CK(cudaMemcpyAsync(ctx->c_checkpoints[3 * c + a], ctx->c_cur[a], m[a] * 4, cudaMemcpyDeviceToDevice, s));
+        }
+        launch_add_force(ctx->L, F, ctx->c_cur[0], ctx->c_cur[1], ctx->c_cur[2], fx, fy, fz, dt, ctx->c_star[0],
+                         ctx->c_star[1], ctx->c_star[2], s);
+        mhdproj_stats one{};
+        begin_scalars(ctx);
+        launch_rhs(ctx->L, F, ctx->c_star[0], ctx->c_star[1], ctx->c_star[2], s);
+        CK(cudaMemsetAsync(ctx->phi64, 0, ctx->n * 8, s));
+        rc = solve(ctx, ctx->phi64, &one);
+        if (rc) return rc;
+        launch_correct(ctx->L, F, ctx->phi64, ctx->c_star[0], ctx->c_star[1], ctx->c_star[2], ctx->c_cur[0],
+                       ctx->c_cur[1], ctx->c_cur[2], nullptr, dt, s);
+        total.iterations += one.iterations;
+        total.refinements += one.refinements;
+        total.true_relative_residual = std::max(total.true_relative_residual, one.true_relative_residual);
+    }
+    launch_outlet_objective(ctx->L, F, ctx->c_cur[2], nullptr, s);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev_b, s));
+    rc = read_scalars(ctx);
+    if (rc) return rc;
+    if (objective) *objective = ctx->h_sc->objective;
+    const float* cur[3] = {ctx->c_cur[0], ctx->c_cur[1], ctx->c_cur[2]};
+    float* uf[3] = {ufx, ufy, ufz};
+    for (int a = 0; a < 3; a++)
+        if (uf[a]) CK(cudaMemcpyAsync(uf[a], cur[a], m[a] * 4, cudaMemcpyDeviceToDevice, s));
+    rc = wait_stream(ctx);
+    if (rc) return rc;
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev_a, ctx->ev_b));
+    total.elapsed_ms = ms;
+    total.relative_residual = (float)total.true_relative_residual;
+    ctx->c_steps = steps;
+    ctx->c_every = checkpoint_every;
+    ctx->c_dt = dt;
+    if (stats) *stats = total;
+    return 0;
+}
+
+extern "C" int mhdproj_chain_backward(mhdproj_ctx* ctx, float* gfx, float* gfy, float* gfz, mhdproj_stats* stats) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (!ctx->c_ready || ctx->c_steps < 1) return fail(ctx, MHDPROJ_ERR_STATE, "run mhdproj_chain_forward first");
+    if (!gfx || !gfy || !gfz) return fail(ctx, MHDPROJ_ERR_INVALID, "gradient arrays must not be NULL");
+    const long long m[3] = {ctx->nfx, ctx->nfy, ctx->nfz};
+    cudaStream_t s = ctx->stream;
+    CK(cudaEventRecord(ctx->ev_a, s));
+    // lambda_K = dJ/du_K: 2 w on the outlet faces of the final state, 0 elsewhere
+    for (int a = 0; a < 3; a++) {
+        CK(cudaMemsetAsync(ctx->c_lam[a], 0, m[a] * 4, s));
+        CK(cudaMemsetAsync(ctx->c_grad[a], 0, m[a] * 8, s));
+    }
+    if (ctx->outlet) launch_outlet_objective(ctx->L, fields(ctx), ctx->c_cur[2], ctx->c_lam[2], s);
+    Fields F = fields(ctx);
+    mhdproj_stats total{};
+    float* lam[3] = {ctx->c_lam[0], ctx->c_lam[1], ctx->c_lam[2]};
+    float* nxt[3] = {ctx->c_lam2[0], ctx->c_lam2[1], ctx->c_lam2[2]};
+    for (int k = ctx->c_steps - 1; k >= 0; k--) {
+        mhdproj_stats one{};
+        int rc = vjp_gb300(ctx, lam[0], lam[1], lam[2], nullptr, ctx->c_dt, nxt[0], nxt[1], nxt[2], &one);
+        if (rc) return rc;
+        launch_force_grad(ctx->L, F, nxt[0], nxt[1], nxt[2], ctx->c_dt, ctx->c_grad[0], ctx->c_grad[1], ctx->c_grad[2], s);
+        std::swap(lam[0], nxt[0]);
+        std::swap(lam[1], nxt[1]);
+        std::swap(lam[2], nxt[2]);
+        total.iterations += one.iterations;
+        total.refinements += one.refinements;
+        total.true_relative_residual = std::max(total.true_relative_residual, one.true_relative_residual);
+    }
+    float* out[3] = {gfx, gfy, gfz};
+    for (int a = 0; a < 3; a++) k_d2f<<<152 * 4, 256, 0, s>>>(ctx->c_grad[a], out[a], m[a]);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev_b, s));
+    int rc = wait_stream(ctx);
+    if (rc) return rc;
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev_a, ctx->ev_b));
+    total.elapsed_ms = ms;
+    total.relative_residual = (float)total.true_relative_residual;
+    if (stats) *stats = total;
+    return 0;
+}
+
+// --------------------------------------------------------------- probes
+extern "C" int mhdproj_apply_operator(mhdproj_ctx* ctx, const float* x, float* y) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients first");
+    if (ctx->ref) {
+        int rc = ref_apply_operator(ctx->ref, x, y, ctx->err);
+        if (rc) return rc;
+        return wait_stream(ctx);
+    }
+    launch_apply(ctx->L, fields(ctx), x, y, ctx->stream);
+    CK(cudaGetLastError());
+    return wait_stream(ctx);
+}
+
+extern "C" int mhdproj_apply_preconditioner(mhdproj_ctx* ctx, const float* r, float* z) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients first");
+    if (ctx->ref) {
+        int rc = ref_apply_preconditioner(ctx->ref, r, z, ctx->err);
+        if (rc) return rc;
+        return wait_stream(ctx);
+    }
+    CK(cudaMemcpyAsync(ctx->r, r, ctx->n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    launch_set_sigma(ctx->sc, 1.0f, ctx->stream);
+    enqueue_precondition(ctx);
+    CK(cudaMemcpyAsync(z, ctx->z, ctx->n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaGetLastError());
+    return wait_stream(ctx);
+}
+
+extern "C" int mhdproj_copy_coefficients(mhdproj_ctx* ctx, float* coef4) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients first");
+    if (ctx->ref) {
+        int rc = ref_copy_coefficients(ctx->ref, coef4, ctx->err);
+        if (rc) return rc;
+        return wait_stream(ctx);
+    }
+    CK(cudaMemcpyAsync(coef4, ctx->coef, ctx->n * sizeof(float4), cudaMemcpyDeviceToDevice, ctx->stream));
+    return wait_stream(ctx);
+}
+
+extern "C" int mhdproj_copy_potential(mhdproj_ctx* ctx, double* phi) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (ctx->ref) {
+        int rc = ref_copy_potential(ctx->ref, phi, ctx->err);
+        if (rc) return rc;
+        return wait_stream(ctx);
+    }
+    CK(cudaMemcpyAsync(phi, ctx->phi64, ctx->n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    return wait_stream(ctx);
+}
+
+extern "C" int mhdproj_copy_topology(mhdproj_ctx* ctx, uint32_t* mask_host, uint32_t* components) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (!ctx->have_topology) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients first");
+    if (mask_host) {
+        if (ctx->ref)
+            for (long long i = 0; i < ctx->n; i++) mask_host[i] = ctx->h_mask[i];
+        else
+            for (long long i = 0; i < ctx->n; i++) mask_host[i] = ctx->h_cls[i];
+    }
+    if (components) *components = ctx->components;
+    return 0;
+}
+
+// ------------------------------------------------------------ utilities
+extern "C" int mhdproj_hierarchy(const uint32_t dims[4], uint32_t* levels, uint64_t* coarse_cells) {
+    return host_hierarchy(dims, levels, coarse_cells) ? MHDPROJ_ERR_INVALID : 0;
+}
+extern "C" uint32_t mhdproj_anchors(uint32_t* mask, const uint32_t dims[3], uint32_t periodic) {
+    return host_anchors(mask, dims, periodic);
+}

@@ -1,0 +1,87 @@
+// kernels.h -- host-side launchers of the projection kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "common.cuh"
+
+namespace mhdproj {
+
+struct Launch {
+    dim3 grid, block;
+    Grid3 g;
+    int nblocks;
+};
+// 32x8 tiles over (x, y), z split into runs so that about `target` blocks run.
+Launch tile_launch(int nx, int ny, int nz, int periodic, int target_blocks);
+
+struct Fields {
+    // GB300 solver fine-level state (all device pointers)
+    const uint8_t* cls;
+    const float* alpha;
+    float4* coef;
+    void* coef_lo;     // FP16/BF16 copy (mixed precision) or nullptr
+    int coef_lo_kind;  // 0 none, 1 fp16, 2 bf16
+    float* gtop;
+    double* b64;
+    double* phi64;
+    float *r, *z, *p, *q, *e;
+    Scalars* sc;
+    double* partials;
+    int outlet;
+    float h, rho_l, rho_air;
+    long long n_active;
+};
+
+// ---- GB300 solver kernels (gb300_kernels.cu)
+void launch_coefficients(const Launch& L, const Fields& F, cudaStream_t s);
+void launch_init_scalars(Scalars* sc, double tol2, double abs_floor, double inner_floor2, cudaStream_t s);
+void launch_rhs(const Launch& L, const Fields& F, const float* u, const float* v, const float* w, cudaStream_t s);
+void launch_residual64(const Launch& L, const Fields& F, const double* x64, cudaStream_t s);
+void launch_spmv_pq(const Launch& L, const Fields& F, cudaStream_t s);
+void launch_update(const Launch& L, const Fields& F, cudaStream_t s);
+void launch_dot_rz(const Launch& L, const Fields& F, int init, cudaStream_t s);
+void launch_search(const Launch& L, const Fields& F, cudaStream_t s);
+void launch_accumulate(const Launch& L, const Fields& F, double* x64, cudaStream_t s);
+void launch_correct(const Launch& L, const Fields& F, const double* phi, const float* us, const float* vs,
+                    const float* ws, float* uo, float* vo, float* wo, float* po, float dt, cudaStream_t s);
+void launch_divergence(const Launch& L, const Fields& F, const float* u, const float* v, const float* w,
+                       cudaStream_t s);
+void launch_apply(const Launch& L, const Fields& F, const float* x, float* y, cudaStream_t s);
+void launch_set_sigma(Scalars* sc, float sigma, cudaStream_t s);
+void launch_scale(const Launch& L, const float* in, float* out, float scale, const Scalars* sc, cudaStream_t s);
+// adjoint and chain
+void launch_adj_rhs(const Launch& L, const Fields& F, const float* gu, const float* gv, const float* gw,
+                    const float* gp, float dt, cudaStream_t s);
+void launch_adj_correct(const Launch& L, const Fields& F, const double* psi, const float* gu, const float* gv,
+                        const float* gw, float* ou, float* ov, float* ow, cudaStream_t s);
+void launch_add_force(const Launch& L, const Fields& F, const float* u, const float* v, const float* w,
+                      const float* fu, const float* fv, const float* fw, float dt, float* su, float* sv, float* sw,
+                      cudaStream_t s);
+void launch_force_grad(const Launch& L, const Fields& F, const float* lu, const float* lv, const float* lw, float dt,
+                       double* gu, double* gv, double* gw, cudaStream_t s);
+void launch_outlet_objective(const Launch& L, const Fields& F, const float* w, float* seed_w, cudaStream_t s);
+
+// ---- multigrid (mg_kernels.cu)
+struct MGLevel {
+    Launch L;
+    float4* coef32;  // FP32 master coefficients (level 0: the fine cache)
+    void* coef_lo;   // level-precision copy (nullptr in FP32 mode)
+    void* r;         // level residual (level 0: the CG residual, FP32)
+    void* e;         // level correction (level 0: the preconditioned residual z, FP32)
+    void* tmp;       // half-step scratch for levels with odd periodic extents
+    bool odd_periodic;
+};
+struct MGPlan {
+    int precision;  // 0 fp32, 1 fp16, 2 bf16
+    int nlevels;
+    MGLevel lv[32];
+    float* ainv;    // dense inverse of the coarsest operator (m x m)
+    int m;
+    float prolong;  // coarse-correction weight
+    Scalars* sc;
+};
+void mg_build(const MGPlan& P, cudaStream_t s);
+void mg_vcycle(const MGPlan& P, cudaStream_t s);
+cudaError_t mg_prepare_attributes();
+
+}  // namespace mhdproj

@@ -1,0 +1,366 @@
+// mg_kernels.cu -- the GB300 solver's multigrid preconditioner.
+//
+// Hierarchy: the reference's 2x2x2 aggregation (src/fluid/multigrid.rs:25-65:
+// halve with ceiling until every extent is <= 4) with piecewise-constant
+// prolongation P and the Galerkin coarse graph P^T A P (multigrid.wgsl:50-65:
+// crossing edges summed, reactions summed, internal edges dropped).  Each
+// level is stored scaled by a power of two so FP16 fields stay in range:
+//   coarse coefficients   A_{l+1} = 1/4 P^T A_l P
+//   restriction           r_{l+1} = 1/4 P^T (r_l - A_l e_l)
+//   prolongation          e_l    += w P e_{l+1}          (w = 2 by default)
+// which is a coarse correction of w P (P^T A P)^-1 P^T.  Smoothing is one
+// red-black Gauss-Seidel sweep before (red, black) and after (black, red) the
+// coarse correction, and the coarsest level (<= 64 cells) is solved exactly
+// with a dense inverse, so the V-cycle is a fixed symmetric operator.
+// Level fields (coefficients and vectors of levels >= 1, the fine smoother's
+// coefficients) are FP32, FP16 or BF16; arithmetic is FP32.
+#include "kernels.h"
+
+namespace mhdproj {
+
+#define TILE_BEGIN(G)                                      \
+    const int x = blockIdx.x * TX + threadIdx.x;           \
+    const int y = blockIdx.y * TY + threadIdx.y;           \
+    const bool in_xy = x < (G).nx && y < (G).ny;           \
+    const int z0 = blockIdx.z * (G).zper;                  \
+    const int z1 = min((G).nz, z0 + (G).zper);             \
+    for (int z = z0; z < z1; z++)
+
+template <int CK> __device__ __forceinline__ float4 ldc(const void* p, int i);
+template <> __device__ __forceinline__ float4 ldc<0>(const void* p, int i) {
+    return load_coef(reinterpret_cast<const float4*>(p), i);
+}
+template <> __device__ __forceinline__ float4 ldc<1>(const void* p, int i) {
+    return load_coef_h(reinterpret_cast<const uint2*>(p), i);
+}
+template <> __device__ __forceinline__ float4 ldc<2>(const void* p, int i) {
+    return load_coef_b(reinterpret_cast<const uint2*>(p), i);
+}
+
+struct Stencil {
+    int xm, xp, ym, yp, zm, zp;
+    float bxl, byl, bzl, bxh, byh, bzh, react, diag;
+};
+template <int CK>
+__device__ __forceinline__ Stencil stencil(const Grid3& g, const void* coef, int x, int y, int z) {
+    Stencil s;
+    const int sy = g.nx, sz = g.nx * g.ny;
+    const int i = x + sy * y + sz * z;
+    int c;
+    c = wrap_or_neg(x - 1, g.nx, g.periodic & 1); s.xm = c < 0 ? -1 : i + (c - x);
+    c = wrap_or_neg(x + 1, g.nx, g.periodic & 1); s.xp = c < 0 ? -1 : i + (c - x);
+    c = wrap_or_neg(y - 1, g.ny, g.periodic & 2); s.ym = c < 0 ? -1 : i + (c - y) * sy;
+    c = wrap_or_neg(y + 1, g.ny, g.periodic & 2); s.yp = c < 0 ? -1 : i + (c - y) * sy;
+    c = wrap_or_neg(z - 1, g.nz, g.periodic & 4); s.zm = c < 0 ? -1 : i + (c - z) * sz;
+    c = wrap_or_neg(z + 1, g.nz, g.periodic & 4); s.zp = c < 0 ? -1 : i + (c - z) * sz;
+    const float4 own = ldc<CK>(coef, i);
+    s.bxl = own.x;
+    s.byl = own.y;
+    s.bzl = own.z;
+    s.react = own.w;
+    s.bxh = s.xp >= 0 ? ldc<CK>(coef, s.xp).x : 0.0f;
+    s.byh = s.yp >= 0 ? ldc<CK>(coef, s.yp).y : 0.0f;
+    s.bzh = s.zp >= 0 ? ldc<CK>(coef, s.zp).z : 0.0f;
+    s.diag = ((s.bxl + s.bxh) + (s.byl + s.byh)) + ((s.bzl + s.bzh) + s.react);
+    return s;
+}
+// sum of beta * e over the six neighbours
+template <class VT>
+__device__ __forceinline__ float neighbour_sum(const Stencil& s, const VT* e) {
+    float acc = 0.0f;
+    if (s.bxl != 0.0f) acc = fmaf(s.bxl, to_f(e[s.xm]), acc);
+    if (s.bxh != 0.0f) acc = fmaf(s.bxh, to_f(e[s.xp]), acc);
+    if (s.byl != 0.0f) acc = fmaf(s.byl, to_f(e[s.ym]), acc);
+    if (s.byh != 0.0f) acc = fmaf(s.byh, to_f(e[s.yp]), acc);
+    if (s.bzl != 0.0f) acc = fmaf(s.bzl, to_f(e[s.zm]), acc);
+    if (s.bzh != 0.0f) acc = fmaf(s.bzh, to_f(e[s.zp]), acc);
+    return acc;
+}
+
+// One red-black Gauss-Seidel half-step on `color` cells.  ZERO: the first
+// half-step from a zero correction (e = rhs/diag on color cells, 0 elsewhere).
+// OUT: write color cells to `out` instead of in place (levels whose periodic
+// extents are odd have same-colour neighbours across the wrap).
+template <int CK, class VT, bool FINE, bool ZERO, bool OUT>
+__global__ void __launch_bounds__(TILE_THREADS) k_smooth(Grid3 g, const void* __restrict__ coef,
+                                                         const VT* __restrict__ r, VT* e, VT* out, int color,
+                                                         const Scalars* sc) {
+    if (sc->converged) return;
+    const float sigma = FINE ? sc->sigma : 1.0f;
+    TILE_BEGIN(g) {
+        if (!in_xy) continue;
+        const int i = x + g.nx * (y + g.ny * z);
+        if (((x + y + z) & 1) != color) {
+            if (ZERO) e[i] = from_f<VT>(0.0f);
+            continue;
+        }
+        const Stencil s = stencil<CK>(g, coef, x, y, z);
+        float val = 0.0f;
+        if (s.diag > 0.0f) {
+            const float rhs = sigma * to_f(r[i]);
+            if (ZERO) val = rhs / s.diag;
+            else val = (rhs + neighbour_sum<VT>(s, e)) / s.diag;
+        }
+        if (OUT) out[i] = from_f<VT>(val);
+        else e[i] = from_f<VT>(val);
+    }
+}
+template <class VT>
+__global__ void __launch_bounds__(TILE_THREADS) k_copy_color(Grid3 g, const VT* __restrict__ in, VT* __restrict__ e,
+                                                             int color, const Scalars* sc) {
+    if (sc->converged) return;
+    TILE_BEGIN(g) {
+        if (!in_xy) continue;
+        if (((x + y + z) & 1) != color) continue;
+        const int i = x + g.nx * (y + g.ny * z);
+        e[i] = in[i];
+    }
+}
+
+// Residual of the children and restriction: rc[Q] = 1/4 sum (rhs - A e).
+template <int CK, class VTf, bool FINE, class VTc>
+__global__ void __launch_bounds__(TILE_THREADS) k_restrict(Grid3 gf, Grid3 gc, const void* __restrict__ coef,
+                                                           const VTf* __restrict__ r, const VTf* __restrict__ e,
+                                                           VTc* __restrict__ rc, const Scalars* sc) {
+    if (sc->converged) return;
+    const float sigma = FINE ? sc->sigma : 1.0f;
+    TILE_BEGIN(gc) {
+        if (!in_xy) continue;
+        float sum = 0.0f;
+#pragma unroll
+        for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+            for (int dy = 0; dy < 2; dy++)
+#pragma unroll
+                for (int dx = 0; dx < 2; dx++) {
+                    const int cx = 2 * x + dx, cy = 2 * y + dy, cz = 2 * z + dz;
+                    if (cx >= gf.nx || cy >= gf.ny || cz >= gf.nz) continue;
+                    const int ci = cx + gf.nx * (cy + gf.ny * cz);
+                    const Stencil s = stencil<CK>(gf, coef, cx, cy, cz);
+                    const float ec = to_f(e[ci]);
+                    const float res = sigma * to_f(r[ci]) - (s.diag * ec - neighbour_sum<VTf>(s, e));
+                    sum += res;
+                }
+        rc[x + gc.nx * (y + gc.ny * z)] = from_f<VTc>(0.25f * sum);
+    }
+}
+
+template <class VTf, class VTc>
+__global__ void __launch_bounds__(TILE_THREADS) k_prolong(Grid3 gf, Grid3 gc, VTf* __restrict__ e,
+                                                          const VTc* __restrict__ ec, float w, const Scalars* sc) {
+    if (sc->converged) return;
+    TILE_BEGIN(gf) {
+        if (!in_xy) continue;
+        const int i = x + gf.nx * (y + gf.ny * z);
+        const int Q = (x >> 1) + gc.nx * ((y >> 1) + gc.ny * (z >> 1));
+        e[i] = from_f<VTf>(fmaf(w, to_f(ec[Q]), to_f(e[i])));
+    }
+}
+
+// Exact coarsest solve: e = Ainv * rhs (m <= 64).
+template <class VT, bool FINE>
+__global__ void k_coarse_solve(int m, const float* __restrict__ ainv, const VT* __restrict__ r, VT* __restrict__ e,
+                               const Scalars* sc) {
+    if (sc->converged) return;
+    __shared__ float rhs[64];
+    const float sigma = FINE ? sc->sigma : 1.0f;
+    const int t = threadIdx.x;
+    if (t < m) rhs[t] = sigma * to_f(r[t]);
+    __syncthreads();
+    if (t < m) {
+        float s = 0.0f;
+        for (int k = 0; k < m; k++) s = fmaf(ainv[t * m + k], rhs[k], s);
+        e[t] = from_f<VT>(s);
+    }
+}
+
+// Galerkin coarse graph of one level from the FP32 master of the finer one.
+template <int CKLO>
+__global__ void __launch_bounds__(TILE_THREADS) k_mg_build(Grid3 gf, Grid3 gc, const float4* __restrict__ cf,
+                                                           float4* __restrict__ cc, void* __restrict__ lo) {
+    TILE_BEGIN(gc) {
+        if (!in_xy) continue;
+        float c[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int dz = 0; dz < 2; dz++)
+            for (int dy = 0; dy < 2; dy++)
+                for (int dx = 0; dx < 2; dx++) {
+                    const int cx = 2 * x + dx, cy = 2 * y + dy, cz = 2 * z + dz;
+                    if (cx >= gf.nx || cy >= gf.ny || cz >= gf.nz) continue;
+                    const int ci = cx + gf.nx * (cy + gf.ny * cz);
+                    const float4 f = cf[ci];
+                    c[3] += f.w;
+                    const float fb[3] = {f.x, f.y, f.z};
+                    const int cc3[3] = {cx, cy, cz}, n3[3] = {gf.nx, gf.ny, gf.nz}, q3[3] = {x, y, z};
+#pragma unroll
+                    for (int a = 0; a < 3; a++) {
+                        const int l = wrap_or_neg(cc3[a] - 1, n3[a], gf.periodic & (1 << a));
+                        if (l < 0) continue;
+                        const float beta = fb[a];
+                        if (beta == 0.0f) continue;
+                        // The low neighbour differs from the child only along a.
+                        if ((l >> 1) == q3[a]) continue;
+                        c[a] += beta;
+                    }
+                }
+        const float4 out = make_float4(c[0] * 0.25f, c[1] * 0.25f, c[2] * 0.25f, c[3] * 0.25f);
+        const int Q = x + gc.nx * (y + gc.ny * z);
+        cc[Q] = out;
+        if (CKLO == 1) reinterpret_cast<uint2*>(lo)[Q] = pack_coef_h(out);
+        if (CKLO == 2) reinterpret_cast<uint2*>(lo)[Q] = pack_coef_b(out);
+    }
+}
+
+// Dense inverse of the coarsest operator by Gauss-Jordan in FP64, one block.
+// Rows of empty aggregates (diagonal 0) become identity rows and are zeroed
+// in the stored inverse.  The result is symmetrised.
+__global__ void k_coarse_invert(Grid3 g, const float4* __restrict__ coef, float* __restrict__ ainv) {
+    extern __shared__ double A[];  // m x 2m
+    const int m = g.nx * g.ny * g.nz;
+    const int w = 2 * m;
+    const int t = threadIdx.x, nt = blockDim.x;
+    __shared__ int active[64];
+    for (int k = t; k < m * w; k += nt) A[k] = 0.0;
+    __syncthreads();
+    if (t < m) {
+        const int x = t % g.nx, y = (t / g.nx) % g.ny, z = t / (g.nx * g.ny);
+        const float4 c = coef[t];
+        double d = c.w;
+        const int n3[3] = {g.nx, g.ny, g.nz}, p3[3] = {x, y, z};
+        const float lowb[3] = {c.x, c.y, c.z};
+        for (int a = 0; a < 3; a++) {
+            const int stride = a == 0 ? 1 : (a == 1 ? g.nx : g.nx * g.ny);
+            const int lm = wrap_or_neg(p3[a] - 1, n3[a], g.periodic & (1 << a));
+            const int lp = wrap_or_neg(p3[a] + 1, n3[a], g.periodic & (1 << a));
+            if (lm >= 0 && lowb[a] != 0.0f) {
+                d += lowb[a];
+                A[t * w + (t + (lm - p3[a]) * stride)] -= lowb[a];
+            }
+            if (lp >= 0) {
+                const int j = t + (lp - p3[a]) * stride;
+                const float bh = (a == 0 ? coef[j].x : (a == 1 ? coef[j].y : coef[j].z));
+                if (bh != 0.0f) {
+                    d += bh;
+                    A[t * w + j] -= bh;
+                }
+            }
+        }
+        A[t * w + t] += d;
+        active[t] = d > 0.0;
+        A[t * w + m + t] = 1.0;
+    }
+    __syncthreads();
+    if (t < m && !active[t]) {
+        for (int k = 0; k < m; k++) A[t * w + k] = 0.0;
+        A[t * w + t] = 1.0;
+    }
+    __syncthreads();
+    for (int c = 0; c < m; c++) {
+        const double piv = A[c * w + c];
+        __syncthreads();
+        const bool ok = fabs(piv) > 1e-300;
+        for (int k = t; k < w; k += nt)
+            if (ok) A[c * w + k] /= piv;
+        __syncthreads();
+        for (int k = t; k < m * w; k += nt) {
+            const int r = k / w, col = k % w;
+            if (r == c || !ok) continue;
+            const double f = A[r * w + c];
+            if (f != 0.0 && col != c) A[k] -= f * A[c * w + col];
+        }
+        __syncthreads();
+        for (int r = t; r < m; r += nt)
+            if (r != c && ok) A[r * w + c] = 0.0;
+        __syncthreads();
+    }
+    for (int k = t; k < m * m; k += nt) {
+        const int i = k / m, j = k % m;
+        const double v = (active[i] && active[j]) ? 0.5 * (A[i * w + m + j] + A[j * w + m + i]) : 0.0;
+        ainv[k] = (float)v;
+    }
+}
+
+// ------------------------------------------------------------- host side
+template <int CK, class VT>
+static void enqueue_smooth(const MGPlan& P, int l, int color, bool zero, cudaStream_t s) {
+    const MGLevel& L = P.lv[l];
+    const void* coef = P.precision == 0 ? (const void*)L.coef32 : L.coef_lo;
+    if (l == 0) {
+        const float* r = (const float*)L.r;
+        float* e = (float*)L.e;
+        if (zero) k_smooth<CK, float, true, true, false><<<L.L.grid, L.L.block, 0, s>>>(L.L.g, coef, r, e, e, color, P.sc);
+        else if (!L.odd_periodic)
+            k_smooth<CK, float, true, false, false><<<L.L.grid, L.L.block, 0, s>>>(L.L.g, coef, r, e, e, color, P.sc);
+        else {
+            float* t = (float*)L.tmp;
+            k_smooth<CK, float, true, false, true><<<L.L.grid, L.L.block, 0, s>>>(L.L.g, coef, r, e, t, color, P.sc);
+            k_copy_color<float><<<L.L.grid, L.L.block, 0, s>>>(L.L.g, t, e, color, P.sc);
+        }
+    } else {
+        const VT* r = (const VT*)L.r;
+        VT* e = (VT*)L.e;
+        if (zero) k_smooth<CK, VT, false, true, false><<<L.L.grid, L.L.block, 0, s>>>(L.L.g, coef, r, e, e, color, P.sc);
+        else if (!L.odd_periodic)
+            k_smooth<CK, VT, false, false, false><<<L.L.grid, L.L.block, 0, s>>>(L.L.g, coef, r, e, e, color, P.sc);
+        else {
+            VT* t = (VT*)L.tmp;
+            k_smooth<CK, VT, false, false, true><<<L.L.grid, L.L.block, 0, s>>>(L.L.g, coef, r, e, t, color, P.sc);
+            k_copy_color<VT><<<L.L.grid, L.L.block, 0, s>>>(L.L.g, t, e, color, P.sc);
+        }
+    }
+}
+
+template <int CK, class VT>
+static void vcycle_impl(const MGPlan& P, cudaStream_t s) {
+    const int nl = P.nlevels;
+    for (int l = 0; l + 1 < nl; l++) {
+        enqueue_smooth<CK, VT>(P, l, 0, true, s);
+        enqueue_smooth<CK, VT>(P, l, 1, false, s);
+        const MGLevel &F = P.lv[l], &C = P.lv[l + 1];
+        const void* coef = P.precision == 0 ? (const void*)F.coef32 : F.coef_lo;
+        if (l == 0)
+            k_restrict<CK, float, true, VT><<<C.L.grid, C.L.block, 0, s>>>(F.L.g, C.L.g, coef, (const float*)F.r,
+                                                                           (const float*)F.e, (VT*)C.r, P.sc);
+        else
+            k_restrict<CK, VT, false, VT><<<C.L.grid, C.L.block, 0, s>>>(F.L.g, C.L.g, coef, (const VT*)F.r,
+                                                                         (const VT*)F.e, (VT*)C.r, P.sc);
+    }
+    const MGLevel& K = P.lv[nl - 1];
+    if (nl == 1) k_coarse_solve<float, true><<<1, 64, 0, s>>>(P.m, P.ainv, (const float*)K.r, (float*)K.e, P.sc);
+    else k_coarse_solve<VT, false><<<1, 64, 0, s>>>(P.m, P.ainv, (const VT*)K.r, (VT*)K.e, P.sc);
+    for (int l = nl - 2; l >= 0; l--) {
+        const MGLevel &F = P.lv[l], &C = P.lv[l + 1];
+        if (l == 0)
+            k_prolong<float, VT><<<F.L.grid, F.L.block, 0, s>>>(F.L.g, C.L.g, (float*)F.e, (const VT*)C.e, P.prolong, P.sc);
+        else
+            k_prolong<VT, VT><<<F.L.grid, F.L.block, 0, s>>>(F.L.g, C.L.g, (VT*)F.e, (const VT*)C.e, P.prolong, P.sc);
+        enqueue_smooth<CK, VT>(P, l, 1, false, s);
+        enqueue_smooth<CK, VT>(P, l, 0, false, s);
+    }
+}
+
+void mg_vcycle(const MGPlan& P, cudaStream_t s) {
+    if (P.precision == 1) vcycle_impl<1, __half>(P, s);
+    else if (P.precision == 2) vcycle_impl<2, __nv_bfloat16>(P, s);
+    else vcycle_impl<0, float>(P, s);
+}
+
+void mg_build(const MGPlan& P, cudaStream_t s) {
+    for (int l = 1; l < P.nlevels; l++) {
+        const MGLevel &F = P.lv[l - 1], &C = P.lv[l];
+        if (P.precision == 1)
+            k_mg_build<1><<<C.L.grid, C.L.block, 0, s>>>(F.L.g, C.L.g, F.coef32, C.coef32, C.coef_lo);
+        else if (P.precision == 2)
+            k_mg_build<2><<<C.L.grid, C.L.block, 0, s>>>(F.L.g, C.L.g, F.coef32, C.coef32, C.coef_lo);
+        else
+            k_mg_build<0><<<C.L.grid, C.L.block, 0, s>>>(F.L.g, C.L.g, F.coef32, C.coef32, nullptr);
+    }
+    const MGLevel& K = P.lv[P.nlevels - 1];
+    const size_t smem = (size_t)P.m * 2 * P.m * sizeof(double);
+    k_coarse_invert<<<1, 256, smem, s>>>(K.L.g, K.coef32, P.ainv);
+}
+
+cudaError_t mg_prepare_attributes() {
+    return cudaFuncSetAttribute(k_coarse_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 128 * 8);
+}
+
+}  // namespace mhdproj

@@ -1,0 +1,23 @@
+// reference.h -- the reference solver (FP32 Jacobi-CG / aggregation-MG CG with
+// the reference's gauges and convergence tests) behind the same context.
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include "../../include/mhdproj.h"
+
+namespace mhdproj {
+struct RefState;
+int ref_create(RefState** out, const mhdproj_grid* grid, const mhdproj_options* opt, cudaStream_t stream,
+               std::string& err);
+void ref_destroy(RefState* s);
+void ref_set_stream(RefState* s, cudaStream_t stream);
+int ref_set_topology(RefState* s, const uint32_t* mask_host, uint32_t components, std::string& err);
+int ref_set_coefficients(RefState* s, const float* alpha, float rho_l, float rho_air, std::string& err);
+int ref_set_phase_drag(RefState* s, const float* phase, float drag_rate, float dt, std::string& err);
+int ref_project(RefState* s, const float* us, const float* vs, const float* ws, float* uo, float* vo, float* wo,
+                float* po, float dt, int warm, mhdproj_stats* st, std::string& err);
+int ref_apply_operator(RefState* s, const float* x, float* y, std::string& err);
+int ref_apply_preconditioner(RefState* s, const float* r, float* z, std::string& err);
+int ref_copy_coefficients(RefState* s, float* coef4, std::string& err);
+int ref_copy_potential(RefState* s, double* phi, std::string& err);
+}  // namespace mhdproj

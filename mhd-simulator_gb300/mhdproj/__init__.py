@@ -1,0 +1,325 @@
+"""Python mirror of the projection interface, over the C ABI of libmhdproj.so.
+
+The reference's projection is a private Rust method,
+``FluidState::project(warm_start) -> Result<(u32 iterations, f32 residual), String>``
+(src/fluid/mod.rs:1015-1115), working on buffers its ``FluidState`` owns.  This
+module keeps that shape: a :class:`PressureProjection` owns the solver state,
+:meth:`PressureProjection.set_coefficients` plays the part of the coefficient
+cache and gauge set-up (pressure_coefficients, anchors), and
+:meth:`PressureProjection.project` returns ``(iterations, residual)`` or raises
+:class:`ProjectionError` with the reference's messages.
+
+Device memory comes from torch (CUDA tensors, passed as raw pointers); the
+CUDA work is the library's own kernels.  There is no CPU fallback: without a
+built library or a GPU every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmhdproj.so")
+
+SOLVERS = {"reference": 0, "gb300": 1}
+PRECISIONS = {"fp32": 0, "fp16": 1, "bf16": 2}
+PRECONDITIONERS = {"auto": -1, "jacobi": 0, "multigrid": 1}
+STATUS = {
+    0: "ok",
+    1: "invalid argument",
+    2: "CUDA error",
+    3: "not converged",
+    4: "non-finite residual",
+    5: "no progress",
+    6: "call order",
+    7: "out of memory",
+    8: "timeout",
+}
+
+
+class Grid(C.Structure):
+    _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("nz", C.c_uint32), ("h", C.c_float),
+                ("periodic", C.c_uint32), ("boundary", C.c_int32)]
+
+
+class Options(C.Structure):
+    _fields_ = [("solver", C.c_int32), ("precision", C.c_int32), ("preconditioner", C.c_int32),
+                ("rel_tol", C.c_float), ("abs_div_tol", C.c_float), ("max_iterations", C.c_uint32),
+                ("max_refinements", C.c_int32), ("two_phase", C.c_int32), ("gauge", C.c_int32),
+                ("compute_divergence", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("refinements", C.c_uint32), ("relative_residual", C.c_float),
+                ("true_relative_residual", C.c_double), ("max_divergence", C.c_double),
+                ("rms_divergence", C.c_double), ("elapsed_ms", C.c_float), ("meanfree", C.c_int32),
+                ("multigrid", C.c_int32), ("levels", C.c_uint32), ("coarse_cells", C.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ProjectionError(RuntimeError):
+    """A failed projection; ``code`` is the mhdproj_status value."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+        self.status = STATUS.get(code, "unknown")
+
+
+_lib = None
+_vp = C.c_void_p
+
+
+def load():
+    """Load libmhdproj.so (built by ``mhdproj.build.build()``).  Raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with mhdproj.build.build() (needs nvcc)")
+    L = C.CDLL(LIB_PATH)
+    L.mhdproj_default_options.argtypes = [C.POINTER(Options)]
+    L.mhdproj_create.argtypes = [C.POINTER(Grid), C.POINTER(Options), C.POINTER(_vp)]
+    L.mhdproj_destroy.argtypes = [_vp]
+    L.mhdproj_last_error.argtypes = [_vp]
+    L.mhdproj_last_error.restype = C.c_char_p
+    L.mhdproj_set_stream.argtypes = [_vp, _vp]
+    L.mhdproj_set_coefficients.argtypes = [_vp, _vp, _vp, C.c_float, C.c_float]
+    L.mhdproj_set_phase_drag.argtypes = [_vp, _vp, C.c_float, C.c_float]
+    L.mhdproj_project.argtypes = [_vp] + [_vp] * 7 + [C.c_float, C.c_int, C.POINTER(Stats)]
+    L.mhdproj_project_host.argtypes = [_vp, _vp, _vp, C.c_float, C.c_float] + [_vp] * 7 + [C.c_float, C.c_int,
+                                                                                          C.POINTER(Stats)]
+    L.mhdproj_project_vjp.argtypes = [_vp] + [_vp] * 4 + [C.c_float] + [_vp] * 3 + [C.POINTER(Stats)]
+    L.mhdproj_chain_forward.argtypes = [_vp] + [_vp] * 6 + [C.c_float, C.c_int, C.c_int] + [_vp] * 3 + [
+        C.POINTER(C.c_double), C.POINTER(Stats)]
+    L.mhdproj_chain_backward.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(Stats)]
+    L.mhdproj_apply_operator.argtypes = [_vp, _vp, _vp]
+    L.mhdproj_apply_preconditioner.argtypes = [_vp, _vp, _vp]
+    L.mhdproj_copy_coefficients.argtypes = [_vp, _vp]
+    L.mhdproj_copy_potential.argtypes = [_vp, _vp]
+    L.mhdproj_copy_topology.argtypes = [_vp, _vp, C.POINTER(C.c_uint32)]
+    L.mhdproj_hierarchy.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)]
+    L.mhdproj_anchors.argtypes = [_vp, C.POINTER(C.c_uint32), C.c_uint32]
+    L.mhdproj_anchors.restype = C.c_uint32
+    _lib = L
+    return L
+
+
+EXPORTED = [
+    "mhdproj_default_options", "mhdproj_create", "mhdproj_destroy", "mhdproj_last_error", "mhdproj_set_stream",
+    "mhdproj_set_coefficients", "mhdproj_set_phase_drag", "mhdproj_project", "mhdproj_project_host",
+    "mhdproj_project_vjp", "mhdproj_chain_forward", "mhdproj_chain_backward", "mhdproj_apply_operator",
+    "mhdproj_apply_preconditioner", "mhdproj_copy_coefficients", "mhdproj_copy_potential", "mhdproj_copy_topology",
+    "mhdproj_hierarchy", "mhdproj_anchors",
+]
+
+
+def hierarchy(dims4):
+    """hierarchy() of src/fluid/multigrid.rs:25-65: (levels, coarse cells); raises on rejected grids."""
+    L = load()
+    d = (C.c_uint32 * 4)(*[int(v) & 0xFFFFFFFF for v in dims4])
+    nl, cc = C.c_uint32(), C.c_uint64()
+    if L.mhdproj_hierarchy(d, C.byref(nl), C.byref(cc)):
+        raise ValueError("Invalid pressure grid dimensions")
+    return nl.value, cc.value
+
+
+def anchors(mask, dims, periodic_bits=0):
+    """anchors() of src/fluid/mod.rs:1447-1493 on a 0/1 mask: (components, encoded mask)."""
+    L = load()
+    m = np.ascontiguousarray(mask, dtype=np.uint32).reshape(-1).copy()
+    comps = L.mhdproj_anchors(m.ctypes.data_as(_vp), (C.c_uint32 * 3)(*dims), periodic_bits)
+    return int(comps), m
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("expected a contiguous CUDA tensor")
+    return C.c_void_p(t.data_ptr())
+
+
+def _host_ptr(a):
+    return None if a is None else a.ctypes.data_as(_vp)
+
+
+class PressureProjection:
+    """One projection context (mhdproj_ctx) on the current CUDA device.
+
+    dims = (nx, ny, nz); h the cell size in metres; periodic a triple of
+    booleans; outlet selects a Dirichlet p = 0 top z-face.  Face velocity
+    tensors have shapes (nz, ny, nx+1), (nz, ny+1, nx), (nz+1, ny, nx); cell
+    tensors (nz, ny, nx).
+    """
+
+    def __init__(self, dims, h, periodic=(False, False, False), outlet=True, solver="gb300", precision="fp16",
+                 preconditioner="auto", rel_tol=1e-6, abs_div_tol=0.0, max_iterations=20000, max_refinements=4,
+                 two_phase=True, gauge=-1, compute_divergence=False, stream=None):
+        import torch
+
+        self._torch = torch
+        L = load()
+        self.dims = tuple(int(d) for d in dims)
+        self.h = float(h)
+        bits = sum(1 << a for a, p in enumerate(periodic) if p)
+        self.periodic_bits = bits
+        g = Grid(self.dims[0], self.dims[1], self.dims[2], self.h, bits, 1 if outlet else 0)
+        o = Options()
+        L.mhdproj_default_options(C.byref(o))
+        o.solver = SOLVERS[solver]
+        o.precision = PRECISIONS[precision]
+        o.preconditioner = PRECONDITIONERS[preconditioner]
+        o.rel_tol = rel_tol
+        o.abs_div_tol = abs_div_tol
+        o.max_iterations = max_iterations
+        o.max_refinements = max_refinements
+        o.two_phase = int(two_phase)
+        o.gauge = gauge
+        o.compute_divergence = int(compute_divergence)
+        self.options = o
+        h_ = C.c_void_p()
+        rc = L.mhdproj_create(C.byref(g), C.byref(o), C.byref(h_))
+        if rc:
+            raise ProjectionError(rc, L.mhdproj_last_error(None).decode())
+        self._ctx = h_
+        self._lib = L
+        s = stream if stream is not None else torch.cuda.current_stream()
+        self._check(L.mhdproj_set_stream(self._ctx, C.c_void_p(s.cuda_stream)))
+        self.solver = solver
+
+    # ------------------------------------------------------------ helpers
+    def _check(self, rc):
+        if rc:
+            raise ProjectionError(rc, self._lib.mhdproj_last_error(self._ctx).decode())
+
+    def face_shapes(self):
+        nx, ny, nz = self.dims
+        return (nz, ny, nx + 1), (nz, ny + 1, nx), (nz + 1, ny, nx)
+
+    def cell_shape(self):
+        nx, ny, nz = self.dims
+        return (nz, ny, nx)
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._lib.mhdproj_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---------------------------------------------------------- interface
+    def set_coefficients(self, alpha, solid, rho_liquid, rho_air):
+        self._check(self._lib.mhdproj_set_coefficients(self._ctx, _ptr(alpha), _ptr(solid), rho_liquid, rho_air))
+
+    def set_phase_drag(self, phase, drag_rate, dt):
+        self._check(self._lib.mhdproj_set_phase_drag(self._ctx, _ptr(phase), drag_rate, dt))
+
+    def project(self, u_star, dt, warm_start=False, out=None, pressure=True):
+        """Project (u*, v*, w*) -> ((u, v, w), p, stats)."""
+        torch = self._torch
+        if out is None:
+            out = tuple(torch.empty_like(t) for t in u_star)
+        p = torch.empty(self.cell_shape(), dtype=torch.float32, device=u_star[0].device) if pressure else None
+        st = Stats()
+        self._check(self._lib.mhdproj_project(self._ctx, *[_ptr(t) for t in u_star], *[_ptr(t) for t in out],
+                                              _ptr(p), dt, int(warm_start), C.byref(st)))
+        return out, p, st
+
+    def project_host(self, alpha, solid, rho_liquid, rho_air, u_star, dt, warm_start=False, out=None, p_out=None):
+        """The same call on numpy host arrays (copies inside the call)."""
+        if out is None:
+            out = tuple(np.empty_like(a) for a in u_star)
+        if p_out is None:
+            p_out = np.empty(self.cell_shape(), np.float32)
+        st = Stats()
+        self._check(self._lib.mhdproj_project_host(self._ctx, _host_ptr(alpha), _host_ptr(solid), rho_liquid, rho_air,
+                                                   *[_host_ptr(a) for a in u_star], *[_host_ptr(a) for a in out],
+                                                   _host_ptr(p_out), dt, int(warm_start), C.byref(st)))
+        return out, p_out, st
+
+    def vjp(self, grad_u, grad_p, dt):
+        torch = self._torch
+        out = tuple(torch.empty_like(t) for t in grad_u)
+        st = Stats()
+        self._check(self._lib.mhdproj_project_vjp(self._ctx, *[_ptr(t) for t in grad_u], _ptr(grad_p), dt,
+                                                  *[_ptr(t) for t in out], C.byref(st)))
+        return out, st
+
+    def chain_forward(self, u0, force, dt, steps, checkpoint_every=4):
+        torch = self._torch
+        uf = tuple(torch.empty_like(t) for t in u0)
+        J = C.c_double()
+        st = Stats()
+        self._check(self._lib.mhdproj_chain_forward(self._ctx, *[_ptr(t) for t in u0], *[_ptr(t) for t in force], dt,
+                                                    steps, checkpoint_every, *[_ptr(t) for t in uf], C.byref(J),
+                                                    C.byref(st)))
+        return uf, J.value, st
+
+    def chain_backward(self, like):
+        torch = self._torch
+        g = tuple(torch.empty_like(t) for t in like)
+        st = Stats()
+        self._check(self._lib.mhdproj_chain_backward(self._ctx, *[_ptr(t) for t in g], C.byref(st)))
+        return g, st
+
+    def apply_operator(self, x):
+        y = self._torch.empty_like(x)
+        self._check(self._lib.mhdproj_apply_operator(self._ctx, _ptr(x), _ptr(y)))
+        return y
+
+    def apply_preconditioner(self, r):
+        z = self._torch.empty_like(r)
+        self._check(self._lib.mhdproj_apply_preconditioner(self._ctx, _ptr(r), _ptr(z)))
+        return z
+
+    def coefficients(self):
+        torch = self._torch
+        c = torch.empty(self.cell_shape() + (4,), dtype=torch.float32, device="cuda")
+        self._check(self._lib.mhdproj_copy_coefficients(self._ctx, _ptr(c)))
+        return c
+
+    def potential(self):
+        torch = self._torch
+        phi = torch.empty(self.cell_shape(), dtype=torch.float64, device="cuda")
+        self._check(self._lib.mhdproj_copy_potential(self._ctx, _ptr(phi)))
+        return phi
+
+    def topology(self):
+        n = self.dims[0] * self.dims[1] * self.dims[2]
+        m = np.zeros(n, np.uint32)
+        comps = C.c_uint32()
+        self._check(self._lib.mhdproj_copy_topology(self._ctx, m.ctypes.data_as(_vp), C.byref(comps)))
+        return m, comps.value
+
+
+def autograd_projection():
+    """torch.autograd.Function pair over forward projection and its VJP:
+    ``ProjectFn.apply(proj, dt, u, v, w) -> (u', v', w', p)``."""
+    import torch
+
+    class ProjectFn(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, proj, dt, u, v, w):
+            (uo, vo, wo), p, _ = proj.project((u.contiguous(), v.contiguous(), w.contiguous()), dt)
+            ctx.proj = proj
+            ctx.dt = dt
+            return uo, vo, wo, p
+
+        @staticmethod
+        def backward(ctx, gu, gv, gw, gp):
+            grads = [g.contiguous() if g is not None else None for g in (gu, gv, gw)]
+            shapes = ctx.proj.face_shapes()
+            grads = [g if g is not None else torch.zeros(s, device="cuda") for g, s in zip(grads, shapes)]
+            (a, b, c), _ = ctx.proj.vjp(tuple(grads), gp.contiguous() if gp is not None else None, ctx.dt)
+            return None, None, a, b, c
+
+    return ProjectFn

@@ -1,0 +1,190 @@
+"""Seeded synthetic inputs for the projection workloads.
+
+The reference measures no public benchmark or dataset for this path, so every
+workload is a deterministic synthetic field: a counter-based splitmix64
+stream per field (seed, field id), uniform doubles from the top 53 bits,
+Box-Muller normals in double, cast to FP32.
+
+Workloads (grid sizes at scale 1):
+  jet64        64^3, h=0.1 mm, single-phase liquid rho=6440, solid outside a
+               z-aligned cylinder of radius 28 cells, outlet on the top z-face,
+               face velocities N(0, 0.05 m/s) zeroed on closed faces.
+  jet128       128^3, h=0.05 mm, rho 6440:1.2.  Liquid fraction: tanh-smoothed
+               (width 1.5 cells) union of a z-cylinder jet of radius 10 cells and
+               a sphere drop of radius 16 cells at seeded offsets.  Solid nozzle:
+               tapered annulus in the bottom 32 layers, inner radius 24 -> 12
+               cells, outer radius = inner + 8 cells.  Velocities N(0, 0.2) where
+               the face liquid fraction >= 1/2, N(0, 0.02) elsewhere.
+  jet256       jet128 scaled 2x (h=0.025 mm, radii 20/32, width 3, annulus
+               48 -> 24 over 64 layers, outer = inner + 16).
+  adjoint128   jet128 plus a face body force N(0, 1e5 N/m^3) on liquid faces,
+               dt = 1e-6 s.
+  column512    512x256x256, h=0.025 mm, liquid column of radius 20 cells along
+               x plus 4 seeded drops of radius 8..14 cells, no solids.
+A ``scale`` argument shrinks a workload geometrically for oracle-sized tests.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _mix(z):
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def uniform(seed: int, field: int, count: int) -> np.ndarray:
+    """Uniform doubles in (0, 1) from a counter-based splitmix64 stream."""
+    with np.errstate(over="ignore"):
+        base = _mix(np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15) + np.uint64(field) * np.uint64(0xD1B54A32D192ED03))
+        ctr = np.arange(1, count + 1, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15) + base
+        z = _mix(ctr)
+    return ((z >> np.uint64(11)).astype(np.float64) + 0.5) * (1.0 / 9007199254740992.0)
+
+
+def normal(seed: int, field: int, count: int) -> np.ndarray:
+    """Box-Muller normals (double) from two uniform streams."""
+    u1 = uniform(seed, 2 * field + 1, count)
+    u2 = uniform(seed, 2 * field + 2, count)
+    return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+
+
+def _centres(n):
+    return np.arange(n, dtype=np.float64) + 0.5
+
+
+def _open_faces(solid, periodic=0, outlet=True):
+    """Masks of open faces (both adjacent cells non-solid, or an outlet face)."""
+    nz, ny, nx = solid.shape
+    fluid = solid == 0
+    fx = np.zeros((nz, ny, nx + 1), bool)
+    fx[:, :, 1:nx] = fluid[:, :, :-1] & fluid[:, :, 1:]
+    if periodic & 1:
+        fx[:, :, 0] = fx[:, :, nx] = fluid[:, :, -1] & fluid[:, :, 0]
+    fy = np.zeros((nz, ny + 1, nx), bool)
+    fy[:, 1:ny, :] = fluid[:, :-1, :] & fluid[:, 1:, :]
+    if periodic & 2:
+        fy[:, 0, :] = fy[:, ny, :] = fluid[:, -1, :] & fluid[:, 0, :]
+    fz = np.zeros((nz + 1, ny, nx), bool)
+    fz[1:nz] = fluid[:-1] & fluid[1:]
+    if periodic & 4:
+        fz[0] = fz[nz] = fluid[-1] & fluid[0]
+    elif outlet:
+        fz[nz] = fluid[-1]
+    return fx, fy, fz
+
+
+def _face_alpha(alpha):
+    nz, ny, nx = alpha.shape
+    ax = np.zeros((nz, ny, nx + 1))
+    ax[:, :, 1:nx] = 0.5 * (alpha[:, :, :-1] + alpha[:, :, 1:])
+    ax[:, :, 0] = alpha[:, :, 0]
+    ax[:, :, nx] = alpha[:, :, -1]
+    ay = np.zeros((nz, ny + 1, nx))
+    ay[:, 1:ny] = 0.5 * (alpha[:, :-1] + alpha[:, 1:])
+    ay[:, 0] = alpha[:, 0]
+    ay[:, ny] = alpha[:, -1]
+    az = np.zeros((nz + 1, ny, nx))
+    az[1:nz] = 0.5 * (alpha[:-1] + alpha[1:])
+    az[0] = alpha[0]
+    az[nz] = alpha[-1]
+    return ax, ay, az
+
+
+def _smooth(d, width):
+    return 0.5 * (1.0 - np.tanh(d / width))
+
+
+def _velocities(seed, alpha, solid, sd_liquid, sd_air, periodic=0, outlet=True, field0=10):
+    out = []
+    opens = _open_faces(solid, periodic, outlet)
+    for a, (fa, op) in enumerate(zip(_face_alpha(alpha), opens)):
+        z = normal(seed, field0 + a, fa.size).reshape(fa.shape)
+        sd = np.where(fa >= 0.5, sd_liquid, sd_air)
+        v = (z * sd).astype(np.float32)
+        v[~op] = 0.0
+        out.append(np.ascontiguousarray(v))
+    return out
+
+
+def _jet(n, scale, seed, h):
+    """Two-phase jet + drop with a tapered annular nozzle (jet128 geometry at scale 1)."""
+    c = _centres(n)
+    z, y, x = np.meshgrid(c, c, c, indexing="ij")
+    off = uniform(seed, 1, 5)
+    mid = n / 2.0
+    cx = mid + (off[0] * 8.0 - 4.0) * scale
+    cy = mid + (off[1] * 8.0 - 4.0) * scale
+    sx = mid + (off[2] * 16.0 - 8.0) * scale
+    sy = mid + (off[3] * 16.0 - 8.0) * scale
+    sz = n * 0.625 + (off[4] * 16.0 - 8.0) * scale
+    w = 1.5 * scale
+    d_cyl = np.sqrt((x - cx) ** 2 + (y - cy) ** 2) - 10.0 * scale
+    d_sph = np.sqrt((x - sx) ** 2 + (y - sy) ** 2 + (z - sz) ** 2) - 16.0 * scale
+    alpha = np.maximum(_smooth(d_cyl, w), _smooth(d_sph, w))
+    r = np.sqrt((x - mid) ** 2 + (y - mid) ** 2)
+    layers = 32.0 * scale
+    inner = 24.0 * scale - 12.0 * scale * np.clip(z / layers, 0.0, 1.0)
+    outer = inner + 8.0 * scale
+    solid = ((z < layers) & (r >= inner) & (r <= outer)).astype(np.uint8)
+    return alpha.astype(np.float32), solid
+
+
+def make_case(name: str, seed: int = 1, scale: float = 1.0) -> dict:
+    """Return a workload dict: dims (nx, ny, nz), h, rho_liquid, rho_air, alpha,
+    solid, u, v, w (face arrays shaped (nz, ny, nx+1) etc.), dt, periodic,
+    outlet, tol and (adjoint128) force fu, fv, fw."""
+    if name == "jet64":
+        n = int(round(64 * scale))
+        h = 1e-4 / scale
+        c = _centres(n)
+        _, y, x = np.meshgrid(c, c, c, indexing="ij")
+        solid = (np.sqrt((x - n / 2.0) ** 2 + (y - n / 2.0) ** 2) > 28.0 * scale).astype(np.uint8)
+        alpha = np.ones((n, n, n), np.float32)
+        u, v, w = _velocities(seed, alpha, solid, 0.05, 0.05)
+        return dict(name=name, dims=(n, n, n), h=h, rho_liquid=6440.0, rho_air=6440.0, alpha=alpha, solid=solid,
+                    u=u, v=v, w=w, dt=1e-5, periodic=0, outlet=True, tol=1e-6)
+    if name in ("jet128", "jet256", "adjoint128"):
+        base = 256 if name == "jet256" else 128
+        n = int(round(base * scale))
+        s = n / 128.0
+        h = 5e-5 * 128.0 / n
+        alpha, solid = _jet(n, s, seed, h)
+        u, v, w = _velocities(seed, alpha, solid, 0.2, 0.02)
+        case = dict(name=name, dims=(n, n, n), h=h, rho_liquid=6440.0, rho_air=1.2, alpha=alpha, solid=solid,
+                    u=u, v=v, w=w, dt=1e-5, periodic=0, outlet=True, tol=1e-6)
+        if name == "adjoint128":
+            case["dt"] = 1e-6
+            fa = _face_alpha(alpha.astype(np.float64))
+            opens = _open_faces(solid)
+            forces = []
+            for a, (f, op) in enumerate(zip(fa, opens)):
+                z = normal(seed, 40 + a, f.size).reshape(f.shape) * 1e5
+                z[(f < 0.5) | ~op] = 0.0
+                forces.append(np.ascontiguousarray(z.astype(np.float32)))
+            case["fu"], case["fv"], case["fw"] = forces
+            case["steps"] = 8
+            case["checkpoint_every"] = 4
+        return case
+    if name == "column512":
+        nx, ny, nz = int(round(512 * scale)), int(round(256 * scale)), int(round(256 * scale))
+        h = 2.5e-5 / scale
+        cx, cy, cz = _centres(nx), _centres(ny), _centres(nz)
+        z, y, x = np.meshgrid(cz, cy, cx, indexing="ij")
+        w = 3.0 * scale
+        alpha = _smooth(np.sqrt((y - ny / 2.0) ** 2 + (z - nz / 2.0) ** 2) - 20.0 * scale, w)
+        p = uniform(seed, 3, 16)
+        for k in range(4):
+            px, py, pz = p[4 * k] * nx, (0.2 + 0.6 * p[4 * k + 1]) * ny, (0.2 + 0.6 * p[4 * k + 2]) * nz
+            rad = (8.0 + 6.0 * p[4 * k + 3]) * scale
+            d = np.sqrt((x - px) ** 2 + (y - py) ** 2 + (z - pz) ** 2) - rad
+            alpha = np.maximum(alpha, _smooth(d, w))
+        alpha = alpha.astype(np.float32)
+        solid = np.zeros(alpha.shape, np.uint8)
+        u, v, wv = _velocities(seed, alpha, solid, 0.2, 0.02)
+        return dict(name=name, dims=(nx, ny, nz), h=h, rho_liquid=6440.0, rho_air=1.2, alpha=alpha, solid=solid,
+                    u=u, v=v, w=wv, dt=1e-5, periodic=0, outlet=True, tol=1e-6)
+    raise ValueError(f"unknown workload {name!r}")

@@ -1,0 +1,182 @@
+/*
+ * mhd_oracle.h -- CPU oracle for the MAC pressure projection.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links this code;
+ * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it,
+ * and only as the checker or the timed CPU baseline.
+ *
+ * Two parts:
+ *
+ *  oref_*  A line-by-line FP32 restatement of the reference projection as it
+ *          runs in the reference's WGSL shaders (src/fluid/solver.wgsl,
+ *          src/fluid/multigrid.wgsl, src/fluid/pressure_subspace.wgsl,
+ *          src/periodic.wgsl) driven by the host logic of
+ *          src/fluid/mod.rs:969-1115 and src/fluid/multigrid.rs:25-329.
+ *          Buffers keep the reference layout (vec4 per (n+1)^3 face-cell,
+ *          vec4 work per cell).  Workgroup reductions are replayed in the
+ *          reference's order (256-lane tree, then a 256-stride final pass).
+ *
+ *  onat_*  An FP64 solver for the GB300 path's own discrete problem
+ *          (two-phase mobility, solid walls, optional Dirichlet outlet on the
+ *          top z-face, pinned gauges for components without an outlet) and
+ *          its adjoint.  The face mobilities are computed in FP32 with the
+ *          same operation order as the GPU, then the system is solved in FP64
+ *          to a 1e-13 relative residual.
+ *
+ * Parity status: the reference runs only through wgpu/Vulkan, which neither
+ * this machine nor the GPU machine can run, so the restatement is pinned by the
+ * reference's own known-answer tests (hierarchy sizes, gauge anchors) and its
+ * analytic acceptance tests (periodic cosine potential, manufactured gradient,
+ * Galerkin identity, V-cycle symmetry, fused coarse solve, cached/uncached
+ * operator) -- not by stored reference output vectors, which do not exist.
+ */
+#ifndef MHD_ORACLE_H
+#define MHD_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- reference */
+
+/* Projection lanes of Params (src/fluid/mod.rs:120-130). */
+typedef struct {
+    uint32_t dims[4];    /* nx, ny, nz, n */
+    uint32_t faces[4];   /* nx+1, ny+1, nz+1, nf */
+    uint32_t flags[4];   /* x periodic bits, w thermal-phase drag enabled */
+    float physical[4];   /* h, dt, nu, rho_liquid */
+    float initial[4];    /* w: inverse fluid-cell count in mean-free mode */
+    float solve[4];      /* tol^2, absolute floor, bound, mushy drag rate */
+    float surface[4];    /* x enabled, y rho_air */
+} oref_params;
+
+typedef struct {
+    int32_t status;        /* 0 ok, 1 not converged, 2 non-finite, 3 no progress */
+    uint32_t iterations;
+    float residual;        /* sqrt(s[1]/s[2]) of the last convergence read */
+    int32_t meanfree;      /* gauge mode chosen by configure_pressure_projection */
+    int32_t multigrid;     /* preconditioner used */
+    uint32_t levels;       /* multigrid levels (0 when Jacobi) */
+    uint64_t coarse_cells;
+} oref_result;
+
+/* anchors(): src/fluid/mod.rs:1447-1493.  mask in: 0/1; out: encoded. */
+uint32_t oref_anchors(uint32_t *mask, const uint32_t dims[3], uint32_t periodic_bits);
+
+/* hierarchy(): src/fluid/multigrid.rs:25-65.  Returns 0 on success and fills
+ * the number of levels and total coarse cells; nonzero for rejected dims. */
+int oref_hierarchy(const uint32_t dims[4], uint32_t *levels, uint64_t *coarse_cells,
+                   uint32_t *level_dims /* 4*levels, may be NULL */, uint32_t max_levels);
+
+/* Fill Params the way FluidState::new + configure_pressure_projection do. */
+void oref_make_params(oref_params *p, const uint32_t dims[3], float h, float dt,
+                      float rho_liquid, float rho_air, int two_phase, uint32_t periodic_bits,
+                      float rel_tol, float abs_div_tol, uint32_t fluid_cells,
+                      int thermal_drag, float drag_rate);
+
+/* FluidState::project(warm_start) (src/fluid/mod.rs:1015-1115) with the
+ * configure/gauge selection of :978-1002.
+ *   force_mg: -1 automatic (cells >= 96^3), 0 Jacobi-CG, 1 aggregation MG-CG
+ *   force_meanfree: -1 automatic (components == 1), 0 pinned, 1 mean-free if connected
+ *   predicted: vec4[nf] candidate face velocities (modified by a warm start)
+ *   velocity:  vec4[nf] out: projected face velocities
+ *   work:      vec4[n]  out: x = pressure potential
+ *   occupancy: liquid fraction per cell (FluidCell.reserved.z)
+ *   phase:     phase fraction per cell (FluidCell.reserved.y) or NULL
+ *   old_pressure: FluidCell.pressure.x per cell for warm_start, else NULL */
+void oref_project(const oref_params *params, const uint32_t *mask, uint32_t components,
+                  const float *occupancy, const float *phase, const float *old_pressure,
+                  float *predicted, float *velocity, float *work, uint32_t max_iterations,
+                  int warm_start, int force_mg, int force_meanfree, oref_result *result);
+
+/* pressure_coefficients (solver.wgsl:93-103) into velocity vec4[nf]. */
+void oref_coefficients(const oref_params *params, const uint32_t *mask, const float *occupancy,
+                       const float *phase, float *velocity);
+/* apply() (cached, solver.wgsl:78-92) and laplacian()/diagonal() (uncached,
+ * :60-69) for every fluid cell; kind 0 reads work.x, 1 reads work.z. */
+void oref_apply_cached(const oref_params *params, const uint32_t *mask, const float *velocity,
+                       const float *work, uint32_t kind, float *out);
+void oref_apply_uncached(const oref_params *params, const uint32_t *mask, const float *occupancy,
+                         const float *phase, const float *work, uint32_t kind, float *out,
+                         float *diag_out);
+
+/* Aggregation multigrid probes (multigrid.wgsl) on a prepared fine state:
+ * velocity holds the coefficient cache, work the fine vectors. */
+typedef struct oref_mg oref_mg;
+oref_mg *oref_mg_create(const oref_params *params, const uint32_t *mask, const float *velocity,
+                        int meanfree);
+void oref_mg_destroy(oref_mg *mg);
+uint32_t oref_mg_levels(const oref_mg *mg, uint32_t *level_dims /* 4 per level */,
+                        uint32_t *offsets /* per level */);
+void oref_mg_build(oref_mg *mg);
+/* The fixed V-cycle: work.y (residual) -> work.w (correction). */
+void oref_mg_apply(oref_mg *mg, float *work);
+/* Direct access for probes: coarse coeff/value vec4 buffers. */
+float *oref_mg_coeff(oref_mg *mg);
+float *oref_mg_value(oref_mg *mg);
+/* probe_action (multigrid_probes.wgsl:7) at a level; fine results go to
+ * predicted_w[n], coarse results to value.z. */
+void oref_mg_probe_action(oref_mg *mg, uint32_t level, const float *work, float *predicted_w);
+/* coarse_solve at the coarsest level vs. the clear + 8 smooth ping-pongs. */
+void oref_mg_coarse_solve(oref_mg *mg, float *work);
+void oref_mg_coarse_jacobi_sequence(oref_mg *mg, float *work);
+
+/* ------------------------------------------------------------------- native */
+
+typedef struct {
+    uint32_t nx, ny, nz;
+    uint32_t periodic;     /* bit a: axis a periodic */
+    int32_t outlet;        /* 1: Dirichlet p=0 on the top z-face */
+    float h;
+    float rho_liquid, rho_air;
+} onat_grid;
+
+/* Cell classes: 0 solid, 1 active fluid, 2 pinned gauge cell.  Components that
+ * touch an outlet face get no gauge; every other component is pinned at its
+ * first cell in x-fastest order (the root the reference's anchors() picks). */
+uint32_t onat_classify(const onat_grid *g, const uint8_t *solid, uint8_t *cls);
+
+/* Low-face mobilities and reactions, FP32, coef[4*n] = (bx, by, bz, reaction);
+ * gtop[nx*ny] = outlet conductance 2*rho_l/rho(cell) (0 without an outlet). */
+void onat_coefficients(const onat_grid *g, const float *alpha, const uint8_t *cls, float *coef,
+                       float *gtop);
+/* b = -h * sum of open-face velocity differences (FP64). */
+void onat_rhs(const onat_grid *g, const uint8_t *cls, const float *gtop, const float *u,
+              const float *v, const float *w, double *b);
+void onat_apply(const onat_grid *g, const float *coef, const double *x, double *y);
+/* FP64 PCG (symmetric Gauss-Seidel preconditioner) to ||b-Ax|| <= rtol ||b||. */
+int onat_solve(const onat_grid *g, const float *coef, const uint8_t *cls, const double *b,
+               double *x, double rtol, int max_it, int *iterations, double *rel_residual);
+/* Gradient subtraction: out = u* - beta * grad(phi) / h, 0 on closed faces. */
+void onat_correct(const onat_grid *g, const float *alpha, const uint8_t *cls, const float *gtop,
+                  const double *phi, const float *us, const float *vs, const float *ws,
+                  double *u, double *v, double *w);
+/* Whole projection in FP64; pressure p = rho_l * phi / dt. */
+int onat_project(const onat_grid *g, const float *alpha, const uint8_t *solid, const float *us,
+                 const float *vs, const float *ws, float dt, double rtol, double *phi, double *u,
+                 double *v, double *w, double *p, int *iterations, double *rel_residual);
+/* Vector-Jacobian product of the projection: given dL/du (faces) and dL/dp
+ * (cells, may be NULL) return dL/du* (faces). */
+int onat_project_vjp(const onat_grid *g, const float *alpha, const uint8_t *solid, const double *gu,
+                     const double *gv, const double *gw, const double *gp, float dt, double rtol,
+                     double *gus, double *gvs, double *gws);
+/* Coarse-correction weight of the V-cycle used as the FP64 preconditioner. */
+void onat_set_prolongation(double w);
+/* Max and RMS cell divergence sum(u_high-u_low)/h over active cells. */
+void onat_divergence(const onat_grid *g, const uint8_t *cls, const float *gtop, const double *u,
+                     const double *v, const double *w, double *max_abs, double *rms);
+
+/* Chain u_{k+1} = P(u_k + dt f / rho_face), J = sum over outlet faces of w^2.
+ * Forward returns J; the adjoint returns dJ/df on the faces. */
+int onat_chain_forward(const onat_grid *g, const float *alpha, const uint8_t *solid,
+                       const float *u0, const float *v0, const float *w0, const float *fu,
+                       const float *fv, const float *fw, float dt, int steps, double rtol,
+                       double *uk, double *vk, double *wk, double *objective);
+int onat_chain_adjoint(const onat_grid *g, const float *alpha, const uint8_t *solid,
+                       const double *uk, const double *vk, const double *wk, float dt, int steps,
+                       double rtol, double *gfu, double *gfv, double *gfw);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,286 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+and by bench.py's CPU-baseline leg, and there only as the checker or as the
+timed CPU baseline.  The product library never loads it.
+
+``oref_*`` restates the reference projection in FP32 with the reference's
+buffer layout (vec4 per (n+1)^3 face-cell); ``onat_*`` solves the GB300
+path's discrete problem in FP64.  See mhd_oracle.h for the citations.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+
+
+class OrefParams(C.Structure):
+    _fields_ = [
+        ("dims", C.c_uint32 * 4),
+        ("faces", C.c_uint32 * 4),
+        ("flags", C.c_uint32 * 4),
+        ("physical", C.c_float * 4),
+        ("initial", C.c_float * 4),
+        ("solve", C.c_float * 4),
+        ("surface", C.c_float * 4),
+    ]
+
+
+class OrefResult(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32),
+        ("iterations", C.c_uint32),
+        ("residual", C.c_float),
+        ("meanfree", C.c_int32),
+        ("multigrid", C.c_int32),
+        ("levels", C.c_uint32),
+        ("coarse_cells", C.c_uint64),
+    ]
+
+
+class OnatGrid(C.Structure):
+    _fields_ = [
+        ("nx", C.c_uint32),
+        ("ny", C.c_uint32),
+        ("nz", C.c_uint32),
+        ("periodic", C.c_uint32),
+        ("outlet", C.c_int32),
+        ("h", C.c_float),
+        ("rho_liquid", C.c_float),
+        ("rho_air", C.c_float),
+    ]
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so with the Makefile recipe next to this file."""
+    if force or not os.path.exists(LIB_PATH) or _stale():
+        subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    return LIB_PATH
+
+
+def _stale() -> bool:
+    t = os.path.getmtime(LIB_PATH)
+    return any(
+        os.path.getmtime(os.path.join(HERE, f)) > t
+        for f in ("oracle_ref.c", "oracle_native.c", "mhd_oracle.h")
+    )
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        L.oref_anchors.argtypes = [_u32p, C.POINTER(C.c_uint32), C.c_uint32]
+        L.oref_anchors.restype = C.c_uint32
+        L.oref_hierarchy.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint64),
+                                     C.c_void_p, C.c_uint32]
+        L.oref_hierarchy.restype = C.c_int
+        L.oref_make_params.argtypes = [C.POINTER(OrefParams), C.POINTER(C.c_uint32), C.c_float, C.c_float,
+                                       C.c_float, C.c_float, C.c_int, C.c_uint32, C.c_float, C.c_float,
+                                       C.c_uint32, C.c_int, C.c_float]
+        L.oref_project.argtypes = [C.POINTER(OrefParams), _u32p, C.c_uint32, _f32p, C.c_void_p, C.c_void_p,
+                                   _f32p, _f32p, _f32p, C.c_uint32, C.c_int, C.c_int, C.c_int,
+                                   C.POINTER(OrefResult)]
+        L.oref_coefficients.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, C.c_void_p, _f32p]
+        L.oref_apply_cached.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, _f32p, C.c_uint32, _f32p]
+        L.oref_apply_uncached.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, C.c_void_p, _f32p, C.c_uint32,
+                                          _f32p, _f32p]
+        L.oref_mg_create.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, C.c_int]
+        L.oref_mg_create.restype = C.c_void_p
+        L.oref_mg_destroy.argtypes = [C.c_void_p]
+        L.oref_mg_levels.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oref_mg_levels.restype = C.c_uint32
+        L.oref_mg_build.argtypes = [C.c_void_p]
+        L.oref_mg_apply.argtypes = [C.c_void_p, _f32p]
+        L.oref_mg_coeff.argtypes = [C.c_void_p]
+        L.oref_mg_coeff.restype = C.POINTER(C.c_float)
+        L.oref_mg_value.argtypes = [C.c_void_p]
+        L.oref_mg_value.restype = C.POINTER(C.c_float)
+        L.oref_mg_probe_action.argtypes = [C.c_void_p, C.c_uint32, _f32p, _f32p]
+        L.oref_mg_coarse_solve.argtypes = [C.c_void_p, _f32p]
+        L.oref_mg_coarse_jacobi_sequence.argtypes = [C.c_void_p, _f32p]
+
+        g = C.POINTER(OnatGrid)
+        L.onat_classify.argtypes = [g, _u8p, _u8p]
+        L.onat_classify.restype = C.c_uint32
+        L.onat_coefficients.argtypes = [g, _f32p, _u8p, _f32p, _f32p]
+        L.onat_rhs.argtypes = [g, _u8p, _f32p, _f32p, _f32p, _f32p, _f64p]
+        L.onat_apply.argtypes = [g, _f32p, _f64p, _f64p]
+        L.onat_solve.argtypes = [g, _f32p, _u8p, _f64p, _f64p, C.c_double, C.c_int, C.POINTER(C.c_int),
+                                 C.POINTER(C.c_double)]
+        L.onat_correct.argtypes = [g, _f32p, _u8p, _f32p, _f64p, _f32p, _f32p, _f32p, _f64p, _f64p, _f64p]
+        L.onat_project.argtypes = [g, _f32p, _u8p, _f32p, _f32p, _f32p, C.c_float, C.c_double, _f64p, _f64p,
+                                   _f64p, _f64p, _f64p, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        L.onat_project_vjp.argtypes = [g, _f32p, _u8p, _f64p, _f64p, _f64p, C.c_void_p, C.c_float, C.c_double,
+                                       _f64p, _f64p, _f64p]
+        L.onat_divergence.argtypes = [g, _u8p, _f32p, _f64p, _f64p, _f64p, C.POINTER(C.c_double),
+                                      C.POINTER(C.c_double)]
+        L.onat_chain_forward.argtypes = [g, _f32p, _u8p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, C.c_float,
+                                         C.c_int, C.c_double, _f64p, _f64p, _f64p, C.POINTER(C.c_double)]
+        L.onat_chain_adjoint.argtypes = [g, _f32p, _u8p, _f64p, _f64p, _f64p, C.c_float, C.c_int, C.c_double,
+                                         _f64p, _f64p, _f64p]
+        _lib = L
+    return _lib
+
+
+# ----------------------------------------------------------------- reference
+def anchors(mask, dims, periodic_bits=0):
+    """anchors() of src/fluid/mod.rs:1447-1493: returns (components, encoded mask)."""
+    m = np.ascontiguousarray(mask, dtype=np.uint32).copy()
+    d = (C.c_uint32 * 3)(*dims)
+    comps = lib().oref_anchors(m, d, periodic_bits)
+    return int(comps), m
+
+
+def hierarchy(dims4):
+    """hierarchy() of src/fluid/multigrid.rs:25-65: (levels, coarse cells) or None if rejected."""
+    d = (C.c_uint32 * 4)(*[int(v) & 0xFFFFFFFF for v in dims4])
+    nl = C.c_uint32()
+    cc = C.c_uint64()
+    buf = (C.c_uint32 * (4 * 64))()
+    rc = lib().oref_hierarchy(d, C.byref(nl), C.byref(cc), C.cast(buf, C.c_void_p), 64)
+    if rc:
+        return None
+    levels = [tuple(buf[4 * l:4 * l + 4]) for l in range(nl.value)]
+    return levels, cc.value
+
+
+def make_params(dims, h, dt, rho_liquid, rho_air=None, two_phase=False, periodic_bits=0, rel_tol=1e-5,
+                abs_div_tol=1e-5, fluid_cells=0, thermal_drag=False, drag_rate=1e6):
+    p = OrefParams()
+    d = (C.c_uint32 * 3)(*dims)
+    lib().oref_make_params(C.byref(p), d, h, dt, rho_liquid, rho_liquid if rho_air is None else rho_air,
+                           int(two_phase), periodic_bits, rel_tol, abs_div_tol, fluid_cells, int(thermal_drag),
+                           drag_rate)
+    return p
+
+
+def ref_project(params, mask, components, occupancy, predicted, max_iterations=1000, warm_start=False,
+                old_pressure=None, phase=None, force_mg=-1, force_meanfree=-1):
+    """FluidState::project on the restated FP32 pipeline.
+
+    predicted: float32 (nf, 4) candidate velocities; returns (result, velocity (nf,4), work (n,4))."""
+    n = params.dims[3]
+    nf = params.faces[3]
+    pred = np.ascontiguousarray(predicted, dtype=np.float32).reshape(nf, 4).copy()
+    vel = np.zeros((nf, 4), np.float32)
+    work = np.zeros((n, 4), np.float32)
+    res = OrefResult()
+    ph = None if phase is None else np.ascontiguousarray(phase, dtype=np.float32)
+    op = None if old_pressure is None else np.ascontiguousarray(old_pressure, dtype=np.float32)
+    lib().oref_project(C.byref(params), np.ascontiguousarray(mask, dtype=np.uint32), components,
+                       np.ascontiguousarray(occupancy, dtype=np.float32),
+                       None if ph is None else ph.ctypes.data_as(C.c_void_p),
+                       None if op is None else op.ctypes.data_as(C.c_void_p),
+                       pred.reshape(-1), vel.reshape(-1), work.reshape(-1), max_iterations, int(warm_start),
+                       force_mg, force_meanfree, C.byref(res))
+    return res, vel, work, pred
+
+
+# -------------------------------------------------------------------- native
+def grid(nx, ny, nz, h, rho_liquid, rho_air, periodic=0, outlet=True):
+    return OnatGrid(nx, ny, nz, periodic, int(outlet), h, rho_liquid, rho_air)
+
+
+def classify(g, solid):
+    cls = np.zeros(g.nx * g.ny * g.nz, np.uint8)
+    pinned = lib().onat_classify(C.byref(g), np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1), cls)
+    return int(pinned), cls
+
+
+def coefficients(g, alpha, cls):
+    n = g.nx * g.ny * g.nz
+    coef = np.zeros(4 * n, np.float32)
+    gtop = np.zeros(g.nx * g.ny, np.float32)
+    lib().onat_coefficients(C.byref(g), np.ascontiguousarray(alpha, dtype=np.float32).reshape(-1), cls, coef,
+                            gtop)
+    return coef.reshape(n, 4), gtop
+
+
+def rhs(g, cls, gtop, u, v, w):
+    b = np.zeros(g.nx * g.ny * g.nz, np.float64)
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+    lib().onat_rhs(C.byref(g), cls, gtop, f(u), f(v), f(w), b)
+    return b
+
+
+def apply(g, coef, x):
+    y = np.zeros_like(x, dtype=np.float64)
+    lib().onat_apply(C.byref(g), np.ascontiguousarray(coef, dtype=np.float32).reshape(-1),
+                     np.ascontiguousarray(x, dtype=np.float64), y)
+    return y
+
+
+def face_shapes(g):
+    return ((g.nz, g.ny, g.nx + 1), (g.nz, g.ny + 1, g.nx), (g.nz + 1, g.ny, g.nx))
+
+
+def project(g, alpha, solid, u, v, w, dt, rtol=1e-13):
+    """FP64 projection: returns dict(phi, u, v, w, p, iterations, residual, status)."""
+    n = g.nx * g.ny * g.nz
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+    su, sv, sw = face_shapes(g)
+    phi = np.zeros(n)
+    uo, vo, wo = np.zeros(int(np.prod(su))), np.zeros(int(np.prod(sv))), np.zeros(int(np.prod(sw)))
+    p = np.zeros(n)
+    it = C.c_int()
+    rel = C.c_double()
+    st = lib().onat_project(C.byref(g), f(alpha), np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1),
+                            f(u), f(v), f(w), dt, rtol, phi, uo, vo, wo, p, C.byref(it), C.byref(rel))
+    return dict(phi=phi, u=uo, v=vo, w=wo, p=p, iterations=it.value, residual=rel.value, status=st)
+
+
+def project_vjp(g, alpha, solid, gu, gv, gw, gp, dt, rtol=1e-13):
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+    d = lambda a: np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+    su, sv, sw = face_shapes(g)
+    ou, ov, ow = np.zeros(int(np.prod(su))), np.zeros(int(np.prod(sv))), np.zeros(int(np.prod(sw)))
+    gpp = None if gp is None else d(gp)
+    st = lib().onat_project_vjp(C.byref(g), f(alpha), np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1),
+                                d(gu), d(gv), d(gw), None if gpp is None else gpp.ctypes.data_as(C.c_void_p), dt,
+                                rtol, ou, ov, ow)
+    return st, ou, ov, ow
+
+
+def divergence(g, cls, gtop, u, v, w):
+    mx = C.c_double()
+    rms = C.c_double()
+    d = lambda a: np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+    lib().onat_divergence(C.byref(g), cls, gtop, d(u), d(v), d(w), C.byref(mx), C.byref(rms))
+    return mx.value, rms.value
+
+
+def chain_forward(g, alpha, solid, u0, v0, w0, fu, fv, fw, dt, steps, rtol=1e-13):
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+    su, sv, sw = face_shapes(g)
+    uk, vk, wk = np.zeros(int(np.prod(su))), np.zeros(int(np.prod(sv))), np.zeros(int(np.prod(sw)))
+    J = C.c_double()
+    st = lib().onat_chain_forward(C.byref(g), f(alpha), np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1),
+                                  f(u0), f(v0), f(w0), f(fu), f(fv), f(fw), dt, steps, rtol, uk, vk, wk,
+                                  C.byref(J))
+    return st, J.value, (uk, vk, wk)
+
+
+def chain_adjoint(g, alpha, solid, uk, vk, wk, dt, steps, rtol=1e-13):
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+    d = lambda a: np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+    su, sv, sw = face_shapes(g)
+    gu, gv, gw = np.zeros(int(np.prod(su))), np.zeros(int(np.prod(sv))), np.zeros(int(np.prod(sw)))
+    st = lib().onat_chain_adjoint(C.byref(g), f(alpha), np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1),
+                                  d(uk), d(vk), d(wk), dt, steps, rtol, gu, gv, gw)
+    return st, (gu, gv, gw)
