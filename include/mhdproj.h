@@ -202,6 +202,20 @@ int mhdproj_copy_potential(mhdproj_ctx *ctx, double *phi);
  * 1 active, 2 pinned gauge cell.  Returns the number of components. */
 int mhdproj_copy_topology(mhdproj_ctx *ctx, uint32_t *mask_host, uint32_t *components);
 
+/* Measurement hook: after a projection, time the fine-level kernels of one CG
+ * iteration (and the set-up kernels) in isolation, `reps` launches each on the
+ * context stream between CUDA events.  For each kernel: its name, the mean
+ * device time of one launch, the algorithmic bytes of one launch, and how many
+ * times one CG iteration launches it.  Leaves the solver state undefined until
+ * the next mhdproj_project. */
+typedef struct {
+    char name[32];
+    float ms;
+    double bytes;
+    int per_iteration;
+} mhdproj_kernel_time;
+int mhdproj_profile_kernels(mhdproj_ctx *ctx, int reps, mhdproj_kernel_time *out, int max_out, int *count);
+
 /* Host utilities, mirroring src/fluid/multigrid.rs:25-65 and src/fluid/mod.rs:1447-1493. */
 /* Aggregation hierarchy: halve (ceil) until every dimension is <= 4.  Returns
  * 0 and the level count / coarse-cell total, or MHDPROJ_ERR_INVALID for zero,

@@ -885,6 +885,73 @@ extern "C" int mhdproj_copy_topology(mhdproj_ctx* ctx, uint32_t* mask_host, uint
     return 0;
 }
 
+// ---------------------------------------------------------- measurement
+extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kernel_time* out, int max_out, int* count) {
+    if (!ctx || !out || !count) return MHDPROJ_ERR_INVALID;
+    if (ctx->ref) return fail(ctx, MHDPROJ_ERR_INVALID, "kernel profiling covers the GB300 solver");
+    if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients first");
+    if (reps < 1) reps = 1;
+    cudaStream_t s = ctx->stream;
+    Fields F = fields(ctx);
+    const double n = (double)ctx->n;
+    const double cb = ctx->opt.precision == 0 ? 16.0 : 8.0;  // smoother coefficient bytes per cell
+    struct Item {
+        const char* name;
+        double bytes_per_cell;
+        int per_it;
+        int kind;
+    };
+    // Algorithmic bytes per cell: the compulsory traffic of each kernel's
+    // fields, every field touched once per launch.
+    const Item items[] = {
+        {"spmv_dot", 20.0, 1, 0},             // p 4 + beta 12 -> q 4
+        {"update_norm", 24.0, 1, 1},          // e, p, r, q 16 -> e, r 8
+        {"fine_smooth_half", 12.0 + cb, 4, 2},  // r 4 + coef + z 4 -> z 4
+        {"fine_restrict", 8.0 + cb + 0.25, 1, 3},
+        {"fine_prolong", 8.25, 1, 4},
+        {"dot_rz", 8.0, 1, 5},
+        {"search", 12.0, 1, 6},
+        {"residual64", 24.0, 0, 7},           // x 4 + beta 12 + b 4 -> r 4 (survey K7)
+        {"coefficients", 29.0, 0, 8},         // alpha 4 + solid 1 -> 16 + 8 (survey K0)
+    };
+    int k = 0;
+    for (const Item& it : items) {
+        if (k >= max_out) break;
+        if (!ctx->use_mg && (it.kind >= 2 && it.kind <= 4)) continue;
+        launch_set_sigma(ctx->sc, 1.0f, s);  // clears the converged flag
+        CK(cudaEventRecord(ctx->ev_a, s));
+        for (int r = 0; r < reps; r++) {
+            switch (it.kind) {
+                case 0: launch_spmv_pq(ctx->L, F, s); break;
+                case 1: launch_update(ctx->L, F, s); break;
+                case 2: mg_fine_smooth(ctx->mg, r & 1, s); break;
+                case 3: mg_fine_restrict(ctx->mg, s); break;
+                case 4: mg_fine_prolong(ctx->mg, s); break;
+                case 5: launch_dot_rz(ctx->L, F, 0, s); break;
+                case 6: launch_search(ctx->L, F, s); break;
+                case 7: launch_residual64(ctx->L, F, ctx->phi64, s); break;
+                case 8: launch_coefficients(ctx->L, F, s); break;
+            }
+            if (it.kind == 1 || it.kind == 5 || it.kind == 7) launch_set_sigma(ctx->sc, 1.0f, s);
+        }
+        CK(cudaEventRecord(ctx->ev_b, s));
+        CK(cudaGetLastError());
+        int rc = wait_stream(ctx);
+        if (rc) return rc;
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ctx->ev_a, ctx->ev_b));
+        mhdproj_kernel_time& o = out[k++];
+        memset(&o, 0, sizeof o);
+        snprintf(o.name, sizeof o.name, "%s", it.name);
+        o.ms = ms / reps;
+        o.bytes = it.bytes_per_cell * n;
+        o.per_iteration = it.per_it;
+    }
+    *count = k;
+    ctx->have_solution = false;
+    return 0;
+}
+
 // ------------------------------------------------------------ utilities
 extern "C" int mhdproj_hierarchy(const uint32_t dims[4], uint32_t* levels, uint64_t* coarse_cells) {
     return host_hierarchy(dims, levels, coarse_cells) ? MHDPROJ_ERR_INVALID : 0;

@@ -81,6 +81,10 @@ struct MGPlan {
     Scalars* sc;
 };
 void mg_build(const MGPlan& P, cudaStream_t s);
+// single fine-level stages, for measurement
+void mg_fine_smooth(const MGPlan& P, int color, cudaStream_t s);
+void mg_fine_restrict(const MGPlan& P, cudaStream_t s);
+void mg_fine_prolong(const MGPlan& P, cudaStream_t s);
 void mg_vcycle(const MGPlan& P, cudaStream_t s);
 cudaError_t mg_prepare_attributes();
 

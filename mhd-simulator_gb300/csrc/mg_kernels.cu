@@ -344,6 +344,36 @@ void mg_vcycle(const MGPlan& P, cudaStream_t s) {
     else vcycle_impl<0, float>(P, s);
 }
 
+template <int CK, class VT>
+static void fine_restrict_impl(const MGPlan& P, cudaStream_t s) {
+    const MGLevel &F = P.lv[0], &C = P.lv[1];
+    const void* coef = P.precision == 0 ? (const void*)F.coef32 : F.coef_lo;
+    k_restrict<CK, float, true, VT><<<C.L.grid, C.L.block, 0, s>>>(F.L.g, C.L.g, coef, (const float*)F.r,
+                                                                   (const float*)F.e, (VT*)C.r, P.sc);
+}
+template <class VT>
+static void fine_prolong_impl(const MGPlan& P, cudaStream_t s) {
+    const MGLevel &F = P.lv[0], &C = P.lv[1];
+    k_prolong<float, VT><<<F.L.grid, F.L.block, 0, s>>>(F.L.g, C.L.g, (float*)F.e, (const VT*)C.e, P.prolong, P.sc);
+}
+void mg_fine_smooth(const MGPlan& P, int color, cudaStream_t s) {
+    if (P.precision == 1) enqueue_smooth<1, __half>(P, 0, color, false, s);
+    else if (P.precision == 2) enqueue_smooth<2, __nv_bfloat16>(P, 0, color, false, s);
+    else enqueue_smooth<0, float>(P, 0, color, false, s);
+}
+void mg_fine_restrict(const MGPlan& P, cudaStream_t s) {
+    if (P.nlevels < 2) return;
+    if (P.precision == 1) fine_restrict_impl<1, __half>(P, s);
+    else if (P.precision == 2) fine_restrict_impl<2, __nv_bfloat16>(P, s);
+    else fine_restrict_impl<0, float>(P, s);
+}
+void mg_fine_prolong(const MGPlan& P, cudaStream_t s) {
+    if (P.nlevels < 2) return;
+    if (P.precision == 1) fine_prolong_impl<__half>(P, s);
+    else if (P.precision == 2) fine_prolong_impl<__nv_bfloat16>(P, s);
+    else fine_prolong_impl<float>(P, s);
+}
+
 void mg_build(const MGPlan& P, cudaStream_t s) {
     for (int l = 1; l < P.nlevels; l++) {
         const MGLevel &F = P.lv[l - 1], &C = P.lv[l];

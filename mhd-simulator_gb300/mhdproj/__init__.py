@@ -61,6 +61,10 @@ class Stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class KernelTime(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("ms", C.c_float), ("bytes", C.c_double), ("per_iteration", C.c_int)]
+
+
 class ProjectionError(RuntimeError):
     """A failed projection; ``code`` is the mhdproj_status value."""
 
@@ -102,6 +106,7 @@ def load():
     L.mhdproj_copy_coefficients.argtypes = [_vp, _vp]
     L.mhdproj_copy_potential.argtypes = [_vp, _vp]
     L.mhdproj_copy_topology.argtypes = [_vp, _vp, C.POINTER(C.c_uint32)]
+    L.mhdproj_profile_kernels.argtypes = [_vp, C.c_int, C.POINTER(KernelTime), C.c_int, C.POINTER(C.c_int)]
     L.mhdproj_hierarchy.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)]
     L.mhdproj_anchors.argtypes = [_vp, C.POINTER(C.c_uint32), C.c_uint32]
     L.mhdproj_anchors.restype = C.c_uint32
@@ -114,7 +119,7 @@ EXPORTED = [
     "mhdproj_set_coefficients", "mhdproj_set_phase_drag", "mhdproj_project", "mhdproj_project_host",
     "mhdproj_project_vjp", "mhdproj_chain_forward", "mhdproj_chain_backward", "mhdproj_apply_operator",
     "mhdproj_apply_preconditioner", "mhdproj_copy_coefficients", "mhdproj_copy_potential", "mhdproj_copy_topology",
-    "mhdproj_hierarchy", "mhdproj_anchors",
+    "mhdproj_hierarchy", "mhdproj_anchors", "mhdproj_profile_kernels",
 ]
 
 
@@ -188,11 +193,21 @@ class PressureProjection:
             raise ProjectionError(rc, L.mhdproj_last_error(None).decode())
         self._ctx = h_
         self._lib = L
-        s = stream if stream is not None else torch.cuda.current_stream()
-        self._check(L.mhdproj_set_stream(self._ctx, C.c_void_p(s.cuda_stream)))
+        # The library works on a non-default stream (CUDA graphs cannot be
+        # captured on the legacy default stream); every call first orders it
+        # after torch's current stream, and returns with its own stream idle.
+        if stream is None or stream.cuda_stream == 0:
+            stream = torch.cuda.Stream()
+        self.stream = stream
+        self._check(L.mhdproj_set_stream(self._ctx, C.c_void_p(stream.cuda_stream)))
         self.solver = solver
 
     # ------------------------------------------------------------ helpers
+    def _order(self):
+        cur = self._torch.cuda.current_stream()
+        if cur.cuda_stream != self.stream.cuda_stream:
+            self.stream.wait_stream(cur)
+
     def _check(self, rc):
         if rc:
             raise ProjectionError(rc, self._lib.mhdproj_last_error(self._ctx).decode())
@@ -218,13 +233,16 @@ class PressureProjection:
 
     # ---------------------------------------------------------- interface
     def set_coefficients(self, alpha, solid, rho_liquid, rho_air):
+        self._order()
         self._check(self._lib.mhdproj_set_coefficients(self._ctx, _ptr(alpha), _ptr(solid), rho_liquid, rho_air))
 
     def set_phase_drag(self, phase, drag_rate, dt):
+        self._order()
         self._check(self._lib.mhdproj_set_phase_drag(self._ctx, _ptr(phase), drag_rate, dt))
 
     def project(self, u_star, dt, warm_start=False, out=None, pressure=True):
         """Project (u*, v*, w*) -> ((u, v, w), p, stats)."""
+        self._order()
         torch = self._torch
         if out is None:
             out = tuple(torch.empty_like(t) for t in u_star)
@@ -247,6 +265,7 @@ class PressureProjection:
         return out, p_out, st
 
     def vjp(self, grad_u, grad_p, dt):
+        self._order()
         torch = self._torch
         out = tuple(torch.empty_like(t) for t in grad_u)
         st = Stats()
@@ -255,6 +274,7 @@ class PressureProjection:
         return out, st
 
     def chain_forward(self, u0, force, dt, steps, checkpoint_every=4):
+        self._order()
         torch = self._torch
         uf = tuple(torch.empty_like(t) for t in u0)
         J = C.c_double()
@@ -265,6 +285,7 @@ class PressureProjection:
         return uf, J.value, st
 
     def chain_backward(self, like):
+        self._order()
         torch = self._torch
         g = tuple(torch.empty_like(t) for t in like)
         st = Stats()
@@ -272,26 +293,38 @@ class PressureProjection:
         return g, st
 
     def apply_operator(self, x):
+        self._order()
         y = self._torch.empty_like(x)
         self._check(self._lib.mhdproj_apply_operator(self._ctx, _ptr(x), _ptr(y)))
         return y
 
     def apply_preconditioner(self, r):
+        self._order()
         z = self._torch.empty_like(r)
         self._check(self._lib.mhdproj_apply_preconditioner(self._ctx, _ptr(r), _ptr(z)))
         return z
 
     def coefficients(self):
+        self._order()
         torch = self._torch
         c = torch.empty(self.cell_shape() + (4,), dtype=torch.float32, device="cuda")
         self._check(self._lib.mhdproj_copy_coefficients(self._ctx, _ptr(c)))
         return c
 
     def potential(self):
+        self._order()
         torch = self._torch
         phi = torch.empty(self.cell_shape(), dtype=torch.float64, device="cuda")
         self._check(self._lib.mhdproj_copy_potential(self._ctx, _ptr(phi)))
         return phi
+
+    def profile_kernels(self, reps=20):
+        """Per-kernel mean launch time (ms), algorithmic bytes and launches per CG iteration."""
+        buf = (KernelTime * 16)()
+        n = C.c_int()
+        self._check(self._lib.mhdproj_profile_kernels(self._ctx, reps, buf, 16, C.byref(n)))
+        return [dict(name=buf[i].name.decode(), ms=buf[i].ms, bytes=buf[i].bytes, per_iteration=buf[i].per_iteration)
+                for i in range(n.value)]
 
     def topology(self):
         n = self.dims[0] * self.dims[1] * self.dims[2]
