@@ -108,6 +108,70 @@ template <> __device__ __forceinline__ float from_f<float>(float v) { return v; 
 template <> __device__ __forceinline__ __half from_f<__half>(float v) { return __float2half_rn(v); }
 template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
 
+// ------------------------------------------------ double-FP32 arithmetic
+// GB300 runs FP64 at a small fraction of its FP32 rate, so values that need
+// more than FP32 precision (the refinement residual, the accumulated
+// potential, the right-hand side) are carried as unevaluated sums hi + lo of
+// two FP32 numbers, with error-free transformations (Knuth's TwoSum, the
+// FMA-based TwoProduct; Dekker 1971, Ogita-Rump-Oishi 2005).  That gives
+// about 48 significant bits on the FP32 pipes.
+struct df {
+    float hi, lo;
+};
+__device__ __forceinline__ df two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+__device__ __forceinline__ df fast_two_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ df two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+    df s = two_sum(a.hi, b.hi);
+    const df t = two_sum(a.lo, b.lo);
+    s.lo = __fadd_rn(s.lo, t.hi);
+    s = fast_two_sum(s.hi, s.lo);
+    s.lo = __fadd_rn(s.lo, t.lo);
+    return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df df_neg(df a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
+__device__ __forceinline__ df df_add_f(df a, float b) {
+    df s = two_sum(a.hi, b);
+    s.lo = __fadd_rn(s.lo, a.lo);
+    return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df df_mul_f(df a, float b) {
+    df p = two_prod(a.hi, b);
+    p.lo = __fmaf_rn(a.lo, b, p.lo);
+    return fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ float df_to_f(df a) { return __fadd_rn(a.hi, a.lo); }
+
+// Compensated accumulator of FP32 products (Dot2): exact products, TwoSum
+// accumulation; the thread total is handed to FP64 only once per thread.
+struct Acc {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const df t = two_sum(s, x);
+        s = t.hi;
+        c = __fadd_rn(c, t.lo);
+    }
+    __device__ __forceinline__ void add_prod(float a, float b) {
+        const df p = two_prod(a, b);
+        const df t = two_sum(s, p.hi);
+        s = t.hi;
+        c = __fadd_rn(c, __fadd_rn(t.lo, p.lo));
+    }
+    __device__ __forceinline__ double total() const { return (double)s + (double)c; }
+};
+
 // ------------------------------------------------------- reductions
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);

@@ -49,7 +49,9 @@ struct mhdproj_ctx {
     float* gtop = nullptr;
     float rho_l = 0.f, rho_air = 0.f;
     // solver state
-    double *b64 = nullptr, *phi64 = nullptr, *psi64 = nullptr;
+    // double-FP32 pairs: right-hand side, potential, adjoint potential
+    float *b_hi = nullptr, *b_lo = nullptr, *phi_hi = nullptr, *phi_lo = nullptr;
+    float *psi_hi = nullptr, *psi_lo = nullptr;
     float *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *e = nullptr, *ztmp = nullptr;
     Scalars* sc = nullptr;
     Scalars* h_sc = nullptr;
@@ -111,8 +113,8 @@ static Fields fields(mhdproj_ctx* c) {
     F.coef_lo = c->coef_lo;
     F.coef_lo_kind = c->opt.precision;
     F.gtop = c->gtop;
-    F.b64 = c->b64;
-    F.phi64 = c->phi64;
+    F.b_hi = c->b_hi;
+    F.b_lo = c->b_lo;
     F.r = c->r;
     F.z = c->z;
     F.p = c->p;
@@ -289,9 +291,12 @@ extern "C" int mhdproj_create(const mhdproj_grid* grid, const mhdproj_options* o
              CK(dalloc(ctx, &ctx->coef, n * sizeof(float4)));
              if (ctx->opt.precision != 0) CK(dalloc(ctx, (uint2**)&ctx->coef_lo, n * sizeof(uint2)));
              CK(dalloc(ctx, &ctx->gtop, (size_t)grid->nx * grid->ny * 4));
-             CK(dalloc(ctx, &ctx->b64, n * 8));
-             CK(dalloc(ctx, &ctx->phi64, n * 8));
-             CK(dalloc(ctx, &ctx->psi64, n * 8));
+             CK(dalloc(ctx, &ctx->b_hi, n * 4));
+             CK(dalloc(ctx, &ctx->b_lo, n * 4));
+             CK(dalloc(ctx, &ctx->phi_hi, n * 4));
+             CK(dalloc(ctx, &ctx->phi_lo, n * 4));
+             CK(dalloc(ctx, &ctx->psi_hi, n * 4));
+             CK(dalloc(ctx, &ctx->psi_lo, n * 4));
              CK(dalloc(ctx, &ctx->r, n * 4));
              CK(dalloc(ctx, &ctx->z, n * 4));
              CK(dalloc(ctx, &ctx->p, n * 4));
@@ -480,14 +485,16 @@ static int launch_iterations(mhdproj_ctx* ctx, int count) {
     return 0;
 }
 
-// Solve A x = b64 (already in ctx->b64 with ||b||^2 in sc->bb) by CG with
-// FP64 refinement.  x64 holds the initial guess.  Returns 0 or an error.
-static int solve(mhdproj_ctx* ctx, double* x64, mhdproj_stats* st) {
+// Solve A x = b (the double-FP32 pair in ctx->b_hi/b_lo, ||b||^2 in sc->bb)
+// by CG with iterative refinement: each pass solves A e = r in FP32 and adds
+// e to the double-FP32 solution x, whose residual b - A x is recomputed in
+// double-FP32.  x holds the initial guess.  Returns 0 or an error.
+static int solve(mhdproj_ctx* ctx, float* x_hi, float* x_lo, mhdproj_stats* st) {
     Fields F = fields(ctx);
     const double tol2 = (double)ctx->opt.rel_tol * ctx->opt.rel_tol;
     (void)tol2;
     int passes = 0;
-    launch_residual64(ctx->L, F, x64, ctx->stream);
+    launch_residual(ctx->L, F, x_hi, x_lo, ctx->stream);
     enqueue_precondition(ctx);
     launch_dot_rz(ctx->L, F, 1, ctx->stream);
     CK(cudaGetLastError());
@@ -530,9 +537,9 @@ static int solve(mhdproj_ctx* ctx, double* x64, mhdproj_stats* st) {
             rr_prev = T.rr;
             it_prev = T.iterations;
         }
-        launch_accumulate(ctx->L, F, x64, ctx->stream);
+        launch_accumulate(ctx->L, F, x_hi, x_lo, ctx->stream);
         passes++;
-        launch_residual64(ctx->L, F, x64, ctx->stream);
+        launch_residual(ctx->L, F, x_hi, x_lo, ctx->stream);
         enqueue_precondition(ctx);
         launch_dot_rz(ctx->L, F, 1, ctx->stream);
         CK(cudaGetLastError());
@@ -570,11 +577,14 @@ static int project_gb300(mhdproj_ctx* ctx, const float* us, const float* vs, con
     begin_scalars(ctx);
     Fields F = fields(ctx);
     launch_rhs(ctx->L, F, us, vs, ws, ctx->stream);
-    if (!warm || !ctx->have_solution) CK(cudaMemsetAsync(ctx->phi64, 0, ctx->n * 8, ctx->stream));
+    if (!warm || !ctx->have_solution) {
+        CK(cudaMemsetAsync(ctx->phi_hi, 0, ctx->n * 4, ctx->stream));
+        CK(cudaMemsetAsync(ctx->phi_lo, 0, ctx->n * 4, ctx->stream));
+    }
     mhdproj_stats local{};
-    int rc = solve(ctx, ctx->phi64, &local);
+    int rc = solve(ctx, ctx->phi_hi, ctx->phi_lo, &local);
     if (rc) return rc;
-    launch_correct(ctx->L, F, ctx->phi64, us, vs, ws, uo, vo, wo, po, dt, ctx->stream);
+    launch_correct(ctx->L, F, ctx->phi_hi, ctx->phi_lo, us, vs, ws, uo, vo, wo, po, dt, ctx->stream);
     if (ctx->opt.compute_divergence) launch_divergence(ctx->L, F, uo, vo, wo, ctx->stream);
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev_b, ctx->stream));
@@ -658,10 +668,11 @@ static int vjp_gb300(mhdproj_ctx* ctx, const float* gu, const float* gv, const f
     begin_scalars(ctx);
     Fields F = fields(ctx);
     launch_adj_rhs(ctx->L, F, gu, gv, gw, gp, dt, ctx->stream);
-    CK(cudaMemsetAsync(ctx->psi64, 0, ctx->n * 8, ctx->stream));
-    int rc = solve(ctx, ctx->psi64, st);
+    CK(cudaMemsetAsync(ctx->psi_hi, 0, ctx->n * 4, ctx->stream));
+    CK(cudaMemsetAsync(ctx->psi_lo, 0, ctx->n * 4, ctx->stream));
+    int rc = solve(ctx, ctx->psi_hi, ctx->psi_lo, st);
     if (rc) return rc;
-    launch_adj_correct(ctx->L, F, ctx->psi64, gu, gv, gw, ou, ov, ow, ctx->stream);
+    launch_adj_correct(ctx->L, F, ctx->psi_hi, ctx->psi_lo, gu, gv, gw, ou, ov, ow, ctx->stream);
     CK(cudaGetLastError());
     return 0;
 }
@@ -744,10 +755,11 @@ extern "C" int mhdproj_chain_forward(mhdproj_ctx* ctx, const float* u0x, const f
         mhdproj_stats one{};
         begin_scalars(ctx);
         launch_rhs(ctx->L, F, ctx->c_star[0], ctx->c_star[1], ctx->c_star[2], s);
-        CK(cudaMemsetAsync(ctx->phi64, 0, ctx->n * 8, s));
-        rc = solve(ctx, ctx->phi64, &one);
+        CK(cudaMemsetAsync(ctx->phi_hi, 0, ctx->n * 4, s));
+        CK(cudaMemsetAsync(ctx->phi_lo, 0, ctx->n * 4, s));
+        rc = solve(ctx, ctx->phi_hi, ctx->phi_lo, &one);
         if (rc) return rc;
-        launch_correct(ctx->L, F, ctx->phi64, ctx->c_star[0], ctx->c_star[1], ctx->c_star[2], ctx->c_cur[0],
+        launch_correct(ctx->L, F, ctx->phi_hi, ctx->phi_lo, ctx->c_star[0], ctx->c_star[1], ctx->c_star[2], ctx->c_cur[0],
                        ctx->c_cur[1], ctx->c_cur[2], nullptr, dt, s);
         total.iterations += one.iterations;
         total.refinements += one.refinements;
@@ -868,7 +880,8 @@ extern "C" int mhdproj_copy_potential(mhdproj_ctx* ctx, double* phi) {
         if (rc) return rc;
         return wait_stream(ctx);
     }
-    CK(cudaMemcpyAsync(phi, ctx->phi64, ctx->n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    launch_to_double(ctx->phi_hi, ctx->phi_lo, phi, ctx->n, ctx->stream);
+    CK(cudaGetLastError());
     return wait_stream(ctx);
 }
 
@@ -911,7 +924,7 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
         {"fine_prolong", 8.25, 1, 4},
         {"dot_rz", 8.0, 1, 5},
         {"search", 12.0, 1, 6},
-        {"residual64", 24.0, 0, 7},           // x 4 + beta 12 + b 4 -> r 4 (survey K7)
+        {"refinement_residual", 24.0, 0, 7},  // x 4 + beta 12 + b 4 -> r 4 (survey K7)
         {"coefficients", 29.0, 0, 8},         // alpha 4 + solid 1 -> 16 + 8 (survey K0)
     };
     int k = 0;
@@ -929,7 +942,7 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
                 case 4: mg_fine_prolong(ctx->mg, s); break;
                 case 5: launch_dot_rz(ctx->L, F, 0, s); break;
                 case 6: launch_search(ctx->L, F, s); break;
-                case 7: launch_residual64(ctx->L, F, ctx->phi64, s); break;
+                case 7: launch_residual(ctx->L, F, ctx->phi_hi, ctx->phi_lo, s); break;
                 case 8: launch_coefficients(ctx->L, F, s); break;
             }
             if (it.kind == 1 || it.kind == 5 || it.kind == 7) launch_set_sigma(ctx->sc, 1.0f, s);

@@ -3,12 +3,15 @@
 // Layout in HBM (x-fastest, cell i = x + nx*(y + ny*z)):
 //   coef  float4[n]  (beta_x, beta_y, beta_z of the low faces, reaction)
 //   cls   uint8[n]   0 solid, 1 active, 2 pinned gauge cell
-//   b64, phi64 double[n]; r, z, p, q, e float[n]
+//   b (hi, lo), phi (hi, lo) float[n] pairs; r, z, p, q, e float[n]
 //   faces u[(nx+1) ny nz], v[nx (ny+1) nz], w[nx ny (nz+1)]
 // Every kernel walks 32x8 (x, y) tiles over a run of z, so warps read 128-byte
-// rows and neighbouring z-planes are reused from L2.  Reductions are FP64:
-// warp shuffles, one partial per block, and a deterministic fixed-order sum
-// in the last block to finish, which also updates the CG scalars.
+// rows and neighbouring z-planes are reused from L2.  Reductions take
+// error-free FP32 products and compensated sums per thread, then FP64 warp
+// shuffles, one partial per block, and a deterministic fixed-order sum in the
+// last block, which also updates the CG scalars.  Quantities that need more
+// than FP32 (right-hand side, accumulated potential, refinement residual) are
+// double-FP32 pairs (see common.cuh).
 #include "kernels.h"
 
 namespace mhdproj {
@@ -118,47 +121,51 @@ __global__ void __launch_bounds__(TILE_THREADS) k_coefficients(Grid3 g, int outl
 }
 
 // ------------------------------------------------------------------ rhs
-// b = -h * sum over open faces of (u_high - u_low), FP64; ||b||^2.
+// b = -h * sum over open faces of (u_high - u_low) as a double-FP32 pair;
+// ||b||^2.
 __global__ void __launch_bounds__(TILE_THREADS) k_rhs(Grid3 g, int outlet, float h, const uint8_t* __restrict__ cls,
                                                       const float* __restrict__ u, const float* __restrict__ v,
-                                                      const float* __restrict__ w, double* __restrict__ b,
-                                                      Scalars* sc, double* partials, int nblocks) {
+                                                      const float* __restrict__ w, float* __restrict__ b_hi,
+                                                      float* __restrict__ b_lo, Scalars* sc, double* partials,
+                                                      int nblocks) {
     __shared__ double sh[8 * 1];
-    double acc[1] = {0.0};
+    Acc acc;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     TILE_BEGIN(g) {
         if (!in_xy) continue;
         const int i = cell_index(g, x, y, z);
-        double bi = 0.0;
+        df bi = {0.0f, 0.0f};
         if (cls[i] == 1) {
             const Nbr nb = neighbours(g, x, y, z);
-            double sum = 0.0;
+            df sum = {0.0f, 0.0f};
             {
                 const int hx = (x + 1 == nx && (g.periodic & 1)) ? 0 : x + 1;
-                const double lo = (nb.xm >= 0 && cls[nb.xm] != 0) ? (double)u[x + (nx + 1) * (y + ny * z)] : 0.0;
-                const double hi = (nb.xp >= 0 && cls[nb.xp] != 0) ? (double)u[hx + (nx + 1) * (y + ny * z)] : 0.0;
-                sum += hi - lo;
+                const float lo = (nb.xm >= 0 && cls[nb.xm] != 0) ? u[x + (nx + 1) * (y + ny * z)] : 0.0f;
+                const float hi = (nb.xp >= 0 && cls[nb.xp] != 0) ? u[hx + (nx + 1) * (y + ny * z)] : 0.0f;
+                sum = df_add(sum, two_sum(hi, -lo));
             }
             {
                 const int hy = (y + 1 == ny && (g.periodic & 2)) ? 0 : y + 1;
-                const double lo = (nb.ym >= 0 && cls[nb.ym] != 0) ? (double)v[x + nx * (y + (ny + 1) * z)] : 0.0;
-                const double hi = (nb.yp >= 0 && cls[nb.yp] != 0) ? (double)v[x + nx * (hy + (ny + 1) * z)] : 0.0;
-                sum += hi - lo;
+                const float lo = (nb.ym >= 0 && cls[nb.ym] != 0) ? v[x + nx * (y + (ny + 1) * z)] : 0.0f;
+                const float hi = (nb.yp >= 0 && cls[nb.yp] != 0) ? v[x + nx * (hy + (ny + 1) * z)] : 0.0f;
+                sum = df_add(sum, two_sum(hi, -lo));
             }
             {
                 const int hz = (z + 1 == nz && (g.periodic & 4)) ? 0 : z + 1;
-                const double lo = (nb.zm >= 0 && cls[nb.zm] != 0) ? (double)w[x + nx * (y + ny * z)] : 0.0;
-                const bool hopen = (nb.zp >= 0 && cls[nb.zp] != 0) || (outlet && z + 1 == nz);
-                const double hi = hopen ? (double)w[x + nx * (y + ny * hz)] : 0.0;
-                sum += hi - lo;
+                const float lo = (nb.zm >= 0 && cls[nb.zm] != 0) ? w[x + nx * (y + ny * z)] : 0.0f;
+                const bool hopen = (nb.zp >= 0 && cls[nb.zp] != 0) || (nb.zp < 0 && outlet && z + 1 == nz);
+                const float hi = hopen ? w[x + nx * (y + ny * hz)] : 0.0f;
+                sum = df_add(sum, two_sum(hi, -lo));
             }
-            bi = -(double)h * sum;
+            bi = df_mul_f(sum, -h);
         }
-        b[i] = bi;
-        acc[0] += bi * bi;
+        b_hi[i] = bi.hi;
+        b_lo[i] = bi.lo;
+        acc.add_prod(bi.hi, bi.hi);
     }
-    block_sum<1>(acc, sh);
-    if (store_partials_is_last<1>(acc, partials, nblocks, &sc->ticket[0])) {
+    double v1[1] = {acc.total()};
+    block_sum<1>(v1, sh);
+    if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[0])) {
         double tot[1];
         finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[0]);
         if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -185,25 +192,45 @@ __device__ __forceinline__ T apply_cell(const Grid3& g, const float4* __restrict
 }
 
 // ------------------------------------------------- refinement residual
-// r = b - A x in FP64 (x FP64), stored FP32 for the inner solve; e = 0.
-__global__ void __launch_bounds__(TILE_THREADS) k_residual64(Grid3 g, const float4* __restrict__ coef,
-                                                             const double* __restrict__ b,
-                                                             const double* __restrict__ x64, float* __restrict__ r,
-                                                             float* __restrict__ e, Scalars* sc, double* partials,
-                                                             int nblocks, long long n_active) {
+// (A x)_i in double-FP32 from a double-FP32 x and the FP32 mobilities.
+__device__ __forceinline__ df apply_cell_df(const float4* __restrict__ coef, const float* __restrict__ xh,
+                                            const float* __restrict__ xl, int i, const Nbr& nb) {
+    const float4 c = coef[i];
+    const df xi = {xh[i], xl[i]};
+    df acc = df_mul_f(xi, c.w);
+    if (c.x != 0.f) acc = df_add(acc, df_mul_f(df_sub(xi, df{xh[nb.xm], xl[nb.xm]}), c.x));
+    if (c.y != 0.f) acc = df_add(acc, df_mul_f(df_sub(xi, df{xh[nb.ym], xl[nb.ym]}), c.y));
+    if (c.z != 0.f) acc = df_add(acc, df_mul_f(df_sub(xi, df{xh[nb.zm], xl[nb.zm]}), c.z));
+    if (nb.xp >= 0) { const float bh = coef[nb.xp].x; if (bh != 0.f) acc = df_add(acc, df_mul_f(df_sub(xi, df{xh[nb.xp], xl[nb.xp]}), bh)); }
+    if (nb.yp >= 0) { const float bh = coef[nb.yp].y; if (bh != 0.f) acc = df_add(acc, df_mul_f(df_sub(xi, df{xh[nb.yp], xl[nb.yp]}), bh)); }
+    if (nb.zp >= 0) { const float bh = coef[nb.zp].z; if (bh != 0.f) acc = df_add(acc, df_mul_f(df_sub(xi, df{xh[nb.zp], xl[nb.zp]}), bh)); }
+    return acc;
+}
+
+// r = b - A x in double-FP32 (x a double-FP32 pair), stored FP32 for the
+// inner solve; e = 0.
+__global__ void __launch_bounds__(TILE_THREADS) k_residual(Grid3 g, const float4* __restrict__ coef,
+                                                           const float* __restrict__ b_hi,
+                                                           const float* __restrict__ b_lo,
+                                                           const float* __restrict__ x_hi,
+                                                           const float* __restrict__ x_lo, float* __restrict__ r,
+                                                           float* __restrict__ e, Scalars* sc, double* partials,
+                                                           int nblocks, long long n_active) {
     __shared__ double sh[8 * 1];
-    double acc[1] = {0.0};
+    Acc acc;
     TILE_BEGIN(g) {
         if (!in_xy) continue;
         const int i = cell_index(g, x, y, z);
         const Nbr nb = neighbours(g, x, y, z);
-        const double ri = b[i] - apply_cell<double>(g, coef, x64, i, nb);
-        r[i] = (float)ri;
+        const df res = df_sub(df{b_hi[i], b_lo[i]}, apply_cell_df(coef, x_hi, x_lo, i, nb));
+        const float ri = df_to_f(res);
+        r[i] = ri;
         e[i] = 0.0f;
-        acc[0] += ri * ri;
+        acc.add_prod(ri, ri);
     }
-    block_sum<1>(acc, sh);
-    if (store_partials_is_last<1>(acc, partials, nblocks, &sc->ticket[1])) {
+    double v1[1] = {acc.total()};
+    block_sum<1>(v1, sh);
+    if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[1])) {
         double tot[1];
         finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[1]);
         if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -228,17 +255,18 @@ __global__ void __launch_bounds__(TILE_THREADS) k_spmv_pq(Grid3 g, const float4*
                                                           Scalars* sc, double* partials, int nblocks) {
     if (sc->converged) return;
     __shared__ double sh[8 * 1];
-    double acc[1] = {0.0};
+    Acc acc;
     TILE_BEGIN(g) {
         if (!in_xy) continue;
         const int i = cell_index(g, x, y, z);
         const Nbr nb = neighbours(g, x, y, z);
         const float qi = apply_cell<float>(g, coef, p, i, nb);
         q[i] = qi;
-        acc[0] += (double)p[i] * (double)qi;
+        acc.add_prod(p[i], qi);
     }
-    block_sum<1>(acc, sh);
-    if (store_partials_is_last<1>(acc, partials, nblocks, &sc->ticket[2])) {
+    double v1[1] = {acc.total()};
+    block_sum<1>(v1, sh);
+    if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[2])) {
         double tot[1];
         finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[2]);
         if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -264,7 +292,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_update(Grid3 g, float* __restr
                                                          long long n_active) {
     if (sc->converged) return;
     __shared__ double sh[8 * 1];
-    double acc[1] = {0.0};
+    Acc acc;
     const float a = sc->alpha_f;
     TILE_BEGIN(g) {
         if (!in_xy) continue;
@@ -272,10 +300,11 @@ __global__ void __launch_bounds__(TILE_THREADS) k_update(Grid3 g, float* __restr
         e[i] = fmaf(a, p[i], e[i]);
         const float ri = fmaf(-a, q[i], r[i]);
         r[i] = ri;
-        acc[0] += (double)ri * (double)ri;
+        acc.add_prod(ri, ri);
     }
-    block_sum<1>(acc, sh);
-    if (store_partials_is_last<1>(acc, partials, nblocks, &sc->ticket[3])) {
+    double v1[1] = {acc.total()};
+    block_sum<1>(v1, sh);
+    if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[3])) {
         double tot[1];
         finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[3]);
         if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -300,17 +329,18 @@ __global__ void __launch_bounds__(TILE_THREADS) k_dot_rz(Grid3 g, const float* _
                                                          Scalars* sc, double* partials, int nblocks) {
     if (sc->converged) return;
     __shared__ double sh[8 * 1];
-    double acc[1] = {0.0};
+    Acc acc;
     const float is = sc->inv_sigma;
     TILE_BEGIN(g) {
         if (!in_xy) continue;
         const int i = cell_index(g, x, y, z);
         const float zi = zv[i] * is;
         if (init) p[i] = zi;
-        acc[0] += (double)r[i] * (double)zi;
+        acc.add_prod(r[i], zi);
     }
-    block_sum<1>(acc, sh);
-    if (store_partials_is_last<1>(acc, partials, nblocks, &sc->ticket[4])) {
+    double v1[1] = {acc.total()};
+    block_sum<1>(v1, sh);
+    if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[4])) {
         double tot[1];
         finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[4]);
         if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -343,13 +373,20 @@ __global__ void __launch_bounds__(TILE_THREADS) k_search(Grid3 g, const float* _
     }
 }
 
-__global__ void __launch_bounds__(TILE_THREADS) k_accumulate(Grid3 g, double* __restrict__ x64,
-                                                             const float* __restrict__ e) {
+__global__ void __launch_bounds__(TILE_THREADS) k_accumulate(Grid3 g, float* __restrict__ x_hi,
+                                                             float* __restrict__ x_lo, const float* __restrict__ e) {
     TILE_BEGIN(g) {
         if (!in_xy) continue;
         const int i = cell_index(g, x, y, z);
-        x64[i] += (double)e[i];
+        const df v = df_add_f(df{x_hi[i], x_lo[i]}, e[i]);
+        x_hi[i] = v.hi;
+        x_lo[i] = v.lo;
     }
+}
+__global__ void k_to_double(const float* __restrict__ hi, const float* __restrict__ lo, double* __restrict__ out,
+                            long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (double)hi[i] + (double)lo[i];
 }
 
 __global__ void __launch_bounds__(TILE_THREADS) k_apply(Grid3 g, const float4* __restrict__ coef,
@@ -372,35 +409,36 @@ __global__ void __launch_bounds__(TILE_THREADS) k_scale(Grid3 g, const float* __
 
 // ---------------------------------------------------- gradient subtraction
 // u = u* - beta (phi_R - phi_L) / h on open faces, the outlet face uses its
-// conductance against p = 0 on the face, closed faces are 0.  Each thread
-// owns the low faces of its cell; the thread at index 0 of a periodic axis
-// also writes the duplicate last face, the thread at the high end of a closed
-// axis writes that wall face.
+// conductance against p = 0 on the face, closed faces are 0.  Potential
+// differences are taken in double-FP32 before rounding.  Each thread owns the
+// low faces of its cell; the thread at index 0 of a periodic axis also writes
+// the duplicate last face, the thread at the high end of a closed axis writes
+// that wall face.
+__device__ __forceinline__ float grad_term(float bt, df pi, df pj, float inv_h) {
+    return __fmul_rn(__fmul_rn(bt, df_to_f(df_sub(pi, pj))), inv_h);
+}
 __global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, float h, float rho_l, float rho_air,
-                                                          double p_scale, const uint8_t* __restrict__ cls,
+                                                          float p_scale, const uint8_t* __restrict__ cls,
                                                           const float* __restrict__ alpha,
                                                           const float* __restrict__ gtop,
-                                                          const double* __restrict__ phi,
+                                                          const float* __restrict__ ph, const float* __restrict__ pl,
                                                           const float* __restrict__ us, const float* __restrict__ vs,
                                                           const float* __restrict__ ws, float* __restrict__ uo,
                                                           float* __restrict__ vo, float* __restrict__ wo,
                                                           float* __restrict__ po) {
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const double hd = (double)h;
+    const float inv_h = 1.0f / h;
     TILE_BEGIN(g) {
         if (!in_xy) continue;
         const int i = cell_index(g, x, y, z);
         const Nbr nb = neighbours(g, x, y, z);
         const uint8_t ci = cls[i];
-        const double pi = phi[i];
-        // x low face
+        const df pi = {ph[i], pl[i]};
         {
             const int f = x + (nx + 1) * (y + ny * z);
             float out = 0.0f;
-            if (nb.xm >= 0 && ci != 0 && cls[nb.xm] != 0) {
-                const float bt = beta_of(alpha[nb.xm], alpha[i], rho_l, rho_air);
-                out = (float)((double)us[f] - (double)bt * (pi - phi[nb.xm]) / hd);
-            }
+            if (nb.xm >= 0 && ci != 0 && cls[nb.xm] != 0)
+                out = us[f] - grad_term(beta_of(alpha[nb.xm], alpha[i], rho_l, rho_air), pi, df{ph[nb.xm], pl[nb.xm]}, inv_h);
             uo[f] = out;
             if (x == 0 && (g.periodic & 1)) uo[nx + (nx + 1) * (y + ny * z)] = out;
             if (x == nx - 1 && !(g.periodic & 1)) uo[nx + (nx + 1) * (y + ny * z)] = 0.0f;
@@ -408,10 +446,8 @@ __global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, f
         {
             const int f = x + nx * (y + (ny + 1) * z);
             float out = 0.0f;
-            if (nb.ym >= 0 && ci != 0 && cls[nb.ym] != 0) {
-                const float bt = beta_of(alpha[nb.ym], alpha[i], rho_l, rho_air);
-                out = (float)((double)vs[f] - (double)bt * (pi - phi[nb.ym]) / hd);
-            }
+            if (nb.ym >= 0 && ci != 0 && cls[nb.ym] != 0)
+                out = vs[f] - grad_term(beta_of(alpha[nb.ym], alpha[i], rho_l, rho_air), pi, df{ph[nb.ym], pl[nb.ym]}, inv_h);
             vo[f] = out;
             if (y == 0 && (g.periodic & 2)) vo[x + nx * (ny + (ny + 1) * z)] = out;
             if (y == ny - 1 && !(g.periodic & 2)) vo[x + nx * (ny + (ny + 1) * z)] = 0.0f;
@@ -419,20 +455,18 @@ __global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, f
         {
             const int f = x + nx * (y + ny * z);
             float out = 0.0f;
-            if (nb.zm >= 0 && ci != 0 && cls[nb.zm] != 0) {
-                const float bt = beta_of(alpha[nb.zm], alpha[i], rho_l, rho_air);
-                out = (float)((double)ws[f] - (double)bt * (pi - phi[nb.zm]) / hd);
-            }
+            if (nb.zm >= 0 && ci != 0 && cls[nb.zm] != 0)
+                out = ws[f] - grad_term(beta_of(alpha[nb.zm], alpha[i], rho_l, rho_air), pi, df{ph[nb.zm], pl[nb.zm]}, inv_h);
             wo[f] = out;
             const int ft = x + nx * (y + ny * nz);
             if (z == 0 && (g.periodic & 4)) wo[ft] = out;
             if (z == nz - 1 && !(g.periodic & 4)) {
                 float top = 0.0f;
-                if (outlet && ci != 0) top = (float)((double)ws[ft] + (double)gtop[x + nx * y] * pi / hd);
+                if (outlet && ci != 0) top = ws[ft] + __fmul_rn(__fmul_rn(gtop[x + nx * y], df_to_f(pi)), inv_h);
                 wo[ft] = top;
             }
         }
-        if (po) po[i] = ci != 0 ? (float)(p_scale * pi) : 0.0f;
+        if (po) po[i] = ci != 0 ? __fmul_rn(p_scale, df_to_f(pi)) : 0.0f;
     }
 }
 
@@ -442,54 +476,51 @@ __global__ void __launch_bounds__(TILE_THREADS) k_divergence(Grid3 g, float h, c
                                                              const float* __restrict__ w, Scalars* sc,
                                                              double* partials, int nblocks) {
     __shared__ double sh[8 * 2];
-    double acc[2] = {0.0, 0.0};
+    __shared__ double shm[8];
+    float mx = 0.0f;
+    Acc acc;
     const int nx = g.nx, ny = g.ny;
+    const float inv_h = 1.0f / h;
     TILE_BEGIN(g) {
         if (!in_xy) continue;
         const int i = cell_index(g, x, y, z);
         if (cls[i] != 1) continue;
-        double d = (double)u[x + 1 + (nx + 1) * (y + ny * z)] - (double)u[x + (nx + 1) * (y + ny * z)];
-        d += (double)v[x + nx * (y + 1 + (ny + 1) * z)] - (double)v[x + nx * (y + (ny + 1) * z)];
-        d += (double)w[x + nx * (y + ny * (z + 1))] - (double)w[x + nx * (y + ny * z)];
-        d /= (double)h;
-        acc[0] = fmax(acc[0], fabs(d));
-        acc[1] += d * d;
+        df d = two_sum(u[x + 1 + (nx + 1) * (y + ny * z)], -u[x + (nx + 1) * (y + ny * z)]);
+        d = df_add(d, two_sum(v[x + nx * (y + 1 + (ny + 1) * z)], -v[x + nx * (y + (ny + 1) * z)]));
+        d = df_add(d, two_sum(w[x + nx * (y + ny * (z + 1))], -w[x + nx * (y + ny * z)]));
+        const float dv = df_to_f(d) * inv_h;
+        mx = fmaxf(mx, fabsf(dv));
+        acc.add_prod(dv, dv);
     }
-    // max via a separate warp/block path: reuse block_sum on -max trick is not
-    // valid, so reduce the max explicitly.
+    const int t = threadIdx.x + blockDim.x * threadIdx.y;
+    double m = warp_max((double)mx);
+    if ((t & 31) == 0) shm[t >> 5] = m;
+    double v2[2] = {0.0, acc.total()};
     {
-        const int t = threadIdx.x + blockDim.x * threadIdx.y;
-        double m = warp_max(acc[0]);
-        __shared__ double shm[8];
-        if ((t & 31) == 0) shm[t >> 5] = m;
-        __syncthreads();
-        if (t < 32) {
-            double mm = t < 8 ? shm[t] : 0.0;
-            acc[0] = warp_max(mm);
-        }
-        __syncthreads();
+        double s1[1] = {v2[1]};
+        block_sum<1>(s1, sh);  // contains the barrier that publishes shm
+        v2[1] = s1[0];
     }
-    {
-        double s1[1] = {acc[1]};
-        block_sum<1>(s1, sh);
-        acc[1] = s1[0];
+    if (t == 0) {
+        double mm = 0.0;
+        for (int k = 0; k < 8; k++) mm = fmax(mm, shm[k]);
+        v2[0] = mm;
     }
-    if (store_partials_is_last<2>(acc, partials, nblocks, &sc->ticket[5])) {
+    if (store_partials_is_last<2>(v2, partials, nblocks, &sc->ticket[5])) {
         __threadfence();
-        const int t = threadIdx.x + blockDim.x * threadIdx.y;
-        double m = 0.0, s = 0.0;
+        double mb = 0.0, sb = 0.0;
         for (int b = t; b < nblocks; b += TILE_THREADS) {
-            m = fmax(m, ((volatile double*)partials)[b]);
-            s += ((volatile double*)partials)[nblocks + b];
+            mb = fmax(mb, ((volatile double*)partials)[b]);
+            sb += ((volatile double*)partials)[nblocks + b];
         }
-        m = warp_max(m);
-        __shared__ double shm2[8];
-        if ((t & 31) == 0) shm2[t >> 5] = m;
-        double s1[1] = {s};
+        mb = warp_max(mb);
+        __syncthreads();
+        if ((t & 31) == 0) shm[t >> 5] = mb;
+        double s1[1] = {sb};
         block_sum<1>(s1, sh);
         if (t == 0) {
             double mm = 0.0;
-            for (int k = 0; k < 8; k++) mm = fmax(mm, shm2[k]);
+            for (int k = 0; k < 8; k++) mm = fmax(mm, shm[k]);
             sc->divmax = mm;
             sc->div2 = s1[0];
             sc->ticket[5] = 0u;
@@ -499,70 +530,71 @@ __global__ void __launch_bounds__(TILE_THREADS) k_divergence(Grid3 g, float h, c
 
 // ----------------------------------------------------------- adjoint
 // g_phi = d u / d phi ^T g_u + rho_l/dt g_p on active cells (the transposed
-// gradient), FP64, into b64; ||b||^2.  Gradients of a periodic duplicate face
-// are folded into the canonical face.
+// gradient), a double-FP32 right-hand side; ||b||^2.  Gradients of a periodic
+// duplicate face are folded into the canonical face.
 __global__ void __launch_bounds__(TILE_THREADS) k_adj_rhs(Grid3 g, int outlet, float h, float rho_l, float rho_air,
-                                                          double p_scale, const uint8_t* __restrict__ cls,
+                                                          float p_scale, const uint8_t* __restrict__ cls,
                                                           const float* __restrict__ alpha,
                                                           const float* __restrict__ gtop,
                                                           const float* __restrict__ gu, const float* __restrict__ gv,
                                                           const float* __restrict__ gw, const float* __restrict__ gp,
-                                                          double* __restrict__ b, Scalars* sc, double* partials,
-                                                          int nblocks) {
+                                                          float* __restrict__ b_hi, float* __restrict__ b_lo,
+                                                          Scalars* sc, double* partials, int nblocks) {
     __shared__ double sh[8 * 1];
-    double acc[1] = {0.0};
+    Acc acc;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const double inv_h = 1.0 / (double)h;
+    const float inv_h = 1.0f / h;
     TILE_BEGIN(g) {
         if (!in_xy) continue;
         const int i = cell_index(g, x, y, z);
-        double s = 0.0;
+        df s = {0.0f, 0.0f};
         if (cls[i] == 1) {
             const Nbr nb = neighbours(g, x, y, z);
             const float ai = alpha[i];
-            // x faces
             if (nb.xm >= 0 && cls[nb.xm] != 0) {
-                double gf = gu[x + (nx + 1) * (y + ny * z)];
+                float gf = gu[x + (nx + 1) * (y + ny * z)];
                 if (x == 0) gf += gu[nx + (nx + 1) * (y + ny * z)];
-                s -= (double)beta_of(alpha[nb.xm], ai, rho_l, rho_air) * inv_h * gf;
+                s = df_add(s, two_prod(-beta_of(alpha[nb.xm], ai, rho_l, rho_air) * inv_h, gf));
             }
             if (nb.xp >= 0 && cls[nb.xp] != 0) {
                 const int hx = x + 1 == nx ? 0 : x + 1;
-                double gf = gu[hx + (nx + 1) * (y + ny * z)];
+                float gf = gu[hx + (nx + 1) * (y + ny * z)];
                 if (hx == 0) gf += gu[nx + (nx + 1) * (y + ny * z)];
-                s += (double)beta_of(ai, alpha[nb.xp], rho_l, rho_air) * inv_h * gf;
+                s = df_add(s, two_prod(beta_of(ai, alpha[nb.xp], rho_l, rho_air) * inv_h, gf));
             }
             if (nb.ym >= 0 && cls[nb.ym] != 0) {
-                double gf = gv[x + nx * (y + (ny + 1) * z)];
+                float gf = gv[x + nx * (y + (ny + 1) * z)];
                 if (y == 0) gf += gv[x + nx * (ny + (ny + 1) * z)];
-                s -= (double)beta_of(alpha[nb.ym], ai, rho_l, rho_air) * inv_h * gf;
+                s = df_add(s, two_prod(-beta_of(alpha[nb.ym], ai, rho_l, rho_air) * inv_h, gf));
             }
             if (nb.yp >= 0 && cls[nb.yp] != 0) {
                 const int hy = y + 1 == ny ? 0 : y + 1;
-                double gf = gv[x + nx * (hy + (ny + 1) * z)];
+                float gf = gv[x + nx * (hy + (ny + 1) * z)];
                 if (hy == 0) gf += gv[x + nx * (ny + (ny + 1) * z)];
-                s += (double)beta_of(ai, alpha[nb.yp], rho_l, rho_air) * inv_h * gf;
+                s = df_add(s, two_prod(beta_of(ai, alpha[nb.yp], rho_l, rho_air) * inv_h, gf));
             }
             if (nb.zm >= 0 && cls[nb.zm] != 0) {
-                double gf = gw[x + nx * (y + ny * z)];
+                float gf = gw[x + nx * (y + ny * z)];
                 if (z == 0) gf += gw[x + nx * (y + ny * nz)];
-                s -= (double)beta_of(alpha[nb.zm], ai, rho_l, rho_air) * inv_h * gf;
+                s = df_add(s, two_prod(-beta_of(alpha[nb.zm], ai, rho_l, rho_air) * inv_h, gf));
             }
             if (nb.zp >= 0 && cls[nb.zp] != 0) {
                 const int hz = z + 1 == nz ? 0 : z + 1;
-                double gf = gw[x + nx * (y + ny * hz)];
+                float gf = gw[x + nx * (y + ny * hz)];
                 if (hz == 0) gf += gw[x + nx * (y + ny * nz)];
-                s += (double)beta_of(ai, alpha[nb.zp], rho_l, rho_air) * inv_h * gf;
+                s = df_add(s, two_prod(beta_of(ai, alpha[nb.zp], rho_l, rho_air) * inv_h, gf));
             } else if (nb.zp < 0 && outlet && z == nz - 1) {
-                s += (double)gtop[x + nx * y] * inv_h * (double)gw[x + nx * (y + ny * nz)];
+                s = df_add(s, two_prod(gtop[x + nx * y] * inv_h, gw[x + nx * (y + ny * nz)]));
             }
-            if (gp) s += p_scale * (double)gp[i];
+            if (gp) s = df_add(s, two_prod(p_scale, gp[i]));
         }
-        b[i] = s;
-        acc[0] += s * s;
+        b_hi[i] = s.hi;
+        b_lo[i] = s.lo;
+        acc.add_prod(s.hi, s.hi);
     }
-    block_sum<1>(acc, sh);
-    if (store_partials_is_last<1>(acc, partials, nblocks, &sc->ticket[0])) {
+    double v1[1] = {acc.total()};
+    block_sum<1>(v1, sh);
+    if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[0])) {
         double tot[1];
         finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[0]);
         if (threadIdx.x == 0 && threadIdx.y == 0) {
@@ -575,26 +607,25 @@ __global__ void __launch_bounds__(TILE_THREADS) k_adj_rhs(Grid3 g, int outlet, f
 // g_u* = g_u (folded) - h D^T psi on open faces; 0 on closed and duplicate faces.
 __global__ void __launch_bounds__(TILE_THREADS) k_adj_correct(Grid3 g, int outlet, float h,
                                                               const uint8_t* __restrict__ cls,
-                                                              const double* __restrict__ psi,
+                                                              const float* __restrict__ sh_, const float* __restrict__ sl_,
                                                               const float* __restrict__ gu,
                                                               const float* __restrict__ gv,
                                                               const float* __restrict__ gw, float* __restrict__ ou,
                                                               float* __restrict__ ov, float* __restrict__ ow) {
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const double hd = (double)h;
     TILE_BEGIN(g) {
         if (!in_xy) continue;
         const int i = cell_index(g, x, y, z);
         const Nbr nb = neighbours(g, x, y, z);
         const uint8_t ci = cls[i];
-        const double si = psi[i];
+        const df si = {sh_[i], sl_[i]};
         {
             const int f = x + (nx + 1) * (y + ny * z), fd = nx + (nx + 1) * (y + ny * z);
             float out = 0.0f;
             if (nb.xm >= 0 && ci != 0 && cls[nb.xm] != 0) {
-                double gf = gu[f];
+                float gf = gu[f];
                 if (x == 0) gf += gu[fd];
-                out = (float)(gf - hd * psi[nb.xm] + hd * si);
+                out = gf + h * df_to_f(df_sub(si, df{sh_[nb.xm], sl_[nb.xm]}));
             }
             ou[f] = out;
             if (x == nx - 1) ou[fd] = 0.0f;
@@ -603,9 +634,9 @@ __global__ void __launch_bounds__(TILE_THREADS) k_adj_correct(Grid3 g, int outle
             const int f = x + nx * (y + (ny + 1) * z), fd = x + nx * (ny + (ny + 1) * z);
             float out = 0.0f;
             if (nb.ym >= 0 && ci != 0 && cls[nb.ym] != 0) {
-                double gf = gv[f];
+                float gf = gv[f];
                 if (y == 0) gf += gv[fd];
-                out = (float)(gf - hd * psi[nb.ym] + hd * si);
+                out = gf + h * df_to_f(df_sub(si, df{sh_[nb.ym], sl_[nb.ym]}));
             }
             ov[f] = out;
             if (y == ny - 1) ov[fd] = 0.0f;
@@ -614,14 +645,14 @@ __global__ void __launch_bounds__(TILE_THREADS) k_adj_correct(Grid3 g, int outle
             const int f = x + nx * (y + ny * z), fd = x + nx * (y + ny * nz);
             float out = 0.0f;
             if (nb.zm >= 0 && ci != 0 && cls[nb.zm] != 0) {
-                double gf = gw[f];
+                float gf = gw[f];
                 if (z == 0 && (g.periodic & 4)) gf += gw[fd];
-                out = (float)(gf - hd * psi[nb.zm] + hd * si);
+                out = gf + h * df_to_f(df_sub(si, df{sh_[nb.zm], sl_[nb.zm]}));
             }
             ow[f] = out;
             if (z == nz - 1) {
                 float top = 0.0f;
-                if (outlet && !(g.periodic & 4) && ci != 0) top = (float)((double)gw[fd] - hd * si);
+                if (outlet && !(g.periodic & 4) && ci != 0) top = gw[fd] - h * df_to_f(si);
                 ow[fd] = top;
             }
         }
@@ -769,11 +800,11 @@ void launch_init_scalars(Scalars* sc, double tol2, double abs_floor, double inne
 }
 void launch_set_sigma(Scalars* sc, float sigma, cudaStream_t s) { k_set_sigma<<<1, 1, 0, s>>>(sc, sigma); }
 void launch_rhs(const Launch& L, const Fields& F, const float* u, const float* v, const float* w, cudaStream_t s) {
-    k_rhs<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.h, F.cls, u, v, w, F.b64, F.sc, F.partials, L.nblocks);
+    k_rhs<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.h, F.cls, u, v, w, F.b_hi, F.b_lo, F.sc, F.partials, L.nblocks);
 }
-void launch_residual64(const Launch& L, const Fields& F, const double* x64, cudaStream_t s) {
-    k_residual64<<<L.grid, L.block, 0, s>>>(L.g, F.coef, F.b64, x64, F.r, F.e, F.sc, F.partials, L.nblocks,
-                                            F.n_active);
+void launch_residual(const Launch& L, const Fields& F, const float* x_hi, const float* x_lo, cudaStream_t s) {
+    k_residual<<<L.grid, L.block, 0, s>>>(L.g, F.coef, F.b_hi, F.b_lo, x_hi, x_lo, F.r, F.e, F.sc, F.partials,
+                                          L.nblocks, F.n_active);
 }
 void launch_spmv_pq(const Launch& L, const Fields& F, cudaStream_t s) {
     k_spmv_pq<<<L.grid, L.block, 0, s>>>(L.g, F.coef, F.p, F.q, F.sc, F.partials, L.nblocks);
@@ -787,14 +818,18 @@ void launch_dot_rz(const Launch& L, const Fields& F, int init, cudaStream_t s) {
 void launch_search(const Launch& L, const Fields& F, cudaStream_t s) {
     k_search<<<L.grid, L.block, 0, s>>>(L.g, F.z, F.p, F.sc);
 }
-void launch_accumulate(const Launch& L, const Fields& F, double* x64, cudaStream_t s) {
-    k_accumulate<<<L.grid, L.block, 0, s>>>(L.g, x64, F.e);
+void launch_accumulate(const Launch& L, const Fields& F, float* x_hi, float* x_lo, cudaStream_t s) {
+    k_accumulate<<<L.grid, L.block, 0, s>>>(L.g, x_hi, x_lo, F.e);
 }
-void launch_correct(const Launch& L, const Fields& F, const double* phi, const float* us, const float* vs,
-                    const float* ws, float* uo, float* vo, float* wo, float* po, float dt, cudaStream_t s) {
-    const double p_scale = (double)F.rho_l / (double)dt;
-    k_correct<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.h, F.rho_l, F.rho_air, p_scale, F.cls, F.alpha, F.gtop, phi,
-                                         us, vs, ws, uo, vo, wo, po);
+void launch_to_double(const float* hi, const float* lo, double* out, long long n, cudaStream_t s) {
+    k_to_double<<<152 * 4, 256, 0, s>>>(hi, lo, out, n);
+}
+void launch_correct(const Launch& L, const Fields& F, const float* ph, const float* pl, const float* us,
+                    const float* vs, const float* ws, float* uo, float* vo, float* wo, float* po, float dt,
+                    cudaStream_t s) {
+    const float p_scale = (float)((double)F.rho_l / (double)dt);
+    k_correct<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.h, F.rho_l, F.rho_air, p_scale, F.cls, F.alpha, F.gtop, ph,
+                                         pl, us, vs, ws, uo, vo, wo, po);
 }
 void launch_divergence(const Launch& L, const Fields& F, const float* u, const float* v, const float* w,
                        cudaStream_t s) {
@@ -808,13 +843,13 @@ void launch_scale(const Launch& L, const float* in, float* out, float scale, con
 }
 void launch_adj_rhs(const Launch& L, const Fields& F, const float* gu, const float* gv, const float* gw,
                     const float* gp, float dt, cudaStream_t s) {
-    const double p_scale = (double)F.rho_l / (double)dt;
+    const float p_scale = (float)((double)F.rho_l / (double)dt);
     k_adj_rhs<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.h, F.rho_l, F.rho_air, p_scale, F.cls, F.alpha, F.gtop, gu,
-                                         gv, gw, gp, F.b64, F.sc, F.partials, L.nblocks);
+                                         gv, gw, gp, F.b_hi, F.b_lo, F.sc, F.partials, L.nblocks);
 }
-void launch_adj_correct(const Launch& L, const Fields& F, const double* psi, const float* gu, const float* gv,
-                        const float* gw, float* ou, float* ov, float* ow, cudaStream_t s) {
-    k_adj_correct<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.h, F.cls, psi, gu, gv, gw, ou, ov, ow);
+void launch_adj_correct(const Launch& L, const Fields& F, const float* psi_hi, const float* psi_lo, const float* gu,
+                        const float* gv, const float* gw, float* ou, float* ov, float* ow, cudaStream_t s) {
+    k_adj_correct<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.h, F.cls, psi_hi, psi_lo, gu, gv, gw, ou, ov, ow);
 }
 void launch_add_force(const Launch& L, const Fields& F, const float* u, const float* v, const float* w,
                       const float* fu, const float* fv, const float* fw, float dt, float* su, float* sv, float* sw,

@@ -22,8 +22,7 @@ struct Fields {
     void* coef_lo;     // FP16/BF16 copy (mixed precision) or nullptr
     int coef_lo_kind;  // 0 none, 1 fp16, 2 bf16
     float* gtop;
-    double* b64;
-    double* phi64;
+    float *b_hi, *b_lo;
     float *r, *z, *p, *q, *e;
     Scalars* sc;
     double* partials;
@@ -36,14 +35,16 @@ struct Fields {
 void launch_coefficients(const Launch& L, const Fields& F, cudaStream_t s);
 void launch_init_scalars(Scalars* sc, double tol2, double abs_floor, double inner_floor2, cudaStream_t s);
 void launch_rhs(const Launch& L, const Fields& F, const float* u, const float* v, const float* w, cudaStream_t s);
-void launch_residual64(const Launch& L, const Fields& F, const double* x64, cudaStream_t s);
+void launch_residual(const Launch& L, const Fields& F, const float* x_hi, const float* x_lo, cudaStream_t s);
 void launch_spmv_pq(const Launch& L, const Fields& F, cudaStream_t s);
 void launch_update(const Launch& L, const Fields& F, cudaStream_t s);
 void launch_dot_rz(const Launch& L, const Fields& F, int init, cudaStream_t s);
 void launch_search(const Launch& L, const Fields& F, cudaStream_t s);
-void launch_accumulate(const Launch& L, const Fields& F, double* x64, cudaStream_t s);
-void launch_correct(const Launch& L, const Fields& F, const double* phi, const float* us, const float* vs,
-                    const float* ws, float* uo, float* vo, float* wo, float* po, float dt, cudaStream_t s);
+void launch_accumulate(const Launch& L, const Fields& F, float* x_hi, float* x_lo, cudaStream_t s);
+void launch_to_double(const float* hi, const float* lo, double* out, long long n, cudaStream_t s);
+void launch_correct(const Launch& L, const Fields& F, const float* ph, const float* pl, const float* us,
+                    const float* vs, const float* ws, float* uo, float* vo, float* wo, float* po, float dt,
+                    cudaStream_t s);
 void launch_divergence(const Launch& L, const Fields& F, const float* u, const float* v, const float* w,
                        cudaStream_t s);
 void launch_apply(const Launch& L, const Fields& F, const float* x, float* y, cudaStream_t s);
@@ -52,8 +53,8 @@ void launch_scale(const Launch& L, const float* in, float* out, float scale, con
 // adjoint and chain
 void launch_adj_rhs(const Launch& L, const Fields& F, const float* gu, const float* gv, const float* gw,
                     const float* gp, float dt, cudaStream_t s);
-void launch_adj_correct(const Launch& L, const Fields& F, const double* psi, const float* gu, const float* gv,
-                        const float* gw, float* ou, float* ov, float* ow, cudaStream_t s);
+void launch_adj_correct(const Launch& L, const Fields& F, const float* psi_hi, const float* psi_lo, const float* gu,
+                        const float* gv, const float* gw, float* ou, float* ov, float* ow, cudaStream_t s);
 void launch_add_force(const Launch& L, const Fields& F, const float* u, const float* v, const float* w,
                       const float* fu, const float* fv, const float* fw, float dt, float* su, float* sv, float* sw,
                       cudaStream_t s);
