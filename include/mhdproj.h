@@ -216,6 +216,24 @@ typedef struct {
 } mhdproj_kernel_time;
 int mhdproj_profile_kernels(mhdproj_ctx *ctx, int reps, mhdproj_kernel_time *out, int max_out, int *count);
 
+/* Divergence statistics of a face-velocity field that allocate nothing.
+ * No counterpart in the reference: it exists for callers that cannot allocate
+ * device memory while they run (a time loop that reserved its whole budget at
+ * start-up, or a diagnostics hook on another library's stream with no
+ * projection context).  Computes out[0] = max |div u| and out[1] = RMS div u
+ * (1/s) over the non-solid cells, div u = sum of (u_high - u_low) / h, from
+ * device arrays solid (nx*ny*nz) and u, v, w (the face layout above), on the
+ * given cudaStream_t (NULL: legacy default stream); returns when the result is
+ * on the host.  The reduction scratch is a fixed 96 KiB array in the library's
+ * device image (kept by every GPU that loads the library until exit), so an
+ * x-y plane may hold at most 4096 tiles of 32x8 cells (nx*ny up to about one
+ * million); larger planes return MHDPROJ_ERR_INVALID with a message from
+ * mhdproj_last_error(NULL).  All calls on a device share the array: calls
+ * that overlap on the GPU race.  The first call on each device looks up the
+ * array's device address; make it before any stream capture. */
+int mhdproj_divergence_noalloc(const mhdproj_grid *grid, const uint8_t *solid, const float *u, const float *v,
+                               const float *w, double *out, void *stream);
+
 /* Host utilities, mirroring src/fluid/multigrid.rs:25-65 and src/fluid/mod.rs:1447-1493. */
 /* Aggregation hierarchy: halve (ceil) until every dimension is <= 4.  Returns
  * 0 and the level count / coarse-cell total, or MHDPROJ_ERR_INVALID for zero,

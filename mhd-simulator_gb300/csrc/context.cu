@@ -20,6 +20,11 @@
 using namespace mhdproj;
 
 static thread_local std::string g_create_error;
+namespace mhdproj {
+// Message for entry points that run without a context (read with
+// mhdproj_last_error(NULL)).
+void set_global_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace mhdproj
 
 struct mhdproj_ctx {
     mhdproj_grid grid{};

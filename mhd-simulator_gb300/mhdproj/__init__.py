@@ -107,6 +107,7 @@ def load():
     L.mhdproj_copy_potential.argtypes = [_vp, _vp]
     L.mhdproj_copy_topology.argtypes = [_vp, _vp, C.POINTER(C.c_uint32)]
     L.mhdproj_profile_kernels.argtypes = [_vp, C.c_int, C.POINTER(KernelTime), C.c_int, C.POINTER(C.c_int)]
+    L.mhdproj_divergence_noalloc.argtypes = [C.POINTER(Grid), _vp, _vp, _vp, _vp, C.POINTER(C.c_double), _vp]
     L.mhdproj_hierarchy.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)]
     L.mhdproj_anchors.argtypes = [_vp, C.POINTER(C.c_uint32), C.c_uint32]
     L.mhdproj_anchors.restype = C.c_uint32
@@ -119,8 +120,25 @@ EXPORTED = [
     "mhdproj_set_coefficients", "mhdproj_set_phase_drag", "mhdproj_project", "mhdproj_project_host",
     "mhdproj_project_vjp", "mhdproj_chain_forward", "mhdproj_chain_backward", "mhdproj_apply_operator",
     "mhdproj_apply_preconditioner", "mhdproj_copy_coefficients", "mhdproj_copy_potential", "mhdproj_copy_topology",
-    "mhdproj_hierarchy", "mhdproj_anchors", "mhdproj_profile_kernels",
+    "mhdproj_hierarchy", "mhdproj_anchors", "mhdproj_profile_kernels", "mhdproj_divergence_noalloc",
 ]
+
+
+def divergence_noalloc(dims, h, solid, u, v, w, stream=None):
+    """Max and RMS divergence (1/s) of a face field over non-solid cells, with
+    no device allocation (mhdproj_divergence_noalloc)."""
+    import torch
+
+    L = load()
+    g = Grid(int(dims[0]), int(dims[1]), int(dims[2]), float(h), 0, 0)
+    out = (C.c_double * 2)()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    s.synchronize()
+    rc = L.mhdproj_divergence_noalloc(C.byref(g), _ptr(solid), _ptr(u), _ptr(v), _ptr(w), out,
+                                      C.c_void_p(s.cuda_stream))
+    if rc:
+        raise ProjectionError(rc, L.mhdproj_last_error(None).decode())
+    return out[0], out[1]
 
 
 def hierarchy(dims4):
