@@ -53,6 +53,37 @@ __device__ __forceinline__ int wrap_or_neg(int c, int n, bool periodic) {
     return c;
 }
 
+// A thread's (x, y) column for kernels that march along z: neighbour offsets
+// are computed once; an absent neighbour (closed boundary) gets offset 0 so
+// every load stays in bounds, and its coefficient is zero by construction.
+struct Column {
+    int i0, sxy, nz;
+    int dxm, dxp, dym, dyp;
+    bool hxp, hyp, pz;
+    __device__ __forceinline__ Column(const Grid3& g, int x, int y) {
+        sxy = g.nx * g.ny;
+        nz = g.nz;
+        i0 = x + g.nx * y;
+        const bool px = g.periodic & 1, py = g.periodic & 2;
+        pz = (g.periodic & 4) != 0;
+        dxm = x > 0 ? -1 : (px ? g.nx - 1 : 0);
+        dxp = x + 1 < g.nx ? 1 : (px ? -(g.nx - 1) : 0);
+        hxp = x + 1 < g.nx || px;
+        dym = y > 0 ? -g.nx : (py ? g.nx * (g.ny - 1) : 0);
+        dyp = y + 1 < g.ny ? g.nx : (py ? -g.nx * (g.ny - 1) : 0);
+        hyp = y + 1 < g.ny || py;
+    }
+    __device__ __forceinline__ int at(int z) const { return i0 + z * sxy; }
+    __device__ __forceinline__ bool zexists(int z) const { return pz || (z >= 0 && z < nz); }
+    // index of plane z (wrapped when periodic, clamped otherwise)
+    __device__ __forceinline__ int zat(int z) const {
+        int w = z;
+        if (w < 0) w = pz ? w + nz : 0;
+        else if (w >= nz) w = pz ? w - nz : nz - 1;
+        return at(w);
+    }
+};
+
 // ------------------------------------------------ rounding-explicit FP32
 // The mobility is computed with an operation order shared with the CPU
 // oracle; explicit intrinsics stop the compiler from fusing multiply-adds.

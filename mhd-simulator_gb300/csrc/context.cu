@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -63,6 +64,7 @@ struct mhdproj_ctx {
     double* partials = nullptr;
     MGPlan mg{};
     bool use_mg = false;
+    bool staged = true;  // finest-level stencils through shared-memory staging
     cudaGraphExec_t it_graph = nullptr;
     bool graph_failed = false;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_sync = nullptr;
@@ -180,6 +182,7 @@ static int build_levels(mhdproj_ctx* ctx) {
     P.precision = ctx->opt.precision;
     P.sc = ctx->sc;
     P.prolong = 2.0f;
+    P.staged = ctx->staged;
     int d[3] = {(int)ctx->grid.nx, (int)ctx->grid.ny, (int)ctx->grid.nz};
     const int per = (int)ctx->grid.periodic;
     const size_t vbytes = P.precision == 0 ? 4 : 2;
@@ -208,7 +211,9 @@ static int build_levels(mhdproj_ctx* ctx) {
             if (L.odd_periodic) CK(dalloc(ctx, (char**)&L.tmp, n * vbytes));
         }
         P.nlevels++;
-        if (d[0] <= 4 && d[1] <= 4 && d[2] <= 4) break;
+        // Coarsen until every extent is at most 2: the coarsest operator
+        // (<= 8 cells) is inverted exactly once per coefficient set.
+        if (d[0] <= 2 && d[1] <= 2 && d[2] <= 2) break;
         if (P.nlevels >= 31) return fail(ctx, MHDPROJ_ERR_INVALID, "multigrid hierarchy too deep");
         for (int a = 0; a < 3; a++) d[a] = (d[a] + 1) / 2;
     }
@@ -308,6 +313,11 @@ extern "C" int mhdproj_create(const mhdproj_grid* grid, const mhdproj_options* o
              CK(dalloc(ctx, &ctx->q, n * 4));
              CK(dalloc(ctx, &ctx->e, n * 4));
              ctx->use_mg = ctx->opt.preconditioner != MHDPROJ_PRECOND_JACOBI;
+             {
+                 const char* ev = getenv("MHDPROJ_STAGED");
+                 if (ev && ev[0] == '0') ctx->staged = false;
+             }
+             CK(staged_prepare_attributes());
              if (ctx->use_mg) {
                  int r = build_levels(ctx);
                  if (r) return r;
@@ -458,7 +468,8 @@ static void enqueue_precondition(mhdproj_ctx* ctx) {
 }
 static void enqueue_iteration_body(mhdproj_ctx* ctx) {
     Fields F = fields(ctx);
-    launch_spmv_pq(ctx->L, F, ctx->stream);
+    if (ctx->staged) launch_spmv_staged(ctx->L, F, ctx->stream);
+    else launch_spmv_pq(ctx->L, F, ctx->stream);
     launch_update(ctx->L, F, ctx->stream);
     enqueue_precondition(ctx);
     launch_dot_rz(ctx->L, F, 0, ctx->stream);
@@ -940,7 +951,10 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
         CK(cudaEventRecord(ctx->ev_a, s));
         for (int r = 0; r < reps; r++) {
             switch (it.kind) {
-                case 0: launch_spmv_pq(ctx->L, F, s); break;
+                case 0:
+                    if (ctx->staged) launch_spmv_staged(ctx->L, F, s);
+                    else launch_spmv_pq(ctx->L, F, s);
+                    break;
                 case 1: launch_update(ctx->L, F, s); break;
                 case 2: mg_fine_smooth(ctx->mg, r & 1, s); break;
                 case 3: mg_fine_restrict(ctx->mg, s); break;

@@ -250,19 +250,50 @@ __global__ void __launch_bounds__(TILE_THREADS) k_residual(Grid3 g, const float4
 }
 
 // --------------------------------------------------------- CG kernels
+// q = A p and p.q.  Each thread marches its column along z keeping p at
+// z-1, z, z+1 and the coefficient records at z, z+1 in registers and loading
+// plane z+2 one step ahead; in-plane neighbours come from L1.
 __global__ void __launch_bounds__(TILE_THREADS) k_spmv_pq(Grid3 g, const float4* __restrict__ coef,
                                                           const float* __restrict__ p, float* __restrict__ q,
                                                           Scalars* sc, double* partials, int nblocks) {
     if (sc->converged) return;
     __shared__ double sh[8 * 1];
     Acc acc;
-    TILE_BEGIN(g) {
-        if (!in_xy) continue;
-        const int i = cell_index(g, x, y, z);
-        const Nbr nb = neighbours(g, x, y, z);
-        const float qi = apply_cell<float>(g, coef, p, i, nb);
-        q[i] = qi;
-        acc.add_prod(p[i], qi);
+    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
+    const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
+    if (x < g.nx && y < g.ny) {
+        const Column C(g, x, y);
+        const float* coefs = reinterpret_cast<const float*>(coef);
+        const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        float pm = p[C.zat(z0 - 1)], pc = p[C.at(z0)], pn = p[C.zat(z0 + 1)];
+        float4 cc = coef[C.at(z0)];
+        float4 cn = C.zexists(z0 + 1) ? coef[C.zat(z0 + 1)] : zero4;
+        for (int z = z0; z < z1; z++) {
+            const int i = C.at(z);
+            float pnn = 0.f;
+            float4 cnn = zero4;
+            if (z + 1 < z1) {
+                pnn = p[C.zat(z + 2)];
+                if (C.zexists(z + 2)) cnn = coef[C.zat(z + 2)];
+            }
+            const float pxm = p[i + C.dxm], pxp = p[i + C.dxp], pym = p[i + C.dym], pyp = p[i + C.dyp];
+            const float bxh = C.hxp ? coefs[4 * (i + C.dxp)] : 0.f;
+            const float byh = C.hyp ? coefs[4 * (i + C.dyp) + 1] : 0.f;
+            float qv = cc.w * pc;
+            qv = fmaf(cc.x, pc - pxm, qv);
+            qv = fmaf(bxh, pc - pxp, qv);
+            qv = fmaf(cc.y, pc - pym, qv);
+            qv = fmaf(byh, pc - pyp, qv);
+            qv = fmaf(cc.z, pc - pm, qv);
+            qv = fmaf(cn.z, pc - pn, qv);
+            q[i] = qv;
+            acc.add_prod(pc, qv);
+            pm = pc;
+            pc = pn;
+            pn = pnn;
+            cc = cn;
+            cn = cnn;
+        }
     }
     double v1[1] = {acc.total()};
     block_sum<1>(v1, sh);
@@ -286,17 +317,47 @@ __global__ void __launch_bounds__(TILE_THREADS) k_spmv_pq(Grid3 g, const float4*
     }
 }
 
-__global__ void __launch_bounds__(TILE_THREADS) k_update(Grid3 g, float* __restrict__ e, float* __restrict__ r,
-                                                         const float* __restrict__ p, const float* __restrict__ q,
-                                                         Scalars* sc, double* partials, int nblocks,
-                                                         long long n_active) {
+// Streaming kernels walk the column four planes at a time with all loads
+// issued before any store, so each thread keeps several requests in flight.
+#define STREAM_BEGIN(G)                                                             \
+    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y; \
+    const int z0 = blockIdx.z * (G).zper, z1 = min((G).nz, z0 + (G).zper);          \
+    const int sxy = (G).nx * (G).ny;                                                \
+    const bool inside = x < (G).nx && y < (G).ny;                                   \
+    const int base = x + (G).nx * y;
+
+// The vector updates and dot products are pure streams: flat grid-stride
+// loops over float4 chunks give long contiguous bursts (the column walk of the
+// stencil kernels would scatter 128-byte requests over many DRAM pages).
+constexpr int FLAT_BLOCKS = 152 * 8;
+
+__global__ void __launch_bounds__(256) k_update(long long n, float* __restrict__ e, float* __restrict__ r,
+                                                const float* __restrict__ p, const float* __restrict__ q, Scalars* sc,
+                                                double* partials, int nblocks, long long n_active) {
     if (sc->converged) return;
     __shared__ double sh[8 * 1];
     Acc acc;
     const float a = sc->alpha_f;
-    TILE_BEGIN(g) {
-        if (!in_xy) continue;
-        const int i = cell_index(g, x, y, z);
+    const long long n4 = n >> 2;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    float4* e4 = reinterpret_cast<float4*>(e);
+    float4* r4 = reinterpret_cast<float4*>(r);
+    const float4* p4 = reinterpret_cast<const float4*>(p);
+    const float4* q4 = reinterpret_cast<const float4*>(q);
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n4; k += stride) {
+        const float4 ev = e4[k], rv = r4[k], pv = p4[k], qv = q4[k];
+        const float4 en = make_float4(fmaf(a, pv.x, ev.x), fmaf(a, pv.y, ev.y), fmaf(a, pv.z, ev.z), fmaf(a, pv.w, ev.w));
+        const float4 rn = make_float4(fmaf(-a, qv.x, rv.x), fmaf(-a, qv.y, rv.y), fmaf(-a, qv.z, rv.z),
+                                      fmaf(-a, qv.w, rv.w));
+        e4[k] = en;
+        r4[k] = rn;
+        acc.add_prod(rn.x, rn.x);
+        acc.add_prod(rn.y, rn.y);
+        acc.add_prod(rn.z, rn.z);
+        acc.add_prod(rn.w, rn.w);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (n & 3)) {
+        const long long i = (n4 << 2) + threadIdx.x;
         e[i] = fmaf(a, p[i], e[i]);
         const float ri = fmaf(-a, q[i], r[i]);
         r[i] = ri;
@@ -307,7 +368,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_update(Grid3 g, float* __restr
     if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[3])) {
         double tot[1];
         finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[3]);
-        if (threadIdx.x == 0 && threadIdx.y == 0) {
+        if (threadIdx.x == 0) {
             const double rr = tot[0];
             sc->rr = rr;
             sc->iterations += 1;
@@ -324,16 +385,29 @@ __global__ void __launch_bounds__(TILE_THREADS) k_update(Grid3 g, float* __restr
 }
 
 // rz = r . z / sigma; init: p = z / sigma.
-__global__ void __launch_bounds__(TILE_THREADS) k_dot_rz(Grid3 g, const float* __restrict__ r,
-                                                         const float* __restrict__ zv, float* __restrict__ p, int init,
-                                                         Scalars* sc, double* partials, int nblocks) {
+__global__ void __launch_bounds__(256) k_dot_rz(long long n, const float* __restrict__ r, const float* __restrict__ zv,
+                                                float* __restrict__ p, int init, Scalars* sc, double* partials,
+                                                int nblocks) {
     if (sc->converged) return;
     __shared__ double sh[8 * 1];
     Acc acc;
     const float is = sc->inv_sigma;
-    TILE_BEGIN(g) {
-        if (!in_xy) continue;
-        const int i = cell_index(g, x, y, z);
+    const long long n4 = n >> 2;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const float4* r4 = reinterpret_cast<const float4*>(r);
+    const float4* z4 = reinterpret_cast<const float4*>(zv);
+    float4* p4 = reinterpret_cast<float4*>(p);
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n4; k += stride) {
+        const float4 rv = r4[k], zz = z4[k];
+        const float4 zs = make_float4(zz.x * is, zz.y * is, zz.z * is, zz.w * is);
+        if (init) p4[k] = zs;
+        acc.add_prod(rv.x, zs.x);
+        acc.add_prod(rv.y, zs.y);
+        acc.add_prod(rv.z, zs.z);
+        acc.add_prod(rv.w, zs.w);
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (n & 3)) {
+        const long long i = (n4 << 2) + threadIdx.x;
         const float zi = zv[i] * is;
         if (init) p[i] = zi;
         acc.add_prod(r[i], zi);
@@ -343,7 +417,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_dot_rz(Grid3 g, const float* _
     if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[4])) {
         double tot[1];
         finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[4]);
-        if (threadIdx.x == 0 && threadIdx.y == 0) {
+        if (threadIdx.x == 0) {
             const double rz = tot[0];
             if (!isfinite(rz)) {
                 sc->nonfinite = 1;
@@ -362,13 +436,21 @@ __global__ void __launch_bounds__(TILE_THREADS) k_dot_rz(Grid3 g, const float* _
     }
 }
 
-__global__ void __launch_bounds__(TILE_THREADS) k_search(Grid3 g, const float* __restrict__ zv, float* __restrict__ p,
-                                                         const Scalars* sc) {
+__global__ void __launch_bounds__(256) k_search(long long n, const float* __restrict__ zv, float* __restrict__ p,
+                                                const Scalars* sc) {
     if (sc->converged) return;
     const float is = sc->inv_sigma, bt = sc->beta_f;
-    TILE_BEGIN(g) {
-        if (!in_xy) continue;
-        const int i = cell_index(g, x, y, z);
+    const long long n4 = n >> 2;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const float4* z4 = reinterpret_cast<const float4*>(zv);
+    float4* p4 = reinterpret_cast<float4*>(p);
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n4; k += stride) {
+        const float4 zz = z4[k], pv = p4[k];
+        p4[k] = make_float4(fmaf(bt, pv.x, zz.x * is), fmaf(bt, pv.y, zz.y * is), fmaf(bt, pv.z, zz.z * is),
+                            fmaf(bt, pv.w, zz.w * is));
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (n & 3)) {
+        const long long i = (n4 << 2) + threadIdx.x;
         p[i] = fmaf(bt, p[i], zv[i] * is);
     }
 }
@@ -776,6 +858,7 @@ Launch tile_launch(int nx, int ny, int nz, int periodic, int target_blocks) {
     if (zc > nz) zc = nz;
     if (zc < 1) zc = 1;
     int zper = (nz + zc - 1) / zc;
+    if ((zper & 1) && zper < nz) zper += 1;  // even runs: restriction pairs planes within a block
     zc = (nz + zper - 1) / zper;
     while ((long long)tiles * zc > MAX_REDUCE_BLOCKS && zper < nz) {
         zper *= 2;
@@ -809,14 +892,23 @@ void launch_residual(const Launch& L, const Fields& F, const float* x_hi, const 
 void launch_spmv_pq(const Launch& L, const Fields& F, cudaStream_t s) {
     k_spmv_pq<<<L.grid, L.block, 0, s>>>(L.g, F.coef, F.p, F.q, F.sc, F.partials, L.nblocks);
 }
+static int flat_blocks(long long n) {
+    const long long want = (n / 4 + 255) / 256;
+    return (int)(want < 1 ? 1 : (want < FLAT_BLOCKS ? want : FLAT_BLOCKS));
+}
 void launch_update(const Launch& L, const Fields& F, cudaStream_t s) {
-    k_update<<<L.grid, L.block, 0, s>>>(L.g, F.e, F.r, F.p, F.q, F.sc, F.partials, L.nblocks, F.n_active);
+    const long long n = L.g.n();
+    const int nb = flat_blocks(n);
+    k_update<<<nb, 256, 0, s>>>(n, F.e, F.r, F.p, F.q, F.sc, F.partials, nb, F.n_active);
 }
 void launch_dot_rz(const Launch& L, const Fields& F, int init, cudaStream_t s) {
-    k_dot_rz<<<L.grid, L.block, 0, s>>>(L.g, F.r, F.z, F.p, init, F.sc, F.partials, L.nblocks);
+    const long long n = L.g.n();
+    const int nb = flat_blocks(n);
+    k_dot_rz<<<nb, 256, 0, s>>>(n, F.r, F.z, F.p, init, F.sc, F.partials, nb);
 }
 void launch_search(const Launch& L, const Fields& F, cudaStream_t s) {
-    k_search<<<L.grid, L.block, 0, s>>>(L.g, F.z, F.p, F.sc);
+    const long long n = L.g.n();
+    k_search<<<flat_blocks(n), 256, 0, s>>>(n, F.z, F.p, F.sc);
 }
 void launch_accumulate(const Launch& L, const Fields& F, float* x_hi, float* x_lo, cudaStream_t s) {
     k_accumulate<<<L.grid, L.block, 0, s>>>(L.g, x_hi, x_lo, F.e);

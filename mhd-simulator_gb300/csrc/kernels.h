@@ -62,6 +62,14 @@ void launch_force_grad(const Launch& L, const Fields& F, const float* lu, const 
                        double* gu, double* gv, double* gw, cudaStream_t s);
 void launch_outlet_objective(const Launch& L, const Fields& F, const float* w, float* seed_w, cudaStream_t s);
 
+// ---- finest-level kernels with shared-memory plane staging (fine_kernels.cu)
+void launch_spmv_staged(const Launch& L, const Fields& F, cudaStream_t s);
+void launch_smooth_staged(int ck, const Launch& L, const void* coef, const float* r, float* e, float* tmp, int color,
+                          bool zero, bool out_of_place, const Scalars* sc, cudaStream_t s);
+void launch_restrict_staged(int ck, const Launch& L, const Grid3& gc, const void* coef, const float* r, const float* e,
+                            void* rc, const Scalars* sc, cudaStream_t s);
+cudaError_t staged_prepare_attributes();
+
 // ---- multigrid (mg_kernels.cu)
 struct MGLevel {
     Launch L;
@@ -80,6 +88,7 @@ struct MGPlan {
     int m;
     float prolong;  // coarse-correction weight
     Scalars* sc;
+    bool staged;    // finest level through the shared-memory staged kernels
 };
 void mg_build(const MGPlan& P, cudaStream_t s);
 // single fine-level stages, for measurement

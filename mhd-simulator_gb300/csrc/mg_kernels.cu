@@ -10,8 +10,9 @@
 //   prolongation          e_l    += w P e_{l+1}          (w = 2 by default)
 // which is a coarse correction of w P (P^T A P)^-1 P^T.  Smoothing is one
 // red-black Gauss-Seidel sweep before (red, black) and after (black, red) the
-// coarse correction, and the coarsest level (<= 64 cells) is solved exactly
-// with a dense inverse, so the V-cycle is a fixed symmetric operator.
+// coarse correction, and the coarsest level (every extent <= 2, at most 8
+// cells) is solved exactly with a dense inverse, so the V-cycle is a fixed
+// symmetric operator.
 // Level fields (coefficients and vectors of levels >= 1, the fine smoother's
 // coefficients) are FP32, FP16 or BF16; arithmetic is FP32.
 #include "kernels.h"
@@ -77,32 +78,95 @@ __device__ __forceinline__ float neighbour_sum(const Stencil& s, const VT* e) {
     return acc;
 }
 
+template <int CK> __device__ __forceinline__ float ldc_x(const void* p, int i);
+template <> __device__ __forceinline__ float ldc_x<0>(const void* p, int i) {
+    return __ldg(reinterpret_cast<const float*>(p) + 4 * i);
+}
+template <> __device__ __forceinline__ float ldc_x<1>(const void* p, int i) {
+    return __half2float(__ldg(reinterpret_cast<const __half*>(p) + 4 * i));
+}
+template <> __device__ __forceinline__ float ldc_x<2>(const void* p, int i) {
+    return __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(p) + 4 * i));
+}
+template <int CK> __device__ __forceinline__ float ldc_y(const void* p, int i);
+template <> __device__ __forceinline__ float ldc_y<0>(const void* p, int i) {
+    return __ldg(reinterpret_cast<const float*>(p) + 4 * i + 1);
+}
+template <> __device__ __forceinline__ float ldc_y<1>(const void* p, int i) {
+    return __half2float(__ldg(reinterpret_cast<const __half*>(p) + 4 * i + 1));
+}
+template <> __device__ __forceinline__ float ldc_y<2>(const void* p, int i) {
+    return __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(p) + 4 * i + 1));
+}
+
 // One red-black Gauss-Seidel half-step on `color` cells.  ZERO: the first
 // half-step from a zero correction (e = rhs/diag on color cells, 0 elsewhere).
 // OUT: write color cells to `out` instead of in place (levels whose periodic
-// extents are odd have same-colour neighbours across the wrap).
+// extents are odd have same-colour neighbours across the wrap).  Each thread
+// marches its column along z with the coefficient records at z, z+1 and the
+// corrections at z-1, z+1 in registers, loading plane z+2 one step ahead.
 template <int CK, class VT, bool FINE, bool ZERO, bool OUT>
 __global__ void __launch_bounds__(TILE_THREADS) k_smooth(Grid3 g, const void* __restrict__ coef,
                                                          const VT* __restrict__ r, VT* e, VT* out, int color,
                                                          const Scalars* sc) {
     if (sc->converged) return;
     const float sigma = FINE ? sc->sigma : 1.0f;
-    TILE_BEGIN(g) {
-        if (!in_xy) continue;
-        const int i = x + g.nx * (y + g.ny * z);
-        if (((x + y + z) & 1) != color) {
-            if (ZERO) e[i] = from_f<VT>(0.0f);
-            continue;
+    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
+    const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
+    if (x >= g.nx || y >= g.ny) return;
+    const Column C(g, x, y);
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 cc = ldc<CK>(coef, C.at(z0));
+    float4 cn = C.zexists(z0 + 1) ? ldc<CK>(coef, C.zat(z0 + 1)) : zero4;
+    float em = 0.f, ec = 0.f, en = 0.f;
+    if (!ZERO) {
+        em = to_f(e[C.zat(z0 - 1)]);
+        ec = to_f(e[C.at(z0)]);
+        en = to_f(e[C.zat(z0 + 1)]);
+    }
+    for (int z = z0; z < z1; z++) {
+        const int i = C.at(z);
+        float4 cnn = zero4;
+        float enn = 0.f;
+        if (z + 1 < z1) {
+            if (C.zexists(z + 2)) cnn = ldc<CK>(coef, C.zat(z + 2));
+            if (!ZERO) enn = to_f(e[C.zat(z + 2)]);
         }
-        const Stencil s = stencil<CK>(g, coef, x, y, z);
-        float val = 0.0f;
-        if (s.diag > 0.0f) {
-            const float rhs = sigma * to_f(r[i]);
-            if (ZERO) val = rhs / s.diag;
-            else val = (rhs + neighbour_sum<VT>(s, e)) / s.diag;
+        if (((x + y + z) & 1) == color) {
+            const float bxh = C.hxp ? ldc_x<CK>(coef, i + C.dxp) : 0.f;
+            const float byh = C.hyp ? ldc_y<CK>(coef, i + C.dyp) : 0.f;
+            const float d = ((cc.x + bxh) + (cc.y + byh)) + ((cc.z + cn.z) + cc.w);
+            float val = 0.f;
+            if (d > 0.f) {
+                const float rhs = sigma * to_f(r[i]);
+                if (ZERO) {
+                    val = rhs / d;
+                } else {
+                    float acc = rhs;
+                    acc = fmaf(cc.x, to_f(e[i + C.dxm]), acc);
+                    acc = fmaf(bxh, to_f(e[i + C.dxp]), acc);
+                    acc = fmaf(cc.y, to_f(e[i + C.dym]), acc);
+                    acc = fmaf(byh, to_f(e[i + C.dyp]), acc);
+                    acc = fmaf(cc.z, em, acc);
+                    acc = fmaf(cn.z, en, acc);
+                    val = acc / d;
+                }
+            }
+            if (OUT) out[i] = from_f<VT>(val);
+            else e[i] = from_f<VT>(val);
+        } else if (ZERO) {
+            e[i] = from_f<VT>(0.0f);
         }
-        if (OUT) out[i] = from_f<VT>(val);
-        else e[i] = from_f<VT>(val);
+        cc = cn;
+        cn = cnn;
+        if (!ZERO) {
+            // Carry the values read before this half-step: a cell of this
+            // colour is never the z-neighbour of another cell of this colour,
+            // so its old value is only used when it is not updated.
+            em = ec;
+            ec = en;
+            en = enn;
+        }
     }
 }
 template <class VT>
@@ -117,31 +181,71 @@ __global__ void __launch_bounds__(TILE_THREADS) k_copy_color(Grid3 g, const VT* 
     }
 }
 
-// Residual of the children and restriction: rc[Q] = 1/4 sum (rhs - A e).
+// Residual of the children and restriction: rc[Q] = 1/4 sum (rhs - A e),
+// launched over the fine grid with an even z run per block.  A thread forms
+// the residual of its cell for two planes (the z pair), adds its x partner by
+// a warp shuffle and its y partner through shared memory; the thread at the
+// even (x, y) corner writes the coarse value.
 template <int CK, class VTf, bool FINE, class VTc>
 __global__ void __launch_bounds__(TILE_THREADS) k_restrict(Grid3 gf, Grid3 gc, const void* __restrict__ coef,
                                                            const VTf* __restrict__ r, const VTf* __restrict__ e,
                                                            VTc* __restrict__ rc, const Scalars* sc) {
     if (sc->converged) return;
+    __shared__ float ypart[TY][TX];
     const float sigma = FINE ? sc->sigma : 1.0f;
-    TILE_BEGIN(gc) {
-        if (!in_xy) continue;
-        float sum = 0.0f;
+    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
+    const int z0 = blockIdx.z * gf.zper, z1 = min(gf.nz, z0 + gf.zper);
+    const bool inside = x < gf.nx && y < gf.ny;
+    const Column C(gf, inside ? x : 0, inside ? y : 0);
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 cc = zero4, cn = zero4;
+    float em = 0.f, ec = 0.f, en = 0.f;
+    if (inside && z0 < z1) {
+        cc = ldc<CK>(coef, C.at(z0));
+        cn = C.zexists(z0 + 1) ? ldc<CK>(coef, C.zat(z0 + 1)) : zero4;
+        em = to_f(e[C.zat(z0 - 1)]);
+        ec = to_f(e[C.at(z0)]);
+        en = to_f(e[C.zat(z0 + 1)]);
+    }
+    for (int z = z0; z < z1; z += 2) {
+        float part = 0.f;
 #pragma unroll
-        for (int dz = 0; dz < 2; dz++)
-#pragma unroll
-            for (int dy = 0; dy < 2; dy++)
-#pragma unroll
-                for (int dx = 0; dx < 2; dx++) {
-                    const int cx = 2 * x + dx, cy = 2 * y + dy, cz = 2 * z + dz;
-                    if (cx >= gf.nx || cy >= gf.ny || cz >= gf.nz) continue;
-                    const int ci = cx + gf.nx * (cy + gf.ny * cz);
-                    const Stencil s = stencil<CK>(gf, coef, cx, cy, cz);
-                    const float ec = to_f(e[ci]);
-                    const float res = sigma * to_f(r[ci]) - (s.diag * ec - neighbour_sum<VTf>(s, e));
-                    sum += res;
+        for (int k = 0; k < 2; k++) {
+            const int zz = z + k;
+            if (inside && zz < z1) {
+                const int i = C.at(zz);
+                float4 cnn = zero4;
+                float enn = 0.f;
+                if (zz + 1 < z1) {
+                    if (C.zexists(zz + 2)) cnn = ldc<CK>(coef, C.zat(zz + 2));
+                    enn = to_f(e[C.zat(zz + 2)]);
                 }
-        rc[x + gc.nx * (y + gc.ny * z)] = from_f<VTc>(0.25f * sum);
+                const float bxh = C.hxp ? ldc_x<CK>(coef, i + C.dxp) : 0.f;
+                const float byh = C.hyp ? ldc_y<CK>(coef, i + C.dyp) : 0.f;
+                const float d = ((cc.x + bxh) + (cc.y + byh)) + ((cc.z + cn.z) + cc.w);
+                float nsum = 0.f;
+                nsum = fmaf(cc.x, to_f(e[i + C.dxm]), nsum);
+                nsum = fmaf(bxh, to_f(e[i + C.dxp]), nsum);
+                nsum = fmaf(cc.y, to_f(e[i + C.dym]), nsum);
+                nsum = fmaf(byh, to_f(e[i + C.dyp]), nsum);
+                nsum = fmaf(cc.z, em, nsum);
+                nsum = fmaf(cn.z, en, nsum);
+                part += sigma * to_f(r[i]) - (d * ec - nsum);
+                cc = cn;
+                cn = cnn;
+                em = ec;
+                ec = en;
+                en = enn;
+            }
+        }
+        part += __shfl_xor_sync(0xffffffffu, part, 1);
+        ypart[threadIdx.y][threadIdx.x] = part;
+        __syncthreads();
+        if (inside && !(threadIdx.x & 1) && !(threadIdx.y & 1)) {
+            const float tot = part + ypart[threadIdx.y + 1][threadIdx.x];
+            rc[(x >> 1) + gc.nx * ((y >> 1) + gc.ny * (z >> 1))] = from_f<VTc>(0.25f * tot);
+        }
+        __syncthreads();
     }
 }
 
@@ -149,11 +253,25 @@ template <class VTf, class VTc>
 __global__ void __launch_bounds__(TILE_THREADS) k_prolong(Grid3 gf, Grid3 gc, VTf* __restrict__ e,
                                                           const VTc* __restrict__ ec, float w, const Scalars* sc) {
     if (sc->converged) return;
-    TILE_BEGIN(gf) {
-        if (!in_xy) continue;
-        const int i = x + gf.nx * (y + gf.ny * z);
-        const int Q = (x >> 1) + gc.nx * ((y >> 1) + gc.ny * (z >> 1));
-        e[i] = from_f<VTf>(fmaf(w, to_f(ec[Q]), to_f(e[i])));
+    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
+    const int z0 = blockIdx.z * gf.zper, z1 = min(gf.nz, z0 + gf.zper);
+    if (x >= gf.nx || y >= gf.ny) return;
+    const int sxy = gf.nx * gf.ny, base = x + gf.nx * y;
+    const int cbase = (x >> 1) + gc.nx * (y >> 1), csxy = gc.nx * gc.ny;
+    int z = z0;
+    for (; z + 3 < z1; z += 4) {
+        float ev[4], cv[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            ev[k] = to_f(e[base + (z + k) * sxy]);
+            cv[k] = to_f(ec[cbase + ((z + k) >> 1) * csxy]);
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) e[base + (z + k) * sxy] = from_f<VTf>(fmaf(w, cv[k], ev[k]));
+    }
+    for (; z < z1; z++) {
+        const int i = base + z * sxy;
+        e[i] = from_f<VTf>(fmaf(w, to_f(ec[cbase + (z >> 1) * csxy]), to_f(e[i])));
     }
 }
 
@@ -284,6 +402,13 @@ template <int CK, class VT>
 static void enqueue_smooth(const MGPlan& P, int l, int color, bool zero, cudaStream_t s) {
     const MGLevel& L = P.lv[l];
     const void* coef = P.precision == 0 ? (const void*)L.coef32 : L.coef_lo;
+    if (l == 0 && P.staged) {
+        launch_smooth_staged(CK, L.L, coef, (const float*)L.r, (float*)L.e, (float*)L.tmp, color, zero,
+                             L.odd_periodic, P.sc, s);
+        if (!zero && L.odd_periodic)
+            k_copy_color<float><<<L.L.grid, L.L.block, 0, s>>>(L.L.g, (const float*)L.tmp, (float*)L.e, color, P.sc);
+        return;
+    }
     if (l == 0) {
         const float* r = (const float*)L.r;
         float* e = (float*)L.e;
@@ -317,11 +442,13 @@ static void vcycle_impl(const MGPlan& P, cudaStream_t s) {
         enqueue_smooth<CK, VT>(P, l, 1, false, s);
         const MGLevel &F = P.lv[l], &C = P.lv[l + 1];
         const void* coef = P.precision == 0 ? (const void*)F.coef32 : F.coef_lo;
-        if (l == 0)
-            k_restrict<CK, float, true, VT><<<C.L.grid, C.L.block, 0, s>>>(F.L.g, C.L.g, coef, (const float*)F.r,
+        if (l == 0 && P.staged)
+            launch_restrict_staged(CK, F.L, C.L.g, coef, (const float*)F.r, (const float*)F.e, C.r, P.sc, s);
+        else if (l == 0)
+            k_restrict<CK, float, true, VT><<<F.L.grid, F.L.block, 0, s>>>(F.L.g, C.L.g, coef, (const float*)F.r,
                                                                            (const float*)F.e, (VT*)C.r, P.sc);
         else
-            k_restrict<CK, VT, false, VT><<<C.L.grid, C.L.block, 0, s>>>(F.L.g, C.L.g, coef, (const VT*)F.r,
+            k_restrict<CK, VT, false, VT><<<F.L.grid, F.L.block, 0, s>>>(F.L.g, C.L.g, coef, (const VT*)F.r,
                                                                          (const VT*)F.e, (VT*)C.r, P.sc);
     }
     const MGLevel& K = P.lv[nl - 1];
@@ -348,7 +475,11 @@ template <int CK, class VT>
 static void fine_restrict_impl(const MGPlan& P, cudaStream_t s) {
     const MGLevel &F = P.lv[0], &C = P.lv[1];
     const void* coef = P.precision == 0 ? (const void*)F.coef32 : F.coef_lo;
-    k_restrict<CK, float, true, VT><<<C.L.grid, C.L.block, 0, s>>>(F.L.g, C.L.g, coef, (const float*)F.r,
+    if (P.staged) {
+        launch_restrict_staged(CK, F.L, C.L.g, coef, (const float*)F.r, (const float*)F.e, C.r, P.sc, s);
+        return;
+    }
+    k_restrict<CK, float, true, VT><<<F.L.grid, F.L.block, 0, s>>>(F.L.g, C.L.g, coef, (const float*)F.r,
                                                                    (const float*)F.e, (VT*)C.r, P.sc);
 }
 template <class VT>
