@@ -316,6 +316,7 @@ extern "C" int mhdproj_create(const mhdproj_grid* grid, const mhdproj_options* o
              {
                  const char* ev = getenv("MHDPROJ_STAGED");
                  if (ev && ev[0] == '0') ctx->staged = false;
+                 if (!staged_supported(ctx->L.g)) ctx->staged = false;
              }
              CK(staged_prepare_attributes());
              if (ctx->use_mg) {

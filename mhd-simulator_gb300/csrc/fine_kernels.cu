@@ -1,35 +1,43 @@
 // fine_kernels.cu -- the finest-level stencil kernels with shared-memory
 // plane staging.
 //
-// A block owns a 32 x 8 (x, y) tile and marches it along z.  A ring of four
-// plane slots in shared memory holds, per plane: the vector tile with a
-// one-cell halo (34 x 10), the coefficient records of the tile plus its +x
-// column and +y row (33 x 9; the high faces), and the right-hand side of the
-// tile.  Planes are fetched with cp.async four steps ahead of the plane being
-// computed, so every warp keeps global loads in flight while it computes from
-// shared memory; each value is read from HBM once per block (halo re-reads
-// hit L2).  Outside a closed boundary the copies are zero-filled, which gives
-// the zero coefficient of a wall face; periodic axes wrap the source index.
+// A block of 32 x 8 threads owns a 64 x 8 (x, y) tile -- each thread an
+// x-pair of cells -- and marches it along z.  A ring of plane slots in
+// shared memory holds, per plane: the vector tile with its halo (columns
+// x0-2 .. x0+65, rows y0-1 .. y0+8), the coefficient records of the tile plus
+// its +x column and +y row (the high faces), and the right-hand side of the
+// tile.  Planes are fetched with 8- and 16-byte cp.async two planes ahead of
+// the plane being computed, so loads stay in flight while warps compute from
+// shared memory, and every value is read from HBM once per block (halo
+// re-reads hit L2).  Outside a closed boundary copies are zero-filled, which
+// is the zero coefficient of a wall face; periodic axes wrap the source.
+// The kernels need an even nx (cell pairs never straddle the domain edge);
+// other grids use the per-cell kernels of mg_kernels.cu / gb300_kernels.cu.
 //
-// Red-black half-steps update the cells of one colour in place: a cell of
-// that colour is never a neighbour of another cell of the same colour (odd
-// periodic extents use the out-of-place variant), so the staged snapshots are
-// the values every update must read.
+// In a red-black half-step exactly one cell of each pair has the colour being
+// updated, so every lane works.  Cells of one colour are never neighbours of
+// each other (odd periodic extents use the out-of-place variant), so the
+// staged snapshots are exactly the values each update reads.
+#include <algorithm>
+#include <cmath>
+
 #include "kernels.h"
 
 namespace mhdproj {
 
 namespace {
-constexpr int EW = TX + 2, EH = TY + 2;  // vector tile with halo
-constexpr int CW = TX + 1, CH = TY + 1;  // coefficient tile (own + high neighbours)
-constexpr int PF = 4;     // prefetch distance in planes
-constexpr int NSLOT = 8;  // ring slots: planes z-1 .. z+PF
+constexpr int PX = 2 * TX;               // cells per tile row
+constexpr int EW = PX + 4, EH = TY + 2;  // vector tile: x0-2 .. x0+PX+1 (pairs)
+constexpr int EP = EW / 2;               // float2 pairs per vector row
+constexpr int CW = PX + 2, CH = TY + 1;  // coefficient tile: x0 .. x0+PX (+1 pad)
+// Ring depth: planes z-1 .. z+PF.  Two planes ahead with five blocks per SM
+// keeps about 100 KB of copies in flight per SM, twice what the HBM latency
+// needs, while leaving room for 40 resident warps.
+template <int CK> struct Depth {
+    static constexpr int NSLOT = 4;
+    static constexpr int PF = NSLOT - 2;
+};
 
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem, bool valid) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    const int n = valid ? 4 : 0;
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(n) : "memory");
-}
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem, bool valid) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
     const int n = valid ? 8 : 0;
@@ -41,6 +49,7 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool va
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(n) : "memory");
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PF>
 __device__ __forceinline__ void cp_wait_pf() { asm volatile("cp.async.wait_group %0;\n" ::"n"(PF - 1) : "memory"); }
 __device__ __forceinline__ void cp_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
@@ -75,21 +84,28 @@ __device__ __forceinline__ int axis_src(int c, int n, bool periodic, bool* ok) {
     return c;
 }
 
-template <int CK, bool WANT_E, bool WANT_R>
+template <int CK>
 struct Ring {
     using CT = typename CoefStore<CK>::T;
+    static constexpr int NSLOT = Depth<CK>::NSLOT;
     float e[NSLOT][EH][EW];
     CT c[NSLOT][CH][CW];
-    float r[NSLOT][TY][TX];
+    float r[NSLOT][TY][PX];
 };
 
-// A thread's share of the plane copies, resolved once per block: the
-// in-plane source offset and x-y validity of each element it copies.  A plane
-// fetch is then a handful of cp.async with one plane offset added.
+// A thread's share of the plane copies, resolved once per block.  Vector
+// tile: 10 rows x 34 float2 pairs; coefficients: 9 rows x 65 records (16-byte
+// FP32 records) or 9 rows x (32 record pairs + 1 record) (8-byte records);
+// right-hand side: 8 rows x 32 float2.
+template <int CK>
 struct Fetcher {
-    int eoff[2], coff[2], roff;   // in-plane source offsets
-    short eslot[2], cslot[2];     // destination element index within a slot
-    bool eok[2], cok[2], rok, ehas[2], chas[2];
+    static constexpr int NE = EH * EP;
+    static constexpr int CPR = (CK == 0) ? PX + 1 : TX + 1;
+    static constexpr int NC = CH * CPR;
+    int eoff[2], coff[3], roff;
+    short edst[2], cdst[3];
+    unsigned char csize[3];  // 0 none, 1 one record, 2 two records
+    bool eok[2], cok[3], rok;
     long long sxy;
     int nz;
     bool pz;
@@ -99,41 +115,49 @@ struct Fetcher {
         sxy = (long long)g.nx * g.ny;
         nz = g.nz;
         pz = (g.periodic & 4) != 0;
+        const bool px = g.periodic & 1, py = g.periodic & 2;
 #pragma unroll
         for (int j = 0; j < 2; j++) {
             const int k = t + j * TILE_THREADS;
-            ehas[j] = k < EH * EW;
-            eslot[j] = (short)k;
             eok[j] = false;
             eoff[j] = 0;
-            if (ehas[j]) {
-                const int ty = k / EW, tx = k - ty * EW;
+            edst[j] = -1;
+            if (k < NE) {
+                const int ty = k / EP, pi = k - ty * EP;
                 bool okx, oky;
-                const int sx = axis_src(x0 - 1 + tx, g.nx, g.periodic & 1, &okx);
-                const int sy = axis_src(y0 - 1 + ty, g.ny, g.periodic & 2, &oky);
+                const int sx = axis_src(x0 - 2 + 2 * pi, g.nx, px, &okx);
+                const int sy = axis_src(y0 - 1 + ty, g.ny, py, &oky);
                 eok[j] = okx && oky;
                 eoff[j] = eok[j] ? sx + g.nx * sy : 0;
-            }
-            chas[j] = k < CH * CW;
-            cslot[j] = (short)k;
-            cok[j] = false;
-            coff[j] = 0;
-            if (chas[j]) {
-                const int ty = k / CW, tx = k - ty * CW;
-                bool okx, oky;
-                const int sx = axis_src(x0 + tx, g.nx, g.periodic & 1, &okx);
-                const int sy = axis_src(y0 + ty, g.ny, g.periodic & 2, &oky);
-                cok[j] = okx && oky;
-                coff[j] = cok[j] ? sx + g.nx * sy : 0;
+                edst[j] = (short)(ty * EW + 2 * pi);
             }
         }
-        const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
-        rok = x < g.nx && y < g.ny;
-        roff = rok ? x + g.nx * y : 0;
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            const int k = t + j * TILE_THREADS;
+            cok[j] = false;
+            coff[j] = 0;
+            cdst[j] = 0;
+            csize[j] = 0;
+            if (k < NC) {
+                const int ty = k / CPR, ci = k - ty * CPR;
+                const int cx = (CK == 0) ? ci : (ci < TX ? 2 * ci : PX);
+                bool okx, oky;
+                const int sx = axis_src(x0 + cx, g.nx, px, &okx);
+                const int sy = axis_src(y0 + ty, g.ny, py, &oky);
+                cok[j] = okx && oky;
+                coff[j] = cok[j] ? sx + g.nx * sy : 0;
+                cdst[j] = (short)(ty * CW + cx);
+                csize[j] = (CK != 0 && ci < TX) ? 2 : 1;
+            }
+        }
+        const int rx = x0 + 2 * threadIdx.x, ry = y0 + threadIdx.y;
+        rok = rx < g.nx && ry < g.ny;
+        roff = rok ? rx + g.nx * ry : 0;
     }
 
-    template <int CK, bool WANT_E, bool WANT_R>
-    __device__ __forceinline__ void fetch(Ring<CK, WANT_E, WANT_R>& R, int zz, int slot, const float* ev,
+    template <bool WANT_E, bool WANT_R>
+    __device__ __forceinline__ void fetch(Ring<CK>& R, int zz, int slot, const float* ev,
                                           const typename CoefStore<CK>::T* coef, const float* rv) const {
         bool okz;
         const int sz = axis_src(zz, nz, pz, &okz);
@@ -142,74 +166,96 @@ struct Fetcher {
             float* dst = &R.e[slot][0][0];
 #pragma unroll
             for (int j = 0; j < 2; j++)
-                if (ehas[j]) {
+                if (edst[j] >= 0) {
                     const bool ok = eok[j] && okz;
-                    cp_async4(dst + eslot[j], ev + (ok ? plane + eoff[j] : 0), ok);
+                    cp_async8(dst + edst[j], ev + (ok ? plane + eoff[j] : 0), ok);
                 }
         }
-        auto* cdst = &R.c[slot][0][0];
+        auto* cd = &R.c[slot][0][0];
 #pragma unroll
-        for (int j = 0; j < 2; j++)
-            if (chas[j]) {
+        for (int j = 0; j < 3; j++)
+            if (csize[j]) {
                 const bool ok = cok[j] && okz;
                 const auto* src = coef + (ok ? plane + coff[j] : 0);
-                if (CK == 0) cp_async16(cdst + cslot[j], src, ok);
-                else cp_async8(cdst + cslot[j], src, ok);
+                if (CK == 0 || csize[j] == 2) cp_async16(cd + cdst[j], src, ok);
+                else cp_async8(cd + cdst[j], src, ok);
             }
         if (WANT_R) {
             const bool ok = rok && zz >= 0 && zz < nz;
-            cp_async4(&R.r[slot][threadIdx.y][threadIdx.x], rv + (ok ? plane + roff : 0), ok);
+            cp_async8(&R.r[slot][threadIdx.y][2 * threadIdx.x], rv + (ok ? plane + roff : 0), ok);
         }
     }
 };
 
-__device__ __forceinline__ int slot_of(int zz, int z0) { return (zz - z0 + 1) & (NSLOT - 1); }
-static_assert(NSLOT >= PF + 2 && (NSLOT & (NSLOT - 1)) == 0, "ring must hold planes z-1 .. z+PF");
+template <int CK>
+__device__ __forceinline__ int slot_of(int zz, int z0) { return (zz - z0 + 1) & (Depth<CK>::NSLOT - 1); }
+
+// Prologue: planes z0-1 .. z0+PF-1 in flight, one commit group each (z0-1
+// and z0 together).
+template <bool WANT_E, bool WANT_R, int CK>
+__device__ __forceinline__ void prologue(const Fetcher<CK>& F, Ring<CK>& R, int z0, int z1, const float* ev,
+                                         const typename CoefStore<CK>::T* coef, const float* rv) {
+    constexpr int PF = Depth<CK>::PF;
+    F.template fetch<WANT_E, WANT_R>(R, z0 - 1, slot_of<CK>(z0 - 1, z0), ev, coef, rv);
+    F.template fetch<WANT_E, WANT_R>(R, z0, slot_of<CK>(z0, z0), ev, coef, rv);
+    cp_commit();
+#pragma unroll
+    for (int k = 1; k < PF; k++) {
+        if (z0 + k <= z1) F.template fetch<WANT_E, WANT_R>(R, z0 + k, slot_of<CK>(z0 + k, z0), ev, coef, rv);
+        cp_commit();
+    }
+}
+// Next plane in flight, then wait until planes up to z+1 have landed.
+template <bool WANT_E, bool WANT_R, int CK>
+__device__ __forceinline__ void advance(const Fetcher<CK>& F, Ring<CK>& R, int z, int z0, int z1, const float* ev,
+                                        const typename CoefStore<CK>::T* coef, const float* rv) {
+    constexpr int PF = Depth<CK>::PF;
+    if (z + PF <= z1) F.template fetch<WANT_E, WANT_R>(R, z + PF, slot_of<CK>(z + PF, z0), ev, coef, rv);
+    cp_commit();
+    cp_wait_pf<PF>();
+    __syncthreads();
+}
 }  // namespace
 
 // --------------------------------------------------------------- SpMV
-template <int CKD>  // coefficient storage of the operator: always FP32 here
 __global__ void __launch_bounds__(TILE_THREADS) k_spmv_staged(Grid3 g, const float4* __restrict__ coef,
                                                               const float* __restrict__ p, float* __restrict__ q,
                                                               Scalars* sc, double* partials, int nblocks) {
     if (sc->converged) return;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto& R = *reinterpret_cast<Ring<0, true, false>*>(smem_raw);
+    auto& R = *reinterpret_cast<Ring<0>*>(smem_raw);
     __shared__ double sh[8];
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * TY;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x = x0 + 2 * tx, y = y0 + ty;
     const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
     const bool inside = x < g.nx && y < g.ny;
-    const int tx = threadIdx.x, ty = threadIdx.y;
     Acc acc;
-    const Fetcher F(g, x0, y0);
-    F.fetch(R, z0 - 1, slot_of(z0 - 1, z0), p, coef, nullptr);
-    F.fetch(R, z0, slot_of(z0, z0), p, coef, nullptr);
-    cp_commit();
-#pragma unroll
-    for (int k = 1; k < PF; k++) {
-        if (z0 + k <= z1) F.fetch(R, z0 + k, slot_of(z0 + k, z0), p, coef, nullptr);
-        cp_commit();
-    }
+    const Fetcher<0> F(g, x0, y0);
+    prologue<true, false>(F, R, z0, z1, p, coef, nullptr);
     for (int z = z0; z < z1; z++) {
-        if (z + PF <= z1) F.fetch(R, z + PF, slot_of(z + PF, z0), p, coef, nullptr);
-        cp_commit();
-        cp_wait_pf();
-        __syncthreads();
+        advance<true, false>(F, R, z, z0, z1, p, coef, nullptr);
         if (inside) {
-            const int s = slot_of(z, z0), sm = slot_of(z - 1, z0), sp = slot_of(z + 1, z0);
-            const float4 cc = R.c[s][ty][tx];
-            const float bxh = R.c[s][ty][tx + 1].x, byh = R.c[s][ty + 1][tx].y, bzh = R.c[sp][ty][tx].z;
-            const float pc = R.e[s][ty + 1][tx + 1];
-            float qv = cc.w * pc;
-            qv = fmaf(cc.x, pc - R.e[s][ty + 1][tx], qv);
-            qv = fmaf(bxh, pc - R.e[s][ty + 1][tx + 2], qv);
-            qv = fmaf(cc.y, pc - R.e[s][ty][tx + 1], qv);
-            qv = fmaf(byh, pc - R.e[s][ty + 2][tx + 1], qv);
-            qv = fmaf(cc.z, pc - R.e[sm][ty + 1][tx + 1], qv);
-            qv = fmaf(bzh, pc - R.e[sp][ty + 1][tx + 1], qv);
-            q[x + g.nx * (y + g.ny * z)] = qv;
-            acc.add_prod(pc, qv);
+            const int s = slot_of<0>(z, z0), sm = slot_of<0>(z - 1, z0), sp = slot_of<0>(z + 1, z0);
+            const float* er = &R.e[s][ty + 1][0];
+            float qv[2];
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const int cx = 2 * tx + k, ex = cx + 2;
+                const float4 cc = R.c[s][ty][cx];
+                const float bxh = R.c[s][ty][cx + 1].x, byh = R.c[s][ty + 1][cx].y, bzh = R.c[sp][ty][cx].z;
+                const float pc = er[ex];
+                float v = cc.w * pc;
+                v = fmaf(cc.x, pc - er[ex - 1], v);
+                v = fmaf(bxh, pc - er[ex + 1], v);
+                v = fmaf(cc.y, pc - R.e[s][ty][ex], v);
+                v = fmaf(byh, pc - R.e[s][ty + 2][ex], v);
+                v = fmaf(cc.z, pc - R.e[sm][ty + 1][ex], v);
+                v = fmaf(bzh, pc - R.e[sp][ty + 1][ex], v);
+                qv[k] = v;
+                acc.add_prod(pc, v);
+            }
+            *reinterpret_cast<float2*>(q + x + (long long)g.nx * (y + (long long)g.ny * z)) = make_float2(qv[0], qv[1]);
         }
         __syncthreads();
     }
@@ -238,7 +284,9 @@ __global__ void __launch_bounds__(TILE_THREADS) k_spmv_staged(Grid3 g, const flo
 
 // ------------------------------------------------------- smoother half-step
 // Fine level: rhs = sigma * r (FP32), correction z (FP32), coefficients in the
-// level precision.  ZERO: first half-step from zero (no vector staging).
+// level precision.  ZERO: first half-step from zero (no vector staging).  The
+// division uses the fast reciprocal: each cell's factor is a fixed number, so
+// the sweep is still a fixed linear map and the V-cycle stays symmetric.
 template <int CK, bool ZERO, bool OUT>
 __global__ void __launch_bounds__(TILE_THREADS) k_smooth_staged(Grid3 g, const void* __restrict__ coef_v,
                                                                 const float* __restrict__ r, float* e, float* out,
@@ -247,56 +295,49 @@ __global__ void __launch_bounds__(TILE_THREADS) k_smooth_staged(Grid3 g, const v
     using CT = typename CoefStore<CK>::T;
     const CT* coef = reinterpret_cast<const CT*>(coef_v);
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto& R = *reinterpret_cast<Ring<CK, !ZERO, true>*>(smem_raw);
+    auto& R = *reinterpret_cast<Ring<CK>*>(smem_raw);
     const float sigma = sc->sigma;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * TY;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x = x0 + 2 * tx, y = y0 + ty;
     const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
     const bool inside = x < g.nx && y < g.ny;
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const Fetcher F(g, x0, y0);
-    F.fetch(R, z0 - 1, slot_of(z0 - 1, z0), e, coef, r);
-    F.fetch(R, z0, slot_of(z0, z0), e, coef, r);
-    cp_commit();
-#pragma unroll
-    for (int k = 1; k < PF; k++) {
-        if (z0 + k <= z1) F.fetch(R, z0 + k, slot_of(z0 + k, z0), e, coef, r);
-        cp_commit();
-    }
+    const Fetcher<CK> F(g, x0, y0);
+    prologue<!ZERO, true>(F, R, z0, z1, e, coef, r);
     for (int z = z0; z < z1; z++) {
-        if (z + PF <= z1) F.fetch(R, z + PF, slot_of(z + PF, z0), e, coef, r);
-        cp_commit();
-        cp_wait_pf();
-        __syncthreads();
+        advance<!ZERO, true>(F, R, z, z0, z1, e, coef, r);
         if (inside) {
-            const int i = x + g.nx * (y + g.ny * z);
-            if (((x + y + z) & 1) == color) {
-                const int s = slot_of(z, z0), sm = slot_of(z - 1, z0), sp = slot_of(z + 1, z0);
-                const float4 cc = unpack<CK>(R.c[s][ty][tx]);
-                const float bxh = unpack<CK>(R.c[s][ty][tx + 1]).x;
-                const float byh = unpack<CK>(R.c[s][ty + 1][tx]).y;
-                const float bzh = unpack<CK>(R.c[sp][ty][tx]).z;
-                const float d = ((cc.x + bxh) + (cc.y + byh)) + ((cc.z + bzh) + cc.w);
-                float val = 0.f;
-                if (d > 0.f) {
-                    const float rhs = sigma * R.r[s][ty][tx];
-                    if (ZERO) {
-                        val = rhs / d;
-                    } else {
-                        float acc = rhs;
-                        acc = fmaf(cc.x, R.e[s][ty + 1][tx], acc);
-                        acc = fmaf(bxh, R.e[s][ty + 1][tx + 2], acc);
-                        acc = fmaf(cc.y, R.e[s][ty][tx + 1], acc);
-                        acc = fmaf(byh, R.e[s][ty + 2][tx + 1], acc);
-                        acc = fmaf(cc.z, R.e[sm][ty + 1][tx + 1], acc);
-                        acc = fmaf(bzh, R.e[sp][ty + 1][tx + 1], acc);
-                        val = acc / d;
-                    }
+            const int s = slot_of<CK>(z, z0), sp = slot_of<CK>(z + 1, z0);
+            const int k = (color - (y + z)) & 1;  // the pair member of this colour
+            const int cx = 2 * tx + k, ex = cx + 2;
+            const float4 cc = unpack<CK>(R.c[s][ty][cx]);
+            const float bxh = unpack<CK>(R.c[s][ty][cx + 1]).x;
+            const float byh = unpack<CK>(R.c[s][ty + 1][cx]).y;
+            const float bzh = unpack<CK>(R.c[sp][ty][cx]).z;
+            const float d = ((cc.x + bxh) + (cc.y + byh)) + ((cc.z + bzh) + cc.w);
+            float val = 0.f;
+            if (d > 0.f) {
+                float acc = sigma * R.r[s][ty][cx];
+                if (!ZERO) {
+                    const int sm = slot_of<CK>(z - 1, z0);
+                    const float* er = &R.e[s][ty + 1][0];
+                    acc = fmaf(cc.x, er[ex - 1], acc);
+                    acc = fmaf(bxh, er[ex + 1], acc);
+                    acc = fmaf(cc.y, R.e[s][ty][ex], acc);
+                    acc = fmaf(byh, R.e[s][ty + 2][ex], acc);
+                    acc = fmaf(cc.z, R.e[sm][ty + 1][ex], acc);
+                    acc = fmaf(bzh, R.e[sp][ty + 1][ex], acc);
                 }
-                if (OUT) out[i] = val;
-                else e[i] = val;
-            } else if (ZERO) {
-                e[i] = 0.f;
+                val = __fdividef(acc, d);
+            }
+            const long long i0 = x + (long long)g.nx * (y + (long long)g.ny * z);
+            if (ZERO) {
+                // both members written: the other colour starts at zero
+                *reinterpret_cast<float2*>(e + i0) = k ? make_float2(0.f, val) : make_float2(val, 0.f);
+            } else if (OUT) {
+                out[i0 + k] = val;
+            } else {
+                e[i0 + k] = val;
             }
         }
         __syncthreads();
@@ -305,9 +346,9 @@ __global__ void __launch_bounds__(TILE_THREADS) k_smooth_staged(Grid3 g, const v
 }
 
 // -------------------------------------------------- residual + restriction
-// rc[Q] = 1/4 sum over the 2x2x2 children of (sigma r - A z); the z pair is
-// summed over two steps, the x pair by a shuffle, the y pair through shared
-// memory.  Requires an even z run per block.
+// rc[Q] = 1/4 sum over the 2x2x2 children of (sigma r - A z): the x pair is a
+// thread's own two cells, the z pair two consecutive planes, the y pair goes
+// through shared memory.  Requires an even z run per block.
 template <int CK, class VTc>
 __global__ void __launch_bounds__(TILE_THREADS) k_restrict_staged(Grid3 g, Grid3 gc, const void* __restrict__ coef_v,
                                                                   const float* __restrict__ r,
@@ -317,53 +358,47 @@ __global__ void __launch_bounds__(TILE_THREADS) k_restrict_staged(Grid3 g, Grid3
     using CT = typename CoefStore<CK>::T;
     const CT* coef = reinterpret_cast<const CT*>(coef_v);
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto& R = *reinterpret_cast<Ring<CK, true, true>*>(smem_raw);
+    auto& R = *reinterpret_cast<Ring<CK>*>(smem_raw);
     __shared__ float ypart[TY][TX];
     const float sigma = sc->sigma;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * TY;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x = x0 + 2 * tx, y = y0 + ty;
     const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
     const bool inside = x < g.nx && y < g.ny;
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const Fetcher F(g, x0, y0);
-    F.fetch(R, z0 - 1, slot_of(z0 - 1, z0), e, coef, r);
-    F.fetch(R, z0, slot_of(z0, z0), e, coef, r);
-    cp_commit();
-#pragma unroll
-    for (int k = 1; k < PF; k++) {
-        if (z0 + k <= z1) F.fetch(R, z0 + k, slot_of(z0 + k, z0), e, coef, r);
-        cp_commit();
-    }
+    const Fetcher<CK> F(g, x0, y0);
+    prologue<true, true>(F, R, z0, z1, e, coef, r);
     float part = 0.f;
     for (int z = z0; z < z1; z++) {
-        if (z + PF <= z1) F.fetch(R, z + PF, slot_of(z + PF, z0), e, coef, r);
-        cp_commit();
-        cp_wait_pf();
-        __syncthreads();
+        advance<true, true>(F, R, z, z0, z1, e, coef, r);
         if (inside) {
-            const int s = slot_of(z, z0), sm = slot_of(z - 1, z0), sp = slot_of(z + 1, z0);
-            const float4 cc = unpack<CK>(R.c[s][ty][tx]);
-            const float bxh = unpack<CK>(R.c[s][ty][tx + 1]).x;
-            const float byh = unpack<CK>(R.c[s][ty + 1][tx]).y;
-            const float bzh = unpack<CK>(R.c[sp][ty][tx]).z;
-            const float d = ((cc.x + bxh) + (cc.y + byh)) + ((cc.z + bzh) + cc.w);
-            float nsum = 0.f;
-            nsum = fmaf(cc.x, R.e[s][ty + 1][tx], nsum);
-            nsum = fmaf(bxh, R.e[s][ty + 1][tx + 2], nsum);
-            nsum = fmaf(cc.y, R.e[s][ty][tx + 1], nsum);
-            nsum = fmaf(byh, R.e[s][ty + 2][tx + 1], nsum);
-            nsum = fmaf(cc.z, R.e[sm][ty + 1][tx + 1], nsum);
-            nsum = fmaf(bzh, R.e[sp][ty + 1][tx + 1], nsum);
-            part += sigma * R.r[s][ty][tx] - (d * R.e[s][ty + 1][tx + 1] - nsum);
+            const int s = slot_of<CK>(z, z0), sm = slot_of<CK>(z - 1, z0), sp = slot_of<CK>(z + 1, z0);
+            const float* er = &R.e[s][ty + 1][0];
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const int cx = 2 * tx + k, ex = cx + 2;
+                const float4 cc = unpack<CK>(R.c[s][ty][cx]);
+                const float bxh = unpack<CK>(R.c[s][ty][cx + 1]).x;
+                const float byh = unpack<CK>(R.c[s][ty + 1][cx]).y;
+                const float bzh = unpack<CK>(R.c[sp][ty][cx]).z;
+                const float d = ((cc.x + bxh) + (cc.y + byh)) + ((cc.z + bzh) + cc.w);
+                float nsum = 0.f;
+                nsum = fmaf(cc.x, er[ex - 1], nsum);
+                nsum = fmaf(bxh, er[ex + 1], nsum);
+                nsum = fmaf(cc.y, R.e[s][ty][ex], nsum);
+                nsum = fmaf(byh, R.e[s][ty + 2][ex], nsum);
+                nsum = fmaf(cc.z, R.e[sm][ty + 1][ex], nsum);
+                nsum = fmaf(bzh, R.e[sp][ty + 1][ex], nsum);
+                part += sigma * R.r[s][ty][cx] - (d * er[ex] - nsum);
+            }
         }
         const bool last_of_pair = ((z - z0) & 1) || z + 1 == z1;
         if (last_of_pair) {
-            float v = part + __shfl_xor_sync(0xffffffffu, part, 1);
-            ypart[ty][tx] = v;
+            ypart[ty][tx] = part;
             __syncthreads();
-            if (inside && !(tx & 1) && !(ty & 1)) {
-                const float tot = v + ypart[ty + 1][tx];
-                rc[(x >> 1) + gc.nx * ((y >> 1) + gc.ny * (z >> 1))] = from_f<VTc>(0.25f * tot);
+            if (inside && !(ty & 1)) {
+                const float tot = part + ypart[ty + 1][tx];
+                rc[(x >> 1) + (long long)gc.nx * ((y >> 1) + (long long)gc.ny * (z >> 1))] = from_f<VTc>(0.25f * tot);
             }
             part = 0.f;
         }
@@ -373,25 +408,60 @@ __global__ void __launch_bounds__(TILE_THREADS) k_restrict_staged(Grid3 g, Grid3
 }
 
 // ------------------------------------------------------------ launchers
-template <int CK>
-static size_t ring_bytes(bool want_e, bool want_r) {
-    (void)want_e;
-    (void)want_r;
-    return sizeof(Ring<CK, true, true>);
+// Blocks per SM of each staged kernel (from the occupancy calculator) and the
+// SM count: the z split is chosen so that the grid fills whole waves.
+namespace {
+int g_sms = 0;
+int g_occ[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+enum { OCC_SPMV = 0, OCC_SMOOTH_F32, OCC_SMOOTH_LO, OCC_RESTRICT_F32, OCC_RESTRICT_LO };
+}  // namespace
+
+static Launch pair_launch(const Launch& L, int occ_kind) {
+    Launch P = L;
+    const int gx = (L.g.nx + PX - 1) / PX, gy = (L.g.ny + TY - 1) / TY, nz = L.g.nz;
+    const int tiles = gx * gy;
+    const int cap = (g_sms > 0 ? g_sms : 152) * (g_occ[occ_kind] > 0 ? g_occ[occ_kind] : 2);
+    // candidate even z runs of at least 8 planes (or the whole column):
+    // pick the one whose grid wastes the least of its last wave
+    int best_zper = nz, best_zc = 1;
+    double best = -1.0;
+    for (int zc = 1; zc <= nz; zc++) {
+        int zper = (nz + zc - 1) / zc;
+        if ((zper & 1) && zper < nz) zper++;
+        if (zper < 8 && zc > 1) break;
+        const int zcr = (nz + zper - 1) / zper;
+        const long long blocks = (long long)tiles * zcr;
+        if (blocks > MAX_REDUCE_BLOCKS) break;
+        const double waves = (double)blocks / cap;
+        // fullness of the last wave times the share of fetched planes that
+        // are computed (each run also fetches the planes just below and above)
+        const double score = waves / std::ceil(waves) * ((double)zper / (zper + 2));
+        if (score > best) {
+            best = score;
+            best_zper = zper;
+            best_zc = zcr;
+        }
+    }
+    P.grid = dim3(gx, gy, best_zc);
+    P.g.zper = best_zper;
+    P.nblocks = tiles * best_zc;
+    return P;
 }
+bool staged_supported(const Grid3& g) { return (g.nx % 2) == 0; }
 
 void launch_spmv_staged(const Launch& L, const Fields& F, cudaStream_t s) {
-    k_spmv_staged<0><<<L.grid, L.block, sizeof(Ring<0, true, false>), s>>>(L.g, F.coef, F.p, F.q, F.sc, F.partials,
-                                                                           L.nblocks);
+    const Launch P = pair_launch(L, OCC_SPMV);
+    k_spmv_staged<<<P.grid, P.block, sizeof(Ring<0>), s>>>(P.g, F.coef, F.p, F.q, F.sc, F.partials, P.nblocks);
 }
 
 template <int CK>
 static void smooth_staged_impl(const Launch& L, const void* coef, const float* r, float* e, float* tmp, int color,
                                bool zero, bool out_of_place, const Scalars* sc, cudaStream_t s) {
-    const size_t sm = ring_bytes<CK>(true, true);
-    if (zero) k_smooth_staged<CK, true, false><<<L.grid, L.block, sm, s>>>(L.g, coef, r, e, e, color, sc);
-    else if (!out_of_place) k_smooth_staged<CK, false, false><<<L.grid, L.block, sm, s>>>(L.g, coef, r, e, e, color, sc);
-    else k_smooth_staged<CK, false, true><<<L.grid, L.block, sm, s>>>(L.g, coef, r, e, tmp, color, sc);
+    const Launch P = pair_launch(L, CK == 0 ? OCC_SMOOTH_F32 : OCC_SMOOTH_LO);
+    const size_t sm = sizeof(Ring<CK>);
+    if (zero) k_smooth_staged<CK, true, false><<<P.grid, P.block, sm, s>>>(P.g, coef, r, e, e, color, sc);
+    else if (!out_of_place) k_smooth_staged<CK, false, false><<<P.grid, P.block, sm, s>>>(P.g, coef, r, e, e, color, sc);
+    else k_smooth_staged<CK, false, true><<<P.grid, P.block, sm, s>>>(P.g, coef, r, e, tmp, color, sc);
 }
 void launch_smooth_staged(int ck, const Launch& L, const void* coef, const float* r, float* e, float* tmp, int color,
                           bool zero, bool out_of_place, const Scalars* sc, cudaStream_t s) {
@@ -403,7 +473,8 @@ void launch_smooth_staged(int ck, const Launch& L, const void* coef, const float
 template <int CK, class VTc>
 static void restrict_staged_impl(const Launch& L, const Grid3& gc, const void* coef, const float* r, const float* e,
                                  void* rc, const Scalars* sc, cudaStream_t s) {
-    k_restrict_staged<CK, VTc><<<L.grid, L.block, ring_bytes<CK>(true, true), s>>>(L.g, gc, coef, r, e, (VTc*)rc, sc);
+    const Launch P = pair_launch(L, CK == 0 ? OCC_RESTRICT_F32 : OCC_RESTRICT_LO);
+    k_restrict_staged<CK, VTc><<<P.grid, P.block, sizeof(Ring<CK>), s>>>(P.g, gc, coef, r, e, (VTc*)rc, sc);
 }
 void launch_restrict_staged(int ck, const Launch& L, const Grid3& gc, const void* coef, const float* r, const float* e,
                             void* rc, const Scalars* sc, cudaStream_t s) {
@@ -417,19 +488,31 @@ cudaError_t staged_prepare_attributes() {
     auto set = [&](const void* fn, size_t bytes) {
         if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     };
-    set((const void*)k_spmv_staged<0>, sizeof(Ring<0, true, false>));
-    set((const void*)k_smooth_staged<0, true, false>, sizeof(Ring<0, true, true>));
-    set((const void*)k_smooth_staged<0, false, false>, sizeof(Ring<0, true, true>));
-    set((const void*)k_smooth_staged<0, false, true>, sizeof(Ring<0, true, true>));
-    set((const void*)k_smooth_staged<1, true, false>, sizeof(Ring<1, true, true>));
-    set((const void*)k_smooth_staged<1, false, false>, sizeof(Ring<1, true, true>));
-    set((const void*)k_smooth_staged<1, false, true>, sizeof(Ring<1, true, true>));
-    set((const void*)k_smooth_staged<2, true, false>, sizeof(Ring<2, true, true>));
-    set((const void*)k_smooth_staged<2, false, false>, sizeof(Ring<2, true, true>));
-    set((const void*)k_smooth_staged<2, false, true>, sizeof(Ring<2, true, true>));
-    set((const void*)k_restrict_staged<0, float>, sizeof(Ring<0, true, true>));
-    set((const void*)k_restrict_staged<1, __half>, sizeof(Ring<1, true, true>));
-    set((const void*)k_restrict_staged<2, __nv_bfloat16>, sizeof(Ring<2, true, true>));
+    set((const void*)k_spmv_staged, sizeof(Ring<0>));
+    set((const void*)k_smooth_staged<0, true, false>, sizeof(Ring<0>));
+    set((const void*)k_smooth_staged<0, false, false>, sizeof(Ring<0>));
+    set((const void*)k_smooth_staged<0, false, true>, sizeof(Ring<0>));
+    set((const void*)k_smooth_staged<1, true, false>, sizeof(Ring<1>));
+    set((const void*)k_smooth_staged<1, false, false>, sizeof(Ring<1>));
+    set((const void*)k_smooth_staged<1, false, true>, sizeof(Ring<1>));
+    set((const void*)k_smooth_staged<2, true, false>, sizeof(Ring<2>));
+    set((const void*)k_smooth_staged<2, false, false>, sizeof(Ring<2>));
+    set((const void*)k_smooth_staged<2, false, true>, sizeof(Ring<2>));
+    set((const void*)k_restrict_staged<0, float>, sizeof(Ring<0>));
+    set((const void*)k_restrict_staged<1, __half>, sizeof(Ring<1>));
+    set((const void*)k_restrict_staged<2, __nv_bfloat16>, sizeof(Ring<2>));
+    if (e != cudaSuccess) return e;
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    auto occ = [&](int kind, const void* fn, size_t bytes) {
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_occ[kind], fn, TILE_THREADS, bytes);
+    };
+    occ(OCC_SPMV, (const void*)k_spmv_staged, sizeof(Ring<0>));
+    occ(OCC_SMOOTH_F32, (const void*)k_smooth_staged<0, false, false>, sizeof(Ring<0>));
+    occ(OCC_SMOOTH_LO, (const void*)k_smooth_staged<1, false, false>, sizeof(Ring<1>));
+    occ(OCC_RESTRICT_F32, (const void*)k_restrict_staged<0, float>, sizeof(Ring<0>));
+    occ(OCC_RESTRICT_LO, (const void*)k_restrict_staged<1, __half>, sizeof(Ring<1>));
     return e;
 }
 

@@ -69,6 +69,7 @@ void launch_smooth_staged(int ck, const Launch& L, const void* coef, const float
 void launch_restrict_staged(int ck, const Launch& L, const Grid3& gc, const void* coef, const float* r, const float* e,
                             void* rc, const Scalars* sc, cudaStream_t s);
 cudaError_t staged_prepare_attributes();
+bool staged_supported(const Grid3& g);
 
 // ---- multigrid (mg_kernels.cu)
 struct MGLevel {
