@@ -37,13 +37,17 @@ struct Scalars {
     double objective;   // chain objective / misc reductions
     double divmax, div2;// divergence statistics
     float alpha_f, beta_f, sigma, inv_sigma;
+    float inv_sigma_z;  // 1/sigma of the V-cycle that produced the current z
+    int first;          // the next search step starts a CG pass (p = z, no x update)
+    int pidx;           // search-direction buffer written last (pipelined CG)
+    int max_total;      // iteration cap checked on the device (pipelined CG)
     int converged;      // inner solve finished
     int outer_done;     // true residual meets the target
     int iterations;     // inner iterations of this solve
     int total_iterations;
     int nonfinite;      // a reduction produced NaN/Inf
     int breakdown;      // p.Ap <= 0
-    unsigned int ticket[8];
+    unsigned int ticket[12];
 };
 
 // ------------------------------------------------------------ indexing
@@ -202,6 +206,22 @@ struct Acc {
     }
     __device__ __forceinline__ double total() const { return (double)s + (double)c; }
 };
+
+// Power-of-two scale that brings the RMS residual near 1/16, so FP16 level
+// fields keep their values inside the normal range.
+__device__ __forceinline__ void set_sigma_from(Scalars* sc, double rr, long long n_active) {
+    double rms = n_active > 0 ? sqrt(rr / (double)n_active) : 0.0;
+    if (rms > 0.0 && isfinite(rms)) {
+        int ex;
+        frexp(rms, &ex);
+        double s = ldexp(1.0, -ex - 4);
+        sc->sigma = (float)s;
+        sc->inv_sigma = (float)(1.0 / s);
+    } else {
+        sc->sigma = 1.0f;
+        sc->inv_sigma = 1.0f;
+    }
+}
 
 // ------------------------------------------------------- reductions
 __device__ __forceinline__ double warp_sum(double v) {

@@ -65,6 +65,9 @@ struct mhdproj_ctx {
     MGPlan mg{};
     bool use_mg = false;
     bool staged = true;  // finest-level stencils through shared-memory staging
+    // pipelined CG: search+SpMV, fused V-cycle passes; ping-pong r and p
+    bool pipelined = false;
+    float *r1 = nullptr, *p1 = nullptr;
     cudaGraphExec_t it_graph = nullptr;
     bool graph_failed = false;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_sync = nullptr;
@@ -219,6 +222,33 @@ static int build_levels(mhdproj_ctx* ctx) {
     }
     P.m = d[0] * d[1] * d[2];
     CK(dalloc(ctx, &P.ainv, (size_t)P.m * P.m * sizeof(float)));
+    // Levels run as fused pre-/post-smoothing passes: a prefix of the levels
+    // that have a coarser level, an even x extent and even periodic extents,
+    // down to 16^3 cells; smaller levels use the per-level kernels.
+    P.fused_levels = 0;
+    P.e0 = nullptr;
+    if (ctx->pipelined && P.nlevels >= 2) {
+        int F = 0;
+        while (F < P.nlevels - 1) {
+            const Grid3& g = P.lv[F].L.g;
+            if (!fused_supported(g)) break;
+            if (F > 0 && g.n() < 4096) break;
+            F++;
+        }
+        if (F == 0) {
+            ctx->pipelined = false;
+        } else {
+            P.fused_levels = F;
+            CK(dalloc(ctx, &P.e0, (size_t)ctx->n * 4));
+            const size_t rbytes = P.precision == 0 ? 16 : 8;
+            for (int l = 0; l < F; l++) {
+                CK(dalloc(ctx, (char**)&P.lv[l].sm, (size_t)P.lv[l].L.g.n() * rbytes));
+                if (l > 0) CK(dalloc(ctx, (char**)&P.lv[l].eo, (size_t)P.lv[l].L.g.n() * vbytes));
+            }
+        }
+    } else {
+        ctx->pipelined = false;
+    }
     return 0;
 }
 
@@ -317,8 +347,15 @@ extern "C" int mhdproj_create(const mhdproj_grid* grid, const mhdproj_options* o
                  const char* ev = getenv("MHDPROJ_STAGED");
                  if (ev && ev[0] == '0') ctx->staged = false;
                  if (!staged_supported(ctx->L.g)) ctx->staged = false;
+                 const char* pv = getenv("MHDPROJ_PIPELINED");
+                 ctx->pipelined = ctx->use_mg && ctx->staged && fused_supported(ctx->L.g) && !(pv && pv[0] == '0');
              }
              CK(staged_prepare_attributes());
+             if (ctx->pipelined) {
+                 CK(fused_prepare_attributes());
+                 CK(dalloc(ctx, &ctx->r1, n * 4));
+                 CK(dalloc(ctx, &ctx->p1, n * 4));
+             }
              if (ctx->use_mg) {
                  int r = build_levels(ctx);
                  if (r) return r;
@@ -431,6 +468,7 @@ extern "C" int mhdproj_set_coefficients(mhdproj_ctx* ctx, const float* alpha, co
     CK(cudaGetLastError());
     if (ctx->use_mg) {
         mg_build(ctx->mg, ctx->stream);
+        if (ctx->pipelined) mg_smoother_records(ctx->mg, ctx->stream);
         CK(cudaGetLastError());
     }
     ctx->have_coef = true;
@@ -467,7 +505,32 @@ static void enqueue_precondition(mhdproj_ctx* ctx) {
     if (ctx->use_mg) mg_vcycle(ctx->mg, ctx->stream);
     else k_jacobi<<<ctx->L.grid, ctx->L.block, 0, ctx->stream>>>(ctx->L.g, ctx->coef, ctx->r, ctx->z, ctx->sc);
 }
+// Pass start of the pipelined CG: z = B r0 and rz (the first search step
+// then takes p = z).
+static void enqueue_pass_start(mhdproj_ctx* ctx) {
+    if (ctx->pipelined) {
+        mg_vcycle_fused(ctx->mg, ctx->r, nullptr, nullptr, false, ctx->partials, ctx->n_active, ctx->stream);
+        return;
+    }
+    enqueue_precondition(ctx);
+    Fields F = fields(ctx);
+    launch_dot_rz(ctx->L, F, 1, ctx->stream);
+}
+// Two pipelined CG iterations with the r and p buffers swapping roles.
+static void enqueue_pipelined_pair(mhdproj_ctx* ctx) {
+    float* rb[2] = {ctx->r, ctx->r1};
+    float* pb[2] = {ctx->p, ctx->p1};
+    for (int par = 0; par < 2; par++) {
+        launch_search_spmv(ctx->L, ctx->coef, ctx->z, pb[par], pb[1 - par], ctx->e, ctx->q, ctx->sc, ctx->partials,
+                           1 - par, ctx->stream);
+        mg_vcycle_fused(ctx->mg, rb[par], ctx->q, rb[1 - par], true, ctx->partials, ctx->n_active, ctx->stream);
+    }
+}
 static void enqueue_iteration_body(mhdproj_ctx* ctx) {
+    if (ctx->pipelined) {
+        enqueue_pipelined_pair(ctx);
+        return;
+    }
     Fields F = fields(ctx);
     if (ctx->staged) launch_spmv_staged(ctx->L, F, ctx->stream);
     else launch_spmv_pq(ctx->L, F, ctx->stream);
@@ -494,7 +557,9 @@ static int launch_iterations(mhdproj_ctx* ctx, int count) {
             ctx->it_graph = nullptr;
         }
     }
-    for (int k = 0; k < count; k++) {
+    // a pipelined graph holds two iterations
+    const int launches = ctx->pipelined ? (count + 1) / 2 : count;
+    for (int k = 0; k < launches; k++) {
         if (ctx->it_graph) CK(cudaGraphLaunch(ctx->it_graph, ctx->stream));
         else enqueue_iteration_body(ctx);
     }
@@ -512,8 +577,7 @@ static int solve(mhdproj_ctx* ctx, float* x_hi, float* x_lo, mhdproj_stats* st) 
     (void)tol2;
     int passes = 0;
     launch_residual(ctx->L, F, x_hi, x_lo, ctx->stream);
-    enqueue_precondition(ctx);
-    launch_dot_rz(ctx->L, F, 1, ctx->stream);
+    enqueue_pass_start(ctx);
     CK(cudaGetLastError());
     int rc = read_scalars(ctx);
     if (rc) return rc;
@@ -554,11 +618,11 @@ static int solve(mhdproj_ctx* ctx, float* x_hi, float* x_lo, mhdproj_stats* st) 
             rr_prev = T.rr;
             it_prev = T.iterations;
         }
-        launch_accumulate(ctx->L, F, x_hi, x_lo, ctx->stream);
+        if (ctx->pipelined) launch_accumulate_pipelined(ctx->L, x_hi, x_lo, ctx->e, ctx->p, ctx->p1, ctx->sc, ctx->stream);
+        else launch_accumulate(ctx->L, F, x_hi, x_lo, ctx->stream);
         passes++;
         launch_residual(ctx->L, F, x_hi, x_lo, ctx->stream);
-        enqueue_precondition(ctx);
-        launch_dot_rz(ctx->L, F, 1, ctx->stream);
+        enqueue_pass_start(ctx);
         CK(cudaGetLastError());
         rc = read_scalars(ctx);
         if (rc) return rc;
@@ -584,7 +648,7 @@ static void begin_scalars(mhdproj_ctx* ctx) {
     const double h = ctx->grid.h;
     const double abs_floor = (double)ctx->opt.abs_div_tol * ctx->opt.abs_div_tol * h * h * h * h * (double)ctx->n_active;
     // FP32 CG reduces its own residual by about 1e-5 reliably; refine beyond.
-    launch_init_scalars(ctx->sc, tol2, abs_floor, 1e-10, ctx->stream);
+    launch_init_scalars(ctx->sc, tol2, abs_floor, 1e-10, (int)ctx->opt.max_iterations, ctx->stream);
 }
 
 static int project_gb300(mhdproj_ctx* ctx, const float* us, const float* vs, const float* ws, float* uo, float* vo,
@@ -933,7 +997,8 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
     };
     // Algorithmic bytes per cell: the compulsory traffic of each kernel's
     // fields, every field touched once per launch.
-    const Item items[] = {
+    const double vbc = ctx->opt.precision == 0 ? 4.0 : 2.0;   // level-1 vector bytes per cell
+    const Item classic[] = {
         {"spmv_dot", 20.0, 1, 0},             // p 4 + beta 12 -> q 4
         {"update_norm", 24.0, 1, 1},          // e, p, r, q 16 -> e, r 8
         {"fine_smooth_half", 12.0 + cb, 4, 2},  // r 4 + coef + z 4 -> z 4
@@ -944,11 +1009,26 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
         {"refinement_residual", 24.0, 0, 7},  // x 4 + beta 12 + b 4 -> r 4 (survey K7)
         {"coefficients", 29.0, 0, 8},         // alpha 4 + solid 1 -> 16 + 8 (survey K0)
     };
+    const Item pipelined[] = {
+        // z 4 + p_old 4 + coef 16 + x 4 -> p 4 + x 4 + q 4
+        {"search_spmv", 40.0, 1, 10},
+        // r 4 + q 4 + coef -> r 4 + e 4 + coarse r (1/8 cell)
+        {"presmooth_restrict", 16.0 + cb + vbc / 8.0, 1, 11},
+        // e 4 + coarse e (1/8 cell) + r 4 + coef -> z 4
+        {"prolong_postsmooth", 12.0 + cb + vbc / 8.0, 1, 12},
+        {"refinement_residual", 24.0, 0, 7},
+        {"coefficients", 29.0, 0, 8},
+    };
+    const Item* items = ctx->pipelined ? pipelined : classic;
+    const int n_items = ctx->pipelined ? (int)(sizeof pipelined / sizeof pipelined[0])
+                                       : (int)(sizeof classic / sizeof classic[0]);
     int k = 0;
-    for (const Item& it : items) {
+    for (int ii = 0; ii < n_items; ii++) {
+        const Item& it = items[ii];
         if (k >= max_out) break;
         if (!ctx->use_mg && (it.kind >= 2 && it.kind <= 4)) continue;
         launch_set_sigma(ctx->sc, 1.0f, s);  // clears the converged flag
+        if (it.kind >= 10) launch_profile_reset(ctx->sc, s);
         CK(cudaEventRecord(ctx->ev_a, s));
         for (int r = 0; r < reps; r++) {
             switch (it.kind) {
@@ -964,8 +1044,15 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
                 case 6: launch_search(ctx->L, F, s); break;
                 case 7: launch_residual(ctx->L, F, ctx->phi_hi, ctx->phi_lo, s); break;
                 case 8: launch_coefficients(ctx->L, F, s); break;
+                case 10:
+                    launch_search_spmv(ctx->L, ctx->coef, ctx->z, ctx->p, ctx->p1, ctx->e, ctx->q, ctx->sc,
+                                       ctx->partials, 1, s);
+                    break;
+                case 11: mg_fused_pre(ctx->mg, ctx->r, ctx->q, ctx->r1, ctx->partials, s); break;
+                case 12: mg_fused_post(ctx->mg, ctx->r1, ctx->partials, ctx->n_active, s); break;
             }
             if (it.kind == 1 || it.kind == 5 || it.kind == 7) launch_set_sigma(ctx->sc, 1.0f, s);
+            if (it.kind >= 10) launch_profile_reset(ctx->sc, s);
         }
         CK(cudaEventRecord(ctx->ev_b, s));
         CK(cudaGetLastError());

@@ -20,8 +20,10 @@
 // staged snapshots are exactly the values each update reads.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 #include "kernels.h"
+#include "staged.cuh"
 
 namespace mhdproj {
 
@@ -38,51 +40,10 @@ template <int CK> struct Depth {
     static constexpr int PF = NSLOT - 2;
 };
 
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, bool valid) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    const int n = valid ? 8 : 0;
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(n) : "memory");
-}
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    const int n = valid ? 16 : 0;
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(n) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+using namespace staged;
 template <int PF>
-__device__ __forceinline__ void cp_wait_pf() { asm volatile("cp.async.wait_group %0;\n" ::"n"(PF - 1) : "memory"); }
-__device__ __forceinline__ void cp_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
-template <int CK> struct CoefStore { using T = uint2; };
-template <> struct CoefStore<0> { using T = float4; };
-
-template <int CK> __device__ __forceinline__ float4 unpack(const typename CoefStore<CK>::T& v);
-template <> __device__ __forceinline__ float4 unpack<0>(const float4& v) { return v; }
-template <> __device__ __forceinline__ float4 unpack<1>(const uint2& u) {
-    const __half2 a = *reinterpret_cast<const __half2*>(&u.x), b = *reinterpret_cast<const __half2*>(&u.y);
-    const float2 fa = __half22float2(a), fb = __half22float2(b);
-    return make_float4(fa.x, fa.y, fb.x, fb.y);
-}
-template <> __device__ __forceinline__ float4 unpack<2>(const uint2& u) {
-    const __nv_bfloat162 a = *reinterpret_cast<const __nv_bfloat162*>(&u.x);
-    const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162*>(&u.y);
-    const float2 fa = __bfloat1622float2(a), fb = __bfloat1622float2(b);
-    return make_float4(fa.x, fa.y, fb.x, fb.y);
-}
-
-// Wrapped or absent coordinate along one axis.
-__device__ __forceinline__ int axis_src(int c, int n, bool periodic, bool* ok) {
-    if (c < 0) {
-        *ok = periodic;
-        return periodic ? c + n : 0;
-    }
-    if (c >= n) {
-        *ok = periodic;
-        return periodic ? c - n : n - 1;
-    }
-    *ok = true;
-    return c;
-}
+__device__ __forceinline__ void cp_wait_pf() { cp_wait<PF - 1>(); }
+__device__ __forceinline__ void cp_wait0() { cp_wait<0>(); }
 
 template <int CK>
 struct Ring {
@@ -282,6 +243,227 @@ __global__ void __launch_bounds__(TILE_THREADS) k_spmv_staged(Grid3 g, const flo
     }
 }
 
+// ------------------------------------------------- search step + SpMV
+// Pipelined CG step: the new search direction p = z / sigma_z + beta p_old is
+// formed plane by plane over the tile with its 1-cell halo (halo values are
+// recomputed by the neighbouring tiles from the same inputs), written for the
+// tile, and q = A p, p . q follow one plane behind.  The solution update of
+// the previous step, x += alpha_prev p_old, rides along (the residual update
+// happens in the pre-smoothing pass).  At the start of a CG pass p = z / sigma_z
+// and x is left alone.  Staged vector rows span x0-4 .. x0+67 (16-byte
+// copies of four cells; nx must be a multiple of 4).
+namespace {
+constexpr int SW = PX + 8;             // 72 staged columns: x0-4 .. x0+67
+constexpr int SG = SW / 4;             // 18 four-cell groups per row
+constexpr int NSV = EH * SG;           // 180 vector copies per plane
+constexpr int NSX = TY * (PX / 4);     // 128 copies of the tile's x
+constexpr int NSC = CH * (PX + 1);     // 585 coefficient records
+}  // namespace
+// A step forms p on plane zA and q on plane zA-1 and stages plane zA+1;
+// ring sizes 2 and 4 let the z loop unroll four times with compile-time slots.
+struct SearchRing {
+    float4 c[4][CH][CW];   // planes zA-2 .. zA+1 (x0 .. x0+64, y0 .. y0+8)
+    float zt[2][EH][SW];   // planes zA .. zA+1 (y0-1 .. y0+8)
+    float po[2][EH][SW];
+    float xs[2][TY][PX];
+    float pn[4][EH][SW];   // planes zA-3 .. zA
+};
+
+__global__ void __launch_bounds__(TILE_THREADS) k_search_spmv(Grid3 g, const float4* __restrict__ coef,
+                                                              const float* __restrict__ zv,
+                                                              const float* __restrict__ p_old,
+                                                              float* __restrict__ p_new, float* __restrict__ xs,
+                                                              float* __restrict__ q, Scalars* sc, double* partials,
+                                                              int nblocks, int pidx_new) {
+    if (sc->converged) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto& S = *reinterpret_cast<SearchRing*>(smem_raw);
+    __shared__ double sh[8];
+    const bool first = sc->first != 0;
+    const float is = sc->inv_sigma_z, bt = sc->beta_f, ap = sc->alpha_f;
+    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * TY;
+    const int tx = threadIdx.x, ty = threadIdx.y, t = tx + TX * ty;
+    const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
+    const bool px = g.periodic & 1, py = g.periodic & 2, pz = (g.periodic & 4) != 0;
+    const long long sxy = (long long)g.nx * g.ny;
+    // copy descriptors
+    int voff = 0, xoff = 0, coff[3] = {0, 0, 0};
+    short vdst = -1, xdst = -1, cdst[3] = {-1, -1, -1};
+    bool vok = false, xok = false, cok[3] = {false, false, false};
+    if (t < NSV) {
+        const int row = t / SG, gi = t - row * SG;
+        bool okx, oky;
+        const int sx = axis_src(x0 - 4 + 4 * gi, g.nx, px, &okx);
+        const int sy = axis_src(y0 - 1 + row, g.ny, py, &oky);
+        vok = okx && oky;
+        voff = vok ? sx + g.nx * sy : 0;
+        vdst = (short)(row * SW + 4 * gi);
+    }
+    if (t < NSX) {
+        const int row = t / (PX / 4), gi = t - row * (PX / 4);
+        const int gx = x0 + 4 * gi, gy = y0 + row;
+        xok = gx < g.nx && gy < g.ny;
+        xoff = xok ? gx + g.nx * gy : 0;
+        xdst = (short)(row * PX + 4 * gi);
+    }
+#pragma unroll
+    for (int u = 0; u < 3; u++) {
+        const int k = t + u * TILE_THREADS;
+        if (k < NSC) {
+            const int row = k / (PX + 1), cx = k - row * (PX + 1);
+            bool okx, oky;
+            const int sx = axis_src(x0 + cx, g.nx, px, &okx);
+            const int sy = axis_src(y0 + row, g.ny, py, &oky);
+            cok[u] = okx && oky;
+            coff[u] = cok[u] ? sx + g.nx * sy : 0;
+            cdst[u] = (short)(row * CW + cx);
+        }
+    }
+    auto fetch = [&](int zz, int s2, int s4) {
+        bool okz;
+        const int sz = axis_src(zz, g.nz, pz, &okz);
+        const long long plane = (long long)sz * sxy;
+        if (vdst >= 0) {
+            const bool ok = vok && okz;
+            const long long o = ok ? plane + voff : 0;
+            cp_async16(&S.zt[s2][0][0] + vdst, zv + o, ok);
+            if (!first) cp_async16(&S.po[s2][0][0] + vdst, p_old + o, ok);
+        }
+        if (!first && xdst >= 0) {
+            const bool ok = xok && zz >= 0 && zz < g.nz;
+            cp_async16(&S.xs[s2][0][0] + xdst, xs + (ok ? plane + xoff : 0), ok);
+        }
+#pragma unroll
+        for (int u = 0; u < 3; u++)
+            if (cdst[u] >= 0) {
+                const bool ok = cok[u] && okz;
+                cp_async16(&S.c[s4][0][0] + cdst[u], coef + (ok ? plane + coff[u] : 0), ok);
+            }
+    };
+    // pair tasks over x0-2 .. x0+65, y0-1 .. y0+8: flat offsets, tile pairs'
+    // in-plane offsets (-1 off the tile) and their x staging offsets
+    constexpr int NT = EH * EP;
+    int toff[2] = {-1, -1}, town[2] = {-1, -1}, txo[2] = {0, 0};
+#pragma unroll
+    for (int u = 0; u < 2; u++) {
+        const int k = t + u * TILE_THREADS;
+        if (k < NT) {
+            const int row = k / EP, pc = k - row * EP;
+            toff[u] = row * SW + 2 + 2 * pc;
+            const int gx = x0 - 2 + 2 * pc, gy = y0 - 1 + row;
+            if (row >= 1 && row <= TY && pc >= 1 && pc <= TX && gx < g.nx && gy < g.ny) {
+                town[u] = gx + g.nx * gy;
+                txo[u] = (row - 1) * PX + 2 * pc - 2;
+            }
+        }
+    }
+    Acc acc;
+    const int ox = x0 + 2 * tx, oy = y0 + ty;
+    const bool own_inside = ox < g.nx && oy < g.ny;
+    const int oo = (ty + 1) * SW + 4 + 2 * tx, co = ty * CW + 2 * tx;
+    const long long og = ox + (long long)g.nx * oy;
+    auto step = [&](auto ph, int zA) {
+        constexpr int P = decltype(ph)::value;
+        fetch(zA + 1, (P + 1) & 1, (P + 1) & 3);
+        cp_commit();
+        cp_wait<1>();
+        __syncthreads();
+        {
+            const float* ZT = &S.zt[P & 1][0][0];
+            const float* PO = &S.po[P & 1][0][0];
+            const float* XS = &S.xs[P & 1][0][0];
+            float* PN = &S.pn[P][0][0];
+            const bool zin = zA >= z0 && zA < z1;
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int o = toff[u];
+                if (o < 0) break;
+                const float2 zz = *reinterpret_cast<const float2*>(ZT + o);
+                float2 pn, po = make_float2(0.f, 0.f);
+                if (first) {
+                    pn = make_float2(zz.x * is, zz.y * is);
+                } else {
+                    po = *reinterpret_cast<const float2*>(PO + o);
+                    pn = make_float2(fmaf(bt, po.x, zz.x * is), fmaf(bt, po.y, zz.y * is));
+                }
+                *reinterpret_cast<float2*>(PN + o) = pn;
+                if (zin && town[u] >= 0) {
+                    const long long i0 = town[u] + sxy * zA;
+                    *reinterpret_cast<float2*>(p_new + i0) = pn;
+                    if (!first) {
+                        const float2 xv = *reinterpret_cast<const float2*>(XS + txo[u]);
+                        *reinterpret_cast<float2*>(xs + i0) = make_float2(fmaf(ap, po.x, xv.x), fmaf(ap, po.y, xv.y));
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        const int z = zA - 1;
+        if (z >= z0 && z < z1 && own_inside) {
+            const float* Pc = &S.pn[(P + 3) & 3][0][0];
+            const float* PM = &S.pn[(P + 2) & 3][0][0];
+            const float* PP = &S.pn[P][0][0];
+            const float4* C = &S.c[(P + 3) & 3][0][0];
+            const float4* CN = &S.c[P][0][0];
+            float qv[2];
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const int o = oo + k, c = co + k;
+                const float4 cc = C[c];
+                const float bxh = C[c + 1].x, byh = C[c + CW].y, bzh = CN[c].z;
+                const float pc = Pc[o];
+                float v = cc.w * pc;
+                v = fmaf(cc.x, pc - Pc[o - 1], v);
+                v = fmaf(bxh, pc - Pc[o + 1], v);
+                v = fmaf(cc.y, pc - Pc[o - SW], v);
+                v = fmaf(byh, pc - Pc[o + SW], v);
+                v = fmaf(cc.z, pc - PM[o], v);
+                v = fmaf(bzh, pc - PP[o], v);
+                qv[k] = v;
+                acc.add_prod(pc, v);
+            }
+            *reinterpret_cast<float2*>(q + og + sxy * z) = make_float2(qv[0], qv[1]);
+        }
+        __syncthreads();
+    };
+    const int zs = z0 - 1, zend = z1;  // p over zs .. zend, q over z0 .. z1-1
+    fetch(zs, 0, 0);
+    cp_commit();
+    for (int zA = zs;;) {
+        step(std::integral_constant<int, 0>{}, zA);
+        if (++zA > zend) break;
+        step(std::integral_constant<int, 1>{}, zA);
+        if (++zA > zend) break;
+        step(std::integral_constant<int, 2>{}, zA);
+        if (++zA > zend) break;
+        step(std::integral_constant<int, 3>{}, zA);
+        if (++zA > zend) break;
+    }
+    cp_wait0();
+    double v1[1] = {acc.total()};
+    block_sum<1>(v1, sh);
+    if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[10])) {
+        double tot[1];
+        finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[10]);
+        if (t == 0) {
+            const double pq = tot[0];
+            sc->pq = pq;
+            if (!(pq > 0.0) || !isfinite(pq)) {
+                sc->breakdown = 1;
+                if (!isfinite(pq)) sc->nonfinite = 1;
+                sc->converged = 1;
+                sc->alpha = 0.0;
+                sc->alpha_f = 0.0f;
+            } else {
+                sc->alpha = sc->rz / pq;
+                sc->alpha_f = (float)sc->alpha;
+            }
+            sc->first = 0;
+            sc->pidx = pidx_new;
+        }
+    }
+}
+
 // ------------------------------------------------------- smoother half-step
 // Fine level: rhs = sigma * r (FP32), correction z (FP32), coefficients in the
 // level precision.  ZERO: first half-step from zero (no vector staging).  The
@@ -413,7 +595,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_restrict_staged(Grid3 g, Grid3
 namespace {
 int g_sms = 0;
 int g_occ[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-enum { OCC_SPMV = 0, OCC_SMOOTH_F32, OCC_SMOOTH_LO, OCC_RESTRICT_F32, OCC_RESTRICT_LO };
+enum { OCC_SPMV = 0, OCC_SMOOTH_F32, OCC_SMOOTH_LO, OCC_RESTRICT_F32, OCC_RESTRICT_LO, OCC_SEARCH };
 }  // namespace
 
 static Launch pair_launch(const Launch& L, int occ_kind) {
@@ -454,6 +636,13 @@ void launch_spmv_staged(const Launch& L, const Fields& F, cudaStream_t s) {
     k_spmv_staged<<<P.grid, P.block, sizeof(Ring<0>), s>>>(P.g, F.coef, F.p, F.q, F.sc, F.partials, P.nblocks);
 }
 
+void launch_search_spmv(const Launch& L, const float4* coef, const float* z, const float* p_old, float* p_new,
+                        float* x, float* q, Scalars* sc, double* partials, int pidx_new, cudaStream_t s) {
+    const Launch P = pair_launch(L, OCC_SEARCH);
+    k_search_spmv<<<P.grid, P.block, sizeof(SearchRing), s>>>(P.g, coef, z, p_old, p_new, x, q, sc, partials,
+                                                              P.nblocks, pidx_new);
+}
+
 template <int CK>
 static void smooth_staged_impl(const Launch& L, const void* coef, const float* r, float* e, float* tmp, int color,
                                bool zero, bool out_of_place, const Scalars* sc, cudaStream_t s) {
@@ -489,6 +678,7 @@ cudaError_t staged_prepare_attributes() {
         if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     };
     set((const void*)k_spmv_staged, sizeof(Ring<0>));
+    set((const void*)k_search_spmv, sizeof(SearchRing));
     set((const void*)k_smooth_staged<0, true, false>, sizeof(Ring<0>));
     set((const void*)k_smooth_staged<0, false, false>, sizeof(Ring<0>));
     set((const void*)k_smooth_staged<0, false, true>, sizeof(Ring<0>));
@@ -509,6 +699,7 @@ cudaError_t staged_prepare_attributes() {
         if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_occ[kind], fn, TILE_THREADS, bytes);
     };
     occ(OCC_SPMV, (const void*)k_spmv_staged, sizeof(Ring<0>));
+    occ(OCC_SEARCH, (const void*)k_search_spmv, sizeof(SearchRing));
     occ(OCC_SMOOTH_F32, (const void*)k_smooth_staged<0, false, false>, sizeof(Ring<0>));
     occ(OCC_SMOOTH_LO, (const void*)k_smooth_staged<1, false, false>, sizeof(Ring<1>));
     occ(OCC_RESTRICT_F32, (const void*)k_restrict_staged<0, float>, sizeof(Ring<0>));

@@ -1,0 +1,810 @@
+// fused_kernels.cu -- the multigrid V-cycle's per-level work in two passes
+// over HBM instead of six.
+//
+// Pre-smoothing pass (k_presmooth_restrict), per level:
+//   [fine level, inside CG] r <- r - alpha q       (the CG residual update)
+//   red half-step from a zero correction            e_red   = sigma r / d
+//   black half-step                                 e_black = (sigma r + sum beta e_red) / d
+//   residual and restriction                        rc      = 1/4 P^T (sigma r - A e)
+// Post-smoothing pass (k_prolong_postsmooth), per level:
+//   prolongation                                    e <- e + w P ec
+//   black half-step, then red half-step             z       = the smoothed correction
+//   [fine level] r . z for the CG step length.
+// Both march a 64 x 8 (x, y) tile along z.  The stages of one pass run as a
+// pipeline over planes: the pre-smoothing pass forms the residual and the red
+// values of plane z, the black values of plane z-1 and the restricted
+// residual of plane z-2 in the same step, so every input plane is read from
+// HBM once.  A stage needs its neighbours' results, so each stage runs on a
+// region one cell wider than the next: the red values cover the tile with a
+// 2-cell halo, the black values a 1-cell halo, the residual the tile itself.
+// Halo cells are recomputed by both neighbouring tiles from the same inputs
+// in the same order, so the values agree bit for bit.  Inputs are staged with
+// zero-filling 16-byte cp.async two planes ahead of the red stage; a staged
+// row spans x0-4 .. x0+67 so every copy is a 16-byte-aligned group of cells.
+//
+// The smoother reads per-cell records (beta_x, beta_y, beta_z of the low
+// faces, diagonal) prepared once per coefficient set, the diagonal rounded
+// up to the record precision: the level operator stays diagonally dominant,
+// so the V-cycle stays a fixed symmetric positive definite operator.
+// Requirements: nx a multiple of 4 and even extents on periodic axes.
+#include <algorithm>
+#include <cmath>
+#include <type_traits>
+
+#include "kernels.h"
+#include "staged.cuh"
+
+namespace mhdproj {
+
+namespace {
+using namespace staged;
+
+constexpr int PX = 2 * TX;       // 64 cells per tile row
+constexpr int XO = 4;            // staged rows start at x0 - XO
+constexpr int RW = PX + 2 * XO;  // 72 staged columns: x0-4 .. x0+67
+constexpr int RH = TY + 4;       // vector rows:  y0-2 .. y0+9
+constexpr int CH = TY + 5;       // record rows:  y0-2 .. y0+10
+constexpr int NG = RW / 4;       // 18 four-cell groups per staged row
+constexpr int NVEC = RH * NG;    // 216 vector copies per plane
+constexpr int RP = (PX + 4) / 2; // 34 pairs of the 2-halo region (x0-2 .. x0+65)
+constexpr int NRED = RH * RP;    // 408 red-stage pair tasks
+constexpr int NBLK = (TY + 2) * RP;  // 340 black-stage pair tasks (rows y0-1 .. y0+8)
+static_assert(NVEC <= TILE_THREADS, "one vector copy per thread");
+static_assert(NRED <= 2 * TILE_THREADS && NBLK <= 2 * TILE_THREADS, "two tasks per thread");
+
+template <class VT> __device__ __forceinline__ float2 ld2(const VT* p);
+template <> __device__ __forceinline__ float2 ld2<float>(const float* p) { return *reinterpret_cast<const float2*>(p); }
+template <> __device__ __forceinline__ float2 ld2<__half>(const __half* p) {
+    return __half22float2(*reinterpret_cast<const __half2*>(p));
+}
+template <> __device__ __forceinline__ float2 ld2<__nv_bfloat16>(const __nv_bfloat16* p) {
+    return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p));
+}
+template <class VT> __device__ __forceinline__ void st2(VT* p, float2 v);
+template <> __device__ __forceinline__ void st2<float>(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+template <> __device__ __forceinline__ void st2<__half>(__half* p, float2 v) {
+    *reinterpret_cast<__half2*>(p) = __floats2half2_rn(v.x, v.y);
+}
+template <> __device__ __forceinline__ void st2<__nv_bfloat16>(__nv_bfloat16* p, float2 v) {
+    *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(v.x, v.y);
+}
+// 16-byte (FP32) or 8-byte (FP16/BF16) copy of four consecutive cells.
+template <class VT>
+__device__ __forceinline__ void cp_async_quad(void* smem, const VT* gmem, bool valid) {
+    if (sizeof(VT) == 4) cp_async16(smem, gmem, valid);
+    else cp_async8(smem, gmem, valid);
+}
+
+// A thread's share of one plane's copies, resolved once per block: one
+// four-cell group of the vector rows (12 rows x 18 groups) and two (8-byte
+// records) or four (16-byte records) 16-byte copies of the record rows
+// (13 rows x 72 records).
+template <int CK>
+struct RegionFetch {
+    using CT = typename CoefStore<CK>::T;
+    static constexpr int RPC = (CK == 0) ? 1 : 2;  // records per 16-byte copy
+    static constexpr int NCT = (CK == 0) ? 4 : 2;
+    static constexpr int NCTOT = CH * (RW / RPC);
+    static_assert(NCTOT <= NCT * TILE_THREADS, "record copies per thread");
+    int voff, coff[NCT];
+    short vdst, cdst[NCT];
+    bool vok, cok[NCT];
+    long long sxy;
+    int nz;
+    bool pz;
+
+    __device__ __forceinline__ RegionFetch(const Grid3& g, int x0, int y0, int t) {
+        sxy = (long long)g.nx * g.ny;
+        nz = g.nz;
+        pz = (g.periodic & 4) != 0;
+        const bool px = g.periodic & 1, py = g.periodic & 2;
+        vdst = -1;
+        vok = false;
+        voff = 0;
+        if (t < NVEC) {
+            const int row = t / NG, gi = t - row * NG;
+            bool okx, oky;
+            const int sx = axis_src(x0 - XO + 4 * gi, g.nx, px, &okx);
+            const int sy = axis_src(y0 - 2 + row, g.ny, py, &oky);
+            vok = okx && oky;
+            voff = vok ? sx + g.nx * sy : 0;
+            vdst = (short)(row * RW + 4 * gi);
+        }
+#pragma unroll
+        for (int j = 0; j < NCT; j++) {
+            const int k = t + j * TILE_THREADS;
+            cdst[j] = -1;
+            cok[j] = false;
+            coff[j] = 0;
+            if (k < NCTOT) {
+                const int per = RW / RPC;
+                const int row = k / per, ci = k - row * per;
+                bool okx, oky;
+                const int sx = axis_src(x0 - XO + RPC * ci, g.nx, px, &okx);
+                const int sy = axis_src(y0 - 2 + row, g.ny, py, &oky);
+                cok[j] = okx && oky;
+                coff[j] = cok[j] ? sx + g.nx * sy : 0;
+                cdst[j] = (short)(row * RW + RPC * ci);
+            }
+        }
+    }
+    __device__ __forceinline__ long long plane(int zz, bool* okz) const {
+        const int sz = axis_src(zz, nz, pz, okz);
+        return (long long)sz * sxy;
+    }
+    template <class VA>
+    __device__ __forceinline__ void vec(VA* dst, const VA* src, long long pl, bool okz) const {
+        if (vdst >= 0) {
+            const bool ok = vok && okz;
+            cp_async_quad<VA>(dst + vdst, src + (ok ? pl + voff : 0), ok);
+        }
+    }
+    __device__ __forceinline__ void recs(CT* dst, const CT* src, long long pl, bool okz) const {
+#pragma unroll
+        for (int j = 0; j < NCT; j++)
+            if (cdst[j] >= 0) {
+                const bool ok = cok[j] && okz;
+                cp_async16(dst + cdst[j], src + (ok ? pl + coff[j] : 0), ok);
+            }
+    }
+};
+
+// sum of beta * e over the six neighbours added to acc, in the per-cell
+// kernels' order; *d = the cell's diagonal.  Flat offset o into [rows][RW]
+// planes; c/cn: record planes z, z+1; e/em/ep: correction planes z, z-1, z+1.
+template <int CK, class CT>
+__device__ __forceinline__ float gs_sum(const CT* c, const CT* cn, const float* e, const float* em, const float* ep,
+                                        int o, float acc, float* d) {
+    const float4 own = unpack<CK>(c[o]);
+    const float bxh = unpack<CK>(c[o + 1]).x;
+    const float byh = unpack<CK>(c[o + RW]).y;
+    const float bzh = unpack<CK>(cn[o]).z;
+    acc = fmaf(own.x, e[o - 1], acc);
+    acc = fmaf(bxh, e[o + 1], acc);
+    acc = fmaf(own.y, e[o - RW], acc);
+    acc = fmaf(byh, e[o + RW], acc);
+    acc = fmaf(own.z, em[o], acc);
+    acc = fmaf(bzh, ep[o], acc);
+    *d = own.w;
+    return acc;
+}
+
+// A thread's pair tasks of the red (2-halo) and black (1-halo) stages,
+// resolved once per block: flat offsets of the pair's first cell, the colour
+// parity of its row, and for red tasks on the tile the in-plane offset of the
+// pair (-1 otherwise).  Black tasks at the region's x edges update only the
+// member inside the 1-halo.
+struct PairTasks {
+    int roff[2], rpar[2], rown[2];
+    int boff[2], bpar[2], bedge[2];
+    __device__ __forceinline__ PairTasks(const Grid3& g, int x0, int y0, int t) {
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int k = t + u * TILE_THREADS;
+            roff[u] = -1;
+            rpar[u] = 0;
+            rown[u] = -1;
+            if (k < NRED) {
+                const int row = k / RP, pc = k - row * RP;
+                roff[u] = row * RW + 2 + 2 * pc;
+                rpar[u] = (y0 - 2 + row) & 1;
+                const int gx = x0 - 2 + 2 * pc, gy = y0 - 2 + row;
+                if (row >= 2 && row < TY + 2 && pc >= 1 && pc <= TX && gx < g.nx && gy < g.ny) rown[u] = gx + g.nx * gy;
+            }
+            boff[u] = -1;
+            bpar[u] = 0;
+            bedge[u] = 0;
+            if (k < NBLK) {
+                const int rr = k / RP, pc = k - rr * RP, row = rr + 1;
+                boff[u] = row * RW + 2 + 2 * pc;
+                bpar[u] = (1 + y0 - 2 + row) & 1;
+                bedge[u] = pc == 0 ? 1 : (pc == RP - 1 ? 2 : 0);
+            }
+        }
+    }
+    // black member of black task u at plane z, or -1 when it lies outside the 1-halo
+    __device__ __forceinline__ int black(int u, int z) const {
+        const int m = (bpar[u] + z) & 1;
+        if ((bedge[u] == 1 && m == 0) || (bedge[u] == 2 && m == 1)) return -1;
+        return boff[u] + m;
+    }
+};
+
+// Plane rings.  A step handles planes zA (red / prolongation stage), zA-1
+// (black stage) and zA-2 (tile stage) and stages plane zA+1 for the next
+// step; ring sizes are 2 or 4, so the z loop is unrolled four times and
+// every slot is a compile-time offset.
+template <int CK, class VT, bool UPDATE>
+struct PreRing {
+    using CT = typename CoefStore<CK>::T;
+    CT c[4][CH][RW];                 // records, planes zA-2 .. zA+1
+    VT rin[2][RH][RW];               // residual in, planes zA .. zA+1
+    float q[UPDATE ? 2 : 1][RH][RW];
+    float rn[2][RH][RW];             // updated residual, planes zA-1 .. zA
+    float er[4][RH][RW];             // correction, planes zA-3 .. zA
+    float ypart[TY][TX];
+};
+template <int CK, class VT>
+struct PostRing {
+    using CT = typename CoefStore<CK>::T;
+    CT c[4][CH][RW];                 // records, planes zA-2 .. zA+1
+    VT rr[4][RH][RW];                // right-hand side, planes zA-2 .. zA+1
+    VT eo[2][RH][RW];                // pre-smoothed correction, planes zA .. zA+1
+    float ep[4][RH][RW];             // prolonged / smoothed correction, planes zA-3 .. zA
+};
+template <int N>
+using Phase = std::integral_constant<int, N>;
+}  // namespace
+
+// ------------------------------------------------------ pre-smoothing pass
+// Level residual rin (VT) -> correction e (VT, own cells) and the coarse
+// residual rc.  UPDATE (finest level inside CG): the residual is first
+// updated, r_out = rin - alpha q, written for the tile's cells, and ||r_out||^2
+// decides convergence.  FINE: the right-hand side is sigma * r.
+// After the two half-steps the residual of a black cell is zero (its update
+// solves its own equation) and that of a red cell is sum beta * e over its
+// black neighbours (its red value solved the equation with them at zero), so
+// the restriction sums those neighbour terms over the red cells.
+template <int CK, class VT, class VTc, bool UPDATE, bool FINE>
+__global__ void __launch_bounds__(TILE_THREADS) k_presmooth_restrict(Grid3 g, Grid3 gc, const void* __restrict__ sm_v,
+                                                                     const VT* __restrict__ rin,
+                                                                     const float* __restrict__ q,
+                                                                     float* __restrict__ r_out, VT* __restrict__ e,
+                                                                     VTc* __restrict__ rc, Scalars* sc,
+                                                                     double* partials, int nblocks) {
+    if (sc->converged) return;
+    using CT = typename CoefStore<CK>::T;
+    const CT* sm = reinterpret_cast<const CT*>(sm_v);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto& S = *reinterpret_cast<PreRing<CK, VT, UPDATE>*>(smem_raw);
+    __shared__ double sh[8];
+    const float sigma = FINE ? sc->sigma : 1.0f;
+    const float alpha = UPDATE ? sc->alpha_f : 0.0f;
+    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * TY;
+    const int tx = threadIdx.x, ty = threadIdx.y, t = tx + TX * ty;
+    const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
+    const RegionFetch<CK> F(g, x0, y0, t);
+    const PairTasks T(g, x0, y0, t);
+    const long long sxy = (long long)g.nx * g.ny;
+    Acc acc;
+    float part = 0.f;
+    const int ox = x0 + 2 * tx, oy = y0 + ty;  // the thread's own pair
+    const bool own_inside = ox < g.nx && oy < g.ny;
+    const int oo = (ty + 2) * RW + XO + 2 * tx;  // its flat offset
+    const long long og = ox + (long long)g.nx * oy;
+    auto fetch = [&](int zz, int c4, int v2) {
+        bool okz;
+        const long long pl = F.plane(zz, &okz);
+        F.recs(&S.c[c4][0][0], sm, pl, okz);
+        F.vec(&S.rin[v2][0][0], rin, pl, okz);
+        if (UPDATE) F.vec(&S.q[v2][0][0], q, pl, okz);
+    };
+    auto step = [&](auto ph, int zA) {
+        constexpr int P = decltype(ph)::value;
+        fetch(zA + 1, (P + 1) & 3, (P + 1) & 1);
+        cp_commit();
+        cp_wait<1>();
+        __syncthreads();
+        // ---- red stage: plane zA over the 2-halo region
+        {
+            const VT* RI = &S.rin[P & 1][0][0];
+            const float* Q = &S.q[UPDATE ? (P & 1) : 0][0][0];
+            const CT* C = &S.c[P][0][0];
+            float* RN = &S.rn[P & 1][0][0];
+            float* ER = &S.er[P][0][0];
+            const bool zin = zA >= z0 && zA < z1;
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int o = T.roff[u];
+                if (o < 0) break;
+                const float2 rv = ld2<VT>(RI + o);
+                float2 rn = rv;
+                if (UPDATE) {
+                    const float2 qv = *reinterpret_cast<const float2*>(Q + o);
+                    rn = make_float2(fmaf(-alpha, qv.x, rv.x), fmaf(-alpha, qv.y, rv.y));
+                }
+                const int m = (T.rpar[u] + zA) & 1;  // pair member of colour 0 (x0 even)
+                const float d = unpack<CK>(C[o + m]).w;
+                const float ev = d > 0.f ? __fdividef(sigma * (m ? rn.y : rn.x), d) : 0.f;
+                *reinterpret_cast<float2*>(RN + o) = rn;
+                *reinterpret_cast<float2*>(ER + o) = m ? make_float2(0.f, ev) : make_float2(ev, 0.f);
+                if (UPDATE && zin && T.rown[u] >= 0) {
+                    *reinterpret_cast<float2*>(r_out + T.rown[u] + sxy * zA) = rn;
+                    acc.add_prod(rn.x, rn.x);
+                    acc.add_prod(rn.y, rn.y);
+                }
+            }
+        }
+        __syncthreads();
+        // ---- black stage: plane zA-1 over the 1-halo region, in place
+        const int zB = zA - 1;
+        if (zB >= z0 - 1) {
+            const CT* C = &S.c[(P + 3) & 3][0][0];
+            const CT* CN = &S.c[P][0][0];
+            const float* RN = &S.rn[(P + 1) & 1][0][0];
+            float* E = &S.er[(P + 3) & 3][0][0];
+            const float* EM = &S.er[(P + 2) & 3][0][0];
+            const float* EP = &S.er[P][0][0];
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int o = T.black(u, zB);
+                if (o < 0) continue;
+                float d;
+                const float s = gs_sum<CK>(C, CN, E, EM, EP, o, sigma * RN[o], &d);
+                E[o] = d > 0.f ? __fdividef(s, d) : 0.f;
+            }
+        }
+        __syncthreads();
+        // ---- correction out and restriction: plane zA-2 over the tile
+        const int zC = zA - 2;
+        if (zC >= z0 && zC < z1) {
+            const CT* C = &S.c[(P + 2) & 3][0][0];
+            const CT* CN = &S.c[(P + 3) & 3][0][0];
+            const float* E = &S.er[(P + 2) & 3][0][0];
+            const float* EM = &S.er[(P + 1) & 3][0][0];
+            const float* EP = &S.er[(P + 3) & 3][0][0];
+            const int m = (y0 + ty + zC) & 1;  // red member of the own pair
+            float d;
+            part += gs_sum<CK>(C, CN, E, EM, EP, oo + m, 0.f, &d);
+            if (own_inside) st2<VT>(e + og + sxy * zC, *reinterpret_cast<const float2*>(E + oo));
+            if (((zC - z0) & 1) || zC + 1 == z1) {
+                S.ypart[ty][tx] = part;
+                __syncthreads();
+                if (own_inside && !(ty & 1)) {
+                    const float tot = part + S.ypart[ty + 1][tx];
+                    rc[(ox >> 1) + (long long)gc.nx * ((oy >> 1) + (long long)gc.ny * (zC >> 1))] =
+                        from_f<VTc>(0.25f * tot);
+                }
+                part = 0.f;
+            }
+        }
+        __syncthreads();
+    };
+    const int zs = z0 - 2, zend = z1 + 1;  // red stage over zs .. zend
+    fetch(zs, 0, 0);
+    cp_commit();
+    for (int zA = zs;;) {
+        step(Phase<0>{}, zA);
+        if (++zA > zend) break;
+        step(Phase<1>{}, zA);
+        if (++zA > zend) break;
+        step(Phase<2>{}, zA);
+        if (++zA > zend) break;
+        step(Phase<3>{}, zA);
+        if (++zA > zend) break;
+    }
+    cp_wait<0>();
+    if (UPDATE) {
+        double v1[1] = {acc.total()};
+        block_sum<1>(v1, sh);
+        if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[8])) {
+            double tot[1];
+            finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[8]);
+            if (t == 0) {
+                const double rr = tot[0];
+                sc->rr = rr;
+                sc->iterations += 1;
+                sc->total_iterations += 1;
+                if (!isfinite(rr)) {
+                    sc->nonfinite = 1;
+                    sc->converged = 1;
+                } else if (rr <= sc->rr_target || sc->total_iterations >= sc->max_total) {
+                    sc->converged = 1;
+                }
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------- post-smoothing pass
+// e (pre-smoothed, VT) + w * P ec -> black, red half-steps -> out (VT).  DOT
+// (finest level): r . out / sigma gives rz and beta; the next V-cycle's sigma
+// is then taken from ||r||^2.
+template <int CK, class VT, class VTc, bool DOT, bool FINE>
+__global__ void __launch_bounds__(TILE_THREADS) k_prolong_postsmooth(Grid3 g, Grid3 gc, const void* __restrict__ sm_v,
+                                                                     const VT* __restrict__ e,
+                                                                     const VTc* __restrict__ ec,
+                                                                     const VT* __restrict__ r, VT* __restrict__ out,
+                                                                     float w, Scalars* sc, double* partials,
+                                                                     int nblocks, long long n_active) {
+    if (sc->converged) return;
+    using CT = typename CoefStore<CK>::T;
+    const CT* sm = reinterpret_cast<const CT*>(sm_v);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    auto& S = *reinterpret_cast<PostRing<CK, VT>*>(smem_raw);
+    __shared__ double sh[8];
+    const float sigma = FINE ? sc->sigma : 1.0f;
+    const float is = FINE ? sc->inv_sigma : 1.0f;
+    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * TY;
+    const int tx = threadIdx.x, ty = threadIdx.y, t = tx + TX * ty;
+    const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
+    const RegionFetch<CK> F(g, x0, y0, t);
+    const PairTasks T(g, x0, y0, t);
+    const long long sxy = (long long)g.nx * g.ny;
+    // Coarse parents of the red-stage pairs: in-plane offsets, validity.
+    int pofs[2];
+    bool pok[2];
+    {
+        const bool px = g.periodic & 1, py = g.periodic & 2;
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int k = t + u * TILE_THREADS;
+            pofs[u] = 0;
+            pok[u] = false;
+            if (k < NRED) {
+                const int row = k / RP, pc = k - row * RP;
+                bool okx, oky;
+                const int sx = axis_src(x0 - 2 + 2 * pc, g.nx, px, &okx);
+                const int sy = axis_src(y0 - 2 + row, g.ny, py, &oky);
+                pok[u] = okx && oky;
+                pofs[u] = pok[u] ? (sx >> 1) + gc.nx * (sy >> 1) : 0;
+            }
+        }
+    }
+    const long long csxy = (long long)gc.nx * gc.ny;
+    auto parents = [&](int zz, float* v) {
+        bool okz;
+        const int sz = axis_src(zz, g.nz, (g.periodic & 4) != 0, &okz);
+        const long long cpl = (long long)(sz >> 1) * csxy;
+#pragma unroll
+        for (int u = 0; u < 2; u++) v[u] = (pok[u] && okz) ? to_f(__ldg(ec + cpl + pofs[u])) : 0.f;
+    };
+    auto fetch = [&](int zz, int c4, int v2) {
+        bool okz;
+        const long long pl = F.plane(zz, &okz);
+        F.recs(&S.c[c4][0][0], sm, pl, okz);
+        F.vec(&S.rr[c4][0][0], r, pl, okz);
+        F.vec(&S.eo[v2][0][0], e, pl, okz);
+    };
+    float pc_cur[2], pc_nxt[2];
+    Acc acc;
+    const int ox = x0 + 2 * tx, oy = y0 + ty;
+    const bool own_inside = ox < g.nx && oy < g.ny;
+    const int oo = (ty + 2) * RW + XO + 2 * tx;
+    const long long og = ox + (long long)g.nx * oy;
+    auto step = [&](auto ph, int zA) {
+        constexpr int P = decltype(ph)::value;
+        fetch(zA + 1, (P + 1) & 3, (P + 1) & 1);
+        cp_commit();
+        parents(zA + 1, pc_nxt);  // consumed one step later
+        cp_wait<1>();
+        __syncthreads();
+        // ---- prolongation: plane zA over the 2-halo region
+        {
+            const VT* EO = &S.eo[P & 1][0][0];
+            float* EP = &S.ep[P][0][0];
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int o = T.roff[u];
+                if (o < 0) break;
+                const float2 ev = ld2<VT>(EO + o);
+                const float cv = pc_cur[u];
+                *reinterpret_cast<float2*>(EP + o) = make_float2(fmaf(w, cv, ev.x), fmaf(w, cv, ev.y));
+            }
+        }
+        __syncthreads();
+        // ---- black half-step: plane zA-1 over the 1-halo region, in place
+        const int zB = zA - 1;
+        if (zB >= z0 - 1) {
+            const CT* C = &S.c[(P + 3) & 3][0][0];
+            const CT* CN = &S.c[P][0][0];
+            const VT* RR = &S.rr[(P + 3) & 3][0][0];
+            float* E = &S.ep[(P + 3) & 3][0][0];
+            const float* EM = &S.ep[(P + 2) & 3][0][0];
+            const float* EP = &S.ep[P][0][0];
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int o = T.black(u, zB);
+                if (o < 0) continue;
+                float d;
+                const float s = gs_sum<CK>(C, CN, E, EM, EP, o, sigma * to_f(RR[o]), &d);
+                E[o] = d > 0.f ? __fdividef(s, d) : 0.f;
+            }
+        }
+        __syncthreads();
+        // ---- red half-step: plane zA-2 over the tile, out = z
+        const int zC = zA - 2;
+        if (zC >= z0 && zC < z1) {
+            const CT* C = &S.c[(P + 2) & 3][0][0];
+            const CT* CN = &S.c[(P + 3) & 3][0][0];
+            const VT* RR = &S.rr[(P + 2) & 3][0][0];
+            const float* E = &S.ep[(P + 2) & 3][0][0];
+            const float* EM = &S.ep[(P + 1) & 3][0][0];
+            const float* EP = &S.ep[(P + 3) & 3][0][0];
+            const int m = (y0 + ty + zC) & 1;  // the pair member of colour 0
+            const float2 rv = ld2<VT>(RR + oo);
+            float d;
+            const float s = gs_sum<CK>(C, CN, E, EM, EP, oo + m, sigma * (m ? rv.y : rv.x), &d);
+            const float zr = d > 0.f ? __fdividef(s, d) : 0.f;
+            const float zb = E[oo + 1 - m];
+            const float2 zv = m ? make_float2(zb, zr) : make_float2(zr, zb);
+            if (own_inside) {
+                st2<VT>(out + og + sxy * zC, zv);
+                if (DOT) {
+                    acc.add_prod(rv.x, zv.x * is);
+                    acc.add_prod(rv.y, zv.y * is);
+                }
+            }
+        }
+        __syncthreads();
+        pc_cur[0] = pc_nxt[0];
+        pc_cur[1] = pc_nxt[1];
+    };
+    const int zs = z0 - 2, zend = z1 + 1;
+    fetch(zs, 0, 0);
+    cp_commit();
+    parents(zs, pc_cur);
+    for (int zA = zs;;) {
+        step(Phase<0>{}, zA);
+        if (++zA > zend) break;
+        step(Phase<1>{}, zA);
+        if (++zA > zend) break;
+        step(Phase<2>{}, zA);
+        if (++zA > zend) break;
+        step(Phase<3>{}, zA);
+        if (++zA > zend) break;
+    }
+    cp_wait<0>();
+    if (DOT) {
+        double v1[1] = {acc.total()};
+        block_sum<1>(v1, sh);
+        if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[9])) {
+            double tot[1];
+            finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[9]);
+            if (t == 0) {
+                const double rz = tot[0];
+                if (!isfinite(rz)) {
+                    sc->nonfinite = 1;
+                    sc->converged = 1;
+                } else if (!(rz > 0.0)) {
+                    sc->breakdown = 1;
+                    sc->converged = 1;
+                } else if (sc->first) {
+                    sc->rz = rz;
+                    sc->beta = 0.0;
+                    sc->beta_f = 0.0f;
+                } else {
+                    sc->beta = rz / sc->rz;
+                    sc->beta_f = (float)sc->beta;
+                    sc->rz = rz;
+                }
+                // z is in units of this V-cycle's sigma; the next V-cycle
+                // scales by the RMS of the residual it will be given.
+                sc->inv_sigma_z = sc->inv_sigma;
+                set_sigma_from(sc, sc->rr, n_active);
+            }
+        }
+    }
+}
+
+// --------------------------------------------------- smoother records
+// (beta_x, beta_y, beta_z, diagonal) per cell from the level's coefficient
+// records (beta_x, beta_y, beta_z, reaction); the diagonal is the FP32 sum of
+// the record-precision values, rounded up to the record precision.
+template <int CK>
+__global__ void __launch_bounds__(TILE_THREADS) k_smoother_records(Grid3 g, const void* __restrict__ coef_v,
+                                                                   void* __restrict__ sm_v) {
+    using CT = typename CoefStore<CK>::T;
+    const CT* coef = reinterpret_cast<const CT*>(coef_v);
+    CT* sm = reinterpret_cast<CT*>(sm_v);
+    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
+    if (x >= g.nx || y >= g.ny) return;
+    const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    for (int z = z0; z < z1; z++) {
+        const long long i = x + sy * y + sz * z;
+        const float4 c = unpack<CK>(coef[i]);
+        const int xp = wrap_or_neg(x + 1, g.nx, g.periodic & 1);
+        const int yp = wrap_or_neg(y + 1, g.ny, g.periodic & 2);
+        const int zp = wrap_or_neg(z + 1, g.nz, g.periodic & 4);
+        const float bxh = xp >= 0 ? unpack<CK>(coef[xp + sy * y + sz * z]).x : 0.f;
+        const float byh = yp >= 0 ? unpack<CK>(coef[x + sy * yp + sz * z]).y : 0.f;
+        const float bzh = zp >= 0 ? unpack<CK>(coef[x + sy * y + sz * zp]).z : 0.f;
+        const float d = ((c.x + bxh) + (c.y + byh)) + ((c.z + bzh) + c.w);
+        CT out;
+        if (CK == 0) {
+            reinterpret_cast<float4&>(out) = make_float4(c.x, c.y, c.z, d);
+        } else {
+            // the three betas are exact in the record precision already
+            uint2 u = reinterpret_cast<const uint2&>(coef[i]);
+            unsigned short dh;
+            if (CK == 1) {
+                const __half h = __float2half_ru(d);
+                dh = *reinterpret_cast<const unsigned short*>(&h);
+            } else {
+                const __nv_bfloat16 h = __float2bfloat16_ru(d);
+                dh = *reinterpret_cast<const unsigned short*>(&h);
+            }
+            u.y = (u.y & 0x0000ffffu) | ((unsigned)dh << 16);
+            reinterpret_cast<uint2&>(out) = u;
+        }
+        sm[i] = out;
+    }
+}
+
+// ------------------------------------------------------------ launchers
+namespace {
+int f_sms = 0;
+int f_occ[12] = {};
+enum { O_PRE_F32 = 0, O_PRE_LO, O_PRE_LO_UPD, O_PRE_F32_UPD, O_PRE_COARSE, O_POST_F32, O_POST_LO, O_POST_COARSE };
+
+// Even z runs chosen so the grid fills whole waves of resident blocks; each
+// run also computes two planes below and above it.
+Launch fused_launch(const Grid3& g0, int occ_kind) {
+    Launch P;
+    P.g = g0;
+    P.block = dim3(TX, TY, 1);
+    const int gx = (g0.nx + PX - 1) / PX, gy = (g0.ny + TY - 1) / TY, nz = g0.nz;
+    const int tiles = gx * gy;
+    const int cap = (f_sms > 0 ? f_sms : 152) * (f_occ[occ_kind] > 0 ? f_occ[occ_kind] : 1);
+    int best_zper = nz + (nz & 1), best_zc = 1;
+    double best = -1.0;
+    for (int zc = 1; zc <= nz; zc++) {
+        int zper = (nz + zc - 1) / zc;
+        if (zper & 1) zper++;
+        if (zper < 4 && zc > 1) break;
+        const int zcr = (nz + zper - 1) / zper;
+        const long long blocks = (long long)tiles * zcr;
+        if (blocks > MAX_REDUCE_BLOCKS) break;
+        const double waves = (double)blocks / cap;
+        const double score = waves / std::ceil(waves) * ((double)zper / (zper + 4));
+        if (score > best) {
+            best = score;
+            best_zper = zper;
+            best_zc = zcr;
+        }
+    }
+    P.grid = dim3(gx, gy, best_zc);
+    P.g.zper = best_zper;
+    P.nblocks = tiles * best_zc;
+    return P;
+}
+}  // namespace
+
+bool fused_supported(const Grid3& g) {
+    if (g.nx % 4) return false;
+    for (int a = 0; a < 3; a++) {
+        const int n = a == 0 ? g.nx : (a == 1 ? g.ny : g.nz);
+        if ((g.periodic & (1 << a)) && (n & 1)) return false;
+    }
+    return true;
+}
+
+template <int CK, class VT, class VTc, bool UPDATE, bool FINE>
+static void pre_impl(const Grid3& g, const Grid3& gc, const void* sm, const void* rin, const float* q, float* r_out,
+                     void* e, void* rc, Scalars* sc, double* partials, int occ_kind, cudaStream_t s) {
+    const Launch P = fused_launch(g, occ_kind);
+    k_presmooth_restrict<CK, VT, VTc, UPDATE, FINE><<<P.grid, P.block, sizeof(PreRing<CK, VT, UPDATE>), s>>>(
+        P.g, gc, sm, (const VT*)rin, q, r_out, (VT*)e, (VTc*)rc, sc, partials, P.nblocks);
+}
+template <int CK, class VT, class VTc, bool DOT, bool FINE>
+static void post_impl(const Grid3& g, const Grid3& gc, const void* sm, const void* e, const void* ec, const void* r,
+                      void* out, float w, Scalars* sc, double* partials, long long n_active, int occ_kind,
+                      cudaStream_t s) {
+    const Launch P = fused_launch(g, occ_kind);
+    k_prolong_postsmooth<CK, VT, VTc, DOT, FINE><<<P.grid, P.block, sizeof(PostRing<CK, VT>), s>>>(
+        P.g, gc, sm, (const VT*)e, (const VTc*)ec, (const VT*)r, (VT*)out, w, sc, partials, P.nblocks, n_active);
+}
+
+template <int CK, class VT>
+static void vcycle_fused_impl(const MGPlan& P, const float* r_in, const float* q, float* r_out, bool update,
+                              double* partials, long long n_active, cudaStream_t s) {
+    const int F = P.fused_levels;
+    if (update)
+        pre_impl<CK, float, VT, true, true>(P.lv[0].L.g, P.lv[1].L.g, P.lv[0].sm, r_in, q, r_out, P.e0, P.lv[1].r,
+                                            P.sc, partials, CK == 0 ? O_PRE_F32_UPD : O_PRE_LO_UPD, s);
+    else
+        pre_impl<CK, float, VT, false, true>(P.lv[0].L.g, P.lv[1].L.g, P.lv[0].sm, r_in, nullptr, nullptr, P.e0,
+                                             P.lv[1].r, P.sc, partials, CK == 0 ? O_PRE_F32 : O_PRE_LO, s);
+    for (int l = 1; l < F; l++) {
+        const MGLevel &L = P.lv[l], &C = P.lv[l + 1];
+        pre_impl<CK, VT, VT, false, false>(L.L.g, C.L.g, L.sm, L.r, nullptr, nullptr, L.e, C.r, P.sc, partials,
+                                           O_PRE_COARSE, s);
+    }
+    mg_vcycle_from(P, F, s);
+    for (int l = F - 1; l >= 1; l--) {
+        const MGLevel &L = P.lv[l], &C = P.lv[l + 1];
+        const void* ec = (l + 1 < F) ? C.eo : C.e;
+        post_impl<CK, VT, VT, false, false>(L.L.g, C.L.g, L.sm, L.e, ec, L.r, L.eo, P.prolong, P.sc, partials,
+                                            n_active, O_POST_COARSE, s);
+    }
+    const void* ec1 = (1 < F) ? P.lv[1].eo : P.lv[1].e;
+    post_impl<CK, float, VT, true, true>(P.lv[0].L.g, P.lv[1].L.g, P.lv[0].sm, P.e0, ec1, update ? r_out : r_in,
+                                         P.lv[0].e, P.prolong, P.sc, partials, n_active,
+                                         CK == 0 ? O_POST_F32 : O_POST_LO, s);
+}
+
+void mg_vcycle_fused(const MGPlan& P, const float* r_in, const float* q, float* r_out, bool update, double* partials,
+                     long long n_active, cudaStream_t s) {
+    if (P.precision == 1) vcycle_fused_impl<1, __half>(P, r_in, q, r_out, update, partials, n_active, s);
+    else if (P.precision == 2) vcycle_fused_impl<2, __nv_bfloat16>(P, r_in, q, r_out, update, partials, n_active, s);
+    else vcycle_fused_impl<0, float>(P, r_in, q, r_out, update, partials, n_active, s);
+}
+
+template <int CK>
+static void records_impl(const MGPlan& P, cudaStream_t s) {
+    for (int l = 0; l < P.fused_levels; l++) {
+        const MGLevel& L = P.lv[l];
+        const void* coef = CK == 0 ? (const void*)L.coef32 : L.coef_lo;
+        k_smoother_records<CK><<<L.L.grid, L.L.block, 0, s>>>(L.L.g, coef, L.sm);
+    }
+}
+void mg_smoother_records(const MGPlan& P, cudaStream_t s) {
+    if (P.precision == 1) records_impl<1>(P, s);
+    else if (P.precision == 2) records_impl<2>(P, s);
+    else records_impl<0>(P, s);
+}
+
+// Single passes, for measurement.
+void mg_fused_pre(const MGPlan& P, const float* r_in, const float* q, float* r_out, double* partials,
+                  cudaStream_t s) {
+    const Grid3 &g = P.lv[0].L.g, &gc = P.lv[1].L.g;
+    const void* sm = P.lv[0].sm;
+    if (P.precision == 1)
+        pre_impl<1, float, __half, true, true>(g, gc, sm, r_in, q, r_out, P.e0, P.lv[1].r, P.sc, partials, O_PRE_LO_UPD, s);
+    else if (P.precision == 2)
+        pre_impl<2, float, __nv_bfloat16, true, true>(g, gc, sm, r_in, q, r_out, P.e0, P.lv[1].r, P.sc, partials,
+                                                      O_PRE_LO_UPD, s);
+    else
+        pre_impl<0, float, float, true, true>(g, gc, sm, r_in, q, r_out, P.e0, P.lv[1].r, P.sc, partials, O_PRE_F32_UPD,
+                                              s);
+}
+void mg_fused_post(const MGPlan& P, const float* r, double* partials, long long n_active, cudaStream_t s) {
+    const Grid3 &g = P.lv[0].L.g, &gc = P.lv[1].L.g;
+    const void* sm = P.lv[0].sm;
+    const void* ec1 = (1 < P.fused_levels) ? P.lv[1].eo : P.lv[1].e;
+    if (P.precision == 1)
+        post_impl<1, float, __half, true, true>(g, gc, sm, P.e0, ec1, r, P.lv[0].e, P.prolong, P.sc, partials, n_active,
+                                                O_POST_LO, s);
+    else if (P.precision == 2)
+        post_impl<2, float, __nv_bfloat16, true, true>(g, gc, sm, P.e0, ec1, r, P.lv[0].e, P.prolong, P.sc, partials,
+                                                       n_active, O_POST_LO, s);
+    else
+        post_impl<0, float, float, true, true>(g, gc, sm, P.e0, ec1, r, P.lv[0].e, P.prolong, P.sc, partials, n_active,
+                                               O_POST_F32, s);
+}
+
+template <int CK, class VT, class VTc, bool UPDATE, bool FINE>
+static cudaError_t prep_pre(int kind) {
+    const void* fn = (const void*)k_presmooth_restrict<CK, VT, VTc, UPDATE, FINE>;
+    const size_t bytes = sizeof(PreRing<CK, VT, UPDATE>);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess && kind >= 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f_occ[kind], fn, TILE_THREADS, bytes);
+    return e;
+}
+template <int CK, class VT, class VTc, bool DOT, bool FINE>
+static cudaError_t prep_post(int kind) {
+    const void* fn = (const void*)k_prolong_postsmooth<CK, VT, VTc, DOT, FINE>;
+    const size_t bytes = sizeof(PostRing<CK, VT>);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess && kind >= 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f_occ[kind], fn, TILE_THREADS, bytes);
+    return e;
+}
+
+cudaError_t fused_prepare_attributes() {
+    cudaError_t e = cudaSuccess;
+    int dev = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&f_sms, cudaDevAttrMultiProcessorCount, dev);
+#define PREP(x) \
+    if (e == cudaSuccess) e = (x)
+    PREP((prep_pre<0, float, float, false, true>(O_PRE_F32)));
+    PREP((prep_pre<0, float, float, true, true>(O_PRE_F32_UPD)));
+    PREP((prep_pre<1, float, __half, false, true>(O_PRE_LO)));
+    PREP((prep_pre<1, float, __half, true, true>(O_PRE_LO_UPD)));
+    PREP((prep_pre<2, float, __nv_bfloat16, false, true>(-1)));
+    PREP((prep_pre<2, float, __nv_bfloat16, true, true>(-1)));
+    PREP((prep_pre<0, float, float, false, false>(-1)));
+    PREP((prep_pre<1, __half, __half, false, false>(O_PRE_COARSE)));
+    PREP((prep_pre<2, __nv_bfloat16, __nv_bfloat16, false, false>(-1)));
+    PREP((prep_post<0, float, float, true, true>(O_POST_F32)));
+    PREP((prep_post<1, float, __half, true, true>(O_POST_LO)));
+    PREP((prep_post<2, float, __nv_bfloat16, true, true>(-1)));
+    PREP((prep_post<0, float, float, false, false>(-1)));
+    PREP((prep_post<1, __half, __half, false, false>(O_POST_COARSE)));
+    PREP((prep_post<2, __nv_bfloat16, __nv_bfloat16, false, false>(-1)));
+#undef PREP
+    return e;
+}
+
+}  // namespace mhdproj

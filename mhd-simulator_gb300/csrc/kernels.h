@@ -33,7 +33,8 @@ struct Fields {
 
 // ---- GB300 solver kernels (gb300_kernels.cu)
 void launch_coefficients(const Launch& L, const Fields& F, cudaStream_t s);
-void launch_init_scalars(Scalars* sc, double tol2, double abs_floor, double inner_floor2, cudaStream_t s);
+void launch_init_scalars(Scalars* sc, double tol2, double abs_floor, double inner_floor2, int max_total,
+                         cudaStream_t s);
 void launch_rhs(const Launch& L, const Fields& F, const float* u, const float* v, const float* w, cudaStream_t s);
 void launch_residual(const Launch& L, const Fields& F, const float* x_hi, const float* x_lo, cudaStream_t s);
 void launch_spmv_pq(const Launch& L, const Fields& F, cudaStream_t s);
@@ -49,6 +50,7 @@ void launch_divergence(const Launch& L, const Fields& F, const float* u, const f
                        cudaStream_t s);
 void launch_apply(const Launch& L, const Fields& F, const float* x, float* y, cudaStream_t s);
 void launch_set_sigma(Scalars* sc, float sigma, cudaStream_t s);
+void launch_profile_reset(Scalars* sc, cudaStream_t s);
 void launch_scale(const Launch& L, const float* in, float* out, float scale, const Scalars* sc, cudaStream_t s);
 // adjoint and chain
 void launch_adj_rhs(const Launch& L, const Fields& F, const float* gu, const float* gv, const float* gw,
@@ -79,6 +81,8 @@ struct MGLevel {
     void* r;         // level residual (level 0: the CG residual, FP32)
     void* e;         // level correction (level 0: the preconditioned residual z, FP32)
     void* tmp;       // half-step scratch for levels with odd periodic extents
+    void* eo;        // post-smoothing output of a fused level >= 1 (level precision)
+    void* sm;        // smoother records (beta_x, beta_y, beta_z, diagonal) of a fused level
     bool odd_periodic;
 };
 struct MGPlan {
@@ -90,6 +94,8 @@ struct MGPlan {
     float prolong;  // coarse-correction weight
     Scalars* sc;
     bool staged;    // finest level through the shared-memory staged kernels
+    int fused_levels;  // levels 0 .. fused_levels-1 run as fused pre-/post-smoothing passes (0: none)
+    float* e0;         // fine-level pre-smoothed correction of the fused passes
 };
 void mg_build(const MGPlan& P, cudaStream_t s);
 // single fine-level stages, for measurement
@@ -97,6 +103,23 @@ void mg_fine_smooth(const MGPlan& P, int color, cudaStream_t s);
 void mg_fine_restrict(const MGPlan& P, cudaStream_t s);
 void mg_fine_prolong(const MGPlan& P, cudaStream_t s);
 void mg_vcycle(const MGPlan& P, cudaStream_t s);
+void mg_vcycle_from(const MGPlan& P, int l0, cudaStream_t s);
+
+// ---- pipelined CG with fused V-cycle passes (fused_kernels.cu, fine_kernels.cu)
+bool fused_supported(const Grid3& g);
+cudaError_t fused_prepare_attributes();
+// One V-cycle z = B(sigma r) / sigma through the fused passes; update: the
+// residual is first updated, r_out = r_in - alpha q.  Ends with rz and beta.
+void mg_vcycle_fused(const MGPlan& P, const float* r_in, const float* q, float* r_out, bool update, double* partials,
+                     long long n_active, cudaStream_t s);
+void mg_fused_pre(const MGPlan& P, const float* r_in, const float* q, float* r_out, double* partials, cudaStream_t s);
+void mg_fused_post(const MGPlan& P, const float* r, double* partials, long long n_active, cudaStream_t s);
+// Smoother records of the fused levels, after every coefficient change.
+void mg_smoother_records(const MGPlan& P, cudaStream_t s);
+void launch_search_spmv(const Launch& L, const float4* coef, const float* z, const float* p_old, float* p_new,
+                        float* x, float* q, Scalars* sc, double* partials, int pidx_new, cudaStream_t s);
+void launch_accumulate_pipelined(const Launch& L, float* x_hi, float* x_lo, const float* x, const float* p0,
+                                 const float* p1, const Scalars* sc, cudaStream_t s);
 cudaError_t mg_prepare_attributes();
 
 }  // namespace mhdproj

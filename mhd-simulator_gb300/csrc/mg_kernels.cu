@@ -434,10 +434,13 @@ static void enqueue_smooth(const MGPlan& P, int l, int color, bool zero, cudaStr
     }
 }
 
+// Levels l0 .. nlevels-1 of the V-cycle: pre-smoothing and restriction down
+// from l0, the exact coarsest solve, prolongation and post-smoothing back up
+// to l0.  The caller prolongs level l0's correction further up.
 template <int CK, class VT>
-static void vcycle_impl(const MGPlan& P, cudaStream_t s) {
+static void vcycle_impl(const MGPlan& P, int l0, cudaStream_t s) {
     const int nl = P.nlevels;
-    for (int l = 0; l + 1 < nl; l++) {
+    for (int l = l0; l + 1 < nl; l++) {
         enqueue_smooth<CK, VT>(P, l, 0, true, s);
         enqueue_smooth<CK, VT>(P, l, 1, false, s);
         const MGLevel &F = P.lv[l], &C = P.lv[l + 1];
@@ -454,7 +457,7 @@ static void vcycle_impl(const MGPlan& P, cudaStream_t s) {
     const MGLevel& K = P.lv[nl - 1];
     if (nl == 1) k_coarse_solve<float, true><<<1, 64, 0, s>>>(P.m, P.ainv, (const float*)K.r, (float*)K.e, P.sc);
     else k_coarse_solve<VT, false><<<1, 64, 0, s>>>(P.m, P.ainv, (const VT*)K.r, (VT*)K.e, P.sc);
-    for (int l = nl - 2; l >= 0; l--) {
+    for (int l = nl - 2; l >= l0; l--) {
         const MGLevel &F = P.lv[l], &C = P.lv[l + 1];
         if (l == 0)
             k_prolong<float, VT><<<F.L.grid, F.L.block, 0, s>>>(F.L.g, C.L.g, (float*)F.e, (const VT*)C.e, P.prolong, P.sc);
@@ -465,11 +468,13 @@ static void vcycle_impl(const MGPlan& P, cudaStream_t s) {
     }
 }
 
-void mg_vcycle(const MGPlan& P, cudaStream_t s) {
-    if (P.precision == 1) vcycle_impl<1, __half>(P, s);
-    else if (P.precision == 2) vcycle_impl<2, __nv_bfloat16>(P, s);
-    else vcycle_impl<0, float>(P, s);
+void mg_vcycle_from(const MGPlan& P, int l0, cudaStream_t s) {
+    if (P.precision == 1) vcycle_impl<1, __half>(P, l0, s);
+    else if (P.precision == 2) vcycle_impl<2, __nv_bfloat16>(P, l0, s);
+    else vcycle_impl<0, float>(P, l0, s);
 }
+
+void mg_vcycle(const MGPlan& P, cudaStream_t s) { mg_vcycle_from(P, 0, s); }
 
 template <int CK, class VT>
 static void fine_restrict_impl(const MGPlan& P, cudaStream_t s) {

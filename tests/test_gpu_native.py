@@ -164,12 +164,16 @@ def test_preconditioner_is_symmetric_positive(gpu, oracle_lib, precision):
 
 
 def test_adjoint_identity_and_oracle(gpu, oracle_lib):
-    """<P a, b> == <a, P^T b> on the GPU, and the GPU VJP equals the FP64 oracle's."""
+    """<P a, b> == <a, P^T b> on the GPU, and the GPU VJP equals the FP64 oracle's.
+
+    Both solves stop on a relative residual; the error that reaches the
+    identity is up to the condition number times that, so the solves run at
+    1e-10, where both sit at the FP32 rounding floor of the outputs."""
     import mhdproj
 
     torch = gpu
     c = synth.make_case("jet128", scale=0.25)
-    pr = make(mhdproj, c, precision="fp16", rel_tol=1e-9)
+    pr = make(mhdproj, c, precision="fp16", rel_tol=1e-10)
     a, s, us = tensors(torch, c)
     pr.set_coefficients(a, s, c["rho_liquid"], c["rho_air"])
     rng = np.random.default_rng(11)
