@@ -216,6 +216,13 @@ typedef struct {
 } mhdproj_kernel_time;
 int mhdproj_profile_kernels(mhdproj_ctx *ctx, int reps, mhdproj_kernel_time *out, int max_out, int *count);
 
+/* Measurement hook, no counterpart in the reference: the number of kernels
+ * this context has launched on the GPU since it was created (GB300 solver:
+ * coefficient set-up, projections, adjoints and chains; launches inside a
+ * replayed CUDA graph count one each, kernels that return early because the
+ * solve has converged included). */
+int mhdproj_kernel_launches(mhdproj_ctx *ctx, uint64_t *count);
+
 /* Divergence statistics of a face-velocity field that allocate nothing.
  * No counterpart in the reference: it exists for callers that cannot allocate
  * device memory while they run (a time loop that reserved its whole budget at

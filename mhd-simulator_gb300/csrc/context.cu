@@ -68,6 +68,8 @@ struct mhdproj_ctx {
     // pipelined CG: search+SpMV, fused V-cycle passes; ping-pong r and p
     bool pipelined = false;
     float *r1 = nullptr, *p1 = nullptr;
+    uint64_t launches = 0;        // kernels launched (measurement)
+    uint64_t graph_kernels = 0;   // kernels per replay of it_graph
     cudaGraphExec_t it_graph = nullptr;
     bool graph_failed = false;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_sync = nullptr;
@@ -409,6 +411,7 @@ static int update_topology(mhdproj_ctx* ctx, const uint8_t* solid, bool* changed
     if (ctx->have_topology) {
         CK(cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
         k_compare_u8<<<152 * 4, 256, 0, ctx->stream>>>(solid, ctx->d_solid_prev, ctx->n, ctx->d_flag);
+        ctx->launches += 1;
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(ctx->h_flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         int rc = wait_stream(ctx);
@@ -465,10 +468,15 @@ extern "C" int mhdproj_set_coefficients(mhdproj_ctx* ctx, const float* alpha, co
     CK(cudaMemcpyAsync(ctx->alpha, alpha, ctx->n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     Fields F = fields(ctx);
     launch_coefficients(ctx->L, F, ctx->stream);
+    ctx->launches += 1;
     CK(cudaGetLastError());
     if (ctx->use_mg) {
         mg_build(ctx->mg, ctx->stream);
-        if (ctx->pipelined) mg_smoother_records(ctx->mg, ctx->stream);
+        ctx->launches += (uint64_t)ctx->mg.nlevels;  // Galerkin levels and the coarsest inverse
+        if (ctx->pipelined) {
+            mg_smoother_records(ctx->mg, ctx->stream);
+            ctx->launches += (uint64_t)ctx->mg.fused_levels;
+        }
         CK(cudaGetLastError());
     }
     ctx->have_coef = true;
@@ -501,6 +509,29 @@ __global__ void k_jacobi(Grid3 g, const float4* __restrict__ coef, const float* 
         z[i] = d > 0.f ? sc->sigma * r[i] / d : 0.f;
     }
 }
+// Kernel counts of the enqueue paths (the launch counter of the context).
+static uint64_t kernels_vcycle_from(const MGPlan& P, int from) {
+    uint64_t k = 1;  // coarsest solve
+    for (int l = from; l + 1 < P.nlevels; l++) {
+        const uint64_t copy = P.lv[l].odd_periodic ? 1 : 0;
+        k += 2 + copy + 1;      // red from zero, black (+ copy), restriction
+        k += 1 + 2 + 2 * copy;  // prolongation, black, red (+ copies)
+    }
+    return k;
+}
+static uint64_t kernels_precondition(const mhdproj_ctx* ctx) {
+    if (!ctx->use_mg) return 1;
+    if (ctx->pipelined) return 2 * (uint64_t)ctx->mg.fused_levels + kernels_vcycle_from(ctx->mg, ctx->mg.fused_levels);
+    return kernels_vcycle_from(ctx->mg, 0);
+}
+static uint64_t kernels_iteration(const mhdproj_ctx* ctx) {
+    if (ctx->pipelined) return 1 + kernels_precondition(ctx);  // search+SpMV, V-cycle passes
+    return 4 + kernels_precondition(ctx);                       // SpMV, update, V-cycle, dot, search
+}
+static uint64_t kernels_pass_start(const mhdproj_ctx* ctx) {
+    return kernels_precondition(ctx) + (ctx->pipelined ? 0 : 1);
+}
+
 static void enqueue_precondition(mhdproj_ctx* ctx) {
     if (ctx->use_mg) mg_vcycle(ctx->mg, ctx->stream);
     else k_jacobi<<<ctx->L.grid, ctx->L.block, 0, ctx->stream>>>(ctx->L.g, ctx->coef, ctx->r, ctx->z, ctx->sc);
@@ -559,9 +590,11 @@ static int launch_iterations(mhdproj_ctx* ctx, int count) {
     }
     // a pipelined graph holds two iterations
     const int launches = ctx->pipelined ? (count + 1) / 2 : count;
+    const uint64_t body = kernels_iteration(ctx) * (ctx->pipelined ? 2 : 1);
     for (int k = 0; k < launches; k++) {
         if (ctx->it_graph) CK(cudaGraphLaunch(ctx->it_graph, ctx->stream));
         else enqueue_iteration_body(ctx);
+        ctx->launches += body;
     }
     CK(cudaGetLastError());
     return 0;
@@ -571,13 +604,15 @@ static int launch_iterations(mhdproj_ctx* ctx, int count) {
 // by CG with iterative refinement: each pass solves A e = r in FP32 and adds
 // e to the double-FP32 solution x, whose residual b - A x is recomputed in
 // double-FP32.  x holds the initial guess.  Returns 0 or an error.
-static int solve(mhdproj_ctx* ctx, float* x_hi, float* x_lo, mhdproj_stats* st) {
+static int solve(mhdproj_ctx* ctx, float* x_hi, float* x_lo, mhdproj_stats* st, bool x_zero = false) {
     Fields F = fields(ctx);
     const double tol2 = (double)ctx->opt.rel_tol * ctx->opt.rel_tol;
     (void)tol2;
     int passes = 0;
-    launch_residual(ctx->L, F, x_hi, x_lo, ctx->stream);
+    // x_zero: the right-hand-side kernel already set up the first pass (r = b)
+    if (!x_zero) launch_residual(ctx->L, F, x_hi, x_lo, ctx->stream);
     enqueue_pass_start(ctx);
+    ctx->launches += (x_zero ? 0 : 1) + kernels_pass_start(ctx);
     CK(cudaGetLastError());
     int rc = read_scalars(ctx);
     if (rc) return rc;
@@ -623,6 +658,7 @@ static int solve(mhdproj_ctx* ctx, float* x_hi, float* x_lo, mhdproj_stats* st) 
         passes++;
         launch_residual(ctx->L, F, x_hi, x_lo, ctx->stream);
         enqueue_pass_start(ctx);
+        ctx->launches += 2 + kernels_pass_start(ctx);  // accumulate, residual, pass start
         CK(cudaGetLastError());
         rc = read_scalars(ctx);
         if (rc) return rc;
@@ -657,16 +693,22 @@ static int project_gb300(mhdproj_ctx* ctx, const float* us, const float* vs, con
     CK(cudaEventRecord(ctx->ev_a, ctx->stream));
     begin_scalars(ctx);
     Fields F = fields(ctx);
-    launch_rhs(ctx->L, F, us, vs, ws, ctx->stream);
-    if (!warm || !ctx->have_solution) {
+    const bool from_zero = !warm || !ctx->have_solution;
+    launch_rhs(ctx->L, F, us, vs, ws, ctx->stream, from_zero);
+    ctx->launches += 2;
+    if (from_zero) {
         CK(cudaMemsetAsync(ctx->phi_hi, 0, ctx->n * 4, ctx->stream));
         CK(cudaMemsetAsync(ctx->phi_lo, 0, ctx->n * 4, ctx->stream));
     }
     mhdproj_stats local{};
-    int rc = solve(ctx, ctx->phi_hi, ctx->phi_lo, &local);
+    int rc = solve(ctx, ctx->phi_hi, ctx->phi_lo, &local, from_zero);
     if (rc) return rc;
     launch_correct(ctx->L, F, ctx->phi_hi, ctx->phi_lo, us, vs, ws, uo, vo, wo, po, dt, ctx->stream);
-    if (ctx->opt.compute_divergence) launch_divergence(ctx->L, F, uo, vo, wo, ctx->stream);
+    ctx->launches += 1;
+    if (ctx->opt.compute_divergence) {
+        launch_divergence(ctx->L, F, uo, vo, wo, ctx->stream);
+        ctx->launches += 1;
+    }
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev_b, ctx->stream));
     if (ctx->opt.compute_divergence) {
@@ -749,11 +791,13 @@ static int vjp_gb300(mhdproj_ctx* ctx, const float* gu, const float* gv, const f
     begin_scalars(ctx);
     Fields F = fields(ctx);
     launch_adj_rhs(ctx->L, F, gu, gv, gw, gp, dt, ctx->stream);
+    ctx->launches += 2;
     CK(cudaMemsetAsync(ctx->psi_hi, 0, ctx->n * 4, ctx->stream));
     CK(cudaMemsetAsync(ctx->psi_lo, 0, ctx->n * 4, ctx->stream));
     int rc = solve(ctx, ctx->psi_hi, ctx->psi_lo, st);
     if (rc) return rc;
     launch_adj_correct(ctx->L, F, ctx->psi_hi, ctx->psi_lo, gu, gv, gw, ou, ov, ow, ctx->stream);
+    ctx->launches += 1;
     CK(cudaGetLastError());
     return 0;
 }
@@ -1069,6 +1113,12 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
     }
     *count = k;
     ctx->have_solution = false;
+    return 0;
+}
+
+extern "C" int mhdproj_kernel_launches(mhdproj_ctx* ctx, uint64_t* count) {
+    if (!ctx || !count) return MHDPROJ_ERR_INVALID;
+    *count = ctx->launches;
     return 0;
 }
 

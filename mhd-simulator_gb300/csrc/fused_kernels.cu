@@ -40,17 +40,19 @@ namespace {
 using namespace staged;
 
 constexpr int PX = 2 * TX;       // 64 cells per tile row
+constexpr int FTY = 8;           // tile rows (one thread row per tile row)
+constexpr int FT = TX * FTY;     // 256 threads per block
 constexpr int XO = 4;            // staged rows start at x0 - XO
 constexpr int RW = PX + 2 * XO;  // 72 staged columns: x0-4 .. x0+67
-constexpr int RH = TY + 4;       // vector rows:  y0-2 .. y0+9
-constexpr int CH = TY + 5;       // record rows:  y0-2 .. y0+10
+constexpr int RH = FTY + 4;      // vector rows:  y0-2 .. y0+FTY+1
+constexpr int CH = FTY + 5;      // record rows:  y0-2 .. y0+FTY+2
 constexpr int NG = RW / 4;       // 18 four-cell groups per staged row
 constexpr int NVEC = RH * NG;    // 216 vector copies per plane
 constexpr int RP = (PX + 4) / 2; // 34 pairs of the 2-halo region (x0-2 .. x0+65)
 constexpr int NRED = RH * RP;    // 408 red-stage pair tasks
-constexpr int NBLK = (TY + 2) * RP;  // 340 black-stage pair tasks (rows y0-1 .. y0+8)
-static_assert(NVEC <= TILE_THREADS, "one vector copy per thread");
-static_assert(NRED <= 2 * TILE_THREADS && NBLK <= 2 * TILE_THREADS, "two tasks per thread");
+constexpr int NBLK = (FTY + 2) * RP;  // 340 black-stage pair tasks (rows y0-1 .. y0+FTY)
+static_assert(NVEC <= FT, "one vector copy per thread");
+static_assert(NRED <= 2 * FT && NBLK <= 2 * FT, "two tasks per thread");
 
 template <class VT> __device__ __forceinline__ float2 ld2(const VT* p);
 template <> __device__ __forceinline__ float2 ld2<float>(const float* p) { return *reinterpret_cast<const float2*>(p); }
@@ -85,7 +87,7 @@ struct RegionFetch {
     static constexpr int RPC = (CK == 0) ? 1 : 2;  // records per 16-byte copy
     static constexpr int NCT = (CK == 0) ? 4 : 2;
     static constexpr int NCTOT = CH * (RW / RPC);
-    static_assert(NCTOT <= NCT * TILE_THREADS, "record copies per thread");
+    static_assert(NCTOT <= NCT * FT, "record copies per thread");
     int voff, coff[NCT];
     short vdst, cdst[NCT];
     bool vok, cok[NCT];
@@ -112,7 +114,7 @@ struct RegionFetch {
         }
 #pragma unroll
         for (int j = 0; j < NCT; j++) {
-            const int k = t + j * TILE_THREADS;
+            const int k = t + j * FT;
             cdst[j] = -1;
             cok[j] = false;
             coff[j] = 0;
@@ -180,7 +182,7 @@ struct PairTasks {
     __device__ __forceinline__ PairTasks(const Grid3& g, int x0, int y0, int t) {
 #pragma unroll
         for (int u = 0; u < 2; u++) {
-            const int k = t + u * TILE_THREADS;
+            const int k = t + u * FT;
             roff[u] = -1;
             rpar[u] = 0;
             rown[u] = -1;
@@ -189,7 +191,7 @@ struct PairTasks {
                 roff[u] = row * RW + 2 + 2 * pc;
                 rpar[u] = (y0 - 2 + row) & 1;
                 const int gx = x0 - 2 + 2 * pc, gy = y0 - 2 + row;
-                if (row >= 2 && row < TY + 2 && pc >= 1 && pc <= TX && gx < g.nx && gy < g.ny) rown[u] = gx + g.nx * gy;
+                if (row >= 2 && row < FTY + 2 && pc >= 1 && pc <= TX && gx < g.nx && gy < g.ny) rown[u] = gx + g.nx * gy;
             }
             boff[u] = -1;
             bpar[u] = 0;
@@ -222,7 +224,7 @@ struct PreRing {
     float q[UPDATE ? 2 : 1][RH][RW];
     float rn[2][RH][RW];             // updated residual, planes zA-1 .. zA
     float er[4][RH][RW];             // correction, planes zA-3 .. zA
-    float ypart[TY][TX];
+    float ypart[FTY][TX];
 };
 template <int CK, class VT>
 struct PostRing {
@@ -246,7 +248,7 @@ using Phase = std::integral_constant<int, N>;
 // black neighbours (its red value solved the equation with them at zero), so
 // the restriction sums those neighbour terms over the red cells.
 template <int CK, class VT, class VTc, bool UPDATE, bool FINE>
-__global__ void __launch_bounds__(TILE_THREADS) k_presmooth_restrict(Grid3 g, Grid3 gc, const void* __restrict__ sm_v,
+__global__ void __launch_bounds__(FT) k_presmooth_restrict(Grid3 g, Grid3 gc, const void* __restrict__ sm_v,
                                                                      const VT* __restrict__ rin,
                                                                      const float* __restrict__ q,
                                                                      float* __restrict__ r_out, VT* __restrict__ e,
@@ -257,10 +259,10 @@ __global__ void __launch_bounds__(TILE_THREADS) k_presmooth_restrict(Grid3 g, Gr
     const CT* sm = reinterpret_cast<const CT*>(sm_v);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto& S = *reinterpret_cast<PreRing<CK, VT, UPDATE>*>(smem_raw);
-    __shared__ double sh[8];
+    __shared__ double sh[FT / 32];
     const float sigma = FINE ? sc->sigma : 1.0f;
     const float alpha = UPDATE ? sc->alpha_f : 0.0f;
-    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * TY;
+    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * FTY;
     const int tx = threadIdx.x, ty = threadIdx.y, t = tx + TX * ty;
     const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
     const RegionFetch<CK> F(g, x0, y0, t);
@@ -401,7 +403,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_presmooth_restrict(Grid3 g, Gr
 // (finest level): r . out / sigma gives rz and beta; the next V-cycle's sigma
 // is then taken from ||r||^2.
 template <int CK, class VT, class VTc, bool DOT, bool FINE>
-__global__ void __launch_bounds__(TILE_THREADS) k_prolong_postsmooth(Grid3 g, Grid3 gc, const void* __restrict__ sm_v,
+__global__ void __launch_bounds__(FT) k_prolong_postsmooth(Grid3 g, Grid3 gc, const void* __restrict__ sm_v,
                                                                      const VT* __restrict__ e,
                                                                      const VTc* __restrict__ ec,
                                                                      const VT* __restrict__ r, VT* __restrict__ out,
@@ -412,10 +414,10 @@ __global__ void __launch_bounds__(TILE_THREADS) k_prolong_postsmooth(Grid3 g, Gr
     const CT* sm = reinterpret_cast<const CT*>(sm_v);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto& S = *reinterpret_cast<PostRing<CK, VT>*>(smem_raw);
-    __shared__ double sh[8];
+    __shared__ double sh[FT / 32];
     const float sigma = FINE ? sc->sigma : 1.0f;
     const float is = FINE ? sc->inv_sigma : 1.0f;
-    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * TY;
+    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * FTY;
     const int tx = threadIdx.x, ty = threadIdx.y, t = tx + TX * ty;
     const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
     const RegionFetch<CK> F(g, x0, y0, t);
@@ -428,7 +430,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_prolong_postsmooth(Grid3 g, Gr
         const bool px = g.periodic & 1, py = g.periodic & 2;
 #pragma unroll
         for (int u = 0; u < 2; u++) {
-            const int k = t + u * TILE_THREADS;
+            const int k = t + u * FT;
             pofs[u] = 0;
             pok[u] = false;
             if (k < NRED) {
@@ -633,8 +635,8 @@ enum { O_PRE_F32 = 0, O_PRE_LO, O_PRE_LO_UPD, O_PRE_F32_UPD, O_PRE_COARSE, O_POS
 Launch fused_launch(const Grid3& g0, int occ_kind) {
     Launch P;
     P.g = g0;
-    P.block = dim3(TX, TY, 1);
-    const int gx = (g0.nx + PX - 1) / PX, gy = (g0.ny + TY - 1) / TY, nz = g0.nz;
+    P.block = dim3(TX, FTY, 1);
+    const int gx = (g0.nx + PX - 1) / PX, gy = (g0.ny + FTY - 1) / FTY, nz = g0.nz;
     const int tiles = gx * gy;
     const int cap = (f_sms > 0 ? f_sms : 152) * (f_occ[occ_kind] > 0 ? f_occ[occ_kind] : 1);
     int best_zper = nz + (nz & 1), best_zc = 1;
@@ -769,7 +771,7 @@ static cudaError_t prep_pre(int kind) {
     const void* fn = (const void*)k_presmooth_restrict<CK, VT, VTc, UPDATE, FINE>;
     const size_t bytes = sizeof(PreRing<CK, VT, UPDATE>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess && kind >= 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f_occ[kind], fn, TILE_THREADS, bytes);
+    if (e == cudaSuccess && kind >= 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f_occ[kind], fn, FT, bytes);
     return e;
 }
 template <int CK, class VT, class VTc, bool DOT, bool FINE>
@@ -777,7 +779,7 @@ static cudaError_t prep_post(int kind) {
     const void* fn = (const void*)k_prolong_postsmooth<CK, VT, VTc, DOT, FINE>;
     const size_t bytes = sizeof(PostRing<CK, VT>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess && kind >= 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f_occ[kind], fn, TILE_THREADS, bytes);
+    if (e == cudaSuccess && kind >= 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f_occ[kind], fn, FT, bytes);
     return e;
 }
 

@@ -111,11 +111,15 @@ __global__ void __launch_bounds__(TILE_THREADS) k_coefficients(Grid3 g, int outl
 // ------------------------------------------------------------------ rhs
 // b = -h * sum over open faces of (u_high - u_low) as a double-FP32 pair;
 // ||b||^2.
+// start_pass: the solve starts from x = 0, so this kernel also sets up its
+// first pass: r = b (rounded to FP32), x = 0 and the pass scalars of
+// k_residual with ||b - A 0||^2 = ||b||^2.
 __global__ void __launch_bounds__(TILE_THREADS) k_rhs(Grid3 g, int outlet, float h, const uint8_t* __restrict__ cls,
                                                       const float* __restrict__ u, const float* __restrict__ v,
                                                       const float* __restrict__ w, float* __restrict__ b_hi,
-                                                      float* __restrict__ b_lo, Scalars* sc, double* partials,
-                                                      int nblocks) {
+                                                      float* __restrict__ b_lo, float* __restrict__ r,
+                                                      float* __restrict__ xs, int start_pass, Scalars* sc,
+                                                      double* partials, int nblocks, long long n_active) {
     __shared__ double sh[8 * 1];
     Acc acc;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
@@ -150,6 +154,10 @@ __global__ void __launch_bounds__(TILE_THREADS) k_rhs(Grid3 g, int outlet, float
         b_hi[i] = bi.hi;
         b_lo[i] = bi.lo;
         acc.add_prod(bi.hi, bi.hi);
+        if (start_pass) {
+            r[i] = df_to_f(bi);
+            xs[i] = 0.0f;
+        }
     }
     double v1[1] = {acc.total()};
     block_sum<1>(v1, sh);
@@ -157,8 +165,23 @@ __global__ void __launch_bounds__(TILE_THREADS) k_rhs(Grid3 g, int outlet, float
         double tot[1];
         finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[0]);
         if (threadIdx.x == 0 && threadIdx.y == 0) {
-            sc->bb = tot[0];
-            if (!isfinite(tot[0])) sc->nonfinite = 1;
+            const double bb = tot[0];
+            sc->bb = bb;
+            if (!isfinite(bb)) sc->nonfinite = 1;
+            if (start_pass) {
+                sc->rr_true = bb;
+                sc->rr = bb;
+                sc->iterations = 0;
+                const double goal = sc->tol2 * bb + sc->abs_floor;
+                const bool done = !(bb > goal) || bb == 0.0;
+                sc->outer_done = done ? 1 : 0;
+                sc->converged = (done || !isfinite(bb)) ? 1 : 0;
+                sc->rr_target = fmax(sc->inner_floor2 * bb, 0.25 * goal);
+                set_sigma_from(sc, bb, n_active);
+                sc->first = 1;
+                sc->alpha = sc->beta = 0.0;
+                sc->alpha_f = sc->beta_f = 0.0f;
+            }
         }
     }
 }
@@ -904,8 +927,10 @@ __global__ void k_profile_reset(Scalars* sc) {
     sc->alpha_f = sc->beta_f = 0.0f;
 }
 void launch_profile_reset(Scalars* sc, cudaStream_t s) { k_profile_reset<<<1, 1, 0, s>>>(sc); }
-void launch_rhs(const Launch& L, const Fields& F, const float* u, const float* v, const float* w, cudaStream_t s) {
-    k_rhs<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.h, F.cls, u, v, w, F.b_hi, F.b_lo, F.sc, F.partials, L.nblocks);
+void launch_rhs(const Launch& L, const Fields& F, const float* u, const float* v, const float* w, cudaStream_t s,
+                bool start_pass) {
+    k_rhs<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.h, F.cls, u, v, w, F.b_hi, F.b_lo, F.r, F.e, start_pass ? 1 : 0,
+                                     F.sc, F.partials, L.nblocks, F.n_active);
 }
 void launch_residual(const Launch& L, const Fields& F, const float* x_hi, const float* x_lo, cudaStream_t s) {
     k_residual<<<L.grid, L.block, 0, s>>>(L.g, F.coef, F.b_hi, F.b_lo, x_hi, x_lo, F.r, F.e, F.sc, F.partials,

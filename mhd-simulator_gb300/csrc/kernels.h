@@ -35,7 +35,9 @@ struct Fields {
 void launch_coefficients(const Launch& L, const Fields& F, cudaStream_t s);
 void launch_init_scalars(Scalars* sc, double tol2, double abs_floor, double inner_floor2, int max_total,
                          cudaStream_t s);
-void launch_rhs(const Launch& L, const Fields& F, const float* u, const float* v, const float* w, cudaStream_t s);
+// start_pass: also r = b, x = 0 and the first pass's scalars (a solve from x = 0)
+void launch_rhs(const Launch& L, const Fields& F, const float* u, const float* v, const float* w, cudaStream_t s,
+                bool start_pass = false);
 void launch_residual(const Launch& L, const Fields& F, const float* x_hi, const float* x_lo, cudaStream_t s);
 void launch_spmv_pq(const Launch& L, const Fields& F, cudaStream_t s);
 void launch_update(const Launch& L, const Fields& F, cudaStream_t s);

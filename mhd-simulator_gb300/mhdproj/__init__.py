@@ -108,6 +108,7 @@ def load():
     L.mhdproj_copy_topology.argtypes = [_vp, _vp, C.POINTER(C.c_uint32)]
     L.mhdproj_profile_kernels.argtypes = [_vp, C.c_int, C.POINTER(KernelTime), C.c_int, C.POINTER(C.c_int)]
     L.mhdproj_divergence_noalloc.argtypes = [C.POINTER(Grid), _vp, _vp, _vp, _vp, C.POINTER(C.c_double), _vp]
+    L.mhdproj_kernel_launches.argtypes = [_vp, C.POINTER(C.c_uint64)]
     L.mhdproj_hierarchy.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)]
     L.mhdproj_anchors.argtypes = [_vp, C.POINTER(C.c_uint32), C.c_uint32]
     L.mhdproj_anchors.restype = C.c_uint32
@@ -121,6 +122,7 @@ EXPORTED = [
     "mhdproj_project_vjp", "mhdproj_chain_forward", "mhdproj_chain_backward", "mhdproj_apply_operator",
     "mhdproj_apply_preconditioner", "mhdproj_copy_coefficients", "mhdproj_copy_potential", "mhdproj_copy_topology",
     "mhdproj_hierarchy", "mhdproj_anchors", "mhdproj_profile_kernels", "mhdproj_divergence_noalloc",
+    "mhdproj_kernel_launches",
 ]
 
 
@@ -335,6 +337,12 @@ class PressureProjection:
         phi = torch.empty(self.cell_shape(), dtype=torch.float64, device="cuda")
         self._check(self._lib.mhdproj_copy_potential(self._ctx, _ptr(phi)))
         return phi
+
+    def kernel_launches(self):
+        """Kernels this context has launched since creation (mhdproj_kernel_launches)."""
+        n = C.c_uint64()
+        self._check(self._lib.mhdproj_kernel_launches(self._ctx, C.byref(n)))
+        return int(n.value)
 
     def profile_kernels(self, reps=20):
         """Per-kernel mean launch time (ms), algorithmic bytes and launches per CG iteration."""
