@@ -216,17 +216,19 @@ static int build_levels(mhdproj_ctx* ctx) {
             if (L.odd_periodic) CK(dalloc(ctx, (char**)&L.tmp, n * vbytes));
         }
         P.nlevels++;
-        // Coarsen until every extent is at most 2: the coarsest operator
-        // (<= 8 cells) is inverted exactly once per coefficient set.
-        if (d[0] <= 2 && d[1] <= 2 && d[2] <= 2) break;
+        // Coarsen until every extent is at most 4 (the reference's own stop):
+        // the coarsest operator (<= 64 cells) is inverted exactly once per
+        // coefficient set.
+        if (d[0] <= 4 && d[1] <= 4 && d[2] <= 4) break;
         if (P.nlevels >= 31) return fail(ctx, MHDPROJ_ERR_INVALID, "multigrid hierarchy too deep");
         for (int a = 0; a < 3; a++) d[a] = (d[a] + 1) / 2;
     }
     P.m = d[0] * d[1] * d[2];
     CK(dalloc(ctx, &P.ainv, (size_t)P.m * P.m * sizeof(float)));
+    mg_plan_bottom(P);
     // Levels run as fused pre-/post-smoothing passes: a prefix of the levels
-    // that have a coarser level, an even x extent and even periodic extents,
-    // down to 16^3 cells; smaller levels use the per-level kernels.
+    // that have a coarser level, an x extent divisible by 4 and even periodic
+    // extents, above 4096 cells; smaller levels run in the bottom sub-cycle.
     P.fused_levels = 0;
     P.e0 = nullptr;
     if (ctx->pipelined && P.nlevels >= 2) {
@@ -234,7 +236,7 @@ static int build_levels(mhdproj_ctx* ctx) {
         while (F < P.nlevels - 1) {
             const Grid3& g = P.lv[F].L.g;
             if (!fused_supported(g)) break;
-            if (F > 0 && g.n() < 4096) break;
+            if (F > 0 && g.n() <= 4096) break;  // the bottom sub-cycle takes over
             F++;
         }
         if (F == 0) {
@@ -246,6 +248,10 @@ static int build_levels(mhdproj_ctx* ctx) {
             for (int l = 0; l < F; l++) {
                 CK(dalloc(ctx, (char**)&P.lv[l].sm, (size_t)P.lv[l].L.g.n() * rbytes));
                 if (l > 0) CK(dalloc(ctx, (char**)&P.lv[l].eo, (size_t)P.lv[l].L.g.n() * vbytes));
+                if (l > 0 && P.w_from > 0 && l >= P.w_from) {
+                    CK(dalloc(ctx, (char**)&P.lv[l].r2, (size_t)P.lv[l].L.g.n() * vbytes));
+                    CK(dalloc(ctx, (char**)&P.lv[l].eo2, (size_t)P.lv[l].L.g.n() * vbytes));
+                }
             }
         }
     } else {
@@ -511,17 +517,24 @@ __global__ void k_jacobi(Grid3 g, const float4* __restrict__ coef, const float* 
 }
 // Kernel counts of the enqueue paths (the launch counter of the context).
 static uint64_t kernels_vcycle_from(const MGPlan& P, int from) {
-    uint64_t k = 1;  // coarsest solve
-    for (int l = from; l + 1 < P.nlevels; l++) {
+    const int lb = (P.bottom_from > 0 && P.bottom_from >= from) ? P.bottom_from : P.nlevels;
+    uint64_t k = 1;  // coarsest solve or the bottom sub-cycle
+    for (int l = from; l + 1 < P.nlevels && l < lb; l++) {
         const uint64_t copy = P.lv[l].odd_periodic ? 1 : 0;
         k += 2 + copy + 1;      // red from zero, black (+ copy), restriction
         k += 1 + 2 + 2 * copy;  // prolongation, black, red (+ copies)
     }
     return k;
 }
+static uint64_t kernels_fused_solve(const MGPlan& P, int l) {
+    if (l >= P.fused_levels) return kernels_vcycle_from(P, l);
+    const uint64_t visit = 2 + kernels_fused_solve(P, l + 1);  // pre, coarser levels, post
+    if (P.w_from > 0 && l >= P.w_from) return 2 * visit + 1;  // + the residual of the second visit
+    return visit;
+}
 static uint64_t kernels_precondition(const mhdproj_ctx* ctx) {
     if (!ctx->use_mg) return 1;
-    if (ctx->pipelined) return 2 * (uint64_t)ctx->mg.fused_levels + kernels_vcycle_from(ctx->mg, ctx->mg.fused_levels);
+    if (ctx->pipelined) return 2 + kernels_fused_solve(ctx->mg, 1);
     return kernels_vcycle_from(ctx->mg, 0);
 }
 static uint64_t kernels_iteration(const mhdproj_ctx* ctx) {

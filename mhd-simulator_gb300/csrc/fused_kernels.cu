@@ -407,8 +407,9 @@ __global__ void __launch_bounds__(FT) k_prolong_postsmooth(Grid3 g, Grid3 gc, co
                                                                      const VT* __restrict__ e,
                                                                      const VTc* __restrict__ ec,
                                                                      const VT* __restrict__ r, VT* __restrict__ out,
-                                                                     float w, Scalars* sc, double* partials,
-                                                                     int nblocks, long long n_active) {
+                                                                     const VT* __restrict__ accum, float w,
+                                                                     Scalars* sc, double* partials, int nblocks,
+                                                                     long long n_active) {
     if (sc->converged) return;
     using CT = typename CoefStore<CK>::T;
     const CT* sm = reinterpret_cast<const CT*>(sm_v);
@@ -519,8 +520,12 @@ __global__ void __launch_bounds__(FT) k_prolong_postsmooth(Grid3 g, Grid3 gc, co
             const float s = gs_sum<CK>(C, CN, E, EM, EP, oo + m, sigma * (m ? rv.y : rv.x), &d);
             const float zr = d > 0.f ? __fdividef(s, d) : 0.f;
             const float zb = E[oo + 1 - m];
-            const float2 zv = m ? make_float2(zb, zr) : make_float2(zr, zb);
+            float2 zv = m ? make_float2(zb, zr) : make_float2(zr, zb);
             if (own_inside) {
+                if (accum) {  // out = accum + z (second W-cycle visit)
+                    const float2 a = ld2<VT>(accum + og + sxy * zC);
+                    zv = make_float2(a.x + zv.x, a.y + zv.y);
+                }
                 st2<VT>(out + og + sxy * zC, zv);
                 if (DOT) {
                     acc.add_prod(rv.x, zv.x * is);
@@ -681,38 +686,88 @@ static void pre_impl(const Grid3& g, const Grid3& gc, const void* sm, const void
 }
 template <int CK, class VT, class VTc, bool DOT, bool FINE>
 static void post_impl(const Grid3& g, const Grid3& gc, const void* sm, const void* e, const void* ec, const void* r,
-                      void* out, float w, Scalars* sc, double* partials, long long n_active, int occ_kind,
-                      cudaStream_t s) {
+                      void* out, const void* accum, float w, Scalars* sc, double* partials, long long n_active,
+                      int occ_kind, cudaStream_t s) {
     const Launch P = fused_launch(g, occ_kind);
     k_prolong_postsmooth<CK, VT, VTc, DOT, FINE><<<P.grid, P.block, sizeof(PostRing<CK, VT>), s>>>(
-        P.g, gc, sm, (const VT*)e, (const VTc*)ec, (const VT*)r, (VT*)out, w, sc, partials, P.nblocks, n_active);
+        P.g, gc, sm, (const VT*)e, (const VTc*)ec, (const VT*)r, (VT*)out, (const VT*)accum, w, sc, partials,
+        P.nblocks, n_active);
+}
+
+// r2 = r - A e on a coarse fused level, with the smoother's operator (the
+// records' betas and diagonal): the right-hand side of a W-cycle level's
+// second visit.
+template <int CK, class VT>
+__global__ void __launch_bounds__(TILE_THREADS) k_level_residual(Grid3 g, const void* __restrict__ sm_v,
+                                                                 const VT* __restrict__ r, const VT* __restrict__ e,
+                                                                 VT* __restrict__ r2, const Scalars* sc) {
+    if (sc->converged) return;
+    using CT = typename CoefStore<CK>::T;
+    const CT* sm = reinterpret_cast<const CT*>(sm_v);
+    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
+    if (x >= g.nx || y >= g.ny) return;
+    const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
+    const long long sy = g.nx, sz = (long long)g.nx * g.ny;
+    const int xm = wrap_or_neg(x - 1, g.nx, g.periodic & 1), xp = wrap_or_neg(x + 1, g.nx, g.periodic & 1);
+    const int ym = wrap_or_neg(y - 1, g.ny, g.periodic & 2), yp = wrap_or_neg(y + 1, g.ny, g.periodic & 2);
+    for (int z = z0; z < z1; z++) {
+        const long long i = x + sy * y + sz * z;
+        const int zm = wrap_or_neg(z - 1, g.nz, g.periodic & 4), zp = wrap_or_neg(z + 1, g.nz, g.periodic & 4);
+        const float4 own = unpack<CK>(sm[i]);
+        const float bxh = xp >= 0 ? unpack<CK>(sm[i + (xp - x)]).x : 0.f;
+        const float byh = yp >= 0 ? unpack<CK>(sm[i + (yp - y) * sy]).y : 0.f;
+        const float bzh = zp >= 0 ? unpack<CK>(sm[i + (zp - z) * sz]).z : 0.f;
+        float nsum = 0.f;
+        nsum = fmaf(own.x, xm >= 0 ? to_f(e[i + (xm - x)]) : 0.f, nsum);
+        nsum = fmaf(bxh, xp >= 0 ? to_f(e[i + (xp - x)]) : 0.f, nsum);
+        nsum = fmaf(own.y, ym >= 0 ? to_f(e[i + (ym - y) * sy]) : 0.f, nsum);
+        nsum = fmaf(byh, yp >= 0 ? to_f(e[i + (yp - y) * sy]) : 0.f, nsum);
+        nsum = fmaf(own.z, zm >= 0 ? to_f(e[i + (zm - z) * sz]) : 0.f, nsum);
+        nsum = fmaf(bzh, zp >= 0 ? to_f(e[i + (zp - z) * sz]) : 0.f, nsum);
+        r2[i] = from_f<VT>(to_f(r[i]) - (own.w * to_f(e[i]) - nsum));
+    }
+}
+
+// The coarse-grid correction of level l >= 1 for its right-hand side lv[l].r:
+// fused passes on fused levels (two visits on W-cycle levels, the second on
+// the residual of the first), the per-level / bottom kernels below.  Returns
+// the buffer that holds the correction.
+template <int CK, class VT>
+static const void* fused_solve_level(const MGPlan& P, int l, double* partials, long long n_active, cudaStream_t s) {
+    if (l >= P.fused_levels) {
+        mg_vcycle_from(P, l, s);
+        return P.lv[l].e;
+    }
+    const MGLevel &L = P.lv[l], &C = P.lv[l + 1];
+    auto visit = [&](const void* rhs, void* out, const void* accum) {
+        pre_impl<CK, VT, VT, false, false>(L.L.g, C.L.g, L.sm, rhs, nullptr, nullptr, L.e, C.r, P.sc, partials,
+                                           O_PRE_COARSE, s);
+        const void* ec = fused_solve_level<CK, VT>(P, l + 1, partials, n_active, s);
+        post_impl<CK, VT, VT, false, false>(L.L.g, C.L.g, L.sm, L.e, ec, rhs, out, accum, P.prolong, P.sc, partials,
+                                            n_active, O_POST_COARSE, s);
+    };
+    visit(L.r, L.eo, nullptr);
+    if (P.w_from > 0 && l >= P.w_from) {
+        k_level_residual<CK, VT><<<L.L.grid, L.L.block, 0, s>>>(L.L.g, L.sm, (const VT*)L.r, (const VT*)L.eo,
+                                                               (VT*)L.r2, P.sc);
+        visit(L.r2, L.eo2, L.eo);
+        return L.eo2;
+    }
+    return L.eo;
 }
 
 template <int CK, class VT>
 static void vcycle_fused_impl(const MGPlan& P, const float* r_in, const float* q, float* r_out, bool update,
                               double* partials, long long n_active, cudaStream_t s) {
-    const int F = P.fused_levels;
     if (update)
         pre_impl<CK, float, VT, true, true>(P.lv[0].L.g, P.lv[1].L.g, P.lv[0].sm, r_in, q, r_out, P.e0, P.lv[1].r,
                                             P.sc, partials, CK == 0 ? O_PRE_F32_UPD : O_PRE_LO_UPD, s);
     else
         pre_impl<CK, float, VT, false, true>(P.lv[0].L.g, P.lv[1].L.g, P.lv[0].sm, r_in, nullptr, nullptr, P.e0,
                                              P.lv[1].r, P.sc, partials, CK == 0 ? O_PRE_F32 : O_PRE_LO, s);
-    for (int l = 1; l < F; l++) {
-        const MGLevel &L = P.lv[l], &C = P.lv[l + 1];
-        pre_impl<CK, VT, VT, false, false>(L.L.g, C.L.g, L.sm, L.r, nullptr, nullptr, L.e, C.r, P.sc, partials,
-                                           O_PRE_COARSE, s);
-    }
-    mg_vcycle_from(P, F, s);
-    for (int l = F - 1; l >= 1; l--) {
-        const MGLevel &L = P.lv[l], &C = P.lv[l + 1];
-        const void* ec = (l + 1 < F) ? C.eo : C.e;
-        post_impl<CK, VT, VT, false, false>(L.L.g, C.L.g, L.sm, L.e, ec, L.r, L.eo, P.prolong, P.sc, partials,
-                                            n_active, O_POST_COARSE, s);
-    }
-    const void* ec1 = (1 < F) ? P.lv[1].eo : P.lv[1].e;
+    const void* ec1 = fused_solve_level<CK, VT>(P, 1, partials, n_active, s);
     post_impl<CK, float, VT, true, true>(P.lv[0].L.g, P.lv[1].L.g, P.lv[0].sm, P.e0, ec1, update ? r_out : r_in,
-                                         P.lv[0].e, P.prolong, P.sc, partials, n_active,
+                                         P.lv[0].e, nullptr, P.prolong, P.sc, partials, n_active,
                                          CK == 0 ? O_POST_F32 : O_POST_LO, s);
 }
 
@@ -756,14 +811,14 @@ void mg_fused_post(const MGPlan& P, const float* r, double* partials, long long 
     const void* sm = P.lv[0].sm;
     const void* ec1 = (1 < P.fused_levels) ? P.lv[1].eo : P.lv[1].e;
     if (P.precision == 1)
-        post_impl<1, float, __half, true, true>(g, gc, sm, P.e0, ec1, r, P.lv[0].e, P.prolong, P.sc, partials, n_active,
-                                                O_POST_LO, s);
+        post_impl<1, float, __half, true, true>(g, gc, sm, P.e0, ec1, r, P.lv[0].e, nullptr, P.prolong, P.sc, partials,
+                                                n_active, O_POST_LO, s);
     else if (P.precision == 2)
-        post_impl<2, float, __nv_bfloat16, true, true>(g, gc, sm, P.e0, ec1, r, P.lv[0].e, P.prolong, P.sc, partials,
-                                                       n_active, O_POST_LO, s);
+        post_impl<2, float, __nv_bfloat16, true, true>(g, gc, sm, P.e0, ec1, r, P.lv[0].e, nullptr, P.prolong, P.sc,
+                                                       partials, n_active, O_POST_LO, s);
     else
-        post_impl<0, float, float, true, true>(g, gc, sm, P.e0, ec1, r, P.lv[0].e, P.prolong, P.sc, partials, n_active,
-                                               O_POST_F32, s);
+        post_impl<0, float, float, true, true>(g, gc, sm, P.e0, ec1, r, P.lv[0].e, nullptr, P.prolong, P.sc, partials,
+                                               n_active, O_POST_F32, s);
 }
 
 template <int CK, class VT, class VTc, bool UPDATE, bool FINE>

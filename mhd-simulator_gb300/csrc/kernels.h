@@ -85,8 +85,37 @@ struct MGLevel {
     void* tmp;       // half-step scratch for levels with odd periodic extents
     void* eo;        // post-smoothing output of a fused level >= 1 (level precision)
     void* sm;        // smoother records (beta_x, beta_y, beta_z, diagonal) of a fused level
+    void* r2;        // second-visit right-hand side of a fused W-cycle level (level precision)
+    void* eo2;       // second-visit output of a fused W-cycle level (level precision)
     bool odd_periodic;
 };
+// The levels of the bottom sub-cycle kernel (shared-memory offsets in floats
+// / float4s).
+struct BottomLevel {
+    Grid3 g;
+    int n;
+    int off;          // r at off, e at off + n, scratch at off + 2n (floats)
+    int coff;         // coefficient records at coff (float4s)
+    int xoff;         // packed cell coordinates, red cells first, at xoff (ints, in float units)
+    int nred;         // cells of colour 0
+    const void* coef; // level-precision records (beta_x, beta_y, beta_z, reaction)
+    void* r;          // level residual in global memory (level precision)
+    void* e;          // level correction in global memory (level precision)
+    bool odd;         // odd periodic extent: half-steps out of place
+};
+enum { BOP_PRE = 0, BOP_POST, BOP_COARSE, BOP_SAVE_RESID, BOP_ADD_SAVED };
+constexpr int BOTTOM_MAX_OPS = 256;
+struct BottomPlan {
+    int nl;
+    BottomLevel lv[8];
+    const float* ainv;
+    int m;
+    float w;
+    int nops;
+    unsigned char ops[BOTTOM_MAX_OPS];  // (op << 4) | level
+};
+constexpr size_t BOTTOM_SMEM_MAX = 200 * 1024;
+
 struct MGPlan {
     int precision;  // 0 fp32, 1 fp16, 2 bf16
     int nlevels;
@@ -97,6 +126,10 @@ struct MGPlan {
     Scalars* sc;
     bool staged;    // finest level through the shared-memory staged kernels
     int fused_levels;  // levels 0 .. fused_levels-1 run as fused pre-/post-smoothing passes (0: none)
+    int bottom_from;   // levels from here down run in one bottom sub-cycle kernel (0: none)
+    int w_from;        // levels from here down (>= 1) take two coarse visits: a W-cycle (0: V-cycle)
+    size_t bottom_smem;
+    BottomPlan bottom;
     float* e0;         // fine-level pre-smoothed correction of the fused passes
 };
 void mg_build(const MGPlan& P, cudaStream_t s);
@@ -106,6 +139,7 @@ void mg_fine_restrict(const MGPlan& P, cudaStream_t s);
 void mg_fine_prolong(const MGPlan& P, cudaStream_t s);
 void mg_vcycle(const MGPlan& P, cudaStream_t s);
 void mg_vcycle_from(const MGPlan& P, int l0, cudaStream_t s);
+void mg_plan_bottom(MGPlan& P);
 
 // ---- pipelined CG with fused V-cycle passes (fused_kernels.cu, fine_kernels.cu)
 bool fused_supported(const Grid3& g);

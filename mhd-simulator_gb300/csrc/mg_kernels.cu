@@ -10,11 +10,14 @@
 //   prolongation          e_l    += w P e_{l+1}          (w = 2 by default)
 // which is a coarse correction of w P (P^T A P)^-1 P^T.  Smoothing is one
 // red-black Gauss-Seidel sweep before (red, black) and after (black, red) the
-// coarse correction, and the coarsest level (every extent <= 2, at most 8
+// coarse correction, and the coarsest level (every extent <= 4, at most 64
 // cells) is solved exactly with a dense inverse, so the V-cycle is a fixed
 // symmetric operator.
 // Level fields (coefficients and vectors of levels >= 1, the fine smoother's
 // coefficients) are FP32, FP16 or BF16; arithmetic is FP32.
+#include <algorithm>
+#include <functional>
+
 #include "kernels.h"
 
 namespace mhdproj {
@@ -397,6 +400,239 @@ __global__ void k_coarse_invert(Grid3 g, const float4* __restrict__ coef, float*
     }
 }
 
+// -------------------------------------------------- bottom sub-cycle
+// The levels of at most 4096 cells in one block of 1024 threads: the whole
+// sub-V-cycle below level B (pre-smoothing and restriction down, the exact
+// coarsest solve, prolongation and post-smoothing up) runs out of shared
+// memory with a barrier between steps instead of a launch per step.  The
+// arithmetic of each cell is that of k_smooth / k_restrict / k_prolong /
+// k_coarse_solve on the same level fields.
+constexpr int BOTTOM_THREADS = 1024;
+
+template <int CK, class VT>
+__global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, const Scalars* sc) {
+    if (sc->converged) return;
+    extern __shared__ float4 bsm4[];
+    float* bsm = reinterpret_cast<float*>(bsm4);
+    const int t = threadIdx.x, nt = blockDim.x;
+    __shared__ int fill[8][2];
+    if (t < 16) fill[t >> 1][t & 1] = 0;
+    __syncthreads();
+    // Per level: coefficient records, and the cells' packed coordinates
+    // (x | y << 10 | z << 20) listed red first, so loops run over the cells
+    // of one colour without index arithmetic.
+    for (int l = 0; l < B.nl; l++) {
+        const BottomLevel& L = B.lv[l];
+        float4* c = bsm4 + L.coff;
+        int* cells = reinterpret_cast<int*>(bsm + L.xoff);
+        for (int i = t; i < L.n; i += nt) {
+            c[i] = ldc<CK>(L.coef, i);
+            const int x = i % L.g.nx, y = (i / L.g.nx) % L.g.ny, z = i / (L.g.nx * L.g.ny);
+            const int col = (x + y + z) & 1;
+            const int k = atomicAdd(&fill[l][col], 1);
+            cells[col ? L.nred + k : k] = x | (y << 10) | (z << 20);
+        }
+    }
+    {
+        const BottomLevel& L = B.lv[0];
+        float* r = bsm + L.off;
+        const VT* rg = reinterpret_cast<const VT*>(L.r);
+        for (int i = t; i < L.n; i += nt) r[i] = to_f(rg[i]);
+    }
+    __syncthreads();
+    auto nb = [](int c, int n, bool per) { return wrap_or_neg(c, n, per); };
+    // the diagonal replaces the reaction in each record (k_smooth's sum order)
+    for (int l = 0; l < B.nl; l++) {
+        const BottomLevel& L = B.lv[l];
+        const Grid3& g = L.g;
+        float4* c = bsm4 + L.coff;
+        float* dtmp = bsm + L.off + 2 * L.n;  // scratch until the cycle starts
+        const bool px = g.periodic & 1, py = g.periodic & 2, pz = g.periodic & 4;
+        for (int i = t; i < L.n; i += nt) {
+            const int x = i % g.nx, y = (i / g.nx) % g.ny, z = i / (g.nx * g.ny);
+            const int xp = nb(x + 1, g.nx, px), yp = nb(y + 1, g.ny, py), zp = nb(z + 1, g.nz, pz);
+            const float4 cc = c[i];
+            const float bxh = xp >= 0 ? c[i + (xp - x)].x : 0.f;
+            const float byh = yp >= 0 ? c[i + (yp - y) * g.nx].y : 0.f;
+            const float bzh = zp >= 0 ? c[i + (zp - z) * g.nx * g.ny].z : 0.f;
+            dtmp[i] = ((cc.x + bxh) + (cc.y + byh)) + ((cc.z + bzh) + cc.w);
+        }
+    }
+    __syncthreads();
+    for (int l = 0; l < B.nl; l++) {
+        const BottomLevel& L = B.lv[l];
+        float4* c = bsm4 + L.coff;
+        const float* dtmp = bsm + L.off + 2 * L.n;
+        for (int i = t; i < L.n; i += nt) c[i].w = dtmp[i];
+    }
+    __syncthreads();
+    // sum of beta * e over the six neighbours (k_smooth order) and the diagonal
+    auto stencil = [&](const BottomLevel& L, const float4* c, const float* e, int x, int y, int z, int i, float acc,
+                       float* d) {
+        const Grid3& g = L.g;
+        const bool px = g.periodic & 1, py = g.periodic & 2, pz = g.periodic & 4;
+        const int sy = g.nx, sz = g.nx * g.ny;
+        const int xm = nb(x - 1, g.nx, px), xp = nb(x + 1, g.nx, px);
+        const int ym = nb(y - 1, g.ny, py), yp = nb(y + 1, g.ny, py);
+        const int zm = nb(z - 1, g.nz, pz), zp = nb(z + 1, g.nz, pz);
+        const float4 cc = c[i];
+        const float bxh = xp >= 0 ? c[i + (xp - x)].x : 0.f;
+        const float byh = yp >= 0 ? c[i + (yp - y) * sy].y : 0.f;
+        const float bzh = zp >= 0 ? c[i + (zp - z) * sz].z : 0.f;
+        *d = cc.w;
+        acc = fmaf(cc.x, xm >= 0 ? e[i + (xm - x)] : 0.f, acc);
+        acc = fmaf(bxh, xp >= 0 ? e[i + (xp - x)] : 0.f, acc);
+        acc = fmaf(cc.y, ym >= 0 ? e[i + (ym - y) * sy] : 0.f, acc);
+        acc = fmaf(byh, yp >= 0 ? e[i + (yp - y) * sy] : 0.f, acc);
+        acc = fmaf(cc.z, zm >= 0 ? e[i + (zm - z) * sz] : 0.f, acc);
+        acc = fmaf(bzh, zp >= 0 ? e[i + (zp - z) * sz] : 0.f, acc);
+        return acc;
+    };
+    auto half_step = [&](int l, int color, bool zero) {
+        const BottomLevel& L = B.lv[l];
+        const Grid3& g = L.g;
+        const float4* c = bsm4 + L.coff;
+        const int* cells = reinterpret_cast<const int*>(bsm + L.xoff);
+        const float* r = bsm + L.off;
+        float* e = bsm + L.off + L.n;
+        float* tmp = bsm + L.off + 2 * L.n;
+        if (zero) {  // from zero: red cells r / d, black cells 0
+            for (int k = t; k < L.n; k += nt) {
+                const int cc = cells[k], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+                const int i = x + g.nx * (y + g.ny * z);
+                float val = 0.f;
+                if (k < L.nred) {
+                    const float d = c[i].w;
+                    if (d > 0.f) val = r[i] / d;
+                }
+                e[i] = val;
+            }
+            __syncthreads();
+            return;
+        }
+        const int k0 = color ? L.nred : 0, k1 = color ? L.n : L.nred;
+        for (int k = k0 + t; k < k1; k += nt) {
+            const int cc = cells[k], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+            const int i = x + g.nx * (y + g.ny * z);
+            float d;
+            const float acc = stencil(L, c, e, x, y, z, i, r[i], &d);
+            const float val = d > 0.f ? acc / d : 0.f;
+            if (L.odd) tmp[i] = val;
+            else e[i] = val;
+        }
+        __syncthreads();
+        if (L.odd) {
+            for (int k = k0 + t; k < k1; k += nt) {
+                const int cc = cells[k], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+                const int i = x + g.nx * (y + g.ny * z);
+                e[i] = tmp[i];
+            }
+            __syncthreads();
+        }
+    };
+    auto restrict_to = [&](int l) {  // level l -> l+1
+        const BottomLevel &F = B.lv[l], &C = B.lv[l + 1];
+        const Grid3 &g = F.g, &gc = C.g;
+        const float4* c = bsm4 + F.coff;
+        const float* r = bsm + F.off;
+        const float* e = bsm + F.off + F.n;
+        float* rc = bsm + C.off;
+        const int* ccells = reinterpret_cast<const int*>(bsm + C.xoff);
+        for (int k = t; k < C.n; k += nt) {
+            const int cq = ccells[k], X = cq & 1023, Y = (cq >> 10) & 1023, Z = cq >> 20;
+            float part = 0.f;
+            for (int dz = 0; dz < 2; dz++)
+                for (int dy = 0; dy < 2; dy++)
+                    for (int dx = 0; dx < 2; dx++) {
+                        const int x = 2 * X + dx, y = 2 * Y + dy, z = 2 * Z + dz;
+                        if (x >= g.nx || y >= g.ny || z >= g.nz) continue;
+                        const int i = x + g.nx * (y + g.ny * z);
+                        float d;
+                        const float nsum = stencil(F, c, e, x, y, z, i, 0.f, &d);
+                        part += r[i] - (d * e[i] - nsum);
+                    }
+            rc[X + gc.nx * (Y + gc.ny * Z)] = 0.25f * part;
+        }
+        __syncthreads();
+    };
+    auto prolong_from = [&](int l) {  // level l+1 -> l
+        const BottomLevel &F = B.lv[l], &C = B.lv[l + 1];
+        const Grid3 &g = F.g, &gc = C.g;
+        float* e = bsm + F.off + F.n;
+        const float* ec = bsm + C.off + C.n;
+        const int* cells = reinterpret_cast<const int*>(bsm + F.xoff);
+        for (int k = t; k < F.n; k += nt) {
+            const int cc = cells[k], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+            const int i = x + g.nx * (y + g.ny * z);
+            e[i] = fmaf(B.w, ec[(x >> 1) + gc.nx * ((y >> 1) + gc.ny * (z >> 1))], e[i]);
+        }
+        __syncthreads();
+    };
+    // The cycle program (host-generated): PRE / POST visits of a level,
+    // the exact coarsest solve, and the second coarse visit of a W-cycle
+    // level: save e and replace r by r - A e, then add the saved e back.
+    for (int k = 0; k < B.nops; k++) {
+        const int op = B.ops[k] >> 4, l = B.ops[k] & 15;
+        if (op == BOP_PRE) {
+            half_step(l, 0, true);
+            half_step(l, 1, false);
+            restrict_to(l);
+        } else if (op == BOP_POST) {
+            prolong_from(l);
+            half_step(l, 1, false);
+            half_step(l, 0, false);
+        } else if (op == BOP_COARSE) {
+            const BottomLevel& K = B.lv[l];
+            const float* r = bsm + K.off;
+            float* e = bsm + K.off + K.n;
+            if (t < B.m) {
+                float sacc = 0.0f;
+                for (int q = 0; q < B.m; q++) sacc = fmaf(B.ainv[t * B.m + q], r[q], sacc);
+                e[t] = sacc;
+            }
+            __syncthreads();
+        } else if (op == BOP_SAVE_RESID) {
+            const BottomLevel& L = B.lv[l];
+            const Grid3& g = L.g;
+            const float4* c = bsm4 + L.coff;
+            const int* cells = reinterpret_cast<const int*>(bsm + L.xoff);
+            float* r = bsm + L.off;
+            const float* e = bsm + L.off + L.n;
+            float* es = bsm + L.off + 3 * L.n;
+            float rn[4];  // each thread's cells, at most 4096 / 1024
+            int cnt = 0;
+            for (int q = t; q < L.n; q += nt) {
+                const int cc = cells[q], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+                const int i = x + g.nx * (y + g.ny * z);
+                float d;
+                const float nsum = stencil(L, c, e, x, y, z, i, 0.f, &d);
+                rn[cnt++] = r[i] - (d * e[i] - nsum);
+            }
+            __syncthreads();
+            cnt = 0;
+            for (int q = t; q < L.n; q += nt) {
+                const int cc = cells[q], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+                const int i = x + g.nx * (y + g.ny * z);
+                r[i] = rn[cnt++];
+                es[i] = e[i];
+            }
+            __syncthreads();
+        } else if (op == BOP_ADD_SAVED) {
+            const BottomLevel& L = B.lv[l];
+            float* e = bsm + L.off + L.n;
+            const float* es = bsm + L.off + 3 * L.n;
+            for (int i = t; i < L.n; i += nt) e[i] += es[i];
+            __syncthreads();
+        }
+    }
+    {
+        const BottomLevel& L = B.lv[0];
+        const float* e = bsm + L.off + L.n;
+        VT* eg = reinterpret_cast<VT*>(L.e);
+        for (int i = t; i < L.n; i += nt) eg[i] = from_f<VT>(e[i]);
+    }
+}
+
 // ------------------------------------------------------------- host side
 template <int CK, class VT>
 static void enqueue_smooth(const MGPlan& P, int l, int color, bool zero, cudaStream_t s) {
@@ -440,7 +676,9 @@ static void enqueue_smooth(const MGPlan& P, int l, int color, bool zero, cudaStr
 template <int CK, class VT>
 static void vcycle_impl(const MGPlan& P, int l0, cudaStream_t s) {
     const int nl = P.nlevels;
-    for (int l = l0; l + 1 < nl; l++) {
+    // levels from P.bottom_from down run in the bottom sub-cycle kernel
+    const int lb = (P.bottom_from > 0 && P.bottom_from >= l0) ? P.bottom_from : nl;
+    for (int l = l0; l + 1 < nl && l < lb; l++) {
         enqueue_smooth<CK, VT>(P, l, 0, true, s);
         enqueue_smooth<CK, VT>(P, l, 1, false, s);
         const MGLevel &F = P.lv[l], &C = P.lv[l + 1];
@@ -454,10 +692,14 @@ static void vcycle_impl(const MGPlan& P, int l0, cudaStream_t s) {
             k_restrict<CK, VT, false, VT><<<F.L.grid, F.L.block, 0, s>>>(F.L.g, C.L.g, coef, (const VT*)F.r,
                                                                          (const VT*)F.e, (VT*)C.r, P.sc);
     }
-    const MGLevel& K = P.lv[nl - 1];
-    if (nl == 1) k_coarse_solve<float, true><<<1, 64, 0, s>>>(P.m, P.ainv, (const float*)K.r, (float*)K.e, P.sc);
-    else k_coarse_solve<VT, false><<<1, 64, 0, s>>>(P.m, P.ainv, (const VT*)K.r, (VT*)K.e, P.sc);
-    for (int l = nl - 2; l >= l0; l--) {
+    if (lb < nl) {
+        k_bottom_vcycle<CK, VT><<<1, BOTTOM_THREADS, P.bottom_smem, s>>>(P.bottom, P.sc);
+    } else {
+        const MGLevel& K = P.lv[nl - 1];
+        if (nl == 1) k_coarse_solve<float, true><<<1, 64, 0, s>>>(P.m, P.ainv, (const float*)K.r, (float*)K.e, P.sc);
+        else k_coarse_solve<VT, false><<<1, 64, 0, s>>>(P.m, P.ainv, (const VT*)K.r, (VT*)K.e, P.sc);
+    }
+    for (int l = std::min(nl - 2, lb - 1); l >= l0; l--) {
         const MGLevel &F = P.lv[l], &C = P.lv[l + 1];
         if (l == 0)
             k_prolong<float, VT><<<F.L.grid, F.L.block, 0, s>>>(F.L.g, C.L.g, (float*)F.e, (const VT*)C.e, P.prolong, P.sc);
@@ -526,7 +768,100 @@ void mg_build(const MGPlan& P, cudaStream_t s) {
 }
 
 cudaError_t mg_prepare_attributes() {
-    return cudaFuncSetAttribute(k_coarse_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 128 * 8);
+    cudaError_t e = cudaFuncSetAttribute(k_coarse_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 128 * 8);
+    const int bmax = (int)BOTTOM_SMEM_MAX;
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bottom_vcycle<0, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bmax);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bottom_vcycle<1, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, bmax);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_bottom_vcycle<2, __nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bmax);
+    return e;
+}
+
+// The bottom sub-cycle from the first level of at most 4096 cells (level >= 1),
+// if its levels fit the shared-memory budget.
+void mg_plan_bottom(MGPlan& P) {
+    P.bottom_from = 0;
+    P.bottom_smem = 0;
+    // W-cycle from the first coarse level of at most 32^3 cells: those levels
+    // cost little next to the fine level and their second visit cuts the CG
+    // iterations by about a third on the jet workloads
+    P.w_from = 0;
+    for (int l = 1; l + 1 < P.nlevels; l++)
+        if (P.lv[l].L.g.n() <= 32768) {
+            P.w_from = l;
+            break;
+        }
+    int lb = -1;
+    for (int l = 1; l < P.nlevels; l++)
+        if (P.lv[l].L.g.n() <= 4096) {
+            lb = l;
+            break;
+        }
+    if (lb < 0 || P.nlevels - lb > 8 || P.m > BOTTOM_THREADS) return;
+    BottomPlan& B = P.bottom;
+    B.nl = P.nlevels - lb;
+    size_t f4 = 0, fl = 0;  // float4 and float counts
+    for (int k = 0; k < B.nl; k++) f4 += (size_t)P.lv[lb + k].L.g.n();
+    for (int k = 0; k < B.nl; k++) {
+        const MGLevel& L = P.lv[lb + k];
+        BottomLevel& b = B.lv[k];
+        b.g = L.L.g;
+        b.n = (int)L.L.g.n();
+        b.coef = P.precision == 0 ? (const void*)L.coef32 : L.coef_lo;
+        b.r = L.r;
+        b.e = L.e;
+        b.odd = L.odd_periodic;
+        b.coff = k == 0 ? 0 : B.lv[k - 1].coff + B.lv[k - 1].n;
+        b.off = (int)(4 * f4 + fl);
+        fl += 4 * (size_t)b.n;  // r, e, scratch, saved e
+        b.xoff = (int)(4 * f4 + fl);
+        fl += (size_t)b.n;      // cell list (ints)
+        int nred = 0;
+        for (int z = 0; z < b.g.nz; z++)
+            for (int y = 0; y < b.g.ny; y++)
+                for (int x = 0; x < b.g.nx; x++) nred += ((x + y + z) & 1) == 0;
+        b.nred = nred;
+    }
+    for (int k = 0; k < B.nl; k++)
+        if (B.lv[k].g.nx > 1023 || B.lv[k].g.ny > 1023 || B.lv[k].g.nz > 1023) return;
+    B.ainv = P.ainv;
+    B.m = P.m;
+    B.w = P.prolong;
+    const size_t bytes = (4 * f4 + fl) * sizeof(float);
+    if (bytes > BOTTOM_SMEM_MAX) return;
+    // the cycle program: level k's coarse correction takes two visits when
+    // level lb + k is a W-cycle level (the program is cut back to V visits
+    // if it would not fit)
+    for (int attempt = 0; attempt < 2; attempt++) {
+        const bool w_ok = attempt == 0;
+        B.nops = 0;
+        bool fits = true;
+        auto emit = [&](int op, int l) {
+            if (B.nops < BOTTOM_MAX_OPS) B.ops[B.nops++] = (unsigned char)((op << 4) | l);
+            else fits = false;
+        };
+        std::function<void(int)> solve_level = [&](int k) {
+            if (k == B.nl - 1) {
+                emit(BOP_COARSE, k);
+                return;
+            }
+            const bool w = w_ok && P.w_from > 0 && lb + k >= P.w_from;
+            emit(BOP_PRE, k);
+            solve_level(k + 1);
+            emit(BOP_POST, k);
+            if (w) {
+                emit(BOP_SAVE_RESID, k);
+                emit(BOP_PRE, k);
+                solve_level(k + 1);
+                emit(BOP_POST, k);
+                emit(BOP_ADD_SAVED, k);
+            }
+        };
+        solve_level(0);
+        if (fits) break;
+    }
+    P.bottom_from = lb;
+    P.bottom_smem = bytes;
 }
 
 }  // namespace mhdproj
