@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstddef>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -248,7 +249,7 @@ static int build_levels(mhdproj_ctx* ctx) {
             for (int l = 0; l < F; l++) {
                 CK(dalloc(ctx, (char**)&P.lv[l].sm, (size_t)P.lv[l].L.g.n() * rbytes));
                 if (l > 0) CK(dalloc(ctx, (char**)&P.lv[l].eo, (size_t)P.lv[l].L.g.n() * vbytes));
-                if (l > 0 && P.w_from > 0 && l >= P.w_from) {
+                if (l > 0 && P.w_from > 0 && l >= P.w_from && l <= P.w_to) {
                     CK(dalloc(ctx, (char**)&P.lv[l].r2, (size_t)P.lv[l].L.g.n() * vbytes));
                     CK(dalloc(ctx, (char**)&P.lv[l].eo2, (size_t)P.lv[l].L.g.n() * vbytes));
                 }
@@ -529,7 +530,7 @@ static uint64_t kernels_vcycle_from(const MGPlan& P, int from) {
 static uint64_t kernels_fused_solve(const MGPlan& P, int l) {
     if (l >= P.fused_levels) return kernels_vcycle_from(P, l);
     const uint64_t visit = 2 + kernels_fused_solve(P, l + 1);  // pre, coarser levels, post
-    if (P.w_from > 0 && l >= P.w_from) return 2 * visit + 1;  // + the residual of the second visit
+    if (P.w_from > 0 && l >= P.w_from && l <= P.w_to) return 2 * visit + 1;  // + the second visit's residual
     return visit;
 }
 static uint64_t kernels_precondition(const mhdproj_ctx* ctx) {
@@ -668,7 +669,21 @@ static int solve(mhdproj_ctx* ctx, float* x_hi, float* x_lo, mhdproj_stats* st, 
         }
         if (ctx->pipelined) launch_accumulate_pipelined(ctx->L, x_hi, x_lo, ctx->e, ctx->p, ctx->p1, ctx->sc, ctx->stream);
         else launch_accumulate(ctx->L, F, x_hi, x_lo, ctx->stream);
-        passes++;
+        if (ctx->h_sc->breakdown && ctx->use_mg && ctx->mg.w_from > 0) {
+            // The W-cycle step lost positive definiteness on this operator:
+            // V-cycles from here on (the iteration graph is recaptured), and
+            // the pass does not count against the refinement limit.
+            ctx->mg.w_disabled = true;
+            mg_plan_bottom(ctx->mg);
+            if (ctx->it_graph) {
+                cudaGraphExecDestroy(ctx->it_graph);
+                ctx->it_graph = nullptr;
+            }
+            CK(cudaMemsetAsync(reinterpret_cast<char*>(ctx->sc) + offsetof(Scalars, breakdown), 0, sizeof(int),
+                               ctx->stream));
+        } else {
+            passes++;
+        }
         launch_residual(ctx->L, F, x_hi, x_lo, ctx->stream);
         enqueue_pass_start(ctx);
         ctx->launches += 2 + kernels_pass_start(ctx);  // accumulate, residual, pass start

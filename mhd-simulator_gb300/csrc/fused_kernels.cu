@@ -747,7 +747,7 @@ static const void* fused_solve_level(const MGPlan& P, int l, double* partials, l
                                             n_active, O_POST_COARSE, s);
     };
     visit(L.r, L.eo, nullptr);
-    if (P.w_from > 0 && l >= P.w_from) {
+    if (P.w_from > 0 && l >= P.w_from && l <= P.w_to) {
         k_level_residual<CK, VT><<<L.L.grid, L.L.block, 0, s>>>(L.L.g, L.sm, (const VT*)L.r, (const VT*)L.eo,
                                                                (VT*)L.r2, P.sc);
         visit(L.r2, L.eo2, L.eo);

@@ -127,7 +127,8 @@ struct MGPlan {
     bool staged;    // finest level through the shared-memory staged kernels
     int fused_levels;  // levels 0 .. fused_levels-1 run as fused pre-/post-smoothing passes (0: none)
     int bottom_from;   // levels from here down run in one bottom sub-cycle kernel (0: none)
-    int w_from;        // levels from here down (>= 1) take two coarse visits: a W-cycle (0: V-cycle)
+    int w_from, w_to;  // levels w_from..w_to (>= 1) take two coarse visits, a W-cycle step (0: none)
+    bool w_disabled;   // the W-cycle step made the preconditioner indefinite here: V-cycles only
     size_t bottom_smem;
     BottomPlan bottom;
     float* e0;         // fine-level pre-smoothed correction of the fused passes

@@ -404,9 +404,11 @@ __global__ void k_coarse_invert(Grid3 g, const float4* __restrict__ coef, float*
 // The levels of at most 4096 cells in one block of 1024 threads: the whole
 // sub-V-cycle below level B (pre-smoothing and restriction down, the exact
 // coarsest solve, prolongation and post-smoothing up) runs out of shared
-// memory with a barrier between steps instead of a launch per step.  The
-// arithmetic of each cell is that of k_smooth / k_restrict / k_prolong /
-// k_coarse_solve on the same level fields.
+// memory with a barrier between steps instead of a launch per step.  Each
+// cell does the operations of k_smooth / k_restrict / k_prolong /
+// k_coarse_solve on the same level fields, with the diagonal summed once per
+// launch and the smoother's division by the fast reciprocal (a fixed factor
+// per cell, so the sub-cycle stays a fixed symmetric operator).
 constexpr int BOTTOM_THREADS = 1024;
 
 template <int CK, class VT>
@@ -497,13 +499,14 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
         float* e = bsm + L.off + L.n;
         float* tmp = bsm + L.off + 2 * L.n;
         if (zero) {  // from zero: red cells r / d, black cells 0
+#pragma unroll 4
             for (int k = t; k < L.n; k += nt) {
                 const int cc = cells[k], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
                 const int i = x + g.nx * (y + g.ny * z);
                 float val = 0.f;
                 if (k < L.nred) {
                     const float d = c[i].w;
-                    if (d > 0.f) val = r[i] / d;
+                    if (d > 0.f) val = __fdividef(r[i], d);
                 }
                 e[i] = val;
             }
@@ -511,12 +514,13 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
             return;
         }
         const int k0 = color ? L.nred : 0, k1 = color ? L.n : L.nred;
+#pragma unroll 2
         for (int k = k0 + t; k < k1; k += nt) {
             const int cc = cells[k], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
             const int i = x + g.nx * (y + g.ny * z);
             float d;
             const float acc = stencil(L, c, e, x, y, z, i, r[i], &d);
-            const float val = d > 0.f ? acc / d : 0.f;
+            const float val = d > 0.f ? __fdividef(acc, d) : 0.f;
             if (L.odd) tmp[i] = val;
             else e[i] = val;
         }
@@ -782,13 +786,18 @@ cudaError_t mg_prepare_attributes() {
 void mg_plan_bottom(MGPlan& P) {
     P.bottom_from = 0;
     P.bottom_smem = 0;
-    // W-cycle from the first coarse level of at most 32^3 cells: those levels
-    // cost little next to the fine level and their second visit cuts the CG
-    // iterations by about a third on the jet workloads
-    P.w_from = 0;
-    for (int l = 1; l + 1 < P.nlevels; l++)
+    // Two coarse visits (a W-cycle step) on the first coarse level of at most
+    // 32^3 cells: it costs little next to the fine level and cuts the CG
+    // iterations by about a quarter on the jet workloads; deeper levels keep
+    // V-cycles (their extra visits cost more barrier steps than they save).
+    // The second visit, e1 + B (r - A e1), is positive definite only while
+    // the inner cycle B converges on that level, which the weight-2 coarse
+    // correction does not guarantee; the solver falls back to V-cycles
+    // (w_disabled) when CG breaks down.
+    P.w_from = P.w_to = 0;
+    for (int l = 1; l + 1 < P.nlevels && !P.w_disabled; l++)
         if (P.lv[l].L.g.n() <= 32768) {
-            P.w_from = l;
+            P.w_from = P.w_to = l;  // two visits on that one level; V-cycles below it
             break;
         }
     int lb = -1;
@@ -845,7 +854,7 @@ void mg_plan_bottom(MGPlan& P) {
                 emit(BOP_COARSE, k);
                 return;
             }
-            const bool w = w_ok && P.w_from > 0 && lb + k >= P.w_from;
+            const bool w = w_ok && P.w_from > 0 && lb + k >= P.w_from && lb + k <= P.w_to;
             emit(BOP_PRE, k);
             solve_level(k + 1);
             emit(BOP_POST, k);
