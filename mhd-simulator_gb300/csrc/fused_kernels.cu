@@ -268,7 +268,9 @@ __global__ void __launch_bounds__(FT) k_presmooth_restrict(Grid3 g, Grid3 gc, co
     const RegionFetch<CK> F(g, x0, y0, t);
     const PairTasks T(g, x0, y0, t);
     const long long sxy = (long long)g.nx * g.ny;
-    Acc acc;
+    // ||r||^2 only steers the stop test and sigma: a per-thread FP32 sum,
+    // FP64 across threads and blocks
+    float rr_thread = 0.f;
     float part = 0.f;
     const int ox = x0 + 2 * tx, oy = y0 + ty;  // the thread's own pair
     const bool own_inside = ox < g.nx && oy < g.ny;
@@ -295,6 +297,7 @@ __global__ void __launch_bounds__(FT) k_presmooth_restrict(Grid3 g, Grid3 gc, co
             float* RN = &S.rn[P & 1][0][0];
             float* ER = &S.er[P][0][0];
             const bool zin = zA >= z0 && zA < z1;
+            float* rplane = UPDATE ? r_out + sxy * zA : nullptr;
 #pragma unroll
             for (int u = 0; u < 2; u++) {
                 const int o = T.roff[u];
@@ -311,9 +314,8 @@ __global__ void __launch_bounds__(FT) k_presmooth_restrict(Grid3 g, Grid3 gc, co
                 *reinterpret_cast<float2*>(RN + o) = rn;
                 *reinterpret_cast<float2*>(ER + o) = m ? make_float2(0.f, ev) : make_float2(ev, 0.f);
                 if (UPDATE && zin && T.rown[u] >= 0) {
-                    *reinterpret_cast<float2*>(r_out + T.rown[u] + sxy * zA) = rn;
-                    acc.add_prod(rn.x, rn.x);
-                    acc.add_prod(rn.y, rn.y);
+                    *reinterpret_cast<float2*>(rplane + T.rown[u]) = rn;
+                    rr_thread = fmaf(rn.x, rn.x, fmaf(rn.y, rn.y, rr_thread));
                 }
             }
         }
@@ -348,7 +350,7 @@ __global__ void __launch_bounds__(FT) k_presmooth_restrict(Grid3 g, Grid3 gc, co
             const int m = (y0 + ty + zC) & 1;  // red member of the own pair
             float d;
             part += gs_sum<CK>(C, CN, E, EM, EP, oo + m, 0.f, &d);
-            if (own_inside) st2<VT>(e + og + sxy * zC, *reinterpret_cast<const float2*>(E + oo));
+            if (own_inside) st2<VT>(e + (og + sxy * zC), *reinterpret_cast<const float2*>(E + oo));
             if (((zC - z0) & 1) || zC + 1 == z1) {
                 S.ypart[ty][tx] = part;
                 __syncthreads();
@@ -377,7 +379,7 @@ __global__ void __launch_bounds__(FT) k_presmooth_restrict(Grid3 g, Grid3 gc, co
     }
     cp_wait<0>();
     if (UPDATE) {
-        double v1[1] = {acc.total()};
+        double v1[1] = {(double)rr_thread};
         block_sum<1>(v1, sh);
         if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[8])) {
             double tot[1];

@@ -16,6 +16,7 @@
 // Level fields (coefficients and vectors of levels >= 1, the fine smoother's
 // coefficients) are FP32, FP16 or BF16; arithmetic is FP32.
 #include <algorithm>
+#include <cstdlib>
 #include <functional>
 
 #include "kernels.h"
@@ -331,16 +332,22 @@ __global__ void __launch_bounds__(TILE_THREADS) k_mg_build(Grid3 gf, Grid3 gc, c
     }
 }
 
-// Dense inverse of the coarsest operator by Gauss-Jordan in FP64, one block.
-// Rows of empty aggregates (diagonal 0) become identity rows and are zeroed
-// in the stored inverse.  The result is symmetrised.
-__global__ void k_coarse_invert(Grid3 g, const float4* __restrict__ coef, float* __restrict__ ainv) {
-    extern __shared__ double A[];  // m x 2m
+// Dense inverse of the coarsest operator (m <= 64 cells) in FP64, one column
+// per block: every block assembles A, factors it A = L L^T (Cholesky; the
+// operator is symmetric positive definite on the active cells) and solves
+// L L^T x = e_b for its column b.  Rows of empty aggregates (diagonal 0) are
+// identity rows during the factorisation and zero in the stored inverse.
+// Spreading the columns over blocks spreads the FP64 work over SMs; each
+// block's factorisation is the same computation, so the columns agree.
+__global__ void __launch_bounds__(256) k_coarse_invert(Grid3 g, const float4* __restrict__ coef,
+                                                       float* __restrict__ ainv) {
+    extern __shared__ double A[];  // m x m, then y/x vectors
     const int m = g.nx * g.ny * g.nz;
-    const int w = 2 * m;
     const int t = threadIdx.x, nt = blockDim.x;
+    const int b = blockIdx.x;
     __shared__ int active[64];
-    for (int k = t; k < m * w; k += nt) A[k] = 0.0;
+    double* v = A + m * m;  // right-hand side / solution
+    for (int k = t; k < m * m; k += nt) A[k] = 0.0;
     __syncthreads();
     if (t < m) {
         const int x = t % g.nx, y = (t / g.nx) % g.ny, z = t / (g.nx * g.ny);
@@ -354,50 +361,68 @@ __global__ void k_coarse_invert(Grid3 g, const float4* __restrict__ coef, float*
             const int lp = wrap_or_neg(p3[a] + 1, n3[a], g.periodic & (1 << a));
             if (lm >= 0 && lowb[a] != 0.0f) {
                 d += lowb[a];
-                A[t * w + (t + (lm - p3[a]) * stride)] -= lowb[a];
+                A[t * m + (t + (lm - p3[a]) * stride)] -= lowb[a];
             }
             if (lp >= 0) {
                 const int j = t + (lp - p3[a]) * stride;
                 const float bh = (a == 0 ? coef[j].x : (a == 1 ? coef[j].y : coef[j].z));
                 if (bh != 0.0f) {
                     d += bh;
-                    A[t * w + j] -= bh;
+                    A[t * m + j] -= bh;
                 }
             }
         }
-        A[t * w + t] += d;
+        A[t * m + t] += d;
         active[t] = d > 0.0;
-        A[t * w + m + t] = 1.0;
     }
     __syncthreads();
     if (t < m && !active[t]) {
-        for (int k = 0; k < m; k++) A[t * w + k] = 0.0;
-        A[t * w + t] = 1.0;
+        for (int k = 0; k < m; k++) A[t * m + k] = A[k * m + t] = 0.0;
+        A[t * m + t] = 1.0;
     }
     __syncthreads();
-    for (int c = 0; c < m; c++) {
-        const double piv = A[c * w + c];
-        __syncthreads();
-        const bool ok = fabs(piv) > 1e-300;
-        for (int k = t; k < w; k += nt)
-            if (ok) A[c * w + k] /= piv;
-        __syncthreads();
-        for (int k = t; k < m * w; k += nt) {
-            const int r = k / w, col = k % w;
-            if (r == c || !ok) continue;
-            const double f = A[r * w + c];
-            if (f != 0.0 && col != c) A[k] -= f * A[c * w + col];
+    // Cholesky, lower triangle in place (a non-positive pivot is treated as
+    // an empty row)
+    const int tx = t & 15, ty = t >> 4;
+    for (int j = 0; j < m; j++) {
+        if (t == 0) {
+            const double piv = A[j * m + j];
+            A[j * m + j] = piv > 1e-300 ? sqrt(piv) : 0.0;
         }
         __syncthreads();
-        for (int r = t; r < m; r += nt)
-            if (r != c && ok) A[r * w + c] = 0.0;
+        const double ljj = A[j * m + j];
+        for (int i = j + 1 + t; i < m; i += nt) A[i * m + j] = ljj > 0.0 ? A[i * m + j] / ljj : 0.0;
+        __syncthreads();
+        for (int i = j + 1 + ty; i < m; i += 16)
+            for (int k = j + 1 + tx; k <= i; k += 16) A[i * m + k] -= A[i * m + j] * A[k * m + j];
         __syncthreads();
     }
-    for (int k = t; k < m * m; k += nt) {
-        const int i = k / m, j = k % m;
-        const double v = (active[i] && active[j]) ? 0.5 * (A[i * w + m + j] + A[j * w + m + i]) : 0.0;
-        ainv[k] = (float)v;
+    // L y = e_b, then L^T x = y (one warp; rows in order)
+    if (t < 32) {
+        for (int i = 0; i < m; i++) {
+            double s = 0.0;
+            for (int k = t; k < i; k += 32) s += A[i * m + k] * v[k];
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (t == 0) {
+                const double lii = A[i * m + i];
+                v[i] = lii > 0.0 ? ((i == b ? 1.0 : 0.0) - s) / lii : 0.0;
+            }
+            __syncwarp();
+        }
+        for (int i = m - 1; i >= 0; i--) {
+            double s = 0.0;
+            for (int k = i + 1 + t; k < m; k += 32) s += A[k * m + i] * v[k];
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (t == 0) {
+                const double lii = A[i * m + i];
+                v[i] = lii > 0.0 ? (v[i] - s) / lii : 0.0;
+            }
+            __syncwarp();
+        }
     }
+    __syncthreads();
+    for (int i = t; i < m; i += nt)
+        ainv[i * m + b] = (active[i] && active[b]) ? (float)v[i] : 0.0f;
 }
 
 // -------------------------------------------------- bottom sub-cycle
@@ -767,12 +792,12 @@ void mg_build(const MGPlan& P, cudaStream_t s) {
             k_mg_build<0><<<C.L.grid, C.L.block, 0, s>>>(F.L.g, C.L.g, F.coef32, C.coef32, nullptr);
     }
     const MGLevel& K = P.lv[P.nlevels - 1];
-    const size_t smem = (size_t)P.m * 2 * P.m * sizeof(double);
-    k_coarse_invert<<<1, 256, smem, s>>>(K.L.g, K.coef32, P.ainv);
+    const size_t smem = ((size_t)P.m * P.m + P.m) * sizeof(double);
+    k_coarse_invert<<<P.m, 256, smem, s>>>(K.L.g, K.coef32, P.ainv);
 }
 
 cudaError_t mg_prepare_attributes() {
-    cudaError_t e = cudaFuncSetAttribute(k_coarse_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 128 * 8);
+    cudaError_t e = cudaFuncSetAttribute(k_coarse_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, (64 * 64 + 64) * 8);
     const int bmax = (int)BOTTOM_SMEM_MAX;
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bottom_vcycle<0, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bmax);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bottom_vcycle<1, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, bmax);
