@@ -18,9 +18,11 @@
 // region one cell wider than the next: the red values cover the tile with a
 // 2-cell halo, the black values a 1-cell halo, the residual the tile itself.
 // Halo cells are recomputed by both neighbouring tiles from the same inputs
-// in the same order, so the values agree bit for bit.  Inputs are staged with
-// zero-filling 16-byte cp.async two planes ahead of the red stage; a staged
-// row spans x0-4 .. x0+67 so every copy is a 16-byte-aligned group of cells.
+// in the same order, so the values agree bit for bit.  The smoother records
+// are staged in shared memory with zero-filling 16-byte cp.async one plane
+// ahead of the red stage (a staged row spans x0-4 .. x0+67, so every copy is
+// a 16-byte-aligned group of records); the vector inputs of the red stage go
+// to registers one plane ahead.  Three barriers per plane.
 //
 // The smoother reads per-cell records (beta_x, beta_y, beta_z of the low
 // faces, diagonal) prepared once per coefficient set, the diagonal rounded
@@ -46,12 +48,9 @@ constexpr int XO = 4;            // staged rows start at x0 - XO
 constexpr int RW = PX + 2 * XO;  // 72 staged columns: x0-4 .. x0+67
 constexpr int RH = FTY + 4;      // vector rows:  y0-2 .. y0+FTY+1
 constexpr int CH = FTY + 5;      // record rows:  y0-2 .. y0+FTY+2
-constexpr int NG = RW / 4;       // 18 four-cell groups per staged row
-constexpr int NVEC = RH * NG;    // 216 vector copies per plane
 constexpr int RP = (PX + 4) / 2; // 34 pairs of the 2-halo region (x0-2 .. x0+65)
 constexpr int NRED = RH * RP;    // 408 red-stage pair tasks
 constexpr int NBLK = (FTY + 2) * RP;  // 340 black-stage pair tasks (rows y0-1 .. y0+FTY)
-static_assert(NVEC <= FT, "one vector copy per thread");
 static_assert(NRED <= 2 * FT && NBLK <= 2 * FT, "two tasks per thread");
 
 template <class VT> __device__ __forceinline__ float2 ld2(const VT* p);
@@ -70,48 +69,53 @@ template <> __device__ __forceinline__ void st2<__half>(__half* p, float2 v) {
 template <> __device__ __forceinline__ void st2<__nv_bfloat16>(__nv_bfloat16* p, float2 v) {
     *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(v.x, v.y);
 }
-// 16-byte (FP32) or 8-byte (FP16/BF16) copy of four consecutive cells.
+// Pairs of consecutive cells as loaded from a vector field, kept in the load
+// type until the stage that uses them (a conversion right after the load
+// would wait for the load).
+template <class VT> struct Raw2 { using T = float2; };
+template <> struct Raw2<__half> { using T = __half2; };
+template <> struct Raw2<__nv_bfloat16> { using T = __nv_bfloat162; };
+__device__ __forceinline__ void zero2(float2& v) { v = make_float2(0.f, 0.f); }
+__device__ __forceinline__ void zero2(__half2& v) { v = __float2half2_rn(0.f); }
+__device__ __forceinline__ void zero2(__nv_bfloat162& v) { v = __float2bfloat162_rn(0.f); }
 template <class VT>
-__device__ __forceinline__ void cp_async_quad(void* smem, const VT* gmem, bool valid) {
-    if (sizeof(VT) == 4) cp_async16(smem, gmem, valid);
-    else cp_async8(smem, gmem, valid);
+__device__ __forceinline__ typename Raw2<VT>::T ldg_pair(const VT* p, bool ok) {
+    using R = typename Raw2<VT>::T;
+    R v;
+    if (ok) v = __ldg(reinterpret_cast<const R*>(p));
+    else zero2(v);
+    return v;
+}
+__device__ __forceinline__ float2 cvt2(const float2& v) { return v; }
+__device__ __forceinline__ float2 cvt2(const __half2& v) { return __half22float2(v); }
+__device__ __forceinline__ float2 cvt2(const __nv_bfloat162& v) { return __bfloat1622float2(v); }
+template <class VT>
+__device__ __forceinline__ VT ldg_one(const VT* p, bool ok) {
+    return ok ? __ldg(p) : from_f<VT>(0.f);
 }
 
-// A thread's share of one plane's copies, resolved once per block: one
-// four-cell group of the vector rows (12 rows x 18 groups) and two (8-byte
-// records) or four (16-byte records) 16-byte copies of the record rows
-// (13 rows x 72 records).
+// A thread's share of one plane's record copies, resolved once per block:
+// two (8-byte records) or four (16-byte records) 16-byte copies of the
+// record rows (13 rows x 72 records).
 template <int CK>
-struct RegionFetch {
+struct RecordFetch {
     using CT = typename CoefStore<CK>::T;
     static constexpr int RPC = (CK == 0) ? 1 : 2;  // records per 16-byte copy
     static constexpr int NCT = (CK == 0) ? 4 : 2;
     static constexpr int NCTOT = CH * (RW / RPC);
     static_assert(NCTOT <= NCT * FT, "record copies per thread");
-    int voff, coff[NCT];
-    short vdst, cdst[NCT];
-    bool vok, cok[NCT];
+    int coff[NCT];
+    short cdst[NCT];
+    bool cok[NCT];
     long long sxy;
     int nz;
     bool pz;
 
-    __device__ __forceinline__ RegionFetch(const Grid3& g, int x0, int y0, int t) {
+    __device__ __forceinline__ RecordFetch(const Grid3& g, int x0, int y0, int t) {
         sxy = (long long)g.nx * g.ny;
         nz = g.nz;
         pz = (g.periodic & 4) != 0;
         const bool px = g.periodic & 1, py = g.periodic & 2;
-        vdst = -1;
-        vok = false;
-        voff = 0;
-        if (t < NVEC) {
-            const int row = t / NG, gi = t - row * NG;
-            bool okx, oky;
-            const int sx = axis_src(x0 - XO + 4 * gi, g.nx, px, &okx);
-            const int sy = axis_src(y0 - 2 + row, g.ny, py, &oky);
-            vok = okx && oky;
-            voff = vok ? sx + g.nx * sy : 0;
-            vdst = (short)(row * RW + 4 * gi);
-        }
 #pragma unroll
         for (int j = 0; j < NCT; j++) {
             const int k = t + j * FT;
@@ -133,13 +137,6 @@ struct RegionFetch {
     __device__ __forceinline__ long long plane(int zz, bool* okz) const {
         const int sz = axis_src(zz, nz, pz, okz);
         return (long long)sz * sxy;
-    }
-    template <class VA>
-    __device__ __forceinline__ void vec(VA* dst, const VA* src, long long pl, bool okz) const {
-        if (vdst >= 0) {
-            const bool ok = vok && okz;
-            cp_async_quad<VA>(dst + vdst, src + (ok ? pl + voff : 0), ok);
-        }
     }
     __device__ __forceinline__ void recs(CT* dst, const CT* src, long long pl, bool okz) const {
 #pragma unroll
@@ -171,27 +168,37 @@ __device__ __forceinline__ float gs_sum(const CT* c, const CT* cn, const float* 
     return acc;
 }
 
-// A thread's pair tasks of the red (2-halo) and black (1-halo) stages,
-// resolved once per block: flat offsets of the pair's first cell, the colour
-// parity of its row, and for red tasks on the tile the in-plane offset of the
-// pair (-1 otherwise).  Black tasks at the region's x edges update only the
-// member inside the 1-halo.
+// A thread's pair tasks of the red / prolongation (2-halo) and black
+// (1-halo) stages, resolved once per block: flat offsets of the pair's first
+// cell, the colour parity of its row, the pair's in-plane offset in the grid
+// (wrapped on periodic axes) and whether it exists, and for tasks on the tile
+// the unwrapped in-plane offset (-1 otherwise).  Black tasks at the region's
+// x edges update only the member inside the 1-halo.
 struct PairTasks {
-    int roff[2], rpar[2], rown[2];
+    int roff[2], rpar[2], rown[2], goff[2];
+    bool gok[2];
     int boff[2], bpar[2], bedge[2];
     __device__ __forceinline__ PairTasks(const Grid3& g, int x0, int y0, int t) {
+        const bool px = g.periodic & 1, py = g.periodic & 2;
 #pragma unroll
         for (int u = 0; u < 2; u++) {
             const int k = t + u * FT;
             roff[u] = -1;
             rpar[u] = 0;
             rown[u] = -1;
+            goff[u] = 0;
+            gok[u] = false;
             if (k < NRED) {
                 const int row = k / RP, pc = k - row * RP;
                 roff[u] = row * RW + 2 + 2 * pc;
                 rpar[u] = (y0 - 2 + row) & 1;
                 const int gx = x0 - 2 + 2 * pc, gy = y0 - 2 + row;
                 if (row >= 2 && row < FTY + 2 && pc >= 1 && pc <= TX && gx < g.nx && gy < g.ny) rown[u] = gx + g.nx * gy;
+                bool okx, oky;
+                const int sx = axis_src(gx, g.nx, px, &okx);
+                const int sy = axis_src(gy, g.ny, py, &oky);
+                gok[u] = okx && oky;
+                goff[u] = gok[u] ? sx + g.nx * sy : 0;
             }
             boff[u] = -1;
             bpar[u] = 0;
@@ -204,6 +211,8 @@ struct PairTasks {
             }
         }
     }
+    // red member (0 or 1) of red task u at plane z
+    __device__ __forceinline__ int red(int u, int z) const { return (rpar[u] + z) & 1; }
     // black member of black task u at plane z, or -1 when it lies outside the 1-halo
     __device__ __forceinline__ int black(int u, int z) const {
         const int m = (bpar[u] + z) & 1;
@@ -212,30 +221,30 @@ struct PairTasks {
     }
 };
 
-// Plane rings.  A step handles planes zA (red / prolongation stage), zA-1
-// (black stage) and zA-2 (tile stage) and stages plane zA+1 for the next
-// step; ring sizes are 2 or 4, so the z loop is unrolled four times and
-// every slot is a compile-time offset.
-template <int CK, class VT, bool UPDATE>
+// Plane rings in shared memory.  A step handles planes zA (red /
+// prolongation stage), zA-1 (black stage) and zA-2 (tile stage) and stages
+// the records of plane zA+1 for the next step; rings of 4 planes, so the z
+// loop is unrolled four times and every slot is a compile-time offset.  The
+// vector inputs go straight to registers, one plane ahead.  In the correction
+// ring the black cells of the newest plane hold their right-hand side sigma r
+// until the black stage replaces it by their value.
+template <int CK>
 struct PreRing {
     using CT = typename CoefStore<CK>::T;
     CT c[4][CH][RW];                 // records, planes zA-2 .. zA+1
-    VT rin[2][RH][RW];               // residual in, planes zA .. zA+1
-    float q[UPDATE ? 2 : 1][RH][RW];
-    float rn[2][RH][RW];             // updated residual, planes zA-1 .. zA
     float er[4][RH][RW];             // correction, planes zA-3 .. zA
     float ypart[FTY][TX];
 };
-template <int CK, class VT>
+template <int CK>
 struct PostRing {
     using CT = typename CoefStore<CK>::T;
     CT c[4][CH][RW];                 // records, planes zA-2 .. zA+1
-    VT rr[4][RH][RW];                // right-hand side, planes zA-2 .. zA+1
-    VT eo[2][RH][RW];                // pre-smoothed correction, planes zA .. zA+1
     float ep[4][RH][RW];             // prolonged / smoothed correction, planes zA-3 .. zA
 };
 template <int N>
 using Phase = std::integral_constant<int, N>;
+template <int CK>
+constexpr int fused_min_blocks() { return CK == 0 ? 3 : 4; }
 }  // namespace
 
 // ------------------------------------------------------ pre-smoothing pass
@@ -247,54 +256,68 @@ using Phase = std::integral_constant<int, N>;
 // solves its own equation) and that of a red cell is sum beta * e over its
 // black neighbours (its red value solved the equation with them at zero), so
 // the restriction sums those neighbour terms over the red cells.
+// rin and q must not alias r_out (other tiles read them as halo).
 template <int CK, class VT, class VTc, bool UPDATE, bool FINE>
-__global__ void __launch_bounds__(FT) k_presmooth_restrict(Grid3 g, Grid3 gc, const void* __restrict__ sm_v,
-                                                                     const VT* __restrict__ rin,
-                                                                     const float* __restrict__ q,
-                                                                     float* __restrict__ r_out, VT* __restrict__ e,
-                                                                     VTc* __restrict__ rc, Scalars* sc,
-                                                                     double* partials, int nblocks) {
+__global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
+    k_presmooth_restrict(Grid3 g, Grid3 gc, const void* __restrict__ sm_v, const VT* __restrict__ rin,
+                         const float* __restrict__ q, float* __restrict__ r_out, VT* __restrict__ e,
+                         VTc* __restrict__ rc, Scalars* sc, double* partials, int nblocks) {
     if (sc->converged) return;
     using CT = typename CoefStore<CK>::T;
+    using R2 = typename Raw2<VT>::T;
     const CT* sm = reinterpret_cast<const CT*>(sm_v);
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto& S = *reinterpret_cast<PreRing<CK, VT, UPDATE>*>(smem_raw);
+    auto& S = *reinterpret_cast<PreRing<CK>*>(smem_raw);
     __shared__ double sh[FT / 32];
     const float sigma = FINE ? sc->sigma : 1.0f;
     const float alpha = UPDATE ? sc->alpha_f : 0.0f;
     const int x0 = blockIdx.x * PX, y0 = blockIdx.y * FTY;
     const int tx = threadIdx.x, ty = threadIdx.y, t = tx + TX * ty;
     const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
-    const RegionFetch<CK> F(g, x0, y0, t);
+    const RecordFetch<CK> F(g, x0, y0, t);
     const PairTasks T(g, x0, y0, t);
     const long long sxy = (long long)g.nx * g.ny;
     // ||r||^2 only steers the stop test and sigma: a per-thread FP32 sum,
     // FP64 across threads and blocks
     float rr_thread = 0.f;
     float part = 0.f;
+    int rc_z = -1;  // coarse plane whose restriction awaits the row pair sum
     const int ox = x0 + 2 * tx, oy = y0 + ty;  // the thread's own pair
     const bool own_inside = ox < g.nx && oy < g.ny;
     const int oo = (ty + 2) * RW + XO + 2 * tx;  // its flat offset
     const long long og = ox + (long long)g.nx * oy;
-    auto fetch = [&](int zz, int c4, int v2) {
+    R2 rv[2], rvn[2];
+    float2 qv[2], qvn[2];
+    // records of plane zz to ring slot c4 (cp.async), the red tasks' residual
+    // (and q) of plane zz to registers
+    auto fetch = [&](int zz, int c4, R2* rd, float2* qd) {
         bool okz;
         const long long pl = F.plane(zz, &okz);
         F.recs(&S.c[c4][0][0], sm, pl, okz);
-        F.vec(&S.rin[v2][0][0], rin, pl, okz);
-        if (UPDATE) F.vec(&S.q[v2][0][0], q, pl, okz);
+        cp_commit();
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const bool ok = T.gok[u] && okz;
+            rd[u] = ldg_pair<VT>(rin + pl + T.goff[u], ok);
+            if (UPDATE) qd[u] = ok ? __ldg(reinterpret_cast<const float2*>(q + pl + T.goff[u])) : make_float2(0.f, 0.f);
+        }
+    };
+    auto flush_rc = [&]() {
+        if (rc_z >= 0 && own_inside && !(ty & 1)) {
+            const float tot = S.ypart[ty][tx] + S.ypart[ty + 1][tx];
+            rc[(ox >> 1) + (long long)gc.nx * ((oy >> 1) + (long long)gc.ny * rc_z)] = from_f<VTc>(0.25f * tot);
+        }
+        rc_z = -1;
     };
     auto step = [&](auto ph, int zA) {
         constexpr int P = decltype(ph)::value;
-        fetch(zA + 1, (P + 1) & 3, (P + 1) & 1);
-        cp_commit();
-        cp_wait<1>();
+        cp_wait<0>();
         __syncthreads();
+        fetch(zA + 1, (P + 1) & 3, rvn, UPDATE ? qvn : nullptr);
+        flush_rc();
         // ---- red stage: plane zA over the 2-halo region
         {
-            const VT* RI = &S.rin[P & 1][0][0];
-            const float* Q = &S.q[UPDATE ? (P & 1) : 0][0][0];
             const CT* C = &S.c[P][0][0];
-            float* RN = &S.rn[P & 1][0][0];
             float* ER = &S.er[P][0][0];
             const bool zin = zA >= z0 && zA < z1;
             float* rplane = UPDATE ? r_out + sxy * zA : nullptr;
@@ -302,17 +325,12 @@ __global__ void __launch_bounds__(FT) k_presmooth_restrict(Grid3 g, Grid3 gc, co
             for (int u = 0; u < 2; u++) {
                 const int o = T.roff[u];
                 if (o < 0) break;
-                const float2 rv = ld2<VT>(RI + o);
-                float2 rn = rv;
-                if (UPDATE) {
-                    const float2 qv = *reinterpret_cast<const float2*>(Q + o);
-                    rn = make_float2(fmaf(-alpha, qv.x, rv.x), fmaf(-alpha, qv.y, rv.y));
-                }
-                const int m = (T.rpar[u] + zA) & 1;  // pair member of colour 0 (x0 even)
+                float2 rn = cvt2(rv[u]);
+                if (UPDATE) rn = make_float2(fmaf(-alpha, qv[u].x, rn.x), fmaf(-alpha, qv[u].y, rn.y));
+                const int m = T.red(u, zA);
                 const float d = unpack<CK>(C[o + m]).w;
                 const float ev = d > 0.f ? __fdividef(sigma * (m ? rn.y : rn.x), d) : 0.f;
-                *reinterpret_cast<float2*>(RN + o) = rn;
-                *reinterpret_cast<float2*>(ER + o) = m ? make_float2(0.f, ev) : make_float2(ev, 0.f);
+                *reinterpret_cast<float2*>(ER + o) = m ? make_float2(sigma * rn.x, ev) : make_float2(ev, sigma * rn.y);
                 if (UPDATE && zin && T.rown[u] >= 0) {
                     *reinterpret_cast<float2*>(rplane + T.rown[u]) = rn;
                     rr_thread = fmaf(rn.x, rn.x, fmaf(rn.y, rn.y, rr_thread));
@@ -325,7 +343,6 @@ __global__ void __launch_bounds__(FT) k_presmooth_restrict(Grid3 g, Grid3 gc, co
         if (zB >= z0 - 1) {
             const CT* C = &S.c[(P + 3) & 3][0][0];
             const CT* CN = &S.c[P][0][0];
-            const float* RN = &S.rn[(P + 1) & 1][0][0];
             float* E = &S.er[(P + 3) & 3][0][0];
             const float* EM = &S.er[(P + 2) & 3][0][0];
             const float* EP = &S.er[P][0][0];
@@ -334,7 +351,7 @@ __global__ void __launch_bounds__(FT) k_presmooth_restrict(Grid3 g, Grid3 gc, co
                 const int o = T.black(u, zB);
                 if (o < 0) continue;
                 float d;
-                const float s = gs_sum<CK>(C, CN, E, EM, EP, o, sigma * RN[o], &d);
+                const float s = gs_sum<CK>(C, CN, E, EM, EP, o, E[o], &d);
                 E[o] = d > 0.f ? __fdividef(s, d) : 0.f;
             }
         }
@@ -352,21 +369,20 @@ __global__ void __launch_bounds__(FT) k_presmooth_restrict(Grid3 g, Grid3 gc, co
             part += gs_sum<CK>(C, CN, E, EM, EP, oo + m, 0.f, &d);
             if (own_inside) st2<VT>(e + (og + sxy * zC), *reinterpret_cast<const float2*>(E + oo));
             if (((zC - z0) & 1) || zC + 1 == z1) {
+                // the row pair sum is formed after the next barrier
                 S.ypart[ty][tx] = part;
-                __syncthreads();
-                if (own_inside && !(ty & 1)) {
-                    const float tot = part + S.ypart[ty + 1][tx];
-                    rc[(ox >> 1) + (long long)gc.nx * ((oy >> 1) + (long long)gc.ny * (zC >> 1))] =
-                        from_f<VTc>(0.25f * tot);
-                }
+                rc_z = zC >> 1;
                 part = 0.f;
             }
         }
-        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            rv[u] = rvn[u];
+            if (UPDATE) qv[u] = qvn[u];
+        }
     };
     const int zs = z0 - 2, zend = z1 + 1;  // red stage over zs .. zend
-    fetch(zs, 0, 0);
-    cp_commit();
+    fetch(zs, 0, rv, UPDATE ? qv : nullptr);
     for (int zA = zs;;) {
         step(Phase<0>{}, zA);
         if (++zA > zend) break;
@@ -378,6 +394,8 @@ __global__ void __launch_bounds__(FT) k_presmooth_restrict(Grid3 g, Grid3 gc, co
         if (++zA > zend) break;
     }
     cp_wait<0>();
+    __syncthreads();
+    flush_rc();
     if (UPDATE) {
         double v1[1] = {(double)rr_thread};
         block_sum<1>(v1, sh);
@@ -403,88 +421,93 @@ __global__ void __launch_bounds__(FT) k_presmooth_restrict(Grid3 g, Grid3 gc, co
 // ----------------------------------------------------- post-smoothing pass
 // e (pre-smoothed, VT) + w * P ec -> black, red half-steps -> out (VT).  DOT
 // (finest level): r . out / sigma gives rz and beta; the next V-cycle's sigma
-// is then taken from ||r||^2.
+// is then taken from ||r||^2.  The black half-step does not read a black
+// cell's own prolonged value, so the prolongation stage leaves sigma r there.
 template <int CK, class VT, class VTc, bool DOT, bool FINE>
-__global__ void __launch_bounds__(FT) k_prolong_postsmooth(Grid3 g, Grid3 gc, const void* __restrict__ sm_v,
-                                                                     const VT* __restrict__ e,
-                                                                     const VTc* __restrict__ ec,
-                                                                     const VT* __restrict__ r, VT* __restrict__ out,
-                                                                     const VT* __restrict__ accum, float w,
-                                                                     Scalars* sc, double* partials, int nblocks,
-                                                                     long long n_active) {
+__global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
+    k_prolong_postsmooth(Grid3 g, Grid3 gc, const void* __restrict__ sm_v, const VT* __restrict__ e,
+                         const VTc* __restrict__ ec, const VT* __restrict__ r, VT* __restrict__ out,
+                         const VT* __restrict__ accum, float w, Scalars* sc, double* partials, int nblocks,
+                         long long n_active) {
     if (sc->converged) return;
     using CT = typename CoefStore<CK>::T;
+    using R2 = typename Raw2<VT>::T;
     const CT* sm = reinterpret_cast<const CT*>(sm_v);
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    auto& S = *reinterpret_cast<PostRing<CK, VT>*>(smem_raw);
+    auto& S = *reinterpret_cast<PostRing<CK>*>(smem_raw);
     __shared__ double sh[FT / 32];
     const float sigma = FINE ? sc->sigma : 1.0f;
     const float is = FINE ? sc->inv_sigma : 1.0f;
     const int x0 = blockIdx.x * PX, y0 = blockIdx.y * FTY;
     const int tx = threadIdx.x, ty = threadIdx.y, t = tx + TX * ty;
     const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
-    const RegionFetch<CK> F(g, x0, y0, t);
+    const RecordFetch<CK> F(g, x0, y0, t);
     const PairTasks T(g, x0, y0, t);
     const long long sxy = (long long)g.nx * g.ny;
-    // Coarse parents of the red-stage pairs: in-plane offsets, validity.
+    // coarse parents of the red-stage pairs: in-plane offsets
     int pofs[2];
-    bool pok[2];
     {
         const bool px = g.periodic & 1, py = g.periodic & 2;
 #pragma unroll
         for (int u = 0; u < 2; u++) {
             const int k = t + u * FT;
             pofs[u] = 0;
-            pok[u] = false;
             if (k < NRED) {
                 const int row = k / RP, pc = k - row * RP;
                 bool okx, oky;
                 const int sx = axis_src(x0 - 2 + 2 * pc, g.nx, px, &okx);
                 const int sy = axis_src(y0 - 2 + row, g.ny, py, &oky);
-                pok[u] = okx && oky;
-                pofs[u] = pok[u] ? (sx >> 1) + gc.nx * (sy >> 1) : 0;
+                pofs[u] = (okx && oky) ? (sx >> 1) + gc.nx * (sy >> 1) : 0;
             }
         }
     }
     const long long csxy = (long long)gc.nx * gc.ny;
-    auto parents = [&](int zz, float* v) {
-        bool okz;
-        const int sz = axis_src(zz, g.nz, (g.periodic & 4) != 0, &okz);
-        const long long cpl = (long long)(sz >> 1) * csxy;
-#pragma unroll
-        for (int u = 0; u < 2; u++) v[u] = (pok[u] && okz) ? to_f(__ldg(ec + cpl + pofs[u])) : 0.f;
-    };
-    auto fetch = [&](int zz, int c4, int v2) {
-        bool okz;
-        const long long pl = F.plane(zz, &okz);
-        F.recs(&S.c[c4][0][0], sm, pl, okz);
-        F.vec(&S.rr[c4][0][0], r, pl, okz);
-        F.vec(&S.eo[v2][0][0], e, pl, okz);
-    };
-    float pc_cur[2], pc_nxt[2];
     Acc acc;
     const int ox = x0 + 2 * tx, oy = y0 + ty;
     const bool own_inside = ox < g.nx && oy < g.ny;
     const int oo = (ty + 2) * RW + XO + 2 * tx;
     const long long og = ox + (long long)g.nx * oy;
+    // registers of plane zA (current) and zA+1 (next): the pre-smoothed
+    // correction of the red-stage pairs, their black member's right-hand
+    // side, the coarse parents, and the own pair's right-hand side of the
+    // next tile plane
+    R2 eov[2], eon[2];
+    VT rbv[2], rbn[2];
+    VTc pcv[2], pcn[2];
+    R2 rov, ron;
+    auto fetch = [&](int zz, int c4, R2* eo, VT* rb, VTc* pc, R2& ro) {
+        bool okz;
+        const int sz = axis_src(zz, g.nz, (g.periodic & 4) != 0, &okz);
+        const long long pl = (long long)sz * sxy, cpl = (long long)(sz >> 1) * csxy;
+        F.recs(&S.c[c4][0][0], sm, pl, okz);
+        cp_commit();
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const bool ok = T.gok[u] && okz;
+            eo[u] = ldg_pair<VT>(e + pl + T.goff[u], ok);
+            rb[u] = ldg_one<VT>(r + pl + T.goff[u] + (1 - T.red(u, zz)), ok);
+            pc[u] = ldg_one<VTc>(ec + cpl + pofs[u], ok);
+        }
+        const int zt = zz - 2;  // tile plane of the next step
+        ro = ldg_pair<VT>(r + og + sxy * zt, own_inside && zt >= z0 && zt < z1);
+    };
     auto step = [&](auto ph, int zA) {
         constexpr int P = decltype(ph)::value;
-        fetch(zA + 1, (P + 1) & 3, (P + 1) & 1);
-        cp_commit();
-        parents(zA + 1, pc_nxt);  // consumed one step later
-        cp_wait<1>();
+        cp_wait<0>();
         __syncthreads();
+        fetch(zA + 1, (P + 1) & 3, eon, rbn, pcn, ron);
         // ---- prolongation: plane zA over the 2-halo region
         {
-            const VT* EO = &S.eo[P & 1][0][0];
             float* EP = &S.ep[P][0][0];
 #pragma unroll
             for (int u = 0; u < 2; u++) {
                 const int o = T.roff[u];
                 if (o < 0) break;
-                const float2 ev = ld2<VT>(EO + o);
-                const float cv = pc_cur[u];
-                *reinterpret_cast<float2*>(EP + o) = make_float2(fmaf(w, cv, ev.x), fmaf(w, cv, ev.y));
+                const float2 ev = cvt2(eov[u]);
+                const float cv = to_f(pcv[u]);
+                const float rb = sigma * to_f(rbv[u]);
+                *reinterpret_cast<float2*>(EP + o) =
+                    T.red(u, zA) ? make_float2(rb, fmaf(w, cv, ev.y)) : make_float2(fmaf(w, cv, ev.x), rb);
             }
         }
         __syncthreads();
@@ -493,7 +516,6 @@ __global__ void __launch_bounds__(FT) k_prolong_postsmooth(Grid3 g, Grid3 gc, co
         if (zB >= z0 - 1) {
             const CT* C = &S.c[(P + 3) & 3][0][0];
             const CT* CN = &S.c[P][0][0];
-            const VT* RR = &S.rr[(P + 3) & 3][0][0];
             float* E = &S.ep[(P + 3) & 3][0][0];
             const float* EM = &S.ep[(P + 2) & 3][0][0];
             const float* EP = &S.ep[P][0][0];
@@ -502,7 +524,7 @@ __global__ void __launch_bounds__(FT) k_prolong_postsmooth(Grid3 g, Grid3 gc, co
                 const int o = T.black(u, zB);
                 if (o < 0) continue;
                 float d;
-                const float s = gs_sum<CK>(C, CN, E, EM, EP, o, sigma * to_f(RR[o]), &d);
+                const float s = gs_sum<CK>(C, CN, E, EM, EP, o, E[o], &d);
                 E[o] = d > 0.f ? __fdividef(s, d) : 0.f;
             }
         }
@@ -512,12 +534,11 @@ __global__ void __launch_bounds__(FT) k_prolong_postsmooth(Grid3 g, Grid3 gc, co
         if (zC >= z0 && zC < z1) {
             const CT* C = &S.c[(P + 2) & 3][0][0];
             const CT* CN = &S.c[(P + 3) & 3][0][0];
-            const VT* RR = &S.rr[(P + 2) & 3][0][0];
             const float* E = &S.ep[(P + 2) & 3][0][0];
             const float* EM = &S.ep[(P + 1) & 3][0][0];
             const float* EP = &S.ep[(P + 3) & 3][0][0];
             const int m = (y0 + ty + zC) & 1;  // the pair member of colour 0
-            const float2 rv = ld2<VT>(RR + oo);
+            const float2 rv = cvt2(rov);
             float d;
             const float s = gs_sum<CK>(C, CN, E, EM, EP, oo + m, sigma * (m ? rv.y : rv.x), &d);
             const float zr = d > 0.f ? __fdividef(s, d) : 0.f;
@@ -535,14 +556,16 @@ __global__ void __launch_bounds__(FT) k_prolong_postsmooth(Grid3 g, Grid3 gc, co
                 }
             }
         }
-        __syncthreads();
-        pc_cur[0] = pc_nxt[0];
-        pc_cur[1] = pc_nxt[1];
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            eov[u] = eon[u];
+            rbv[u] = rbn[u];
+            pcv[u] = pcn[u];
+        }
+        rov = ron;
     };
     const int zs = z0 - 2, zend = z1 + 1;
-    fetch(zs, 0, 0);
-    cp_commit();
-    parents(zs, pc_cur);
+    fetch(zs, 0, eov, rbv, pcv, rov);
     for (int zA = zs;;) {
         step(Phase<0>{}, zA);
         if (++zA > zend) break;
@@ -683,7 +706,7 @@ template <int CK, class VT, class VTc, bool UPDATE, bool FINE>
 static void pre_impl(const Grid3& g, const Grid3& gc, const void* sm, const void* rin, const float* q, float* r_out,
                      void* e, void* rc, Scalars* sc, double* partials, int occ_kind, cudaStream_t s) {
     const Launch P = fused_launch(g, occ_kind);
-    k_presmooth_restrict<CK, VT, VTc, UPDATE, FINE><<<P.grid, P.block, sizeof(PreRing<CK, VT, UPDATE>), s>>>(
+    k_presmooth_restrict<CK, VT, VTc, UPDATE, FINE><<<P.grid, P.block, sizeof(PreRing<CK>), s>>>(
         P.g, gc, sm, (const VT*)rin, q, r_out, (VT*)e, (VTc*)rc, sc, partials, P.nblocks);
 }
 template <int CK, class VT, class VTc, bool DOT, bool FINE>
@@ -691,7 +714,7 @@ static void post_impl(const Grid3& g, const Grid3& gc, const void* sm, const voi
                       void* out, const void* accum, float w, Scalars* sc, double* partials, long long n_active,
                       int occ_kind, cudaStream_t s) {
     const Launch P = fused_launch(g, occ_kind);
-    k_prolong_postsmooth<CK, VT, VTc, DOT, FINE><<<P.grid, P.block, sizeof(PostRing<CK, VT>), s>>>(
+    k_prolong_postsmooth<CK, VT, VTc, DOT, FINE><<<P.grid, P.block, sizeof(PostRing<CK>), s>>>(
         P.g, gc, sm, (const VT*)e, (const VTc*)ec, (const VT*)r, (VT*)out, (const VT*)accum, w, sc, partials,
         P.nblocks, n_active);
 }
@@ -826,7 +849,7 @@ void mg_fused_post(const MGPlan& P, const float* r, double* partials, long long 
 template <int CK, class VT, class VTc, bool UPDATE, bool FINE>
 static cudaError_t prep_pre(int kind) {
     const void* fn = (const void*)k_presmooth_restrict<CK, VT, VTc, UPDATE, FINE>;
-    const size_t bytes = sizeof(PreRing<CK, VT, UPDATE>);
+    const size_t bytes = sizeof(PreRing<CK>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess && kind >= 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f_occ[kind], fn, FT, bytes);
     return e;
@@ -834,7 +857,7 @@ static cudaError_t prep_pre(int kind) {
 template <int CK, class VT, class VTc, bool DOT, bool FINE>
 static cudaError_t prep_post(int kind) {
     const void* fn = (const void*)k_prolong_postsmooth<CK, VT, VTc, DOT, FINE>;
-    const size_t bytes = sizeof(PostRing<CK, VT>);
+    const size_t bytes = sizeof(PostRing<CK>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess && kind >= 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f_occ[kind], fn, FT, bytes);
     return e;
