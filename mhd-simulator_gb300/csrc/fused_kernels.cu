@@ -46,6 +46,7 @@ constexpr int FTY = 8;           // tile rows (one thread row per tile row)
 constexpr int FT = TX * FTY;     // 256 threads per block
 constexpr int XO = 4;            // staged rows start at x0 - XO
 constexpr int RW = PX + 2 * XO;  // 72 staged columns: x0-4 .. x0+67
+constexpr int HW = RW / 2;       // 36 columns per half row (even x, then odd x)
 constexpr int RH = FTY + 4;      // vector rows:  y0-2 .. y0+FTY+1
 constexpr int CH = FTY + 5;      // record rows:  y0-2 .. y0+FTY+2
 constexpr int RP = (PX + 4) / 2; // 34 pairs of the 2-halo region (x0-2 .. x0+65)
@@ -96,13 +97,16 @@ __device__ __forceinline__ VT ldg_one(const VT* p, bool ok) {
 
 // A thread's share of one plane's record copies, resolved once per block:
 // two (8-byte records) or four (16-byte records) 16-byte copies of the
-// record rows (13 rows x 72 records).
+// record rows (13 rows x 2 half rows x 36 records).  A copy of two 8-byte
+// records covers cells x and x+2 of a four-cell group, so both exist or
+// neither does (nx is a multiple of 4).
 template <int CK>
 struct RecordFetch {
     using CT = typename CoefStore<CK>::T;
     static constexpr int RPC = (CK == 0) ? 1 : 2;  // records per 16-byte copy
     static constexpr int NCT = (CK == 0) ? 4 : 2;
-    static constexpr int NCTOT = CH * (RW / RPC);
+    static constexpr int PER = HW / RPC;           // copies per half row
+    static constexpr int NCTOT = CH * 2 * PER;
     static_assert(NCTOT <= NCT * FT, "record copies per thread");
     int coff[NCT];
     short cdst[NCT];
@@ -123,14 +127,14 @@ struct RecordFetch {
             cok[j] = false;
             coff[j] = 0;
             if (k < NCTOT) {
-                const int per = RW / RPC;
-                const int row = k / per, ci = k - row * per;
+                const int row = k / (2 * PER), rem = k - row * 2 * PER;
+                const int h = rem / PER, ci = rem - h * PER;
                 bool okx, oky;
-                const int sx = axis_src(x0 - XO + RPC * ci, g.nx, px, &okx);
+                const int sx = axis_src(x0 - XO + 2 * RPC * ci, g.nx, px, &okx);  // even cell of the copy
                 const int sy = axis_src(y0 - 2 + row, g.ny, py, &oky);
                 cok[j] = okx && oky;
-                coff[j] = cok[j] ? sx + g.nx * sy : 0;
-                cdst[j] = (short)(row * RW + RPC * ci);
+                coff[j] = cok[j] ? g.nx * sy + h * (g.nx >> 1) + (sx >> 1) : 0;
+                cdst[j] = (short)(row * RW + h * HW + RPC * ci);
             }
         }
     }
@@ -148,18 +152,31 @@ struct RecordFetch {
     }
 };
 
+// Shared-memory planes are [rows][2][HW]: each staged row holds its even-x
+// cells, then its odd-x cells, so the cells of one colour in a row are
+// contiguous.  A cell in half h at offset o has its x-1 neighbour at
+// xminus(o, h) and its x+1 neighbour one further.
+__device__ __forceinline__ int xminus(int o, int h) { return h ? o - HW : o + HW - 1; }
+
+// The smoother records in HBM use the same split along whole grid rows: row
+// (y, z) holds its nx/2 even-x records, then its nx/2 odd-x records, so a
+// staged half row is one contiguous run.  Position of column x in its row:
+__device__ __forceinline__ int split_x(int x, int nx) { return (x & 1) * (nx >> 1) + (x >> 1); }
+
 // sum of beta * e over the six neighbours added to acc, in the per-cell
-// kernels' order; *d = the cell's diagonal.  Flat offset o into [rows][RW]
-// planes; c/cn: record planes z, z+1; e/em/ep: correction planes z, z-1, z+1.
+// kernels' order; *d = the cell's diagonal.  Offset o (half h) into the
+// split planes; c/cn: record planes z, z+1; e/em/ep: correction planes z,
+// z-1, z+1.
 template <int CK, class CT>
 __device__ __forceinline__ float gs_sum(const CT* c, const CT* cn, const float* e, const float* em, const float* ep,
-                                        int o, float acc, float* d) {
+                                        int o, int h, float acc, float* d) {
+    const int xm = xminus(o, h);
     const float4 own = unpack<CK>(c[o]);
-    const float bxh = unpack<CK>(c[o + 1]).x;
+    const float bxh = unpack<CK>(c[xm + 1]).x;
     const float byh = unpack<CK>(c[o + RW]).y;
     const float bzh = unpack<CK>(cn[o]).z;
-    acc = fmaf(own.x, e[o - 1], acc);
-    acc = fmaf(bxh, e[o + 1], acc);
+    acc = fmaf(own.x, e[xm], acc);
+    acc = fmaf(bxh, e[xm + 1], acc);
     acc = fmaf(own.y, e[o - RW], acc);
     acc = fmaf(byh, e[o + RW], acc);
     acc = fmaf(own.z, em[o], acc);
@@ -169,8 +186,8 @@ __device__ __forceinline__ float gs_sum(const CT* c, const CT* cn, const float* 
 }
 
 // A thread's pair tasks of the red / prolongation (2-halo) and black
-// (1-halo) stages, resolved once per block: flat offsets of the pair's first
-// cell, the colour parity of its row, the pair's in-plane offset in the grid
+// (1-halo) stages, resolved once per block: split-plane offsets of the pair's
+// even cell (the odd cell is HW further), the colour parity of its row, the pair's in-plane offset in the grid
 // (wrapped on periodic axes) and whether it exists, and for tasks on the tile
 // the unwrapped in-plane offset (-1 otherwise).  Black tasks at the region's
 // x edges update only the member inside the 1-halo.
@@ -190,7 +207,7 @@ struct PairTasks {
             gok[u] = false;
             if (k < NRED) {
                 const int row = k / RP, pc = k - row * RP;
-                roff[u] = row * RW + 2 + 2 * pc;
+                roff[u] = row * RW + 1 + pc;
                 rpar[u] = (y0 - 2 + row) & 1;
                 const int gx = x0 - 2 + 2 * pc, gy = y0 - 2 + row;
                 if (row >= 2 && row < FTY + 2 && pc >= 1 && pc <= TX && gx < g.nx && gy < g.ny) rown[u] = gx + g.nx * gy;
@@ -205,7 +222,7 @@ struct PairTasks {
             bedge[u] = 0;
             if (k < NBLK) {
                 const int rr = k / RP, pc = k - rr * RP, row = rr + 1;
-                boff[u] = row * RW + 2 + 2 * pc;
+                boff[u] = row * RW + 1 + pc;
                 bpar[u] = (1 + y0 - 2 + row) & 1;
                 bedge[u] = pc == 0 ? 1 : (pc == RP - 1 ? 2 : 0);
             }
@@ -213,11 +230,12 @@ struct PairTasks {
     }
     // red member (0 or 1) of red task u at plane z
     __device__ __forceinline__ int red(int u, int z) const { return (rpar[u] + z) & 1; }
-    // black member of black task u at plane z, or -1 when it lies outside the 1-halo
+    // black member (0 or 1) of black task u at plane z, or -1 when it lies
+    // outside the 1-halo
     __device__ __forceinline__ int black(int u, int z) const {
         const int m = (bpar[u] + z) & 1;
         if ((bedge[u] == 1 && m == 0) || (bedge[u] == 2 && m == 1)) return -1;
-        return boff[u] + m;
+        return m;
     }
 };
 
@@ -284,7 +302,7 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
     int rc_z = -1;  // coarse plane whose restriction awaits the row pair sum
     const int ox = x0 + 2 * tx, oy = y0 + ty;  // the thread's own pair
     const bool own_inside = ox < g.nx && oy < g.ny;
-    const int oo = (ty + 2) * RW + XO + 2 * tx;  // its flat offset
+    const int oo = (ty + 2) * RW + XO / 2 + tx;  // split offset of its even cell
     const long long og = ox + (long long)g.nx * oy;
     R2 rv[2], rvn[2];
     float2 qv[2], qvn[2];
@@ -328,9 +346,10 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
                 float2 rn = cvt2(rv[u]);
                 if (UPDATE) rn = make_float2(fmaf(-alpha, qv[u].x, rn.x), fmaf(-alpha, qv[u].y, rn.y));
                 const int m = T.red(u, zA);
-                const float d = unpack<CK>(C[o + m]).w;
+                const float d = unpack<CK>(C[o + m * HW]).w;
                 const float ev = d > 0.f ? __fdividef(sigma * (m ? rn.y : rn.x), d) : 0.f;
-                *reinterpret_cast<float2*>(ER + o) = m ? make_float2(sigma * rn.x, ev) : make_float2(ev, sigma * rn.y);
+                ER[o] = m ? sigma * rn.x : ev;
+                ER[o + HW] = m ? ev : sigma * rn.y;
                 if (UPDATE && zin && T.rown[u] >= 0) {
                     *reinterpret_cast<float2*>(rplane + T.rown[u]) = rn;
                     rr_thread = fmaf(rn.x, rn.x, fmaf(rn.y, rn.y, rr_thread));
@@ -348,10 +367,11 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
             const float* EP = &S.er[P][0][0];
 #pragma unroll
             for (int u = 0; u < 2; u++) {
-                const int o = T.black(u, zB);
-                if (o < 0) continue;
+                const int h = T.black(u, zB);
+                if (h < 0) continue;
+                const int o = T.boff[u] + h * HW;
                 float d;
-                const float s = gs_sum<CK>(C, CN, E, EM, EP, o, E[o], &d);
+                const float s = gs_sum<CK>(C, CN, E, EM, EP, o, h, E[o], &d);
                 E[o] = d > 0.f ? __fdividef(s, d) : 0.f;
             }
         }
@@ -366,8 +386,8 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
             const float* EP = &S.er[(P + 3) & 3][0][0];
             const int m = (y0 + ty + zC) & 1;  // red member of the own pair
             float d;
-            part += gs_sum<CK>(C, CN, E, EM, EP, oo + m, 0.f, &d);
-            if (own_inside) st2<VT>(e + (og + sxy * zC), *reinterpret_cast<const float2*>(E + oo));
+            part += gs_sum<CK>(C, CN, E, EM, EP, oo + m * HW, m, 0.f, &d);
+            if (own_inside) st2<VT>(e + (og + sxy * zC), make_float2(E[oo], E[oo + HW]));
             if (((zC - z0) & 1) || zC + 1 == z1) {
                 // the row pair sum is formed after the next barrier
                 S.ypart[ty][tx] = part;
@@ -465,7 +485,7 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
     Acc acc;
     const int ox = x0 + 2 * tx, oy = y0 + ty;
     const bool own_inside = ox < g.nx && oy < g.ny;
-    const int oo = (ty + 2) * RW + XO + 2 * tx;
+    const int oo = (ty + 2) * RW + XO / 2 + tx;
     const long long og = ox + (long long)g.nx * oy;
     // registers of plane zA (current) and zA+1 (next): the pre-smoothed
     // correction of the red-stage pairs, their black member's right-hand
@@ -506,8 +526,9 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
                 const float2 ev = cvt2(eov[u]);
                 const float cv = to_f(pcv[u]);
                 const float rb = sigma * to_f(rbv[u]);
-                *reinterpret_cast<float2*>(EP + o) =
-                    T.red(u, zA) ? make_float2(rb, fmaf(w, cv, ev.y)) : make_float2(fmaf(w, cv, ev.x), rb);
+                const bool m = T.red(u, zA);
+                EP[o] = m ? rb : fmaf(w, cv, ev.x);
+                EP[o + HW] = m ? fmaf(w, cv, ev.y) : rb;
             }
         }
         __syncthreads();
@@ -521,10 +542,11 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
             const float* EP = &S.ep[P][0][0];
 #pragma unroll
             for (int u = 0; u < 2; u++) {
-                const int o = T.black(u, zB);
-                if (o < 0) continue;
+                const int h = T.black(u, zB);
+                if (h < 0) continue;
+                const int o = T.boff[u] + h * HW;
                 float d;
-                const float s = gs_sum<CK>(C, CN, E, EM, EP, o, E[o], &d);
+                const float s = gs_sum<CK>(C, CN, E, EM, EP, o, h, E[o], &d);
                 E[o] = d > 0.f ? __fdividef(s, d) : 0.f;
             }
         }
@@ -540,9 +562,9 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
             const int m = (y0 + ty + zC) & 1;  // the pair member of colour 0
             const float2 rv = cvt2(rov);
             float d;
-            const float s = gs_sum<CK>(C, CN, E, EM, EP, oo + m, sigma * (m ? rv.y : rv.x), &d);
+            const float s = gs_sum<CK>(C, CN, E, EM, EP, oo + m * HW, m, sigma * (m ? rv.y : rv.x), &d);
             const float zr = d > 0.f ? __fdividef(s, d) : 0.f;
-            const float zb = E[oo + 1 - m];
+            const float zb = E[oo + (1 - m) * HW];
             float2 zv = m ? make_float2(zb, zr) : make_float2(zr, zb);
             if (own_inside) {
                 if (accum) {  // out = accum + z (second W-cycle visit)
@@ -612,7 +634,8 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
 // --------------------------------------------------- smoother records
 // (beta_x, beta_y, beta_z, diagonal) per cell from the level's coefficient
 // records (beta_x, beta_y, beta_z, reaction); the diagonal is the FP32 sum of
-// the record-precision values, rounded up to the record precision.
+// the record-precision values, rounded up to the record precision.  Stored
+// with each grid row split into its even-x and odd-x halves (split_x).
 template <int CK>
 __global__ void __launch_bounds__(TILE_THREADS) k_smoother_records(Grid3 g, const void* __restrict__ coef_v,
                                                                    void* __restrict__ sm_v) {
@@ -650,7 +673,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_smoother_records(Grid3 g, cons
             u.y = (u.y & 0x0000ffffu) | ((unsigned)dh << 16);
             reinterpret_cast<uint2&>(out) = u;
         }
-        sm[i] = out;
+        sm[i + (split_x(x, g.nx) - x)] = out;
     }
 }
 
@@ -735,13 +758,14 @@ __global__ void __launch_bounds__(TILE_THREADS) k_level_residual(Grid3 g, const 
     const long long sy = g.nx, sz = (long long)g.nx * g.ny;
     const int xm = wrap_or_neg(x - 1, g.nx, g.periodic & 1), xp = wrap_or_neg(x + 1, g.nx, g.periodic & 1);
     const int ym = wrap_or_neg(y - 1, g.ny, g.periodic & 2), yp = wrap_or_neg(y + 1, g.ny, g.periodic & 2);
+    const int hx = split_x(x, g.nx), hxp = xp >= 0 ? split_x(xp, g.nx) : 0;
     for (int z = z0; z < z1; z++) {
-        const long long i = x + sy * y + sz * z;
+        const long long i = x + sy * y + sz * z, is = i + (hx - x);
         const int zm = wrap_or_neg(z - 1, g.nz, g.periodic & 4), zp = wrap_or_neg(z + 1, g.nz, g.periodic & 4);
-        const float4 own = unpack<CK>(sm[i]);
-        const float bxh = xp >= 0 ? unpack<CK>(sm[i + (xp - x)]).x : 0.f;
-        const float byh = yp >= 0 ? unpack<CK>(sm[i + (yp - y) * sy]).y : 0.f;
-        const float bzh = zp >= 0 ? unpack<CK>(sm[i + (zp - z) * sz]).z : 0.f;
+        const float4 own = unpack<CK>(sm[is]);
+        const float bxh = xp >= 0 ? unpack<CK>(sm[is + (hxp - hx)]).x : 0.f;
+        const float byh = yp >= 0 ? unpack<CK>(sm[is + (yp - y) * sy]).y : 0.f;
+        const float bzh = zp >= 0 ? unpack<CK>(sm[is + (zp - z) * sz]).z : 0.f;
         float nsum = 0.f;
         nsum = fmaf(own.x, xm >= 0 ? to_f(e[i + (xm - x)]) : 0.f, nsum);
         nsum = fmaf(bxh, xp >= 0 ? to_f(e[i + (xp - x)]) : 0.f, nsum);
