@@ -195,7 +195,7 @@ static int build_levels(mhdproj_ctx* ctx) {
     P.nlevels = 0;
     for (;;) {
         MGLevel& L = P.lv[P.nlevels];
-        L.L = tile_launch(d[0], d[1], d[2], per, 152 * 8);
+        L.L = tile_launch(d[0], d[1], d[2], per, MAX_REDUCE_BLOCKS);
         L.odd_periodic = false;
         for (int a = 0; a < 3; a++)
             if ((per & (1 << a)) && (d[a] & 1) && d[a] >= 3) L.odd_periodic = true;
@@ -325,7 +325,9 @@ extern "C" int mhdproj_create(const mhdproj_grid* grid, const mhdproj_options* o
         fail(ctx, MHDPROJ_ERR_CUDA, "cudaMallocHost failed");
         return bad(MHDPROJ_ERR_CUDA);
     }
-    ctx->L = tile_launch(grid->nx, grid->ny, grid->nz, grid->periodic, 152 * 8);
+    // Per-cell kernels: short z runs in many blocks, so the last wave of
+    // resident blocks is a small share of the launch.
+    ctx->L = tile_launch(grid->nx, grid->ny, grid->nz, grid->periodic, MAX_REDUCE_BLOCKS);
     if ((rc = [&]() -> int {
              CK(dalloc(ctx, &ctx->d_solid_prev, n));
              CK(dalloc(ctx, &ctx->d_cls, n));
