@@ -226,7 +226,12 @@ static int build_levels(mhdproj_ctx* ctx) {
     }
     P.m = d[0] * d[1] * d[2];
     CK(dalloc(ctx, &P.ainv, (size_t)P.m * P.m * sizeof(float)));
+    P.bottom_img = nullptr;
     mg_plan_bottom(P);
+    if (P.bottom_from > 0) {
+        CK(dalloc(ctx, (char**)&P.bottom_img, (size_t)P.bottom.img_floats * sizeof(float)));
+        P.bottom.img = P.bottom_img;
+    }
     // Levels run as fused pre-/post-smoothing passes: a prefix of the levels
     // that have a coarser level, an x extent divisible by 4 and even periodic
     // extents, above 4096 cells; smaller levels run in the bottom sub-cycle.
@@ -481,7 +486,8 @@ extern "C" int mhdproj_set_coefficients(mhdproj_ctx* ctx, const float* alpha, co
     CK(cudaGetLastError());
     if (ctx->use_mg) {
         mg_build(ctx->mg, ctx->stream);
-        ctx->launches += (uint64_t)ctx->mg.nlevels;  // Galerkin levels and the coarsest inverse
+        // Galerkin levels, the coarsest inverse and the bottom sub-cycle's image
+        ctx->launches += (uint64_t)ctx->mg.nlevels + (ctx->mg.bottom_from > 0 && ctx->mg.bottom_img ? 1 : 0);
         if (ctx->pipelined) {
             mg_smoother_records(ctx->mg, ctx->stream);
             ctx->launches += (uint64_t)ctx->mg.fused_levels;

@@ -109,6 +109,9 @@ struct BottomPlan {
     int nl;
     BottomLevel lv[8];
     const float* ainv;
+    const float4* img;  // shared-memory image (records, cell lists, inverse), built per coefficient set
+    int img_floats;     // its size in floats (a multiple of 4)
+    int aoff;           // coarsest inverse at aoff (floats)
     int m;
     float w;
     int nops;
@@ -131,6 +134,7 @@ struct MGPlan {
     bool w_disabled;   // the W-cycle step made the preconditioner indefinite here: V-cycles only
     size_t bottom_smem;
     BottomPlan bottom;
+    float4* bottom_img;  // the bottom sub-cycle's shared-memory image (bottom.img_floats floats)
     float* e0;         // fine-level pre-smoothed correction of the fused passes
 };
 void mg_build(const MGPlan& P, cudaStream_t s);

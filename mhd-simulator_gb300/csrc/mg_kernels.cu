@@ -20,6 +20,7 @@
 #include <functional>
 
 #include "kernels.h"
+#include "staged.cuh"
 
 namespace mhdproj {
 
@@ -436,12 +437,19 @@ __global__ void __launch_bounds__(256) k_coarse_invert(Grid3 g, const float4* __
 // per cell, so the sub-cycle stays a fixed symmetric operator).
 constexpr int BOTTOM_THREADS = 1024;
 
-template <int CK, class VT>
-__global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, const Scalars* sc) {
-    if (sc->converged) return;
+// The shared-memory image of the bottom sub-cycle that depends only on the
+// coefficients, built once per coefficient set: per level the records with
+// the diagonal in place of the reaction (k_smooth's sum order) and the cells'
+// packed coordinates (x | y << 10 | z << 20) listed red first, so loops run
+// over the cells of one colour without index arithmetic; then the coarsest
+// inverse.  Every launch of k_bottom_vcycle copies it in with 16-byte
+// cp.async.
+template <int CK>
+__global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_image(BottomPlan B, float4* __restrict__ img) {
     extern __shared__ float4 bsm4[];
     float* bsm = reinterpret_cast<float*>(bsm4);
     const int t = threadIdx.x, nt = blockDim.x;
+    auto nb = [](int c, int n, bool per) { return wrap_or_neg(c, n, per); };
     __shared__ int fill[8][2];
     if (t < 16) fill[t >> 1][t & 1] = 0;
     __syncthreads();
@@ -460,14 +468,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
             cells[col ? L.nred + k : k] = x | (y << 10) | (z << 20);
         }
     }
-    {
-        const BottomLevel& L = B.lv[0];
-        float* r = bsm + L.off;
-        const VT* rg = reinterpret_cast<const VT*>(L.r);
-        for (int i = t; i < L.n; i += nt) r[i] = to_f(rg[i]);
-    }
     __syncthreads();
-    auto nb = [](int c, int n, bool per) { return wrap_or_neg(c, n, per); };
     // the diagonal replaces the reaction in each record (k_smooth's sum order)
     for (int l = 0; l < B.nl; l++) {
         const BottomLevel& L = B.lv[l];
@@ -493,6 +494,28 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
         for (int i = t; i < L.n; i += nt) c[i].w = dtmp[i];
     }
     __syncthreads();
+    for (int i = t; i < B.m * B.m; i += nt) bsm[B.aoff + i] = B.ainv[i];
+    __syncthreads();
+    for (int i = t; i < B.img_floats / 4; i += nt) img[i] = bsm4[i];
+}
+
+template <int CK, class VT>
+__global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, const Scalars* sc) {
+    if (sc->converged) return;
+    extern __shared__ float4 bsm4[];
+    float* bsm = reinterpret_cast<float*>(bsm4);
+    const int t = threadIdx.x, nt = blockDim.x;
+    for (int i = t; i < B.img_floats / 4; i += nt) staged::cp_async16(bsm4 + i, B.img + i, true);
+    staged::cp_commit();
+    {
+        const BottomLevel& L = B.lv[0];
+        float* r = bsm + L.off;
+        const VT* rg = reinterpret_cast<const VT*>(L.r);
+        for (int i = t; i < L.n; i += nt) r[i] = to_f(rg[i]);
+    }
+    staged::cp_wait<0>();
+    __syncthreads();
+    auto nb = [](int c, int n, bool per) { return wrap_or_neg(c, n, per); };
     // sum of beta * e over the six neighbours (k_smooth order) and the diagonal
     auto stencil = [&](const BottomLevel& L, const float4* c, const float* e, int x, int y, int z, int i, float acc,
                        float* d) {
@@ -559,6 +582,11 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
             __syncthreads();
         }
     };
+    // Restriction right after the pre-smoothing half-steps.  Without odd
+    // periodic extents the residual of a black cell is zero (its update
+    // solved its equation) and that of a red cell is sum beta * e over its
+    // black neighbours, so one pass forms those sums for the red cells and a
+    // second adds each coarse cell's red children.
     auto restrict_to = [&](int l) {  // level l -> l+1
         const BottomLevel &F = B.lv[l], &C = B.lv[l + 1];
         const Grid3 &g = F.g, &gc = C.g;
@@ -567,6 +595,32 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
         const float* e = bsm + F.off + F.n;
         float* rc = bsm + C.off;
         const int* ccells = reinterpret_cast<const int*>(bsm + C.xoff);
+        if (!F.odd) {
+            float* rs = bsm + F.off + 2 * F.n;
+            const int* cells = reinterpret_cast<const int*>(bsm + F.xoff);
+#pragma unroll 2
+            for (int k = t; k < F.nred; k += nt) {
+                const int cc = cells[k], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+                const int i = x + g.nx * (y + g.ny * z);
+                float d;
+                rs[i] = stencil(F, c, e, x, y, z, i, 0.f, &d);
+            }
+            __syncthreads();
+            for (int k = t; k < C.n; k += nt) {
+                const int cq = ccells[k], X = cq & 1023, Y = (cq >> 10) & 1023, Z = cq >> 20;
+                float part = 0.f;
+                for (int dz = 0; dz < 2; dz++)
+                    for (int dy = 0; dy < 2; dy++)
+                        for (int dx = 0; dx < 2; dx++) {
+                            const int x = 2 * X + dx, y = 2 * Y + dy, z = 2 * Z + dz;
+                            if (x >= g.nx || y >= g.ny || z >= g.nz || ((x + y + z) & 1)) continue;
+                            part += rs[x + g.nx * (y + g.ny * z)];
+                        }
+                rc[X + gc.nx * (Y + gc.ny * Z)] = 0.25f * part;
+            }
+            __syncthreads();
+            return;
+        }
         for (int k = t; k < C.n; k += nt) {
             const int cq = ccells[k], X = cq & 1023, Y = (cq >> 10) & 1023, Z = cq >> 20;
             float part = 0.f;
@@ -611,14 +665,18 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
             half_step(l, 1, false);
             half_step(l, 0, false);
         } else if (op == BOP_COARSE) {
+            // e = ainv r, sixteen threads per row (m <= 64)
             const BottomLevel& K = B.lv[l];
             const float* r = bsm + K.off;
             float* e = bsm + K.off + K.n;
-            if (t < B.m) {
-                float sacc = 0.0f;
-                for (int q = 0; q < B.m; q++) sacc = fmaf(B.ainv[t * B.m + q], r[q], sacc);
-                e[t] = sacc;
-            }
+            const float* A = bsm + B.aoff;
+            const int row = t >> 4, lane = t & 15;
+            float sacc = 0.0f;
+            if (row < B.m)
+                for (int q = lane; q < B.m; q += 16) sacc = fmaf(A[row * B.m + q], r[q], sacc);
+#pragma unroll
+            for (int w = 8; w > 0; w >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, w, 16);
+            if (row < B.m && lane == 0) e[row] = sacc;
             __syncthreads();
         } else if (op == BOP_SAVE_RESID) {
             const BottomLevel& L = B.lv[l];
@@ -794,6 +852,11 @@ void mg_build(const MGPlan& P, cudaStream_t s) {
     const MGLevel& K = P.lv[P.nlevels - 1];
     const size_t smem = ((size_t)P.m * P.m + P.m) * sizeof(double);
     k_coarse_invert<<<P.m, 256, smem, s>>>(K.L.g, K.coef32, P.ainv);
+    if (P.bottom_from > 0 && P.bottom_img) {
+        if (P.precision == 1) k_bottom_image<1><<<1, BOTTOM_THREADS, P.bottom_smem, s>>>(P.bottom, P.bottom_img);
+        else if (P.precision == 2) k_bottom_image<2><<<1, BOTTOM_THREADS, P.bottom_smem, s>>>(P.bottom, P.bottom_img);
+        else k_bottom_image<0><<<1, BOTTOM_THREADS, P.bottom_smem, s>>>(P.bottom, P.bottom_img);
+    }
 }
 
 cudaError_t mg_prepare_attributes() {
@@ -803,6 +866,9 @@ cudaError_t mg_prepare_attributes() {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bottom_vcycle<1, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, bmax);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_bottom_vcycle<2, __nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bmax);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bottom_image<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, bmax);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bottom_image<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bmax);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bottom_image<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bmax);
     return e;
 }
 
@@ -831,11 +897,23 @@ void mg_plan_bottom(MGPlan& P) {
             lb = l;
             break;
         }
-    if (lb < 0 || P.nlevels - lb > 8 || P.m > BOTTOM_THREADS) return;
+    if (lb < 0 || P.nlevels - lb > 8 || P.m > BOTTOM_THREADS / 16) return;
     BottomPlan& B = P.bottom;
     B.nl = P.nlevels - lb;
-    size_t f4 = 0, fl = 0;  // float4 and float counts
+    // Shared memory: the image (records of every level as float4s, the
+    // cell lists, the coarsest inverse), then per level r, e, scratch and
+    // saved e (floats).
+    size_t f4 = 0;
     for (int k = 0; k < B.nl; k++) f4 += (size_t)P.lv[lb + k].L.g.n();
+    size_t fl = 4 * f4;
+    for (int k = 0; k < B.nl; k++) {
+        B.lv[k].xoff = (int)fl;
+        fl += (size_t)P.lv[lb + k].L.g.n();  // cell list (ints)
+    }
+    B.aoff = (int)fl;
+    fl += (size_t)P.m * P.m;
+    fl = (fl + 3) & ~(size_t)3;
+    B.img_floats = (int)fl;
     for (int k = 0; k < B.nl; k++) {
         const MGLevel& L = P.lv[lb + k];
         BottomLevel& b = B.lv[k];
@@ -846,10 +924,8 @@ void mg_plan_bottom(MGPlan& P) {
         b.e = L.e;
         b.odd = L.odd_periodic;
         b.coff = k == 0 ? 0 : B.lv[k - 1].coff + B.lv[k - 1].n;
-        b.off = (int)(4 * f4 + fl);
+        b.off = (int)fl;
         fl += 4 * (size_t)b.n;  // r, e, scratch, saved e
-        b.xoff = (int)(4 * f4 + fl);
-        fl += (size_t)b.n;      // cell list (ints)
         int nred = 0;
         for (int z = 0; z < b.g.nz; z++)
             for (int y = 0; y < b.g.ny; y++)
@@ -861,7 +937,8 @@ void mg_plan_bottom(MGPlan& P) {
     B.ainv = P.ainv;
     B.m = P.m;
     B.w = P.prolong;
-    const size_t bytes = (4 * f4 + fl) * sizeof(float);
+    B.img = P.bottom_img;
+    const size_t bytes = fl * sizeof(float);
     if (bytes > BOTTOM_SMEM_MAX) return;
     // the cycle program: level k's coarse correction takes two visits when
     // level lb + k is a W-cycle level (the program is cut back to V visits
