@@ -10,7 +10,7 @@
 //   prolongation                                    e <- e + w P ec
 //   black half-step, then red half-step             z       = the smoothed correction
 //   [fine level] r . z for the CG step length.
-// Both march a 64 x 8 (x, y) tile along z.  The stages of one pass run as a
+// Both march a 64 x 16 (x, y) tile along z.  The stages of one pass run as a
 // pipeline over planes: the pre-smoothing pass forms the residual and the red
 // values of plane z, the black values of plane z-1 and the restricted
 // residual of plane z-2 in the same step, so every input plane is read from
@@ -18,11 +18,18 @@
 // region one cell wider than the next: the red values cover the tile with a
 // 2-cell halo, the black values a 1-cell halo, the residual the tile itself.
 // Halo cells are recomputed by both neighbouring tiles from the same inputs
-// in the same order, so the values agree bit for bit.  The smoother records
-// are staged in shared memory with zero-filling 16-byte cp.async one plane
-// ahead of the red stage (a staged row spans x0-4 .. x0+67, so every copy is
-// a 16-byte-aligned group of records); the vector inputs of the red stage go
-// to registers one plane ahead.  Three barriers per plane.
+// in the same order, so the values agree bit for bit.
+//
+// Work is split in quads, four consecutive cells x0-4+4q .. x0-1+4q of a
+// row.  x0-4 is even, so in a quad the cells of one colour are the two cells
+// of one x parity.  Shared-memory planes are [rows][2][36]: each staged row
+// (x0-4 .. x0+67) holds its even-x cells, then its odd-x cells, so a quad's
+// cells of one colour are two adjacent floats and a warp's accesses are
+// contiguous.  The smoother records are staged one plane ahead with
+// zero-filling 16-byte cp.async (the records in HBM use the same split along
+// whole grid rows, so a staged half row is one contiguous run); the red
+// stage's vector inputs go to registers, loaded once the stage has consumed
+// the previous plane's.  Three barriers per plane.
 //
 // The smoother reads per-cell records (beta_x, beta_y, beta_z of the low
 // faces, diagonal) prepared once per coefficient set, the diagonal rounded
@@ -41,38 +48,64 @@ namespace mhdproj {
 namespace {
 using namespace staged;
 
-constexpr int PX = 2 * TX;       // 64 cells per tile row
-constexpr int FTY = 8;           // tile rows (one thread row per tile row)
-constexpr int FT = TX * FTY;     // 256 threads per block
+constexpr int PX = 64;           // cells per tile row
+constexpr int QX = PX / 4;       // 16 threads per tile row, one quad each
 constexpr int XO = 4;            // staged rows start at x0 - XO
 constexpr int RW = PX + 2 * XO;  // 72 staged columns: x0-4 .. x0+67
 constexpr int HW = RW / 2;       // 36 columns per half row (even x, then odd x)
-constexpr int RH = FTY + 4;      // vector rows:  y0-2 .. y0+FTY+1
-constexpr int CH = FTY + 5;      // record rows:  y0-2 .. y0+FTY+2
-constexpr int RP = (PX + 4) / 2; // 34 pairs of the 2-halo region (x0-2 .. x0+65)
-constexpr int NRED = RH * RP;    // 408 red-stage pair tasks
-constexpr int NBLK = (FTY + 2) * RP;  // 340 black-stage pair tasks (rows y0-1 .. y0+FTY)
-static_assert(NRED <= 2 * FT && NBLK <= 2 * FT, "two tasks per thread");
+constexpr int NQ = RW / 4;       // 18 quads per staged row
+// Tile rows: 16 with 8-byte (FP16/BF16) records, 8 with 16-byte (FP32)
+// records, so that three blocks fit the shared memory of an SM.
+template <int FTY_>
+struct Geo {
+    static constexpr int FTY = FTY_;               // one thread row per tile row
+    static constexpr int FT = QX * FTY;            // threads per block
+    static constexpr int RH = FTY + 4;             // vector rows:  y0-2 .. y0+FTY+1
+    static constexpr int CH = FTY + 5;             // record rows:  y0-2 .. y0+FTY+2
+    static constexpr int NRED = RH * NQ;           // red-stage quads (rows y0-2 .. y0+FTY+1)
+    static constexpr int NBLK = (FTY + 2) * NQ;    // black-stage quads (rows y0-1 .. y0+FTY)
+    static_assert(NRED <= 2 * FT && NBLK <= 2 * FT, "two tasks per thread");
+};
+template <int CK>
+using GeoOf = Geo<CK == 0 ? 8 : 16>;
 
-template <class VT> __device__ __forceinline__ float2 ld2(const VT* p);
-template <> __device__ __forceinline__ float2 ld2<float>(const float* p) { return *reinterpret_cast<const float2*>(p); }
-template <> __device__ __forceinline__ float2 ld2<__half>(const __half* p) {
-    return __half22float2(*reinterpret_cast<const __half2*>(p));
+// Quads of a vector field as loaded (16 bytes FP32, 8 bytes FP16/BF16),
+// kept in the load type until the stage that uses them: a conversion right
+// after the load would wait for the load.
+template <class VT> struct Raw4 { using T = float4; };
+template <> struct Raw4<__half> { using T = uint2; };
+template <> struct Raw4<__nv_bfloat16> { using T = uint2; };
+template <class VT>
+__device__ __forceinline__ typename Raw4<VT>::T ldg_quad(const VT* p, bool ok) {
+    using R = typename Raw4<VT>::T;
+    R v;
+    if (ok) v = __ldg(reinterpret_cast<const R*>(p));
+    else v = R{};  // float4 / uint2: zeros
+    return v;
 }
-template <> __device__ __forceinline__ float2 ld2<__nv_bfloat16>(const __nv_bfloat16* p) {
-    return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(p));
+template <class VT> __device__ __forceinline__ float4 cvt4r(const typename Raw4<VT>::T& v);
+template <> __device__ __forceinline__ float4 cvt4r<float>(const float4& v) { return v; }
+template <> __device__ __forceinline__ float4 cvt4r<__half>(const uint2& u) {
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
 }
-template <class VT> __device__ __forceinline__ void st2(VT* p, float2 v);
-template <> __device__ __forceinline__ void st2<float>(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
-template <> __device__ __forceinline__ void st2<__half>(__half* p, float2 v) {
-    *reinterpret_cast<__half2*>(p) = __floats2half2_rn(v.x, v.y);
+template <> __device__ __forceinline__ float4 cvt4r<__nv_bfloat16>(const uint2& u) {
+    const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
+    const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
 }
-template <> __device__ __forceinline__ void st2<__nv_bfloat16>(__nv_bfloat16* p, float2 v) {
-    *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(v.x, v.y);
+template <class VT> __device__ __forceinline__ void st4(VT* p, float4 v);
+template <> __device__ __forceinline__ void st4<float>(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+template <> __device__ __forceinline__ void st4<__half>(__half* p, float4 v) {
+    const __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
+    *reinterpret_cast<uint2*>(p) = make_uint2(*reinterpret_cast<const unsigned*>(&a), *reinterpret_cast<const unsigned*>(&b));
 }
-// Pairs of consecutive cells as loaded from a vector field, kept in the load
-// type until the stage that uses them (a conversion right after the load
-// would wait for the load).
+template <> __device__ __forceinline__ void st4<__nv_bfloat16>(__nv_bfloat16* p, float4 v) {
+    const __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y), b = __floats2bfloat162_rn(v.z, v.w);
+    *reinterpret_cast<uint2*>(p) = make_uint2(*reinterpret_cast<const unsigned*>(&a), *reinterpret_cast<const unsigned*>(&b));
+}
+// Two consecutive coarse cells (a quad's parents).
 template <class VT> struct Raw2 { using T = float2; };
 template <> struct Raw2<__half> { using T = __half2; };
 template <> struct Raw2<__nv_bfloat16> { using T = __nv_bfloat162; };
@@ -90,24 +123,29 @@ __device__ __forceinline__ typename Raw2<VT>::T ldg_pair(const VT* p, bool ok) {
 __device__ __forceinline__ float2 cvt2(const float2& v) { return v; }
 __device__ __forceinline__ float2 cvt2(const __half2& v) { return __half22float2(v); }
 __device__ __forceinline__ float2 cvt2(const __nv_bfloat162& v) { return __bfloat1622float2(v); }
-template <class VT>
-__device__ __forceinline__ VT ldg_one(const VT* p, bool ok) {
-    return ok ? __ldg(p) : from_f<VT>(0.f);
+template <class VT> __device__ __forceinline__ void st2(VT* p, float2 v);
+template <> __device__ __forceinline__ void st2<float>(float* p, float2 v) { *reinterpret_cast<float2*>(p) = v; }
+template <> __device__ __forceinline__ void st2<__half>(__half* p, float2 v) {
+    *reinterpret_cast<__half2*>(p) = __floats2half2_rn(v.x, v.y);
+}
+template <> __device__ __forceinline__ void st2<__nv_bfloat16>(__nv_bfloat16* p, float2 v) {
+    *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(v.x, v.y);
 }
 
 // A thread's share of one plane's record copies, resolved once per block:
-// two (8-byte records) or four (16-byte records) 16-byte copies of the
-// record rows (13 rows x 2 half rows x 36 records).  A copy of two 8-byte
-// records covers cells x and x+2 of a four-cell group, so both exist or
-// neither does (nx is a multiple of 4).
+// NCT 16-byte copies of the record rows (21 rows x 2 half rows x 36
+// 8-byte records, or 13 rows x 2 x 36 16-byte records).  A copy of two 8-byte
+// records covers cells x and x+2 of a quad, so both exist or neither does
+// (nx is a multiple of 4).
 template <int CK>
 struct RecordFetch {
     using CT = typename CoefStore<CK>::T;
+    using G = GeoOf<CK>;
+    static constexpr int FT = G::FT;
     static constexpr int RPC = (CK == 0) ? 1 : 2;  // records per 16-byte copy
-    static constexpr int NCT = (CK == 0) ? 4 : 2;
     static constexpr int PER = HW / RPC;           // copies per half row
-    static constexpr int NCTOT = CH * 2 * PER;
-    static_assert(NCTOT <= NCT * FT, "record copies per thread");
+    static constexpr int NCTOT = G::CH * 2 * PER;
+    static constexpr int NCT = (NCTOT + FT - 1) / FT;
     int coff[NCT];
     short cdst[NCT];
     bool cok[NCT];
@@ -152,65 +190,97 @@ struct RecordFetch {
     }
 };
 
-// Shared-memory planes are [rows][2][HW]: each staged row holds its even-x
-// cells, then its odd-x cells, so the cells of one colour in a row are
-// contiguous.  A cell in half h at offset o has its x-1 neighbour at
-// xminus(o, h) and its x+1 neighbour one further.
-__device__ __forceinline__ int xminus(int o, int h) { return h ? o - HW : o + HW - 1; }
-
-// The smoother records in HBM use the same split along whole grid rows: row
-// (y, z) holds its nx/2 even-x records, then its nx/2 odd-x records, so a
-// staged half row is one contiguous run.  Position of column x in its row:
+// The smoother records in HBM are split along whole grid rows: row (y, z)
+// holds its nx/2 even-x records, then its nx/2 odd-x records.  Position of
+// column x in its row:
 __device__ __forceinline__ int split_x(int x, int nx) { return (x & 1) * (nx >> 1) + (x >> 1); }
 
-// sum of beta * e over the six neighbours added to acc, in the per-cell
-// kernels' order; *d = the cell's diagonal.  Offset o (half h) into the
-// split planes; c/cn: record planes z, z+1; e/em/ep: correction planes z,
-// z-1, z+1.
+// Two adjacent records of one half row (offsets o, o+1; o even).
 template <int CK, class CT>
-__device__ __forceinline__ float gs_sum(const CT* c, const CT* cn, const float* e, const float* em, const float* ep,
-                                        int o, int h, float acc, float* d) {
-    const int xm = xminus(o, h);
-    const float4 own = unpack<CK>(c[o]);
-    const float bxh = unpack<CK>(c[xm + 1]).x;
-    const float byh = unpack<CK>(c[o + RW]).y;
-    const float bzh = unpack<CK>(cn[o]).z;
-    acc = fmaf(own.x, e[xm], acc);
-    acc = fmaf(bxh, e[xm + 1], acc);
-    acc = fmaf(own.y, e[o - RW], acc);
-    acc = fmaf(byh, e[o + RW], acc);
-    acc = fmaf(own.z, em[o], acc);
-    acc = fmaf(bzh, ep[o], acc);
-    *d = own.w;
-    return acc;
+__device__ __forceinline__ void rec2(const CT* p, float4* a, float4* b) {
+    if constexpr (CK == 0) {
+        *a = unpack<0>(reinterpret_cast<const float4*>(p)[0]);
+        *b = unpack<0>(reinterpret_cast<const float4*>(p)[1]);
+    } else {
+        const uint4 u = *reinterpret_cast<const uint4*>(p);
+        *a = unpack<CK>(make_uint2(u.x, u.y));
+        *b = unpack<CK>(make_uint2(u.z, u.w));
+    }
 }
 
-// A thread's pair tasks of the red / prolongation (2-halo) and black
-// (1-halo) stages, resolved once per block: split-plane offsets of the pair's
-// even cell (the odd cell is HW further), the colour parity of its row, the pair's in-plane offset in the grid
-// (wrapped on periodic axes) and whether it exists, and for tasks on the tile
-// the unwrapped in-plane offset (-1 otherwise).  Black tasks at the region's
-// x edges update only the member inside the 1-halo.
-struct PairTasks {
-    int roff[2], rpar[2], rown[2], goff[2];
+// Sums of beta * e over the six neighbours, added to acc, for the two cells
+// of one colour of a quad: half h, offsets o and o+1 of the split planes
+// (o = row * RW + h * HW + 2q); *d their diagonals.  c/cn: record planes z,
+// z+1; e/em/ep: correction planes z, z-1, z+1.  The x neighbours lie in the
+// other half: for h = 0 (even x) at other[2q-1 .. 2q+1], for h = 1 at
+// other[2q .. 2q+2].
+template <int CK, class CT>
+__device__ __forceinline__ float2 gs_sum2(const CT* c, const CT* cn, const float* e, const float* em,
+                                          const float* ep, int o, int h, float2 acc, float2* d) {
+    const int ot = h ? o - HW : o + HW;  // the other half, same index
+    const float2 f = *reinterpret_cast<const float2*>(e + ot);
+    const float s = e[h ? ot + 2 : ot - 1];
+    const float xm0 = h ? f.x : s, xp0 = h ? f.y : f.x;
+    const float xm1 = h ? f.y : f.x, xp1 = h ? s : f.y;
+    float4 own0, own1, yh0, yh1, zh0, zh1;
+    rec2<CK>(c + o, &own0, &own1);
+    rec2<CK>(c + o + RW, &yh0, &yh1);
+    rec2<CK>(cn + o, &zh0, &zh1);
+    const float bxh0 = unpack<CK>(c[ot + h]).x, bxh1 = unpack<CK>(c[ot + h + 1]).x;
+    const float2 ym = *reinterpret_cast<const float2*>(e + o - RW);
+    const float2 yp = *reinterpret_cast<const float2*>(e + o + RW);
+    const float2 zm = *reinterpret_cast<const float2*>(em + o);
+    const float2 zp = *reinterpret_cast<const float2*>(ep + o);
+    float a0 = acc.x, a1 = acc.y;
+    a0 = fmaf(own0.x, xm0, a0);
+    a1 = fmaf(own1.x, xm1, a1);
+    a0 = fmaf(bxh0, xp0, a0);
+    a1 = fmaf(bxh1, xp1, a1);
+    a0 = fmaf(own0.y, ym.x, a0);
+    a1 = fmaf(own1.y, ym.y, a1);
+    a0 = fmaf(yh0.y, yp.x, a0);
+    a1 = fmaf(yh1.y, yp.y, a1);
+    a0 = fmaf(own0.z, zm.x, a0);
+    a1 = fmaf(own1.z, zm.y, a1);
+    a0 = fmaf(zh0.z, zp.x, a0);
+    a1 = fmaf(zh1.z, zp.y, a1);
+    *d = make_float2(own0.w, own1.w);
+    return make_float2(a0, a1);
+}
+
+__device__ __forceinline__ float2 divide2(float2 s, float2 d) {
+    return make_float2(d.x > 0.f ? __fdividef(s.x, d.x) : 0.f, d.y > 0.f ? __fdividef(s.y, d.y) : 0.f);
+}
+
+// A thread's quad tasks of the red / prolongation (2-halo rows, quads 0..17)
+// and black (1-halo rows) stages, resolved once per block: the split-plane
+// offset of the quad's even half (the odd half is HW further), the row's y,
+// the quad's in-plane offset in the grid (wrapped on periodic axes) and
+// whether it exists, and for quads on the tile the unwrapped in-plane offset
+// (-1 otherwise).  Cells outside the regions (quads 0 and 17 reach two cells
+// beyond the 2-halo) are computed like the others and never read.
+template <class G>
+struct QuadTasks {
+    static constexpr int FT = G::FT, FTY = G::FTY, NRED = G::NRED, NBLK = G::NBLK;
+    int roff[2], ry[2], rown[2], goff[2];
     bool gok[2];
-    int boff[2], bpar[2], bedge[2];
-    __device__ __forceinline__ PairTasks(const Grid3& g, int x0, int y0, int t) {
+    int boff[2], by[2];
+    __device__ __forceinline__ QuadTasks(const Grid3& g, int x0, int y0, int t) {
         const bool px = g.periodic & 1, py = g.periodic & 2;
 #pragma unroll
         for (int u = 0; u < 2; u++) {
             const int k = t + u * FT;
             roff[u] = -1;
-            rpar[u] = 0;
+            ry[u] = 0;
             rown[u] = -1;
             goff[u] = 0;
             gok[u] = false;
             if (k < NRED) {
-                const int row = k / RP, pc = k - row * RP;
-                roff[u] = row * RW + 1 + pc;
-                rpar[u] = (y0 - 2 + row) & 1;
-                const int gx = x0 - 2 + 2 * pc, gy = y0 - 2 + row;
-                if (row >= 2 && row < FTY + 2 && pc >= 1 && pc <= TX && gx < g.nx && gy < g.ny) rown[u] = gx + g.nx * gy;
+                const int row = k / NQ, q = k - row * NQ;
+                roff[u] = row * RW + 2 * q;
+                const int gx = x0 - XO + 4 * q, gy = y0 - 2 + row;
+                ry[u] = gy;
+                if (row >= 2 && row < FTY + 2 && q >= 1 && q <= QX && gx < g.nx && gy < g.ny) rown[u] = gx + g.nx * gy;
                 bool okx, oky;
                 const int sx = axis_src(gx, g.nx, px, &okx);
                 const int sy = axis_src(gy, g.ny, py, &oky);
@@ -218,51 +288,42 @@ struct PairTasks {
                 goff[u] = gok[u] ? sx + g.nx * sy : 0;
             }
             boff[u] = -1;
-            bpar[u] = 0;
-            bedge[u] = 0;
+            by[u] = 0;
             if (k < NBLK) {
-                const int rr = k / RP, pc = k - rr * RP, row = rr + 1;
-                boff[u] = row * RW + 1 + pc;
-                bpar[u] = (1 + y0 - 2 + row) & 1;
-                bedge[u] = pc == 0 ? 1 : (pc == RP - 1 ? 2 : 0);
+                const int rb = k / NQ, q = k - rb * NQ, row = rb + 1;
+                boff[u] = row * RW + 2 * q;
+                by[u] = y0 - 2 + row;
             }
         }
     }
-    // red member (0 or 1) of red task u at plane z
-    __device__ __forceinline__ int red(int u, int z) const { return (rpar[u] + z) & 1; }
-    // black member (0 or 1) of black task u at plane z, or -1 when it lies
-    // outside the 1-halo
-    __device__ __forceinline__ int black(int u, int z) const {
-        const int m = (bpar[u] + z) & 1;
-        if ((bedge[u] == 1 && m == 0) || (bedge[u] == 2 && m == 1)) return -1;
-        return m;
-    }
 };
+// Red half (x parity of the red cells) of row y at plane z; x0-4 is even.
+__device__ __forceinline__ int red_half(int y, int z) { return (y + z) & 1; }
 
 // Plane rings in shared memory.  A step handles planes zA (red /
 // prolongation stage), zA-1 (black stage) and zA-2 (tile stage) and stages
 // the records of plane zA+1 for the next step; rings of 4 planes, so the z
-// loop is unrolled four times and every slot is a compile-time offset.  The
-// vector inputs go straight to registers, one plane ahead.  In the correction
-// ring the black cells of the newest plane hold their right-hand side sigma r
-// until the black stage replaces it by their value.
+// loop is unrolled four times and every slot is a compile-time offset.  In
+// the correction ring the black cells of the newest plane hold their
+// right-hand side sigma r until the black stage replaces it by their value.
 template <int CK>
 struct PreRing {
     using CT = typename CoefStore<CK>::T;
-    CT c[4][CH][RW];                 // records, planes zA-2 .. zA+1
-    float er[4][RH][RW];             // correction, planes zA-3 .. zA
-    float ypart[FTY][TX];
+    using G = GeoOf<CK>;
+    CT c[4][G::CH][RW];              // records, planes zA-2 .. zA+1
+    float er[4][G::RH][RW];          // correction, planes zA-3 .. zA
+    float2 ypart[G::FTY][QX];
 };
 template <int CK>
 struct PostRing {
     using CT = typename CoefStore<CK>::T;
-    CT c[4][CH][RW];                 // records, planes zA-2 .. zA+1
-    float ep[4][RH][RW];             // prolonged / smoothed correction, planes zA-3 .. zA
+    using G = GeoOf<CK>;
+    CT c[4][G::CH][RW];              // records, planes zA-2 .. zA+1
+    float ep[4][G::RH][RW];          // prolonged / smoothed correction, planes zA-3 .. zA
 };
 template <int N>
 using Phase = std::integral_constant<int, N>;
-template <int CK>
-constexpr int fused_min_blocks() { return CK == 0 ? 3 : 4; }
+constexpr int FUSED_MIN_BLOCKS = 3;
 }  // namespace
 
 // ------------------------------------------------------ pre-smoothing pass
@@ -276,13 +337,15 @@ constexpr int fused_min_blocks() { return CK == 0 ? 3 : 4; }
 // the restriction sums those neighbour terms over the red cells.
 // rin and q must not alias r_out (other tiles read them as halo).
 template <int CK, class VT, class VTc, bool UPDATE, bool FINE>
-__global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
+__global__ void __launch_bounds__(GeoOf<CK>::FT, FUSED_MIN_BLOCKS)
     k_presmooth_restrict(Grid3 g, Grid3 gc, const void* __restrict__ sm_v, const VT* __restrict__ rin,
                          const float* __restrict__ q, float* __restrict__ r_out, VT* __restrict__ e,
                          VTc* __restrict__ rc, Scalars* sc, double* partials, int nblocks) {
     if (sc->converged) return;
     using CT = typename CoefStore<CK>::T;
-    using R2 = typename Raw2<VT>::T;
+    using G = GeoOf<CK>;
+    constexpr int FTY = G::FTY, FT = G::FT;
+    using R4 = typename Raw4<VT>::T;
     const CT* sm = reinterpret_cast<const CT*>(sm_v);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto& S = *reinterpret_cast<PreRing<CK>*>(smem_raw);
@@ -290,40 +353,43 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
     const float sigma = FINE ? sc->sigma : 1.0f;
     const float alpha = UPDATE ? sc->alpha_f : 0.0f;
     const int x0 = blockIdx.x * PX, y0 = blockIdx.y * FTY;
-    const int tx = threadIdx.x, ty = threadIdx.y, t = tx + TX * ty;
+    const int tx = threadIdx.x, ty = threadIdx.y, t = tx + QX * ty;
     const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
     const RecordFetch<CK> F(g, x0, y0, t);
-    const PairTasks T(g, x0, y0, t);
+    const QuadTasks<G> T(g, x0, y0, t);
     const long long sxy = (long long)g.nx * g.ny;
     // ||r||^2 only steers the stop test and sigma: a per-thread FP32 sum,
     // FP64 across threads and blocks
     float rr_thread = 0.f;
-    float part = 0.f;
+    float2 part = make_float2(0.f, 0.f);  // restriction sums of the own quad's two parents
     int rc_z = -1;  // coarse plane whose restriction awaits the row pair sum
-    const int ox = x0 + 2 * tx, oy = y0 + ty;  // the thread's own pair
+    const int ox = x0 + 4 * tx, oy = y0 + ty;  // the thread's own quad
     const bool own_inside = ox < g.nx && oy < g.ny;
-    const int oo = (ty + 2) * RW + XO / 2 + tx;  // split offset of its even cell
+    const int oo = (ty + 2) * RW + 2 * (tx + 1);  // split offset of its even half
     const long long og = ox + (long long)g.nx * oy;
-    R2 rv[2], rvn[2];
-    float2 qv[2], qvn[2];
-    // records of plane zz to ring slot c4 (cp.async), the red tasks' residual
-    // (and q) of plane zz to registers
-    auto fetch = [&](int zz, int c4, R2* rd, float2* qd) {
+    R4 rv[2];
+    float4 qv[2];
+    auto stage = [&](int zz, int c4) {
         bool okz;
         const long long pl = F.plane(zz, &okz);
         F.recs(&S.c[c4][0][0], sm, pl, okz);
         cp_commit();
+    };
+    auto load = [&](int zz) {  // the red tasks' residual (and q) of plane zz
+        bool okz;
+        const long long pl = F.plane(zz, &okz);
 #pragma unroll
         for (int u = 0; u < 2; u++) {
             const bool ok = T.gok[u] && okz;
-            rd[u] = ldg_pair<VT>(rin + pl + T.goff[u], ok);
-            if (UPDATE) qd[u] = ok ? __ldg(reinterpret_cast<const float2*>(q + pl + T.goff[u])) : make_float2(0.f, 0.f);
+            rv[u] = ldg_quad<VT>(rin + pl + T.goff[u], ok);
+            if (UPDATE) qv[u] = ok ? __ldg(reinterpret_cast<const float4*>(q + pl + T.goff[u])) : make_float4(0.f, 0.f, 0.f, 0.f);
         }
     };
     auto flush_rc = [&]() {
         if (rc_z >= 0 && own_inside && !(ty & 1)) {
-            const float tot = S.ypart[ty][tx] + S.ypart[ty + 1][tx];
-            rc[(ox >> 1) + (long long)gc.nx * ((oy >> 1) + (long long)gc.ny * rc_z)] = from_f<VTc>(0.25f * tot);
+            const float2 a = S.ypart[ty][tx], b = S.ypart[ty + 1][tx];
+            st2<VTc>(rc + (ox >> 1) + (long long)gc.nx * ((oy >> 1) + (long long)gc.ny * rc_z),
+                     make_float2(0.25f * (a.x + b.x), 0.25f * (a.y + b.y)));
         }
         rc_z = -1;
     };
@@ -331,9 +397,9 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
         constexpr int P = decltype(ph)::value;
         cp_wait<0>();
         __syncthreads();
-        fetch(zA + 1, (P + 1) & 3, rvn, UPDATE ? qvn : nullptr);
+        stage(zA + 1, (P + 1) & 3);
         flush_rc();
-        // ---- red stage: plane zA over the 2-halo region
+        // ---- red stage: plane zA over the 2-halo rows
         {
             const CT* C = &S.c[P][0][0];
             float* ER = &S.er[P][0][0];
@@ -343,21 +409,27 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
             for (int u = 0; u < 2; u++) {
                 const int o = T.roff[u];
                 if (o < 0) break;
-                float2 rn = cvt2(rv[u]);
-                if (UPDATE) rn = make_float2(fmaf(-alpha, qv[u].x, rn.x), fmaf(-alpha, qv[u].y, rn.y));
-                const int m = T.red(u, zA);
-                const float d = unpack<CK>(C[o + m * HW]).w;
-                const float ev = d > 0.f ? __fdividef(sigma * (m ? rn.y : rn.x), d) : 0.f;
-                ER[o] = m ? sigma * rn.x : ev;
-                ER[o + HW] = m ? ev : sigma * rn.y;
+                float4 rn = cvt4r<VT>(rv[u]);
+                if (UPDATE)
+                    rn = make_float4(fmaf(-alpha, qv[u].x, rn.x), fmaf(-alpha, qv[u].y, rn.y),
+                                     fmaf(-alpha, qv[u].z, rn.z), fmaf(-alpha, qv[u].w, rn.w));
+                const int p = red_half(T.ry[u], zA);
+                float4 d0, d1;
+                rec2<CK>(C + o + p * HW, &d0, &d1);
+                const float2 rr = p ? make_float2(rn.y, rn.w) : make_float2(rn.x, rn.z);  // red cells
+                const float2 rb = p ? make_float2(rn.x, rn.z) : make_float2(rn.y, rn.w);  // black cells
+                const float2 ev = divide2(make_float2(sigma * rr.x, sigma * rr.y), make_float2(d0.w, d1.w));
+                *reinterpret_cast<float2*>(ER + o + p * HW) = ev;
+                *reinterpret_cast<float2*>(ER + o + (1 - p) * HW) = make_float2(sigma * rb.x, sigma * rb.y);
                 if (UPDATE && zin && T.rown[u] >= 0) {
-                    *reinterpret_cast<float2*>(rplane + T.rown[u]) = rn;
-                    rr_thread = fmaf(rn.x, rn.x, fmaf(rn.y, rn.y, rr_thread));
+                    *reinterpret_cast<float4*>(rplane + T.rown[u]) = rn;
+                    rr_thread = fmaf(rn.x, rn.x, fmaf(rn.y, rn.y, fmaf(rn.z, rn.z, fmaf(rn.w, rn.w, rr_thread))));
                 }
             }
         }
+        load(zA + 1);
         __syncthreads();
-        // ---- black stage: plane zA-1 over the 1-halo region, in place
+        // ---- black stage: plane zA-1 over the 1-halo rows, in place
         const int zB = zA - 1;
         if (zB >= z0 - 1) {
             const CT* C = &S.c[(P + 3) & 3][0][0];
@@ -367,12 +439,12 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
             const float* EP = &S.er[P][0][0];
 #pragma unroll
             for (int u = 0; u < 2; u++) {
-                const int h = T.black(u, zB);
-                if (h < 0) continue;
+                if (T.boff[u] < 0) break;
+                const int h = 1 - red_half(T.by[u], zB);
                 const int o = T.boff[u] + h * HW;
-                float d;
-                const float s = gs_sum<CK>(C, CN, E, EM, EP, o, h, E[o], &d);
-                E[o] = d > 0.f ? __fdividef(s, d) : 0.f;
+                float2 d;
+                const float2 s = gs_sum2<CK>(C, CN, E, EM, EP, o, h, *reinterpret_cast<const float2*>(E + o), &d);
+                *reinterpret_cast<float2*>(E + o) = divide2(s, d);
             }
         }
         __syncthreads();
@@ -384,25 +456,27 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
             const float* E = &S.er[(P + 2) & 3][0][0];
             const float* EM = &S.er[(P + 1) & 3][0][0];
             const float* EP = &S.er[(P + 3) & 3][0][0];
-            const int m = (y0 + ty + zC) & 1;  // red member of the own pair
-            float d;
-            part += gs_sum<CK>(C, CN, E, EM, EP, oo + m * HW, m, 0.f, &d);
-            if (own_inside) st2<VT>(e + (og + sxy * zC), make_float2(E[oo], E[oo + HW]));
+            const int p = red_half(oy, zC);  // red half of the own quad
+            float2 d;
+            const float2 s = gs_sum2<CK>(C, CN, E, EM, EP, oo + p * HW, p, make_float2(0.f, 0.f), &d);
+            part.x += s.x;
+            part.y += s.y;
+            if (own_inside) {
+                const float2 ev = *reinterpret_cast<const float2*>(E + oo);
+                const float2 od = *reinterpret_cast<const float2*>(E + oo + HW);
+                st4<VT>(e + (og + sxy * zC), make_float4(ev.x, od.x, ev.y, od.y));
+            }
             if (((zC - z0) & 1) || zC + 1 == z1) {
                 // the row pair sum is formed after the next barrier
                 S.ypart[ty][tx] = part;
                 rc_z = zC >> 1;
-                part = 0.f;
+                part = make_float2(0.f, 0.f);
             }
-        }
-#pragma unroll
-        for (int u = 0; u < 2; u++) {
-            rv[u] = rvn[u];
-            if (UPDATE) qv[u] = qvn[u];
         }
     };
     const int zs = z0 - 2, zend = z1 + 1;  // red stage over zs .. zend
-    fetch(zs, 0, rv, UPDATE ? qv : nullptr);
+    stage(zs, 0);
+    load(zs);
     for (int zA = zs;;) {
         step(Phase<0>{}, zA);
         if (++zA > zend) break;
@@ -444,14 +518,17 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
 // is then taken from ||r||^2.  The black half-step does not read a black
 // cell's own prolonged value, so the prolongation stage leaves sigma r there.
 template <int CK, class VT, class VTc, bool DOT, bool FINE>
-__global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
+__global__ void __launch_bounds__(GeoOf<CK>::FT, FUSED_MIN_BLOCKS)
     k_prolong_postsmooth(Grid3 g, Grid3 gc, const void* __restrict__ sm_v, const VT* __restrict__ e,
                          const VTc* __restrict__ ec, const VT* __restrict__ r, VT* __restrict__ out,
                          const VT* __restrict__ accum, float w, Scalars* sc, double* partials, int nblocks,
                          long long n_active) {
     if (sc->converged) return;
     using CT = typename CoefStore<CK>::T;
-    using R2 = typename Raw2<VT>::T;
+    using G = GeoOf<CK>;
+    constexpr int FTY = G::FTY, FT = G::FT;
+    using R4 = typename Raw4<VT>::T;
+    using C2 = typename Raw2<VTc>::T;
     const CT* sm = reinterpret_cast<const CT*>(sm_v);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     auto& S = *reinterpret_cast<PostRing<CK>*>(smem_raw);
@@ -459,12 +536,12 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
     const float sigma = FINE ? sc->sigma : 1.0f;
     const float is = FINE ? sc->inv_sigma : 1.0f;
     const int x0 = blockIdx.x * PX, y0 = blockIdx.y * FTY;
-    const int tx = threadIdx.x, ty = threadIdx.y, t = tx + TX * ty;
+    const int tx = threadIdx.x, ty = threadIdx.y, t = tx + QX * ty;
     const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
     const RecordFetch<CK> F(g, x0, y0, t);
-    const PairTasks T(g, x0, y0, t);
+    const QuadTasks<G> T(g, x0, y0, t);
     const long long sxy = (long long)g.nx * g.ny;
-    // coarse parents of the red-stage pairs: in-plane offsets
+    // coarse parents of the red-stage quads: in-plane offsets of the pair
     int pofs[2];
     {
         const bool px = g.periodic & 1, py = g.periodic & 2;
@@ -472,10 +549,10 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
         for (int u = 0; u < 2; u++) {
             const int k = t + u * FT;
             pofs[u] = 0;
-            if (k < NRED) {
-                const int row = k / RP, pc = k - row * RP;
+            if (k < G::NRED) {
+                const int row = k / NQ, qq = k - row * NQ;
                 bool okx, oky;
-                const int sx = axis_src(x0 - 2 + 2 * pc, g.nx, px, &okx);
+                const int sx = axis_src(x0 - XO + 4 * qq, g.nx, px, &okx);
                 const int sy = axis_src(y0 - 2 + row, g.ny, py, &oky);
                 pofs[u] = (okx && oky) ? (sx >> 1) + gc.nx * (sy >> 1) : 0;
             }
@@ -483,56 +560,62 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
     }
     const long long csxy = (long long)gc.nx * gc.ny;
     Acc acc;
-    const int ox = x0 + 2 * tx, oy = y0 + ty;
+    const int ox = x0 + 4 * tx, oy = y0 + ty;
     const bool own_inside = ox < g.nx && oy < g.ny;
-    const int oo = (ty + 2) * RW + XO / 2 + tx;
+    const int oo = (ty + 2) * RW + 2 * (tx + 1);
     const long long og = ox + (long long)g.nx * oy;
-    // registers of plane zA (current) and zA+1 (next): the pre-smoothed
-    // correction of the red-stage pairs, their black member's right-hand
-    // side, the coarse parents, and the own pair's right-hand side of the
-    // next tile plane
-    R2 eov[2], eon[2];
-    VT rbv[2], rbn[2];
-    VTc pcv[2], pcn[2];
-    R2 rov, ron;
-    auto fetch = [&](int zz, int c4, R2* eo, VT* rb, VTc* pc, R2& ro) {
+    // registers of the red-stage quads of the next plane: the pre-smoothed
+    // correction, the right-hand side (for the black cells) and the coarse
+    // parents; and the own quad's right-hand side of the tile plane
+    R4 eov[2], rqv[2];
+    C2 pcv[2];
+    R4 rov, ron;
+    auto stage = [&](int zz, int c4) {
+        bool okz;
+        const long long pl = F.plane(zz, &okz);
+        F.recs(&S.c[c4][0][0], sm, pl, okz);
+        cp_commit();
+    };
+    auto load = [&](int zz) {
         bool okz;
         const int sz = axis_src(zz, g.nz, (g.periodic & 4) != 0, &okz);
         const long long pl = (long long)sz * sxy, cpl = (long long)(sz >> 1) * csxy;
-        F.recs(&S.c[c4][0][0], sm, pl, okz);
-        cp_commit();
 #pragma unroll
         for (int u = 0; u < 2; u++) {
             const bool ok = T.gok[u] && okz;
-            eo[u] = ldg_pair<VT>(e + pl + T.goff[u], ok);
-            rb[u] = ldg_one<VT>(r + pl + T.goff[u] + (1 - T.red(u, zz)), ok);
-            pc[u] = ldg_one<VTc>(ec + cpl + pofs[u], ok);
+            eov[u] = ldg_quad<VT>(e + pl + T.goff[u], ok);
+            rqv[u] = ldg_quad<VT>(r + pl + T.goff[u], ok);
+            pcv[u] = ldg_pair<VTc>(ec + cpl + pofs[u], ok);
         }
-        const int zt = zz - 2;  // tile plane of the next step
-        ro = ldg_pair<VT>(r + og + sxy * zt, own_inside && zt >= z0 && zt < z1);
+        const int zt = zz - 2;  // the tile plane of the step that uses this plane's red stage
+        ron = ldg_quad<VT>(r + og + sxy * zt, own_inside && zt >= z0 && zt < z1);
     };
     auto step = [&](auto ph, int zA) {
         constexpr int P = decltype(ph)::value;
         cp_wait<0>();
         __syncthreads();
-        fetch(zA + 1, (P + 1) & 3, eon, rbn, pcn, ron);
-        // ---- prolongation: plane zA over the 2-halo region
+        stage(zA + 1, (P + 1) & 3);
+        rov = ron;
+        // ---- prolongation: plane zA over the 2-halo rows
         {
             float* EP = &S.ep[P][0][0];
 #pragma unroll
             for (int u = 0; u < 2; u++) {
                 const int o = T.roff[u];
                 if (o < 0) break;
-                const float2 ev = cvt2(eov[u]);
-                const float cv = to_f(pcv[u]);
-                const float rb = sigma * to_f(rbv[u]);
-                const bool m = T.red(u, zA);
-                EP[o] = m ? rb : fmaf(w, cv, ev.x);
-                EP[o + HW] = m ? fmaf(w, cv, ev.y) : rb;
+                const float4 ev = cvt4r<VT>(eov[u]);
+                const float4 rq = cvt4r<VT>(rqv[u]);
+                const float2 cv = cvt2(pcv[u]);
+                const int p = red_half(T.ry[u], zA);
+                const float2 er = p ? make_float2(ev.y, ev.w) : make_float2(ev.x, ev.z);
+                const float2 rb = p ? make_float2(rq.x, rq.z) : make_float2(rq.y, rq.w);
+                *reinterpret_cast<float2*>(EP + o + p * HW) = make_float2(fmaf(w, cv.x, er.x), fmaf(w, cv.y, er.y));
+                *reinterpret_cast<float2*>(EP + o + (1 - p) * HW) = make_float2(sigma * rb.x, sigma * rb.y);
             }
         }
+        load(zA + 1);
         __syncthreads();
-        // ---- black half-step: plane zA-1 over the 1-halo region, in place
+        // ---- black half-step: plane zA-1 over the 1-halo rows, in place
         const int zB = zA - 1;
         if (zB >= z0 - 1) {
             const CT* C = &S.c[(P + 3) & 3][0][0];
@@ -542,12 +625,12 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
             const float* EP = &S.ep[P][0][0];
 #pragma unroll
             for (int u = 0; u < 2; u++) {
-                const int h = T.black(u, zB);
-                if (h < 0) continue;
+                if (T.boff[u] < 0) break;
+                const int h = 1 - red_half(T.by[u], zB);
                 const int o = T.boff[u] + h * HW;
-                float d;
-                const float s = gs_sum<CK>(C, CN, E, EM, EP, o, h, E[o], &d);
-                E[o] = d > 0.f ? __fdividef(s, d) : 0.f;
+                float2 d;
+                const float2 s = gs_sum2<CK>(C, CN, E, EM, EP, o, h, *reinterpret_cast<const float2*>(E + o), &d);
+                *reinterpret_cast<float2*>(E + o) = divide2(s, d);
             }
         }
         __syncthreads();
@@ -559,35 +642,32 @@ __global__ void __launch_bounds__(FT, fused_min_blocks<CK>())
             const float* E = &S.ep[(P + 2) & 3][0][0];
             const float* EM = &S.ep[(P + 1) & 3][0][0];
             const float* EP = &S.ep[(P + 3) & 3][0][0];
-            const int m = (y0 + ty + zC) & 1;  // the pair member of colour 0
-            const float2 rv = cvt2(rov);
-            float d;
-            const float s = gs_sum<CK>(C, CN, E, EM, EP, oo + m * HW, m, sigma * (m ? rv.y : rv.x), &d);
-            const float zr = d > 0.f ? __fdividef(s, d) : 0.f;
-            const float zb = E[oo + (1 - m) * HW];
-            float2 zv = m ? make_float2(zb, zr) : make_float2(zr, zb);
+            const int p = red_half(oy, zC);
+            const float4 rv = cvt4r<VT>(rov);
+            const float2 rr = p ? make_float2(rv.y, rv.w) : make_float2(rv.x, rv.z);
+            float2 d;
+            const float2 s = gs_sum2<CK>(C, CN, E, EM, EP, oo + p * HW, p, make_float2(sigma * rr.x, sigma * rr.y), &d);
+            const float2 zr = divide2(s, d);
+            const float2 zb = *reinterpret_cast<const float2*>(E + oo + (1 - p) * HW);
+            float4 zv = p ? make_float4(zb.x, zr.x, zb.y, zr.y) : make_float4(zr.x, zb.x, zr.y, zb.y);
             if (own_inside) {
                 if (accum) {  // out = accum + z (second W-cycle visit)
-                    const float2 a = ld2<VT>(accum + og + sxy * zC);
-                    zv = make_float2(a.x + zv.x, a.y + zv.y);
+                    const float4 a = cvt4r<VT>(*reinterpret_cast<const R4*>(accum + og + sxy * zC));
+                    zv = make_float4(a.x + zv.x, a.y + zv.y, a.z + zv.z, a.w + zv.w);
                 }
-                st2<VT>(out + og + sxy * zC, zv);
+                st4<VT>(out + og + sxy * zC, zv);
                 if (DOT) {
                     acc.add_prod(rv.x, zv.x * is);
                     acc.add_prod(rv.y, zv.y * is);
+                    acc.add_prod(rv.z, zv.z * is);
+                    acc.add_prod(rv.w, zv.w * is);
                 }
             }
         }
-#pragma unroll
-        for (int u = 0; u < 2; u++) {
-            eov[u] = eon[u];
-            rbv[u] = rbn[u];
-            pcv[u] = pcn[u];
-        }
-        rov = ron;
     };
     const int zs = z0 - 2, zend = z1 + 1;
-    fetch(zs, 0, eov, rbv, pcv, rov);
+    stage(zs, 0);
+    load(zs);
     for (int zA = zs;;) {
         step(Phase<0>{}, zA);
         if (++zA > zend) break;
@@ -685,11 +765,11 @@ enum { O_PRE_F32 = 0, O_PRE_LO, O_PRE_LO_UPD, O_PRE_F32_UPD, O_PRE_COARSE, O_POS
 
 // Even z runs chosen so the grid fills whole waves of resident blocks; each
 // run also computes two planes below and above it.
-Launch fused_launch(const Grid3& g0, int occ_kind) {
+Launch fused_launch(const Grid3& g0, int occ_kind, int fty) {
     Launch P;
     P.g = g0;
-    P.block = dim3(TX, FTY, 1);
-    const int gx = (g0.nx + PX - 1) / PX, gy = (g0.ny + FTY - 1) / FTY, nz = g0.nz;
+    P.block = dim3(QX, fty, 1);
+    const int gx = (g0.nx + PX - 1) / PX, gy = (g0.ny + fty - 1) / fty, nz = g0.nz;
     const int tiles = gx * gy;
     const int cap = (f_sms > 0 ? f_sms : 152) * (f_occ[occ_kind] > 0 ? f_occ[occ_kind] : 1);
     int best_zper = nz + (nz & 1), best_zc = 1;
@@ -728,7 +808,7 @@ bool fused_supported(const Grid3& g) {
 template <int CK, class VT, class VTc, bool UPDATE, bool FINE>
 static void pre_impl(const Grid3& g, const Grid3& gc, const void* sm, const void* rin, const float* q, float* r_out,
                      void* e, void* rc, Scalars* sc, double* partials, int occ_kind, cudaStream_t s) {
-    const Launch P = fused_launch(g, occ_kind);
+    const Launch P = fused_launch(g, occ_kind, GeoOf<CK>::FTY);
     k_presmooth_restrict<CK, VT, VTc, UPDATE, FINE><<<P.grid, P.block, sizeof(PreRing<CK>), s>>>(
         P.g, gc, sm, (const VT*)rin, q, r_out, (VT*)e, (VTc*)rc, sc, partials, P.nblocks);
 }
@@ -736,7 +816,7 @@ template <int CK, class VT, class VTc, bool DOT, bool FINE>
 static void post_impl(const Grid3& g, const Grid3& gc, const void* sm, const void* e, const void* ec, const void* r,
                       void* out, const void* accum, float w, Scalars* sc, double* partials, long long n_active,
                       int occ_kind, cudaStream_t s) {
-    const Launch P = fused_launch(g, occ_kind);
+    const Launch P = fused_launch(g, occ_kind, GeoOf<CK>::FTY);
     k_prolong_postsmooth<CK, VT, VTc, DOT, FINE><<<P.grid, P.block, sizeof(PostRing<CK>), s>>>(
         P.g, gc, sm, (const VT*)e, (const VTc*)ec, (const VT*)r, (VT*)out, (const VT*)accum, w, sc, partials,
         P.nblocks, n_active);
@@ -875,7 +955,7 @@ static cudaError_t prep_pre(int kind) {
     const void* fn = (const void*)k_presmooth_restrict<CK, VT, VTc, UPDATE, FINE>;
     const size_t bytes = sizeof(PreRing<CK>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess && kind >= 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f_occ[kind], fn, FT, bytes);
+    if (e == cudaSuccess && kind >= 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f_occ[kind], fn, GeoOf<CK>::FT, bytes);
     return e;
 }
 template <int CK, class VT, class VTc, bool DOT, bool FINE>
@@ -883,7 +963,7 @@ static cudaError_t prep_post(int kind) {
     const void* fn = (const void*)k_prolong_postsmooth<CK, VT, VTc, DOT, FINE>;
     const size_t bytes = sizeof(PostRing<CK>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-    if (e == cudaSuccess && kind >= 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f_occ[kind], fn, FT, bytes);
+    if (e == cudaSuccess && kind >= 0) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f_occ[kind], fn, GeoOf<CK>::FT, bytes);
     return e;
 }
 
