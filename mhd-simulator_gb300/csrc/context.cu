@@ -1096,7 +1096,8 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
         {"presmooth_restrict", 16.0 + cb + vbc / 8.0, 1, 11},
         // e 4 + coarse e (1/8 cell) + r 4 + coef -> z 4
         {"prolong_postsmooth", 12.0 + cb + vbc / 8.0, 1, 12},
-        {"refinement_residual", 24.0, 0, 7},
+        // b 8 + x 8 (double-FP32 pairs) + coef 16 -> r 4 + e 4
+        {"refinement_residual", 40.0, 0, 7},
         {"coefficients", 29.0, 0, 8},
     };
     const Item* items = ctx->pipelined ? pipelined : classic;

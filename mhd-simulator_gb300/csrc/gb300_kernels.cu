@@ -80,19 +80,26 @@ __global__ void __launch_bounds__(TILE_THREADS) k_coefficients(Grid3 g, int outl
         const int i = cell_index(g, x, y, z);
         const Nbr nb = neighbours(g, x, y, z);
         float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+        // every load first (guarded by the coordinates only), so the cell's
+        // loads are in flight together
         const uint8_t ci = cls[i];
-        if (ci == 1) {
-            const float ai = alpha[i];
-            if (nb.xm >= 0 && cls[nb.xm] == 1) c.x = beta_of(alpha[nb.xm], ai, rho_l, rho_air);
-            if (nb.ym >= 0 && cls[nb.ym] == 1) c.y = beta_of(alpha[nb.ym], ai, rho_l, rho_air);
-            if (nb.zm >= 0 && cls[nb.zm] == 1) c.z = beta_of(alpha[nb.zm], ai, rho_l, rho_air);
-            float r = 0.0f;
-            const int order[6] = {nb.xm, nb.xp, nb.ym, nb.yp, nb.zm, nb.zp};
+        const float ai = alpha[i];
+        const int order[6] = {nb.xm, nb.xp, nb.ym, nb.yp, nb.zm, nb.zp};
+        uint8_t cn[6];
+        float an[6];
 #pragma unroll
-            for (int k = 0; k < 6; k++) {
-                const int j = order[k];
-                if (j >= 0 && cls[j] == 2) r = __fadd_rn(r, beta_of(ai, alpha[j], rho_l, rho_air));
-            }
+        for (int k = 0; k < 6; k++) {
+            cn[k] = order[k] >= 0 ? cls[order[k]] : (uint8_t)0;
+            an[k] = order[k] >= 0 ? alpha[order[k]] : 0.0f;
+        }
+        if (ci == 1) {
+            if (cn[0] == 1) c.x = beta_of(an[0], ai, rho_l, rho_air);
+            if (cn[2] == 1) c.y = beta_of(an[2], ai, rho_l, rho_air);
+            if (cn[4] == 1) c.z = beta_of(an[4], ai, rho_l, rho_air);
+            float r = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 6; k++)
+                if (cn[k] == 2) r = __fadd_rn(r, beta_of(ai, an[k], rho_l, rho_air));
             if (outlet && z == g.nz - 1) {
                 const float gt = outlet_conductance(ai, rho_l, rho_air);
                 r = __fadd_rn(r, gt);
@@ -127,28 +134,24 @@ __global__ void __launch_bounds__(TILE_THREADS) k_rhs(Grid3 g, int outlet, float
         if (!in_xy) continue;
         const int i = cell_index(g, x, y, z);
         df bi = {0.0f, 0.0f};
-        if (cls[i] == 1) {
-            const Nbr nb = neighbours(g, x, y, z);
+        // every load first (face indices are always valid), then the sums
+        const Nbr nb = neighbours(g, x, y, z);
+        const uint8_t ci = cls[i];
+        const uint8_t cxm = nb.xm >= 0 ? cls[nb.xm] : 0, cxp = nb.xp >= 0 ? cls[nb.xp] : 0;
+        const uint8_t cym = nb.ym >= 0 ? cls[nb.ym] : 0, cyp = nb.yp >= 0 ? cls[nb.yp] : 0;
+        const uint8_t czm = nb.zm >= 0 ? cls[nb.zm] : 0, czp = nb.zp >= 0 ? cls[nb.zp] : 0;
+        const int hx = (x + 1 == nx && (g.periodic & 1)) ? 0 : x + 1;
+        const int hy = (y + 1 == ny && (g.periodic & 2)) ? 0 : y + 1;
+        const int hz = (z + 1 == nz && (g.periodic & 4)) ? 0 : z + 1;
+        const float ulo = u[x + (nx + 1) * (y + ny * z)], uhi = u[hx + (nx + 1) * (y + ny * z)];
+        const float vlo = v[x + nx * (y + (ny + 1) * z)], vhi = v[x + nx * (hy + (ny + 1) * z)];
+        const float wlo = w[x + nx * (y + ny * z)], whi = w[x + nx * (y + ny * hz)];
+        if (ci == 1) {
             df sum = {0.0f, 0.0f};
-            {
-                const int hx = (x + 1 == nx && (g.periodic & 1)) ? 0 : x + 1;
-                const float lo = (nb.xm >= 0 && cls[nb.xm] != 0) ? u[x + (nx + 1) * (y + ny * z)] : 0.0f;
-                const float hi = (nb.xp >= 0 && cls[nb.xp] != 0) ? u[hx + (nx + 1) * (y + ny * z)] : 0.0f;
-                sum = df_add(sum, two_sum(hi, -lo));
-            }
-            {
-                const int hy = (y + 1 == ny && (g.periodic & 2)) ? 0 : y + 1;
-                const float lo = (nb.ym >= 0 && cls[nb.ym] != 0) ? v[x + nx * (y + (ny + 1) * z)] : 0.0f;
-                const float hi = (nb.yp >= 0 && cls[nb.yp] != 0) ? v[x + nx * (hy + (ny + 1) * z)] : 0.0f;
-                sum = df_add(sum, two_sum(hi, -lo));
-            }
-            {
-                const int hz = (z + 1 == nz && (g.periodic & 4)) ? 0 : z + 1;
-                const float lo = (nb.zm >= 0 && cls[nb.zm] != 0) ? w[x + nx * (y + ny * z)] : 0.0f;
-                const bool hopen = (nb.zp >= 0 && cls[nb.zp] != 0) || (nb.zp < 0 && outlet && z + 1 == nz);
-                const float hi = hopen ? w[x + nx * (y + ny * hz)] : 0.0f;
-                sum = df_add(sum, two_sum(hi, -lo));
-            }
+            sum = df_add(sum, two_sum(cxp != 0 ? uhi : 0.0f, -(cxm != 0 ? ulo : 0.0f)));
+            sum = df_add(sum, two_sum(cyp != 0 ? vhi : 0.0f, -(cym != 0 ? vlo : 0.0f)));
+            const bool hopen = (nb.zp >= 0 && czp != 0) || (nb.zp < 0 && outlet && z + 1 == nz);
+            sum = df_add(sum, two_sum(hopen ? whi : 0.0f, -(czm != 0 ? wlo : 0.0f)));
             bi = df_mul_f(sum, -h);
         }
         b_hi[i] = bi.hi;
@@ -203,23 +206,26 @@ __device__ __forceinline__ T apply_cell(const Grid3& g, const float4* __restrict
 }
 
 // ------------------------------------------------- refinement residual
-// (A x)_i in double-FP32 from a double-FP32 x and the FP32 mobilities.
-__device__ __forceinline__ df apply_cell_df(const float4* __restrict__ coef, const float* __restrict__ xh,
-                                            const float* __restrict__ xl, int i, const Nbr& nb) {
-    const float4 c = coef[i];
-    const df xi = {xh[i], xl[i]};
-    df acc = df_mul_f(xi, c.w);
-    if (c.x != 0.f) acc = df_add(acc, df_mul_f(df_sub(xi, df{xh[nb.xm], xl[nb.xm]}), c.x));
-    if (c.y != 0.f) acc = df_add(acc, df_mul_f(df_sub(xi, df{xh[nb.ym], xl[nb.ym]}), c.y));
-    if (c.z != 0.f) acc = df_add(acc, df_mul_f(df_sub(xi, df{xh[nb.zm], xl[nb.zm]}), c.z));
-    if (nb.xp >= 0) { const float bh = coef[nb.xp].x; if (bh != 0.f) acc = df_add(acc, df_mul_f(df_sub(xi, df{xh[nb.xp], xl[nb.xp]}), bh)); }
-    if (nb.yp >= 0) { const float bh = coef[nb.yp].y; if (bh != 0.f) acc = df_add(acc, df_mul_f(df_sub(xi, df{xh[nb.yp], xl[nb.yp]}), bh)); }
-    if (nb.zp >= 0) { const float bh = coef[nb.zp].z; if (bh != 0.f) acc = df_add(acc, df_mul_f(df_sub(xi, df{xh[nb.zp], xl[nb.zp]}), bh)); }
-    return acc;
+// x_i - x_j in double-FP32, left unnormalised: TwoSum of the high parts, the
+// low parts' difference added to its error.
+__device__ __forceinline__ df df_diff_lazy(df a, df b) {
+    const df s = two_sum(a.hi, -b.hi);
+    return {s.hi, __fadd_rn(s.lo, __fsub_rn(a.lo, b.lo))};
+}
+// acc += beta * d: the high product exact (FMA TwoProduct), added by TwoSum;
+// the low terms gathered in acc.lo (renormalised once at the end).
+__device__ __forceinline__ void df_acc_prod(df& acc, df d, float beta) {
+    const float p = __fmul_rn(d.hi, beta);
+    const float pl = __fmaf_rn(d.lo, beta, __fmaf_rn(d.hi, beta, -p));
+    const df s = two_sum(acc.hi, p);
+    acc = {s.hi, __fadd_rn(acc.lo, __fadd_rn(s.lo, pl))};
 }
 
 // r = b - A x in double-FP32 (x a double-FP32 pair), stored FP32 for the
-// inner solve; e = 0.
+// inner solve; e = 0.  Every load of a cell is issued before its arithmetic
+// (an absent neighbour sits behind a zero mobility and reads as x_i), and
+// the seven terms are gathered with lazy double-FP32 sums (about 2^-44
+// relative to the largest term).
 __global__ void __launch_bounds__(TILE_THREADS) k_residual(Grid3 g, const float4* __restrict__ coef,
                                                            const float* __restrict__ b_hi,
                                                            const float* __restrict__ b_lo,
@@ -233,7 +239,24 @@ __global__ void __launch_bounds__(TILE_THREADS) k_residual(Grid3 g, const float4
         if (!in_xy) continue;
         const int i = cell_index(g, x, y, z);
         const Nbr nb = neighbours(g, x, y, z);
-        const df res = df_sub(df{b_hi[i], b_lo[i]}, apply_cell_df(coef, x_hi, x_lo, i, nb));
+        const float4 c = coef[i];
+        const float bxp = nb.xp >= 0 ? coef[nb.xp].x : 0.f;
+        const float byp = nb.yp >= 0 ? coef[nb.yp].y : 0.f;
+        const float bzp = nb.zp >= 0 ? coef[nb.zp].z : 0.f;
+        const df xi = {x_hi[i], x_lo[i]};
+        auto ld = [&](int j) { return j >= 0 ? df{x_hi[j], x_lo[j]} : xi; };
+        const df xxm = ld(nb.xm), xxp = ld(nb.xp), xym = ld(nb.ym), xyp = ld(nb.yp), xzm = ld(nb.zm), xzp = ld(nb.zp);
+        const df bi = {b_hi[i], b_lo[i]};
+        df ax;
+        ax.hi = __fmul_rn(xi.hi, c.w);
+        ax.lo = __fmaf_rn(xi.lo, c.w, __fmaf_rn(xi.hi, c.w, -ax.hi));
+        df_acc_prod(ax, df_diff_lazy(xi, xxm), c.x);
+        df_acc_prod(ax, df_diff_lazy(xi, xym), c.y);
+        df_acc_prod(ax, df_diff_lazy(xi, xzm), c.z);
+        df_acc_prod(ax, df_diff_lazy(xi, xxp), bxp);
+        df_acc_prod(ax, df_diff_lazy(xi, xyp), byp);
+        df_acc_prod(ax, df_diff_lazy(xi, xzp), bzp);
+        const df res = df_sub(bi, fast_two_sum(ax.hi, ax.lo));
         const float ri = df_to_f(res);
         r[i] = ri;
         e[i] = 0.0f;
@@ -548,13 +571,23 @@ __global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, f
         if (!in_xy) continue;
         const int i = cell_index(g, x, y, z);
         const Nbr nb = neighbours(g, x, y, z);
+        // every load first (guarded by the coordinates only), then the faces
         const uint8_t ci = cls[i];
         const df pi = {ph[i], pl[i]};
+        const float ai = alpha[i];
+        const uint8_t cxm = nb.xm >= 0 ? cls[nb.xm] : 0, cym = nb.ym >= 0 ? cls[nb.ym] : 0;
+        const uint8_t czm = nb.zm >= 0 ? cls[nb.zm] : 0;
+        const float axm = nb.xm >= 0 ? alpha[nb.xm] : 0.f, aym = nb.ym >= 0 ? alpha[nb.ym] : 0.f;
+        const float azm = nb.zm >= 0 ? alpha[nb.zm] : 0.f;
+        const df pxm = nb.xm >= 0 ? df{ph[nb.xm], pl[nb.xm]} : pi, pym = nb.ym >= 0 ? df{ph[nb.ym], pl[nb.ym]} : pi;
+        const df pzm = nb.zm >= 0 ? df{ph[nb.zm], pl[nb.zm]} : pi;
+        const float uin = us[x + (nx + 1) * (y + ny * z)], vin = vs[x + nx * (y + (ny + 1) * z)];
+        const float win = ws[x + nx * (y + ny * z)];
         {
             const int f = x + (nx + 1) * (y + ny * z);
             float out = 0.0f;
-            if (nb.xm >= 0 && ci != 0 && cls[nb.xm] != 0)
-                out = us[f] - grad_term(beta_of(alpha[nb.xm], alpha[i], rho_l, rho_air), pi, df{ph[nb.xm], pl[nb.xm]}, inv_h);
+            if (nb.xm >= 0 && ci != 0 && cxm != 0)
+                out = uin - grad_term(beta_of(axm, ai, rho_l, rho_air), pi, pxm, inv_h);
             uo[f] = out;
             if (x == 0 && (g.periodic & 1)) uo[nx + (nx + 1) * (y + ny * z)] = out;
             if (x == nx - 1 && !(g.periodic & 1)) uo[nx + (nx + 1) * (y + ny * z)] = 0.0f;
@@ -562,8 +595,8 @@ __global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, f
         {
             const int f = x + nx * (y + (ny + 1) * z);
             float out = 0.0f;
-            if (nb.ym >= 0 && ci != 0 && cls[nb.ym] != 0)
-                out = vs[f] - grad_term(beta_of(alpha[nb.ym], alpha[i], rho_l, rho_air), pi, df{ph[nb.ym], pl[nb.ym]}, inv_h);
+            if (nb.ym >= 0 && ci != 0 && cym != 0)
+                out = vin - grad_term(beta_of(aym, ai, rho_l, rho_air), pi, pym, inv_h);
             vo[f] = out;
             if (y == 0 && (g.periodic & 2)) vo[x + nx * (ny + (ny + 1) * z)] = out;
             if (y == ny - 1 && !(g.periodic & 2)) vo[x + nx * (ny + (ny + 1) * z)] = 0.0f;
@@ -571,8 +604,8 @@ __global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, f
         {
             const int f = x + nx * (y + ny * z);
             float out = 0.0f;
-            if (nb.zm >= 0 && ci != 0 && cls[nb.zm] != 0)
-                out = ws[f] - grad_term(beta_of(alpha[nb.zm], alpha[i], rho_l, rho_air), pi, df{ph[nb.zm], pl[nb.zm]}, inv_h);
+            if (nb.zm >= 0 && ci != 0 && czm != 0)
+                out = win - grad_term(beta_of(azm, ai, rho_l, rho_air), pi, pzm, inv_h);
             wo[f] = out;
             const int ft = x + nx * (y + ny * nz);
             if (z == 0 && (g.periodic & 4)) wo[ft] = out;
