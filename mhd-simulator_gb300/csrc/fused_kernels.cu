@@ -764,7 +764,8 @@ int f_occ[12] = {};
 enum { O_PRE_F32 = 0, O_PRE_LO, O_PRE_LO_UPD, O_PRE_F32_UPD, O_PRE_COARSE, O_POST_F32, O_POST_LO, O_POST_COARSE };
 
 // Even z runs chosen so the grid fills whole waves of resident blocks; each
-// run also computes two planes below and above it.
+// run also computes two planes below and above it.  On levels too small to
+// fill one wave the score favours the shortest runs (fewest steps per block).
 Launch fused_launch(const Grid3& g0, int occ_kind, int fty) {
     Launch P;
     P.g = g0;
@@ -777,7 +778,7 @@ Launch fused_launch(const Grid3& g0, int occ_kind, int fty) {
     for (int zc = 1; zc <= nz; zc++) {
         int zper = (nz + zc - 1) / zc;
         if (zper & 1) zper++;
-        if (zper < 4 && zc > 1) break;
+        if (zper < 2 && zc > 1) break;
         const int zcr = (nz + zper - 1) / zper;
         const long long blocks = (long long)tiles * zcr;
         if (blocks > MAX_REDUCE_BLOCKS) break;

@@ -383,43 +383,51 @@ __global__ void __launch_bounds__(256) k_coarse_invert(Grid3 g, const float4* __
     }
     __syncthreads();
     // Cholesky, lower triangle in place (a non-positive pivot is treated as
-    // an empty row)
+    // an empty row).  FP64 divisions and square roots are long dependent
+    // sequences on this part, so each pivot takes one reciprocal square root
+    // (rsq[j] = 1 / L_jj, an FP32 seed refined by two Newton-Raphson steps
+    // r <- r (3 - a r^2) / 2 in FP64) and the column is scaled by it.
+    __shared__ double rsq[64];
     const int tx = t & 15, ty = t >> 4;
     for (int j = 0; j < m; j++) {
         if (t == 0) {
             const double piv = A[j * m + j];
-            A[j * m + j] = piv > 1e-300 ? sqrt(piv) : 0.0;
+            double r = 0.0;
+            if (piv > 1e-30 && piv < 1e30) {
+                r = (double)rsqrtf((float)piv);
+                r = r * (1.5 - 0.5 * piv * r * r);
+                r = r * (1.5 - 0.5 * piv * r * r);
+            } else if (piv > 1e-300) {
+                r = 1.0 / sqrt(piv);
+            }
+            A[j * m + j] = piv * r;  // L_jj (0 for an empty row)
+            rsq[j] = r;
         }
         __syncthreads();
-        const double ljj = A[j * m + j];
-        for (int i = j + 1 + t; i < m; i += nt) A[i * m + j] = ljj > 0.0 ? A[i * m + j] / ljj : 0.0;
+        const double rj = rsq[j];
+        for (int i = j + 1 + t; i < m; i += nt) A[i * m + j] *= rj;
         __syncthreads();
         for (int i = j + 1 + ty; i < m; i += 16)
             for (int k = j + 1 + tx; k <= i; k += 16) A[i * m + k] -= A[i * m + j] * A[k * m + j];
         __syncthreads();
     }
-    // L y = e_b, then L^T x = y (one warp; rows in order)
-    if (t < 32) {
-        for (int i = 0; i < m; i++) {
-            double s = 0.0;
-            for (int k = t; k < i; k += 32) s += A[i * m + k] * v[k];
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if (t == 0) {
-                const double lii = A[i * m + i];
-                v[i] = lii > 0.0 ? ((i == b ? 1.0 : 0.0) - s) / lii : 0.0;
-            }
-            __syncwarp();
-        }
-        for (int i = m - 1; i >= 0; i--) {
-            double s = 0.0;
-            for (int k = i + 1 + t; k < m; k += 32) s += A[k * m + i] * v[k];
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if (t == 0) {
-                const double lii = A[i * m + i];
-                v[i] = lii > 0.0 ? (v[i] - s) / lii : 0.0;
-            }
-            __syncwarp();
-        }
+    // L y = e_b, then L^T x = y, column-oriented: thread i keeps v[i]; step j
+    // finishes v[j] and updates the rows after it (before it, going back).
+    if (t < m) v[t] = t == b ? 1.0 : 0.0;
+    __syncthreads();
+    for (int j = 0; j < m; j++) {
+        const double yj = v[j] * rsq[j];
+        __syncthreads();
+        if (t == j) v[j] = yj;
+        else if (t > j && t < m) v[t] -= A[t * m + j] * yj;
+        __syncthreads();
+    }
+    for (int j = m - 1; j >= 0; j--) {
+        const double xj = v[j] * rsq[j];
+        __syncthreads();
+        if (t == j) v[j] = xj;
+        else if (t < j) v[t] -= A[j * m + t] * xj;
+        __syncthreads();
     }
     __syncthreads();
     for (int i = t; i < m; i += nt)
