@@ -170,7 +170,10 @@ class CpuReference:
         self.np, self.oracle, self.threads = np, oracle, threads
         nx, ny, nz = case["dims"]
         mask01 = (case["solid"].reshape(-1) == 0).astype(np.uint32)
+        t0 = time.perf_counter()
         self.comps, self.mask = oracle.anchors(mask01, (nx, ny, nz), 0)
+        # the reference's host breadth-first search (anchors), one thread
+        self.anchors_s = time.perf_counter() - t0
         fluid = int((self.mask != 0).sum())
         self.params = oracle.make_params((nx, ny, nz), case["h"], case["dt"], case["rho_liquid"], case["rho_air"],
                                          True, 0, tol, 0.0, fluid)
@@ -351,6 +354,12 @@ def run_ours(args):
                             "algorithmic_bytes_per_launch": best["bytes"]}
         line["kernels"] = [{"name": k["name"], "us": k["ms"] * 1e3, "GBps": k["bytes"] / (k["ms"] * 1e-3) / 1e9,
                             "per_iteration": k["per_iteration"]} for k in prof]
+        # gauge/topology labelling of the solid mask on the GPU (union-find,
+        # four kernels), run when the mask changes
+        topo = next((k for k in prof if k["name"] == "topology"), None)
+        if topo is not None:
+            line["topology"] = {"gpu_us": topo["ms"] * 1e3, "GBps": topo["bytes"] / (topo["ms"] * 1e-3) / 1e9,
+                                "bytes_per_cell": topo["bytes"] / (nx * ny * nz)}
         # the reference algorithm on this GPU: the bit-exact CUDA port of its
         # FP32 multigrid CG (closed boundaries), for the algorithmic gap
         try:
@@ -376,6 +385,9 @@ def run_ours(args):
         k_ref = reference_iterations(args.workload, args.tol)
         cref = CpuReference(case, threads, args.tol)
         setup, per_it, _ = cref.calibrate()
+        if "topology" in line:
+            line["topology"]["host_search_ms"] = cref.anchors_s * 1e3
+            line["topology"]["host_search"] = "the reference's anchors() breadth-first search (oracle), 1 thread"
         if k_ref is not None:
             line["cpu_baseline"] = {
                 "value": 1.0 / (setup + per_it * k_ref), "unit": UNIT, "cores": threads, "kind": "port",

@@ -44,9 +44,11 @@ struct mhdproj_ctx {
     uint8_t* d_cls = nullptr;
     int* d_flag = nullptr;
     int* h_flag = nullptr;
-    std::vector<uint8_t> h_solid;
-    std::vector<uint8_t> h_cls;
-    std::vector<uint32_t> h_mask;
+    // connected-component labels (u32 per cell), top-layer marks, counts
+    uint32_t* d_labels = nullptr;
+    uint8_t* d_topflag = nullptr;
+    TopoCounts* d_topo = nullptr;
+    TopoCounts* h_topo = nullptr;
     uint32_t components = 0, pinned = 0;
     long long n_active = 0;
     bool have_topology = false, have_coef = false;
@@ -326,7 +328,8 @@ extern "C" int mhdproj_create(const mhdproj_grid* grid, const mhdproj_options* o
         fail(ctx, MHDPROJ_ERR_CUDA, "cudaEventCreate failed");
         return bad(MHDPROJ_ERR_CUDA);
     }
-    if (cudaMallocHost(&ctx->h_sc, sizeof(Scalars)) != cudaSuccess || cudaMallocHost(&ctx->h_flag, sizeof(int)) != cudaSuccess) {
+    if (cudaMallocHost(&ctx->h_sc, sizeof(Scalars)) != cudaSuccess || cudaMallocHost(&ctx->h_flag, sizeof(int)) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_topo, sizeof(TopoCounts)) != cudaSuccess) {
         fail(ctx, MHDPROJ_ERR_CUDA, "cudaMallocHost failed");
         return bad(MHDPROJ_ERR_CUDA);
     }
@@ -337,6 +340,9 @@ extern "C" int mhdproj_create(const mhdproj_grid* grid, const mhdproj_options* o
              CK(dalloc(ctx, &ctx->d_solid_prev, n));
              CK(dalloc(ctx, &ctx->d_cls, n));
              CK(dalloc(ctx, &ctx->d_flag, sizeof(int)));
+             CK(dalloc(ctx, &ctx->d_labels, n * 4));
+             CK(dalloc(ctx, &ctx->d_topo, sizeof(TopoCounts)));
+             if (ctx->outlet && !(grid->periodic & 4)) CK(dalloc(ctx, &ctx->d_topflag, n));
              CK(dalloc(ctx, &ctx->sc, sizeof(Scalars)));
              CK(dalloc(ctx, &ctx->partials, sizeof(double) * 4 * MAX_REDUCE_BLOCKS));
              if (ctx->opt.solver == MHDPROJ_SOLVER_REFERENCE) {
@@ -394,6 +400,7 @@ extern "C" void mhdproj_destroy(mhdproj_ctx* ctx) {
     for (float* p : ctx->c_checkpoints) cudaFree(p);
     if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
     if (ctx->h_flag) cudaFreeHost(ctx->h_flag);
+    if (ctx->h_topo) cudaFreeHost(ctx->h_topo);
     if (ctx->ev_a) cudaEventDestroy(ctx->ev_a);
     if (ctx->ev_b) cudaEventDestroy(ctx->ev_b);
     if (ctx->ev_sync) cudaEventDestroy(ctx->ev_sync);
@@ -434,30 +441,28 @@ static int update_topology(mhdproj_ctx* ctx, const uint8_t* solid, bool* changed
     }
     if (!*changed) return 0;
     CK(cudaMemcpyAsync(ctx->d_solid_prev, solid, ctx->n, cudaMemcpyDeviceToDevice, ctx->stream));
-    ctx->h_solid.resize(ctx->n);
-    CK(cudaMemcpyAsync(ctx->h_solid.data(), solid, ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+    // Components, gauge cells and counts on the GPU; only the counts come back.
+    uint32_t* mask = ctx->ref ? ref_mask(ctx->ref) : nullptr;
+    ctx->launches += (uint64_t)launch_topology(solid, (int)ctx->grid.nx, (int)ctx->grid.ny, (int)ctx->grid.nz,
+                                               (int)ctx->grid.periodic, ctx->ref ? 0 : ctx->outlet, ctx->d_labels,
+                                               ctx->d_topflag, mask, ctx->ref ? nullptr : ctx->d_cls, ctx->d_topo,
+                                               ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ctx->h_topo, ctx->d_topo, sizeof(TopoCounts), cudaMemcpyDeviceToHost, ctx->stream));
     int rc = wait_stream(ctx);
     if (rc) return rc;
-    const uint32_t dims[3] = {ctx->grid.nx, ctx->grid.ny, ctx->grid.nz};
-    if (ctx->opt.solver == MHDPROJ_SOLVER_REFERENCE) {
-        ctx->h_mask.resize(ctx->n);
-        for (long long i = 0; i < ctx->n; i++) ctx->h_mask[i] = ctx->h_solid[i] ? 0u : 1u;
-        ctx->components = host_anchors(ctx->h_mask.data(), dims, ctx->grid.periodic);
-        long long nf = 0;
-        for (long long i = 0; i < ctx->n; i++) nf += ctx->h_mask[i] != 0;
-        ctx->n_active = nf;
-        rc = ref_set_topology(ctx->ref, ctx->h_mask.data(), ctx->components, ctx->err);
-        if (rc) return rc;
+    const TopoCounts t = *ctx->h_topo;
+    if (t.error) {
+        ctx->have_topology = false;
+        return fail(ctx, MHDPROJ_ERR_CUDA, "connected-component labelling exceeded its step bound");
+    }
+    ctx->components = (uint32_t)t.components;
+    if (ctx->ref) {
+        ctx->n_active = (long long)t.fluid;
+        ref_set_topology_device(ctx->ref, ctx->components, (uint32_t)t.fluid);
     } else {
-        ctx->h_cls.resize(ctx->n);
-        ctx->pinned = host_classify(ctx->h_solid.data(), dims, ctx->grid.periodic, ctx->outlet, ctx->h_cls.data(),
-                                    &ctx->components);
-        long long na = 0;
-        for (long long i = 0; i < ctx->n; i++) na += ctx->h_cls[i] == 1;
-        ctx->n_active = na;
-        CK(cudaMemcpyAsync(ctx->d_cls, ctx->h_cls.data(), ctx->n, cudaMemcpyHostToDevice, ctx->stream));
-        rc = wait_stream(ctx);
-        if (rc) return rc;
+        ctx->pinned = (uint32_t)t.pinned;
+        ctx->n_active = (long long)t.active;
     }
     ctx->have_topology = true;
     return 0;
@@ -1050,10 +1055,17 @@ extern "C" int mhdproj_copy_topology(mhdproj_ctx* ctx, uint32_t* mask_host, uint
     if (!ctx) return MHDPROJ_ERR_INVALID;
     if (!ctx->have_topology) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients first");
     if (mask_host) {
-        if (ctx->ref)
-            for (long long i = 0; i < ctx->n; i++) mask_host[i] = ctx->h_mask[i];
-        else
-            for (long long i = 0; i < ctx->n; i++) mask_host[i] = ctx->h_cls[i];
+        if (ctx->ref) {
+            CK(cudaMemcpyAsync(mask_host, ref_mask(ctx->ref), ctx->n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        } else {
+            std::vector<uint8_t> cls(ctx->n);
+            CK(cudaMemcpyAsync(cls.data(), ctx->d_cls, ctx->n, cudaMemcpyDeviceToHost, ctx->stream));
+            int rc = wait_stream(ctx);
+            if (rc) return rc;
+            for (long long i = 0; i < ctx->n; i++) mask_host[i] = cls[i];
+        }
+        int rc = wait_stream(ctx);
+        if (rc) return rc;
     }
     if (components) *components = ctx->components;
     return 0;
@@ -1078,6 +1090,12 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
     // Algorithmic bytes per cell: the compulsory traffic of each kernel's
     // fields, every field touched once per launch.
     const double vbc = ctx->opt.precision == 0 ? 4.0 : 2.0;   // level-1 vector bytes per cell
+    // Connected-component labelling of the solid mask, by kernel: run starts
+    // (solid 1 -> label 4), links (solid 1), roots (solid 1 + label 4 ->
+    // label 4), classes (solid 1 + label 4 -> class 1); with an outlet the
+    // top marks (clear 1, read 1).
+    const bool top_open = ctx->outlet && !(ctx->grid.periodic & 4);
+    const double topo_bytes = 21.0 + (top_open ? 2.0 : 0.0);
     const Item classic[] = {
         {"spmv_dot", 20.0, 1, 0},             // p 4 + beta 12 -> q 4
         {"update_norm", 24.0, 1, 1},          // e, p, r, q 16 -> e, r 8
@@ -1088,6 +1106,7 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
         {"search", 12.0, 1, 6},
         {"refinement_residual", 24.0, 0, 7},  // x 4 + beta 12 + b 4 -> r 4 (survey K7)
         {"coefficients", 29.0, 0, 8},         // alpha 4 + solid 1 -> 16 + 8 (survey K0)
+        {"topology", topo_bytes, 0, 9},
     };
     const Item pipelined[] = {
         // z 4 + p_old 4 + coef 16 + x 4 -> p 4 + x 4 + q 4
@@ -1099,6 +1118,7 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
         // b 8 + x 8 (double-FP32 pairs) + coef 16 -> r 4 + e 4
         {"refinement_residual", 40.0, 0, 7},
         {"coefficients", 29.0, 0, 8},
+        {"topology", topo_bytes, 0, 9},
     };
     const Item* items = ctx->pipelined ? pipelined : classic;
     const int n_items = ctx->pipelined ? (int)(sizeof pipelined / sizeof pipelined[0])
@@ -1125,6 +1145,12 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
                 case 6: launch_search(ctx->L, F, s); break;
                 case 7: launch_residual(ctx->L, F, ctx->phi_hi, ctx->phi_lo, s); break;
                 case 8: launch_coefficients(ctx->L, F, s); break;
+                case 9:
+                    // relabels the current mask: the same classes are rewritten
+                    launch_topology(ctx->d_solid_prev, (int)ctx->grid.nx, (int)ctx->grid.ny, (int)ctx->grid.nz,
+                                    (int)ctx->grid.periodic, ctx->outlet, ctx->d_labels, ctx->d_topflag, nullptr,
+                                    ctx->d_cls, ctx->d_topo, s);
+                    break;
                 case 10:
                     launch_search_spmv(ctx->L, ctx->coef, ctx->z, ctx->p, ctx->p1, ctx->e, ctx->q, ctx->sc,
                                        ctx->partials, 1, s);

@@ -163,4 +163,21 @@ void launch_accumulate_pipelined(const Launch& L, float* x_hi, float* x_lo, cons
                                  const float* p1, const Scalars* sc, cudaStream_t s);
 cudaError_t mg_prepare_attributes();
 
+// ---- connected components of the non-solid cells (topology_kernels.cu)
+struct TopoCounts {
+    unsigned long long components;  // roots (one per component)
+    unsigned long long fluid;       // non-solid cells
+    unsigned long long pinned;      // gauge cells (classes only)
+    unsigned long long active;      // non-solid, non-gauge cells (classes only)
+    int error;                      // a label walk or link hit its bound
+    int pad;
+};
+// labels: u32[n] scratch.  mask_out (optional): the reference's encoding
+// (0 solid, 1 | root << 2, 2 | root << 2).  cls_out (optional): 0 solid,
+// 1 active, 2 pinned gauge cell, where components that reach the top z-layer
+// need no gauge when `outlet` is set on a non-periodic z axis; topflag: u8[n]
+// scratch for that case.  Requires n < 2^31.  Returns the kernels launched.
+int launch_topology(const uint8_t* solid, int nx, int ny, int nz, int periodic, int outlet, uint32_t* labels,
+                    uint8_t* topflag, uint32_t* mask_out, uint8_t* cls_out, TopoCounts* counts, cudaStream_t s);
+
 }  // namespace mhdproj

@@ -12,6 +12,10 @@ int ref_create(RefState** out, const mhdproj_grid* grid, const mhdproj_options* 
 void ref_destroy(RefState* s);
 void ref_set_stream(RefState* s, cudaStream_t stream);
 int ref_set_topology(RefState* s, const uint32_t* mask_host, uint32_t components, std::string& err);
+// The encoded mask in device memory (written by the GPU labelling), and the
+// counts that go with it.
+uint32_t* ref_mask(RefState* s);
+void ref_set_topology_device(RefState* s, uint32_t components, uint32_t fluid_cells);
 int ref_set_coefficients(RefState* s, const float* alpha, float rho_l, float rho_air, std::string& err);
 int ref_set_phase_drag(RefState* s, const float* phase, float drag_rate, float dt, std::string& err);
 int ref_project(RefState* s, const float* us, const float* vs, const float* ws, float* uo, float* vo, float* wo,

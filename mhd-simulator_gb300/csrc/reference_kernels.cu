@@ -1002,6 +1002,14 @@ int ref_set_topology(RefState* s, const uint32_t* mask_host, uint32_t components
     return 0;
 }
 
+uint32_t* ref_mask(RefState* s) { return s->mask; }
+
+void ref_set_topology_device(RefState* s, uint32_t components, uint32_t fluid_cells) {
+    s->fluid_cells = fluid_cells;
+    s->components = components;
+    s->have_topology = true;
+}
+
 int ref_set_phase_drag(RefState* s, const float* phase, float drag_rate, float dt, std::string& err) {
     if (!phase) {
         s->drag = false;

@@ -24,7 +24,8 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler"
 # exactly: no fused multiply-adds.
 EXACT = {"reference_kernels.cu"}
 
-SOURCES = ["context.cu", "gb300_kernels.cu", "fine_kernels.cu", "fused_kernels.cu", "mg_kernels.cu", "reference_kernels.cu", "noalloc.cu"]
+SOURCES = ["context.cu", "gb300_kernels.cu", "fine_kernels.cu", "fused_kernels.cu", "mg_kernels.cu", "reference_kernels.cu", "noalloc.cu",
+           "topology_kernels.cu"]
 HOST_SOURCES = ["topology.cpp"]
 
 
