@@ -46,6 +46,7 @@ struct mhdproj_ctx {
     int* h_flag = nullptr;
     // connected-component labels (u32 per cell), top-layer marks, counts
     uint32_t* d_labels = nullptr;
+    uint32_t* d_roots = nullptr;
     uint8_t* d_topflag = nullptr;
     TopoCounts* d_topo = nullptr;
     TopoCounts* h_topo = nullptr;
@@ -341,6 +342,7 @@ extern "C" int mhdproj_create(const mhdproj_grid* grid, const mhdproj_options* o
              CK(dalloc(ctx, &ctx->d_cls, n));
              CK(dalloc(ctx, &ctx->d_flag, sizeof(int)));
              CK(dalloc(ctx, &ctx->d_labels, n * 4));
+             CK(dalloc(ctx, &ctx->d_roots, (n + 1) / 2 * 4));
              CK(dalloc(ctx, &ctx->d_topo, sizeof(TopoCounts)));
              if (ctx->outlet && !(grid->periodic & 4)) CK(dalloc(ctx, &ctx->d_topflag, n));
              CK(dalloc(ctx, &ctx->sc, sizeof(Scalars)));
@@ -445,8 +447,8 @@ static int update_topology(mhdproj_ctx* ctx, const uint8_t* solid, bool* changed
     uint32_t* mask = ctx->ref ? ref_mask(ctx->ref) : nullptr;
     ctx->launches += (uint64_t)launch_topology(solid, (int)ctx->grid.nx, (int)ctx->grid.ny, (int)ctx->grid.nz,
                                                (int)ctx->grid.periodic, ctx->ref ? 0 : ctx->outlet, ctx->d_labels,
-                                               ctx->d_topflag, mask, ctx->ref ? nullptr : ctx->d_cls, ctx->d_topo,
-                                               ctx->stream);
+                                               ctx->d_roots, ctx->d_topflag, mask, ctx->ref ? nullptr : ctx->d_cls,
+                                               ctx->d_topo, ctx->stream);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(ctx->h_topo, ctx->d_topo, sizeof(TopoCounts), cudaMemcpyDeviceToHost, ctx->stream));
     int rc = wait_stream(ctx);
@@ -462,7 +464,7 @@ static int update_topology(mhdproj_ctx* ctx, const uint8_t* solid, bool* changed
         ref_set_topology_device(ctx->ref, ctx->components, (uint32_t)t.fluid);
     } else {
         ctx->pinned = (uint32_t)t.pinned;
-        ctx->n_active = (long long)t.active;
+        ctx->n_active = (long long)(t.fluid - t.pinned);
     }
     ctx->have_topology = true;
     return 0;
@@ -1091,11 +1093,11 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
     // fields, every field touched once per launch.
     const double vbc = ctx->opt.precision == 0 ? 4.0 : 2.0;   // level-1 vector bytes per cell
     // Connected-component labelling of the solid mask, by kernel: run starts
-    // (solid 1 -> label 4), links (solid 1), roots (solid 1 + label 4 ->
-    // label 4), classes (solid 1 + label 4 -> class 1); with an outlet the
-    // top marks (clear 1, read 1).
+    // (solid 1 -> label 4), links (solid 1), roots and classes (solid 1 ->
+    // class 1); with an outlet the top marks (clear 1).  Labels other than
+    // the run starts are not read again.
     const bool top_open = ctx->outlet && !(ctx->grid.periodic & 4);
-    const double topo_bytes = 21.0 + (top_open ? 2.0 : 0.0);
+    const double topo_bytes = 8.0 + (top_open ? 1.0 : 0.0);
     const Item classic[] = {
         {"spmv_dot", 20.0, 1, 0},             // p 4 + beta 12 -> q 4
         {"update_norm", 24.0, 1, 1},          // e, p, r, q 16 -> e, r 8
@@ -1148,8 +1150,8 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
                 case 9:
                     // relabels the current mask: the same classes are rewritten
                     launch_topology(ctx->d_solid_prev, (int)ctx->grid.nx, (int)ctx->grid.ny, (int)ctx->grid.nz,
-                                    (int)ctx->grid.periodic, ctx->outlet, ctx->d_labels, ctx->d_topflag, nullptr,
-                                    ctx->d_cls, ctx->d_topo, s);
+                                    (int)ctx->grid.periodic, ctx->outlet, ctx->d_labels, ctx->d_roots,
+                                    ctx->d_topflag, nullptr, ctx->d_cls, ctx->d_topo, s);
                     break;
                 case 10:
                     launch_search_spmv(ctx->L, ctx->coef, ctx->z, ctx->p, ctx->p1, ctx->e, ctx->q, ctx->sc,

@@ -168,16 +168,18 @@ struct TopoCounts {
     unsigned long long components;  // roots (one per component)
     unsigned long long fluid;       // non-solid cells
     unsigned long long pinned;      // gauge cells (classes only)
-    unsigned long long active;      // non-solid, non-gauge cells (classes only)
     int error;                      // a label walk or link hit its bound
     int pad;
 };
-// labels: u32[n] scratch.  mask_out (optional): the reference's encoding
-// (0 solid, 1 | root << 2, 2 | root << 2).  cls_out (optional): 0 solid,
-// 1 active, 2 pinned gauge cell, where components that reach the top z-layer
-// need no gauge when `outlet` is set on a non-periodic z axis; topflag: u8[n]
-// scratch for that case.  Requires n < 2^31.  Returns the kernels launched.
+// labels: u32[n] scratch; roots: u32[(n + 1) / 2] scratch (the most
+// components a 6-connected grid can have).  mask_out (optional): the
+// reference's encoding (0 solid, 1 | root << 2, 2 | root << 2).  cls_out
+// (optional): 0 solid, 1 active, 2 pinned gauge cell, where components that
+// reach the top z-layer need no gauge when `outlet` is set on a non-periodic
+// z axis; topflag: u8[n] scratch for that case.  counts: components, fluid
+// cells and (classes) pinned cells; active = fluid - pinned.  Requires
+// n < 2^31.  Returns the kernels launched.
 int launch_topology(const uint8_t* solid, int nx, int ny, int nz, int periodic, int outlet, uint32_t* labels,
-                    uint8_t* topflag, uint32_t* mask_out, uint8_t* cls_out, TopoCounts* counts, cudaStream_t s);
-
+                    uint32_t* roots, uint8_t* topflag, uint32_t* mask_out, uint8_t* cls_out, TopoCounts* counts,
+                    cudaStream_t s);
 }  // namespace mhdproj
