@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-extras", action="store_true", help="skip the FP32/adjoint/e2e/CPU legs")
+    ap.add_argument("--step", action="store_true",
+                    help="only the fluid-step leg: a few mhdproj_fluid_step calls on the workload's geometry as one "
+                         "liquid, then its kernels launched once each (a small launch list for profilers)")
     ap.add_argument("--kernels", action="store_true",
                     help="one projection, then each fine-level kernel of a CG iteration launched once in "
                          "isolation (a small, fixed launch list for profilers); prints the kernel times")
@@ -244,7 +247,37 @@ def run_ours(args):
         ms = e0.elapsed_time(e1)
         return max_over_ranks(ms, pg, dev), sts
 
+    def fluid_step_leg(steps, reps):
+        """FluidState::step without a moving interface on the workload's
+        geometry filled with one liquid: SL-RK2 advection, viscosity, gravity,
+        the warm-started projection, fields and diagnostics."""
+        ps = mhdproj.PressureProjection(case["dims"], case["h"], outlet=True, precision=args.precision,
+                                        rel_tol=args.tol)
+        ps.set_coefficients(alpha, solid, case["rho_liquid"], case["rho_liquid"])
+        su = [x.clone() for x in us]
+        dt_step = 5e-6
+
+        def step_fn(prj):
+            st, _ = prj.fluid_step(su, dt_step, acceleration=(0.0, 0.0, -9.81), viscosity=1e-6, advection=True)
+            return st
+
+        for _ in range(2):
+            step_fn(ps)
+        ms_s, sts_s = timed(ps, steps, step_fn)
+        prof_s = ps.profile_kernels(reps=reps)
+        ps.close()
+        return {"ms_per_step": ms_s / steps, "steps_per_s": 1000.0 * steps / ms_s, "iterations": sts_s[-1]["iterations"],
+                "dt": dt_step, "kinematic_viscosity": 1e-6,
+                "kernels": [{"name": k["name"], "us": k["ms"] * 1e3, "GBps": k["bytes"] / (k["ms"] * 1e-3) / 1e9}
+                            for k in prof_s if k["name"].startswith("step_")]}
+
     pr = make(args.precision)
+    if args.step:
+        out_s = fluid_step_leg(2, 1)
+        if rank == 0:
+            print(json.dumps({"fluid_step": out_s}))
+        pr.close()
+        return
     if args.kernels:
         step(pr)
         prof = pr.profile_kernels(reps=1)
@@ -380,6 +413,10 @@ def run_ours(args):
             pref.close()
         except mhdproj.ProjectionError as exc:
             line["reference_algorithm_gpu"] = {"unavailable": str(exc)}
+        try:
+            line["fluid_step"] = fluid_step_leg(5, 10)
+        except mhdproj.ProjectionError as exc:
+            line["fluid_step"] = {"unavailable": str(exc)}
         # CPU baseline: bounded sample of the reference algorithm on the host cores
         threads = os.cpu_count() or 1
         k_ref = reference_iterations(args.workload, args.tol)

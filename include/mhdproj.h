@@ -241,6 +241,62 @@ int mhdproj_kernel_launches(mhdproj_ctx *ctx, uint64_t *count);
 int mhdproj_divergence_noalloc(const mhdproj_grid *grid, const uint8_t *solid, const float *u, const float *v,
                                const float *w, double *out, void *stream);
 
+/* ------------------------------------------------------------ fluid step
+ * Fields, diagnostics and the fluid time step around the projection. */
+
+/* FluidDiagnostics (src/fluid/mod.rs:84-96) plus the two reductions the next
+ * step's CFL test reads (force_max and max_face_speed, :1140-1141). */
+typedef struct {
+    float max_speed_m_s;        /* max |cell-centred velocity| */
+    float max_divergence_s_inv; /* max |div u| */
+    float rms_divergence_s_inv; /* sqrt(sum div^2 / fluid cells) */
+    float max_pressure_pa;      /* max |p| */
+    float kinetic_energy_j;     /* sum 1/2 rho (face speeds^2) h^3 */
+    float fluid_mass_kg;        /* rho_l * sum melt fraction * h^3 */
+    float net_flux_m3_s;        /* sum div * h^3 */
+    float max_force_density;    /* max |rho_l g + f_em|, N/m^3 */
+    float max_face_speed_m_s;   /* max |u| over the faces of fluid cells */
+    uint32_t nonfinite_cells;   /* cells with non-finite or out-of-range fields */
+} mhdproj_diagnostics;
+
+/* fields + diagnostics of src/fluid/solver.wgsl:256-291, as dispatched after
+ * every accepted step and solid/phase update (src/fluid/mod.rs:899-905,
+ * :1311-1317): for the face velocities u, v, w (device arrays) and the
+ * context's last pressure potential, the FluidCell record of every cell
+ * (cells: 16 floats per cell, velocity xyz + speed, pressure + divergence,
+ * force = rho_l a + f_em, reserved (fluid flag, phase fraction, liquid
+ * fraction, 0); NULL to skip) and the diagnostics.  em_force: device array of
+ * 4 floats per cell holding the EM force density in xyz (NULL: none);
+ * acceleration: body acceleration (m/s^2); dt scales the pressure
+ * (p = rho_l phi / dt).  Returns MHDPROJ_ERR_NONFINITE with "Nonfinite fluid
+ * fields; state restored" when a field is non-finite or out of range (the
+ * outputs are still written). */
+int mhdproj_fields(mhdproj_ctx *ctx, const float *u, const float *v, const float *w, const float *em_force,
+                   const float acceleration[3], float dt, float *cells, mhdproj_diagnostics *diagnostics);
+
+typedef struct {
+    float dt;                  /* FluidConfig::dt_s */
+    float acceleration[3];     /* FluidConfig::acceleration_m_s2 */
+    float kinematic_viscosity; /* nu, m^2/s (Params.physical.z) */
+    int32_t advection;         /* FluidConfig::advection: semi-Lagrangian RK2 momentum transport */
+} mhdproj_step_params;
+
+/* FluidState::step (src/fluid/mod.rs:1246-1333) for a flow without a moving
+ * interface (one density: reference solver with two_phase = 0, GB300 solver
+ * with rho_air = rho_liquid): the velocity CFL test on the previous fields
+ * ("Fluid timestep exceeds the velocity CFL limit; reduce Δt"), predict
+ * (advection), viscous (explicit viscosity, body and EM force, mobility), the
+ * warm-started projection, fields and diagnostics.  u, v, w: device face
+ * arrays, the velocity in and the projected velocity out; p_out (cell array)
+ * and cells (16 floats per cell, written only when the step is accepted) are
+ * optional outputs.  On any error the velocity and p_out are restored to
+ * their values on entry, as the reference rolls back its buffers.  The CFL inputs come from the context's last
+ * fields pass (mhdproj_fields or the previous step); a context without one
+ * first runs a fields pass over the velocity it is given. */
+int mhdproj_fluid_step(mhdproj_ctx *ctx, float *u, float *v, float *w, const float *em_force,
+                       const mhdproj_step_params *params, float *p_out, float *cells, mhdproj_stats *stats,
+                       mhdproj_diagnostics *diagnostics);
+
 /* Host utilities, mirroring src/fluid/multigrid.rs:25-65 and src/fluid/mod.rs:1447-1493. */
 /* Aggregation hierarchy: halve (ceil) until every dimension is <= 4.  Returns
  * 0 and the level count / coarse-cell total, or MHDPROJ_ERR_INVALID for zero,

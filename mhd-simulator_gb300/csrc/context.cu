@@ -89,6 +89,18 @@ struct mhdproj_ctx {
     int c_steps = 0, c_every = 0;
     float c_dt = 0.f;
     bool c_ready = false;
+    // fluid step and fields: rollback copies, predicted and viscous velocity,
+    // reduction partials, and the last fields pass's CFL inputs
+    float *st_prev[3] = {nullptr, nullptr, nullptr}, *st_pred[3] = {nullptr, nullptr, nullptr};
+    float *st_star[3] = {nullptr, nullptr, nullptr}, *st_prev_p = nullptr;
+    float4* st_partials = nullptr;
+    float4* st_scalars = nullptr;
+    float4* h_st_scalars = nullptr;
+    bool have_fields = false;
+    bool step_ran = false;  // the step buffers hold a step's velocities (profiling)
+    float step_dt = 0.f, step_nu = 0.f;
+    float max_face_speed = 0.f, force_max = 0.f;
+    long long n_fluid = 0;
     // reference solver
     RefState* ref = nullptr;
 };
@@ -330,7 +342,8 @@ extern "C" int mhdproj_create(const mhdproj_grid* grid, const mhdproj_options* o
         return bad(MHDPROJ_ERR_CUDA);
     }
     if (cudaMallocHost(&ctx->h_sc, sizeof(Scalars)) != cudaSuccess || cudaMallocHost(&ctx->h_flag, sizeof(int)) != cudaSuccess ||
-        cudaMallocHost(&ctx->h_topo, sizeof(TopoCounts)) != cudaSuccess) {
+        cudaMallocHost(&ctx->h_topo, sizeof(TopoCounts)) != cudaSuccess ||
+        cudaMallocHost(&ctx->h_st_scalars, 3 * sizeof(float4)) != cudaSuccess) {
         fail(ctx, MHDPROJ_ERR_CUDA, "cudaMallocHost failed");
         return bad(MHDPROJ_ERR_CUDA);
     }
@@ -403,6 +416,7 @@ extern "C" void mhdproj_destroy(mhdproj_ctx* ctx) {
     if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
     if (ctx->h_flag) cudaFreeHost(ctx->h_flag);
     if (ctx->h_topo) cudaFreeHost(ctx->h_topo);
+    if (ctx->h_st_scalars) cudaFreeHost(ctx->h_st_scalars);
     if (ctx->ev_a) cudaEventDestroy(ctx->ev_a);
     if (ctx->ev_b) cudaEventDestroy(ctx->ev_b);
     if (ctx->ev_sync) cudaEventDestroy(ctx->ev_sync);
@@ -459,6 +473,7 @@ static int update_topology(mhdproj_ctx* ctx, const uint8_t* solid, bool* changed
         return fail(ctx, MHDPROJ_ERR_CUDA, "connected-component labelling exceeded its step bound");
     }
     ctx->components = (uint32_t)t.components;
+    ctx->n_fluid = (long long)t.fluid;
     if (ctx->ref) {
         ctx->n_active = (long long)t.fluid;
         ref_set_topology_device(ctx->ref, ctx->components, (uint32_t)t.fluid);
@@ -1073,6 +1088,199 @@ extern "C" int mhdproj_copy_topology(mhdproj_ctx* ctx, uint32_t* mask_host, uint
     return 0;
 }
 
+// ----------------------------------------------------------- fluid step
+static int step_buffers(mhdproj_ctx* ctx) {
+    if (ctx->st_partials) return 0;
+    const long long nf[3] = {ctx->nfx, ctx->nfy, ctx->nfz};
+    for (int a = 0; a < 3; a++) {
+        CK(dalloc(ctx, &ctx->st_prev[a], nf[a] * 4));
+        CK(dalloc(ctx, &ctx->st_pred[a], nf[a] * 4));
+        CK(dalloc(ctx, &ctx->st_star[a], nf[a] * 4));
+    }
+    CK(dalloc(ctx, &ctx->st_prev_p, ctx->n * 4));
+    CK(dalloc(ctx, &ctx->st_partials, (size_t)3 * ((ctx->n + 255) / 256) * sizeof(float4)));
+    CK(dalloc(ctx, &ctx->st_scalars, 3 * sizeof(float4)));
+    return 0;
+}
+
+// The fields of a velocity (u, v, w) with the context's potential.
+static StepView step_view(mhdproj_ctx* ctx, const float* u, const float* v, const float* w, const float* em,
+                          const float acc[3], float dt) {
+    StepView sv{};
+    sv.dims[0] = ctx->grid.nx;
+    sv.dims[1] = ctx->grid.ny;
+    sv.dims[2] = ctx->grid.nz;
+    sv.dims[3] = (uint32_t)ctx->n;
+    sv.periodic = ctx->grid.periodic;
+    sv.h = ctx->grid.h;
+    sv.dt = dt;
+    for (int a = 0; a < 3; a++) sv.acc[a] = acc ? acc[a] : 0.0f;
+    sv.vel[0] = u;
+    sv.vel[1] = v;
+    sv.vel[2] = w;
+    sv.em = reinterpret_cast<const float4*>(em);
+    if (ctx->ref) {
+        const RefExport e = ref_export(ctx->ref);
+        sv.mask = e.mask;
+        sv.occ = e.occ;
+        sv.phase = e.phase;
+        sv.phi = e.work;
+        sv.phi_stride = 4;
+        sv.mean_free = e.mean_free;
+        sv.two_phase = e.two_phase;
+        sv.rho_l = e.rho_l;
+        sv.rho_air = e.rho_air;
+        sv.drag_rate = e.drag_rate;
+    } else {
+        sv.cls = ctx->d_cls;
+        sv.occ = ctx->alpha;
+        sv.phi = ctx->phi_hi;
+        sv.phi_stride = 1;
+        sv.two_phase = ctx->rho_air != ctx->rho_l;
+        sv.rho_l = ctx->rho_l;
+        sv.rho_air = ctx->rho_air;
+    }
+    return sv;
+}
+
+// fields + diagnostics, then read_diagnostics (src/fluid/mod.rs:1116-1143).
+// *bad: a field is non-finite or out of range.
+static int run_fields(mhdproj_ctx* ctx, const StepView& sv, float* cells, mhdproj_diagnostics* d, bool* bad) {
+    int rc = step_buffers(ctx);
+    if (rc) return rc;
+    launch_fields(sv, reinterpret_cast<float4*>(cells), ctx->st_partials, ctx->st_scalars, ctx->stream);
+    ctx->launches += 2;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(ctx->h_st_scalars, ctx->st_scalars, 3 * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    rc = wait_stream(ctx);
+    if (rc) return rc;
+    const float* s = reinterpret_cast<const float*>(ctx->h_st_scalars);
+    *bad = s[7] != 0.0f;
+    for (int k = 0; k < 12; k++) *bad = *bad || !std::isfinite(s[k]);
+    const long long fl = ctx->ref ? (long long)ref_export(ctx->ref).fluid_cells : ctx->n_fluid;
+    const float h = ctx->grid.h, h3 = h * h * h;
+    mhdproj_diagnostics out{};
+    out.max_speed_m_s = s[0];
+    out.max_divergence_s_inv = s[1];
+    out.rms_divergence_s_inv = std::sqrt(s[2] / (float)(fl > 1 ? fl : 1));
+    out.kinetic_energy_j = s[3];
+    out.fluid_mass_kg = sv.rho_l * s[9] * h3;
+    out.max_pressure_pa = s[4];
+    out.net_flux_m3_s = s[5] * h3;
+    out.max_force_density = s[6];
+    out.max_face_speed_m_s = s[8];
+    out.nonfinite_cells = std::isfinite(s[7]) && s[7] > 0.f ? (uint32_t)s[7] : 0u;
+    if (d) *d = out;
+    if (!*bad) {
+        ctx->max_face_speed = s[8];
+        ctx->force_max = s[6];
+        ctx->have_fields = true;
+    }
+    return 0;
+}
+
+extern "C" int mhdproj_fields(mhdproj_ctx* ctx, const float* u, const float* v, const float* w, const float* em_force,
+                              const float acceleration[3], float dt, float* cells, mhdproj_diagnostics* diagnostics) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (!u || !v || !w) return fail(ctx, MHDPROJ_ERR_INVALID, "face arrays must not be NULL");
+    if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients first");
+    if (!(dt > 0.f) || !std::isfinite(dt))
+        return fail(ctx, MHDPROJ_ERR_INVALID, "Invalid fluid timestep, initial condition or solver limits/tolerances");
+    const StepView sv = step_view(ctx, u, v, w, em_force, acceleration, dt);
+    bool bad = false;
+    int rc = run_fields(ctx, sv, cells, diagnostics, &bad);
+    if (rc) return rc;
+    if (bad) return fail(ctx, MHDPROJ_ERR_NONFINITE, "Nonfinite fluid fields; state restored");
+    return 0;
+}
+
+// Velocity (and pressure) back to their values on entry.
+static int step_restore(mhdproj_ctx* ctx, float* const vel[3], float* p_out) {
+    const long long nf[3] = {ctx->nfx, ctx->nfy, ctx->nfz};
+    for (int a = 0; a < 3; a++)
+        CK(cudaMemcpyAsync(vel[a], ctx->st_prev[a], nf[a] * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (p_out) CK(cudaMemcpyAsync(p_out, ctx->st_prev_p, ctx->n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    return wait_stream(ctx);
+}
+
+extern "C" int mhdproj_fluid_step(mhdproj_ctx* ctx, float* u, float* v, float* w, const float* em_force,
+                                  const mhdproj_step_params* sp, float* p_out, float* cells, mhdproj_stats* stats,
+                                  mhdproj_diagnostics* diagnostics) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (!u || !v || !w || !sp) return fail(ctx, MHDPROJ_ERR_INVALID, "face arrays and step parameters must not be NULL");
+    if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients first");
+    const float dt = sp->dt;
+    bool ok = dt > 0.f && std::isfinite(dt) && std::isfinite(sp->kinematic_viscosity) && sp->kinematic_viscosity >= 0.f;
+    for (int a = 0; a < 3; a++) ok = ok && std::isfinite(sp->acceleration[a]);
+    if (!ok) return fail(ctx, MHDPROJ_ERR_INVALID, "Invalid fluid timestep, initial condition or solver limits/tolerances");
+    StepView base = step_view(ctx, u, v, w, em_force, sp->acceleration, dt);
+    if (base.two_phase)
+        return fail(ctx, MHDPROJ_ERR_INVALID,
+                    "the fluid step covers flows without a moving interface (one density; reference solver "
+                    "two_phase = 0)");
+    if (ctx->ref && base.phase && dt != ref_export(ctx->ref).drag_dt)
+        return fail(ctx, MHDPROJ_ERR_INVALID,
+                    "the phase-drag mobility was set for a different dt; call mhdproj_set_phase_drag again");
+    int rc = step_buffers(ctx);
+    if (rc) return rc;
+    float* const vel[3] = {u, v, w};
+    // velocity CFL limit (src/fluid/mod.rs:1255-1262) on the last fields
+    if (!ctx->have_fields) {
+        bool bad = false;
+        rc = run_fields(ctx, base, nullptr, nullptr, &bad);
+        if (rc) return rc;
+        if (bad) return fail(ctx, MHDPROJ_ERR_NONFINITE, "Nonfinite fluid fields; state restored");
+    }
+    {
+        const float* g = sp->acceleration;
+        const float acceleration = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]) + ctx->force_max / base.rho_l;
+        if ((ctx->max_face_speed * std::sqrt(3.0f) + acceleration * dt) * dt / ctx->grid.h > 0.9f)
+            return fail(ctx, MHDPROJ_ERR_INVALID, "Fluid timestep exceeds the velocity CFL limit; reduce Δt");
+    }
+    const long long nf[3] = {ctx->nfx, ctx->nfy, ctx->nfz};
+    for (int a = 0; a < 3; a++)
+        CK(cudaMemcpyAsync(ctx->st_prev[a], vel[a], nf[a] * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (p_out) CK(cudaMemcpyAsync(ctx->st_prev_p, p_out, ctx->n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    // predict (advection) and viscous (viscosity, forcing, mobility)
+    StepView sv = base;
+    sv.advection = sp->advection != 0;
+    sv.nu = sp->kinematic_viscosity;
+    launch_predict(sv, ctx->st_pred, ctx->stream);
+    for (int a = 0; a < 3; a++) sv.vel[a] = ctx->st_pred[a];
+    launch_viscous(sv, ctx->st_star, ctx->stream);
+    ctx->launches += 6;
+    CK(cudaGetLastError());
+    ctx->step_ran = true;
+    ctx->step_dt = dt;
+    ctx->step_nu = sp->kinematic_viscosity;
+    // the warm-started projection of the viscous velocity into (u, v, w)
+    rc = mhdproj_project(ctx, ctx->st_star[0], ctx->st_star[1], ctx->st_star[2], u, v, w, p_out, dt, 1, stats);
+    if (rc) {
+        const std::string msg = ctx->err;
+        step_restore(ctx, vel, p_out);
+        ctx->err = msg;
+        return rc;
+    }
+    // fields and diagnostics of the projected velocity; the cell records are
+    // written once the diagnostics accept the step
+    const StepView fv = step_view(ctx, u, v, w, em_force, sp->acceleration, dt);
+    bool bad = false;
+    rc = run_fields(ctx, fv, nullptr, diagnostics, &bad);
+    if (rc) return rc;
+    if (bad) {
+        step_restore(ctx, vel, p_out);
+        return fail(ctx, MHDPROJ_ERR_NONFINITE, "Nonfinite fluid fields; state restored");
+    }
+    if (cells) {
+        launch_fields(fv, reinterpret_cast<float4*>(cells), ctx->st_partials, ctx->st_scalars, ctx->stream);
+        ctx->launches += 2;
+        CK(cudaGetLastError());
+        return wait_stream(ctx);
+    }
+    return 0;
+}
+
+
 // ---------------------------------------------------------- measurement
 extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kernel_time* out, int max_out, int* count) {
     if (!ctx || !out || !count) return MHDPROJ_ERR_INVALID;
@@ -1098,6 +1306,7 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
     // the run starts are not read again.
     const bool top_open = ctx->outlet && !(ctx->grid.periodic & 4);
     const double topo_bytes = 8.0 + (top_open ? 1.0 : 0.0);
+    const double mask_bytes = ctx->ref ? 4.0 : 1.0;
     const Item classic[] = {
         {"spmv_dot", 20.0, 1, 0},             // p 4 + beta 12 -> q 4
         {"update_norm", 24.0, 1, 1},          // e, p, r, q 16 -> e, r 8
@@ -1121,6 +1330,12 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
         {"refinement_residual", 40.0, 0, 7},
         {"coefficients", 29.0, 0, 8},
         {"topology", topo_bytes, 0, 9},
+        // fluid step (after a step has run): per axis launch, the three face
+        // arrays 12 + fluid mask + the axis's output 4
+        {"step_predict", 3.0 * (16.0 + mask_bytes), 0, 20},
+        {"step_viscous", 3.0 * (16.0 + mask_bytes), 0, 21},
+        // faces 12 + mask + potential 4 (+ liquid fraction 4) -> reductions
+        {"step_fields", 20.0 + mask_bytes, 0, 22},
     };
     const Item* items = ctx->pipelined ? pipelined : classic;
     const int n_items = ctx->pipelined ? (int)(sizeof pipelined / sizeof pipelined[0])
@@ -1130,6 +1345,7 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
         const Item& it = items[ii];
         if (k >= max_out) break;
         if (!ctx->use_mg && (it.kind >= 2 && it.kind <= 4)) continue;
+        if (it.kind >= 20 && it.kind <= 22 && !ctx->step_ran) continue;
         launch_set_sigma(ctx->sc, 1.0f, s);  // clears the converged flag
         if (it.kind >= 10) launch_profile_reset(ctx->sc, s);
         CK(cudaEventRecord(ctx->ev_a, s));
@@ -1153,6 +1369,22 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
                                     (int)ctx->grid.periodic, ctx->outlet, ctx->d_labels, ctx->d_roots,
                                     ctx->d_topflag, nullptr, ctx->d_cls, ctx->d_topo, s);
                     break;
+                case 20:
+                case 21:
+                case 22: {
+                    const float g[3] = {0.0f, 0.0f, -9.81f};
+                    StepView sv = step_view(ctx, ctx->st_prev[0], ctx->st_prev[1], ctx->st_prev[2], nullptr, g,
+                                            ctx->step_dt);
+                    sv.advection = 1;
+                    sv.nu = ctx->step_nu;
+                    if (it.kind == 20) launch_predict(sv, ctx->st_pred, s);
+                    if (it.kind == 21) {
+                        for (int a = 0; a < 3; a++) sv.vel[a] = ctx->st_pred[a];
+                        launch_viscous(sv, ctx->st_star, s);
+                    }
+                    if (it.kind == 22) launch_fields(sv, nullptr, ctx->st_partials, ctx->st_scalars, s);
+                    break;
+                }
                 case 10:
                     launch_search_spmv(ctx->L, ctx->coef, ctx->z, ctx->p, ctx->p1, ctx->e, ctx->q, ctx->sc,
                                        ctx->partials, 1, s);

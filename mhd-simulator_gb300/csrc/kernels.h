@@ -182,4 +182,28 @@ struct TopoCounts {
 int launch_topology(const uint8_t* solid, int nx, int ny, int nz, int periodic, int outlet, uint32_t* labels,
                     uint32_t* roots, uint8_t* topflag, uint32_t* mask_out, uint8_t* cls_out, TopoCounts* counts,
                     cudaStream_t s);
+// ---- fluid step and fields (step_kernels.cu)
+struct StepView {
+    uint32_t dims[4];       // nx, ny, nz, n
+    uint32_t periodic;      // bit a: axis a periodic
+    int advection;          // predict: semi-Lagrangian RK2
+    int two_phase;          // density from the liquid fraction (fields only in a step)
+    int mean_free;          // pressure relative to the component root (reference mask)
+    float h, dt, nu, rho_l, rho_air, drag_rate;
+    float acc[3];
+    const uint32_t* mask;   // reference encoding (fluid != 0), or null
+    const uint8_t* cls;     // GB300 classes (fluid != 0) when mask is null
+    const float* occ;       // liquid fraction or null
+    const float* phase;     // thermal phase fraction (phase drag) or null
+    const float* vel[3];    // face arrays read by face()
+    const float4* em;       // EM force density per cell (xyz) or null
+    const float* phi;       // pressure potential, element i at phi[i * phi_stride]
+    int phi_stride;
+};
+void launch_predict(const StepView& s, float* const out[3], cudaStream_t st);
+void launch_viscous(const StepView& s, float* const out[3], cudaStream_t st);
+uint32_t fields_groups(const StepView& s);
+// partials: 3 * fields_groups float4; scalars3: 3 float4 (the 12 diagnostics floats)
+void launch_fields(const StepView& s, float4* cells, float4* partials, float4* scalars3, cudaStream_t st);
+
 }  // namespace mhdproj

@@ -16,6 +16,17 @@ int ref_set_topology(RefState* s, const uint32_t* mask_host, uint32_t components
 // counts that go with it.
 uint32_t* ref_mask(RefState* s);
 void ref_set_topology_device(RefState* s, uint32_t components, uint32_t fluid_cells);
+// What the fluid step and fields kernels read of the reference solver.
+struct RefExport {
+    const uint32_t* mask;
+    const float* occ;
+    const float* phase;  // null without phase drag
+    const float* work;   // float4 per cell, x = pressure potential
+    uint32_t fluid_cells;
+    int mean_free, two_phase;
+    float rho_l, rho_air, drag_rate, drag_dt;
+};
+RefExport ref_export(RefState* s);
 int ref_set_coefficients(RefState* s, const float* alpha, float rho_l, float rho_air, std::string& err);
 int ref_set_phase_drag(RefState* s, const float* phase, float drag_rate, float dt, std::string& err);
 int ref_project(RefState* s, const float* us, const float* vs, const float* ws, float* uo, float* vo, float* wo,

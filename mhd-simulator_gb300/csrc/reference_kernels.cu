@@ -1004,6 +1004,22 @@ int ref_set_topology(RefState* s, const uint32_t* mask_host, uint32_t components
 
 uint32_t* ref_mask(RefState* s) { return s->mask; }
 
+RefExport ref_export(RefState* s) {
+    RefExport e{};
+    e.mask = s->mask;
+    e.occ = s->occ;
+    e.phase = s->drag ? s->phase : nullptr;
+    e.work = reinterpret_cast<const float*>(s->work);
+    e.fluid_cells = s->fluid_cells;
+    e.mean_free = s->p.initial[3] > 0.0f;
+    e.two_phase = s->p.surface[0] > 0.5f;
+    e.rho_l = s->p.physical[3];
+    e.rho_air = s->p.surface[1];
+    e.drag_rate = s->drag_rate;
+    e.drag_dt = s->drag_dt;
+    return e;
+}
+
 void ref_set_topology_device(RefState* s, uint32_t components, uint32_t fluid_cells) {
     s->fluid_cells = fluid_cells;
     s->components = components;

@@ -1,0 +1,345 @@
+// step_kernels.cu -- the fluid step around the projection: semi-Lagrangian
+// advection, explicit viscosity and forcing, and the per-cell fields and
+// diagnostics reductions.
+//
+// Each kernel restates one WGSL entry point of src/fluid/solver.wgsl for a
+// step without a moving interface (FluidState::step, src/fluid/mod.rs:
+// 1246-1333):
+//   ks_predict      predict (:127-141): u at the face, or with advection the
+//                   value at the RK2 departure point, trilinear in the face
+//                   grid of that axis;
+//   ks_viscous      viscous (:143-163): explicit 6-neighbour Laplacian
+//                   (closed tangential neighbours mirrored: no slip), body and
+//                   EM acceleration, times the face mobility;
+//   ks_fields       fields (:256-285): the 16-float cell record (velocity and
+//                   speed, pressure and divergence, force, reserved) and the
+//                   per-workgroup max/sum reductions;
+//   ks_diagnostics  diagnostics (:286-291): the single-workgroup final pass.
+// Faces are the SoA arrays of include/mhdproj.h, one launch per axis.  The
+// arithmetic keeps the reference's operation order without fused
+// multiply-adds (this unit is compiled with -fmad=false) and the reductions
+// replay the reference's 256-lane tree and 256-stride final pass, so results
+// equal the oracle's restatement bit for bit.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kernels.h"
+
+namespace mhdproj {
+
+namespace {
+constexpr int WG = 256;
+
+struct P3 {
+    int v[3];
+};
+
+__device__ __forceinline__ int32_t wrap_periodic(int32_t value, uint32_t size) {  // periodic.wgsl:5
+    if (value >= 0) return (int32_t)((uint32_t)value % size);
+    const uint32_t magnitude = (uint32_t)(-(value + 1)) + 1u;
+    const uint32_t remainder = magnitude % size;
+    return (int32_t)(remainder == 0u ? 0u : size - remainder);
+}
+__device__ __forceinline__ uint32_t cell_index(const StepView& s, P3 q) {
+    return (uint32_t)q.v[0] + s.dims[0] * ((uint32_t)q.v[1] + s.dims[1] * (uint32_t)q.v[2]);
+}
+__device__ __forceinline__ P3 wrap_cell(const StepView& s, P3 q) {
+    for (int a = 0; a < 3; a++)
+        if (s.periodic & (1u << a)) q.v[a] = wrap_periodic(q.v[a], s.dims[a]);
+    return q;
+}
+__device__ __forceinline__ bool valid_cell(const StepView& s, P3 q) {
+    for (int a = 0; a < 3; a++)
+        if (q.v[a] < 0 || q.v[a] >= (int)s.dims[a]) return false;
+    return true;
+}
+__device__ __forceinline__ bool is_fluid_index(const StepView& s, uint32_t i) {
+    return s.mask ? s.mask[i] != 0u : s.cls[i] != 0;
+}
+__device__ __forceinline__ bool fluid(const StepView& s, P3 pos) {
+    const P3 q = wrap_cell(s, pos);
+    if (!valid_cell(s, q)) return false;
+    return is_fluid_index(s, cell_index(s, q));
+}
+__device__ __forceinline__ bool valid_face(const StepView& s, P3 q, int axis) {
+    for (int a = 0; a < 3; a++) {
+        const int lim = (int)s.dims[a] + (a == axis ? 1 : 0);
+        if (q.v[a] < 0 || q.v[a] >= lim) return false;
+    }
+    return true;
+}
+__device__ __forceinline__ bool open_face(const StepView& s, P3 pos, int axis) {  // :32
+    const P3 q = wrap_cell(s, pos);
+    if (!valid_face(s, q, axis)) return false;
+    P3 left = q;
+    left.v[axis] -= 1;
+    return fluid(s, left) && fluid(s, q);
+}
+__device__ __forceinline__ uint32_t face_index(const StepView& s, P3 q, int axis) {
+    const uint32_t nx = s.dims[0], ny = s.dims[1];
+    if (axis == 0) return (uint32_t)q.v[0] + (nx + 1) * ((uint32_t)q.v[1] + ny * (uint32_t)q.v[2]);
+    if (axis == 1) return (uint32_t)q.v[0] + nx * ((uint32_t)q.v[1] + (ny + 1) * (uint32_t)q.v[2]);
+    return (uint32_t)q.v[0] + nx * ((uint32_t)q.v[1] + ny * (uint32_t)q.v[2]);
+}
+// face() (:33-36) over the face arrays in s.vel
+__device__ __forceinline__ float face(const StepView& s, P3 pos, int axis) {
+    const P3 q = wrap_cell(s, pos);
+    if (!open_face(s, q, axis)) return 0.0f;
+    return s.vel[axis][face_index(s, q, axis)];
+}
+__device__ __forceinline__ float occupancy(const StepView& s, P3 pos) {
+    const P3 q = wrap_cell(s, pos);
+    if (!valid_cell(s, q) || !s.occ) return 0.0f;
+    return s.occ[cell_index(s, q)];
+}
+__device__ __forceinline__ float density(const StepView& s, P3 pos) {  // :41, mix(air, liquid, alpha)
+    const float t = occupancy(s, pos);
+    return s.rho_air * (1.0f - t) + s.rho_l * t;
+}
+__device__ __forceinline__ float face_density(const StepView& s, P3 pos, int axis) {  // :42
+    P3 left = pos;
+    left.v[axis] -= 1;
+    return 0.5f * (density(s, left) + density(s, pos));
+}
+__device__ __forceinline__ float mobility(const StepView& s, P3 pos, int axis) {  // :43-51
+    float beta = 1.0f;
+    P3 left = pos;
+    left.v[axis] -= 1;
+    if (s.two_phase) beta = s.rho_l / face_density(s, pos, axis);
+    if (!s.phase) return beta;
+    if (!fluid(s, pos) || !fluid(s, left)) return 0.0f;
+    const float fa = s.phase[cell_index(s, wrap_cell(s, pos))];
+    const float fb = s.phase[cell_index(s, wrap_cell(s, left))];
+    const float f = fminf(fa, fb);
+    const float drag = s.drag_rate * (1.0f - f) * (1.0f - f) / (f * f * f + 1e-3f);
+    return beta / (1.0f + s.dt * drag);
+}
+__device__ __forceinline__ float em_force(const StepView& s, P3 pos, int axis) {  // :108
+    const P3 q = wrap_cell(s, pos);
+    if (!s.em || !valid_cell(s, q)) return 0.0f;
+    const float4 f = s.em[cell_index(s, q)];
+    return axis == 0 ? f.x : (axis == 1 ? f.y : f.z);
+}
+// sample_component (:109-116): trilinear in the face grid of `axis`.
+__device__ float sample_component(const StepView& s, const float position[3], int axis) {
+    int base[3];
+    float fraction[3];
+    for (int a = 0; a < 3; a++) {
+        const float q = position[a] - (a == axis ? 0.0f : 0.5f);
+        const float fl = floorf(q);
+        base[a] = (int)fl;
+        fraction[a] = q - fl;  // fract()
+    }
+    float value = 0.0f;
+#pragma unroll
+    for (int z = 0; z < 2; z++)
+#pragma unroll
+        for (int y = 0; y < 2; y++)
+#pragma unroll
+            for (int x = 0; x < 2; x++) {
+                const float wx = x ? fraction[0] : 1.0f - fraction[0];
+                const float wy = y ? fraction[1] : 1.0f - fraction[1];
+                const float wz = z ? fraction[2] : 1.0f - fraction[2];
+                P3 c;
+                c.v[0] = base[0] + x;
+                c.v[1] = base[1] + y;
+                c.v[2] = base[2] + z;
+                value += face(s, c, axis) * wx * wy * wz;
+            }
+    return value;
+}
+
+__device__ __forceinline__ bool face_position(const StepView& s, int axis, uint32_t f, P3* pos) {
+    uint32_t d[3] = {s.dims[0], s.dims[1], s.dims[2]};
+    d[axis] += 1;
+    if (f >= d[0] * d[1] * d[2]) return false;
+    pos->v[0] = (int)(f % d[0]);
+    pos->v[1] = (int)((f / d[0]) % d[1]);
+    pos->v[2] = (int)(f / (d[0] * d[1]));
+    return true;
+}
+
+__global__ void ks_predict(StepView s, int axis, float* __restrict__ out) {
+    const uint32_t f = blockIdx.x * WG + threadIdx.x;
+    P3 pos;
+    if (!face_position(s, axis, f, &pos)) return;
+    float value = 0.0f;
+    if (open_face(s, pos, axis)) {
+        const float center = face(s, pos, axis);
+        value = center;
+        if (s.advection) {
+            float at[3];
+            for (int a = 0; a < 3; a++) at[a] = (float)pos.v[a] + 0.5f;
+            at[axis] -= 0.5f;
+            float v[3], mid[3], vm[3], back[3];
+            for (int a = 0; a < 3; a++) v[a] = sample_component(s, at, a);
+            const float half = 0.5f * s.dt / s.h;
+            for (int a = 0; a < 3; a++) mid[a] = at[a] - v[a] * half;
+            for (int a = 0; a < 3; a++) vm[a] = sample_component(s, mid, a);
+            const float full = s.dt / s.h;
+            for (int a = 0; a < 3; a++) back[a] = at[a] - vm[a] * full;
+            value = sample_component(s, back, axis);
+        }
+    }
+    out[f] = value;
+}
+
+__global__ void ks_viscous(StepView s, int axis, float* __restrict__ out) {
+    const uint32_t f = blockIdx.x * WG + threadIdx.x;
+    P3 pos;
+    if (!face_position(s, axis, f, &pos)) return;
+    float value = 0.0f;
+    if (open_face(s, pos, axis)) {
+        const float center = face(s, pos, axis);
+        float laplace = 0.0f;
+        if (!s.two_phase)
+            for (int d = 0; d < 3; d++)
+                for (int sign = -1; sign <= 1; sign += 2) {
+                    P3 q = pos;
+                    q.v[d] += sign;
+                    float neighbor = face(s, q, axis);
+                    if (!open_face(s, q, axis) && d != axis) neighbor = -center;
+                    laplace += neighbor - center;
+                }
+        P3 left = pos;
+        left.v[axis] -= 1;
+        const float rho = s.rho_l;
+        const float acc = s.acc[axis] + (em_force(s, left, axis) + em_force(s, pos, axis)) / (2.0f * rho) + 0.0f;
+        const float beta = mobility(s, pos, axis);
+        value = (center + s.nu * s.dt / (s.h * s.h) * laplace + s.dt * acc) * beta;
+    }
+    out[f] = value;
+}
+
+__global__ void ks_fields(StepView s, float4* __restrict__ cells, float4* __restrict__ partials) {
+    __shared__ float4 ra[WG], rb[WG];
+    __shared__ float2 rc[WG];
+    const int l = threadIdx.x;
+    const uint32_t i = blockIdx.x * WG + l;
+    const uint32_t groups = gridDim.x;
+    float4 stats = make_float4(0.f, 0.f, 0.f, 0.f), other = make_float4(0.f, 0.f, 0.f, 0.f);
+    float max_face = 0.0f, melt = 0.0f;
+    if (i < s.dims[3]) {
+        float4 o0 = make_float4(0.f, 0.f, 0.f, 0.f), o1 = o0, o2 = o0, o3 = o0;
+        const float oy = s.phase ? s.phase[i] : 0.0f;
+        const float oz = s.occ ? s.occ[i] : 0.0f;
+        if (s.two_phase) o3 = make_float4(0.0f, oy, oz, 0.0f);
+        if (is_fluid_index(s, i)) {
+            P3 pos;
+            pos.v[0] = (int)(i % s.dims[0]);
+            pos.v[1] = (int)((i / s.dims[0]) % s.dims[1]);
+            pos.v[2] = (int)(i / (s.dims[0] * s.dims[1]));
+            float v[3], face_energy = 0.0f, div = 0.0f;
+            for (int axis = 0; axis < 3; axis++) {
+                P3 q = pos;
+                q.v[axis] += 1;
+                const float a = face(s, pos, axis), b = face(s, q, axis);
+                v[axis] = 0.5f * (a + b);
+                face_energy += 0.5f * (a * a + b * b);
+                max_face = fmaxf(max_face, fmaxf(fabsf(a), fabsf(b)));
+                div += b - a;  // divergence(pos, false), :104-106
+            }
+            div = div / s.h;
+            melt = s.phase ? oy : 1.0f;
+            if (s.two_phase) melt *= oz;
+            const float speed = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            const float x = s.phi[(size_t)i * s.phi_stride];
+            const float pv = s.mean_free ? x - s.phi[(size_t)(s.mask[i] >> 2u) * s.phi_stride] : x;
+            const float pressure = pv * s.rho_l / s.dt;
+            float force[3];
+            for (int a = 0; a < 3; a++) force[a] = s.rho_l * s.acc[a] + em_force(s, pos, a);
+            o0 = make_float4(v[0], v[1], v[2], speed);
+            o1 = make_float4(pressure, div, 0.0f, 0.0f);
+            o2 = make_float4(force[0], force[1], force[2], 0.0f);
+            o3 = make_float4(1.0f, s.phase ? oy : 1.0f, oz, 0.0f);
+            bool bad = v[0] != v[0] || v[1] != v[1] || v[2] != v[2];
+            bad = bad || force[0] != force[0] || force[1] != force[1] || force[2] != force[2];
+            bad = bad || fabsf(force[0]) > 1e30f || fabsf(force[1]) > 1e30f || fabsf(force[2]) > 1e30f;
+            bad = bad || speed > 1e25f || !(fabsf(pressure) < 1e30f) || !(fabsf(div) < 1e30f);
+            const float rho = s.two_phase ? density(s, pos) : s.rho_l;
+            stats = make_float4(speed, fabsf(div), div * div, 0.5f * rho * face_energy * s.h * s.h * s.h);
+            other = make_float4(fabsf(pressure), div,
+                                sqrtf(force[0] * force[0] + force[1] * force[1] + force[2] * force[2]),
+                                bad ? 1.0f : 0.0f);
+        }
+        if (cells) {
+            float4* c = cells + (size_t)4 * i;
+            c[0] = o0;
+            c[1] = o1;
+            c[2] = o2;
+            c[3] = o3;
+        }
+    }
+    ra[l] = stats;
+    rb[l] = other;
+    rc[l] = make_float2(max_face, melt);
+    __syncthreads();
+    for (int st = 128; st > 0; st /= 2) {
+        if (l < st) {
+            const float4 a = ra[l], a2 = ra[l + st], b = rb[l], b2 = rb[l + st];
+            ra[l] = make_float4(fmaxf(a.x, a2.x), fmaxf(a.y, a2.y), a.z + a2.z, a.w + a2.w);
+            rb[l] = make_float4(fmaxf(b.x, b2.x), b.y + b2.y, fmaxf(b.z, b2.z), b.w + b2.w);
+            rc[l] = make_float2(fmaxf(rc[l].x, rc[l + st].x), rc[l].y + rc[l + st].y);
+        }
+        __syncthreads();
+    }
+    if (l == 0) {
+        partials[blockIdx.x] = ra[0];
+        partials[groups + blockIdx.x] = rb[0];
+        partials[2 * groups + blockIdx.x] = make_float4(rc[0].x, rc[0].y, 0.0f, 0.0f);
+    }
+}
+
+__global__ void ks_diagnostics(const float4* __restrict__ partials, uint32_t groups, float4* __restrict__ out) {
+    __shared__ float4 ra[WG], rb[WG];
+    __shared__ float2 rc[WG];
+    const int l = threadIdx.x;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+    float2 c = make_float2(0.f, 0.f);
+    for (uint32_t i = (uint32_t)l; i < groups; i += WG) {
+        const float4 fs = partials[2 * groups + i], x = partials[i], y = partials[groups + i];
+        c = make_float2(fmaxf(c.x, fs.x), c.y + fs.y);
+        a = make_float4(fmaxf(a.x, x.x), fmaxf(a.y, x.y), a.z + x.z, a.w + x.w);
+        b = make_float4(fmaxf(b.x, y.x), b.y + y.y, fmaxf(b.z, y.z), b.w + y.w);
+    }
+    ra[l] = a;
+    rb[l] = b;
+    rc[l] = c;
+    __syncthreads();
+    for (int st = 128; st > 0; st /= 2) {
+        if (l < st) {
+            const float4 p = ra[l], p2 = ra[l + st], q = rb[l], q2 = rb[l + st];
+            ra[l] = make_float4(fmaxf(p.x, p2.x), fmaxf(p.y, p2.y), p.z + p2.z, p.w + p2.w);
+            rb[l] = make_float4(fmaxf(q.x, q2.x), q.y + q2.y, fmaxf(q.z, q2.z), q.w + q2.w);
+            rc[l] = make_float2(fmaxf(rc[l].x, rc[l + st].x), rc[l].y + rc[l + st].y);
+        }
+        __syncthreads();
+    }
+    if (l == 0) {
+        out[0] = ra[0];
+        out[1] = rb[0];
+        out[2] = make_float4(rc[0].x, rc[0].y, 0.0f, 0.0f);
+    }
+}
+}  // namespace
+
+static unsigned face_blocks(const StepView& s, int axis) {
+    uint64_t d[3] = {s.dims[0], s.dims[1], s.dims[2]};
+    d[axis] += 1;
+    return (unsigned)((d[0] * d[1] * d[2] + WG - 1) / WG);
+}
+
+void launch_predict(const StepView& s, float* const out[3], cudaStream_t st) {
+    for (int a = 0; a < 3; a++) ks_predict<<<face_blocks(s, a), WG, 0, st>>>(s, a, out[a]);
+}
+void launch_viscous(const StepView& s, float* const out[3], cudaStream_t st) {
+    for (int a = 0; a < 3; a++) ks_viscous<<<face_blocks(s, a), WG, 0, st>>>(s, a, out[a]);
+}
+uint32_t fields_groups(const StepView& s) { return (s.dims[3] + WG - 1) / WG; }
+void launch_fields(const StepView& s, float4* cells, float4* partials, float4* scalars3, cudaStream_t st) {
+    const uint32_t groups = fields_groups(s);
+    ks_fields<<<groups, WG, 0, st>>>(s, cells, partials);
+    ks_diagnostics<<<1, WG, 0, st>>>(partials, groups, scalars3);
+}
+
+}  // namespace mhdproj

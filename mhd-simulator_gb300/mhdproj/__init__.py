@@ -61,6 +61,23 @@ class Stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Diagnostics(C.Structure):
+    """mhdproj_diagnostics: FluidDiagnostics plus the CFL inputs of the next step."""
+    _fields_ = [("max_speed_m_s", C.c_float), ("max_divergence_s_inv", C.c_float),
+                ("rms_divergence_s_inv", C.c_float), ("max_pressure_pa", C.c_float),
+                ("kinetic_energy_j", C.c_float), ("fluid_mass_kg", C.c_float), ("net_flux_m3_s", C.c_float),
+                ("max_force_density", C.c_float), ("max_face_speed_m_s", C.c_float),
+                ("nonfinite_cells", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class StepParams(C.Structure):
+    _fields_ = [("dt", C.c_float), ("acceleration", C.c_float * 3), ("kinematic_viscosity", C.c_float),
+                ("advection", C.c_int32)]
+
+
 class KernelTime(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("ms", C.c_float), ("bytes", C.c_double), ("per_iteration", C.c_int)]
 
@@ -112,6 +129,10 @@ def load():
     L.mhdproj_hierarchy.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)]
     L.mhdproj_anchors.argtypes = [_vp, C.POINTER(C.c_uint32), C.c_uint32]
     L.mhdproj_anchors.restype = C.c_uint32
+    L.mhdproj_fields.argtypes = [_vp] + [_vp] * 4 + [C.POINTER(C.c_float * 3), C.c_float, _vp,
+                                                     C.POINTER(Diagnostics)]
+    L.mhdproj_fluid_step.argtypes = [_vp] + [_vp] * 4 + [C.POINTER(StepParams), _vp, _vp, C.POINTER(Stats),
+                                                         C.POINTER(Diagnostics)]
     _lib = L
     return L
 
@@ -122,7 +143,7 @@ EXPORTED = [
     "mhdproj_project_vjp", "mhdproj_chain_forward", "mhdproj_chain_backward", "mhdproj_apply_operator",
     "mhdproj_apply_preconditioner", "mhdproj_copy_coefficients", "mhdproj_copy_potential", "mhdproj_copy_topology",
     "mhdproj_hierarchy", "mhdproj_anchors", "mhdproj_profile_kernels", "mhdproj_divergence_noalloc",
-    "mhdproj_kernel_launches",
+    "mhdproj_kernel_launches", "mhdproj_fields", "mhdproj_fluid_step",
 ]
 
 
@@ -351,6 +372,35 @@ class PressureProjection:
         self._check(self._lib.mhdproj_profile_kernels(self._ctx, reps, buf, 16, C.byref(n)))
         return [dict(name=buf[i].name.decode(), ms=buf[i].ms, bytes=buf[i].bytes, per_iteration=buf[i].per_iteration)
                 for i in range(n.value)]
+
+    def fields(self, u, dt, em_force=None, acceleration=(0.0, 0.0, 0.0), cells=True):
+        """fields + diagnostics (mhdproj_fields) of face velocities u = (u, v, w)
+        with the last pressure potential: returns (cells (nz, ny, nx, 16) or
+        None, diagnostics dict).  em_force: (nz, ny, nx, 4) force density."""
+        self._order()
+        torch = self._torch
+        out = torch.empty(self.cell_shape() + (16,), dtype=torch.float32, device=u[0].device) if cells else None
+        d = Diagnostics()
+        acc = (C.c_float * 3)(*acceleration)
+        self._check(self._lib.mhdproj_fields(self._ctx, _ptr(u[0]), _ptr(u[1]), _ptr(u[2]),
+                                             None if em_force is None else _ptr(em_force), C.byref(acc), dt,
+                                             None if out is None else _ptr(out), C.byref(d)))
+        return out, d.as_dict()
+
+    def fluid_step(self, u, dt, acceleration=(0.0, 0.0, -9.81), viscosity=0.0, advection=True, em_force=None,
+                   p_out=None, cells=None):
+        """One FluidState::step (mhdproj_fluid_step) in place on u = (u, v, w):
+        returns (stats dict, diagnostics dict).  p_out / cells: optional
+        device outputs (cells shaped (nz, ny, nx, 16))."""
+        self._order()
+        sp = StepParams(dt, (C.c_float * 3)(*acceleration), viscosity, int(bool(advection)))
+        st = Stats()
+        d = Diagnostics()
+        self._check(self._lib.mhdproj_fluid_step(self._ctx, _ptr(u[0]), _ptr(u[1]), _ptr(u[2]),
+                                                 None if em_force is None else _ptr(em_force), C.byref(sp),
+                                                 None if p_out is None else _ptr(p_out),
+                                                 None if cells is None else _ptr(cells), C.byref(st), C.byref(d)))
+        return st.as_dict(), d.as_dict()
 
     def topology(self):
         n = self.dims[0] * self.dims[1] * self.dims[2]

@@ -89,6 +89,22 @@ void oref_project(const oref_params *params, const uint32_t *mask, uint32_t comp
                   float *predicted, float *velocity, float *work, uint32_t max_iterations,
                   int warm_start, int force_mg, int force_meanfree, oref_result *result);
 
+/* Fluid step without a moving interface (FluidState::step,
+ * src/fluid/mod.rs:1246-1333): predict (solver.wgsl:127-141; flags[1] =
+ * semi-Lagrangian RK2 advection), viscous (:143-163 with surface.x = 0;
+ * physical[2] = kinematic viscosity), then fields and diagnostics
+ * (:256-291).  Face buffers are vec4[nf]; em is vec4 per cell (force density
+ * in .xyz) or NULL; reserved_in vec4 per cell or NULL; cells 16 floats per
+ * cell or NULL; scalars the 12 diagnostics floats (max speed, max |div|,
+ * sum div^2, kinetic energy, max |p|, sum div, max |force|, bad cells, max
+ * face speed, melt sum, 0, 0). */
+void oref_predict(const oref_params *params, const uint32_t *mask, const float *velocity, float *predicted);
+void oref_viscous(const oref_params *params, const uint32_t *mask, const float *occupancy, const float *phase,
+                  const float *em, const float acceleration[3], const float *predicted, float *velocity);
+void oref_fields(const oref_params *params, const uint32_t *mask, const float *occupancy, const float *work,
+                 const float *velocity, const float *em, const float acceleration[3], const float *reserved_in,
+                 float *cells, float scalars[12]);
+
 /* pressure_coefficients (solver.wgsl:93-103) into velocity vec4[nf]. */
 void oref_coefficients(const oref_params *params, const uint32_t *mask, const float *occupancy,
                        const float *phase, float *velocity);

@@ -100,6 +100,11 @@ def lib():
         L.oref_apply_cached.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, _f32p, C.c_uint32, _f32p]
         L.oref_apply_uncached.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, C.c_void_p, _f32p, C.c_uint32,
                                           _f32p, _f32p]
+        L.oref_predict.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, _f32p]
+        L.oref_viscous.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, C.c_void_p, C.c_void_p, _f32p, _f32p,
+                                   _f32p]
+        L.oref_fields.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, _f32p, _f32p, C.c_void_p, _f32p,
+                                  C.c_void_p, C.c_void_p, _f32p]
         L.oref_mg_create.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, C.c_int]
         L.oref_mg_create.restype = C.c_void_p
         L.oref_mg_destroy.argtypes = [C.c_void_p]
@@ -190,6 +195,48 @@ def ref_project(params, mask, components, occupancy, predicted, max_iterations=1
                        pred.reshape(-1), vel.reshape(-1), work.reshape(-1), max_iterations, int(warm_start),
                        force_mg, force_meanfree, C.byref(res))
     return res, vel, work, pred
+
+
+def _opt(a, dtype=np.float32):
+    if a is None:
+        return None, None
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a, a.ctypes.data_as(C.c_void_p)
+
+
+def predict(params, mask, velocity):
+    """predict (solver.wgsl:127-141): vec4[nf] face records -> predicted vec4[nf]."""
+    vel = np.ascontiguousarray(velocity, np.float32).reshape(-1)
+    out = np.zeros_like(vel)
+    lib().oref_predict(C.byref(params), np.ascontiguousarray(mask, np.uint32), vel, out)
+    return out.reshape(-1, 4)
+
+
+def viscous(params, mask, occupancy, predicted, acceleration, em=None, phase=None):
+    """viscous (solver.wgsl:143-163, no moving interface): predicted vec4[nf] -> velocity vec4[nf]."""
+    pred = np.ascontiguousarray(predicted, np.float32).reshape(-1)
+    out = np.zeros_like(pred)
+    em_a, em_p = _opt(em)
+    ph_a, ph_p = _opt(phase)
+    acc = np.ascontiguousarray(acceleration, np.float32)
+    lib().oref_viscous(C.byref(params), np.ascontiguousarray(mask, np.uint32),
+                       np.ascontiguousarray(occupancy, np.float32), ph_p, em_p, acc, pred, out)
+    return out.reshape(-1, 4)
+
+
+def fields(params, mask, occupancy, work, velocity, acceleration, em=None, reserved=None, cells=True):
+    """fields + diagnostics (solver.wgsl:256-291): returns (cells (n,16) or None, scalars (12,))."""
+    n = params.dims[3]
+    em_a, em_p = _opt(em)
+    rs_a, rs_p = _opt(reserved)
+    out = np.zeros((n, 16), np.float32) if cells else None
+    sc = np.zeros(12, np.float32)
+    lib().oref_fields(C.byref(params), np.ascontiguousarray(mask, np.uint32),
+                      np.ascontiguousarray(occupancy, np.float32), np.ascontiguousarray(work, np.float32).reshape(-1),
+                      np.ascontiguousarray(velocity, np.float32).reshape(-1), em_p,
+                      np.ascontiguousarray(acceleration, np.float32), rs_p,
+                      None if out is None else out.ctypes.data_as(C.c_void_p), sc)
+    return out, sc
 
 
 # -------------------------------------------------------------------- native

@@ -1195,3 +1195,282 @@ void oref_mg_coarse_jacobi_sequence(oref_mg *mg, float *work) {
         mg_jacobi(mg, L, 1);
     }
 }
+
+/* ------------------------------------------- fluid step and fields
+ * predict, viscous, fields and diagnostics of src/fluid/solver.wgsl
+ * (:108-163, :256-291) for a step without a moving interface
+ * (FluidState::step, src/fluid/mod.rs:1246-1333).  em: vec4 per cell, the
+ * force density in .xyz (the force lanes of the EM result), or NULL;
+ * acceleration: the body acceleration of Params.acceleration. */
+
+/* em_force(): :108 */
+static void em_force(const state *s, const float *em, ivec3 pos, float out[3]) {
+    ivec3 q = wrap_cell(s, pos);
+    out[0] = out[1] = out[2] = 0.0f;
+    if (!em || !valid_cell(s, q)) return;
+    const float *f = em + LANES * idx3(q, s->p->dims);
+    out[0] = f[0];
+    out[1] = f[1];
+    out[2] = f[2];
+}
+/* sample_component()/sample_velocity(): :109-117, face(.., false) */
+static float sample_component(const state *s, const float position[3], uint32_t axis) {
+    float q[3];
+    int32_t base[3];
+    float fraction[3];
+    for (int a = 0; a < 3; a++) {
+        const float offset = (uint32_t)a == axis ? 0.0f : 0.5f;
+        q[a] = position[a] - offset;
+        const float fl = floorf(q[a]);
+        base[a] = (int32_t)fl;
+        fraction[a] = q[a] - fl; /* fract() */
+    }
+    float value = 0.0f;
+    for (int z = 0; z < 2; z++)
+        for (int y = 0; y < 2; y++)
+            for (int x = 0; x < 2; x++) {
+                const int o[3] = {x, y, z};
+                float w[3];
+                for (int a = 0; a < 3; a++) w[a] = o[a] > 0 ? fraction[a] : 1.0f - fraction[a];
+                ivec3 c = {{base[0] + x, base[1] + y, base[2] + z}};
+                value += face_value(s, c, axis, 0) * w[0] * w[1] * w[2];
+            }
+    return value;
+}
+static void sample_velocity(const state *s, const float position[3], float out[3]) {
+    for (uint32_t a = 0; a < 3; a++) out[a] = sample_component(s, position, a);
+}
+
+/* predict(): :127-141.  flags.y: semi-Lagrangian RK2 advection. */
+void oref_predict(const oref_params *params, const uint32_t *mask, const float *velocity, float *predicted) {
+    state s;
+    memset(&s, 0, sizeof s);
+    s.p = params;
+    s.mask = mask;
+    s.velocity = (float *)velocity;
+    const oref_params *p = params;
+#pragma omp parallel for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)p->faces[3]; ii++) {
+        const uint32_t i = (uint32_t)ii;
+        const ivec3 pos = decode3(i, p->faces);
+        float out[4] = {0, 0, 0, 0};
+        for (uint32_t axis = 0; axis < 3; axis++) {
+            if (!open_face(&s, pos, axis)) continue;
+            const float center = face_value(&s, pos, axis, 0);
+            float advected = center;
+            if (p->flags[1] != 0u) {
+                float at[3], v[3], mid[3], back[3], vm[3];
+                for (int a = 0; a < 3; a++) at[a] = (float)pos.v[a] + 0.5f;
+                at[axis] -= 0.5f;
+                sample_velocity(&s, at, v);
+                const float half = 0.5f * p->physical[1] / p->physical[0];
+                for (int a = 0; a < 3; a++) mid[a] = at[a] - v[a] * half;
+                sample_velocity(&s, mid, vm);
+                const float full = p->physical[1] / p->physical[0];
+                for (int a = 0; a < 3; a++) back[a] = at[a] - vm[a] * full;
+                advected = sample_component(&s, back, axis);
+            }
+            out[axis] = advected;
+        }
+        memcpy(predicted + LANES * i, out, sizeof out);
+    }
+}
+
+/* viscous(): :143-163 without a moving interface (surface.x = 0): explicit
+ * Laplacian with mirrored (no-slip) closed tangential neighbours, body and EM
+ * acceleration, times the face mobility. */
+void oref_viscous(const oref_params *params, const uint32_t *mask, const float *occupancy, const float *phase,
+                  const float *em, const float acceleration[3], const float *predicted, float *velocity) {
+    state s;
+    memset(&s, 0, sizeof s);
+    s.p = params;
+    s.mask = mask;
+    s.occ = occupancy;
+    s.phase = phase;
+    s.predicted = (float *)predicted;
+    const oref_params *p = params;
+#pragma omp parallel for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)p->faces[3]; ii++) {
+        const uint32_t i = (uint32_t)ii;
+        const ivec3 pos = decode3(i, p->faces);
+        float out[4] = {0, 0, 0, 0};
+        for (uint32_t axis = 0; axis < 3; axis++) {
+            if (!open_face(&s, pos, axis)) continue;
+            const float center = face_value(&s, pos, axis, 1);
+            float laplace = 0.0f;
+            if (p->surface[0] < 0.5f)
+                for (uint32_t d = 0; d < 3; d++)
+                    for (int sign = -1; sign <= 1; sign += 2) {
+                        ivec3 q = pos;
+                        q.v[d] += sign;
+                        float neighbor = face_value(&s, q, axis, 1);
+                        if (!open_face(&s, q, axis) && d != axis) neighbor = -center;
+                        laplace += neighbor - center;
+                    }
+            ivec3 left = pos;
+            left.v[axis] -= 1;
+            const float rho = p->physical[3];
+            float el[3], er[3];
+            em_force(&s, em, left, el);
+            em_force(&s, em, pos, er);
+            const float acc = acceleration[axis] + (el[axis] + er[axis]) / (2.0f * rho) + 0.0f;
+            const float beta = mobility(&s, pos, axis);
+            out[axis] = (center + p->physical[2] * p->physical[1] / (p->physical[0] * p->physical[0]) * laplace +
+                         p->physical[1] * acc) *
+                        beta;
+        }
+        memcpy(velocity + LANES * i, out, sizeof out);
+    }
+}
+
+/* fields() and diagnostics(): :256-291.  cells: 16 floats per cell (velocity
+ * xyz + speed, pressure + divergence, force, reserved) or NULL.  reserved_in:
+ * vec4 per cell, the cells' previous reserved lanes (y phase fraction, z
+ * liquid fraction, w curvature), or NULL for zeros.  scalars: the 12 floats
+ * diagnostics writes to scalars[2..4]. */
+void oref_fields(const oref_params *params, const uint32_t *mask, const float *occupancy, const float *work,
+                 const float *velocity, const float *em, const float acceleration[3], const float *reserved_in,
+                 float *cells, float scalars[12]) {
+    state s;
+    memset(&s, 0, sizeof s);
+    s.p = params;
+    s.mask = mask;
+    s.occ = occupancy;
+    s.velocity = (float *)velocity;
+    s.work = (float *)work;
+    const oref_params *p = params;
+    const uint32_t groups = (p->dims[3] + 255u) / 256u;
+    float *part = (float *)calloc((size_t)3 * LANES * (groups ? groups : 1), sizeof(float));
+#pragma omp parallel for schedule(static)
+    for (int64_t gg = 0; gg < (int64_t)groups; gg++) {
+        float ra[256][4], rb[256][4], rc[256][4];
+        for (uint32_t l = 0; l < 256u; l++) {
+            const uint32_t i = (uint32_t)gg * 256u + l;
+            float stats[4] = {0, 0, 0, 0}, other[4] = {0, 0, 0, 0};
+            float max_face = 0.0f, melt = 0.0f;
+            if (i < p->dims[3]) {
+                float out[16];
+                memset(out, 0, sizeof out);
+                const float *old = reserved_in ? reserved_in + LANES * i : NULL;
+                const float oy = old ? old[1] : 0.0f, oz = old ? old[2] : 0.0f, ow = old ? old[3] : 0.0f;
+                if (p->surface[0] > 0.5f) {
+                    out[13] = oy;
+                    out[14] = oz;
+                    out[15] = ow;
+                }
+                if (mask[i] != 0u) {
+                    const ivec3 pos = decode3(i, p->dims);
+                    float v[3] = {0, 0, 0}, face_energy = 0.0f;
+                    for (uint32_t axis = 0; axis < 3; axis++) {
+                        ivec3 q = pos;
+                        q.v[axis] += 1;
+                        const float a = face_value(&s, pos, axis, 0), b = face_value(&s, q, axis, 0);
+                        v[axis] = 0.5f * (a + b);
+                        face_energy += 0.5f * (a * a + b * b);
+                        max_face = fmaxf(max_face, fmaxf(fabsf(face_value(&s, pos, axis, 0)),
+                                                         fabsf(face_value(&s, q, axis, 0))));
+                    }
+                    melt = p->flags[3] != 0u ? oy : 1.0f;
+                    if (p->surface[0] > 0.5f) melt *= oz;
+                    const float speed = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+                    const float div = divergence(&s, pos, 0);
+                    const float x = work[LANES * i];
+                    const float potential_value =
+                        mean_free_pressure(&s) ? x - work[LANES * (mask[i] >> 2u)] : x;
+                    const float pressure = potential_value * p->physical[3] / p->physical[1];
+                    float force[3];
+                    em_force(&s, em, pos, force);
+                    for (int a = 0; a < 3; a++) force[a] = p->physical[3] * acceleration[a] + force[a];
+                    out[0] = v[0];
+                    out[1] = v[1];
+                    out[2] = v[2];
+                    out[3] = speed;
+                    out[4] = pressure;
+                    out[5] = div;
+                    out[8] = force[0];
+                    out[9] = force[1];
+                    out[10] = force[2];
+                    out[12] = 1.0f;
+                    out[13] = p->flags[3] != 0u ? oy : 1.0f;
+                    out[14] = oz;
+                    out[15] = ow;
+                    int bad = v[0] != v[0] || v[1] != v[1] || v[2] != v[2];
+                    bad = bad || force[0] != force[0] || force[1] != force[1] || force[2] != force[2];
+                    bad = bad || fabsf(force[0]) > 1e30f || fabsf(force[1]) > 1e30f || fabsf(force[2]) > 1e30f;
+                    bad = bad || speed > 1e25f || !(fabsf(pressure) < 1e30f) || !(fabsf(div) < 1e30f);
+                    const float rho = p->surface[0] > 0.5f ? density(&s, pos) : p->physical[3];
+                    stats[0] = speed;
+                    stats[1] = fabsf(div);
+                    stats[2] = div * div;
+                    stats[3] = 0.5f * rho * face_energy * p->physical[0] * p->physical[0] * p->physical[0];
+                    other[0] = fabsf(pressure);
+                    other[1] = div;
+                    other[2] = sqrtf(force[0] * force[0] + force[1] * force[1] + force[2] * force[2]);
+                    other[3] = bad ? 1.0f : 0.0f;
+                }
+                if (cells) memcpy(cells + 16 * (size_t)i, out, sizeof out);
+            }
+            memcpy(ra[l], stats, sizeof stats);
+            memcpy(rb[l], other, sizeof other);
+            rc[l][0] = max_face;
+            rc[l][1] = melt;
+            rc[l][2] = rc[l][3] = 0.0f;
+        }
+        for (uint32_t st = 128u; st > 0u; st /= 2u)
+            for (uint32_t l = 0; l < st; l++) {
+                ra[l][0] = fmaxf(ra[l][0], ra[l + st][0]);
+                ra[l][1] = fmaxf(ra[l][1], ra[l + st][1]);
+                ra[l][2] += ra[l + st][2];
+                ra[l][3] += ra[l + st][3];
+                rb[l][0] = fmaxf(rb[l][0], rb[l + st][0]);
+                rb[l][1] += rb[l + st][1];
+                rb[l][2] = fmaxf(rb[l][2], rb[l + st][2]);
+                rb[l][3] += rb[l + st][3];
+                rc[l][0] = fmaxf(rc[l][0], rc[l + st][0]);
+                rc[l][1] += rc[l + st][1];
+                rc[l][2] = rc[l][3] = 0.0f;
+            }
+        memcpy(part + LANES * gg, ra[0], 4 * sizeof(float));
+        memcpy(part + LANES * (groups + gg), rb[0], 4 * sizeof(float));
+        memcpy(part + LANES * (2 * groups + gg), rc[0], 4 * sizeof(float));
+    }
+    /* diagnostics(): one workgroup, 256-stride loop, then the tree */
+    float ra[256][4], rb[256][4], rc[256][4];
+    for (uint32_t l = 0; l < 256u; l++) {
+        float a[4] = {0, 0, 0, 0}, b[4] = {0, 0, 0, 0}, c[4] = {0, 0, 0, 0};
+        for (uint32_t i = l; i < groups; i += 256u) {
+            const float *fs = part + LANES * (2 * groups + i), *x = part + LANES * i, *y = part + LANES * (groups + i);
+            c[0] = fmaxf(c[0], fs[0]);
+            c[1] = c[1] + fs[1];
+            a[0] = fmaxf(a[0], x[0]);
+            a[1] = fmaxf(a[1], x[1]);
+            a[2] = a[2] + x[2];
+            a[3] = a[3] + x[3];
+            b[0] = fmaxf(b[0], y[0]);
+            b[1] = b[1] + y[1];
+            b[2] = fmaxf(b[2], y[2]);
+            b[3] = b[3] + y[3];
+        }
+        memcpy(ra[l], a, sizeof a);
+        memcpy(rb[l], b, sizeof b);
+        memcpy(rc[l], c, sizeof c);
+    }
+    for (uint32_t st = 128u; st > 0u; st /= 2u)
+        for (uint32_t l = 0; l < st; l++) {
+            ra[l][0] = fmaxf(ra[l][0], ra[l + st][0]);
+            ra[l][1] = fmaxf(ra[l][1], ra[l + st][1]);
+            ra[l][2] += ra[l + st][2];
+            ra[l][3] += ra[l + st][3];
+            rb[l][0] = fmaxf(rb[l][0], rb[l + st][0]);
+            rb[l][1] += rb[l + st][1];
+            rb[l][2] = fmaxf(rb[l][2], rb[l + st][2]);
+            rb[l][3] += rb[l + st][3];
+            rc[l][0] = fmaxf(rc[l][0], rc[l + st][0]);
+            rc[l][1] += rc[l + st][1];
+            rc[l][2] = rc[l][3] = 0.0f;
+        }
+    memcpy(scalars, ra[0], 4 * sizeof(float));
+    memcpy(scalars + 4, rb[0], 4 * sizeof(float));
+    memcpy(scalars + 8, rc[0], 4 * sizeof(float));
+    free(part);
+}

@@ -1,0 +1,97 @@
+"""The oracle's restatement of the fluid step and fields (predict, viscous,
+fields/diagnostics of src/fluid/solver.wgsl:127-163, :256-291) against
+analytic answers: no advection copies the open faces, a uniform periodic
+flow is advected onto itself, a fluid at rest gains dt * g on every open face,
+a uniform flow's diagnostics are its speed, zero divergence and its kinetic
+energy, and solid walls close their faces."""
+import numpy as np
+
+import refcases as R
+
+
+def _params(oracle, dims, h, dt, periodic, nu=0.0, advection=False, fluid=None):
+    n = dims[0] * dims[1] * dims[2]
+    p = oracle.make_params(dims, h, dt, 1000.0, 1000.0, False, periodic, 1e-5, 1e-5, n if fluid is None else fluid,
+                           False, 1e6)
+    p.physical[2] = nu
+    p.flags[1] = int(advection)
+    return p
+
+
+def _uniform(dims, U):
+    nx, ny, nz = dims
+    return (np.full((nz, ny, nx + 1), U[0], np.float32), np.full((nz, ny + 1, nx), U[1], np.float32),
+            np.full((nz + 1, ny, nx), U[2], np.float32))
+
+
+def test_predict_without_advection_copies_open_faces(oracle_lib):
+    dims = (6, 5, 4)
+    rng = np.random.default_rng(1)
+    solid = (rng.random(dims[::-1]) < 0.2).astype(np.uint8)
+    comps, mask = oracle_lib.anchors((solid.reshape(-1) == 0).astype(np.uint32), dims, 0)
+    u = tuple(rng.standard_normal(s).astype(np.float32) for s in ((4, 5, 7), (4, 6, 6), (5, 5, 6)))
+    rec = R.soa_to_records(dims, *u)
+    p = _params(oracle_lib, dims, 1e-3, 1e-4, 0)
+    out = oracle_lib.predict(p, mask, rec)
+    # a face is open when both cells beside it are fluid and it is inside the domain
+    f = (solid == 0)
+    want = np.zeros_like(rec).reshape(dims[2] + 1, dims[1] + 1, dims[0] + 1, 4)
+    uu = np.asarray(u[0])
+    for z in range(dims[2]):
+        for y in range(dims[1]):
+            for x in range(1, dims[0]):
+                if f[z, y, x - 1] and f[z, y, x]:
+                    want[z, y, x, 0] = uu[z, y, x]
+    np.testing.assert_array_equal(out.reshape(want.shape)[..., 0], want[..., 0])
+
+
+def test_uniform_periodic_flow_is_advected_onto_itself(oracle_lib):
+    dims = (8, 6, 5)
+    U = (0.3, -0.2, 0.1)
+    p = _params(oracle_lib, dims, 1e-3, 1e-3, 7, advection=True)
+    mask = np.ones(dims[0] * dims[1] * dims[2], np.uint32)
+    out = oracle_lib.predict(p, mask, R.soa_to_records(dims, *_uniform(dims, U)))
+    got = R.records_to_soa(dims, out)
+    for a in range(3):
+        np.testing.assert_allclose(got[a], U[a], rtol=1e-6)
+
+
+def test_fluid_at_rest_gains_gravity(oracle_lib):
+    dims = (5, 4, 6)
+    dt = 1e-3
+    g = np.array([0.0, 1.5, -9.81], np.float32)
+    nx, ny, nz = dims
+    solid = np.zeros((nz, ny, nx), np.uint8)
+    solid[:, :, 0] = 1
+    comps, mask = oracle_lib.anchors((solid.reshape(-1) == 0).astype(np.uint32), dims, 0)
+    p = _params(oracle_lib, dims, 1e-3, dt, 0, nu=1e-3)
+    n = nx * ny * nz
+    zero = np.zeros(((nx + 1) * (ny + 1) * (nz + 1), 4), np.float32)
+    out = oracle_lib.viscous(p, mask, np.ones(n, np.float32), zero, g)
+    u, v, w = R.records_to_soa(dims, out)
+    assert np.all(u == 0.0)  # the only x faces inside the domain touch the solid column or are walls
+    inner_v = v[:, 1:ny, 1:]
+    np.testing.assert_array_equal(inner_v, np.float32(dt) * g[1])
+    inner_w = w[1:nz, :, 1:]
+    np.testing.assert_array_equal(inner_w, np.float32(dt) * g[2])
+    assert np.all(v[:, 0, :] == 0.0) and np.all(w[0] == 0.0) and np.all(w[nz] == 0.0)
+
+
+def test_uniform_flow_diagnostics(oracle_lib):
+    dims = (8, 8, 4)
+    h, dt, rho = 1e-3, 1e-4, 1000.0
+    U = np.array([0.3, -0.4, 0.0], np.float32)
+    p = _params(oracle_lib, dims, h, dt, 7)
+    n = dims[0] * dims[1] * dims[2]
+    mask = np.ones(n, np.uint32)
+    work = np.zeros((n, 4), np.float32)
+    cells, sc = oracle_lib.fields(p, mask, np.ones(n, np.float32), work,
+                                  R.soa_to_records(dims, *_uniform(dims, U)), np.zeros(3, np.float32))
+    speed = float(np.linalg.norm(U))
+    np.testing.assert_allclose(cells[:, 3], speed, rtol=1e-6)
+    assert np.all(cells[:, 5] == 0.0)  # divergence
+    np.testing.assert_allclose(sc[0], speed, rtol=1e-6)
+    assert sc[1] == 0.0 and sc[2] == 0.0 and sc[7] == 0.0
+    np.testing.assert_allclose(sc[3], 0.5 * rho * speed ** 2 * h ** 3 * n, rtol=1e-5)
+    np.testing.assert_allclose(sc[8], 0.4, rtol=1e-6)  # max face speed
+    assert sc[9] == n  # melt fraction 1 in every fluid cell
