@@ -1245,10 +1245,10 @@ extern "C" int mhdproj_fluid_step(mhdproj_ctx* ctx, float* u, float* v, float* w
     StepView sv = base;
     sv.advection = sp->advection != 0;
     sv.nu = sp->kinematic_viscosity;
-    launch_predict(sv, ctx->st_pred, ctx->stream);
+    launch_predict(sv, ctx->st_pred, ctx->st_star, ctx->stream);
     for (int a = 0; a < 3; a++) sv.vel[a] = ctx->st_pred[a];
     launch_viscous(sv, ctx->st_star, ctx->stream);
-    ctx->launches += 6;
+    ctx->launches += 9;
     CK(cudaGetLastError());
     ctx->step_ran = true;
     ctx->step_dt = dt;
@@ -1377,7 +1377,7 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
                                             ctx->step_dt);
                     sv.advection = 1;
                     sv.nu = ctx->step_nu;
-                    if (it.kind == 20) launch_predict(sv, ctx->st_pred, s);
+                    if (it.kind == 20) launch_predict(sv, ctx->st_pred, ctx->st_star, s);
                     if (it.kind == 21) {
                         for (int a = 0; a < 3; a++) sv.vel[a] = ctx->st_pred[a];
                         launch_viscous(sv, ctx->st_star, s);

@@ -200,7 +200,8 @@ struct StepView {
     const float* phi;       // pressure potential, element i at phi[i * phi_stride]
     int phi_stride;
 };
-void launch_predict(const StepView& s, float* const out[3], cudaStream_t st);
+// masked: three face arrays of scratch (face() of every position)
+void launch_predict(const StepView& s, float* const out[3], float* const masked[3], cudaStream_t st);
 void launch_viscous(const StepView& s, float* const out[3], cudaStream_t st);
 uint32_t fields_groups(const StepView& s);
 // partials: 3 * fields_groups float4; scalars3: 3 float4 (the 12 diagnostics floats)

@@ -5,9 +5,11 @@
 // Each kernel restates one WGSL entry point of src/fluid/solver.wgsl for a
 // step without a moving interface (FluidState::step, src/fluid/mod.rs:
 // 1246-1333):
+//   ks_open_faces   face() of every face position (zero where closed,
+//                   periodic positions canonical), once per step;
 //   ks_predict      predict (:127-141): u at the face, or with advection the
 //                   value at the RK2 departure point, trilinear in the face
-//                   grid of that axis;
+//                   grid of that axis, sampled from those arrays;
 //   ks_viscous      viscous (:143-163): explicit 6-neighbour Laplacian
 //                   (closed tangential neighbours mirrored: no slip), body and
 //                   EM acceleration, times the face mobility;
@@ -87,6 +89,21 @@ __device__ __forceinline__ float face(const StepView& s, P3 pos, int axis) {
     if (!open_face(s, q, axis)) return 0.0f;
     return s.vel[axis][face_index(s, q, axis)];
 }
+// face() over an array that already holds face() of every SoA position
+// (closed faces zero, periodic positions canonical): only the wrap and the
+// domain test remain.
+__device__ __forceinline__ float face_masked(const StepView& s, const float* __restrict__ arr, P3 c, int axis) {
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int n = (int)s.dims[a];
+        if (s.periodic & (1u << a)) {
+            if (c.v[a] < 0 || c.v[a] >= n) c.v[a] = wrap_periodic(c.v[a], (uint32_t)n);
+        } else if (c.v[a] < 0 || c.v[a] >= n + (a == axis ? 1 : 0)) {
+            return 0.0f;
+        }
+    }
+    return __ldg(arr + face_index(s, c, axis));
+}
 __device__ __forceinline__ float occupancy(const StepView& s, P3 pos) {
     const P3 q = wrap_cell(s, pos);
     if (!valid_cell(s, q) || !s.occ) return 0.0f;
@@ -120,8 +137,11 @@ __device__ __forceinline__ float em_force(const StepView& s, P3 pos, int axis) {
     const float4 f = s.em[cell_index(s, q)];
     return axis == 0 ? f.x : (axis == 1 ? f.y : f.z);
 }
-// sample_component (:109-116): trilinear in the face grid of `axis`.
-__device__ float sample_component(const StepView& s, const float position[3], int axis) {
+// sample_component (:109-116): trilinear in the face grid of `axis`, over
+// the masked face arrays m[3].  When all eight taps lie inside the grid
+// without a periodic wrap they are read at fixed strides from one index;
+// either way the products and sums are the same operations in the same order.
+__device__ float sample_component(const StepView& s, const float* const* m, const float position[3], int axis) {
     int base[3];
     float fraction[3];
     for (int a = 0; a < 3; a++) {
@@ -130,7 +150,35 @@ __device__ float sample_component(const StepView& s, const float position[3], in
         base[a] = (int)fl;
         fraction[a] = q - fl;  // fract()
     }
+    const float* __restrict__ arr = m[axis];
+    bool inside = true;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int hi = (s.periodic & (1u << a)) ? (int)s.dims[a] : (int)s.dims[a] + (a == axis ? 1 : 0);
+        inside = inside && base[a] >= 0 && base[a] + 1 < hi;
+    }
     float value = 0.0f;
+    if (inside) {
+        P3 b;
+        b.v[0] = base[0];
+        b.v[1] = base[1];
+        b.v[2] = base[2];
+        const uint32_t i0 = face_index(s, b, axis);
+        const uint32_t row = s.dims[0] + (axis == 0 ? 1u : 0u);
+        const uint32_t plane = row * (s.dims[1] + (axis == 1 ? 1u : 0u));
+#pragma unroll
+        for (int z = 0; z < 2; z++)
+#pragma unroll
+            for (int y = 0; y < 2; y++)
+#pragma unroll
+                for (int x = 0; x < 2; x++) {
+                    const float wx = x ? fraction[0] : 1.0f - fraction[0];
+                    const float wy = y ? fraction[1] : 1.0f - fraction[1];
+                    const float wz = z ? fraction[2] : 1.0f - fraction[2];
+                    value += __ldg(arr + i0 + (uint32_t)x + (uint32_t)y * row + (uint32_t)z * plane) * wx * wy * wz;
+                }
+        return value;
+    }
 #pragma unroll
     for (int z = 0; z < 2; z++)
 #pragma unroll
@@ -144,7 +192,7 @@ __device__ float sample_component(const StepView& s, const float position[3], in
                 c.v[0] = base[0] + x;
                 c.v[1] = base[1] + y;
                 c.v[2] = base[2] + z;
-                value += face(s, c, axis) * wx * wy * wz;
+                value += face_masked(s, arr, c, axis) * wx * wy * wz;
             }
     return value;
 }
@@ -159,26 +207,36 @@ __device__ __forceinline__ bool face_position(const StepView& s, int axis, uint3
     return true;
 }
 
-__global__ void ks_predict(StepView s, int axis, float* __restrict__ out) {
+// face() of every SoA position of one axis: the sampling arrays of predict.
+__global__ void ks_open_faces(StepView s, int axis, float* __restrict__ out) {
     const uint32_t f = blockIdx.x * WG + threadIdx.x;
     P3 pos;
     if (!face_position(s, axis, f, &pos)) return;
+    out[f] = face(s, pos, axis);
+}
+
+__global__ void ks_predict(StepView s, const float* __restrict__ m0, const float* __restrict__ m1,
+                           const float* __restrict__ m2, int axis, float* __restrict__ out) {
+    const uint32_t f = blockIdx.x * WG + threadIdx.x;
+    P3 pos;
+    if (!face_position(s, axis, f, &pos)) return;
+    const float* m[3] = {m0, m1, m2};
     float value = 0.0f;
     if (open_face(s, pos, axis)) {
-        const float center = face(s, pos, axis);
+        const float center = face_masked(s, m[axis], pos, axis);
         value = center;
         if (s.advection) {
             float at[3];
             for (int a = 0; a < 3; a++) at[a] = (float)pos.v[a] + 0.5f;
             at[axis] -= 0.5f;
             float v[3], mid[3], vm[3], back[3];
-            for (int a = 0; a < 3; a++) v[a] = sample_component(s, at, a);
+            for (int a = 0; a < 3; a++) v[a] = sample_component(s, m, at, a);
             const float half = 0.5f * s.dt / s.h;
             for (int a = 0; a < 3; a++) mid[a] = at[a] - v[a] * half;
-            for (int a = 0; a < 3; a++) vm[a] = sample_component(s, mid, a);
+            for (int a = 0; a < 3; a++) vm[a] = sample_component(s, m, mid, a);
             const float full = s.dt / s.h;
             for (int a = 0; a < 3; a++) back[a] = at[a] - vm[a] * full;
-            value = sample_component(s, back, axis);
+            value = sample_component(s, m, back, axis);
         }
     }
     out[f] = value;
@@ -190,14 +248,16 @@ __global__ void ks_viscous(StepView s, int axis, float* __restrict__ out) {
     if (!face_position(s, axis, f, &pos)) return;
     float value = 0.0f;
     if (open_face(s, pos, axis)) {
-        const float center = face(s, pos, axis);
+        // the predicted arrays hold face() of every position (predict writes
+        // zero on closed faces and the canonical value on periodic ones)
+        const float center = face_masked(s, s.vel[axis], pos, axis);
         float laplace = 0.0f;
         if (!s.two_phase)
             for (int d = 0; d < 3; d++)
                 for (int sign = -1; sign <= 1; sign += 2) {
                     P3 q = pos;
                     q.v[d] += sign;
-                    float neighbor = face(s, q, axis);
+                    float neighbor = face_masked(s, s.vel[axis], q, axis);
                     if (!open_face(s, q, axis) && d != axis) neighbor = -center;
                     laplace += neighbor - center;
                 }
@@ -329,8 +389,10 @@ static unsigned face_blocks(const StepView& s, int axis) {
     return (unsigned)((d[0] * d[1] * d[2] + WG - 1) / WG);
 }
 
-void launch_predict(const StepView& s, float* const out[3], cudaStream_t st) {
-    for (int a = 0; a < 3; a++) ks_predict<<<face_blocks(s, a), WG, 0, st>>>(s, a, out[a]);
+void launch_predict(const StepView& s, float* const out[3], float* const masked[3], cudaStream_t st) {
+    for (int a = 0; a < 3; a++) ks_open_faces<<<face_blocks(s, a), WG, 0, st>>>(s, a, masked[a]);
+    for (int a = 0; a < 3; a++)
+        ks_predict<<<face_blocks(s, a), WG, 0, st>>>(s, masked[0], masked[1], masked[2], a, out[a]);
 }
 void launch_viscous(const StepView& s, float* const out[3], cudaStream_t st) {
     for (int a = 0; a < 3; a++) ks_viscous<<<face_blocks(s, a), WG, 0, st>>>(s, a, out[a]);
