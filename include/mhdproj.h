@@ -297,6 +297,19 @@ int mhdproj_fluid_step(mhdproj_ctx *ctx, float *u, float *v, float *w, const flo
                        const mhdproj_step_params *params, float *p_out, float *cells, mhdproj_stats *stats,
                        mhdproj_diagnostics *diagnostics);
 
+/* RunState::export_fields (src/run/export.rs:9-60) for the fluid: writes the
+ * cell records (device array of 16 floats per cell, as filled by
+ * mhdproj_fields or mhdproj_fluid_step) to <directory>/fluid.bin unchanged
+ * (x fastest, then y, then z; host byte order) and publishes
+ * <directory>/metadata.json (format_version 1, step, time_s, origin_m,
+ * cell_m, dims, byte_order, cell_order, files, moving_interface,
+ * forcing_kind) last, by renaming metadata.writing.  The directory must be
+ * new ("Create new frame directory <dir>: <reason>" otherwise, read with
+ * mhdproj_last_error(NULL)); on any failure the directory created by the call
+ * is removed.  origin_m may be NULL (zeros); forcing_kind NULL means "none". */
+int mhdproj_export_fields(const mhdproj_grid *grid, const float *cells, const char *directory, uint64_t step,
+                          double time_s, const float origin_m[3], int moving_interface, const char *forcing_kind);
+
 /* Host utilities, mirroring src/fluid/multigrid.rs:25-65 and src/fluid/mod.rs:1447-1493. */
 /* Aggregation hierarchy: halve (ceil) until every dimension is <= 4.  Returns
  * 0 and the level count / coarse-cell total, or MHDPROJ_ERR_INVALID for zero,

@@ -133,6 +133,8 @@ def load():
                                                      C.POINTER(Diagnostics)]
     L.mhdproj_fluid_step.argtypes = [_vp] + [_vp] * 4 + [C.POINTER(StepParams), _vp, _vp, C.POINTER(Stats),
                                                          C.POINTER(Diagnostics)]
+    L.mhdproj_export_fields.argtypes = [C.POINTER(Grid), _vp, C.c_char_p, C.c_uint64, C.c_double,
+                                        C.POINTER(C.c_float * 3), C.c_int, C.c_char_p]
     _lib = L
     return L
 
@@ -143,7 +145,7 @@ EXPORTED = [
     "mhdproj_project_vjp", "mhdproj_chain_forward", "mhdproj_chain_backward", "mhdproj_apply_operator",
     "mhdproj_apply_preconditioner", "mhdproj_copy_coefficients", "mhdproj_copy_potential", "mhdproj_copy_topology",
     "mhdproj_hierarchy", "mhdproj_anchors", "mhdproj_profile_kernels", "mhdproj_divergence_noalloc",
-    "mhdproj_kernel_launches", "mhdproj_fields", "mhdproj_fluid_step",
+    "mhdproj_kernel_launches", "mhdproj_fields", "mhdproj_fluid_step", "mhdproj_export_fields",
 ]
 
 
@@ -162,6 +164,19 @@ def divergence_noalloc(dims, h, solid, u, v, w, stream=None):
     if rc:
         raise ProjectionError(rc, L.mhdproj_last_error(None).decode())
     return out[0], out[1]
+
+
+def export_fields(dims, h, cells, directory, step=0, time_s=0.0, origin_m=(0.0, 0.0, 0.0), moving_interface=False,
+                  forcing_kind="none"):
+    """Write a frame directory (fluid.bin + metadata.json) from device cell
+    records (mhdproj_export_fields); raises ProjectionError on failure."""
+    L = load()
+    g = Grid(int(dims[0]), int(dims[1]), int(dims[2]), float(h), 0, 0)
+    o = (C.c_float * 3)(*origin_m)
+    rc = L.mhdproj_export_fields(C.byref(g), _ptr(cells), os.fsencode(directory), int(step), float(time_s),
+                                 C.byref(o), int(bool(moving_interface)), forcing_kind.encode())
+    if rc:
+        raise ProjectionError(rc, L.mhdproj_last_error(None).decode())
 
 
 def hierarchy(dims4):

@@ -25,7 +25,7 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler"
 EXACT = {"reference_kernels.cu", "step_kernels.cu"}
 
 SOURCES = ["context.cu", "gb300_kernels.cu", "fine_kernels.cu", "fused_kernels.cu", "mg_kernels.cu", "reference_kernels.cu", "noalloc.cu",
-           "topology_kernels.cu", "step_kernels.cu"]
+           "topology_kernels.cu", "step_kernels.cu", "export_fields.cu"]
 HOST_SOURCES = ["topology.cpp"]
 
 

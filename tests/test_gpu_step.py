@@ -285,3 +285,34 @@ def test_gb300_step_stages(gpu, oracle_lib):
     assert d["max_divergence_s_inv"] == db["max_divergence_s_inv"]
     a.close()
     b.close()
+
+
+def test_export_fields_round_trip(gpu, oracle_lib, tmp_path):
+    """export_fields (src/run/export.rs:9-60): fluid.bin holds the cell
+    records byte for byte, metadata.json is published, and an existing frame
+    directory is refused and left intact."""
+    import json
+
+    import mhdproj
+
+    torch = gpu
+    c = single_phase(R.wall_case((17, 13, 9), (0, 0, 0), True, False), dt=0.02)
+    pr = make_ref_ctx(mhdproj, torch, c, "jacobi")
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    u = [t(c["u"]), t(c["v"]), t(c["w"])]
+    cells = torch.zeros(pr.cell_shape() + (16,), dtype=torch.float32, device="cuda")
+    pr.fluid_step(u, c["dt"], acceleration=(0.0, 0.0, -9.81), viscosity=0.1, advection=True, cells=cells)
+    frame = tmp_path / "run" / "frame-00000001"
+    mhdproj.export_fields(c["dims"], c["h"], cells, str(frame), step=1, time_s=0.02, forcing_kind="none")
+    raw = (frame / "fluid.bin").read_bytes()
+    assert raw == cells.cpu().numpy().tobytes()
+    meta = json.loads((frame / "metadata.json").read_text())
+    n = c["dims"][0] * c["dims"][1] * c["dims"][2]
+    assert meta["format_version"] == 1 and meta["step"] == 1 and meta["dims"] == list(c["dims"])
+    assert meta["files"] == [{"physics": "fluid", "file": "fluid.bin", "bytes": n * 64, "f32_components_per_cell": 16}]
+    assert meta["cell_order"] == "x fastest, then y, then z" and not (frame / "metadata.writing").exists()
+    with pytest.raises(mhdproj.ProjectionError) as e:
+        mhdproj.export_fields(c["dims"], c["h"], torch.zeros_like(cells), str(frame), step=2)
+    assert "Create new frame directory" in str(e.value)
+    assert (frame / "fluid.bin").read_bytes() == raw
+    pr.close()
