@@ -93,6 +93,7 @@ struct mhdproj_ctx {
     // reduction partials, and the last fields pass's CFL inputs
     float *st_prev[3] = {nullptr, nullptr, nullptr}, *st_pred[3] = {nullptr, nullptr, nullptr};
     float *st_star[3] = {nullptr, nullptr, nullptr}, *st_prev_p = nullptr;
+    uint8_t* st_open[3] = {nullptr, nullptr, nullptr};
     float4* st_partials = nullptr;
     float4* st_scalars = nullptr;
     float4* h_st_scalars = nullptr;
@@ -1096,6 +1097,7 @@ static int step_buffers(mhdproj_ctx* ctx) {
         CK(dalloc(ctx, &ctx->st_prev[a], nf[a] * 4));
         CK(dalloc(ctx, &ctx->st_pred[a], nf[a] * 4));
         CK(dalloc(ctx, &ctx->st_star[a], nf[a] * 4));
+        CK(dalloc(ctx, &ctx->st_open[a], nf[a]));
     }
     CK(dalloc(ctx, &ctx->st_prev_p, ctx->n * 4));
     CK(dalloc(ctx, &ctx->st_partials, (size_t)3 * ((ctx->n + 255) / 256) * sizeof(float4)));
@@ -1245,8 +1247,11 @@ extern "C" int mhdproj_fluid_step(mhdproj_ctx* ctx, float* u, float* v, float* w
     StepView sv = base;
     sv.advection = sp->advection != 0;
     sv.nu = sp->kinematic_viscosity;
-    launch_predict(sv, ctx->st_pred, ctx->st_star, ctx->stream);
-    for (int a = 0; a < 3; a++) sv.vel[a] = ctx->st_pred[a];
+    launch_predict(sv, ctx->st_pred, ctx->st_star, ctx->st_open, ctx->stream);
+    for (int a = 0; a < 3; a++) {
+        sv.vel[a] = ctx->st_pred[a];
+        sv.open[a] = ctx->st_open[a];
+    }
     launch_viscous(sv, ctx->st_star, ctx->stream);
     ctx->launches += 9;
     CK(cudaGetLastError());
@@ -1377,9 +1382,12 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
                                             ctx->step_dt);
                     sv.advection = 1;
                     sv.nu = ctx->step_nu;
-                    if (it.kind == 20) launch_predict(sv, ctx->st_pred, ctx->st_star, s);
+                    if (it.kind == 20) launch_predict(sv, ctx->st_pred, ctx->st_star, ctx->st_open, s);
                     if (it.kind == 21) {
-                        for (int a = 0; a < 3; a++) sv.vel[a] = ctx->st_pred[a];
+                        for (int a = 0; a < 3; a++) {
+                            sv.vel[a] = ctx->st_pred[a];
+                            sv.open[a] = ctx->st_open[a];
+                        }
                         launch_viscous(sv, ctx->st_star, s);
                     }
                     if (it.kind == 22) launch_fields(sv, nullptr, ctx->st_partials, ctx->st_scalars, s);

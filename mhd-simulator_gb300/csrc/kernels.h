@@ -196,12 +196,15 @@ struct StepView {
     const float* occ;       // liquid fraction or null
     const float* phase;     // thermal phase fraction (phase drag) or null
     const float* vel[3];    // face arrays read by face()
+    const uint8_t* open[3]; // open_face() flags per face position (viscous)
     const float4* em;       // EM force density per cell (xyz) or null
     const float* phi;       // pressure potential, element i at phi[i * phi_stride]
     int phi_stride;
 };
-// masked: three face arrays of scratch (face() of every position)
-void launch_predict(const StepView& s, float* const out[3], float* const masked[3], cudaStream_t st);
+// masked / open: three face arrays of scratch each (face() and open_face()
+// of every position); viscous reads the open flags through StepView::open
+void launch_predict(const StepView& s, float* const out[3], float* const masked[3], uint8_t* const open[3],
+                    cudaStream_t st);
 void launch_viscous(const StepView& s, float* const out[3], cudaStream_t st);
 uint32_t fields_groups(const StepView& s);
 // partials: 3 * fields_groups float4; scalars3: 3 float4 (the 12 diagnostics floats)

@@ -5,14 +5,16 @@
 // Each kernel restates one WGSL entry point of src/fluid/solver.wgsl for a
 // step without a moving interface (FluidState::step, src/fluid/mod.rs:
 // 1246-1333):
-//   ks_open_faces   face() of every face position (zero where closed,
-//                   periodic positions canonical), once per step;
+//   ks_open_faces   face() and open_face() of every face position (zero
+//                   where closed, periodic positions canonical), once per
+//                   step;
 //   ks_predict      predict (:127-141): u at the face, or with advection the
 //                   value at the RK2 departure point, trilinear in the face
 //                   grid of that axis, sampled from those arrays;
 //   ks_viscous      viscous (:143-163): explicit 6-neighbour Laplacian
 //                   (closed tangential neighbours mirrored: no slip), body and
-//                   EM acceleration, times the face mobility;
+//                   EM acceleration, times the face mobility; the open tests
+//                   read the flags of ks_open_faces;
 //   ks_fields       fields (:256-285): the 16-float cell record (velocity and
 //                   speed, pressure and divergence, force, reserved) and the
 //                   per-workgroup max/sum reductions;
@@ -104,6 +106,20 @@ __device__ __forceinline__ float face_masked(const StepView& s, const float* __r
     }
     return __ldg(arr + face_index(s, c, axis));
 }
+// open_face() from the flags ks_open_faces wrote, with face_masked's wrap
+// and domain test.
+__device__ __forceinline__ bool open_masked(const StepView& s, const uint8_t* __restrict__ open, P3 c, int axis) {
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int n = (int)s.dims[a];
+        if (s.periodic & (1u << a)) {
+            if (c.v[a] < 0 || c.v[a] >= n) c.v[a] = wrap_periodic(c.v[a], (uint32_t)n);
+        } else if (c.v[a] < 0 || c.v[a] >= n + (a == axis ? 1 : 0)) {
+            return false;
+        }
+    }
+    return __ldg(open + face_index(s, c, axis)) != 0;
+}
 __device__ __forceinline__ float occupancy(const StepView& s, P3 pos) {
     const P3 q = wrap_cell(s, pos);
     if (!valid_cell(s, q) || !s.occ) return 0.0f;
@@ -141,7 +157,10 @@ __device__ __forceinline__ float em_force(const StepView& s, P3 pos, int axis) {
 // the masked face arrays m[3].  When all eight taps lie inside the grid
 // without a periodic wrap they are read at fixed strides from one index;
 // either way the products and sums are the same operations in the same order.
-__device__ float sample_component(const StepView& s, const float* const* m, const float position[3], int axis) {
+// One out-of-line copy: seven inlined, unrolled samplers overflow the
+// instruction cache.
+__device__ __noinline__ float sample_component(const StepView& s, const float* const* m, const float position[3],
+                                               int axis) {
     int base[3];
     float fraction[3];
     for (int a = 0; a < 3; a++) {
@@ -207,12 +226,14 @@ __device__ __forceinline__ bool face_position(const StepView& s, int axis, uint3
     return true;
 }
 
-// face() of every SoA position of one axis: the sampling arrays of predict.
-__global__ void ks_open_faces(StepView s, int axis, float* __restrict__ out) {
+// face() and open_face() of every SoA position of one axis: the sampling
+// arrays of predict and the open flags of viscous.
+__global__ void ks_open_faces(StepView s, int axis, float* __restrict__ out, uint8_t* __restrict__ open) {
     const uint32_t f = blockIdx.x * WG + threadIdx.x;
     P3 pos;
     if (!face_position(s, axis, f, &pos)) return;
     out[f] = face(s, pos, axis);
+    open[f] = open_face(s, pos, axis) ? 1 : 0;
 }
 
 __global__ void ks_predict(StepView s, const float* __restrict__ m0, const float* __restrict__ m1,
@@ -230,9 +251,11 @@ __global__ void ks_predict(StepView s, const float* __restrict__ m0, const float
             for (int a = 0; a < 3; a++) at[a] = (float)pos.v[a] + 0.5f;
             at[axis] -= 0.5f;
             float v[3], mid[3], vm[3], back[3];
+#pragma unroll 1
             for (int a = 0; a < 3; a++) v[a] = sample_component(s, m, at, a);
             const float half = 0.5f * s.dt / s.h;
             for (int a = 0; a < 3; a++) mid[a] = at[a] - v[a] * half;
+#pragma unroll 1
             for (int a = 0; a < 3; a++) vm[a] = sample_component(s, m, mid, a);
             const float full = s.dt / s.h;
             for (int a = 0; a < 3; a++) back[a] = at[a] - vm[a] * full;
@@ -246,21 +269,46 @@ __global__ void ks_viscous(StepView s, int axis, float* __restrict__ out) {
     const uint32_t f = blockIdx.x * WG + threadIdx.x;
     P3 pos;
     if (!face_position(s, axis, f, &pos)) return;
+    const uint8_t* __restrict__ open = s.open[axis];
     float value = 0.0f;
-    if (open_face(s, pos, axis)) {
+    if (open[f]) {  // open_face(pos, axis)
         // the predicted arrays hold face() of every position (predict writes
         // zero on closed faces and the canonical value on periodic ones)
-        const float center = face_masked(s, s.vel[axis], pos, axis);
+        const float* __restrict__ vel = s.vel[axis];
+        bool interior = true;  // all six neighbours in the array without a wrap
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const int hi = (s.periodic & (1u << a)) ? (int)s.dims[a] : (int)s.dims[a] + (a == axis ? 1 : 0);
+            interior = interior && pos.v[a] >= 1 && pos.v[a] + 1 < hi;
+        }
+        const float center = interior ? __ldg(vel + f) : face_masked(s, vel, pos, axis);
         float laplace = 0.0f;
-        if (!s.two_phase)
-            for (int d = 0; d < 3; d++)
-                for (int sign = -1; sign <= 1; sign += 2) {
-                    P3 q = pos;
-                    q.v[d] += sign;
-                    float neighbor = face_masked(s, s.vel[axis], q, axis);
-                    if (!open_face(s, q, axis) && d != axis) neighbor = -center;
-                    laplace += neighbor - center;
-                }
+        if (!s.two_phase) {
+            if (interior) {
+                const uint32_t row = s.dims[0] + (axis == 0 ? 1u : 0u);
+                const uint32_t step[3] = {1u, row, row * (s.dims[1] + (axis == 1 ? 1u : 0u))};
+#pragma unroll
+                for (int d = 0; d < 3; d++)
+#pragma unroll
+                    for (int sign = -1; sign <= 1; sign += 2) {
+                        const uint32_t q = sign < 0 ? f - step[d] : f + step[d];
+                        float neighbor = __ldg(vel + q);
+                        if (!__ldg(open + q) && d != axis) neighbor = -center;
+                        laplace += neighbor - center;
+                    }
+            } else {
+#pragma unroll
+                for (int d = 0; d < 3; d++)
+#pragma unroll
+                    for (int sign = -1; sign <= 1; sign += 2) {
+                        P3 q = pos;
+                        q.v[d] += sign;
+                        float neighbor = face_masked(s, vel, q, axis);
+                        if (!open_masked(s, open, q, axis) && d != axis) neighbor = -center;
+                        laplace += neighbor - center;
+                    }
+            }
+        }
         P3 left = pos;
         left.v[axis] -= 1;
         const float rho = s.rho_l;
@@ -389,8 +437,9 @@ static unsigned face_blocks(const StepView& s, int axis) {
     return (unsigned)((d[0] * d[1] * d[2] + WG - 1) / WG);
 }
 
-void launch_predict(const StepView& s, float* const out[3], float* const masked[3], cudaStream_t st) {
-    for (int a = 0; a < 3; a++) ks_open_faces<<<face_blocks(s, a), WG, 0, st>>>(s, a, masked[a]);
+void launch_predict(const StepView& s, float* const out[3], float* const masked[3], uint8_t* const open[3],
+                    cudaStream_t st) {
+    for (int a = 0; a < 3; a++) ks_open_faces<<<face_blocks(s, a), WG, 0, st>>>(s, a, masked[a], open[a]);
     for (int a = 0; a < 3; a++)
         ks_predict<<<face_blocks(s, a), WG, 0, st>>>(s, masked[0], masked[1], masked[2], a, out[a]);
 }
