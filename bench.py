@@ -271,6 +271,52 @@ def run_ours(args):
                 "kernels": [{"name": k["name"], "us": k["ms"] * 1e3, "GBps": k["bytes"] / (k["ms"] * 1e-3) / 1e9}
                             for k in prof_s if k["name"].startswith("step_")]}
 
+    def chain_leg(name, scale, steps, every, reps):
+        """Forward chain u_{k+1} = P(u_k + dt f / rho_face) of `steps` steps
+        and its gradient dJ/df (outlet-plane objective, checkpoints every
+        `every` steps), each timed on the library stream; plus the device
+        memory the context holds (free memory before creation minus the
+        lowest free memory after the chain)."""
+        c = synth.make_case(name, seed=args.seed + rank, scale=scale)
+        ta = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+        torch.cuda.synchronize(dev)
+        free0 = torch.cuda.mem_get_info(dev)[0]
+        pc = mhdproj.PressureProjection(c["dims"], c["h"], outlet=True, precision=args.precision, rel_tol=args.tol)
+        pc.set_coefficients(ta(c["alpha"]), ta(c["solid"]), c["rho_liquid"], c["rho_air"])
+        u0 = (ta(c["u"]), ta(c["v"]), ta(c["w"]))
+        rng = np.random.default_rng(args.seed + 40)
+        if "fu" in c:
+            f = tuple(ta(c[k]) for k in ("fu", "fv", "fw"))
+        else:
+            f = tuple(ta((rng.standard_normal(x.shape) * 1e5 * (x != 0)).astype(np.float32)) for x in
+                      (c["u"], c["v"], c["w"]))
+        dt_c = 1e-6
+        fwd = lambda prj: prj.chain_forward(u0, f, dt_c, steps, every)[2]
+        bwd = lambda prj: prj.chain_backward(u0)[1]
+        fwd(pc)
+        bwd(pc)
+        ms_f, st_f = timed(pc, reps, fwd)
+        ms_b, _ = timed(pc, reps, bwd)
+        # a single projection of the same workload for projections/s
+        us_c = (ta(c["u"]), ta(c["v"]), ta(c["w"]))
+        out_c = tuple(torch.empty_like(x) for x in us_c)
+        proj = lambda prj: prj.project(us_c, c["dt"], out=out_c)[2]
+        proj(pc)
+        ms_p, st_p = timed(pc, reps, proj)
+        torch.cuda.synchronize(dev)
+        used = free0 - torch.cuda.mem_get_info(dev)[0]
+        pc.close()
+        nx_, ny_, nz_ = c["dims"]
+        peak_c, _ = hbm_peak()
+        bytes_c = projection_bytes(nx_ * ny_ * nz_, st_p[-1].iterations, st_p[-1].refinements, args.precision)
+        return {"projection_model_gb": bytes_c / 1e9,
+                "projection_hbm_fraction": bytes_c / (ms_p / reps * 1e-3) / 1e9 / peak_c,
+                "workload": f"{name}: {nx_}x{ny_}x{nz_} cells", "steps": steps, "checkpoint_every": every,
+                "forward_ms": ms_f / reps, "backward_ms": ms_b / reps, "backward_over_forward": ms_b / ms_f,
+                "projections_per_s": 1000.0 * reps / ms_p, "projection_ms": ms_p / reps,
+                "iterations": st_p[-1].iterations, "true_relative_residual": st_p[-1].true_relative_residual,
+                "device_memory_gb": used / 1e9}
+
     pr = make(args.precision)
     if args.step:
         out_s = fluid_step_leg(2, 1)
@@ -324,6 +370,11 @@ def run_ours(args):
         "clocks": clk,
         "gpu_launches": launches,
     }
+    peak0, _ = hbm_peak()
+    pbytes = projection_bytes(nx * ny * nz, its[-1], sts[-1].refinements, args.precision)
+    line["projection_hbm"] = {"model_gb": pbytes / 1e9, "achieved_gbs": pbytes / (ms_per * 1e-3) / 1e9,
+                              "fraction": pbytes / (ms_per * 1e-3) / 1e9 / peak0,
+                              "model": "N (95 + 24 R + 112 k) bytes: compulsory traffic of one projection"}
     if rank == 0 and not args.no_extras:
         # FP32-level comparator (same algorithm, FP32 multigrid fields)
         p32 = make("fp32")
@@ -413,6 +464,11 @@ def run_ours(args):
             pref.close()
         except mhdproj.ProjectionError as exc:
             line["reference_algorithm_gpu"] = {"unavailable": str(exc)}
+        # BASELINE configs 4 (128^3 adjoint chain, K = 8, checkpoints every 4)
+        # and 5 (512x256x256 column, K = 4): forward, gradient, projection
+        # throughput and device memory
+        line["adjoint128_chain"] = chain_leg("adjoint128", 1.0, 8, 4, 3)
+        line["column512"] = chain_leg("column512", 1.0, 4, 4, 3)
         try:
             line["fluid_step"] = fluid_step_leg(5, 10)
         except mhdproj.ProjectionError as exc:
@@ -441,6 +497,14 @@ def run_ours(args):
         print(json.dumps(line))
     if pg is not None:
         pg.destroy_process_group()
+
+
+def projection_bytes(n, iterations, refinements, precision):
+    """Compulsory HBM bytes of one projection: N (95 + 24 R + k (52 + 60))
+    with FP16/BF16 levels, N (95 + 24 R + 148 k) with FP32 levels (k CG
+    iterations, R refinement residuals after the first pass)."""
+    per_it = 112.0 if precision != "fp32" else 148.0
+    return n * (95.0 + 24.0 * refinements + per_it * iterations)
 
 
 def measured_traffic(workload, precision, kernel):
