@@ -338,10 +338,29 @@ __global__ void ks_fields(StepView s, float4* __restrict__ cells, float4* __rest
             pos.v[1] = (int)((i / s.dims[0]) % s.dims[1]);
             pos.v[2] = (int)(i / (s.dims[0] * s.dims[1]));
             float v[3], face_energy = 0.0f, div = 0.0f;
+            // Inside the grid (no wrap, no edge) a face of this fluid cell is
+            // open exactly when the neighbour across it is fluid.
+            bool interior = true;
+#pragma unroll
+            for (int a = 0; a < 3; a++) interior = interior && pos.v[a] >= 1 && pos.v[a] + 1 < (int)s.dims[a];
+            const uint32_t nx = s.dims[0], ny = s.dims[1];
+            const uint32_t cstep[3] = {1u, nx, nx * ny};
+            const uint32_t flo[3] = {(uint32_t)pos.v[0] + (nx + 1) * ((uint32_t)pos.v[1] + ny * (uint32_t)pos.v[2]),
+                                     (uint32_t)pos.v[0] + nx * ((uint32_t)pos.v[1] + (ny + 1) * (uint32_t)pos.v[2]),
+                                     i};
+            const uint32_t fstep[3] = {1u, nx, nx * ny};
+#pragma unroll
             for (int axis = 0; axis < 3; axis++) {
                 P3 q = pos;
                 q.v[axis] += 1;
-                const float a = face(s, pos, axis), b = face(s, q, axis);
+                float a, b;
+                if (interior) {
+                    a = is_fluid_index(s, i - cstep[axis]) ? __ldg(s.vel[axis] + flo[axis]) : 0.0f;
+                    b = is_fluid_index(s, i + cstep[axis]) ? __ldg(s.vel[axis] + flo[axis] + fstep[axis]) : 0.0f;
+                } else {
+                    a = face(s, pos, axis);
+                    b = face(s, q, axis);
+                }
                 v[axis] = 0.5f * (a + b);
                 face_energy += 0.5f * (a * a + b * b);
                 max_face = fmaxf(max_face, fmaxf(fabsf(a), fabsf(b)));
