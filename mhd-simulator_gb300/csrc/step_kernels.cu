@@ -153,38 +153,77 @@ __device__ __forceinline__ float em_force(const StepView& s, P3 pos, int axis) {
     const float4 f = s.em[cell_index(s, q)];
     return axis == 0 ? f.x : (axis == 1 ? f.y : f.z);
 }
-// sample_component (:109-116): trilinear in the face grid of `axis`, over
-// the masked face arrays m[3].  When all eight taps lie inside the grid
-// without a periodic wrap they are read at fixed strides from one index;
-// either way the products and sums are the same operations in the same order.
-// One out-of-line copy: seven inlined, unrolled samplers overflow the
-// instruction cache.
-__device__ __noinline__ float sample_component(const StepView& s, const float* const* m, const float position[3],
-                                               int axis) {
+// The sampled grid of sample_component: extents, periodic bits and the face
+// array of one component, passed by value so the sampler keeps them in
+// registers.
+struct SampleGrid {
+    int nx, ny, nz;
+    uint32_t periodic;
+    const float* __restrict__ arr;
+};
+
+template <int C>
+__device__ __forceinline__ float tap(const SampleGrid& g, int x, int y, int z) {
+    // face() over the masked array: wrap periodic axes, zero outside the grid
+    const int n[3] = {g.nx, g.ny, g.nz};
+    int c[3] = {x, y, z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        if (g.periodic & (1u << a)) {
+            if (c[a] < 0 || c[a] >= n[a]) c[a] = wrap_periodic(c[a], (uint32_t)n[a]);
+        } else if (c[a] < 0 || c[a] >= n[a] + (a == C ? 1 : 0)) {
+            return 0.0f;
+        }
+    }
+    const uint32_t row = (uint32_t)g.nx + (C == 0 ? 1u : 0u);
+    const uint32_t col = (uint32_t)g.ny + (C == 1 ? 1u : 0u);
+    return __ldg(g.arr + (uint32_t)c[0] + row * ((uint32_t)c[1] + col * (uint32_t)c[2]));
+}
+
+// The eight taps of a sample that touches the grid's edge or wraps.
+template <int C>
+__device__ __noinline__ float sample_edge(SampleGrid g, int bx, int by, int bz, float fx, float fy, float fz) {
+    float value = 0.0f;
+#pragma unroll 1
+    for (int k = 0; k < 8; k++) {
+        const int x = k & 1, y = (k >> 1) & 1, z = k >> 2;
+        const float wx = x ? fx : 1.0f - fx;
+        const float wy = y ? fy : 1.0f - fy;
+        const float wz = z ? fz : 1.0f - fz;
+        value += tap<C>(g, bx + x, by + y, bz + z) * wx * wy * wz;
+    }
+    return value;
+}
+
+// sample_component (:109-116): trilinear in the face grid of component C at
+// (px, py, pz).  When all eight taps lie inside the grid without a periodic
+// wrap they are read at fixed strides from one index; either way the products
+// and sums are the same operations in the same order.  One out-of-line copy
+// per component: inlined, unrolled samplers overflow the instruction cache.
+template <int C>
+__device__ __noinline__ float sample_component(SampleGrid g, float px, float py, float pz) {
+    const float pos[3] = {px, py, pz};
     int base[3];
     float fraction[3];
+#pragma unroll
     for (int a = 0; a < 3; a++) {
-        const float q = position[a] - (a == axis ? 0.0f : 0.5f);
+        const float q = pos[a] - (a == C ? 0.0f : 0.5f);
         const float fl = floorf(q);
         base[a] = (int)fl;
         fraction[a] = q - fl;  // fract()
     }
-    const float* __restrict__ arr = m[axis];
+    const int n[3] = {g.nx, g.ny, g.nz};
     bool inside = true;
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        const int hi = (s.periodic & (1u << a)) ? (int)s.dims[a] : (int)s.dims[a] + (a == axis ? 1 : 0);
+        const int hi = (g.periodic & (1u << a)) ? n[a] : n[a] + (a == C ? 1 : 0);
         inside = inside && base[a] >= 0 && base[a] + 1 < hi;
     }
     float value = 0.0f;
     if (inside) {
-        P3 b;
-        b.v[0] = base[0];
-        b.v[1] = base[1];
-        b.v[2] = base[2];
-        const uint32_t i0 = face_index(s, b, axis);
-        const uint32_t row = s.dims[0] + (axis == 0 ? 1u : 0u);
-        const uint32_t plane = row * (s.dims[1] + (axis == 1 ? 1u : 0u));
+        const uint32_t row = (uint32_t)g.nx + (C == 0 ? 1u : 0u);
+        const uint32_t plane = row * ((uint32_t)g.ny + (C == 1 ? 1u : 0u));
+        const float* __restrict__ p0 = g.arr + (uint32_t)base[0] + row * (uint32_t)base[1] + plane * (uint32_t)base[2];
 #pragma unroll
         for (int z = 0; z < 2; z++)
 #pragma unroll
@@ -194,26 +233,11 @@ __device__ __noinline__ float sample_component(const StepView& s, const float* c
                     const float wx = x ? fraction[0] : 1.0f - fraction[0];
                     const float wy = y ? fraction[1] : 1.0f - fraction[1];
                     const float wz = z ? fraction[2] : 1.0f - fraction[2];
-                    value += __ldg(arr + i0 + (uint32_t)x + (uint32_t)y * row + (uint32_t)z * plane) * wx * wy * wz;
+                    value += __ldg(p0 + (uint32_t)x + (uint32_t)y * row + (uint32_t)z * plane) * wx * wy * wz;
                 }
         return value;
     }
-#pragma unroll
-    for (int z = 0; z < 2; z++)
-#pragma unroll
-        for (int y = 0; y < 2; y++)
-#pragma unroll
-            for (int x = 0; x < 2; x++) {
-                const float wx = x ? fraction[0] : 1.0f - fraction[0];
-                const float wy = y ? fraction[1] : 1.0f - fraction[1];
-                const float wz = z ? fraction[2] : 1.0f - fraction[2];
-                P3 c;
-                c.v[0] = base[0] + x;
-                c.v[1] = base[1] + y;
-                c.v[2] = base[2] + z;
-                value += face_masked(s, arr, c, axis) * wx * wy * wz;
-            }
-    return value;
+    return sample_edge<C>(g, base[0], base[1], base[2], fraction[0], fraction[1], fraction[2]);
 }
 
 __device__ __forceinline__ bool face_position(const StepView& s, int axis, uint32_t f, P3* pos) {
@@ -236,30 +260,37 @@ __global__ void ks_open_faces(StepView s, int axis, float* __restrict__ out, uin
     open[f] = open_face(s, pos, axis) ? 1 : 0;
 }
 
+template <int AXIS>
 __global__ void ks_predict(StepView s, const float* __restrict__ m0, const float* __restrict__ m1,
-                           const float* __restrict__ m2, int axis, float* __restrict__ out) {
+                           const float* __restrict__ m2, float* __restrict__ out) {
     const uint32_t f = blockIdx.x * WG + threadIdx.x;
     P3 pos;
-    if (!face_position(s, axis, f, &pos)) return;
+    if (!face_position(s, AXIS, f, &pos)) return;
     const float* m[3] = {m0, m1, m2};
     float value = 0.0f;
-    if (open_face(s, pos, axis)) {
-        const float center = face_masked(s, m[axis], pos, axis);
+    if (open_face(s, pos, AXIS)) {
+        const float center = face_masked(s, m[AXIS], pos, AXIS);
         value = center;
         if (s.advection) {
+            const int nx = (int)s.dims[0], ny = (int)s.dims[1], nz = (int)s.dims[2];
+            const SampleGrid g0{nx, ny, nz, s.periodic, m0}, g1{nx, ny, nz, s.periodic, m1},
+                g2{nx, ny, nz, s.periodic, m2};
             float at[3];
             for (int a = 0; a < 3; a++) at[a] = (float)pos.v[a] + 0.5f;
-            at[axis] -= 0.5f;
-            float v[3], mid[3], vm[3], back[3];
-#pragma unroll 1
-            for (int a = 0; a < 3; a++) v[a] = sample_component(s, m, at, a);
+            at[AXIS] -= 0.5f;
+            const float v0 = sample_component<0>(g0, at[0], at[1], at[2]);
+            const float v1 = sample_component<1>(g1, at[0], at[1], at[2]);
+            const float v2 = sample_component<2>(g2, at[0], at[1], at[2]);
             const float half = 0.5f * s.dt / s.h;
-            for (int a = 0; a < 3; a++) mid[a] = at[a] - v[a] * half;
-#pragma unroll 1
-            for (int a = 0; a < 3; a++) vm[a] = sample_component(s, m, mid, a);
+            const float mx = at[0] - v0 * half, my = at[1] - v1 * half, mz = at[2] - v2 * half;
+            const float w0 = sample_component<0>(g0, mx, my, mz);
+            const float w1 = sample_component<1>(g1, mx, my, mz);
+            const float w2 = sample_component<2>(g2, mx, my, mz);
             const float full = s.dt / s.h;
-            for (int a = 0; a < 3; a++) back[a] = at[a] - vm[a] * full;
-            value = sample_component(s, m, back, axis);
+            const float bx = at[0] - w0 * full, by = at[1] - w1 * full, bz = at[2] - w2 * full;
+            if (AXIS == 0) value = sample_component<0>(g0, bx, by, bz);
+            else if (AXIS == 1) value = sample_component<1>(g1, bx, by, bz);
+            else value = sample_component<2>(g2, bx, by, bz);
         }
     }
     out[f] = value;
@@ -459,8 +490,9 @@ static unsigned face_blocks(const StepView& s, int axis) {
 void launch_predict(const StepView& s, float* const out[3], float* const masked[3], uint8_t* const open[3],
                     cudaStream_t st) {
     for (int a = 0; a < 3; a++) ks_open_faces<<<face_blocks(s, a), WG, 0, st>>>(s, a, masked[a], open[a]);
-    for (int a = 0; a < 3; a++)
-        ks_predict<<<face_blocks(s, a), WG, 0, st>>>(s, masked[0], masked[1], masked[2], a, out[a]);
+    ks_predict<0><<<face_blocks(s, 0), WG, 0, st>>>(s, masked[0], masked[1], masked[2], out[0]);
+    ks_predict<1><<<face_blocks(s, 1), WG, 0, st>>>(s, masked[0], masked[1], masked[2], out[1]);
+    ks_predict<2><<<face_blocks(s, 2), WG, 0, st>>>(s, masked[0], masked[1], masked[2], out[2]);
 }
 void launch_viscous(const StepView& s, float* const out[3], cudaStream_t st) {
     for (int a = 0; a < 3; a++) ks_viscous<<<face_blocks(s, a), WG, 0, st>>>(s, a, out[a]);
