@@ -287,6 +287,48 @@ def test_gb300_step_stages(gpu, oracle_lib):
     b.close()
 
 
+def test_gb300_step_periodic_pinned(gpu, oracle_lib):
+    """GB300 solver on a periodic x-y domain without an outlet (pinned gauge
+    cells): the step equals the oracle's predict + viscous projected by a
+    second context, bit for bit, over two chained steps."""
+    import mhdproj
+    from mhdproj import synth
+
+    torch = gpu
+    c = synth.make_case("jet128", scale=0.25)  # 32^3 nozzle geometry
+    dims = c["dims"]
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    dt, nu = 1e-5, 1e-6
+    acc = np.array([0.5, 0.0, -9.81], np.float32)
+
+    def ctx():
+        pr = mhdproj.PressureProjection(dims, c["h"], periodic=(True, True, False), outlet=False, precision="fp16",
+                                        rel_tol=1e-8)
+        pr.set_coefficients(t(c["alpha"]), t(c["solid"]), c["rho_liquid"], c["rho_liquid"])
+        return pr
+
+    a, b = ctx(), ctx()
+    u = [t(c["u"]), t(c["v"]), t(c["w"])]
+    ub = [x.clone() for x in u]
+    g = oracle_lib.grid(dims[0], dims[1], dims[2], c["h"], c["rho_liquid"], c["rho_liquid"], 3, False)
+    _, cls = oracle_lib.classify(g, c["solid"])
+    mask = (cls != 0).astype(np.uint32)
+    p = oracle_lib.make_params(dims, c["h"], dt, c["rho_liquid"], c["rho_liquid"], False, 3, 1e-5, 0.0,
+                               int(mask.sum()), False, 1e6)
+    p.physical[2] = nu
+    p.flags[1] = 1
+    for k in range(2):
+        a.fluid_step(u, dt, acceleration=tuple(acc), viscosity=nu, advection=True)
+        pred = oracle_lib.predict(p, mask, R.soa_to_records(dims, *(x.cpu().numpy() for x in ub)))
+        visc = oracle_lib.viscous(p, mask, np.asarray(c["alpha"], np.float32).reshape(-1), pred, acc)
+        (u0, u1, u2), _, _ = b.project(tuple(t(x) for x in R.records_to_soa(dims, visc)), dt, warm_start=True)
+        ub = [u0, u1, u2]
+        for x, y in zip(u, ub):
+            assert torch.equal(x, y), k
+    a.close()
+    b.close()
+
+
 def test_export_fields_round_trip(gpu, oracle_lib, tmp_path):
     """export_fields (src/run/export.rs:9-60): fluid.bin holds the cell
     records byte for byte, metadata.json is published, and an existing frame

@@ -136,3 +136,14 @@ def test_jet256_geometry(gpu, oracle_lib):
     rng = np.random.default_rng(11)
     solid = _solid_case(rng, (256, 256, 256), 0.3)
     _check_reference(gpu, mhdproj, oracle_lib, (256, 256, 256), 0, solid)
+
+
+def test_column512_dims_random_mask(gpu, oracle_lib):
+    """The 512x256x256 grid of the large column workload (33.5 M cells, rows
+    of 16 warp chunks), with a random mask near the percolation threshold."""
+    import mhdproj
+
+    rng = np.random.default_rng(13)
+    dims = (512, 256, 256)
+    solid = _solid_case(rng, dims, 0.31)
+    _check_reference(gpu, mhdproj, oracle_lib, dims, 0, solid)
