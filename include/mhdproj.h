@@ -257,6 +257,7 @@ typedef struct {
     float max_force_density;    /* max |rho_l g + f_em|, N/m^3 */
     float max_face_speed_m_s;   /* max |u| over the faces of fluid cells */
     uint32_t nonfinite_cells;   /* cells with non-finite or out-of-range fields */
+    uint32_t viscous_substeps;  /* FluidDiagnostics::viscous_substeps of the last step */
 } mhdproj_diagnostics;
 
 /* fields + diagnostics of src/fluid/solver.wgsl:256-291, as dispatched after
@@ -279,14 +280,28 @@ typedef struct {
     float acceleration[3];     /* FluidConfig::acceleration_m_s2 */
     float kinematic_viscosity; /* nu, m^2/s (Params.physical.z) */
     int32_t advection;         /* FluidConfig::advection: semi-Lagrangian RK2 momentum transport */
+    /* moving interface only (two-phase density): */
+    float surface_tension;     /* sigma, N/m (Params.surface.z) */
+    float air_viscosity;       /* dynamic viscosity of the air, Pa s (Params.surface.w) */
+    uint32_t max_viscous_substeps; /* FluidConfig::max_viscous_substeps (0: 4096) */
+    const float *curvature;    /* interface curvature per cell, 1/m (reserved.w), device array or NULL */
 } mhdproj_step_params;
 
-/* FluidState::step (src/fluid/mod.rs:1246-1333) for a flow without a moving
- * interface (one density: reference solver with two_phase = 0, GB300 solver
- * with rho_air = rho_liquid): the velocity CFL test on the previous fields
- * ("Fluid timestep exceeds the velocity CFL limit; reduce Δt"), predict
- * (advection), viscous (explicit viscosity, body and EM force, mobility), the
- * warm-started projection, fields and diagnostics.  u, v, w: device face
+/* FluidState::step (src/fluid/mod.rs:1246-1333): the velocity CFL test on
+ * the previous fields ("Fluid timestep exceeds the velocity CFL limit; reduce
+ * Δt"), predict, viscous (body and EM force, mobility), the warm-started
+ * projection, fields and diagnostics.  Without a moving interface (one
+ * density: reference solver with two_phase = 0, GB300 solver with rho_air =
+ * rho_liquid) predict advects (semi-Lagrangian RK2) and viscous adds the
+ * explicit viscous term.  With one (reference solver two_phase = 1, GB300
+ * solver rho_air != rho_liquid) the momentum is not advected here (the
+ * interface transport does it), the capillary / conservative CFL test applies
+ * ("Moving-interface capillary or conservative CFL limit exceeded; reduce
+ * common timestep"), the Newtonian stresses diffuse the predicted velocity
+ * by explicit Euler substeps or damped RKC2 stages
+ * (diffuse_surface_stress, :1160-1240; "Viscosity requires N equivalent Euler
+ * substeps, above the M work limit; ..."), and viscous adds the capillary
+ * force from the curvature with face densities.  u, v, w: device face
  * arrays, the velocity in and the projected velocity out; p_out (cell array)
  * and cells (16 floats per cell, written only when the step is accepted) are
  * optional outputs.  On any error the velocity and p_out are restored to

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
+#include <cfloat>
 #include <chrono>
 #include <cmath>
 #include <cstddef>
@@ -99,6 +101,11 @@ struct mhdproj_ctx {
     float4* h_st_scalars = nullptr;
     bool have_fields = false;
     bool step_ran = false;  // the step buffers hold a step's velocities (profiling)
+    // moving-interface stress workspace (allocated by the first such step)
+    float* st_mu = nullptr;
+    float4 *st_t4 = nullptr, *st_y0 = nullptr, *st_f0 = nullptr;
+    float2* st_t2 = nullptr;
+    unsigned int* st_bound = nullptr;
     float step_dt = 0.f, step_nu = 0.f;
     float max_face_speed = 0.f, force_max = 0.f;
     long long n_fluid = 0;
@@ -1205,6 +1212,145 @@ static int step_restore(mhdproj_ctx* ctx, float* const vel[3], float* p_out) {
     return wait_stream(ctx);
 }
 
+static int stress_buffers(mhdproj_ctx* ctx) {
+    if (ctx->st_mu) return 0;
+    CK(dalloc(ctx, &ctx->st_mu, ctx->n * 4));
+    CK(dalloc(ctx, &ctx->st_t4, ctx->n * sizeof(float4)));
+    CK(dalloc(ctx, &ctx->st_t2, ctx->n * sizeof(float2)));
+    CK(dalloc(ctx, &ctx->st_y0, ctx->n * sizeof(float4)));
+    CK(dalloc(ctx, &ctx->st_f0, ctx->n * sizeof(float4)));
+    CK(dalloc(ctx, &ctx->st_bound, sizeof(unsigned int)));
+    return 0;
+}
+
+// stabilized::schedule (src/fluid/stabilized.rs:11-50): rows of the damped
+// second-order Runge-Kutta-Chebyshev method (Verwer, Hundsdorfer & Sommeijer
+// 1990) for `euler_steps` equivalent Euler steps of dt: mu, nu, 1 - mu - nu,
+// operator time, initial-operator time (FP64 recurrences rounded to FP32).
+static std::vector<std::array<float, 5>> rkc_schedule(double dt, uint32_t euler_steps) {
+    const double damping = 0.05;
+    const double stiffness = 1.8 * (double)euler_steps;
+    const uint32_t cap = (uint32_t)std::ceil(3.0 * std::sqrt((double)euler_steps)) + 2u;
+    std::vector<std::array<float, 5>> rows;
+    for (uint32_t stages = 2; stages <= cap; stages++) {
+        const double w0 = 1.0 + damping / ((double)stages * (double)stages);
+        std::vector<double> t{1.0, w0}, d{0.0, 1.0}, dd{0.0, 0.0};
+        for (uint32_t j = 2; j <= stages; j++) {
+            t.push_back(2.0 * w0 * t[j - 1] - t[j - 2]);
+            d.push_back(2.0 * t[j - 1] + 2.0 * w0 * d[j - 1] - d[j - 2]);
+            dd.push_back(4.0 * d[j - 1] + 2.0 * w0 * dd[j - 1] - dd[j - 2]);
+        }
+        const double w1 = d[stages] / dd[stages];
+        if (stiffness > 0.9 * (1.0 + w0) / w1) continue;
+        std::vector<double> b(t.size(), 0.0);
+        for (size_t j = 2; j < t.size(); j++) b[j] = dd[j] / (d[j] * d[j]);
+        b[0] = b[2];
+        b[1] = b[2];
+        rows.push_back({1.0f, 0.0f, 0.0f, (float)(dt * b[1] * w1), 0.0f});
+        for (uint32_t j = 2; j <= stages; j++) {
+            const float mu = (float)(2.0 * w0 * b[j] / b[j - 1]);
+            const float nu = (float)(-b[j] / b[j - 2]);
+            const double op = dt * 2.0 * w1 * b[j] / b[j - 1];
+            const double a = 1.0 - b[j - 1] * t[j - 1];
+            rows.push_back({mu, nu, 1.0f - mu - nu, (float)op, (float)(-a * op)});
+        }
+        return rows;
+    }
+    return rows;
+}
+
+// FluidState::diffuse_surface_stress (src/fluid/mod.rs:1160-1240) on the
+// predicted velocity in st_pred; st_prev holds the step's starting velocity
+// (copied into st_star, the second RKC stage buffer).  *substeps: Euler
+// substeps or RKC stages.
+static int diffuse_surface_stress(mhdproj_ctx* ctx, StepView S, float dt, uint32_t max_substeps,
+                                  uint32_t* substeps) {
+    *substeps = 0;
+    // global_viscous_bound (:1146-1159): valid for every accepted fraction
+    // distribution, rounded upward
+    const double liquid = S.rho_l, ambient = S.rho_air;
+    const double slack = (double)1e-5f + 4.0 * (double)FLT_EPSILON;
+    const double floor_rho = std::min(liquid, ambient) - std::fabs(liquid - ambient) * slack;
+    const double mu = (double)std::max(S.nu * S.rho_l, S.mu_air);
+    const double h = ctx->grid.h;
+    double count = 0.0;
+    const double host_bound = 24.0 * mu / (floor_rho * h * h) * (1.0 + 32.0 * (double)FLT_EPSILON);
+    for (int a = 0; a < 3; a++) S.vel[a] = ctx->st_pred[a];
+    if (floor_rho > 0.0 && (double)dt * host_bound <= 1.8) {
+        if (host_bound == 0.0) return 0;
+        count = 1.0;
+    } else {
+        CK(cudaMemsetAsync(ctx->st_bound, 0, sizeof(unsigned int), ctx->stream));
+        launch_viscosity_bound(S, ctx->st_bound, ctx->stream);
+        ctx->launches += 3;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(ctx->h_st_scalars, ctx->st_bound, sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+        int rc = wait_stream(ctx);
+        if (rc) return rc;
+        unsigned int bits;
+        memcpy(&bits, ctx->h_st_scalars, sizeof bits);
+        float bound;
+        memcpy(&bound, &bits, sizeof bound);
+        if (!std::isfinite(bound) || bound < 0.f)
+            return fail(ctx, MHDPROJ_ERR_NONFINITE, "Nonfinite viscous stability bound");
+        if (bound == 0.f) return 0;
+        count = std::max(std::ceil((double)dt * (double)bound / 1.8), 1.0);
+    }
+    if (count > (double)max_substeps)
+        return fail(ctx, MHDPROJ_ERR_INVALID,
+                    "Viscosity requires %.0f equivalent Euler substeps, above the %u work limit; reduce the common "
+                    "timestep or increase Viscosity work limit",
+                    count, max_substeps);
+    const uint32_t steps = (uint32_t)count;
+    const long long nf[3] = {ctx->nfx, ctx->nfy, ctx->nfz};
+    float* const P[3] = {ctx->st_pred[0], ctx->st_pred[1], ctx->st_pred[2]};
+    float* const V[3] = {ctx->st_star[0], ctx->st_star[1], ctx->st_star[2]};
+    auto copy3 = [&](float* const dst[3], float* const src[3]) -> int {
+        for (int a = 0; a < 3; a++)
+            CK(cudaMemcpyAsync(dst[a], src[a], nf[a] * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+        return 0;
+    };
+    if (steps > 8u) {
+        const auto rows = rkc_schedule((double)dt, steps);
+        int rc = copy3(V, ctx->st_prev);  // the stage before the first one: the starting velocity
+        if (rc) return rc;
+        for (int a = 0; a < 3; a++) S.vel[a] = P[a];
+        launch_stress_coefficients(S, ctx->stream);
+        launch_stress_tensor(S, ctx->stream);
+        launch_stress_save_initial(S, ctx->stream);
+        ctx->launches += 3;
+        for (size_t i = 0; i < rows.size(); i++) {
+            const bool odd = i % 2 == 1;
+            for (int a = 0; a < 3; a++) S.vel[a] = odd ? V[a] : P[a];
+            if (i > 0) {
+                launch_stress_tensor(S, ctx->stream);
+                ctx->launches += 1;
+            }
+            launch_stress_stage(S, rows[i].data(), odd ? P : V, ctx->stream);
+            ctx->launches += 3;
+        }
+        CK(cudaGetLastError());
+        if (rows.size() % 2 == 1) {
+            rc = copy3(P, V);
+            if (rc) return rc;
+        }
+        *substeps = (uint32_t)rows.size();
+        return 0;
+    }
+    const float dt_sub = (float)((double)dt / (double)steps);
+    for (uint32_t k = 0; k < steps; k++) {
+        for (int a = 0; a < 3; a++) S.vel[a] = P[a];
+        launch_stress_diffuse(S, dt_sub, V, ctx->stream);
+        ctx->launches += 3;
+        int rc = copy3(P, V);
+        if (rc) return rc;
+    }
+    CK(cudaGetLastError());
+    *substeps = steps;
+    return 0;
+}
+
 extern "C" int mhdproj_fluid_step(mhdproj_ctx* ctx, float* u, float* v, float* w, const float* em_force,
                                   const mhdproj_step_params* sp, float* p_out, float* cells, mhdproj_stats* stats,
                                   mhdproj_diagnostics* diagnostics) {
@@ -1215,11 +1361,16 @@ extern "C" int mhdproj_fluid_step(mhdproj_ctx* ctx, float* u, float* v, float* w
     bool ok = dt > 0.f && std::isfinite(dt) && std::isfinite(sp->kinematic_viscosity) && sp->kinematic_viscosity >= 0.f;
     for (int a = 0; a < 3; a++) ok = ok && std::isfinite(sp->acceleration[a]);
     if (!ok) return fail(ctx, MHDPROJ_ERR_INVALID, "Invalid fluid timestep, initial condition or solver limits/tolerances");
+    ok = std::isfinite(sp->surface_tension) && sp->surface_tension >= 0.f && std::isfinite(sp->air_viscosity) &&
+         sp->air_viscosity >= 0.f;
+    if (!ok) return fail(ctx, MHDPROJ_ERR_INVALID, "surface tension and air viscosity must be finite and >= 0");
     StepView base = step_view(ctx, u, v, w, em_force, sp->acceleration, dt);
-    if (base.two_phase)
-        return fail(ctx, MHDPROJ_ERR_INVALID,
-                    "the fluid step covers flows without a moving interface (one density; reference solver "
-                    "two_phase = 0)");
+    const bool surface = base.two_phase != 0;  // a moving interface: two densities
+    base.nu = sp->kinematic_viscosity;
+    base.sigma = sp->surface_tension;
+    base.mu_air = sp->air_viscosity;
+    base.curv = sp->curvature;
+    const uint32_t max_substeps = sp->max_viscous_substeps ? sp->max_viscous_substeps : 4096u;
     if (ctx->ref && base.phase && dt != ref_export(ctx->ref).drag_dt)
         return fail(ctx, MHDPROJ_ERR_INVALID,
                     "the phase-drag mobility was set for a different dt; call mhdproj_set_phase_drag again");
@@ -1238,6 +1389,15 @@ extern "C" int mhdproj_fluid_step(mhdproj_ctx* ctx, float* u, float* v, float* w
         const float acceleration = std::sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]) + ctx->force_max / base.rho_l;
         if ((ctx->max_face_speed * std::sqrt(3.0f) + acceleration * dt) * dt / ctx->grid.h > 0.9f)
             return fail(ctx, MHDPROJ_ERR_INVALID, "Fluid timestep exceeds the velocity CFL limit; reduce Δt");
+        if (surface) {  // :1263-1275
+            const float h = ctx->grid.h, sigma = sp->surface_tension;
+            const float pi = 3.14159265358979323846f;
+            const float capillary =
+                sigma > 0.f ? std::sqrt((base.rho_l + base.rho_air) * (h * h * h) / (2.f * pi * sigma)) : INFINITY;
+            if (dt > capillary || 3.f * (ctx->max_face_speed + acceleration * dt) * dt / h > 0.45f)
+                return fail(ctx, MHDPROJ_ERR_INVALID,
+                            "Moving-interface capillary or conservative CFL limit exceeded; reduce common timestep");
+        }
     }
     const long long nf[3] = {ctx->nfx, ctx->nfy, ctx->nfz};
     for (int a = 0; a < 3; a++)
@@ -1245,15 +1405,34 @@ extern "C" int mhdproj_fluid_step(mhdproj_ctx* ctx, float* u, float* v, float* w
     if (p_out) CK(cudaMemcpyAsync(ctx->st_prev_p, p_out, ctx->n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     // predict (advection) and viscous (viscosity, forcing, mobility)
     StepView sv = base;
-    sv.advection = sp->advection != 0;
-    sv.nu = sp->kinematic_viscosity;
+    // with a moving interface the interface transport carries the momentum
+    sv.advection = !surface && sp->advection != 0;
     launch_predict(sv, ctx->st_pred, ctx->st_star, ctx->st_open, ctx->stream);
+    ctx->launches += 6;
+    uint32_t substeps = 0;
+    if (surface) {
+        rc = stress_buffers(ctx);
+        if (rc) return rc;
+        StepView ss = sv;
+        ss.mu_c = ctx->st_mu;
+        ss.t4 = ctx->st_t4;
+        ss.t2 = ctx->st_t2;
+        ss.y0 = ctx->st_y0;
+        ss.f0 = ctx->st_f0;
+        rc = diffuse_surface_stress(ctx, ss, dt, max_substeps, &substeps);
+        if (rc) {
+            const std::string msg = ctx->err;
+            step_restore(ctx, vel, p_out);
+            ctx->err = msg;
+            return rc;
+        }
+    }
     for (int a = 0; a < 3; a++) {
         sv.vel[a] = ctx->st_pred[a];
         sv.open[a] = ctx->st_open[a];
     }
     launch_viscous(sv, ctx->st_star, ctx->stream);
-    ctx->launches += 9;
+    ctx->launches += 3;
     CK(cudaGetLastError());
     ctx->step_ran = true;
     ctx->step_dt = dt;
@@ -1268,10 +1447,12 @@ extern "C" int mhdproj_fluid_step(mhdproj_ctx* ctx, float* u, float* v, float* w
     }
     // fields and diagnostics of the projected velocity; the cell records are
     // written once the diagnostics accept the step
-    const StepView fv = step_view(ctx, u, v, w, em_force, sp->acceleration, dt);
+    StepView fv = step_view(ctx, u, v, w, em_force, sp->acceleration, dt);
+    fv.curv = sp->curvature;
     bool bad = false;
     rc = run_fields(ctx, fv, nullptr, diagnostics, &bad);
     if (rc) return rc;
+    if (diagnostics) diagnostics->viscous_substeps = substeps;
     if (bad) {
         step_restore(ctx, vel, p_out);
         return fail(ctx, MHDPROJ_ERR_NONFINITE, "Nonfinite fluid fields; state restored");

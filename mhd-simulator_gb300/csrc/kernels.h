@@ -200,12 +200,33 @@ struct StepView {
     const float4* em;       // EM force density per cell (xyz) or null
     const float* phi;       // pressure potential, element i at phi[i * phi_stride]
     int phi_stride;
+    // moving interface (two_phase): surface tension, air dynamic viscosity,
+    // interface curvature per cell (or null), and the stress workspace
+    float sigma, mu_air;
+    const float* curv;
+    float* mu_c;            // cell viscosity cached for a diffusion macro-step
+    float4* t4;             // normal stresses xx, yy, zz and shear xy per cell
+    float2* t2;             // shear xz, yz per cell
+    float4* y0;             // RKC initial face values per cell (lanes x, y, z)
+    float4* f0;             // RKC initial stress acceleration per cell
 };
 // masked / open: three face arrays of scratch each (face() and open_face()
 // of every position); viscous reads the open flags through StepView::open
 void launch_predict(const StepView& s, float* const out[3], float* const masked[3], uint8_t* const open[3],
                     cudaStream_t st);
 void launch_viscous(const StepView& s, float* const out[3], cudaStream_t st);
+// Moving-interface stress diffusion (s.vel: the face arrays the stresses
+// read).  Cell viscosities into s.mu_c; the shared stress tensor into s.t4/t2;
+// RKC initial state into s.y0/f0; one RKC stage out = blend of the stage
+// arrays; one explicit Euler substep out = u + dt_sub a(u); the stability
+// bound (max over faces) into *bound (a float, cleared by the caller).
+void launch_stress_coefficients(const StepView& s, cudaStream_t st);
+void launch_stress_tensor(const StepView& s, cudaStream_t st);
+void launch_stress_save_initial(const StepView& s, cudaStream_t st);
+// row: mu, nu, 1 - mu - nu, op, initial-operator weight
+void launch_stress_stage(const StepView& s, const float row[5], float* const io[3], cudaStream_t st);
+void launch_stress_diffuse(const StepView& s, float dt_sub, float* const out[3], cudaStream_t st);
+void launch_viscosity_bound(const StepView& s, unsigned int* bound_bits, cudaStream_t st);
 uint32_t fields_groups(const StepView& s);
 // partials: 3 * fields_groups float4; scalars3: 3 float4 (the 12 diagnostics floats)
 void launch_fields(const StepView& s, float4* cells, float4* partials, float4* scalars3, cudaStream_t st);

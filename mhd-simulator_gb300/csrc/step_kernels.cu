@@ -296,6 +296,20 @@ __global__ void ks_predict(StepView s, const float* __restrict__ m0, const float
     out[f] = value;
 }
 
+// capillary_force (:52-57): sigma k (alpha_R - alpha_L) / h with the
+// interface-weighted curvature of the two cells.
+__device__ float capillary_force(const StepView& s, P3 pos, int axis) {
+    if (!s.two_phase || !open_face(s, pos, axis)) return 0.0f;
+    P3 left = pos;
+    left.v[axis] -= 1;
+    const float al = occupancy(s, left), ar = occupancy(s, pos);
+    const float kl = s.curv ? s.curv[cell_index(s, wrap_cell(s, left))] : 0.0f;
+    const float kr = s.curv ? s.curv[cell_index(s, wrap_cell(s, pos))] : 0.0f;
+    const float wl = al * (1.0f - al), wr = ar * (1.0f - ar);
+    const float k = wl + wr > 1e-6f ? (wl * kl + wr * kr) / fmaxf(wl + wr, 1e-20f) : 0.5f * (kl + kr);
+    return s.sigma * k * (ar - al) / s.h;
+}
+
 __global__ void ks_viscous(StepView s, int axis, float* __restrict__ out) {
     const uint32_t f = blockIdx.x * WG + threadIdx.x;
     P3 pos;
@@ -342,12 +356,187 @@ __global__ void ks_viscous(StepView s, int axis, float* __restrict__ out) {
         }
         P3 left = pos;
         left.v[axis] -= 1;
-        const float rho = s.rho_l;
-        const float acc = s.acc[axis] + (em_force(s, left, axis) + em_force(s, pos, axis)) / (2.0f * rho) + 0.0f;
-        const float beta = mobility(s, pos, axis);
+        float rho = s.rho_l, capillary = 0.0f;
+        if (s.two_phase) {
+            rho = face_density(s, pos, axis);
+            capillary = capillary_force(s, pos, axis) / rho;
+        }
+        const float acc =
+            s.acc[axis] + (em_force(s, left, axis) + em_force(s, pos, axis)) / (2.0f * rho) + capillary;
+        float beta = mobility(s, pos, axis);
+        if (s.two_phase) beta *= rho / s.rho_l;
         value = (center + s.nu * s.dt / (s.h * s.h) * laplace + s.dt * acc) * beta;
     }
     out[f] = value;
+}
+
+// ------------------------------------------------ moving-interface stresses
+// src/fluid/viscosity.wgsl: symmetric Newtonian stresses on the MAC grid,
+// normal stresses at cells, shear stresses at edges.
+__device__ __forceinline__ P3 shifted(P3 q, int a, int d) {
+    q.v[a] += d;
+    return q;
+}
+__device__ float dynamic_mu(const StepView& s, P3 q) {  // :3-6
+    if (!fluid(s, q)) return 0.0f;
+    const float t = fminf(fmaxf(occupancy(s, q), 0.0f), 1.0f);
+    const float mu_l = s.nu * s.rho_l;
+    return s.mu_air * (1.0f - t) + mu_l * t;
+}
+__device__ float coefficient_mu(const StepView& s, P3 q, bool cached) {  // :12-16
+    if (!cached) return dynamic_mu(s, q);
+    const P3 at = wrap_cell(s, q);
+    if (!valid_cell(s, at)) return 0.0f;
+    return s.mu_c[cell_index(s, at)];
+}
+__device__ float edge_mu(const StepView& s, P3 q, int i, int j, bool cached) {  // :17-24
+    float total = 0.0f, count = 0.0f;
+    for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 2; b++) {
+            P3 at = q;
+            at.v[i] -= a;
+            at.v[j] -= b;
+            if (fluid(s, at)) {
+                total += coefficient_mu(s, at, cached);
+                count += 1.0f;
+            }
+        }
+    return total / fmaxf(count, 1.0f);
+}
+__device__ float normal_stress(const StepView& s, P3 q, int i, bool cached) {  // :30-33
+    if (!fluid(s, q)) return 0.0f;
+    return 2.0f * coefficient_mu(s, q, cached) * (face(s, shifted(q, i, 1), i) - face(s, q, i)) / s.h;
+}
+__device__ float shear_stress(const StepView& s, P3 q, int i, int j, bool cached) {  // :34-44
+    const P3 lower_i = shifted(q, j, -1), lower_j = shifted(q, i, -1);
+    float ui1 = face(s, q, i), ui0 = face(s, lower_i, i);
+    float uj1 = face(s, q, j), uj0 = face(s, lower_j, j);
+    // odd tangential ghosts: zero velocity on the wall
+    if (!open_face(s, q, i) && open_face(s, lower_i, i)) ui1 = -ui0;
+    if (!open_face(s, lower_i, i) && open_face(s, q, i)) ui0 = -ui1;
+    if (!open_face(s, q, j) && open_face(s, lower_j, j)) uj1 = -uj0;
+    if (!open_face(s, lower_j, j) && open_face(s, q, j)) uj0 = -uj1;
+    return edge_mu(s, q, i, j, cached) * (ui1 - ui0 + uj1 - uj0) / s.h;
+}
+__device__ float tensor_normal(const StepView& s, P3 q, int i) {  // :55-58
+    const P3 at = wrap_cell(s, q);
+    if (!valid_cell(s, at)) return 0.0f;
+    const float4 t = s.t4[cell_index(s, at)];
+    return i == 0 ? t.x : (i == 1 ? t.y : t.z);
+}
+__device__ float tensor_shear(const StepView& s, P3 q, int i, int j) {  // :59-66
+    const P3 at = wrap_cell(s, q);
+    if (!valid_cell(s, at)) return shear_stress(s, q, i, j, true);
+    const uint32_t c = cell_index(s, at);
+    const int plane = i + j;
+    if (plane == 1) return s.t4[c].w;
+    const float2 t = s.t2[c];
+    return plane == 2 ? t.x : t.y;
+}
+__device__ float stress_acceleration(const StepView& s, P3 q, int i, bool cached) {  // :67-80
+    const P3 left = shifted(q, i, -1);
+    float divergence = 0.0f;
+    if (cached) {
+        divergence = tensor_normal(s, q, i) - tensor_normal(s, left, i);
+        for (int j = 0; j < 3; j++)
+            if (j != i) divergence += tensor_shear(s, shifted(q, j, 1), i, j) - tensor_shear(s, q, i, j);
+    } else {
+        divergence = normal_stress(s, q, i, false) - normal_stress(s, left, i, false);
+        for (int j = 0; j < 3; j++)
+            if (j != i)
+                divergence += shear_stress(s, shifted(q, j, 1), i, j, false) - shear_stress(s, q, i, j, false);
+    }
+    return divergence / (s.h * face_density(s, q, i));
+}
+__device__ __forceinline__ P3 cell_position(const StepView& s, uint32_t i) {
+    P3 q;
+    q.v[0] = (int)(i % s.dims[0]);
+    q.v[1] = (int)((i / s.dims[0]) % s.dims[1]);
+    q.v[2] = (int)(i / (s.dims[0] * s.dims[1]));
+    return q;
+}
+
+__global__ void ks_stress_coefficients(StepView s) {  // stress_coefficients (:25-29)
+    const uint32_t i = blockIdx.x * WG + threadIdx.x;
+    if (i >= s.dims[3]) return;
+    s.mu_c[i] = dynamic_mu(s, cell_position(s, i));
+}
+__global__ void ks_stress_tensor(StepView s) {  // stress_tensor (:47-54)
+    const uint32_t i = blockIdx.x * WG + threadIdx.x;
+    if (i >= s.dims[3]) return;
+    const P3 q = cell_position(s, i);
+    s.t4[i] = make_float4(normal_stress(s, q, 0, true), normal_stress(s, q, 1, true), normal_stress(s, q, 2, true),
+                          shear_stress(s, q, 0, 1, true));
+    s.t2[i] = make_float2(shear_stress(s, q, 0, 2, true), shear_stress(s, q, 1, 2, true));
+}
+__global__ void ks_stress_save_initial(StepView s) {  // stress_save_initial (stabilized.wgsl:6-15)
+    const uint32_t i = blockIdx.x * WG + threadIdx.x;
+    if (i >= s.dims[3]) return;
+    const P3 q = cell_position(s, i);
+    float y[3] = {0.0f, 0.0f, 0.0f}, op[3] = {0.0f, 0.0f, 0.0f};
+    for (int axis = 0; axis < 3; axis++)
+        if (open_face(s, q, axis)) {
+            y[axis] = face(s, q, axis);
+            op[axis] = stress_acceleration(s, q, axis, true);
+        }
+    s.y0[i] = make_float4(y[0], y[1], y[2], 0.0f);
+    s.f0[i] = make_float4(op[0], op[1], op[2], 0.0f);
+}
+// stress_stabilized (stabilized.wgsl:16-30): io holds the stage before the
+// previous one (read) and receives the new stage; s.vel the previous stage.
+__global__ void ks_stress_stage(StepView s, int axis, float bx, float by, float bz, float bw, float ix,
+                                float* __restrict__ io) {
+    const uint32_t f = blockIdx.x * WG + threadIdx.x;
+    P3 pos;
+    if (!face_position(s, axis, f, &pos)) return;
+    const float older = io[f];
+    float value = 0.0f;
+    if (open_face(s, pos, axis)) {
+        const uint32_t cell = cell_index(s, wrap_cell(s, pos));
+        const float previous = face(s, pos, axis);
+        const float4 y = s.y0[cell], op = s.f0[cell];
+        const float initial = axis == 0 ? y.x : (axis == 1 ? y.y : y.z);
+        const float initial_op = axis == 0 ? op.x : (axis == 1 ? op.y : op.z);
+        value = bx * previous + by * older + bz * initial + bw * stress_acceleration(s, pos, axis, true) +
+                ix * initial_op;
+    }
+    io[f] = value;
+}
+// stress_diffuse (:100-107): one explicit Euler substep.
+__global__ void ks_stress_diffuse(StepView s, int axis, float dt_sub, float* __restrict__ out) {
+    const uint32_t f = blockIdx.x * WG + threadIdx.x;
+    P3 pos;
+    if (!face_position(s, axis, f, &pos)) return;
+    float value = 0.0f;
+    if (open_face(s, pos, axis)) value = face(s, pos, axis) + dt_sub * stress_acceleration(s, pos, axis, false);
+    out[f] = value;
+}
+// viscosity_bound (:81-96): 4 x the absolute row sum of rho^-1 div(tau) over
+// the open faces; the block maximum goes to *bound_bits as float bits (all
+// values are non-negative, so the unsigned maximum is the float maximum).
+__global__ void ks_viscosity_bound(StepView s, int axis, unsigned int* bound_bits) {
+    __shared__ float red[WG];
+    const uint32_t f = blockIdx.x * WG + threadIdx.x;
+    float bound = 0.0f;
+    P3 q;
+    if (face_position(s, axis, f, &q) && open_face(s, q, axis)) {
+        const P3 left = shifted(q, axis, -1);
+        float sum = dynamic_mu(s, q) + dynamic_mu(s, left);
+        for (int j = 0; j < 3; j++)
+            if (j != axis) sum += edge_mu(s, q, axis, j, false) + edge_mu(s, shifted(q, j, 1), axis, j, false);
+        bound = 4.0f * sum / (face_density(s, q, axis) * s.h * s.h);
+    }
+    red[threadIdx.x] = bound;
+    __syncthreads();
+    for (int d = WG / 2; d > 0; d /= 2) {
+        if ((int)threadIdx.x < d) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + d]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const float b = red[0];
+        // a non-finite bound is kept as the largest bit pattern: the host rejects it
+        atomicMax(bound_bits, (b == b) ? __float_as_uint(b) : 0xFFFFFFFFu);
+    }
 }
 
 __global__ void ks_fields(StepView s, float4* __restrict__ cells, float4* __restrict__ partials) {
@@ -362,7 +551,8 @@ __global__ void ks_fields(StepView s, float4* __restrict__ cells, float4* __rest
         float4 o0 = make_float4(0.f, 0.f, 0.f, 0.f), o1 = o0, o2 = o0, o3 = o0;
         const float oy = s.phase ? s.phase[i] : 0.0f;
         const float oz = s.occ ? s.occ[i] : 0.0f;
-        if (s.two_phase) o3 = make_float4(0.0f, oy, oz, 0.0f);
+        const float ow = s.curv ? s.curv[i] : 0.0f;
+        if (s.two_phase) o3 = make_float4(0.0f, oy, oz, ow);
         if (is_fluid_index(s, i)) {
             P3 pos;
             pos.v[0] = (int)(i % s.dims[0]);
@@ -409,7 +599,7 @@ __global__ void ks_fields(StepView s, float4* __restrict__ cells, float4* __rest
             o0 = make_float4(v[0], v[1], v[2], speed);
             o1 = make_float4(pressure, div, 0.0f, 0.0f);
             o2 = make_float4(force[0], force[1], force[2], 0.0f);
-            o3 = make_float4(1.0f, s.phase ? oy : 1.0f, oz, 0.0f);
+            o3 = make_float4(1.0f, s.phase ? oy : 1.0f, oz, ow);
             bool bad = v[0] != v[0] || v[1] != v[1] || v[2] != v[2];
             bad = bad || force[0] != force[0] || force[1] != force[1] || force[2] != force[2];
             bad = bad || fabsf(force[0]) > 1e30f || fabsf(force[1]) > 1e30f || fabsf(force[2]) > 1e30f;
@@ -496,6 +686,24 @@ void launch_predict(const StepView& s, float* const out[3], float* const masked[
 }
 void launch_viscous(const StepView& s, float* const out[3], cudaStream_t st) {
     for (int a = 0; a < 3; a++) ks_viscous<<<face_blocks(s, a), WG, 0, st>>>(s, a, out[a]);
+}
+static unsigned cell_blocks(const StepView& s) { return (s.dims[3] + WG - 1) / WG; }
+void launch_stress_coefficients(const StepView& s, cudaStream_t st) {
+    ks_stress_coefficients<<<cell_blocks(s), WG, 0, st>>>(s);
+}
+void launch_stress_tensor(const StepView& s, cudaStream_t st) { ks_stress_tensor<<<cell_blocks(s), WG, 0, st>>>(s); }
+void launch_stress_save_initial(const StepView& s, cudaStream_t st) {
+    ks_stress_save_initial<<<cell_blocks(s), WG, 0, st>>>(s);
+}
+void launch_stress_stage(const StepView& s, const float row[5], float* const io[3], cudaStream_t st) {
+    for (int a = 0; a < 3; a++)
+        ks_stress_stage<<<face_blocks(s, a), WG, 0, st>>>(s, a, row[0], row[1], row[2], row[3], row[4], io[a]);
+}
+void launch_stress_diffuse(const StepView& s, float dt_sub, float* const out[3], cudaStream_t st) {
+    for (int a = 0; a < 3; a++) ks_stress_diffuse<<<face_blocks(s, a), WG, 0, st>>>(s, a, dt_sub, out[a]);
+}
+void launch_viscosity_bound(const StepView& s, unsigned int* bound_bits, cudaStream_t st) {
+    for (int a = 0; a < 3; a++) ks_viscosity_bound<<<face_blocks(s, a), WG, 0, st>>>(s, a, bound_bits);
 }
 uint32_t fields_groups(const StepView& s) { return (s.dims[3] + WG - 1) / WG; }
 void launch_fields(const StepView& s, float4* cells, float4* partials, float4* scalars3, cudaStream_t st) {

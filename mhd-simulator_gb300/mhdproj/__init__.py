@@ -67,7 +67,7 @@ class Diagnostics(C.Structure):
                 ("rms_divergence_s_inv", C.c_float), ("max_pressure_pa", C.c_float),
                 ("kinetic_energy_j", C.c_float), ("fluid_mass_kg", C.c_float), ("net_flux_m3_s", C.c_float),
                 ("max_force_density", C.c_float), ("max_face_speed_m_s", C.c_float),
-                ("nonfinite_cells", C.c_uint32)]
+                ("nonfinite_cells", C.c_uint32), ("viscous_substeps", C.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -75,7 +75,8 @@ class Diagnostics(C.Structure):
 
 class StepParams(C.Structure):
     _fields_ = [("dt", C.c_float), ("acceleration", C.c_float * 3), ("kinematic_viscosity", C.c_float),
-                ("advection", C.c_int32)]
+                ("advection", C.c_int32), ("surface_tension", C.c_float), ("air_viscosity", C.c_float),
+                ("max_viscous_substeps", C.c_uint32), ("curvature", C.c_void_p)]
 
 
 class KernelTime(C.Structure):
@@ -403,12 +404,17 @@ class PressureProjection:
         return out, d.as_dict()
 
     def fluid_step(self, u, dt, acceleration=(0.0, 0.0, -9.81), viscosity=0.0, advection=True, em_force=None,
-                   p_out=None, cells=None):
+                   p_out=None, cells=None, surface_tension=0.0, air_viscosity=0.0, max_viscous_substeps=4096,
+                   curvature=None):
         """One FluidState::step (mhdproj_fluid_step) in place on u = (u, v, w):
         returns (stats dict, diagnostics dict).  p_out / cells: optional
-        device outputs (cells shaped (nz, ny, nx, 16))."""
+        device outputs (cells shaped (nz, ny, nx, 16)).  surface_tension,
+        air_viscosity, max_viscous_substeps and curvature (a cell tensor)
+        apply with a moving interface."""
         self._order()
-        sp = StepParams(dt, (C.c_float * 3)(*acceleration), viscosity, int(bool(advection)))
+        sp = StepParams(dt, (C.c_float * 3)(*acceleration), viscosity, int(bool(advection)), surface_tension,
+                        air_viscosity, max_viscous_substeps,
+                        None if curvature is None else _ptr(curvature).value)
         st = Stats()
         d = Diagnostics()
         self._check(self._lib.mhdproj_fluid_step(self._ctx, _ptr(u[0]), _ptr(u[1]), _ptr(u[2]),

@@ -101,6 +101,22 @@ void oref_project(const oref_params *params, const uint32_t *mask, uint32_t comp
 void oref_predict(const oref_params *params, const uint32_t *mask, const float *velocity, float *predicted);
 void oref_viscous(const oref_params *params, const uint32_t *mask, const float *occupancy, const float *phase,
                   const float *em, const float acceleration[3], const float *predicted, float *velocity);
+/* viscous() with a moving interface (surface.x = 1): face density, capillary
+ * force sigma k (alpha_R - alpha_L) / h from the per-cell curvature (or
+ * NULL), mobility times rho_face / rho_l, no explicit Laplacian. */
+void oref_viscous_surface(const oref_params *params, const uint32_t *mask, const float *occupancy, const float *phase,
+                          const float *em, const float acceleration[3], const float *curvature, float sigma,
+                          const float *predicted, float *velocity);
+/* FluidState::diffuse_surface_stress (src/fluid/mod.rs:1160-1240): Euler
+ * substeps or damped RKC2 stages of the Newtonian stress operator of
+ * src/fluid/viscosity.wgsl on `predicted` (in/out); `velocity` holds the
+ * step's starting velocity and serves as the second stage buffer.  Returns 0,
+ * 1 (non-finite bound) or 2 (more substeps than max_substeps). */
+int oref_diffuse_surface_stress(const oref_params *params, const uint32_t *mask, const float *occupancy,
+                                const float *phase, float mu_air, float dt, uint32_t max_substeps,
+                                float *predicted, float *velocity, uint32_t *substeps, float *gpu_bound);
+/* stabilized::schedule: rows of 8 floats; returns the row count. */
+uint32_t oref_rkc_schedule(double dt, uint32_t euler_steps, float *rows, uint32_t cap);
 void oref_fields(const oref_params *params, const uint32_t *mask, const float *occupancy, const float *work,
                  const float *velocity, const float *em, const float acceleration[3], const float *reserved_in,
                  float *cells, float scalars[12]);

@@ -103,6 +103,14 @@ def lib():
         L.oref_predict.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, _f32p]
         L.oref_viscous.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, C.c_void_p, C.c_void_p, _f32p, _f32p,
                                    _f32p]
+        L.oref_viscous_surface.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, C.c_void_p, C.c_void_p, _f32p,
+                                           C.c_void_p, C.c_float, _f32p, _f32p]
+        L.oref_diffuse_surface_stress.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, C.c_void_p, C.c_float,
+                                                  C.c_float, C.c_uint32, _f32p, _f32p, C.POINTER(C.c_uint32),
+                                                  C.POINTER(C.c_float)]
+        L.oref_diffuse_surface_stress.restype = C.c_int
+        L.oref_rkc_schedule.argtypes = [C.c_double, C.c_uint32, _f32p, C.c_uint32]
+        L.oref_rkc_schedule.restype = C.c_uint32
         L.oref_fields.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, _f32p, _f32p, C.c_void_p, _f32p,
                                   C.c_void_p, C.c_void_p, _f32p]
         L.oref_mg_create.argtypes = [C.POINTER(OrefParams), _u32p, _f32p, C.c_int]
@@ -222,6 +230,43 @@ def viscous(params, mask, occupancy, predicted, acceleration, em=None, phase=Non
     lib().oref_viscous(C.byref(params), np.ascontiguousarray(mask, np.uint32),
                        np.ascontiguousarray(occupancy, np.float32), ph_p, em_p, acc, pred, out)
     return out.reshape(-1, 4)
+
+
+def viscous_surface(params, mask, occupancy, predicted, acceleration, curvature=None, sigma=0.0, em=None,
+                    phase=None):
+    """viscous with a moving interface (capillary force, face densities)."""
+    pred = np.ascontiguousarray(predicted, np.float32).reshape(-1)
+    out = np.zeros_like(pred)
+    em_a, em_p = _opt(em)
+    ph_a, ph_p = _opt(phase)
+    cv_a, cv_p = _opt(curvature)
+    acc = np.ascontiguousarray(acceleration, np.float32)
+    lib().oref_viscous_surface(C.byref(params), np.ascontiguousarray(mask, np.uint32),
+                               np.ascontiguousarray(occupancy, np.float32), ph_p, em_p, acc, cv_p, sigma, pred, out)
+    return out.reshape(-1, 4)
+
+
+def diffuse_surface_stress(params, mask, occupancy, predicted, velocity, mu_air, dt, max_substeps=4096,
+                           phase=None):
+    """FluidState::diffuse_surface_stress: returns (status, substeps, gpu bound or -1,
+    diffused predicted vec4[nf])."""
+    pred = np.ascontiguousarray(predicted, np.float32).reshape(-1).copy()
+    vel = np.ascontiguousarray(velocity, np.float32).reshape(-1).copy()
+    ph_a, ph_p = _opt(phase)
+    sub = C.c_uint32()
+    bound = C.c_float()
+    st = lib().oref_diffuse_surface_stress(C.byref(params), np.ascontiguousarray(mask, np.uint32),
+                                           np.ascontiguousarray(occupancy, np.float32), ph_p, mu_air, dt,
+                                           max_substeps, pred, vel, C.byref(sub), C.byref(bound))
+    return st, sub.value, bound.value, pred.reshape(-1, 4)
+
+
+def rkc_schedule(dt, euler_steps):
+    """stabilized::schedule rows (n, 8)."""
+    cap = int(np.ceil(3.0 * np.sqrt(euler_steps))) + 2
+    rows = np.zeros(8 * cap, np.float32)
+    n = lib().oref_rkc_schedule(dt, euler_steps, rows, cap)
+    return rows.reshape(cap, 8)[:n]
 
 
 def fields(params, mask, occupancy, work, velocity, acceleration, em=None, reserved=None, cells=True):

@@ -1279,8 +1279,25 @@ void oref_predict(const oref_params *params, const uint32_t *mask, const float *
 /* viscous(): :143-163 without a moving interface (surface.x = 0): explicit
  * Laplacian with mirrored (no-slip) closed tangential neighbours, body and EM
  * acceleration, times the face mobility. */
+/* capillary_force(): :52-57, curvature per cell (reserved.w) or NULL */
+static float capillary_force(const state *s, const float *curv, float sigma, ivec3 pos, uint32_t axis) {
+    if (s->p->surface[0] < 0.5f || !open_face(s, pos, axis)) return 0.0f;
+    ivec3 left = pos;
+    left.v[axis] -= 1;
+    const float al = occupancy(s, left), ar = occupancy(s, pos);
+    const float kl = curv ? curv[idx3(wrap_cell(s, left), s->p->dims)] : 0.0f;
+    const float kr = curv ? curv[idx3(wrap_cell(s, pos), s->p->dims)] : 0.0f;
+    const float wl = al * (1.0f - al), wr = ar * (1.0f - ar);
+    const float k = wl + wr > 1e-6f ? (wl * kl + wr * kr) / fmaxf(wl + wr, 1e-20f) : 0.5f * (kl + kr);
+    return sigma * k * (ar - al) / s->p->physical[0];
+}
 void oref_viscous(const oref_params *params, const uint32_t *mask, const float *occupancy, const float *phase,
                   const float *em, const float acceleration[3], const float *predicted, float *velocity) {
+    oref_viscous_surface(params, mask, occupancy, phase, em, acceleration, NULL, 0.0f, predicted, velocity);
+}
+void oref_viscous_surface(const oref_params *params, const uint32_t *mask, const float *occupancy, const float *phase,
+                          const float *em, const float acceleration[3], const float *curvature, float sigma,
+                          const float *predicted, float *velocity) {
     state s;
     memset(&s, 0, sizeof s);
     s.p = params;
@@ -1309,12 +1326,17 @@ void oref_viscous(const oref_params *params, const uint32_t *mask, const float *
                     }
             ivec3 left = pos;
             left.v[axis] -= 1;
-            const float rho = p->physical[3];
+            float rho = p->physical[3], capillary = 0.0f;
+            if (p->surface[0] > 0.5f) {
+                rho = face_density(&s, pos, axis);
+                capillary = capillary_force(&s, curvature, sigma, pos, axis) / rho;
+            }
             float el[3], er[3];
             em_force(&s, em, left, el);
             em_force(&s, em, pos, er);
-            const float acc = acceleration[axis] + (el[axis] + er[axis]) / (2.0f * rho) + 0.0f;
-            const float beta = mobility(&s, pos, axis);
+            const float acc = acceleration[axis] + (el[axis] + er[axis]) / (2.0f * rho) + capillary;
+            float beta = mobility(&s, pos, axis);
+            if (p->surface[0] > 0.5f) beta *= rho / p->physical[3];
             out[axis] = (center + p->physical[2] * p->physical[1] / (p->physical[0] * p->physical[0]) * laplace +
                          p->physical[1] * acc) *
                         beta;
@@ -1473,4 +1495,309 @@ void oref_fields(const oref_params *params, const uint32_t *mask, const float *o
     memcpy(scalars + 4, rb[0], 4 * sizeof(float));
     memcpy(scalars + 8, rc[0], 4 * sizeof(float));
     free(part);
+}
+
+/* ----------------------------------------- moving-interface stresses
+ * src/fluid/viscosity.wgsl and stabilized.wgsl with the host sequencing of
+ * FluidState::diffuse_surface_stress (src/fluid/mod.rs:1160-1240) and
+ * stabilized::schedule/encode (src/fluid/stabilized.rs).  The per-cell lanes
+ * the shaders borrow from the display packet (pressure.w viscosity,
+ * pressure.y/z shear, velocity/force RKC initial state) are separate arrays
+ * here. */
+typedef struct {
+    state s;
+    float mu_air;
+    float *mu;    /* cached cell viscosity */
+    float *t4;    /* xx, yy, zz, xy per cell */
+    float *t2;    /* xz, yz per cell */
+    float *y0;    /* 4 per cell */
+    float *f0;    /* 4 per cell */
+} stress_state;
+
+static ivec3 shifted(ivec3 q, uint32_t a, int d) {
+    q.v[a] += d;
+    return q;
+}
+static float dynamic_mu(const stress_state *S, ivec3 q) {
+    if (!fluid(&S->s, q)) return 0.0f;
+    const float t = fminf(fmaxf(occupancy(&S->s, q), 0.0f), 1.0f);
+    const float mu_l = S->s.p->physical[2] * S->s.p->physical[3];
+    return S->mu_air * (1.0f - t) + mu_l * t;
+}
+static float coefficient_mu(const stress_state *S, ivec3 q, int cached) {
+    if (!cached) return dynamic_mu(S, q);
+    ivec3 at = wrap_cell(&S->s, q);
+    if (!valid_cell(&S->s, at)) return 0.0f;
+    return S->mu[idx3(at, S->s.p->dims)];
+}
+static float edge_mu_c(const stress_state *S, ivec3 q, uint32_t i, uint32_t j, int cached) {
+    float total = 0.0f, count = 0.0f;
+    for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 2; b++) {
+            ivec3 at = q;
+            at.v[i] -= a;
+            at.v[j] -= b;
+            if (fluid(&S->s, at)) {
+                total += coefficient_mu(S, at, cached);
+                count += 1.0f;
+            }
+        }
+    return total / fmaxf(count, 1.0f);
+}
+static float sface(const stress_state *S, ivec3 q, uint32_t i) { return face_value(&S->s, q, i, 1); }
+static float normal_stress(const stress_state *S, ivec3 q, uint32_t i, int cached) {
+    if (!fluid(&S->s, q)) return 0.0f;
+    return 2.0f * coefficient_mu(S, q, cached) * (sface(S, shifted(q, i, 1), i) - sface(S, q, i)) /
+           S->s.p->physical[0];
+}
+static float shear_stress(const stress_state *S, ivec3 q, uint32_t i, uint32_t j, int cached) {
+    const ivec3 lower_i = shifted(q, j, -1), lower_j = shifted(q, i, -1);
+    float ui1 = sface(S, q, i), ui0 = sface(S, lower_i, i);
+    float uj1 = sface(S, q, j), uj0 = sface(S, lower_j, j);
+    if (!open_face(&S->s, q, i) && open_face(&S->s, lower_i, i)) ui1 = -ui0;
+    if (!open_face(&S->s, lower_i, i) && open_face(&S->s, q, i)) ui0 = -ui1;
+    if (!open_face(&S->s, q, j) && open_face(&S->s, lower_j, j)) uj1 = -uj0;
+    if (!open_face(&S->s, lower_j, j) && open_face(&S->s, q, j)) uj0 = -uj1;
+    return edge_mu_c(S, q, i, j, cached) * (ui1 - ui0 + uj1 - uj0) / S->s.p->physical[0];
+}
+static float tensor_normal(const stress_state *S, ivec3 q, uint32_t i) {
+    ivec3 at = wrap_cell(&S->s, q);
+    if (!valid_cell(&S->s, at)) return 0.0f;
+    return S->t4[4 * (size_t)idx3(at, S->s.p->dims) + i];
+}
+static float tensor_shear(const stress_state *S, ivec3 q, uint32_t i, uint32_t j) {
+    ivec3 at = wrap_cell(&S->s, q);
+    if (!valid_cell(&S->s, at)) return shear_stress(S, q, i, j, 1);
+    const size_t c = idx3(at, S->s.p->dims);
+    const uint32_t plane = i + j;
+    if (plane == 1u) return S->t4[4 * c + 3];
+    return S->t2[2 * c + (plane - 2u)];
+}
+static float stress_acceleration(const stress_state *S, ivec3 q, uint32_t i, int cached) {
+    const ivec3 left = shifted(q, i, -1);
+    float divergence = 0.0f;
+    if (cached) {
+        divergence = tensor_normal(S, q, i) - tensor_normal(S, left, i);
+        for (uint32_t j = 0; j < 3; j++)
+            if (j != i) divergence += tensor_shear(S, shifted(q, j, 1), i, j) - tensor_shear(S, q, i, j);
+    } else {
+        divergence = normal_stress(S, q, i, 0) - normal_stress(S, left, i, 0);
+        for (uint32_t j = 0; j < 3; j++)
+            if (j != i) divergence += shear_stress(S, shifted(q, j, 1), i, j, 0) - shear_stress(S, q, i, j, 0);
+    }
+    return divergence / (S->s.p->physical[0] * face_density(&S->s, q, i));
+}
+static void k_stress_coefficients(stress_state *S) {
+    const oref_params *p = S->s.p;
+#pragma omp parallel for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)p->dims[3]; ii++) S->mu[ii] = dynamic_mu(S, decode3((uint32_t)ii, p->dims));
+}
+static void k_stress_tensor(stress_state *S) {
+    const oref_params *p = S->s.p;
+#pragma omp parallel for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)p->dims[3]; ii++) {
+        const ivec3 q = decode3((uint32_t)ii, p->dims);
+        float *t = S->t4 + 4 * ii;
+        t[0] = normal_stress(S, q, 0, 1);
+        t[1] = normal_stress(S, q, 1, 1);
+        t[2] = normal_stress(S, q, 2, 1);
+        t[3] = shear_stress(S, q, 0, 1, 1);
+        S->t2[2 * ii] = shear_stress(S, q, 0, 2, 1);
+        S->t2[2 * ii + 1] = shear_stress(S, q, 1, 2, 1);
+    }
+}
+static void k_stress_save_initial(stress_state *S) {
+    const oref_params *p = S->s.p;
+#pragma omp parallel for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)p->dims[3]; ii++) {
+        const ivec3 q = decode3((uint32_t)ii, p->dims);
+        float y[4] = {0, 0, 0, 0}, op[4] = {0, 0, 0, 0};
+        for (uint32_t axis = 0; axis < 3; axis++)
+            if (open_face(&S->s, q, axis)) {
+                y[axis] = sface(S, q, axis);
+                op[axis] = stress_acceleration(S, q, axis, 1);
+            }
+        memcpy(S->y0 + 4 * ii, y, sizeof y);
+        memcpy(S->f0 + 4 * ii, op, sizeof op);
+    }
+}
+/* stress_stabilized: out (the velocity binding) = blend of the previous stage
+ * (predicted binding), the stage before (out's old content), the initial
+ * state and the operators. */
+static void k_stress_stabilized(stress_state *S, const float row[8], float *out) {
+    const oref_params *p = S->s.p;
+#pragma omp parallel for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)p->faces[3]; ii++) {
+        const uint32_t i = (uint32_t)ii;
+        const ivec3 q = decode3(i, p->faces);
+        float older[4], res[4] = {0, 0, 0, 0};
+        memcpy(older, out + LANES * i, sizeof older);
+        for (uint32_t axis = 0; axis < 3; axis++)
+            if (open_face(&S->s, q, axis)) {
+                const size_t cell = idx3(wrap_cell(&S->s, q), p->dims);
+                const float previous = sface(S, q, axis);
+                const float initial = S->y0[4 * cell + axis], initial_op = S->f0[4 * cell + axis];
+                res[axis] = row[0] * previous + row[1] * older[axis] + row[2] * initial +
+                            row[3] * stress_acceleration(S, q, axis, 1) + row[4] * initial_op;
+            }
+        memcpy(out + LANES * i, res, sizeof res);
+    }
+}
+static void k_stress_diffuse(stress_state *S, float dt_sub, float *out) {
+    const oref_params *p = S->s.p;
+#pragma omp parallel for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)p->faces[3]; ii++) {
+        const uint32_t i = (uint32_t)ii;
+        const ivec3 q = decode3(i, p->faces);
+        float res[4] = {0, 0, 0, 0};
+        for (uint32_t axis = 0; axis < 3; axis++)
+            if (open_face(&S->s, q, axis)) res[axis] = sface(S, q, axis) + dt_sub * stress_acceleration(S, q, axis, 0);
+        memcpy(out + LANES * i, res, sizeof res);
+    }
+}
+static float k_viscosity_bound(stress_state *S) {
+    const oref_params *p = S->s.p;
+    float best = 0.0f;
+#pragma omp parallel for schedule(static) reduction(max : best)
+    for (int64_t ii = 0; ii < (int64_t)p->faces[3]; ii++) {
+        const ivec3 q = decode3((uint32_t)ii, p->faces);
+        for (uint32_t c = 0; c < 3; c++)
+            if (open_face(&S->s, q, c)) {
+                const ivec3 left = shifted(q, c, -1);
+                float sum = dynamic_mu(S, q) + dynamic_mu(S, left);
+                for (uint32_t j = 0; j < 3; j++)
+                    if (j != c) sum += edge_mu_c(S, q, c, j, 0) + edge_mu_c(S, shifted(q, j, 1), c, j, 0);
+                const float b = 4.0f * sum / (face_density(&S->s, q, c) * p->physical[0] * p->physical[0]);
+                if (b > best) best = b;
+            }
+    }
+    return best;
+}
+
+/* stabilized::schedule (src/fluid/stabilized.rs:11-50): damped RKC2 rows
+ * (mu, nu, 1-mu-nu, operator time, initial-operator time) for `euler_steps`
+ * equivalent Euler steps of dt.  Returns the row count (<= cap). */
+#define RKC_DAMPING 0.05
+static uint32_t rkc_capacity(uint32_t euler_limit) { return (uint32_t)ceil(3.0 * sqrt((double)euler_limit)) + 2u; }
+uint32_t oref_rkc_schedule(double dt, uint32_t euler_steps, float *rows, uint32_t cap) {
+    const double stiffness = 1.8 * (double)euler_steps;
+    const uint32_t smax = rkc_capacity(euler_steps);
+    double *t = (double *)malloc((smax + 2) * sizeof(double)), *d = (double *)malloc((smax + 2) * sizeof(double));
+    double *dd = (double *)malloc((smax + 2) * sizeof(double)), *b = (double *)malloc((smax + 2) * sizeof(double));
+    uint32_t out = 0;
+    for (uint32_t stages = 2; stages <= smax; stages++) {
+        const double w0 = 1.0 + RKC_DAMPING / ((double)stages * (double)stages);
+        t[0] = 1.0; t[1] = w0; d[0] = 0.0; d[1] = 1.0; dd[0] = 0.0; dd[1] = 0.0;
+        for (uint32_t j = 2; j <= stages; j++) {
+            t[j] = 2.0 * w0 * t[j - 1] - t[j - 2];
+            d[j] = 2.0 * t[j - 1] + 2.0 * w0 * d[j - 1] - d[j - 2];
+            dd[j] = 4.0 * d[j - 1] + 2.0 * w0 * dd[j - 1] - dd[j - 2];
+        }
+        const double w1 = d[stages] / dd[stages];
+        if (stiffness > 0.9 * (1.0 + w0) / w1) continue;
+        for (uint32_t j = 0; j <= stages; j++) b[j] = 0.0;
+        for (uint32_t j = 2; j <= stages; j++) b[j] = dd[j] / (d[j] * d[j]);
+        b[0] = b[2];
+        b[1] = b[2];
+        if (cap < stages) break;
+        float *r = rows;
+        memset(r, 0, 8 * sizeof(float));
+        r[0] = 1.0f;
+        r[3] = (float)(dt * b[1] * w1);
+        out = 1;
+        for (uint32_t j = 2; j <= stages; j++) {
+            const float mu = (float)(2.0 * w0 * b[j] / b[j - 1]);
+            const float nu = (float)(-b[j] / b[j - 2]);
+            const double op = dt * 2.0 * w1 * b[j] / b[j - 1];
+            const double a = 1.0 - b[j - 1] * t[j - 1];
+            r = rows + 8 * out;
+            memset(r, 0, 8 * sizeof(float));
+            r[0] = mu;
+            r[1] = nu;
+            r[2] = 1.0f - mu - nu;
+            r[3] = (float)op;
+            r[4] = (float)(-a * op);
+            out++;
+        }
+        break;
+    }
+    free(t); free(d); free(dd); free(b);
+    return out;
+}
+
+/* FluidState::diffuse_surface_stress on the face records: `predicted` holds
+ * the stage input (the predicted velocity) and receives the diffused
+ * velocity; `velocity` holds the step's starting velocity (the RKC stages
+ * alternate the two buffers as the reference does).  Returns 0, 1 for a
+ * non-finite bound, 2 for too many substeps; *substeps the Euler substeps or
+ * RKC stages run. */
+int oref_diffuse_surface_stress(const oref_params *params, const uint32_t *mask, const float *occupancy,
+                                const float *phase, float mu_air, float dt, uint32_t max_substeps,
+                                float *predicted, float *velocity, uint32_t *substeps, float *gpu_bound) {
+    stress_state S;
+    memset(&S, 0, sizeof S);
+    S.s.p = params;
+    S.s.mask = mask;
+    S.s.occ = occupancy;
+    S.s.phase = phase;
+    S.mu_air = mu_air;
+    const uint32_t n = params->dims[3], nf = params->faces[3];
+    *substeps = 0;
+    if (gpu_bound) *gpu_bound = -1.0f;
+    /* global_viscous_bound (src/fluid/mod.rs:1146-1159) */
+    const double liquid = params->physical[3], ambient = params->surface[1];
+    const double slack = (double)1e-5f + 4.0 * (double)1.1920929e-7f;
+    const double floor_rho = fmin(liquid, ambient) - fabs(liquid - ambient) * slack;
+    const double mu = (double)fmaxf(params->physical[2] * params->physical[3], mu_air);
+    const double h = params->physical[0];
+    double count;
+    if (floor_rho > 0.0 && (double)dt * (24.0 * mu / (floor_rho * h * h) * (1.0 + 32.0 * (double)1.1920929e-7f)) <= 1.8) {
+        const double bound = 24.0 * mu / (floor_rho * h * h) * (1.0 + 32.0 * (double)1.1920929e-7f);
+        if (bound == 0.0) return 0;
+        count = 1.0;
+    } else {
+        const float bound = k_viscosity_bound(&S);
+        if (gpu_bound) *gpu_bound = bound;
+        if (!isfinite(bound) || bound < 0.0f) return 1;
+        if (bound == 0.0f) return 0;
+        count = fmax(ceil((double)dt * (double)bound / 1.8), 1.0);
+    }
+    if (count > (double)max_substeps) return 2;
+    const uint32_t steps = (uint32_t)count;
+    S.mu = (float *)calloc(n, sizeof(float));
+    S.t4 = (float *)calloc((size_t)4 * n, sizeof(float));
+    S.t2 = (float *)calloc((size_t)2 * n, sizeof(float));
+    S.y0 = (float *)calloc((size_t)4 * n, sizeof(float));
+    S.f0 = (float *)calloc((size_t)4 * n, sizeof(float));
+    if (steps > 8u) {
+        const uint32_t cap = rkc_capacity(steps);
+        float *rows = (float *)calloc((size_t)8 * cap, sizeof(float));
+        const uint32_t nrows = oref_rkc_schedule((double)dt, steps, rows, cap);
+        float *bufs[2] = {velocity, predicted}; /* parity 0: velocity binding, predicted binding */
+        S.s.velocity = bufs[0];
+        S.s.predicted = bufs[1];
+        k_stress_coefficients(&S);
+        k_stress_tensor(&S);
+        k_stress_save_initial(&S);
+        for (uint32_t i = 0; i < nrows; i++) {
+            const uint32_t par = i % 2u;
+            S.s.velocity = par ? bufs[1] : bufs[0];
+            S.s.predicted = par ? bufs[0] : bufs[1];
+            if (i > 0) k_stress_tensor(&S);
+            k_stress_stabilized(&S, rows + 8 * i, S.s.velocity);
+        }
+        if (nrows % 2u == 1u) memcpy(predicted, velocity, (size_t)LANES * nf * sizeof(float));
+        *substeps = nrows;
+        free(rows);
+    } else {
+        const float dt_sub = (float)((double)dt / (double)steps);
+        S.s.predicted = predicted;
+        for (uint32_t k = 0; k < steps; k++) {
+            k_stress_diffuse(&S, dt_sub, velocity);
+            memcpy(predicted, velocity, (size_t)LANES * nf * sizeof(float));
+        }
+        *substeps = steps;
+    }
+    free(S.mu); free(S.t4); free(S.t2); free(S.y0); free(S.f0);
+    return 0;
 }

@@ -329,6 +329,123 @@ def test_gb300_step_periodic_pinned(gpu, oracle_lib):
     b.close()
 
 
+def interface_case(seed=4):
+    """A 17x13x9 two-phase box of 1 mm cells: liquid fraction uniform in
+    [0, 1] (interface cells everywhere), a solid wall at x = 8 with the gap
+    cell (1, 1), 1000:1.2 densities, velocities N(0, 0.01 m/s), curvature
+    N(0, 200 1/m)."""
+    c = R.wall_case((17, 13, 9), (0, 0, 0), True, False, seed=seed)
+    rng = np.random.default_rng(seed)
+    c = dict(c)
+    c["h"] = 1e-3
+    c["rho_liquid"], c["rho_air"] = 1000.0, 1.2
+    c["two_phase"] = True
+    c["alpha"] = rng.uniform(0.0, 1.0, c["alpha"].shape).astype(np.float32)
+    for k in "uvw":
+        c[k] = (0.01 * c[k]).astype(np.float32)
+    c["curvature"] = rng.normal(0.0, 200.0, c["alpha"].shape).astype(np.float32)
+    c["dt"] = 1e-4
+    c["rel_tol"], c["abs_div_tol"] = 1e-5, 1e-5
+    return c
+
+
+INTERFACE_CASES = [
+    # air viscosity, expected substep path: host bound (1 Euler), GPU bound with Euler substeps, RKC stages
+    ("host_bound", 1e-6, 1e-7),
+    ("euler", 4e-2, 1e-6),
+    ("rkc", 0.2, 1e-6),
+]
+
+
+@pytest.mark.parametrize("name,mu_air,nu", INTERFACE_CASES)
+def test_reference_interface_step_bit_exact(gpu, oracle_lib, name, mu_air, nu):
+    """The moving-interface step (no advection here, capillary force, stress
+    diffusion by Euler substeps or RKC2 stages, face densities) on the
+    reference solver equals the oracle's chain bit for bit over two steps."""
+    import mhdproj
+
+    torch = gpu
+    c = interface_case()
+    dims = c["dims"]
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    sigma = 0.07
+    acc = np.array([0.0, 0.0, -9.81], np.float32)
+    per = tuple(bool(c["periodic"] & (1 << a)) for a in range(3))
+    pr = mhdproj.PressureProjection(dims, c["h"], periodic=per, outlet=False, solver="reference",
+                                    preconditioner="jacobi", rel_tol=c["rel_tol"], abs_div_tol=c["abs_div_tol"],
+                                    two_phase=True, max_iterations=20000)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    pr.set_coefficients(t(c["alpha"]), t(c["solid"]), c["rho_liquid"], c["rho_air"])
+    u = [t(c["u"]), t(c["v"]), t(c["w"])]
+    curv = t(c["curvature"])
+    cells = torch.zeros((nz, ny, nx, 16), dtype=torch.float32, device="cuda")
+    p_out = torch.zeros((nz, ny, nx), dtype=torch.float32, device="cuda")
+    mask01 = (np.asarray(c["solid"]).reshape(-1) == 0).astype(np.uint32)
+    comps, mask = oracle_lib.anchors(mask01, dims, 0)
+    fluid = int((mask != 0).sum())
+    occ = np.asarray(c["alpha"], np.float32).reshape(-1)
+    vel = (c["u"], c["v"], c["w"])
+    old_p = np.zeros(n, np.float32)
+    paths = set()
+    for k in range(2):
+        st, d = pr.fluid_step(u, c["dt"], acceleration=tuple(acc), viscosity=nu, advection=True, p_out=p_out,
+                              cells=cells, surface_tension=sigma, air_viscosity=mu_air, curvature=curv)
+        torch.cuda.synchronize()
+        prm = oracle_lib.make_params(dims, c["h"], c["dt"], c["rho_liquid"], c["rho_air"], True, 0, c["rel_tol"],
+                                     c["abs_div_tol"], fluid, False, 1e6)
+        prm.physical[2] = nu
+        prm.flags[1] = 0  # the interface transport advects the momentum
+        rec = R.soa_to_records(dims, *vel)
+        pred = oracle_lib.predict(prm, mask, rec)
+        status, sub, gbound, pred = oracle_lib.diffuse_surface_stress(prm, mask, occ, pred, rec, mu_air, c["dt"])
+        assert status == 0
+        paths.add("host" if gbound < 0 else ("rkc" if sub > 0 and gbound * c["dt"] / 1.8 > 8 else "euler"))
+        assert d["viscous_substeps"] == sub, (k, d["viscous_substeps"], sub)
+        visc = oracle_lib.viscous_surface(prm, mask, occ, pred, acc, curvature=c["curvature"].reshape(-1),
+                                          sigma=sigma)
+        ref = R.run_oracle(oracle_lib, c, preconditioner="jacobi", warm_start=True, old_pressure=old_p,
+                           u=R.records_to_soa(dims, visc))
+        assert ref["result"].status == 0
+        assert st["iterations"] == ref["result"].iterations, k
+        for a, key in enumerate("uvw"):
+            assert np.array_equal(bits(u[a].cpu().numpy()), bits(ref[key])), (k, key)
+        assert np.array_equal(bits(p_out.cpu().numpy().reshape(-1)), bits(ref["p"])), k
+        reserved = np.zeros((n, 4), np.float32)
+        reserved[:, 2] = occ
+        reserved[:, 3] = c["curvature"].reshape(-1)
+        ocells, sc = oracle_lib.fields(ref["params"], mask, occ, ref["work"],
+                                       R.soa_to_records(dims, ref["u"], ref["v"], ref["w"]), acc, reserved=reserved)
+        assert np.array_equal(bits(cells.cpu().numpy().reshape(n, 16)), bits(ocells)), k
+        assert np.float32(d["kinetic_energy_j"]) == np.float32(sc[3])
+        vel = (ref["u"], ref["v"], ref["w"])
+        old_p = ref["p"]
+    want = {"host_bound": "host", "euler": "euler", "rkc": "rkc"}[name]
+    assert paths == {want}, paths
+    pr.close()
+
+
+def test_interface_step_substep_limit(gpu, oracle_lib):
+    """More equivalent Euler substeps than the work limit: the reference's
+    message, velocity restored."""
+    import mhdproj
+
+    torch = gpu
+    c = interface_case()
+    pr = mhdproj.PressureProjection(c["dims"], c["h"], outlet=False, solver="reference", preconditioner="jacobi",
+                                    rel_tol=1e-5, abs_div_tol=1e-5, two_phase=True)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    pr.set_coefficients(t(c["alpha"]), t(c["solid"]), c["rho_liquid"], c["rho_air"])
+    u = [t(c["u"]), t(c["v"]), t(c["w"])]
+    before = [a.clone() for a in u]
+    with pytest.raises(mhdproj.ProjectionError) as e:
+        pr.fluid_step(u, c["dt"], viscosity=1e-6, surface_tension=0.07, air_viscosity=0.2, max_viscous_substeps=4)
+    assert "equivalent Euler substeps, above the 4 work limit" in str(e.value)
+    for a, b in zip(u, before):
+        assert torch.equal(a, b)
+    pr.close()
+
+
 def test_export_fields_round_trip(gpu, oracle_lib, tmp_path):
     """export_fields (src/run/export.rs:9-60): fluid.bin holds the cell
     records byte for byte, metadata.json is published, and an existing frame

@@ -95,3 +95,48 @@ def test_uniform_flow_diagnostics(oracle_lib):
     np.testing.assert_allclose(sc[3], 0.5 * rho * speed ** 2 * h ** 3 * n, rtol=1e-5)
     np.testing.assert_allclose(sc[8], 0.4, rtol=1e-6)  # max face speed
     assert sc[9] == n  # melt fraction 1 in every fluid cell
+
+
+def _amplification(rows, lam):
+    previous = older = 1.0
+    for r in rows:
+        nxt = (float(r[0]) + float(r[3]) * lam) * previous + float(r[1]) * older + float(r[2]) + float(r[4]) * lam
+        older, previous = previous, nxt
+    return previous
+
+
+def test_rkc_schedule_is_stable_and_consistent(oracle_lib):
+    """stabilized::schedule's own acceptance test (src/fluid/stabilized.rs:
+    235-258): constants are preserved, the amplification stays inside the
+    unit disk on [-1.8 N, 0], and the error against exp(-1) shrinks with the
+    step."""
+    for steps in (1, 9, 64, 1000, 4096):
+        rows = oracle_lib.rkc_schedule(1.0, steps)
+        assert len(rows) <= int(np.ceil(3 * np.sqrt(steps))) + 2
+        assert abs(_amplification(rows, 0.0) - 1.0) < 2e-5
+        for i in range(0, 2001, 25):
+            z = -(i / 2000.0) * 1.8 * steps
+            assert abs(_amplification(rows, z)) <= 1.0001, (steps, z)
+    errors = []
+    for n in (1, 2, 4, 8):
+        rows = oracle_lib.rkc_schedule(1.0 / n, 1000)
+        errors.append(abs(_amplification(rows, -1.0) ** n - np.exp(-1.0)))
+    assert all(b < 0.3 * a for a, b in zip(errors, errors[1:])), errors
+
+
+def test_stress_diffusion_keeps_uniform_periodic_flow(oracle_lib):
+    """A uniform flow in a periodic two-phase box has no stress: Euler and
+    RKC diffusion leave it unchanged."""
+    dims = (8, 6, 4)
+    n = dims[0] * dims[1] * dims[2]
+    p = oracle_lib.make_params(dims, 1e-3, 1e-4, 1000.0, 1.2, True, 7, 1e-5, 1e-5, n, False, 1e6)
+    p.physical[2] = 1e-6
+    mask = np.ones(n, np.uint32)
+    occ = np.random.default_rng(2).uniform(0, 1, n).astype(np.float32)
+    rec = R.soa_to_records(dims, *_uniform(dims, (0.01, -0.02, 0.005)))
+    for mu_air in (1.8e-5, 2e-3, 1e-2):
+        st, sub, _, out = oracle_lib.diffuse_surface_stress(p, mask, occ, rec, rec, mu_air, 1e-4)
+        assert st == 0 and sub >= 1
+        got = R.records_to_soa(dims, out)
+        for a, U in enumerate((0.01, -0.02, 0.005)):
+            np.testing.assert_allclose(got[a], U, rtol=1e-5)
