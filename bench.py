@@ -247,18 +247,24 @@ def run_ours(args):
         ms = e0.elapsed_time(e1)
         return max_over_ranks(ms, pg, dev), sts
 
-    def fluid_step_leg(steps, reps):
-        """FluidState::step without a moving interface on the workload's
-        geometry filled with one liquid: SL-RK2 advection, viscosity, gravity,
-        the warm-started projection, fields and diagnostics."""
+    def fluid_step_leg(steps, reps, two_phase=False):
+        """FluidState::step on the workload's geometry.  One liquid: SL-RK2
+        advection, viscosity, gravity, the warm-started projection, fields and
+        diagnostics.  Two phases (the workload's densities): a moving
+        interface, so Newtonian stress diffusion (liquid-metal viscosity
+        3.7e-7 m^2/s, air 1.8e-5 Pa s), capillary force (sigma 0.5 N/m, zero
+        curvature), face densities, the projection, fields."""
         ps = mhdproj.PressureProjection(case["dims"], case["h"], outlet=True, precision=args.precision,
                                         rel_tol=args.tol)
-        ps.set_coefficients(alpha, solid, case["rho_liquid"], case["rho_liquid"])
+        ps.set_coefficients(alpha, solid, case["rho_liquid"], case["rho_air"] if two_phase else case["rho_liquid"])
         su = [x.clone() for x in us]
-        dt_step = 5e-6
+        dt_step = 2e-6 if two_phase else 5e-6
+        nu_step = 3.7e-7 if two_phase else 1e-6
 
         def step_fn(prj):
-            st, _ = prj.fluid_step(su, dt_step, acceleration=(0.0, 0.0, -9.81), viscosity=1e-6, advection=True)
+            st, d = prj.fluid_step(su, dt_step, acceleration=(0.0, 0.0, -9.81), viscosity=nu_step, advection=True,
+                                   surface_tension=0.5, air_viscosity=1.8e-5)
+            st["viscous_substeps"] = d["viscous_substeps"]
             return st
 
         for _ in range(2):
@@ -267,7 +273,8 @@ def run_ours(args):
         prof_s = ps.profile_kernels(reps=reps)
         ps.close()
         return {"ms_per_step": ms_s / steps, "steps_per_s": 1000.0 * steps / ms_s, "iterations": sts_s[-1]["iterations"],
-                "dt": dt_step, "kinematic_viscosity": 1e-6,
+                "viscous_substeps": sts_s[-1]["viscous_substeps"], "dt": dt_step, "kinematic_viscosity": nu_step,
+                "densities": [case["rho_liquid"], case["rho_air"] if two_phase else case["rho_liquid"]],
                 "kernels": [{"name": k["name"], "us": k["ms"] * 1e3, "GBps": k["bytes"] / (k["ms"] * 1e-3) / 1e9}
                             for k in prof_s if k["name"].startswith("step_")]}
 
@@ -320,8 +327,9 @@ def run_ours(args):
     pr = make(args.precision)
     if args.step:
         out_s = fluid_step_leg(2, 1)
+        out_t = fluid_step_leg(2, 1, two_phase=True)
         if rank == 0:
-            print(json.dumps({"fluid_step": out_s}))
+            print(json.dumps({"fluid_step": out_s, "fluid_step_two_phase": out_t}))
         pr.close()
         return
     if args.kernels:
@@ -469,10 +477,11 @@ def run_ours(args):
         # throughput and device memory
         line["adjoint128_chain"] = chain_leg("adjoint128", 1.0, 8, 4, 3)
         line["column512"] = chain_leg("column512", 1.0, 4, 4, 3)
-        try:
-            line["fluid_step"] = fluid_step_leg(5, 10)
-        except mhdproj.ProjectionError as exc:
-            line["fluid_step"] = {"unavailable": str(exc)}
+        for key, tp in (("fluid_step", False), ("fluid_step_two_phase", True)):
+            try:
+                line[key] = fluid_step_leg(5, 10, two_phase=tp)
+            except mhdproj.ProjectionError as exc:
+                line[key] = {"unavailable": str(exc)}
         # CPU baseline: bounded sample of the reference algorithm on the host cores
         threads = os.cpu_count() or 1
         k_ref = reference_iterations(args.workload, args.tol)

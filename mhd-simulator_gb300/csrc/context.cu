@@ -105,6 +105,7 @@ struct mhdproj_ctx {
     float* st_mu = nullptr;
     float4 *st_t4 = nullptr, *st_y0 = nullptr, *st_f0 = nullptr;
     float2* st_t2 = nullptr;
+    float* st_t9 = nullptr;
     unsigned int* st_bound = nullptr;
     float step_dt = 0.f, step_nu = 0.f;
     float max_face_speed = 0.f, force_max = 0.f;
@@ -1219,6 +1220,9 @@ static int stress_buffers(mhdproj_ctx* ctx) {
     CK(dalloc(ctx, &ctx->st_t2, ctx->n * sizeof(float2)));
     CK(dalloc(ctx, &ctx->st_y0, ctx->n * sizeof(float4)));
     CK(dalloc(ctx, &ctx->st_f0, ctx->n * sizeof(float4)));
+    const long long ghosts = 2ll * ((long long)ctx->grid.ny * ctx->grid.nz + (long long)ctx->grid.nx * ctx->grid.nz +
+                                    (long long)ctx->grid.nx * ctx->grid.ny);
+    CK(dalloc(ctx, &ctx->st_t9, (ctx->n * 9 + ghosts) * sizeof(float)));
     CK(dalloc(ctx, &ctx->st_bound, sizeof(unsigned int)));
     return 0;
 }
@@ -1281,8 +1285,9 @@ static int diffuse_surface_stress(mhdproj_ctx* ctx, StepView S, float dt, uint32
         count = 1.0;
     } else {
         CK(cudaMemsetAsync(ctx->st_bound, 0, sizeof(unsigned int), ctx->stream));
+        launch_stress_coefficients(S, ctx->stream);
         launch_viscosity_bound(S, ctx->st_bound, ctx->stream);
-        ctx->launches += 3;
+        ctx->launches += 7;
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(ctx->h_st_scalars, ctx->st_bound, sizeof(unsigned int), cudaMemcpyDeviceToHost,
                            ctx->stream));
@@ -1339,10 +1344,12 @@ static int diffuse_surface_stress(mhdproj_ctx* ctx, StepView S, float dt, uint32
         return 0;
     }
     const float dt_sub = (float)((double)dt / (double)steps);
+    launch_stress_coefficients(S, ctx->stream);  // the cell viscosity the stresses read
+    ctx->launches += 1;
     for (uint32_t k = 0; k < steps; k++) {
         for (int a = 0; a < 3; a++) S.vel[a] = P[a];
-        launch_stress_diffuse(S, dt_sub, V, ctx->stream);
-        ctx->launches += 3;
+        launch_stress_diffuse(S, dt_sub, ctx->st_t9, V, ctx->stream);
+        ctx->launches += 6;
         int rc = copy3(P, V);
         if (rc) return rc;
     }

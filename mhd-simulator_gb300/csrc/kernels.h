@@ -219,13 +219,17 @@ void launch_viscous(const StepView& s, float* const out[3], cudaStream_t st);
 // read).  Cell viscosities into s.mu_c; the shared stress tensor into s.t4/t2;
 // RKC initial state into s.y0/f0; one RKC stage out = blend of the stage
 // arrays; one explicit Euler substep out = u + dt_sub a(u); the stability
-// bound (max over faces) into *bound (a float, cleared by the caller).
+// bound (max over faces) into *bound_bits (float bits, cleared by the caller).
 void launch_stress_coefficients(const StepView& s, cudaStream_t st);
 void launch_stress_tensor(const StepView& s, cudaStream_t st);
 void launch_stress_save_initial(const StepView& s, cudaStream_t st);
 // row: mu, nu, 1 - mu - nu, op, initial-operator weight
 void launch_stress_stage(const StepView& s, const float row[5], float* const io[3], cudaStream_t st);
-void launch_stress_diffuse(const StepView& s, float dt_sub, float* const out[3], cudaStream_t st);
+// t9: 9 n + 2 (ny nz + nx nz + nx ny) floats of scratch (per-cell normal and
+// ordered-pair shear stresses, and the shears one layer past the high faces);
+// needs s.mu_c filled by launch_stress_coefficients
+void launch_stress_diffuse(const StepView& s, float dt_sub, float* t9, float* const out[3], cudaStream_t st);
+// needs s.mu_c filled by launch_stress_coefficients
 void launch_viscosity_bound(const StepView& s, unsigned int* bound_bits, cudaStream_t st);
 uint32_t fields_groups(const StepView& s);
 // partials: 3 * fields_groups float4; scalars3: 3 float4 (the 12 diagnostics floats)

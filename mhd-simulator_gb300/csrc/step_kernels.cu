@@ -377,19 +377,19 @@ __device__ __forceinline__ P3 shifted(P3 q, int a, int d) {
     q.v[a] += d;
     return q;
 }
-__device__ float dynamic_mu(const StepView& s, P3 q) {  // :3-6
+__device__ __forceinline__ float dynamic_mu(const StepView& s, P3 q) {  // :3-6
     if (!fluid(s, q)) return 0.0f;
     const float t = fminf(fmaxf(occupancy(s, q), 0.0f), 1.0f);
     const float mu_l = s.nu * s.rho_l;
     return s.mu_air * (1.0f - t) + mu_l * t;
 }
-__device__ float coefficient_mu(const StepView& s, P3 q, bool cached) {  // :12-16
+__device__ __forceinline__ float coefficient_mu(const StepView& s, P3 q, bool cached) {  // :12-16
     if (!cached) return dynamic_mu(s, q);
     const P3 at = wrap_cell(s, q);
     if (!valid_cell(s, at)) return 0.0f;
     return s.mu_c[cell_index(s, at)];
 }
-__device__ float edge_mu(const StepView& s, P3 q, int i, int j, bool cached) {  // :17-24
+__device__ __forceinline__ float edge_mu(const StepView& s, P3 q, int i, int j, bool cached) {  // :17-24
     float total = 0.0f, count = 0.0f;
     for (int a = 0; a < 2; a++)
         for (int b = 0; b < 2; b++) {
@@ -403,11 +403,11 @@ __device__ float edge_mu(const StepView& s, P3 q, int i, int j, bool cached) {  
         }
     return total / fmaxf(count, 1.0f);
 }
-__device__ float normal_stress(const StepView& s, P3 q, int i, bool cached) {  // :30-33
+__device__ __forceinline__ float normal_stress(const StepView& s, P3 q, int i, bool cached) {  // :30-33
     if (!fluid(s, q)) return 0.0f;
     return 2.0f * coefficient_mu(s, q, cached) * (face(s, shifted(q, i, 1), i) - face(s, q, i)) / s.h;
 }
-__device__ float shear_stress(const StepView& s, P3 q, int i, int j, bool cached) {  // :34-44
+__device__ __forceinline__ float shear_stress(const StepView& s, P3 q, int i, int j, bool cached) {  // :34-44
     const P3 lower_i = shifted(q, j, -1), lower_j = shifted(q, i, -1);
     float ui1 = face(s, q, i), ui0 = face(s, lower_i, i);
     float uj1 = face(s, q, j), uj0 = face(s, lower_j, j);
@@ -418,13 +418,13 @@ __device__ float shear_stress(const StepView& s, P3 q, int i, int j, bool cached
     if (!open_face(s, lower_j, j) && open_face(s, q, j)) uj0 = -uj1;
     return edge_mu(s, q, i, j, cached) * (ui1 - ui0 + uj1 - uj0) / s.h;
 }
-__device__ float tensor_normal(const StepView& s, P3 q, int i) {  // :55-58
+__device__ __forceinline__ float tensor_normal(const StepView& s, P3 q, int i) {  // :55-58
     const P3 at = wrap_cell(s, q);
     if (!valid_cell(s, at)) return 0.0f;
     const float4 t = s.t4[cell_index(s, at)];
     return i == 0 ? t.x : (i == 1 ? t.y : t.z);
 }
-__device__ float tensor_shear(const StepView& s, P3 q, int i, int j) {  // :59-66
+__device__ __forceinline__ float tensor_shear(const StepView& s, P3 q, int i, int j) {  // :59-66
     const P3 at = wrap_cell(s, q);
     if (!valid_cell(s, at)) return shear_stress(s, q, i, j, true);
     const uint32_t c = cell_index(s, at);
@@ -433,15 +433,17 @@ __device__ float tensor_shear(const StepView& s, P3 q, int i, int j) {  // :59-6
     const float2 t = s.t2[c];
     return plane == 2 ? t.x : t.y;
 }
-__device__ float stress_acceleration(const StepView& s, P3 q, int i, bool cached) {  // :67-80
+__device__ __forceinline__ float stress_acceleration(const StepView& s, P3 q, int i, bool cached) {  // :67-80
     const P3 left = shifted(q, i, -1);
     float divergence = 0.0f;
     if (cached) {
         divergence = tensor_normal(s, q, i) - tensor_normal(s, left, i);
+#pragma unroll
         for (int j = 0; j < 3; j++)
             if (j != i) divergence += tensor_shear(s, shifted(q, j, 1), i, j) - tensor_shear(s, q, i, j);
     } else {
         divergence = normal_stress(s, q, i, false) - normal_stress(s, left, i, false);
+#pragma unroll
         for (int j = 0; j < 3; j++)
             if (j != i)
                 divergence += shear_stress(s, shifted(q, j, 1), i, j, false) - shear_stress(s, q, i, j, false);
@@ -484,8 +486,9 @@ __global__ void ks_stress_save_initial(StepView s) {  // stress_save_initial (st
 }
 // stress_stabilized (stabilized.wgsl:16-30): io holds the stage before the
 // previous one (read) and receives the new stage; s.vel the previous stage.
-__global__ void ks_stress_stage(StepView s, int axis, float bx, float by, float bz, float bw, float ix,
-                                float* __restrict__ io) {
+template <int AXIS>
+__global__ void ks_stress_stage(StepView s, float bx, float by, float bz, float bw, float ix, float* __restrict__ io) {
+    constexpr int axis = AXIS;
     const uint32_t f = blockIdx.x * WG + threadIdx.x;
     P3 pos;
     if (!face_position(s, axis, f, &pos)) return;
@@ -502,30 +505,270 @@ __global__ void ks_stress_stage(StepView s, int axis, float bx, float by, float 
     }
     io[f] = value;
 }
+// The uncached stress operator of stress_diffuse evaluated from per-cell
+// stresses: the 3 normal stresses and the shear stress of every ordered axis
+// pair (i, j) (the operator evaluates shear(q, i, j) for the face axis i, so
+// both orders are kept: they sum in different orders).  The cached cell
+// viscosity equals dynamic_mu() wherever the uncached operator reads it, so
+// every stress, and so every result, is the one the uncached operator
+// computes.  Layout: 9 planes of n floats.
+__device__ __forceinline__ int pair_slot(int i, int j) { return 3 + 2 * i + (j > i ? j - 1 : j); }
+// Interior cells (every neighbour the stresses touch inside the grid, no
+// wrap): the same stresses from ten fluid flags, seven cell viscosities and
+// twelve face values read at fixed strides.  F/M/U below follow face(),
+// open_face(), coefficient_mu() and edge_mu() term by term.
+__device__ __forceinline__ void stress_cells_interior(const StepView& s, uint32_t i, P3 q, float* __restrict__ t9) {
+    const uint32_t nx = s.dims[0], ny = s.dims[1];
+    const size_t n = s.dims[3];
+    const uint32_t cs[3] = {1u, nx, nx * ny};
+    // face index of position q in each axis array, and the strides of that array
+    const uint32_t fi[3] = {(uint32_t)q.v[0] + (nx + 1) * ((uint32_t)q.v[1] + ny * (uint32_t)q.v[2]),
+                            (uint32_t)q.v[0] + nx * ((uint32_t)q.v[1] + (ny + 1) * (uint32_t)q.v[2]), i};
+    const uint32_t fs[3][3] = {{1u, nx + 1, (nx + 1) * ny}, {1u, nx, nx * (ny + 1)}, {1u, nx, nx * ny}};
+    auto F = [&](int dx, int dy, int dz) {
+        return is_fluid_index(s, i + (uint32_t)(dx * (int)cs[0] + dy * (int)cs[1] + dz * (int)cs[2]));
+    };
+    auto M = [&](int dx, int dy, int dz) {
+        return s.mu_c[i + (uint32_t)(dx * (int)cs[0] + dy * (int)cs[1] + dz * (int)cs[2])];
+    };
+    const bool f0 = F(0, 0, 0);
+    const bool fm[3] = {F(-1, 0, 0), F(0, -1, 0), F(0, 0, -1)};
+    const bool fp[3] = {F(1, 0, 0), F(0, 1, 0), F(0, 0, 1)};
+    // fluid(q - e_a - e_b), a < b: (0,1), (0,2), (1,2)
+    const bool fmm[3] = {F(-1, -1, 0), F(-1, 0, -1), F(0, -1, -1)};
+    auto fmm_of = [&](int a, int b) { return fmm[a + b - 1]; };
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float v = 0.0f;
+        if (f0) {
+            const float lo = (fm[a] && f0) ? __ldg(s.vel[a] + fi[a]) : 0.0f;
+            const float hi = (f0 && fp[a]) ? __ldg(s.vel[a] + fi[a] + fs[a][a]) : 0.0f;
+            v = 2.0f * s.mu_c[i] * (hi - lo) / s.h;
+        }
+        t9[a * n + i] = v;
+    }
+    const float mu0 = s.mu_c[i];
+    const float mum[3] = {M(-1, 0, 0), M(0, -1, 0), M(0, 0, -1)};
+    const float mumm[3] = {M(-1, -1, 0), M(-1, 0, -1), M(0, -1, -1)};
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            if (a == b) continue;
+            // faces: (q, a), (q - e_b, a), (q, b), (q - e_a, b)
+            const bool o_ai1 = fm[a] && f0;               // open_face(q, a)
+            const bool o_ai0 = fmm_of(a, b) && fm[b];     // open_face(q - e_b, a)
+            const bool o_bj1 = fm[b] && f0;               // open_face(q, b)
+            const bool o_bj0 = fmm_of(a, b) && fm[a];     // open_face(q - e_a, b)
+            float ui1 = o_ai1 ? __ldg(s.vel[a] + fi[a]) : 0.0f;
+            float ui0 = o_ai0 ? __ldg(s.vel[a] + fi[a] - fs[a][b]) : 0.0f;
+            float uj1 = o_bj1 ? __ldg(s.vel[b] + fi[b]) : 0.0f;
+            float uj0 = o_bj0 ? __ldg(s.vel[b] + fi[b] - fs[b][a]) : 0.0f;
+            if (!o_ai1 && o_ai0) ui1 = -ui0;
+            if (!o_ai0 && o_ai1) ui0 = -ui1;
+            if (!o_bj1 && o_bj0) uj1 = -uj0;
+            if (!o_bj0 && o_bj1) uj0 = -uj1;
+            // edge_mu(q, a, b): cells q, q - e_b, q - e_a, q - e_a - e_b in that order
+            float total = 0.0f, count = 0.0f;
+            if (f0) { total += mu0; count += 1.0f; }
+            if (fm[b]) { total += mum[b]; count += 1.0f; }
+            if (fm[a]) { total += mum[a]; count += 1.0f; }
+            if (fmm_of(a, b)) { total += mumm[a + b - 1]; count += 1.0f; }
+            const float emu = total / fmaxf(count, 1.0f);
+            t9[pair_slot(a, b) * n + i] = emu * (ui1 - ui0 + uj1 - uj0) / s.h;
+        }
+}
+__device__ __forceinline__ bool stress_interior(const StepView& s, P3 q) {
+    bool interior = true;
+#pragma unroll
+    for (int a = 0; a < 3; a++) interior = interior && q.v[a] >= 1 && q.v[a] + 2 <= (int)s.dims[a];
+    return interior;
+}
+// Two launches over the cells, interior cells in one and the cells on the
+// grid's faces (the general stresses) in the other, so that no warp runs both
+// paths and each kernel's code stays small.
+__global__ void ks_stress_cells(StepView s, float* __restrict__ t9) {
+    const uint32_t i = blockIdx.x * WG + threadIdx.x;
+    if (i >= s.dims[3]) return;
+    const P3 q = cell_position(s, i);
+    if (stress_interior(s, q)) stress_cells_interior(s, i, q, t9);
+}
+// The shell of a box of extents d (positions with a coordinate at 0 or
+// d - 1), numbered densely so consecutive lanes take consecutive positions:
+// the z = 0 and z = d2-1 planes, the y = 0 and y = d1-1 rows of the planes
+// between, then the x = 0 and x = d0-1 positions of the rows between.  A box
+// with an extent below 3 has no interior: every position is listed.
+__host__ __device__ inline uint64_t shell_count(const int d[3]) {
+    const uint64_t n = (uint64_t)d[0] * d[1] * d[2];
+    if (d[0] < 3 || d[1] < 3 || d[2] < 3) return n;
+    return n - (uint64_t)(d[0] - 2) * (d[1] - 2) * (d[2] - 2);
+}
+__device__ __forceinline__ bool shell_position(const int d[3], uint32_t t, P3* q) {
+    const int nx = d[0], ny = d[1], nz = d[2];
+    if (nx < 3 || ny < 3 || nz < 3) {
+        if ((uint64_t)t >= (uint64_t)nx * ny * nz) return false;
+        q->v[0] = (int)(t % nx);
+        q->v[1] = (int)((t / nx) % ny);
+        q->v[2] = (int)(t / ((uint32_t)nx * ny));
+        return true;
+    }
+    const uint32_t plane = (uint32_t)(nx * ny), rows = (uint32_t)(2 * nx * (nz - 2)), cols = (uint32_t)(2 * (ny - 2) * (nz - 2));
+    if (t < 2 * plane) {
+        const uint32_t r = t % plane;
+        q->v[0] = (int)(r % nx);
+        q->v[1] = (int)(r / nx);
+        q->v[2] = t < plane ? 0 : nz - 1;
+        return true;
+    }
+    t -= 2 * plane;
+    if (t < rows) {
+        const uint32_t half = (uint32_t)(nx * (nz - 2)), r = t % half;
+        q->v[0] = (int)(r % nx);
+        q->v[1] = t < half ? 0 : ny - 1;
+        q->v[2] = 1 + (int)(r / nx);
+        return true;
+    }
+    t -= rows;
+    if (t < cols) {
+        const uint32_t half = (uint32_t)((ny - 2) * (nz - 2)), r = t % half;
+        q->v[0] = t < half ? 0 : nx - 1;
+        q->v[1] = 1 + (int)(r % (ny - 2));
+        q->v[2] = 1 + (int)(r / (ny - 2));
+        return true;
+    }
+    return false;
+}
+__host__ __device__ inline void cell_extents(const StepView& s, int d[3]) {
+    d[0] = (int)s.dims[0];
+    d[1] = (int)s.dims[1];
+    d[2] = (int)s.dims[2];
+}
+__global__ void ks_stress_cells_edge(StepView s, float* __restrict__ t9) {
+    P3 q;
+    int d[3];
+    cell_extents(s, d);
+    if (!shell_position(d, blockIdx.x * WG + threadIdx.x, &q)) return;
+    const uint32_t i = cell_index(s, q);
+    const size_t n = s.dims[3];
+    // compact loops: this kernel runs few cells, and unrolled general stresses
+    // overflow the instruction cache
+#pragma unroll 1
+    for (int a = 0; a < 3; a++) t9[a * n + i] = normal_stress(s, q, a, true);
+#pragma unroll 1
+    for (int a = 0; a < 3; a++)
+#pragma unroll 1
+        for (int b = 0; b < 3; b++)
+            if (a != b) t9[pair_slot(a, b) * n + i] = shear_stress(s, q, a, b, true);
+}
+__device__ __forceinline__ float cell_normal(const StepView& s, const float* __restrict__ t9, P3 q, int i) {
+    const P3 at = wrap_cell(s, q);
+    if (!valid_cell(s, at)) return 0.0f;  // normal_stress: not a fluid cell
+    return t9[(size_t)i * s.dims[3] + cell_index(s, at)];
+}
+// Shear stresses one layer past the high faces of the grid (q[j] = n_j; the
+// Euler operator reads shear(pos + e_j, i, j) there): for each j the plane of
+// the other two axes a < b, for i = a then i = b.  Layout: j = 0 planes, then
+// j = 1, then j = 2.
+__device__ __forceinline__ size_t ghost_index(const StepView& s, P3 q, int i, int j) {
+    const int a = j == 0 ? 1 : 0, b = j == 2 ? 1 : 2;
+    const size_t plane = (size_t)s.dims[a] * s.dims[b];
+    size_t base = 0;
+    if (j >= 1) base += 2ull * s.dims[1] * s.dims[2];
+    if (j >= 2) base += 2ull * s.dims[0] * s.dims[2];
+    return base + (i == a ? 0 : plane) + (size_t)q.v[a] + (size_t)s.dims[a] * (size_t)q.v[b];
+}
+__host__ __device__ inline uint64_t ghost_count(const StepView& s) {
+    return 2ull * ((uint64_t)s.dims[1] * s.dims[2] + (uint64_t)s.dims[0] * s.dims[2] + (uint64_t)s.dims[0] * s.dims[1]);
+}
+__global__ void ks_stress_ghosts(StepView s, float* __restrict__ g) {
+    uint64_t t = (uint64_t)blockIdx.x * WG + threadIdx.x;
+    if (t >= ghost_count(s)) return;
+    int j = 0;
+    for (; j < 3; j++) {
+        const int a = j == 0 ? 1 : 0, b = j == 2 ? 1 : 2;
+        const uint64_t span = 2ull * s.dims[a] * s.dims[b];
+        if (t < span) break;
+        t -= span;
+    }
+    const int a = j == 0 ? 1 : 0, b = j == 2 ? 1 : 2;
+    const uint64_t plane = (uint64_t)s.dims[a] * s.dims[b];
+    const int i = t < plane ? a : b;
+    const uint64_t r = t % plane;
+    P3 q;
+    q.v[j] = (int)s.dims[j];
+    q.v[a] = (int)(r % s.dims[a]);
+    q.v[b] = (int)(r / s.dims[a]);
+    g[ghost_index(s, q, i, j)] = shear_stress(s, q, i, j, true);
+}
+__device__ __forceinline__ float cell_shear(const StepView& s, const float* __restrict__ t9, P3 q, int i, int j) {
+    const P3 at = wrap_cell(s, q);
+    if (!valid_cell(s, at)) return t9[9ull * s.dims[3] + ghost_index(s, q, i, j)];  // one past a high face
+    return t9[(size_t)pair_slot(i, j) * s.dims[3] + cell_index(s, at)];
+}
 // stress_diffuse (:100-107): one explicit Euler substep.
-__global__ void ks_stress_diffuse(StepView s, int axis, float dt_sub, float* __restrict__ out) {
+template <int AXIS>
+__global__ void ks_stress_diffuse(StepView s, float dt_sub, const float* __restrict__ t9, float* __restrict__ out) {
+    constexpr int axis = AXIS;
     const uint32_t f = blockIdx.x * WG + threadIdx.x;
     P3 pos;
     if (!face_position(s, axis, f, &pos)) return;
     float value = 0.0f;
-    if (open_face(s, pos, axis)) value = face(s, pos, axis) + dt_sub * stress_acceleration(s, pos, axis, false);
+    if (open_face(s, pos, axis)) {
+        const P3 left = shifted(pos, axis, -1);
+        float divergence = cell_normal(s, t9, pos, axis) - cell_normal(s, t9, left, axis);
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+            if (j != axis)
+                divergence += cell_shear(s, t9, shifted(pos, j, 1), axis, j) - cell_shear(s, t9, pos, axis, j);
+        const float acc = divergence / (s.h * face_density(s, pos, axis));
+        value = face(s, pos, axis) + dt_sub * acc;
+    }
     out[f] = value;
 }
 // viscosity_bound (:81-96): 4 x the absolute row sum of rho^-1 div(tau) over
 // the open faces; the block maximum goes to *bound_bits as float bits (all
 // values are non-negative, so the unsigned maximum is the float maximum).
-__global__ void ks_viscosity_bound(StepView s, int axis, unsigned int* bound_bits) {
-    __shared__ float red[WG];
-    const uint32_t f = blockIdx.x * WG + threadIdx.x;
-    float bound = 0.0f;
-    P3 q;
-    if (face_position(s, axis, f, &q) && open_face(s, q, axis)) {
-        const P3 left = shifted(q, axis, -1);
-        float sum = dynamic_mu(s, q) + dynamic_mu(s, left);
-        for (int j = 0; j < 3; j++)
-            if (j != axis) sum += edge_mu(s, q, axis, j, false) + edge_mu(s, shifted(q, j, 1), axis, j, false);
-        bound = 4.0f * sum / (face_density(s, q, axis) * s.h * s.h);
+// The bound of an interior face (every cell it reads inside the grid, no
+// wrap): cell viscosities and fluid flags by fixed strides, summed in the
+// order of the general expression below.
+template <int AXIS>
+__device__ __forceinline__ float viscosity_bound_interior(const StepView& s, P3 q, bool* open) {
+    const uint32_t nx = s.dims[0], ny = s.dims[1];
+    const int cs[3] = {1, (int)nx, (int)(nx * ny)};
+    const uint32_t c = cell_index(s, q), l = c - (uint32_t)cs[AXIS];
+    *open = is_fluid_index(s, l) && is_fluid_index(s, c);
+    if (!*open) return 0.0f;
+    float sum = s.mu_c[c] + s.mu_c[l];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        if (j == AXIS) continue;
+        const uint32_t d = (uint32_t)cs[j];
+        // edge_mu(q, AXIS, j): q, q - e_j, q - e_AXIS, q - e_AXIS - e_j
+        float t1 = 0.0f, n1 = 0.0f;
+        const uint32_t e1[4] = {c, c - d, l, l - d};
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (is_fluid_index(s, e1[k])) {
+                t1 += s.mu_c[e1[k]];
+                n1 += 1.0f;
+            }
+        // edge_mu(q + e_j, AXIS, j): q + e_j, q, q + e_j - e_AXIS, q - e_AXIS
+        float t2 = 0.0f, n2 = 0.0f;
+        const uint32_t e2[4] = {c + d, c, l + d, l};
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (is_fluid_index(s, e2[k])) {
+                t2 += s.mu_c[e2[k]];
+                n2 += 1.0f;
+            }
+        sum += t1 / fmaxf(n1, 1.0f) + t2 / fmaxf(n2, 1.0f);
     }
+    const float al = s.occ[l], ar = s.occ[c];
+    const float rl = s.rho_air * (1.0f - al) + s.rho_l * al, rr = s.rho_air * (1.0f - ar) + s.rho_l * ar;
+    return 4.0f * sum / (0.5f * (rl + rr) * s.h * s.h);
+}
+__device__ __forceinline__ void block_max_to(float bound, unsigned int* bound_bits) {
+    __shared__ float red[WG];
     red[threadIdx.x] = bound;
     __syncthreads();
     for (int d = WG / 2; d > 0; d /= 2) {
@@ -537,6 +780,55 @@ __global__ void ks_viscosity_bound(StepView s, int axis, unsigned int* bound_bit
         // a non-finite bound is kept as the largest bit pattern: the host rejects it
         atomicMax(bound_bits, (b == b) ? __float_as_uint(b) : 0xFFFFFFFFu);
     }
+}
+// The face grid of AXIS: extents n + 1 along AXIS.  Its interior (shell
+// excluded) is exactly the faces whose cells all lie inside the grid.
+template <int AXIS>
+__host__ __device__ inline void face_extents(const StepView& s, int d[3]) {
+    cell_extents(s, d);
+    d[AXIS] += 1;
+}
+template <int AXIS>
+__device__ __forceinline__ float viscosity_bound_general(const StepView& s, P3 q) {
+    constexpr int axis = AXIS;
+    if (!open_face(s, q, axis)) return 0.0f;
+    const P3 left = shifted(q, axis, -1);
+    // the cached cell viscosity (ks_stress_coefficients) equals dynamic_mu()
+    float sum = coefficient_mu(s, q, true) + coefficient_mu(s, left, true);
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+        if (j != axis) sum += edge_mu(s, q, axis, j, true) + edge_mu(s, shifted(q, j, 1), axis, j, true);
+    return 4.0f * sum / (face_density(s, q, axis) * s.h * s.h);
+}
+// viscosity_bound (:81-96): 4 x the absolute row sum of rho^-1 div(tau) over
+// the open faces, maximum over faces into *bound_bits as float bits (values
+// are non-negative, so the unsigned maximum is the float maximum).  Interior
+// faces here, the face grid's shell in ks_viscosity_bound_edge.
+template <int AXIS>
+__global__ void ks_viscosity_bound(StepView s, unsigned int* bound_bits) {
+    const uint32_t f = blockIdx.x * WG + threadIdx.x;
+    float bound = 0.0f;
+    P3 q;
+    int d[3];
+    face_extents<AXIS>(s, d);
+    if (face_position(s, AXIS, f, &q)) {
+        bool interior = true;
+#pragma unroll
+        for (int a = 0; a < 3; a++) interior = interior && q.v[a] >= 1 && q.v[a] + 2 <= d[a];
+        if (interior) {
+            bool open;
+            bound = s.occ ? viscosity_bound_interior<AXIS>(s, q, &open) : viscosity_bound_general<AXIS>(s, q);
+        }
+    }
+    block_max_to(bound, bound_bits);
+}
+template <int AXIS>
+__global__ void ks_viscosity_bound_edge(StepView s, unsigned int* bound_bits) {
+    P3 q;
+    int d[3];
+    face_extents<AXIS>(s, d);
+    const float bound = shell_position(d, blockIdx.x * WG + threadIdx.x, &q) ? viscosity_bound_general<AXIS>(s, q) : 0.0f;
+    block_max_to(bound, bound_bits);
 }
 
 __global__ void ks_fields(StepView s, float4* __restrict__ cells, float4* __restrict__ partials) {
@@ -696,14 +988,31 @@ void launch_stress_save_initial(const StepView& s, cudaStream_t st) {
     ks_stress_save_initial<<<cell_blocks(s), WG, 0, st>>>(s);
 }
 void launch_stress_stage(const StepView& s, const float row[5], float* const io[3], cudaStream_t st) {
-    for (int a = 0; a < 3; a++)
-        ks_stress_stage<<<face_blocks(s, a), WG, 0, st>>>(s, a, row[0], row[1], row[2], row[3], row[4], io[a]);
+    ks_stress_stage<0><<<face_blocks(s, 0), WG, 0, st>>>(s, row[0], row[1], row[2], row[3], row[4], io[0]);
+    ks_stress_stage<1><<<face_blocks(s, 1), WG, 0, st>>>(s, row[0], row[1], row[2], row[3], row[4], io[1]);
+    ks_stress_stage<2><<<face_blocks(s, 2), WG, 0, st>>>(s, row[0], row[1], row[2], row[3], row[4], io[2]);
 }
-void launch_stress_diffuse(const StepView& s, float dt_sub, float* const out[3], cudaStream_t st) {
-    for (int a = 0; a < 3; a++) ks_stress_diffuse<<<face_blocks(s, a), WG, 0, st>>>(s, a, dt_sub, out[a]);
+void launch_stress_diffuse(const StepView& s, float dt_sub, float* t9, float* const out[3], cudaStream_t st) {
+    ks_stress_cells<<<cell_blocks(s), WG, 0, st>>>(s, t9);
+    int d[3];
+    cell_extents(s, d);
+    ks_stress_cells_edge<<<(unsigned)((shell_count(d) + WG - 1) / WG), WG, 0, st>>>(s, t9);
+    ks_stress_ghosts<<<(unsigned)((ghost_count(s) + WG - 1) / WG), WG, 0, st>>>(s, t9 + 9ull * s.dims[3]);
+    ks_stress_diffuse<0><<<face_blocks(s, 0), WG, 0, st>>>(s, dt_sub, t9, out[0]);
+    ks_stress_diffuse<1><<<face_blocks(s, 1), WG, 0, st>>>(s, dt_sub, t9, out[1]);
+    ks_stress_diffuse<2><<<face_blocks(s, 2), WG, 0, st>>>(s, dt_sub, t9, out[2]);
+}
+template <int AXIS>
+static void viscosity_bound_axis(const StepView& s, unsigned int* bound_bits, cudaStream_t st) {
+    int d[3];
+    face_extents<AXIS>(s, d);
+    ks_viscosity_bound<AXIS><<<face_blocks(s, AXIS), WG, 0, st>>>(s, bound_bits);
+    ks_viscosity_bound_edge<AXIS><<<(unsigned)((shell_count(d) + WG - 1) / WG), WG, 0, st>>>(s, bound_bits);
 }
 void launch_viscosity_bound(const StepView& s, unsigned int* bound_bits, cudaStream_t st) {
-    for (int a = 0; a < 3; a++) ks_viscosity_bound<<<face_blocks(s, a), WG, 0, st>>>(s, a, bound_bits);
+    viscosity_bound_axis<0>(s, bound_bits, st);
+    viscosity_bound_axis<1>(s, bound_bits, st);
+    viscosity_bound_axis<2>(s, bound_bits, st);
 }
 uint32_t fields_groups(const StepView& s) { return (s.dims[3] + WG - 1) / WG; }
 void launch_fields(const StepView& s, float4* cells, float4* partials, float4* scalars3, cudaStream_t st) {
