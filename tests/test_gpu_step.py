@@ -425,6 +425,49 @@ def test_reference_interface_step_bit_exact(gpu, oracle_lib, name, mu_air, nu):
     pr.close()
 
 
+def test_gb300_interface_step_stages(gpu, oracle_lib):
+    """GB300 solver with two densities (a moving interface): the step equals
+    the oracle's predict, stress diffusion (several Euler substeps) and capillary
+    viscous stages projected by a second context with a warm start, bit for
+    bit; fields with the curvature in the reserved lane."""
+    import mhdproj
+
+    torch = gpu
+    c = interface_case(seed=6)
+    dims = c["dims"]
+    nx, ny, nz = dims
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    dt, nu, mu_air, sigma = c["dt"], 1e-6, 4e-2, 0.07
+    acc = np.array([0.0, 0.0, -9.81], np.float32)
+
+    def ctx():
+        pr = mhdproj.PressureProjection(dims, c["h"], outlet=True, precision="fp32", rel_tol=1e-8)
+        pr.set_coefficients(t(c["alpha"]), t(c["solid"]), c["rho_liquid"], c["rho_air"])
+        return pr
+
+    a, b = ctx(), ctx()
+    u = [t(c["u"]), t(c["v"]), t(c["w"])]
+    st, d = a.fluid_step(u, dt, acceleration=tuple(acc), viscosity=nu, surface_tension=sigma, air_viscosity=mu_air,
+                         curvature=t(c["curvature"]))
+    g = oracle_lib.grid(nx, ny, nz, c["h"], c["rho_liquid"], c["rho_air"], 0, True)
+    _, cls = oracle_lib.classify(g, c["solid"])
+    mask = (cls != 0).astype(np.uint32)
+    p = oracle_lib.make_params(dims, c["h"], dt, c["rho_liquid"], c["rho_air"], True, 0, 1e-5, 0.0,
+                               int(mask.sum()), False, 1e6)
+    p.physical[2] = nu
+    occ = np.asarray(c["alpha"], np.float32).reshape(-1)
+    rec = R.soa_to_records(dims, c["u"], c["v"], c["w"])
+    pred = oracle_lib.predict(p, mask, rec)
+    status, sub, _, pred = oracle_lib.diffuse_surface_stress(p, mask, occ, pred, rec, mu_air, dt)
+    assert status == 0 and 1 < sub <= 8 and d["viscous_substeps"] == sub  # several Euler substeps
+    visc = oracle_lib.viscous_surface(p, mask, occ, pred, acc, curvature=c["curvature"].reshape(-1), sigma=sigma)
+    (u0, u1, u2), _, _ = b.project(tuple(t(x) for x in R.records_to_soa(dims, visc)), dt, warm_start=True)
+    for x, y in zip(u, (u0, u1, u2)):
+        assert torch.equal(x, y)
+    a.close()
+    b.close()
+
+
 def test_interface_step_substep_limit(gpu, oracle_lib):
     """More equivalent Euler substeps than the work limit: the reference's
     message, velocity restored."""
