@@ -395,6 +395,17 @@ def run_ours(args):
                                "true_relative_residual": st32[-1].true_relative_residual}
         line["mixed_vs_fp32"] = (1000.0 / ms_per) / (1000.0 / ms32)
         p32.close()
+        # BF16 levels, and the FP16 levels at a 1e-8 relative residual
+        for key, prec, tol in (("bf16_levels", "bf16", args.tol), ("fp16_tol_1e-8", "fp16", 1e-8)):
+            pv = mhdproj.PressureProjection(case["dims"], case["h"], outlet=True, precision=prec, rel_tol=tol)
+            for _ in range(2):
+                step(pv)
+            msv, stv = timed(pv, max(3, args.steps // 2))
+            msv /= len(stv)
+            line[key] = {"projections_per_s": 1000.0 / msv, "ms_per_step": msv, "iterations": stv[-1].iterations,
+                         "refinements": stv[-1].refinements,
+                         "true_relative_residual": stv[-1].true_relative_residual}
+            pv.close()
         # adjoint / forward cost on the same coefficients
         gu = tuple(torch.randn_like(x) for x in us)
 

@@ -226,6 +226,45 @@ def test_chain_gradient_matches_oracle_and_finite_differences(gpu, oracle_lib):
         assert abs(fd - ad) <= 1e-4 * abs(fd)
 
 
+def test_chain_gradient_full_size_16_directions(gpu):
+    """The 128^3 adjoint configuration in full: K = 8 steps, checkpoints every
+    4, gradient of the outlet-plane objective against central differences of
+    the GPU forward chain on 16 seeded directions.  The chain is affine in f
+    for fixed coefficients, so J is quadratic and a central difference has no
+    truncation error at any step: eps = 100 |f| / |d| lifts J(f + eps d) -
+    J(f - eps d) far above the FP32 rounding of J (at eps = 1e-3 |f| / |d| the
+    difference is about 1e-7 J, the size of that rounding; the FP64 oracle's
+    chain, differenced at 1e-3 |f|, checks the same gradient on the 32^3
+    case).  The comparison measures the adjoint's accuracy, to 1e-4
+    relative."""
+    import mhdproj
+
+    torch = gpu
+    c = synth.make_case("adjoint128")
+    pr = make(mhdproj, c, precision="fp16", rel_tol=1e-10)
+    a, s, us = tensors(torch, c)
+    pr.set_coefficients(a, s, c["rho_liquid"], c["rho_air"])
+    f = [torch.from_numpy(x).cuda() for x in (c["fu"], c["fv"], c["fw"])]
+    steps, every = c["steps"], c["checkpoint_every"]
+    _, J, _ = pr.chain_forward(us, tuple(f), c["dt"], steps, every)
+    grad, _ = pr.chain_backward(us)
+    fn = math.sqrt(sum(float((x.double() ** 2).sum()) for x in f))
+    gen = torch.Generator(device="cuda").manual_seed(16)
+    worst = 0.0
+    for _ in range(16):
+        d = [torch.randn(x.shape, generator=gen, device="cuda", dtype=torch.float32) * (x != 0) for x in f]
+        dn = math.sqrt(sum(float((x.double() ** 2).sum()) for x in d))
+        eps = 100.0 * fn / dn
+        fp = tuple((x + eps * y).contiguous() for x, y in zip(f, d))
+        fm = tuple((x - eps * y).contiguous() for x, y in zip(f, d))
+        _, Jp, _ = pr.chain_forward(us, fp, c["dt"], steps, every)
+        _, Jm, _ = pr.chain_forward(us, fm, c["dt"], steps, every)
+        fd = (Jp - Jm) / (2 * eps)
+        ad = sum(float((g.double() * y.double()).sum()) for g, y in zip(grad, d))
+        worst = max(worst, abs(fd - ad) / abs(fd))
+    assert worst < 1e-4, worst
+
+
 def test_failures_leave_outputs_untouched(gpu):
     import mhdproj
 
