@@ -140,3 +140,57 @@ def test_stress_diffusion_keeps_uniform_periodic_flow(oracle_lib):
         got = R.records_to_soa(dims, out)
         for a, U in enumerate((0.01, -0.02, 0.005)):
             np.testing.assert_allclose(got[a], U, rtol=1e-5)
+
+
+def test_capillary_force_of_a_planar_interface(oracle_lib):
+    """viscous() with a moving interface on a fluid at rest, no gravity:
+    across a face between liquid fractions a_L and a_R with uniform curvature
+    k the capillary acceleration is sigma k (a_R - a_L) / (h rho_face)
+    (solver.wgsl:52-57, :152-153), applied over dt and scaled by the
+    mobility times rho_face / rho_l."""
+    dims = (6, 4, 4)
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    h, dt, sigma, k = 1e-3, 1e-5, 0.5, 250.0
+    rho_l, rho_a = 1000.0, 1.2
+    p = oracle_lib.make_params(dims, h, dt, rho_l, rho_a, True, 6, 1e-5, 1e-5, n, False, 1e6)
+    mask = np.ones(n, np.uint32)
+    x = np.arange(n) % nx
+    occ = np.clip((x - 1.0) / 3.0, 0.0, 1.0).astype(np.float32)  # 0, 0, 1/3, 2/3, 1, 1 along x
+    zero = np.zeros(((nx + 1) * (ny + 1) * (nz + 1), 4), np.float32)
+    curv = np.full(n, k, np.float32)
+    out = oracle_lib.viscous_surface(p, mask, occ, zero, np.zeros(3, np.float32), curvature=curv, sigma=sigma)
+    u = R.records_to_soa(dims, out)[0]
+    for f in range(1, nx):
+        al, ar = float(occ[f - 1]), float(occ[f])
+        rl, rr = rho_a * (1 - al) + rho_l * al, rho_a * (1 - ar) + rho_l * ar
+        rf = 0.5 * (rl + rr)
+        beta = (rho_l / rf) * (rf / rho_l)
+        want = dt * (sigma * k * (ar - al) / h / rf) * beta
+        np.testing.assert_allclose(u[:, :, f], want, rtol=2e-6, atol=1e-12)
+
+
+def test_stress_diffusion_keeps_linear_shear_flow(oracle_lib):
+    """u_x = gamma y between two walls in y (periodic x and z) in one liquid
+    of constant viscosity: the stress is uniform, its divergence vanishes
+    inside, and only the faces next to the walls feel the no-slip ghosts."""
+    dims = (6, 8, 4)
+    nx, ny, nz = dims
+    n = nx * ny * nz
+    h, dt = 1e-3, 1e-4
+    p = oracle_lib.make_params(dims, h, dt, 1000.0, 999.0, True, 5, 1e-5, 1e-5, n, False, 1e6)
+    p.physical[2] = 1e-6
+    mask = np.ones(n, np.uint32)
+    occ = np.ones(n, np.float32)
+    gamma = 10.0
+    u = np.zeros((nz, ny, nx + 1), np.float32)
+    for y in range(ny):
+        u[:, y, :] = gamma * (y + 0.5 - ny / 2) * h
+    v = np.zeros((nz, ny + 1, nx), np.float32)
+    w = np.zeros((nz + 1, ny, nx), np.float32)
+    rec = R.soa_to_records(dims, u, v, w)
+    st, sub, _, out = oracle_lib.diffuse_surface_stress(p, mask, occ, rec, rec, 1e-3, dt)
+    assert st == 0 and sub >= 1
+    uo = R.records_to_soa(dims, out)[0]
+    np.testing.assert_allclose(uo[:, 1:ny - 1, :], u[:, 1:ny - 1, :], rtol=1e-5, atol=1e-9)
+    assert np.all(np.abs(uo[:, 0, :]) < np.abs(u[:, 0, :]))  # the walls slow the outer rows
