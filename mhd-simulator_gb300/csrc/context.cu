@@ -83,6 +83,9 @@ struct mhdproj_ctx {
     // host-buffer staging
     float *s_alpha = nullptr, *s_u = nullptr, *s_v = nullptr, *s_w = nullptr, *s_p = nullptr;
     uint8_t* s_solid = nullptr;
+    // copy streams of the host-buffer path (created with its staging buffers)
+    cudaStream_t cp[2] = {nullptr, nullptr};
+    cudaEvent_t cp_ev[3] = {nullptr, nullptr, nullptr};
     // chain
     float *c_cur[3] = {nullptr, nullptr, nullptr}, *c_star[3] = {nullptr, nullptr, nullptr};
     float *c_lam[3] = {nullptr, nullptr, nullptr}, *c_lam2[3] = {nullptr, nullptr, nullptr};
@@ -425,6 +428,10 @@ extern "C" void mhdproj_destroy(mhdproj_ctx* ctx) {
     if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
     if (ctx->h_flag) cudaFreeHost(ctx->h_flag);
     if (ctx->h_topo) cudaFreeHost(ctx->h_topo);
+    for (cudaStream_t c : ctx->cp)
+        if (c) cudaStreamDestroy(c);
+    for (cudaEvent_t e : ctx->cp_ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->h_st_scalars) cudaFreeHost(ctx->h_st_scalars);
     if (ctx->ev_a) cudaEventDestroy(ctx->ev_a);
     if (ctx->ev_b) cudaEventDestroy(ctx->ev_b);
@@ -834,21 +841,58 @@ extern "C" int mhdproj_project_host(mhdproj_ctx* ctx, const float* alpha, const 
         CK(dalloc(ctx, &ctx->s_w, ctx->nfz * 4));
         CK(dalloc(ctx, &ctx->s_p, ctx->n * 4));
     }
+    if (!ctx->cp[0]) {
+        for (int k = 0; k < 2; k++) CK(cudaStreamCreateWithFlags(&ctx->cp[k], cudaStreamNonBlocking));
+        for (int k = 0; k < 3; k++) CK(cudaEventCreateWithFlags(&ctx->cp_ev[k], cudaEventDisableTiming));
+    }
+    // The copies run on three streams (the context's and two copy streams),
+    // each array in three slices, so several copy engines share the link;
+    // the face velocities arrive while the coefficients are being built.
     cudaStream_t s = ctx->stream;
-    CK(cudaMemcpyAsync(ctx->s_alpha, alpha, ctx->n * 4, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(ctx->s_solid, solid, ctx->n, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(ctx->s_u, usx, ctx->nfx * 4, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(ctx->s_v, usy, ctx->nfy * 4, cudaMemcpyHostToDevice, s));
-    CK(cudaMemcpyAsync(ctx->s_w, usz, ctx->nfz * 4, cudaMemcpyHostToDevice, s));
-    int rc = mhdproj_set_coefficients(ctx, ctx->s_alpha, ctx->s_solid, rho_liquid, rho_air);
+    cudaStream_t st3[3] = {s, ctx->cp[0], ctx->cp[1]};
+    auto spread = [&](void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) -> int {
+        const size_t slice = (bytes / 3 + 255) & ~(size_t)255;
+        for (int k = 0; k < 3; k++) {
+            const size_t off = std::min(bytes, slice * (size_t)k), end = std::min(bytes, slice * (size_t)(k + 1));
+            if (end > off)
+                CK(cudaMemcpyAsync((char*)dst + off, (const char*)src + off, end - off, kind, st3[k]));
+        }
+        return 0;
+    };
+    // the copy streams start after the context stream's earlier work
+    CK(cudaEventRecord(ctx->cp_ev[0], s));
+    for (int k = 0; k < 2; k++) CK(cudaStreamWaitEvent(ctx->cp[k], ctx->cp_ev[0], 0));
+    int rc = spread(ctx->s_alpha, alpha, ctx->n * 4, cudaMemcpyHostToDevice);
+    if (!rc) rc = spread(ctx->s_solid, solid, ctx->n, cudaMemcpyHostToDevice);
     if (rc) return rc;
+    for (int k = 0; k < 2; k++) {
+        CK(cudaEventRecord(ctx->cp_ev[1 + k], ctx->cp[k]));
+        CK(cudaStreamWaitEvent(s, ctx->cp_ev[1 + k], 0));  // alpha and solid complete on the context stream
+    }
+    // face velocities on the copy streams, behind the coefficient set-up
+    CK(cudaMemcpyAsync(ctx->s_u, usx, ctx->nfx * 4, cudaMemcpyHostToDevice, ctx->cp[0]));
+    CK(cudaMemcpyAsync(ctx->s_v, usy, ctx->nfy * 4, cudaMemcpyHostToDevice, ctx->cp[1]));
+    CK(cudaMemcpyAsync(ctx->s_w, usz, ctx->nfz * 4, cudaMemcpyHostToDevice, ctx->cp[0]));
+    rc = mhdproj_set_coefficients(ctx, ctx->s_alpha, ctx->s_solid, rho_liquid, rho_air);
+    if (rc) return rc;
+    for (int k = 0; k < 2; k++) {
+        CK(cudaEventRecord(ctx->cp_ev[1 + k], ctx->cp[k]));
+        CK(cudaStreamWaitEvent(s, ctx->cp_ev[1 + k], 0));
+    }
     rc = mhdproj_project(ctx, ctx->s_u, ctx->s_v, ctx->s_w, ctx->s_u, ctx->s_v, ctx->s_w, ctx->s_p, dt, warm_start,
                          stats);
     if (rc) return rc;
-    CK(cudaMemcpyAsync(uox, ctx->s_u, ctx->nfx * 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(uoy, ctx->s_v, ctx->nfy * 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(uoz, ctx->s_w, ctx->nfz * 4, cudaMemcpyDeviceToHost, s));
-    if (p_out) CK(cudaMemcpyAsync(p_out, ctx->s_p, ctx->n * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(ctx->cp_ev[0], s));
+    for (int k = 0; k < 2; k++) CK(cudaStreamWaitEvent(ctx->cp[k], ctx->cp_ev[0], 0));
+    rc = spread(uox, ctx->s_u, ctx->nfx * 4, cudaMemcpyDeviceToHost);
+    if (!rc) rc = spread(uoy, ctx->s_v, ctx->nfy * 4, cudaMemcpyDeviceToHost);
+    if (!rc) rc = spread(uoz, ctx->s_w, ctx->nfz * 4, cudaMemcpyDeviceToHost);
+    if (!rc && p_out) rc = spread(p_out, ctx->s_p, ctx->n * 4, cudaMemcpyDeviceToHost);
+    if (rc) return rc;
+    for (int k = 0; k < 2; k++) {
+        CK(cudaEventRecord(ctx->cp_ev[1 + k], ctx->cp[k]));
+        CK(cudaStreamWaitEvent(s, ctx->cp_ev[1 + k], 0));
+    }
     return wait_stream(ctx);
 }
 
