@@ -19,6 +19,16 @@
 //                   speed, pressure and divergence, force, reserved) and the
 //                   per-workgroup max/sum reductions;
 //   ks_diagnostics  diagnostics (:286-291): the single-workgroup final pass.
+// With a moving interface (two densities) viscous adds the capillary force
+// with face densities, and the Newtonian stresses of src/fluid/viscosity.wgsl
+// diffuse the predicted velocity first (diffuse_surface_stress,
+// src/fluid/mod.rs:1160-1240):
+//   ks_viscosity_bound(_edge)  the stability bound, max over faces;
+//   ks_stress_coefficients     the cell viscosity of the step;
+//   ks_stress_cells(_edge), ks_stress_ghosts, ks_stress_diffuse
+//                              one explicit Euler substep;
+//   ks_stress_tensor, ks_stress_save_initial, ks_stress_stage
+//                              the damped RKC2 stages (stabilized.wgsl).
 // Faces are the SoA arrays of include/mhdproj.h, one launch per axis.  The
 // arithmetic keeps the reference's operation order without fused
 // multiply-adds (this unit is compiled with -fmad=false) and the reductions
