@@ -3,7 +3,8 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links this code;
  * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it,
- * and only as the checker or the timed CPU baseline.
+ * and only as the expected results the GPU path is compared with or as the
+ * timed CPU baseline.
  *
  * Two parts:
  *

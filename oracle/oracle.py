@@ -1,8 +1,8 @@
 """ctypes binding of the CPU oracle (oracle/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
-and by bench.py's CPU-baseline leg, and there only as the checker or as the
-timed CPU baseline.  The product library never loads it.
+and by bench.py's CPU-baseline leg, and there only as the expected results the
+GPU path is compared with or as the timed CPU baseline.  The product library never loads it.
 
 ``oref_*`` restates the reference projection in FP32 with the reference's
 buffer layout (vec4 per (n+1)^3 face-cell); ``onat_*`` solves the GB300
