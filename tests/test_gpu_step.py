@@ -518,3 +518,68 @@ def test_export_fields_round_trip(gpu, oracle_lib, tmp_path):
     assert "Create new frame directory" in str(e.value)
     assert (frame / "fluid.bin").read_bytes() == raw
     pr.close()
+
+
+def test_step_and_fields_argument_errors(gpu, oracle_lib):
+    """Invalid timesteps, viscosities and surface parameters are refused with
+    the reference's validation text; nothing is touched."""
+    import mhdproj
+
+    torch = gpu
+    c = single_phase(R.wall_case((17, 13, 9), (0, 0, 0), True, False), dt=0.02)
+    pr = make_ref_ctx(mhdproj, torch, c, "jacobi")
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    u = [t(c["u"]), t(c["v"]), t(c["w"])]
+    before = [a.clone() for a in u]
+    for kw in (dict(dt=0.0), dict(dt=float("nan")), dict(dt=0.02, viscosity=-1.0),
+               dict(dt=0.02, surface_tension=-1.0), dict(dt=0.02, air_viscosity=float("inf"))):
+        dt = kw.pop("dt")
+        with pytest.raises(mhdproj.ProjectionError) as e:
+            pr.fluid_step(u, dt, **kw)
+        assert e.value.status == "invalid argument"
+    for a, b in zip(u, before):
+        assert torch.equal(a, b)
+    with pytest.raises(mhdproj.ProjectionError):
+        pr.fields(u, 0.0)
+    pr.close()
+
+
+def test_gb300_step_with_em_force(gpu, oracle_lib):
+    """GB300 solver with an EM force density: the step equals the oracle's
+    predict + viscous (with the force) projected by a second context."""
+    import mhdproj
+    from mhdproj import synth
+
+    torch = gpu
+    c = synth.make_case("jet64", scale=0.5)
+    dims = c["dims"]
+    nx, ny, nz = dims
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    dt, nu = 2e-5, 1e-6
+    acc = np.array([0.0, 0.0, -9.81], np.float32)
+    rng = np.random.default_rng(9)
+    em = (rng.standard_normal((nz, ny, nx, 4)) * 1e4).astype(np.float32)
+
+    def ctx():
+        pr = mhdproj.PressureProjection(dims, c["h"], outlet=True, precision="bf16", rel_tol=1e-8)
+        pr.set_coefficients(t(c["alpha"]), t(c["solid"]), c["rho_liquid"], c["rho_liquid"])
+        return pr
+
+    a, b = ctx(), ctx()
+    u = [t(c["u"]), t(c["v"]), t(c["w"])]
+    a.fluid_step(u, dt, acceleration=tuple(acc), viscosity=nu, advection=True, em_force=t(em))
+    g = oracle_lib.grid(nx, ny, nz, c["h"], c["rho_liquid"], c["rho_liquid"], 0, True)
+    _, cls = oracle_lib.classify(g, c["solid"])
+    mask = (cls != 0).astype(np.uint32)
+    p = oracle_lib.make_params(dims, c["h"], dt, c["rho_liquid"], c["rho_liquid"], False, 0, 1e-5, 0.0,
+                               int(mask.sum()), False, 1e6)
+    p.physical[2] = nu
+    p.flags[1] = 1
+    pred = oracle_lib.predict(p, mask, R.soa_to_records(dims, c["u"], c["v"], c["w"]))
+    visc = oracle_lib.viscous(p, mask, np.asarray(c["alpha"], np.float32).reshape(-1), pred, acc,
+                              em=em.reshape(-1, 4))
+    (u0, u1, u2), _, _ = b.project(tuple(t(x) for x in R.records_to_soa(dims, visc)), dt, warm_start=True)
+    for x, y in zip(u, (u0, u1, u2)):
+        assert torch.equal(x, y)
+    a.close()
+    b.close()
