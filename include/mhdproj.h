@@ -44,7 +44,8 @@ typedef enum {
     MHDPROJ_ERR_NO_PROGRESS = 5,    /* "Fluid pressure iteration made no progress" */
     MHDPROJ_ERR_STATE = 6,          /* call order (e.g. project before set_coefficients) */
     MHDPROJ_ERR_OUT_OF_MEMORY = 7,  /* workspace does not fit */
-    MHDPROJ_ERR_TIMEOUT = 8         /* a bounded host wait on the device expired */
+    MHDPROJ_ERR_TIMEOUT = 8,        /* a bounded host wait on the device expired */
+    MHDPROJ_ERR_UNSUPPORTED = 9     /* a reference branch this library does not build */
 } mhdproj_status;
 
 typedef enum {
@@ -334,6 +335,99 @@ int mhdproj_hierarchy(const uint32_t dims[4], uint32_t *levels, uint64_t *coarse
  * encodes mask[i] = class | root << 2 (class 1 member, 2 root).  Returns the
  * component count. */
 uint32_t mhdproj_anchors(uint32_t *mask, const uint32_t dims[3], uint32_t periodic);
+
+/* ---------------------------------------------------------------------------
+ * EM induction step: replaces EmState::advance_to (src/em/mod.rs:863-1090)
+ * with its passes in src/em/induction.wgsl.
+ *
+ * The magnetic vector potential lives on the grid's edges: x-edges
+ * (nx x (ny+1) x (nz+1)), then y-edges, then z-edges, each block x-fastest
+ * (src/em/common.wgsl:3-6).  A step solves the backward-Euler curl-curl
+ * system for the reaction potential with Jacobi-preconditioned CG, computes
+ * B, J, the Lorentz force J x B and Joule heat per cell, and commits or rolls
+ * back.  The applied potential A_s of coils and magnets is an input (the
+ * reference's source pass, src/em/source.wgsl, is not built); so is the
+ * motional EMF (src/em/motion.wgsl).  Not built either: the nodal
+ * preconditioner that the reference switches to after 1024 Jacobi
+ * iterations when max_iterations exceeds 1024 (reported as
+ * MHDPROJ_ERR_UNSUPPORTED with the state restored), and body integrals.
+ * ------------------------------------------------------------------------- */
+typedef struct mhdproj_em_ctx mhdproj_em_ctx;
+
+typedef enum {
+    MHDPROJ_EM_INDUCTION = 0,   /* Mode::Induction: conductors, time steps */
+    MHDPROJ_EM_APPLIED = 1      /* Mode::Applied: every cell is vacuum, initial solves only */
+} mhdproj_em_mode;
+
+typedef struct {
+    uint32_t nx, ny, nz;
+    float cell_m;               /* GridSi::cell_m */
+    float origin_m[3];          /* GridSi::origin_m (edge positions for applied fields) */
+    double dt_s;                /* EmConfig::dt_s */
+    float relative_tolerance;   /* EmConfig::relative_tolerance */
+    uint32_t max_iterations;    /* EmConfig::max_iterations */
+    int32_t mode;               /* mhdproj_em_mode */
+} mhdproj_em_config;
+
+/* Diagnostics (src/em/mod.rs:33-46) and the solver's status record. */
+typedef struct {
+    float maxima[4];            /* max |B| T, |J| A/m^2, |J x B| N/m^3, heat W/m^3 */
+    float force_n[3];           /* sum of J x B over the cells, N */
+    float power_w;              /* Joule power, W */
+    float divergence_j_scaled;  /* max |div J| h^2 per cell, A */
+    float max_edge_j;           /* max |J| on an edge */
+    float divergence_b_scaled;  /* max |div B| h, T */
+    float magnetic_energy_j;
+    float applied_max_t;
+    float reaction_max_t;
+    uint32_t iterations;
+    float relative_residual;    /* sqrt(rr / bb) of the accepted solve */
+    float conductivity_range[2];/* min sigma > 0 and max sigma over edges, S/m */
+    float device_ms;            /* device time of the step */
+    double elapsed_ms;          /* host time of the call */
+    float status[8];            /* (rz, rr, bb, threshold, alpha, beta, iterations, state) */
+} mhdproj_em_diagnostics;
+
+/* Arrays mhdproj_em_copy can read. */
+typedef enum {
+    MHDPROJ_EM_REACTION = 0,            /* accepted reaction potential, E floats */
+    MHDPROJ_EM_PREVIOUS = 1,            /* previous accepted reaction potential, E floats */
+    MHDPROJ_EM_APPLIED_POTENTIAL = 2,   /* applied potential A_s, E floats */
+    MHDPROJ_EM_CELLS = 3,               /* per cell (B,|B|, J,|J|, JxB,heat, applied B,|applied B|), 16 floats */
+    MHDPROJ_EM_WORK = 4,                /* per edge (x, r, p, w) as the reference's work record, 4 floats */
+    MHDPROJ_EM_EDGE_COEFFICIENTS = 5    /* per edge (sigma, diagonal, flags, motional EMF), 4 floats */
+} mhdproj_em_array;
+
+int mhdproj_em_create(const mhdproj_em_config *config, mhdproj_em_ctx **out);
+void mhdproj_em_destroy(mhdproj_em_ctx *ctx);
+const char *mhdproj_em_last_error(const mhdproj_em_ctx *ctx);
+int mhdproj_em_set_stream(mhdproj_em_ctx *ctx, void *stream);
+/* out: nx, ny, nz, cells, x-edges, y-edges, z-edges, edges. */
+int mhdproj_em_sizes(const mhdproj_em_ctx *ctx, uint64_t out[8]);
+/* Material ids per cell (device; bit 31 marks a partial cell whose fraction
+ * is in bits 8..30 and material in bits 0..7) with (conductivity S/m,
+ * relative permeability) rows per id (host, `count` rows, row 0 = the
+ * background).  Builds the edge coefficients (coefficients +
+ * coefficient_check, induction.wgsl:105-131; also clears the motional EMF).
+ * Fails with the reference's message when a conductor touches the outer
+ * boundary (mod.rs:563-567). */
+int mhdproj_em_set_materials(mhdproj_em_ctx *ctx, const uint32_t *materials, const float *properties,
+                             uint32_t count, float conductivity_range[2]);
+/* Motional EMF per edge (device, E floats; NULL clears it). */
+int mhdproj_em_set_motional_emf(mhdproj_em_ctx *ctx, const float *emf);
+/* Overwrites the accepted reaction potential (device, E floats). */
+int mhdproj_em_set_reaction(mhdproj_em_ctx *ctx, const float *a);
+/* One step to time_s (initial != 0: the source-only solve EmState::new and
+ * evaluate_applied run).  applied: A_s at time_s (device, E floats), or NULL
+ * when the applied field is unchanged.  On failure the state is restored. */
+int mhdproj_em_advance(mhdproj_em_ctx *ctx, double time_s, int initial, const float *applied,
+                       mhdproj_em_diagnostics *diagnostics);
+/* Copies one mhdproj_em_array into `out` (device). */
+int mhdproj_em_copy(mhdproj_em_ctx *ctx, int which, float *out);
+/* q = A p with (air_stencil != 0) or without the seven-point air stencil
+ * (the operator check of src/em/tests.rs:666-738). */
+int mhdproj_em_apply_operator(mhdproj_em_ctx *ctx, const float *p, float *q, int air_stencil);
+int mhdproj_em_kernel_launches(const mhdproj_em_ctx *ctx, uint64_t *count);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,1215 @@
+// em_solver.cu -- the implicit EM induction step of the reference
+// (EmState::advance_to, src/em/mod.rs:863-1090, on the passes of
+// src/em/induction.wgsl) as sm_103a kernels behind the mhdproj_em_* C ABI.
+//
+// Discretisation (reference): magnetic vector potential on the edges of the
+// cell grid, x-edges then y-edges then z-edges, each block x-fastest
+// (src/em/common.wgsl:3-6).  One backward-Euler step solves
+//   (C^T nu C + G + mu0 sigma h^2/dt) x = b
+// for the reaction increment x with Jacobi-preconditioned CG, where C is the
+// edge-to-face curl, nu the face reluctivity, G the nodal gauge on
+// non-conducting nodes and b the applied-field, history and motional terms
+// (induction.wgsl:132-145).  The host sequence -- power-of-two residual
+// rescaling, the prediction guard, 32-iteration batches with a status read
+// between them, true-residual restarts, acceptance, rollback and the
+// prediction history -- follows advance_to.
+//
+// GB300 layout: every vec4 record of the reference is split into planar FP32
+// arrays (applied potential, its history, edge conductivity, diagonal,
+// motional EMF, the CG vectors) plus one byte of gauge/stencil flags per edge;
+// cell conductivity and permeability and the three face reluctivity grids are
+// tabulated once per material update instead of being decoded from material
+// ids inside every operator application.  The 32-iteration batch runs as one
+// CUDA graph.
+//
+// Arithmetic: FP32 in the shader's operation order, compiled without fused
+// multiply-adds; the workgroup sums are 256-lane trees and the single-block
+// reductions accumulate their partials with a stride of 256 before the tree,
+// so results are bit-identical to the FP32 restatement of the same shader.
+//
+// Not built (the caller supplies what they produce): the coil/magnet source
+// summation (src/em/source.wgsl, src/em/sources.rs), the nodal
+// preconditioner that advance_to switches to after 1024 Jacobi iterations
+// when max_iterations exceeds 1024 (src/em/nodal.rs; reported as
+// MHDPROJ_ERR_UNSUPPORTED at that point), and the per-body force integrals.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "mhdproj.h"
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr uint32_t kBatch = 32;        // iterations between status reads (mod.rs:952)
+constexpr uint32_t kNodalSwitch = 1024;  // mod.rs:892
+
+struct EmDev {
+    uint32_t n[3], cells;
+    uint32_t e[3], E;
+    uint32_t initial;  // control.y: the applied-field solve has no mass term
+    float pf;          // origin.w: increment prediction factor
+    float dt, mu0, h, tol2;
+    // edges
+    float *as, *asp, *sig, *diag, *emf;
+    uint8_t* flags;  // bit 0: lower node gauged, bit 1: upper node gauged, bit 2: air stencil
+    float *x, *r, *p, *w, *prev;
+    // cells and faces
+    float *sig_c, *mu_c;
+    float* nu[3];
+    float4* partials;
+    float4* scalars;  // [0] (rz, rr, bb, threshold) [1] (alpha, beta, iterations, status) [2..5] fields [6].x scale
+    float4* results;  // cells x 4: (B,|B|) (J,|J|) (F, heat) (applied B, |applied B|)
+    const uint32_t* materials;
+    const float* props;
+    uint32_t n_props;
+    uint32_t vacuum;
+    uint32_t* err;
+};
+
+__device__ __forceinline__ float fmx(float a, float b) { return a > b ? a : b; }
+__device__ __forceinline__ float fmn(float a, float b) { return a < b ? a : b; }
+
+__device__ __forceinline__ void edge_dims(const EmDev& D, int axis, uint32_t d[3]) {
+    d[0] = D.n[0] + 1;
+    d[1] = D.n[1] + 1;
+    d[2] = D.n[2] + 1;
+    d[axis] -= 1;
+}
+__device__ __forceinline__ bool valid3(const int p[3], const uint32_t d[3]) {
+    return p[0] >= 0 && p[1] >= 0 && p[2] >= 0 && p[0] < (int)d[0] && p[1] < (int)d[1] && p[2] < (int)d[2];
+}
+__device__ __forceinline__ uint32_t edge_offset(const EmDev& D, int axis) {
+    return axis == 0 ? 0u : axis == 1 ? D.e[0] : D.e[0] + D.e[1];
+}
+__device__ __forceinline__ void edge_decode(const EmDev& D, uint32_t i, int p[3], int* axis) {
+    int a = 0;
+    uint32_t q = i;
+    if (q >= D.e[0]) {
+        a = 1;
+        q -= D.e[0];
+        if (q >= D.e[1]) {
+            a = 2;
+            q -= D.e[1];
+        }
+    }
+    uint32_t d[3];
+    edge_dims(D, a, d);
+    p[0] = (int)(q % d[0]);
+    p[1] = (int)((q / d[0]) % d[1]);
+    p[2] = (int)(q / (d[0] * d[1]));
+    *axis = a;
+}
+__device__ __forceinline__ bool on_boundary(const EmDev& D, const int p[3], int axis) {
+    const int a = (axis + 1) % 3, b = (axis + 2) % 3;
+    return p[a] == 0 || (uint32_t)p[a] == D.n[a] || p[b] == 0 || (uint32_t)p[b] == D.n[b];
+}
+
+// kind 0: increment x, 1: search direction p, 2: applied A_s, 4: accepted A,
+// 3: accepted + increment + applied (the total potential).
+template <int KIND>
+__device__ __forceinline__ float a_edge(const EmDev& D, int axis, const int p[3]) {
+    uint32_t d[3];
+    edge_dims(D, axis, d);
+    if (!valid3(p, d)) return 0.0f;
+    const uint32_t i = edge_offset(D, axis) + (uint32_t)p[0] + d[0] * ((uint32_t)p[1] + d[1] * (uint32_t)p[2]);
+    if (KIND == 0) return D.x[i];
+    if (KIND == 1) return D.p[i];
+    if (KIND == 2) return D.as[i];
+    if (KIND == 4) return D.prev[i];
+    return D.prev[i] + D.x[i] + D.as[i];
+}
+__device__ __forceinline__ bool face_valid(const EmDev& D, int axis, const int p[3], uint32_t* idx) {
+    uint32_t d[3] = {D.n[0], D.n[1], D.n[2]};
+    d[axis] += 1;
+    if (!valid3(p, d)) return false;
+    *idx = (uint32_t)p[0] + d[0] * ((uint32_t)p[1] + d[1] * (uint32_t)p[2]);
+    return true;
+}
+template <int KIND>
+__device__ __forceinline__ float curl_face(const EmDev& D, int axis, const int p[3]) {
+    uint32_t fi;
+    if (!face_valid(D, axis, p, &fi)) return 0.0f;
+    const int a = (axis + 1) % 3, b = (axis + 2) % 3;
+    int qa[3] = {p[0], p[1], p[2]}, qb[3] = {p[0], p[1], p[2]};
+    qa[a] += 1;
+    qb[b] += 1;
+    return a_edge<KIND>(D, b, qa) - a_edge<KIND>(D, b, p) - a_edge<KIND>(D, a, qb) + a_edge<KIND>(D, a, p);
+}
+template <int KIND, bool CONTRAST>
+__device__ __forceinline__ float face_term(const EmDev& D, int axis, const int p[3]) {
+    uint32_t fi;
+    if (!face_valid(D, axis, p, &fi)) return 0.0f;
+    float nu = D.nu[axis][fi];
+    if (CONTRAST) nu = 1.0f - nu;
+    return nu * curl_face<KIND>(D, axis, p);
+}
+// Inlined like every helper here: no device function receives the address of
+// the kernel's parameter block.
+template <int KIND, bool CONTRAST>
+__device__ __forceinline__ float adjoint(const EmDev& D, const int p[3], int w) {
+    const int a = (w + 1) % 3, b = (w + 2) % 3;
+    int qa[3] = {p[0], p[1], p[2]}, qb[3] = {p[0], p[1], p[2]};
+    qa[a] -= 1;
+    qb[b] -= 1;
+    return face_term<KIND, CONTRAST>(D, b, p) - face_term<KIND, CONTRAST>(D, b, qa) -
+           face_term<KIND, CONTRAST>(D, a, p) + face_term<KIND, CONTRAST>(D, a, qb);
+}
+template <int KIND>
+__device__ __forceinline__ float node_div(const EmDev& D, const int p[3]) {
+    float value = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        int q[3] = {p[0], p[1], p[2]};
+        q[a] -= 1;
+        value += a_edge<KIND>(D, a, p) - a_edge<KIND>(D, a, q);
+    }
+    return value;
+}
+template <int KIND>
+__device__ __forceinline__ float gauge(const EmDev& D, uint32_t i, const int p[3], int w) {
+    const uint8_t f = D.flags[i];
+    int upper[3] = {p[0], p[1], p[2]};
+    upper[w] += 1;
+    float value = 0.0f;
+    if (f & 1) value += node_div<KIND>(D, p);
+    if (f & 2) value -= node_div<KIND>(D, upper);
+    return value;
+}
+__device__ __forceinline__ float mass(const EmDev& D, uint32_t i) {
+    if (D.initial) return 0.0f;
+    return D.mu0 * D.sig[i] * D.h * D.h / D.dt;
+}
+__device__ __forceinline__ float diagonal(const EmDev& D, uint32_t i) { return fmx(D.diag[i] + mass(D, i), 1e-30f); }
+__device__ __forceinline__ float residual_scale(const EmDev& D) {
+    const float s = D.scalars[6].x;
+    return s > 0.0f ? s : 1.0f;
+}
+__device__ __forceinline__ bool active(const EmDev& D) { return D.scalars[1].w == 0.0f; }
+
+__device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ float4 coef4(float4 a, float4 b) {
+    return make_float4(a.x + b.x, fmn(a.y, b.y), fmx(a.z, b.z), a.w + b.w);
+}
+__device__ __forceinline__ float4 max4(float4 a, float4 b) {
+    return make_float4(fmx(a.x, b.x), fmx(a.y, b.y), fmx(a.z, b.z), fmx(a.w, b.w));
+}
+__device__ __forceinline__ float4 cmix4(float4 a, float4 b) {
+    return make_float4(fmx(a.x, b.x), fmx(a.y, b.y), fmx(a.z, b.z), a.w + b.w);
+}
+
+// 256-lane tree in the shader's pairing (lane l absorbs lane l+s for
+// s = 128, 64, ..., 1); the result is valid in thread 0.
+template <int OP>
+__device__ __forceinline__ float4 tree256(float4 v) {
+    __shared__ float4 red[kBlock];
+    const int l = threadIdx.x;
+    red[l] = v;
+    __syncthreads();
+#pragma unroll
+    for (int s = kBlock / 2; s > 0; s >>= 1) {
+        if (l < s) red[l] = OP == 0 ? add4(red[l], red[l + s]) : coef4(red[l], red[l + s]);
+        __syncthreads();
+    }
+    return red[0];
+}
+// Single-block reduce over n partials: lane l accumulates l, l+256, ... from
+// `init`, then the tree.
+template <int OP>
+__device__ __forceinline__ float4 final_reduce(const float4* partials, uint32_t n, float4 init) {
+    float4 v = init;
+    for (uint32_t i = threadIdx.x; i < n; i += kBlock) v = OP == 0 ? add4(v, partials[i]) : coef4(v, partials[i]);
+    return tree256<OP>(v);
+}
+__device__ __forceinline__ uint32_t groups_of(uint32_t n) { return (n + kBlock - 1) / kBlock; }
+
+// ------------------------------------------------------------ material tables
+__global__ void __launch_bounds__(kBlock) k_em_cells(EmDev D) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= D.cells) return;
+    float sig, mu;
+    if (D.vacuum) {
+        sig = 0.0f;
+        mu = 1.0f;
+    } else {
+        const uint32_t id = D.materials[i];
+        if (id == 0) {
+            sig = D.props[0];
+            mu = D.props[1];
+        } else if (id & 0x80000000u) {
+            const uint32_t m = id & 255u;
+            if (m >= D.n_props) {
+                atomicOr(D.err, 1u);
+                sig = 0.0f;
+                mu = 1.0f;
+            } else {
+                const float alpha = (float)((id >> 8) & 0x7fffffu) / 8388607.0f;
+                sig = alpha * D.props[2 * m];
+                mu = D.props[1] * (1.0f - alpha) + D.props[2 * m + 1] * alpha;
+            }
+        } else if (id >= D.n_props) {
+            atomicOr(D.err, 1u);
+            sig = 0.0f;
+            mu = 1.0f;
+        } else {
+            sig = D.props[2 * id];
+            mu = D.props[2 * id + 1];
+        }
+    }
+    D.sig_c[i] = sig;
+    D.mu_c[i] = mu;
+}
+__device__ __forceinline__ float cell_mu(const EmDev& D, const int p[3]) {
+    const uint32_t d[3] = {D.n[0], D.n[1], D.n[2]};
+    if (!valid3(p, d)) return 1.0f;
+    return D.mu_c[(uint32_t)p[0] + D.n[0] * ((uint32_t)p[1] + D.n[1] * (uint32_t)p[2])];
+}
+__device__ __forceinline__ float cell_sig(const EmDev& D, const int p[3]) {
+    const uint32_t d[3] = {D.n[0], D.n[1], D.n[2]};
+    if (!valid3(p, d)) return 0.0f;
+    return D.sig_c[(uint32_t)p[0] + D.n[0] * ((uint32_t)p[1] + D.n[1] * (uint32_t)p[2])];
+}
+// nu_face (induction.wgsl:32-36): mean of the two cells' reluctivities.
+__global__ void __launch_bounds__(kBlock) k_em_faces(EmDev D, int axis, uint32_t count) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= count) return;
+    uint32_t d[3] = {D.n[0], D.n[1], D.n[2]};
+    d[axis] += 1;
+    int p[3] = {(int)(i % d[0]), (int)((i / d[0]) % d[1]), (int)(i / (d[0] * d[1]))};
+    int q[3] = {p[0], p[1], p[2]};
+    q[axis] -= 1;
+    D.nu[axis][i] = 0.5f / cell_mu(D, p) + 0.5f / cell_mu(D, q);
+}
+__device__ __forceinline__ bool air_node(const EmDev& D, const int p[3]) {
+    for (int k = 0; k < 3; k++)
+        if (p[k] <= 0 || p[k] >= (int)D.n[k]) return false;
+    for (int x = 0; x < 2; x++)
+        for (int y = 0; y < 2; y++)
+            for (int z = 0; z < 2; z++) {
+                const int q[3] = {p[0] - x, p[1] - y, p[2] - z};
+                if (cell_sig(D, q) > 0.0f) return false;
+            }
+    return true;
+}
+__device__ __forceinline__ float nu_at(const EmDev& D, int axis, const int p[3]) {
+    uint32_t fi;
+    return face_valid(D, axis, p, &fi) ? D.nu[axis][fi] : 0.0f;
+}
+// coefficients (induction.wgsl:105-126): edge conductivity, curl diagonal,
+// gauge flags, air-stencil eligibility; partials (conducting boundary edges,
+// min sigma>0, max sigma, conducting edges).
+__global__ void __launch_bounds__(kBlock) k_em_coefficients(EmDev D) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    float4 v = make_float4(0.0f, 1e30f, 0.0f, 0.0f);
+    if (i < D.E) {
+        int p[3], w;
+        edge_decode(D, i, p, &w);
+        const int a = (w + 1) % 3, b = (w + 2) % 3;
+        float sigma = 0.0f;
+        for (int u = 0; u < 2; u++)
+            for (int vv = 0; vv < 2; vv++) {
+                int q[3] = {p[0], p[1], p[2]};
+                q[a] -= u;
+                q[b] -= vv;
+                sigma += 0.25f * cell_sig(D, q);
+            }
+        int qa[3] = {p[0], p[1], p[2]}, qb[3] = {p[0], p[1], p[2]};
+        qa[a] -= 1;
+        qb[b] -= 1;
+        const float nb0 = nu_at(D, b, p), nb1 = nu_at(D, b, qa), na0 = nu_at(D, a, p), na1 = nu_at(D, a, qb);
+        float diag = nb0 + nb1 + na0 + na1;
+        if (on_boundary(D, p, w)) {
+            diag = 1.0f;
+            if (sigma > 0.0f) v.x = 1.0f;
+        }
+        int upper[3] = {p[0], p[1], p[2]};
+        upper[w] += 1;
+        const float lower_air = air_node(D, p) ? 1.0f : 0.0f;
+        const float upper_air = air_node(D, upper) ? 1.0f : 0.0f;
+        const bool scalar_air =
+            lower_air > 0.5f && upper_air > 0.5f && nb0 == 1.0f && nb1 == 1.0f && na0 == 1.0f && na1 == 1.0f;
+        D.flags[i] = (uint8_t)((lower_air > 0.5f ? 1 : 0) | (upper_air > 0.5f ? 2 : 0) | (scalar_air ? 4 : 0));
+        D.emf[i] = 0.0f;
+        D.sig[i] = sigma;
+        D.diag[i] = diag + lower_air + upper_air;
+        v.y = sigma > 0.0f ? sigma : 1e30f;
+        v.z = sigma;
+        v.w = sigma > 0.0f ? 1.0f : 0.0f;
+    }
+    const float4 t = tree256<1>(v);
+    if (threadIdx.x == 0) D.partials[blockIdx.x] = t;
+}
+__global__ void __launch_bounds__(kBlock) k_em_coefficient_check(EmDev D) {
+    const float4 t = final_reduce<1>(D.partials, groups_of(D.E), make_float4(0.0f, 1e30f, 0.0f, 0.0f));
+    if (threadIdx.x == 0) D.scalars[0] = t;
+}
+
+// ------------------------------------------------------------ step passes
+// update_sources: the source pass shifts the history (source.wgsl:16-17),
+// the initial solve has none; an unchanged field holds (hold_source).
+__global__ void __launch_bounds__(kBlock) k_em_sources(EmDev D, const float* applied) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= D.E) return;
+    const float old = D.as[i];
+    if (applied) {
+        const float a = applied[i];
+        D.as[i] = a;
+        D.asp[i] = D.initial ? a : old;
+    } else {
+        D.asp[i] = old;
+    }
+}
+// begin_step (induction.wgsl:248-254)
+__global__ void __launch_bounds__(kBlock) k_em_begin_step(EmDev D) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i == 0) D.scalars[6].x = 1.0f;
+    if (i >= D.E) return;
+    const float accepted = D.x[i];
+    float guess = 0.0f;
+    if (D.pf > 0.0f) {
+        int p[3], w;
+        edge_decode(D, i, p, &w);
+        if (!on_boundary(D, p, w)) guess = D.pf * (accepted - D.prev[i]);
+    }
+    D.prev[i] = accepted;
+    D.x[i] = guess;
+}
+__global__ void __launch_bounds__(kBlock) k_em_zero_guess(EmDev D) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i < D.E) D.x[i] = 0.0f;
+}
+__global__ void __launch_bounds__(kBlock) k_em_commit(EmDev D) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i < D.E) D.x[i] += D.prev[i];
+}
+__global__ void __launch_bounds__(kBlock) k_em_rollback(EmDev D) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= D.E) return;
+    D.x[i] = D.prev[i];
+    D.as[i] = D.asp[i];
+}
+// prepare (induction.wgsl:132-147)
+__global__ void __launch_bounds__(kBlock) k_em_prepare(EmDev D) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (i < D.E) {
+        int p[3], w;
+        edge_decode(D, i, p, &w);
+        const float m = mass(D, i);
+        float b = m * D.dt * D.emf[i] - m * (D.as[i] - D.asp[i]) + adjoint<2, true>(D, p, w) -
+                  adjoint<4, false>(D, p, w) - gauge<4>(D, i, p, w);
+        float r = b;
+        if (D.pf > 0.0f) r -= adjoint<0, false>(D, p, w) + gauge<0>(D, i, p, w) + m * D.x[i];
+        if (on_boundary(D, p, w)) {
+            r = 0.0f;
+            b = 0.0f;
+        }
+        const float physical_l1 = fabsf(b);
+        const float scale = residual_scale(D);
+        b /= scale;
+        r /= scale;
+        const float z = r / diagonal(D, i);
+        D.r[i] = r;
+        D.p[i] = z;
+        D.w[i] = 0.0f;
+        v = make_float4(r * z, r * r, b * b, physical_l1);
+    }
+    const float4 t = tree256<0>(v);
+    if (threadIdx.x == 0) D.partials[blockIdx.x] = t;
+}
+// initial_reduce (induction.wgsl:148-167)
+__global__ void __launch_bounds__(kBlock) k_em_initial_reduce(EmDev D) {
+    const float4 sum = final_reduce<0>(D.partials, groups_of(D.E), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    if (threadIdx.x != 0) return;
+    const float scale = residual_scale(D);
+    float next = scale;
+    if (scale == 1.0f && sum.w > 0.0f && (sum.w < 1e-8f || sum.w > 1e8f)) {
+        int e = (int)((__float_as_uint(sum.w) >> 23) & 255u) - 127;
+        e = e < -100 ? -100 : e > 100 ? 100 : e;
+        next = __uint_as_float((uint32_t)(e + 127) << 23);
+    }
+    float absolute_floor = 1e-38f;
+    if (scale != 1.0f) {
+        const float floor_norm = 1e-19f / scale;
+        absolute_floor = floor_norm * floor_norm;
+    }
+    const float threshold = sum.z * D.tol2 + absolute_floor;
+    D.scalars[6].x = next;
+    D.scalars[0] = make_float4(sum.x, sum.y, sum.z, threshold);
+    D.scalars[1] = make_float4(next != scale ? next : 0.0f, 0.0f, 0.0f, sum.y <= threshold ? 1.0f : 0.0f);
+}
+// apply_operator (induction.wgsl:168-190); AIR = 0 forces the full operator.
+template <bool AIR>
+__global__ void __launch_bounds__(kBlock) k_em_apply(EmDev D) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    float dot = 0.0f;
+    if (i < D.E && active(D)) {
+        float q;
+        if (AIR && (D.flags[i] & 4)) {
+            int axis = 0;
+            if (i >= D.e[0]) {
+                axis = 1;
+                if (i >= D.e[0] + D.e[1]) axis = 2;
+            }
+            uint32_t d[3];
+            edge_dims(D, axis, d);
+            const uint32_t zs = d[0] * d[1];
+            const float c = D.p[i];
+            float result = 0.0f;
+            result += (c - D.p[i - 1]) + (c - D.p[i + 1]);
+            result += (c - D.p[i - d[0]]) + (c - D.p[i + d[0]]);
+            result += (c - D.p[i - zs]) + (c - D.p[i + zs]);
+            q = result;
+        } else {
+            int p[3], w;
+            edge_decode(D, i, p, &w);
+            q = adjoint<1, false>(D, p, w) + gauge<1>(D, i, p, w) + mass(D, i) * D.p[i];
+            if (on_boundary(D, p, w)) q = D.p[i];
+        }
+        D.w[i] = q;
+        dot = D.p[i] * q;
+    }
+    const float4 t = tree256<0>(make_float4(dot, 0.0f, 0.0f, 0.0f));
+    if (threadIdx.x == 0) D.partials[blockIdx.x] = t;
+}
+__global__ void __launch_bounds__(kBlock) k_em_alpha_reduce(EmDev D) {
+    const float4 sum = final_reduce<0>(D.partials, groups_of(D.E), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    if (threadIdx.x == 0 && D.scalars[1].w == 0.0f) {
+        if (sum.x <= 0.0f || fabsf(sum.x) > 3e38f) D.scalars[1].w = 2.0f;
+        else D.scalars[1].x = D.scalars[0].x / sum.x;
+    }
+}
+// update_residual (induction.wgsl:197-208)
+__global__ void __launch_bounds__(kBlock) k_em_update_residual(EmDev D) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (i < D.E && active(D)) {
+        const float alpha = D.scalars[1].x;
+        const float r = D.r[i] - alpha * D.w[i];
+        const float d = diagonal(D, i);
+        D.x[i] = D.x[i] + residual_scale(D) * (alpha * D.p[i]);
+        D.r[i] = r;
+        D.w[i] = d;
+        v = make_float4(r * r / d, r * r, 0.0f, 0.0f);
+    }
+    const float4 t = tree256<0>(v);
+    if (threadIdx.x == 0) D.partials[blockIdx.x] = t;
+}
+__global__ void __launch_bounds__(kBlock) k_em_beta_reduce(EmDev D) {
+    const float4 sum = final_reduce<0>(D.partials, groups_of(D.E), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    if (threadIdx.x == 0 && D.scalars[1].w == 0.0f) {
+        D.scalars[1].y = sum.x / D.scalars[0].x;
+        D.scalars[0].x = sum.x;
+        D.scalars[0].y = sum.y;
+        D.scalars[1].z += 1.0f;
+        if (sum.y <= D.scalars[0].w) D.scalars[1].w = 1.0f;
+        if (fabsf(sum.x) > 3e38f || fabsf(sum.y) > 3e38f) D.scalars[1].w = 2.0f;
+    }
+}
+// update_search, Jacobi branch (induction.wgsl:214)
+__global__ void __launch_bounds__(kBlock) k_em_update_search(EmDev D) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i < D.E && active(D)) {
+        const float z = D.r[i] / D.w[i];
+        D.p[i] = z + D.scalars[1].y * D.p[i];
+    }
+}
+// true_residual (induction.wgsl:230-240)
+__global__ void __launch_bounds__(kBlock) k_em_true_residual(EmDev D) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (i < D.E) {
+        int p[3], w;
+        edge_decode(D, i, p, &w);
+        const float m = mass(D, i);
+        float r = m * D.dt * D.emf[i] - m * (D.x[i] + (D.as[i] - D.asp[i])) + adjoint<2, true>(D, p, w) -
+                  adjoint<4, false>(D, p, w) - gauge<4>(D, i, p, w) - adjoint<0, false>(D, p, w) -
+                  gauge<0>(D, i, p, w);
+        if (on_boundary(D, p, w)) r = 0.0f;
+        r /= residual_scale(D);
+        const float d = diagonal(D, i);
+        D.r[i] = r;
+        D.p[i] = r / d;
+        v = make_float4(r * r / d, r * r, 0.0f, 0.0f);
+    }
+    const float4 t = tree256<0>(v);
+    if (threadIdx.x == 0) D.partials[blockIdx.x] = t;
+}
+__global__ void __launch_bounds__(kBlock) k_em_restart_reduce(EmDev D) {
+    const float4 sum = final_reduce<0>(D.partials, groups_of(D.E), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    if (threadIdx.x == 0) {
+        D.scalars[0].x = sum.x;
+        D.scalars[0].y = sum.y;
+        D.scalars[1].w = sum.y <= D.scalars[0].w ? 1.0f : 0.0f;
+    }
+}
+
+// ------------------------------------------------------------ fields
+__device__ __forceinline__ float electric_edge(const EmDev& D, int axis, const int p[3]) {
+    uint32_t d[3];
+    edge_dims(D, axis, d);
+    if (D.initial || !valid3(p, d)) return 0.0f;
+    const uint32_t i = edge_offset(D, axis) + (uint32_t)p[0] + d[0] * ((uint32_t)p[1] + d[1] * (uint32_t)p[2]);
+    return -(D.x[i] + (D.as[i] - D.asp[i])) / D.dt + D.emf[i];
+}
+__device__ __forceinline__ float current_edge(const EmDev& D, int axis, const int p[3]) {
+    uint32_t d[3];
+    edge_dims(D, axis, d);
+    if (!valid3(p, d)) return 0.0f;
+    const uint32_t i = edge_offset(D, axis) + (uint32_t)p[0] + d[0] * ((uint32_t)p[1] + d[1] * (uint32_t)p[2]);
+    return D.sig[i] * electric_edge(D, axis, p);
+}
+__device__ __forceinline__ float len3(float x, float y, float z) { return sqrtf(x * x + y * y + z * z); }
+
+// fields (induction.wgsl:188-216): per cell B, J, J x B, Joule heat, applied B
+// and the four workgroup reductions (maxima; force and power; div J, max edge
+// J, div B, magnetic energy; applied and reaction maxima).
+__global__ void __launch_bounds__(kBlock) k_em_fields(EmDev D) {
+    __shared__ float4 ra[kBlock], rb[kBlock], rc[kBlock], rd[kBlock];
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    float4 oa = make_float4(0, 0, 0, 0), ob = oa, oc = oa, od = oa;
+    if (i < D.cells) {
+        const uint32_t nx = D.n[0], ny = D.n[1];
+        const int p[3] = {(int)(i % nx), (int)((i / nx) % ny), (int)(i / (nx * ny))};
+        const float sig = D.sig_c[i], mu = D.mu_c[i];
+        const float h = D.h;
+        float mag[3] = {0, 0, 0}, app[3] = {0, 0, 0}, j[3] = {0, 0, 0};
+        float heat = 0.0f, div_b = 0.0f, div_j = 0.0f, max_edge = 0.0f, msq = 0.0f;
+#pragma unroll
+        for (int axis = 0; axis < 3; axis++) {
+            int upper[3] = {p[0], p[1], p[2]};
+            upper[axis] += 1;
+            const float b0 = curl_face<3>(D, axis, p) / h, b1 = curl_face<3>(D, axis, upper) / h;
+            msq += 0.5f * (b0 * b0 + b1 * b1);
+            mag[axis] = 0.5f * (b0 + b1);
+            app[axis] = 0.5f * (curl_face<2>(D, axis, p) + curl_face<2>(D, axis, upper)) / h;
+            div_b += b1 - b0;
+            const int aa = (axis + 1) % 3, bb = (axis + 2) % 3;
+            float es = 0.0f;
+            for (int u = 0; u < 2; u++)
+                for (int v = 0; v < 2; v++) {
+                    int q[3] = {p[0], p[1], p[2]};
+                    q[aa] += u;
+                    q[bb] += v;
+                    const float ee = electric_edge(D, axis, q);
+                    es += 0.25f * ee;
+                    heat += sig * 0.25f * ee * ee;
+                }
+            j[axis] = sig * es;
+            int prev[3] = {p[0], p[1], p[2]};
+            prev[axis] -= 1;
+            const float jp = current_edge(D, axis, p), jm = current_edge(D, axis, prev);
+            div_j += jp - jm;
+            max_edge = fmx(max_edge, fmx(fabsf(jp), fabsf(jm)));
+        }
+        const float f0 = j[1] * mag[2] - j[2] * mag[1], f1 = j[2] * mag[0] - j[0] * mag[2],
+                    f2 = j[0] * mag[1] - j[1] * mag[0];
+        const float bn = len3(mag[0], mag[1], mag[2]), jn = len3(j[0], j[1], j[2]), fn = len3(f0, f1, f2);
+        const float vol = h * h * h;
+        const float an = len3(app[0], app[1], app[2]);
+        float4* out = D.results + 4 * (size_t)i;
+        out[0] = make_float4(mag[0], mag[1], mag[2], bn);
+        out[1] = make_float4(j[0], j[1], j[2], jn);
+        out[2] = make_float4(f0, f1, f2, heat);
+        out[3] = make_float4(app[0], app[1], app[2], an);
+        oa = make_float4(bn, jn, fn, heat);
+        ob = make_float4(f0 * vol, f1 * vol, f2 * vol, heat * vol);
+        oc = make_float4(fabsf(div_j), max_edge, fabsf(div_b), msq * vol / (2.0f * D.mu0 * mu));
+        od = make_float4(an, len3(mag[0] - app[0], mag[1] - app[1], mag[2] - app[2]), 0.0f, 0.0f);
+    }
+    const int l = threadIdx.x;
+    ra[l] = oa;
+    rb[l] = ob;
+    rc[l] = oc;
+    rd[l] = od;
+    __syncthreads();
+    for (int s = kBlock / 2; s > 0; s >>= 1) {
+        if (l < s) {
+            ra[l] = max4(ra[l], ra[l + s]);
+            rb[l] = add4(rb[l], rb[l + s]);
+            rc[l] = cmix4(rc[l], rc[l + s]);
+            rd[l] = max4(rd[l], rd[l + s]);
+        }
+        __syncthreads();
+    }
+    if (l == 0) {
+        float4* P = D.partials + 4 * (size_t)blockIdx.x;
+        P[0] = ra[0];
+        P[1] = rb[0];
+        P[2] = rc[0];
+        P[3] = rd[0];
+    }
+}
+__global__ void __launch_bounds__(kBlock) k_em_field_reduce(EmDev D) {
+    __shared__ float4 ra[kBlock], rb[kBlock], rc[kBlock], rd[kBlock];
+    const uint32_t n = groups_of(D.cells);
+    float4 a = make_float4(0, 0, 0, 0), b = a, c = a, d = a;
+    for (uint32_t i = threadIdx.x; i < n; i += kBlock) {
+        const float4* P = D.partials + 4 * (size_t)i;
+        const float4 v = P[2];
+        a = max4(a, P[0]);
+        b = add4(b, P[1]);
+        c = make_float4(fmx(c.x, v.x), fmx(c.y, v.y), fmx(c.z, v.z), c.w + v.w);
+        d = max4(d, P[3]);
+    }
+    const int l = threadIdx.x;
+    ra[l] = a;
+    rb[l] = b;
+    rc[l] = c;
+    rd[l] = d;
+    __syncthreads();
+    for (int s = kBlock / 2; s > 0; s >>= 1) {
+        if (l < s) {
+            ra[l] = max4(ra[l], ra[l + s]);
+            rb[l] = add4(rb[l], rb[l + s]);
+            rc[l] = cmix4(rc[l], rc[l + s]);
+            rd[l] = max4(rd[l], rd[l + s]);
+        }
+        __syncthreads();
+    }
+    if (l == 0) {
+        D.scalars[2] = ra[0];
+        D.scalars[3] = rb[0];
+        D.scalars[4] = rc[0];
+        D.scalars[5] = rd[0];
+    }
+}
+
+// Interleaves the planar work vectors into the reference's vec4 record
+// (x, r, p, w) for inspection.
+__global__ void k_em_pack_work(EmDev D, float4* out) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i < D.E) out[i] = make_float4(D.x[i], D.r[i], D.p[i], D.w[i]);
+}
+
+__global__ void k_em_pack_coefficients(EmDev D, float4* out) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i < D.E) out[i] = make_float4(D.sig[i], D.diag[i], (float)D.flags[i], D.emf[i]);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host
+struct mhdproj_em_ctx {
+    EmDev D{};
+    mhdproj_em_config cfg{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaEvent_t ev = nullptr, t0 = nullptr, t1 = nullptr;
+    std::vector<void*> allocs;
+    float4* h_sc = nullptr;  // pinned copy of the scalars
+    uint32_t* h_err = nullptr;
+    float4* checkpoint = nullptr;
+    float* d_props = nullptr;
+    uint32_t props_cap = 0;
+    cudaGraphExec_t batch = nullptr;  // kBatch CG iterations
+    uint32_t batch_initial = 0;       // the step constants the batch graph was captured with
+    float batch_dt = 0.0f;
+    bool materials = false;
+    double time_s = 0.0, last_dt = 0.0;
+    bool can_predict = false;
+    float range[2] = {0.0f, 0.0f};
+    uint64_t launches = 0;
+    std::string err;
+};
+
+static std::string g_em_create_error;
+
+static int em_fail(mhdproj_em_ctx* c, int code, const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    else g_em_create_error = buf;
+    return code;
+}
+#define EK(call)                                                                                    \
+    do {                                                                                            \
+        cudaError_t _e = (call);                                                                    \
+        if (_e != cudaSuccess)                                                                      \
+            return em_fail(ctx, _e == cudaErrorMemoryAllocation ? MHDPROJ_ERR_OUT_OF_MEMORY : MHDPROJ_ERR_CUDA, \
+                           "%s: %s", #call, cudaGetErrorString(_e));                                \
+    } while (0)
+
+template <class T>
+static cudaError_t em_alloc(mhdproj_em_ctx* ctx, T** p, size_t bytes) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes ? bytes : 16);
+    if (e != cudaSuccess) return e;
+    ctx->allocs.push_back(q);
+    *p = (T*)q;
+    return cudaMemsetAsync(q, 0, bytes ? bytes : 16, ctx->stream);
+}
+
+static int em_wait(mhdproj_em_ctx* ctx, double timeout_s = 600.0) {
+    EK(cudaEventRecord(ctx->ev, ctx->stream));
+    auto t0 = std::chrono::steady_clock::now();
+    int spins = 0;
+    for (;;) {
+        cudaError_t e = cudaEventQuery(ctx->ev);
+        if (e == cudaSuccess) return 0;
+        if (e != cudaErrorNotReady) return em_fail(ctx, MHDPROJ_ERR_CUDA, "stream wait: %s", cudaGetErrorString(e));
+        if (++spins > 2000) std::this_thread::sleep_for(std::chrono::microseconds(50));
+        else std::this_thread::yield();
+        double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (el > timeout_s)
+            return em_fail(ctx, MHDPROJ_ERR_TIMEOUT, "device work did not finish within %.0f s", timeout_s);
+    }
+}
+
+static unsigned em_groups(uint32_t n) { return (n + kBlock - 1) / kBlock; }
+
+#define EM_LAUNCH(kernel, n, ...)                                                  \
+    do {                                                                           \
+        kernel<<<em_groups(n) ? em_groups(n) : 1, kBlock, 0, ctx->stream>>>(__VA_ARGS__); \
+        ctx->launches++;                                                           \
+    } while (0)
+#define EM_SINGLE(kernel, ...)                                   \
+    do {                                                         \
+        kernel<<<1, kBlock, 0, ctx->stream>>>(__VA_ARGS__);      \
+        ctx->launches++;                                         \
+    } while (0)
+
+static int em_read_status(mhdproj_em_ctx* ctx) {
+    EK(cudaMemcpyAsync(ctx->h_sc, ctx->D.scalars, 8 * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    return em_wait(ctx);
+}
+static bool status_finite(const float4* sc) {
+    const float* v = &sc[0].x;
+    for (int k = 0; k < 8; k++)
+        if (!std::isfinite(v[k])) return false;
+    return true;
+}
+static void em_iteration(mhdproj_em_ctx* ctx) {
+    const EmDev& D = ctx->D;
+    EM_LAUNCH(k_em_apply<true>, D.E, D);
+    EM_SINGLE(k_em_alpha_reduce, D);
+    EM_LAUNCH(k_em_update_residual, D.E, D);
+    EM_SINGLE(k_em_beta_reduce, D);
+    EM_LAUNCH(k_em_update_search, D.E, D);
+}
+// The iteration kernels take EmDev by value, so the graph holds the step
+// constants they read (initial, dt); it is captured again when they change.
+static int em_build_batch(mhdproj_em_ctx* ctx) {
+    if (ctx->batch && ctx->batch_initial == ctx->D.initial && ctx->batch_dt == ctx->D.dt) return 0;
+    if (ctx->batch) {
+        cudaGraphExecDestroy(ctx->batch);
+        ctx->batch = nullptr;
+    }
+    if (!ctx->stream) return 0;  // the legacy default stream cannot be captured: launch directly
+    cudaGraph_t g = nullptr;
+    EK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const uint64_t before = ctx->launches;
+    for (uint32_t k = 0; k < kBatch; k++) em_iteration(ctx);
+    ctx->launches = before;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (e != cudaSuccess) return em_fail(ctx, MHDPROJ_ERR_CUDA, "batch capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&ctx->batch, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return em_fail(ctx, MHDPROJ_ERR_CUDA, "batch instantiate: %s", cudaGetErrorString(e));
+    ctx->batch_initial = ctx->D.initial;
+    ctx->batch_dt = ctx->D.dt;
+    return 0;
+}
+static void em_prepare(mhdproj_em_ctx* ctx) {
+    EM_LAUNCH(k_em_prepare, ctx->D.E, ctx->D);
+    EM_SINGLE(k_em_initial_reduce, ctx->D);
+}
+static void em_restart(mhdproj_em_ctx* ctx) {
+    EM_LAUNCH(k_em_true_residual, ctx->D.E, ctx->D);
+    EM_SINGLE(k_em_restart_reduce, ctx->D);
+}
+
+extern "C" {
+
+const char* mhdproj_em_last_error(const mhdproj_em_ctx* ctx) {
+    return ctx ? ctx->err.c_str() : g_em_create_error.c_str();
+}
+
+void mhdproj_em_destroy(mhdproj_em_ctx* ctx) {
+    if (!ctx) return;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->batch) cudaGraphExecDestroy(ctx->batch);
+    for (void* p : ctx->allocs) cudaFree(p);
+    if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
+    if (ctx->h_err) cudaFreeHost(ctx->h_err);
+    if (ctx->ev) cudaEventDestroy(ctx->ev);
+    if (ctx->t0) cudaEventDestroy(ctx->t0);
+    if (ctx->t1) cudaEventDestroy(ctx->t1);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int mhdproj_em_create(const mhdproj_em_config* cfg, mhdproj_em_ctx** out) {
+    mhdproj_em_ctx* ctx = nullptr;
+    if (!cfg || !out) return em_fail(nullptr, MHDPROJ_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (cfg->nx == 0 || cfg->ny == 0 || cfg->nz == 0)
+        return em_fail(nullptr, MHDPROJ_ERR_INVALID, "EM grid dimensions must be positive");
+    if (!(cfg->cell_m > 0.0f) || !std::isfinite(cfg->cell_m))
+        return em_fail(nullptr, MHDPROJ_ERR_INVALID, "EM cell size must be positive and finite");
+    if (!(cfg->dt_s > 0.0) || !std::isfinite(cfg->dt_s))
+        return em_fail(nullptr, MHDPROJ_ERR_INVALID, "EM time step must be positive and finite");
+    if (!(cfg->relative_tolerance > 0.0f) || cfg->max_iterations == 0)
+        return em_fail(nullptr, MHDPROJ_ERR_INVALID, "EM tolerance and iteration cap must be positive");
+    if (cfg->mode != MHDPROJ_EM_INDUCTION && cfg->mode != MHDPROJ_EM_APPLIED)
+        return em_fail(nullptr, MHDPROJ_ERR_INVALID, "unknown EM mode %d", cfg->mode);
+    const uint64_t x = cfg->nx, y = cfg->ny, z = cfg->nz;
+    const uint64_t counts[3] = {x * (y + 1) * (z + 1), (x + 1) * y * (z + 1), (x + 1) * (y + 1) * z};
+    const uint64_t total = counts[0] + counts[1] + counts[2];
+    if (total > 0xFFFFFFFFull || x * y * z > 0xFFFFFFFFull)  // grid.rs:25-27
+        return em_fail(nullptr, MHDPROJ_ERR_INVALID, "EM grid indexing exceeds u32");
+    ctx = new mhdproj_em_ctx();
+    ctx->cfg = *cfg;
+    EmDev& D = ctx->D;
+    D.n[0] = cfg->nx;
+    D.n[1] = cfg->ny;
+    D.n[2] = cfg->nz;
+    D.cells = (uint32_t)(x * y * z);
+    for (int k = 0; k < 3; k++) D.e[k] = (uint32_t)counts[k];
+    D.E = (uint32_t)total;
+    D.initial = 1;
+    D.pf = 0.0f;
+    D.dt = 1e-5f;  // grid.rs:34; advance sets the configured step
+    D.mu0 = 4e-7f * 3.14159265358979323846f;
+    D.h = cfg->cell_m;
+    D.tol2 = 1e-10f;
+    D.vacuum = cfg->mode == MHDPROJ_EM_APPLIED ? 1u : 0u;
+    auto bail = [&](int code) {
+        mhdproj_em_destroy(ctx);
+        return code;
+    };
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        em_fail(nullptr, MHDPROJ_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
+        delete ctx;
+        return MHDPROJ_ERR_CUDA;
+    }
+    ctx->own_stream = true;
+    const size_t E = D.E, C = D.cells;
+    const size_t groups = std::max(em_groups(D.E), em_groups(D.cells));
+    cudaError_t es[32];
+    int ne = 0;
+    es[ne++] = cudaEventCreateWithFlags(&ctx->ev, cudaEventDisableTiming);
+    es[ne++] = cudaEventCreate(&ctx->t0);
+    es[ne++] = cudaEventCreate(&ctx->t1);
+    es[ne++] = em_alloc(ctx, &D.as, E * 4);
+    es[ne++] = em_alloc(ctx, &D.asp, E * 4);
+    es[ne++] = em_alloc(ctx, &D.sig, E * 4);
+    es[ne++] = em_alloc(ctx, &D.diag, E * 4);
+    es[ne++] = em_alloc(ctx, &D.emf, E * 4);
+    es[ne++] = em_alloc(ctx, &D.flags, E);
+    es[ne++] = em_alloc(ctx, &D.x, E * 4);
+    es[ne++] = em_alloc(ctx, &D.r, E * 4);
+    es[ne++] = em_alloc(ctx, &D.p, E * 4);
+    es[ne++] = em_alloc(ctx, &D.w, E * 4);
+    es[ne++] = em_alloc(ctx, &D.prev, E * 4);
+    es[ne++] = em_alloc(ctx, &D.sig_c, C * 4);
+    es[ne++] = em_alloc(ctx, &D.mu_c, C * 4);
+    for (int a = 0; a < 3; a++) {
+        uint64_t f = (x + (a == 0)) * (y + (a == 1)) * (z + (a == 2));
+        es[ne++] = em_alloc(ctx, &D.nu[a], f * 4);
+    }
+    es[ne++] = em_alloc(ctx, &D.partials, (4 * groups + 4) * sizeof(float4));
+    es[ne++] = em_alloc(ctx, &D.scalars, 8 * sizeof(float4));
+    es[ne++] = em_alloc(ctx, &D.results, 4 * C * sizeof(float4));
+    es[ne++] = em_alloc(ctx, &ctx->checkpoint, 4 * C * sizeof(float4));
+    es[ne++] = em_alloc(ctx, &D.err, 16);
+    es[ne++] = cudaMallocHost(&ctx->h_sc, 8 * sizeof(float4));
+    es[ne++] = cudaMallocHost(&ctx->h_err, 16);
+    for (int k = 0; k < ne; k++)
+        if (es[k] != cudaSuccess) {
+            em_fail(nullptr, es[k] == cudaErrorMemoryAllocation ? MHDPROJ_ERR_OUT_OF_MEMORY : MHDPROJ_ERR_CUDA,
+                    "EM workspace (%.0f MiB): %s", (double)(E * 45 + C * 136) / 1048576.0,
+                    cudaGetErrorString(es[k]));
+            return bail(es[k] == cudaErrorMemoryAllocation ? MHDPROJ_ERR_OUT_OF_MEMORY : MHDPROJ_ERR_CUDA);
+        }
+    e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+        em_fail(nullptr, MHDPROJ_ERR_CUDA, "EM workspace: %s", cudaGetErrorString(e));
+        return bail(MHDPROJ_ERR_CUDA);
+    }
+    *out = ctx;
+    return 0;
+}
+
+int mhdproj_em_set_stream(mhdproj_em_ctx* ctx, void* stream) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    EK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    ctx->own_stream = false;
+    ctx->stream = (cudaStream_t)stream;
+    return 0;
+}
+
+int mhdproj_em_sizes(const mhdproj_em_ctx* ctx, uint64_t out[8]) {
+    if (!ctx || !out) return MHDPROJ_ERR_INVALID;
+    const EmDev& D = ctx->D;
+    out[0] = D.n[0];
+    out[1] = D.n[1];
+    out[2] = D.n[2];
+    out[3] = D.cells;
+    out[4] = D.e[0];
+    out[5] = D.e[1];
+    out[6] = D.e[2];
+    out[7] = D.E;
+    return 0;
+}
+
+int mhdproj_em_set_materials(mhdproj_em_ctx* ctx, const uint32_t* materials, const float* properties,
+                             uint32_t count, float conductivity_range[2]) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (!materials || !properties || count == 0)
+        return em_fail(ctx, MHDPROJ_ERR_INVALID, "materials and at least one property row are required");
+    for (uint32_t k = 0; k < 2 * count; k++)
+        if (!std::isfinite(properties[k]))
+            return em_fail(ctx, MHDPROJ_ERR_INVALID, "material properties must be finite");
+    EmDev& D = ctx->D;
+    if (count > ctx->props_cap) {
+        float* p = nullptr;
+        EK(em_alloc(ctx, &p, (size_t)count * 8));
+        ctx->d_props = p;
+        ctx->props_cap = count;
+    }
+    EK(cudaMemcpyAsync(ctx->d_props, properties, (size_t)count * 8, cudaMemcpyHostToDevice, ctx->stream));
+    D.materials = materials;
+    D.props = ctx->d_props;
+    D.n_props = count;
+    EK(cudaMemsetAsync(D.err, 0, 4, ctx->stream));
+    EM_LAUNCH(k_em_cells, D.cells, D);
+    for (int a = 0; a < 3; a++) {
+        const uint32_t f = (D.n[0] + (a == 0)) * (D.n[1] + (a == 1)) * (D.n[2] + (a == 2));
+        EM_LAUNCH(k_em_faces, f, D, a, f);
+    }
+    EM_LAUNCH(k_em_coefficients, D.E, D);
+    EM_SINGLE(k_em_coefficient_check, D);
+    EK(cudaGetLastError());
+    EK(cudaMemcpyAsync(ctx->h_sc, D.scalars, sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    EK(cudaMemcpyAsync(ctx->h_err, D.err, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    int rc = em_wait(ctx);
+    if (rc) return rc;
+    D.materials = nullptr;
+    const float4 check = ctx->h_sc[0];
+    ctx->range[0] = check.w > 0.0f ? check.y : 0.0f;
+    ctx->range[1] = check.z;
+    if (conductivity_range) {
+        conductivity_range[0] = ctx->range[0];
+        conductivity_range[1] = ctx->range[1];
+    }
+    if (*ctx->h_err) return em_fail(ctx, MHDPROJ_ERR_INVALID, "a material id has no property row");
+    ctx->materials = true;
+    if (check.x > 0.0f)  // mod.rs:563-567 and :748-752
+        return em_fail(ctx, MHDPROJ_ERR_INVALID,
+                       "A conductor touches the EM outer boundary; add air padding to the domain");
+    return 0;
+}
+
+int mhdproj_em_set_motional_emf(mhdproj_em_ctx* ctx, const float* emf) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (emf) EK(cudaMemcpyAsync(ctx->D.emf, emf, (size_t)ctx->D.E * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    else EK(cudaMemsetAsync(ctx->D.emf, 0, (size_t)ctx->D.E * 4, ctx->stream));
+    return em_wait(ctx);
+}
+
+int mhdproj_em_set_reaction(mhdproj_em_ctx* ctx, const float* a) {
+    if (!ctx || !a) return MHDPROJ_ERR_INVALID;
+    EK(cudaMemcpyAsync(ctx->D.x, a, (size_t)ctx->D.E * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    return em_wait(ctx);
+}
+
+int mhdproj_em_copy(mhdproj_em_ctx* ctx, int which, float* out) {
+    if (!ctx || !out) return MHDPROJ_ERR_INVALID;
+    const EmDev& D = ctx->D;
+    const size_t E = D.E, C = D.cells;
+    switch (which) {
+        case MHDPROJ_EM_REACTION:
+            EK(cudaMemcpyAsync(out, D.x, E * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+            break;
+        case MHDPROJ_EM_PREVIOUS:
+            EK(cudaMemcpyAsync(out, D.prev, E * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+            break;
+        case MHDPROJ_EM_APPLIED_POTENTIAL:
+            EK(cudaMemcpyAsync(out, D.as, E * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+            break;
+        case MHDPROJ_EM_CELLS:
+            EK(cudaMemcpyAsync(out, D.results, C * 64, cudaMemcpyDeviceToDevice, ctx->stream));
+            break;
+        case MHDPROJ_EM_WORK:
+            EM_LAUNCH(k_em_pack_work, D.E, D, (float4*)out);
+            break;
+        case MHDPROJ_EM_EDGE_COEFFICIENTS:
+            EM_LAUNCH(k_em_pack_coefficients, D.E, D, (float4*)out);
+            break;
+        default:
+            return em_fail(ctx, MHDPROJ_ERR_INVALID, "unknown EM array %d", which);
+    }
+    EK(cudaGetLastError());
+    return em_wait(ctx);
+}
+
+int mhdproj_em_apply_operator(mhdproj_em_ctx* ctx, const float* p, float* q, int air_stencil) {
+    if (!ctx || !p || !q) return MHDPROJ_ERR_INVALID;
+    if (!ctx->materials) return em_fail(ctx, MHDPROJ_ERR_STATE, "set the EM materials first");
+    EmDev& D = ctx->D;
+    EK(cudaMemcpyAsync(D.p, p, (size_t)D.E * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    EK(cudaMemsetAsync(D.scalars, 0, 8 * sizeof(float4), ctx->stream));
+    if (air_stencil) EM_LAUNCH(k_em_apply<true>, D.E, D);
+    else EM_LAUNCH(k_em_apply<false>, D.E, D);
+    EK(cudaGetLastError());
+    EK(cudaMemcpyAsync(q, D.w, (size_t)D.E * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    return em_wait(ctx);
+}
+
+// EmState::advance_to (src/em/mod.rs:863-1090) without the source summation:
+// `applied` is A_s at time_s (device, one float per edge) or NULL when the
+// applied field is unchanged.
+int mhdproj_em_advance(mhdproj_em_ctx* ctx, double time_s, int initial, const float* applied,
+                       mhdproj_em_diagnostics* diag) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (!ctx->materials) return em_fail(ctx, MHDPROJ_ERR_STATE, "set the EM materials first");
+    if (!std::isfinite(time_s)) return em_fail(ctx, MHDPROJ_ERR_INVALID, "EM time must be finite");
+    if (ctx->cfg.mode == MHDPROJ_EM_APPLIED && (!initial || time_s < 0.0))  // mod.rs:841-858
+        return em_fail(ctx, MHDPROJ_ERR_INVALID, "Applied field time must be nonnegative and mode Applied");
+    const auto started = std::chrono::steady_clock::now();
+    EmDev& D = ctx->D;
+    D.initial = initial ? 1u : 0u;
+    float pf = 0.0f;
+    if (!initial && ctx->can_predict && ctx->last_dt > 0.0) {
+        const float ratio = (float)((time_s - ctx->time_s) / ctx->last_dt);
+        pf = (std::isfinite(ratio) && ratio > 0.0f) ? ratio : 0.0f;
+    }
+    D.pf = pf;
+    D.dt = (float)ctx->cfg.dt_s;
+    D.tol2 = ctx->cfg.relative_tolerance * ctx->cfg.relative_tolerance;
+    const bool allow_nodal = !initial && ctx->cfg.mode == MHDPROJ_EM_INDUCTION && ctx->cfg.max_iterations > kNodalSwitch;
+    EK(cudaEventRecord(ctx->t0, ctx->stream));
+    EM_LAUNCH(k_em_sources, D.E, D, applied);
+    EM_LAUNCH(k_em_begin_step, D.E, D);
+    em_prepare(ctx);
+    EK(cudaGetLastError());
+    int rc = em_read_status(ctx);
+    if (rc) return rc;
+    if (ctx->h_sc[1].x != 0.0f) {  // initial_reduce chose a power-of-two normalisation
+        em_prepare(ctx);
+        if ((rc = em_read_status(ctx))) return rc;
+    }
+    if (pf > 0.0f && (!status_finite(ctx->h_sc) || ctx->h_sc[0].y > ctx->h_sc[0].z)) {
+        D.pf = 0.0f;
+        EM_LAUNCH(k_em_zero_guess, D.E, D);
+        em_prepare(ctx);
+        if ((rc = em_read_status(ctx))) return rc;
+    }
+    rc = em_build_batch(ctx);
+    if (rc) return rc;
+    auto its = [&]() { return (uint32_t)ctx->h_sc[1].z; };
+    const uint32_t cap = ctx->cfg.max_iterations;
+    for (;;) {
+        while (ctx->h_sc[1].w == 0.0f && status_finite(ctx->h_sc) && its() < cap) {
+            const uint32_t batch = std::min(cap - its(), kBatch);
+            if (batch == kBatch && ctx->batch) {
+                EK(cudaGraphLaunch(ctx->batch, ctx->stream));
+                ctx->launches += 5 * kBatch;
+            } else {
+                for (uint32_t k = 0; k < batch; k++) em_iteration(ctx);
+            }
+            EK(cudaGetLastError());
+            if ((rc = em_read_status(ctx))) return rc;
+            if (allow_nodal && ctx->h_sc[1].w == 0.0f && status_finite(ctx->h_sc) && its() >= kNodalSwitch &&
+                its() < cap) {
+                EM_LAUNCH(k_em_rollback, D.E, D);
+                ctx->can_predict = false;
+                if ((rc = em_wait(ctx))) return rc;
+                return em_fail(ctx, MHDPROJ_ERR_UNSUPPORTED,
+                               "EM solve reached %u Jacobi iterations; the nodal preconditioner the reference "
+                               "switches to here is not built (state restored)",
+                               its());
+            }
+        }
+        if (ctx->h_sc[1].w != 1.0f) break;
+        em_restart(ctx);
+        if ((rc = em_read_status(ctx))) return rc;
+        if (ctx->h_sc[1].w == 1.0f || its() >= cap) break;
+    }
+    if (ctx->h_sc[1].w != 1.0f && status_finite(ctx->h_sc)) {
+        em_restart(ctx);
+        if ((rc = em_read_status(ctx))) return rc;
+    }
+    float status[8];
+    memcpy(status, ctx->h_sc, sizeof status);
+    if (diag) {
+        memset(diag, 0, sizeof *diag);
+        memcpy(diag->status, status, sizeof status);
+        diag->iterations = (uint32_t)status[6];
+        diag->relative_residual = std::sqrt(status[1] / std::max(status[2], 1e-38f));
+        diag->conductivity_range[0] = ctx->range[0];
+        diag->conductivity_range[1] = ctx->range[1];
+    }
+    if (status[7] != 1.0f || !status_finite(ctx->h_sc)) {
+        EM_LAUNCH(k_em_rollback, D.E, D);
+        ctx->can_predict = false;
+        rc = em_wait(ctx);
+        if (rc) return rc;
+        return em_fail(ctx, MHDPROJ_ERR_NOT_CONVERGED,
+                       "EM solve did not converge: %u iterations, true relative residual %.3e (requested %.3e); "
+                       "conducting-edge sigma range %.3e..%.3e S/m; state restored",
+                       (uint32_t)status[6], std::sqrt(status[1] / std::max(status[2], 1e-38f)),
+                       ctx->cfg.relative_tolerance, ctx->range[0], ctx->range[1]);
+    }
+    EK(cudaMemcpyAsync(ctx->checkpoint, D.results, (size_t)D.cells * 64, cudaMemcpyDeviceToDevice, ctx->stream));
+    EM_LAUNCH(k_em_fields, D.cells, D);
+    EM_SINGLE(k_em_field_reduce, D);
+    EM_LAUNCH(k_em_commit, D.E, D);
+    EK(cudaEventRecord(ctx->t1, ctx->stream));
+    EK(cudaGetLastError());
+    if ((rc = em_read_status(ctx))) return rc;
+    const float* stats = &ctx->h_sc[2].x;
+    bool finite = true;
+    for (int k = 0; k < 16; k++) finite = finite && std::isfinite(stats[k]);
+    if (!finite) {
+        EM_LAUNCH(k_em_rollback, D.E, D);
+        EK(cudaMemcpyAsync(D.results, ctx->checkpoint, (size_t)D.cells * 64, cudaMemcpyDeviceToDevice,
+                           ctx->stream));
+        ctx->can_predict = false;
+        rc = em_wait(ctx);
+        if (rc) return rc;
+        return em_fail(ctx, MHDPROJ_ERR_NONFINITE, "Nonfinite EM field output; state restored");
+    }
+    ctx->last_dt = initial ? 0.0 : time_s - ctx->time_s;
+    ctx->can_predict = !initial && status[2] > 0.0f;
+    ctx->time_s = time_s;
+    if (diag) {
+        memcpy(diag->maxima, stats, 16);
+        memcpy(diag->force_n, stats + 4, 12);
+        diag->power_w = stats[7];
+        diag->divergence_j_scaled = stats[8];
+        diag->max_edge_j = stats[9];
+        diag->divergence_b_scaled = stats[10];
+        diag->magnetic_energy_j = stats[11];
+        diag->applied_max_t = stats[12];
+        diag->reaction_max_t = stats[13];
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ctx->t0, ctx->t1);
+        diag->device_ms = ms;
+        diag->elapsed_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - started).count();
+    }
+    return 0;
+}
+
+int mhdproj_em_kernel_launches(const mhdproj_em_ctx* ctx, uint64_t* count) {
+    if (!ctx || !count) return MHDPROJ_ERR_INVALID;
+    *count = ctx->launches;
+    return 0;
+}
+
+}  // extern "C"

@@ -36,6 +36,7 @@ STATUS = {
     6: "call order",
     7: "out of memory",
     8: "timeout",
+    9: "unsupported",
 }
 
 
@@ -77,6 +78,26 @@ class StepParams(C.Structure):
     _fields_ = [("dt", C.c_float), ("acceleration", C.c_float * 3), ("kinematic_viscosity", C.c_float),
                 ("advection", C.c_int32), ("surface_tension", C.c_float), ("air_viscosity", C.c_float),
                 ("max_viscous_substeps", C.c_uint32), ("curvature", C.c_void_p)]
+
+
+class EmConfig(C.Structure):
+    _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("nz", C.c_uint32), ("cell_m", C.c_float),
+                ("origin_m", C.c_float * 3), ("dt_s", C.c_double), ("relative_tolerance", C.c_float),
+                ("max_iterations", C.c_uint32), ("mode", C.c_int32)]
+
+
+class EmDiagnostics(C.Structure):
+    _fields_ = [("maxima", C.c_float * 4), ("force_n", C.c_float * 3), ("power_w", C.c_float),
+                ("divergence_j_scaled", C.c_float), ("max_edge_j", C.c_float), ("divergence_b_scaled", C.c_float),
+                ("magnetic_energy_j", C.c_float), ("applied_max_t", C.c_float), ("reaction_max_t", C.c_float),
+                ("iterations", C.c_uint32), ("relative_residual", C.c_float), ("conductivity_range", C.c_float * 2),
+                ("device_ms", C.c_float), ("elapsed_ms", C.c_double), ("status", C.c_float * 8)]
+
+    def stats(self):
+        """The 16 field statistics in the reference's scalars[2..5] order."""
+        return np.array(list(self.maxima) + list(self.force_n) + [self.power_w, self.divergence_j_scaled,
+                        self.max_edge_j, self.divergence_b_scaled, self.magnetic_energy_j, self.applied_max_t,
+                        self.reaction_max_t, 0.0, 0.0], np.float32)
 
 
 class KernelTime(C.Structure):
@@ -136,6 +157,19 @@ def load():
                                                          C.POINTER(Diagnostics)]
     L.mhdproj_export_fields.argtypes = [C.POINTER(Grid), _vp, C.c_char_p, C.c_uint64, C.c_double,
                                         C.POINTER(C.c_float * 3), C.c_int, C.c_char_p]
+    L.mhdproj_em_create.argtypes = [C.POINTER(EmConfig), C.POINTER(_vp)]
+    L.mhdproj_em_destroy.argtypes = [_vp]
+    L.mhdproj_em_last_error.argtypes = [_vp]
+    L.mhdproj_em_last_error.restype = C.c_char_p
+    L.mhdproj_em_set_stream.argtypes = [_vp, _vp]
+    L.mhdproj_em_sizes.argtypes = [_vp, C.POINTER(C.c_uint64 * 8)]
+    L.mhdproj_em_set_materials.argtypes = [_vp, _vp, _vp, C.c_uint32, C.POINTER(C.c_float * 2)]
+    L.mhdproj_em_set_motional_emf.argtypes = [_vp, _vp]
+    L.mhdproj_em_set_reaction.argtypes = [_vp, _vp]
+    L.mhdproj_em_advance.argtypes = [_vp, C.c_double, C.c_int, _vp, C.POINTER(EmDiagnostics)]
+    L.mhdproj_em_copy.argtypes = [_vp, C.c_int, _vp]
+    L.mhdproj_em_apply_operator.argtypes = [_vp, _vp, _vp, C.c_int]
+    L.mhdproj_em_kernel_launches.argtypes = [_vp, C.POINTER(C.c_uint64)]
     _lib = L
     return L
 
@@ -147,6 +181,9 @@ EXPORTED = [
     "mhdproj_apply_preconditioner", "mhdproj_copy_coefficients", "mhdproj_copy_potential", "mhdproj_copy_topology",
     "mhdproj_hierarchy", "mhdproj_anchors", "mhdproj_profile_kernels", "mhdproj_divergence_noalloc",
     "mhdproj_kernel_launches", "mhdproj_fields", "mhdproj_fluid_step", "mhdproj_export_fields",
+    "mhdproj_em_create", "mhdproj_em_destroy", "mhdproj_em_last_error", "mhdproj_em_set_stream", "mhdproj_em_sizes",
+    "mhdproj_em_set_materials", "mhdproj_em_set_motional_emf", "mhdproj_em_set_reaction", "mhdproj_em_advance",
+    "mhdproj_em_copy", "mhdproj_em_apply_operator", "mhdproj_em_kernel_launches",
 ]
 
 
@@ -453,3 +490,126 @@ def autograd_projection():
             return None, None, a, b, c
 
     return ProjectFn
+
+
+EM_MODES = {"induction": 0, "applied": 1}
+EM_ARRAYS = {"reaction": 0, "previous": 1, "applied": 2, "cells": 3, "work": 4, "coefficients": 5}
+
+
+class EmInduction:
+    """The EM induction state (mhdproj_em_ctx), mirroring EmState
+    (src/em/mod.rs): :meth:`set_materials` is the coefficient build of
+    ``EmState::new`` / ``update_material_geometry``, :meth:`advance` is
+    ``advance_to`` with the applied potential A_s supplied by the caller,
+    :meth:`step` is ``EmState::step`` (one ``dt_s`` further).
+
+    Edge arrays are flat float32 CUDA tensors of ``edges`` entries (x-edges,
+    y-edges, z-edges, each x-fastest); cell results are ``(cells, 16)``.
+    """
+
+    def __init__(self, dims, cell_m, dt_s=1e-5, relative_tolerance=1e-5, max_iterations=1000,
+                 origin_m=(0.0, 0.0, 0.0), mode="induction", stream=None):
+        import torch
+
+        self._torch = torch
+        L = load()
+        cfg = EmConfig(int(dims[0]), int(dims[1]), int(dims[2]), float(cell_m), (C.c_float * 3)(*origin_m),
+                       float(dt_s), float(relative_tolerance), int(max_iterations), EM_MODES[mode])
+        h_ = C.c_void_p()
+        rc = L.mhdproj_em_create(C.byref(cfg), C.byref(h_))
+        if rc:
+            raise ProjectionError(rc, L.mhdproj_em_last_error(None).decode())
+        self._ctx = h_
+        self._lib = L
+        self.config = cfg
+        self.dt_s = float(dt_s)
+        self.time_s = 0.0
+        if stream is None or stream.cuda_stream == 0:
+            stream = torch.cuda.Stream()
+        self.stream = stream
+        self._check(L.mhdproj_em_set_stream(self._ctx, C.c_void_p(stream.cuda_stream)))
+        sz = (C.c_uint64 * 8)()
+        self._check(L.mhdproj_em_sizes(self._ctx, C.byref(sz)))
+        self.dims = tuple(int(v) for v in sz[:3])
+        self.cells = int(sz[3])
+        self.edge_counts = tuple(int(v) for v in sz[4:7])
+        self.edges = int(sz[7])
+
+    def _order(self):
+        cur = self._torch.cuda.current_stream()
+        if cur.cuda_stream != self.stream.cuda_stream:
+            self.stream.wait_stream(cur)
+
+    def _check(self, rc):
+        if rc:
+            raise ProjectionError(rc, self._lib.mhdproj_em_last_error(self._ctx).decode())
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._lib.mhdproj_em_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_materials(self, materials, properties):
+        """materials: uint32-valued CUDA tensor (cells), int32 accepted;
+        properties: rows of (conductivity S/m, relative permeability) per id.
+        Returns the conducting-edge conductivity range."""
+        self._order()
+        m = materials.contiguous()
+        pr = np.ascontiguousarray(properties, np.float32).reshape(-1, 2)
+        rng = (C.c_float * 2)()
+        self._check(self._lib.mhdproj_em_set_materials(self._ctx, _ptr(m), _host_ptr(pr), pr.shape[0],
+                                                       C.byref(rng)))
+        self._materials = m
+        return float(rng[0]), float(rng[1])
+
+    def set_motional_emf(self, emf=None):
+        self._order()
+        self._check(self._lib.mhdproj_em_set_motional_emf(self._ctx, _ptr(emf)))
+
+    def set_reaction(self, a):
+        self._order()
+        self._check(self._lib.mhdproj_em_set_reaction(self._ctx, _ptr(a.contiguous())))
+
+    def advance(self, time_s, initial=False, applied=None):
+        """One step to ``time_s``; returns :class:`EmDiagnostics`."""
+        self._order()
+        d = EmDiagnostics()
+        a = None if applied is None else applied.contiguous()
+        self._check(self._lib.mhdproj_em_advance(self._ctx, float(time_s), int(bool(initial)), _ptr(a),
+                                                 C.byref(d)))
+        self.time_s = float(time_s)
+        return d
+
+    def step(self, applied=None):
+        return self.advance(self.time_s + self.dt_s, False, applied)
+
+    def copy(self, which):
+        torch = self._torch
+        k = EM_ARRAYS[which]
+        n = self.cells * 16 if k == 3 else self.edges * 4 if k in (4, 5) else self.edges
+        out = torch.empty(n, dtype=torch.float32, device="cuda")
+        self._order()
+        self._check(self._lib.mhdproj_em_copy(self._ctx, k, _ptr(out)))
+        if k == 3:
+            return out.view(self.cells, 16)
+        if k in (4, 5):
+            return out.view(self.edges, 4)
+        return out
+
+    def apply_operator(self, p, air_stencil=True):
+        q = self._torch.empty_like(p)
+        self._order()
+        self._check(self._lib.mhdproj_em_apply_operator(self._ctx, _ptr(p.contiguous()), _ptr(q),
+                                                        int(bool(air_stencil))))
+        return q
+
+    def kernel_launches(self):
+        n = C.c_uint64()
+        self._check(self._lib.mhdproj_em_kernel_launches(self._ctx, C.byref(n)))
+        return int(n.value)

@@ -22,10 +22,10 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler"
            "-I" + INCLUDE]
 # Units whose FP32 arithmetic must follow the reference's operation order
 # exactly: no fused multiply-adds.
-EXACT = {"reference_kernels.cu", "step_kernels.cu"}
+EXACT = {"reference_kernels.cu", "step_kernels.cu", "em_solver.cu"}
 
 SOURCES = ["context.cu", "gb300_kernels.cu", "fine_kernels.cu", "fused_kernels.cu", "mg_kernels.cu", "reference_kernels.cu", "noalloc.cu",
-           "topology_kernels.cu", "step_kernels.cu", "export_fields.cu"]
+           "topology_kernels.cu", "step_kernels.cu", "export_fields.cu", "em_solver.cu"]
 HOST_SOURCES = ["topology.cpp"]
 
 

@@ -209,6 +209,38 @@ int onat_chain_adjoint(const onat_grid *g, const float *alpha, const uint8_t *so
                        const double *uk, const double *vk, const double *wk, float dt, int steps,
                        double rtol, double *gfu, double *gfv, double *gfw);
 
+/* ---- oem_*: the implicit EM induction solve (oracle_em.c) ----
+ * FP32 restatement of the reference's edge-element A-formulation step:
+ * src/em/induction.wgsl (coefficients, Jacobi-preconditioned CG with
+ * power-of-two residual scaling, true-residual restarts, fields) driven by
+ * EmState::advance_to (src/em/mod.rs:863-1090).  Edges are numbered x-edges,
+ * y-edges, z-edges, each block x-fastest (src/em/common.wgsl:3-6). */
+typedef struct OEm OEm;
+enum { OEM_OK = 0, OEM_NOT_CONVERGED = 1, OEM_NONFINITE = 2, OEM_NODAL_REQUIRED = 3 };
+/* vacuum != 0 is the applied-field mode (every cell reads as air). */
+OEm *oem_new(const uint32_t dims[3], float h, const float origin[3], double dt_s, float rel_tol, uint32_t max_it,
+             int vacuum);
+void oem_free(OEm *s);
+/* out: dims[4] (nx, ny, nz, cells), edges[4] (x, y, z, total). */
+void oem_sizes(const OEm *s, uint32_t out[8]);
+/* Material ids per cell (bit 31: partial cell, fraction in bits 8..30,
+ * material in bits 0..7) and (sigma S/m, relative permeability) per id.
+ * check = (conducting boundary edges, min sigma>0, max sigma, conducting
+ * edges).  Returns -1 when an id has no property row. */
+int oem_set_materials(OEm *s, const uint32_t *materials, const float *props, uint32_t n_props, float check[4]);
+/* Motional EMF per edge (NULL: zero), as set_velocity leaves it. */
+void oem_set_motional(OEm *s, const float *emf);
+/* Overwrite the accepted reaction potential (edges). */
+void oem_set_reaction(OEm *s, const float *a);
+/* which: 0 work (E x 4), 1 previous (E), 2 source (2E x 4), 3 cell results
+ * (cells x 16: B,|B|, J,|J|, F,heat, applied B,|applied B|), 4 scalars (32). */
+void oem_get(const OEm *s, int which, float *out);
+/* q = A p with (use_air = 1) or without the air stencil fast path. */
+void oem_apply_operator(OEm *s, const float *p, float *q, int use_air);
+/* One step to time_s; applied = A_s at that time (NULL: unchanged).
+ * Returns OEM_*; status_out = scalars[0..1], stats_out = scalars[2..5]. */
+int oem_advance(OEm *s, double time_s, int initial, const float *applied, float status_out[8], float stats_out[16]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -73,7 +73,7 @@ def _stale() -> bool:
     t = os.path.getmtime(LIB_PATH)
     return any(
         os.path.getmtime(os.path.join(HERE, f)) > t
-        for f in ("oracle_ref.c", "oracle_native.c", "mhd_oracle.h")
+        for f in ("oracle_ref.c", "oracle_native.c", "oracle_em.c", "mhd_oracle.h")
     )
 
 
@@ -147,6 +147,19 @@ def lib():
                                          C.c_int, C.c_double, _f64p, _f64p, _f64p, C.POINTER(C.c_double)]
         L.onat_chain_adjoint.argtypes = [g, _f32p, _u8p, _f64p, _f64p, _f64p, C.c_float, C.c_int, C.c_double,
                                          _f64p, _f64p, _f64p]
+        L.oem_new.argtypes = [C.POINTER(C.c_uint32), C.c_float, C.POINTER(C.c_float), C.c_double, C.c_float,
+                              C.c_uint32, C.c_int]
+        L.oem_new.restype = C.c_void_p
+        L.oem_free.argtypes = [C.c_void_p]
+        L.oem_sizes.argtypes = [C.c_void_p, _u32p]
+        L.oem_set_materials.argtypes = [C.c_void_p, _u32p, _f32p, C.c_uint32, _f32p]
+        L.oem_set_materials.restype = C.c_int
+        L.oem_set_motional.argtypes = [C.c_void_p, C.c_void_p]
+        L.oem_set_reaction.argtypes = [C.c_void_p, _f32p]
+        L.oem_get.argtypes = [C.c_void_p, C.c_int, _f32p]
+        L.oem_apply_operator.argtypes = [C.c_void_p, _f32p, _f32p, C.c_int]
+        L.oem_advance.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_void_p, _f32p, _f32p]
+        L.oem_advance.restype = C.c_int
         _lib = L
     return _lib
 
@@ -376,3 +389,97 @@ def chain_adjoint(g, alpha, solid, uk, vk, wk, dt, steps, rtol=1e-13):
     st = lib().onat_chain_adjoint(C.byref(g), f(alpha), np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1),
                                   d(uk), d(vk), d(wk), dt, steps, rtol, gu, gv, gw)
     return st, (gu, gv, gw)
+
+
+class EmSolve:
+    """The EM induction step restated in FP32 (oracle_em.c): one instance per
+    grid, mirroring EmState (src/em/mod.rs) without its source summation."""
+
+    OK, NOT_CONVERGED, NONFINITE, NODAL_REQUIRED = 0, 1, 2, 3
+
+    def __init__(self, dims, h, dt=1e-5, rel_tol=1e-5, max_iterations=1000, origin=(0.0, 0.0, 0.0), vacuum=False):
+        L = lib()
+        d = (C.c_uint32 * 3)(*dims)
+        o = (C.c_float * 3)(*origin)
+        self._p = L.oem_new(d, float(h), o, float(dt), float(rel_tol), int(max_iterations), int(bool(vacuum)))
+        if not self._p:
+            raise MemoryError("oem_new")
+        sz = np.zeros(8, np.uint32)
+        L.oem_sizes(self._p, sz)
+        self.dims = tuple(int(v) for v in sz[:3])
+        self.cells = int(sz[3])
+        self.edge_counts = tuple(int(v) for v in sz[4:7])
+        self.edges = int(sz[7])
+
+    def close(self):
+        if self._p:
+            lib().oem_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        self.close()
+
+    def set_materials(self, materials, properties):
+        m = np.ascontiguousarray(materials, np.uint32).reshape(-1)
+        pr = np.ascontiguousarray(properties, np.float32).reshape(-1, 2)
+        check = np.zeros(4, np.float32)
+        rc = lib().oem_set_materials(self._p, m, pr.reshape(-1), pr.shape[0], check)
+        if rc != 0:
+            raise ValueError("material id without a property row")
+        return check
+
+    def set_motional(self, emf=None):
+        e = None if emf is None else np.ascontiguousarray(emf, np.float32)
+        lib().oem_set_motional(self._p, None if e is None else e.ctypes.data)
+        self._keep = e
+
+    def set_reaction(self, a):
+        lib().oem_set_reaction(self._p, np.ascontiguousarray(a, np.float32))
+
+    def work(self):
+        out = np.zeros((self.edges, 4), np.float32)
+        lib().oem_get(self._p, 0, out)
+        return out
+
+    def reaction(self):
+        return self.work()[:, 0].copy()
+
+    def previous(self):
+        out = np.zeros(self.edges, np.float32)
+        lib().oem_get(self._p, 1, out)
+        return out
+
+    def source(self):
+        out = np.zeros((2 * self.edges, 4), np.float32)
+        lib().oem_get(self._p, 2, out)
+        return out
+
+    def results(self):
+        out = np.zeros((self.cells, 16), np.float32)
+        lib().oem_get(self._p, 3, out)
+        return out
+
+    def scalars(self):
+        out = np.zeros(32, np.float32)
+        lib().oem_get(self._p, 4, out)
+        return out
+
+    def apply_operator(self, p, use_air=True):
+        q = np.zeros(self.edges, np.float32)
+        lib().oem_apply_operator(self._p, np.ascontiguousarray(p, np.float32), q, int(bool(use_air)))
+        return q
+
+    def advance(self, time_s, initial=False, applied=None):
+        """Returns (code, status[8], stats[16])."""
+        a = None if applied is None else np.ascontiguousarray(applied, np.float32)
+        st = np.zeros(8, np.float32)
+        stats = np.zeros(16, np.float32)
+        rc = lib().oem_advance(self._p, float(time_s), int(bool(initial)), None if a is None else a.ctypes.data,
+                               st, stats)
+        return rc, st, stats
+
+
+def em_edge_dims(dims, axis):
+    d = [v + 1 for v in dims]
+    d[axis] -= 1
+    return tuple(d)

@@ -83,3 +83,13 @@ def test_create_without_gpu_fails_loudly(lib):
         pytest.skip("a GPU is present")
     with pytest.raises(Exception):
         mhdproj.PressureProjection((8, 8, 8), 1e-3)
+
+
+def test_em_create_without_gpu_fails_loudly(lib):
+    import torch
+    import mhdproj
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(Exception):
+        mhdproj.EmInduction((8, 8, 8), 1e-3)
