@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--step", action="store_true",
                     help="only the fluid-step leg: a few mhdproj_fluid_step calls on the workload's geometry as one "
                          "liquid, then its kernels launched once each (a small launch list for profilers)")
+    ap.add_argument("--em", action="store_true",
+                    help="only the EM induction leg (driven ring, 128^3 and 64^3)")
     ap.add_argument("--kernels", action="store_true",
                     help="one projection, then each fine-level kernel of a CG iteration launched once in "
                          "isolation (a small, fixed launch list for profilers); prints the kernel times")
@@ -324,7 +326,73 @@ def run_ours(args):
                 "iterations": st_p[-1].iterations, "true_relative_residual": st_p[-1].true_relative_residual,
                 "device_memory_gb": used / 1e9}
 
+    def em_leg(n, steps, warm=2):
+        """EmState::step on the driven-ring workload (synth.em_ring): the
+        bit-exact Jacobi-CG induction solve, fields and commit per step, timed
+        on the EM context's stream.  Algorithmic bytes per CG iteration: the
+        operator reads p, the edge flags and conductivity and writes A p
+        (13 B/edge) plus the face reluctivities (about 4 B/edge); the residual
+        update reads r, A p, x, p, the diagonal and conductivity and writes x,
+        r and the diagonal (36 B/edge); the search update reads r, the
+        diagonal and p and writes p (16 B/edge): 69 B per edge."""
+        c = synth.em_ring(n)
+        em = mhdproj.EmInduction(c["dims"], c["h"], dt_s=c["dt"], origin_m=c["origin"])
+        em.set_materials(torch.from_numpy(c["materials"].view(np.int32)).to(dev), c["properties"])
+        dt_e = c["dt"]
+        fields_ = [torch.from_numpy(c["applied"](k * dt_e)).to(dev) for k in range(warm + steps + 1)]
+        em.advance(0.0, initial=True, applied=fields_[0])
+        for k in range(1, warm + 1):
+            em.advance(k * dt_e, applied=fields_[k])
+        counter = [warm]
+
+        def em_step(e):
+            counter[0] += 1
+            return e.advance(counter[0] * dt_e, applied=fields_[counter[0]])
+
+        l0 = em.kernel_launches()
+        ms_e, ds = timed(em, steps, em_step)
+        launches = em.kernel_launches() - l0
+        its = sum(d.iterations for d in ds)
+        em.close()
+        per_it_ms = ms_e / max(its, 1)
+        bytes_it = 69 * (3 * n * (n + 1) ** 2)
+        peak_e, _ = hbm_peak()
+        return {"workload": f"em_ring: {n}^3 cells, {3 * n * (n + 1) ** 2} edges, driven conducting annulus",
+                "steps_per_s": 1000.0 * steps / ms_e, "ms_per_step": ms_e / steps, "iterations_per_step": its / steps,
+                "ms_per_iteration": per_it_ms, "iteration_bytes": bytes_it,
+                "GBps_per_iteration": bytes_it / (per_it_ms * 1e-3) / 1e9,
+                "hbm_fraction_per_iteration": bytes_it / (per_it_ms * 1e-3) / 1e9 / peak_e,
+                "relative_residual": ds[-1].relative_residual, "max_J": ds[-1].maxima[1],
+                "kernel_launches_per_step": launches / steps}
+
+    def em_cpu_leg(n, warm=1):
+        """The oracle's FP32 restatement of the same EM step on the host cores
+        (OpenMP over edge groups), one timed step after `warm` steps."""
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as _o
+
+        c = synth.em_ring(n)
+        s = _o.EmSolve(c["dims"], c["h"], dt=c["dt"], origin=c["origin"])
+        s.set_materials(c["materials"], c["properties"])
+        s.advance(0.0, initial=True, applied=c["applied"](0.0))
+        for k in range(1, warm + 1):
+            s.advance(k * c["dt"], applied=c["applied"](k * c["dt"]))
+        a = c["applied"]((warm + 1) * c["dt"])
+        t0 = time.perf_counter()
+        rc, st, _ = s.advance((warm + 1) * c["dt"], applied=a)
+        sec = time.perf_counter() - t0
+        s.close()
+        return {"steps_per_s": 1.0 / sec, "seconds_per_step": sec, "iterations": int(st[6]), "ok": rc == 0,
+                "cores": os.cpu_count() or 1, "kind": "port",
+                "sample": f"oracle/oracle_em.c on em_ring {n}^3, step {warm + 1} of the driven sequence"}
+
     pr = make(args.precision)
+    if args.em:
+        out_e = {"em_step128": em_leg(128, 5), "em_step64": em_leg(64, 5)}
+        if rank == 0:
+            print(json.dumps(out_e))
+        pr.close()
+        return
     if args.step:
         out_s = fluid_step_leg(2, 1)
         out_t = fluid_step_leg(2, 1, two_phase=True)
@@ -493,6 +561,16 @@ def run_ours(args):
                 line[key] = fluid_step_leg(5, 10, two_phase=tp)
             except mhdproj.ProjectionError as exc:
                 line[key] = {"unavailable": str(exc)}
+        # the EM induction step (src/em): 128^3 on the GPU, and 64^3 on the GPU
+        # beside the oracle's CPU restatement of the same step
+        try:
+            line["em_step"] = em_leg(128, 5)
+            e64 = em_leg(64, 5)
+            if rank == 0 and world == 1:
+                e64["cpu_baseline"] = em_cpu_leg(64)
+            line["em_step64"] = e64
+        except mhdproj.ProjectionError as exc:
+            line["em_step"] = {"unavailable": str(exc)}
         # CPU baseline: bounded sample of the reference algorithm on the host cores
         threads = os.cpu_count() or 1
         k_ref = reference_iterations(args.workload, args.tol)

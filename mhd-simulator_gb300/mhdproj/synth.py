@@ -22,6 +22,15 @@ Workloads (grid sizes at scale 1):
   column512    512x256x256, h=0.025 mm, liquid column of radius 20 cells along
                x plus 4 seeded drops of radius 8..14 cells, no solids.
 A ``scale`` argument shrinks a workload geometrically for oracle-sized tests.
+
+EM workload (:func:`em_ring`): an n^3 box of 1 mm cells (origin at the box
+centre) holding a conducting annulus about the z axis (radii 0.19 n and
+0.38 n cells, the middle third of the height; conductivity 40 x 316
+stainless, 5.33e7 S/m, relative permeability 1) in air, driven by a uniform
+applied field B_z = 0.02 T sin(2 pi 1 kHz t) whose potential A_s = B x r / 2
+is evaluated at the edge midpoints, dt = 1e-5 s -- the induction-heating
+setting of the reference's EM tests (a conductor in a 16 mm box driven by a
+uniform source) scaled to n.
 """
 from __future__ import annotations
 
@@ -188,3 +197,46 @@ def make_case(name: str, seed: int = 1, scale: float = 1.0) -> dict:
         return dict(name=name, dims=(nx, ny, nz), h=h, rho_liquid=6440.0, rho_air=1.2, alpha=alpha, solid=solid,
                     u=u, v=v, w=wv, dt=1e-5, periodic=0, outlet=True, tol=1e-6)
     raise ValueError(f"unknown workload {name!r}")
+
+
+SIGMA_316 = np.float32(1.0 / 0.75e-6)  # S/m, 316 stainless
+
+
+def em_edge_dims(dims, axis):
+    d = [int(v) + 1 for v in dims]
+    d[axis] -= 1
+    return tuple(d)
+
+
+def em_uniform_potential(dims, h, origin, b, scale=1.0):
+    """A_s = scale/2 * B x r at every edge midpoint, edges ordered x-, y-, then
+    z-edges, each block x-fastest (float32, one value per edge)."""
+    blocks = []
+    for axis in range(3):
+        d = em_edge_dims(dims, axis)
+        z, y, x = np.meshgrid(np.arange(d[2]), np.arange(d[1]), np.arange(d[0]), indexing="ij")
+        pos = [x.astype(np.float32), y.astype(np.float32), z.astype(np.float32)]
+        pos[axis] = pos[axis] + np.float32(0.5)
+        r = [np.float32(origin[k]) + pos[k] * np.float32(h) for k in range(3)]
+        bb = [np.float32(v) for v in b]
+        cr = [bb[1] * r[2] - bb[2] * r[1], bb[2] * r[0] - bb[0] * r[2], bb[0] * r[1] - bb[1] * r[0]]
+        blocks.append((np.float32(0.5 * scale) * cr[axis]).reshape(-1))
+    return np.concatenate(blocks).astype(np.float32)
+
+
+def em_ring(n: int) -> dict:
+    """The driven-ring EM workload on an n^3 grid (see the module docstring)."""
+    h = 1e-3
+    origin = (-0.5 * n * h,) * 3
+    m = np.zeros((n, n, n), np.uint32)
+    c = (n - 1) / 2.0
+    y, x = np.mgrid[0:n, 0:n]
+    r = np.hypot(x - c, y - c)
+    ring = (r >= 0.19 * n) & (r <= 0.38 * n)
+    m[n // 3:n - n // 3][:, ring] = 1
+    props = np.array([[0.0, 1.0], [SIGMA_316 * 40, 1.0]], np.float32)
+    b = (0.0, 0.0, 0.02)
+    base = em_uniform_potential((n, n, n), h, origin, b)
+    applied = lambda t: (base * np.float32(np.sin(2 * np.pi * 1e3 * t))).astype(np.float32)
+    return dict(dims=(n, n, n), h=h, origin=origin, materials=m.reshape(-1), properties=props, dt=1e-5,
+                applied=applied)
