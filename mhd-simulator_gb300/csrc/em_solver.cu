@@ -196,6 +196,126 @@ __device__ __forceinline__ float residual_scale(const EmDev& D) {
 }
 __device__ __forceinline__ bool active(const EmDev& D) { return D.scalars[1].w == 0.0f; }
 
+// ---- the same operator with the edge axis fixed at compile time ----
+// adjoint_s/gauge_s repeat adjoint()/gauge() term for term and in the same
+// order; with the axis a template parameter every neighbour offset is a
+// constant, positions stay in registers (the runtime-axis form keeps small
+// position arrays in local memory) and each array is read directly.
+template <int K>
+__device__ __forceinline__ void bump(int& x, int& y, int& z, int s) {
+    if (K == 0) x += s;
+    else if (K == 1) y += s;
+    else z += s;
+}
+template <int K>
+__device__ __forceinline__ int coord(int x, int y, int z) { return K == 0 ? x : K == 1 ? y : z; }
+template <int AX>
+__device__ __forceinline__ float edge_at(const EmDev& D, const float* __restrict__ v, int x, int y, int z) {
+    const int dx = (int)D.n[0] + (AX != 0), dy = (int)D.n[1] + (AX != 1), dz = (int)D.n[2] + (AX != 2);
+    if (x < 0 || y < 0 || z < 0 || x >= dx || y >= dy || z >= dz) return 0.0f;
+    const uint32_t off = AX == 0 ? 0u : AX == 1 ? D.e[0] : D.e[0] + D.e[1];
+    return v[off + (uint32_t)x + (uint32_t)dx * ((uint32_t)y + (uint32_t)dy * (uint32_t)z)];
+}
+template <int F>
+__device__ __forceinline__ bool face_at(const EmDev& D, int x, int y, int z, uint32_t* idx) {
+    const int fx = (int)D.n[0] + (F == 0), fy = (int)D.n[1] + (F == 1), fz = (int)D.n[2] + (F == 2);
+    if (x < 0 || y < 0 || z < 0 || x >= fx || y >= fy || z >= fz) return false;
+    *idx = (uint32_t)x + (uint32_t)fx * ((uint32_t)y + (uint32_t)fy * (uint32_t)z);
+    return true;
+}
+template <int F, bool CONTRAST>
+__device__ __forceinline__ float face_s(const EmDev& D, const float* __restrict__ v, int x, int y, int z) {
+    uint32_t fi;
+    if (!face_at<F>(D, x, y, z, &fi)) return 0.0f;
+    constexpr int A = (F + 1) % 3, B = (F + 2) % 3;
+    float nu = D.nu[F][fi];
+    if (CONTRAST) nu = 1.0f - nu;
+    int ax = x, ay = y, az = z, bx = x, by = y, bz = z;
+    bump<A>(ax, ay, az, 1);
+    bump<B>(bx, by, bz, 1);
+    const float curl = edge_at<B>(D, v, ax, ay, az) - edge_at<B>(D, v, x, y, z) - edge_at<A>(D, v, bx, by, bz) +
+                       edge_at<A>(D, v, x, y, z);
+    return nu * curl;
+}
+template <int W, bool CONTRAST>
+__device__ __forceinline__ float adjoint_s(const EmDev& D, const float* __restrict__ v, int x, int y, int z) {
+    constexpr int A = (W + 1) % 3, B = (W + 2) % 3;
+    int ax = x, ay = y, az = z, bx = x, by = y, bz = z;
+    bump<A>(ax, ay, az, -1);
+    bump<B>(bx, by, bz, -1);
+    return face_s<B, CONTRAST>(D, v, x, y, z) - face_s<B, CONTRAST>(D, v, ax, ay, az) -
+           face_s<A, CONTRAST>(D, v, x, y, z) + face_s<A, CONTRAST>(D, v, bx, by, bz);
+}
+__device__ __forceinline__ float node_div_s(const EmDev& D, const float* __restrict__ v, int x, int y, int z) {
+    float value = 0.0f;
+    value += edge_at<0>(D, v, x, y, z) - edge_at<0>(D, v, x - 1, y, z);
+    value += edge_at<1>(D, v, x, y, z) - edge_at<1>(D, v, x, y - 1, z);
+    value += edge_at<2>(D, v, x, y, z) - edge_at<2>(D, v, x, y, z - 1);
+    return value;
+}
+template <int W>
+__device__ __forceinline__ float gauge_s(const EmDev& D, const float* __restrict__ v, uint8_t f, int x, int y, int z) {
+    float value = 0.0f;
+    if (f & 1) value += node_div_s(D, v, x, y, z);
+    if (f & 2) {
+        int ux = x, uy = y, uz = z;
+        bump<W>(ux, uy, uz, 1);
+        value -= node_div_s(D, v, ux, uy, uz);
+    }
+    return value;
+}
+template <int W>
+__device__ __forceinline__ void decode_s(const EmDev& D, uint32_t q, int& x, int& y, int& z) {
+    const uint32_t dx = D.n[0] + (W != 0), dy = D.n[1] + (W != 1);
+    x = (int)(q % dx);
+    y = (int)((q / dx) % dy);
+    z = (int)(q / (dx * dy));
+}
+template <int W>
+__device__ __forceinline__ bool boundary_s(const EmDev& D, int x, int y, int z) {
+    constexpr int A = (W + 1) % 3, B = (W + 2) % 3;
+    const int pa = coord<A>(x, y, z), pb = coord<B>(x, y, z);
+    return pa == 0 || pa == (int)D.n[A] || pb == 0 || pb == (int)D.n[B];
+}
+// One edge of each pass with its axis W and its index q inside the axis
+// block (k_em_prepare, k_em_apply, k_em_true_residual dispatch on the axis).
+template <int W>
+__device__ __forceinline__ float2 prepare_edge(const EmDev& D, uint32_t i, uint32_t q) {
+    int x, y, z;
+    decode_s<W>(D, q, x, y, z);
+    if (boundary_s<W>(D, x, y, z)) return make_float2(0.0f, 0.0f);
+    const float m = mass(D, i);
+    const uint8_t f = D.flags[i];
+    const float b = m * D.dt * D.emf[i] - m * (D.as[i] - D.asp[i]) + adjoint_s<W, true>(D, D.as, x, y, z) -
+                    adjoint_s<W, false>(D, D.prev, x, y, z) - gauge_s<W>(D, D.prev, f, x, y, z);
+    float r = b;
+    if (D.pf > 0.0f) r -= adjoint_s<W, false>(D, D.x, x, y, z) + gauge_s<W>(D, D.x, f, x, y, z) + m * D.x[i];
+    return make_float2(b, r);
+}
+template <int W>
+__device__ __forceinline__ float apply_edge(const EmDev& D, uint32_t i, uint32_t q) {
+    int x, y, z;
+    decode_s<W>(D, q, x, y, z);
+    const float pv = D.p[i];
+    if (boundary_s<W>(D, x, y, z)) return pv;
+    return adjoint_s<W, false>(D, D.p, x, y, z) + gauge_s<W>(D, D.p, D.flags[i], x, y, z) + mass(D, i) * pv;
+}
+template <int W>
+__device__ __forceinline__ float true_residual_edge(const EmDev& D, uint32_t i, uint32_t q) {
+    int x, y, z;
+    decode_s<W>(D, q, x, y, z);
+    if (boundary_s<W>(D, x, y, z)) return 0.0f;
+    const float m = mass(D, i);
+    const uint8_t f = D.flags[i];
+    return m * D.dt * D.emf[i] - m * (D.x[i] + (D.as[i] - D.asp[i])) + adjoint_s<W, true>(D, D.as, x, y, z) -
+           adjoint_s<W, false>(D, D.prev, x, y, z) - gauge_s<W>(D, D.prev, f, x, y, z) -
+           adjoint_s<W, false>(D, D.x, x, y, z) - gauge_s<W>(D, D.x, f, x, y, z);
+}
+#define EM_BY_AXIS(FN, D, i)                                                         \
+    ((i) < (D).e[0]             ? FN<0>((D), (i), (i))                              \
+     : (i) < (D).e[0] + (D).e[1] ? FN<1>((D), (i), (i) - (D).e[0])                  \
+                                 : FN<2>((D), (i), (i) - (D).e[0] - (D).e[1]))
+
 __device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 __device__ __forceinline__ float4 coef4(float4 a, float4 b) {
     return make_float4(a.x + b.x, fmn(a.y, b.y), fmx(a.z, b.z), a.w + b.w);
@@ -208,7 +328,8 @@ __device__ __forceinline__ float4 cmix4(float4 a, float4 b) {
 }
 
 // 256-lane tree in the shader's pairing (lane l absorbs lane l+s for
-// s = 128, 64, ..., 1); the result is valid in thread 0.
+// s = 128, 64, ..., 1); the last five levels are warp shuffles with the same
+// pairing.  The result is valid in thread 0.
 template <int OP>
 __device__ __forceinline__ float4 tree256(float4 v) {
     __shared__ float4 red[kBlock];
@@ -216,18 +337,39 @@ __device__ __forceinline__ float4 tree256(float4 v) {
     red[l] = v;
     __syncthreads();
 #pragma unroll
-    for (int s = kBlock / 2; s > 0; s >>= 1) {
+    for (int s = kBlock / 2; s >= 32; s >>= 1) {
         if (l < s) red[l] = OP == 0 ? add4(red[l], red[l + s]) : coef4(red[l], red[l + s]);
         __syncthreads();
     }
-    return red[0];
+    float4 w = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (l < 32) {
+        w = red[l];
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) {
+            float4 o;
+            o.x = __shfl_down_sync(0xffffffffu, w.x, s);
+            o.y = __shfl_down_sync(0xffffffffu, w.y, s);
+            o.z = __shfl_down_sync(0xffffffffu, w.z, s);
+            o.w = __shfl_down_sync(0xffffffffu, w.w, s);
+            w = OP == 0 ? add4(w, o) : coef4(w, o);
+        }
+    }
+    return w;
 }
 // Single-block reduce over n partials: lane l accumulates l, l+256, ... from
-// `init`, then the tree.
+// `init` in that order (loads issued eight at a time), then the tree.
 template <int OP>
 __device__ __forceinline__ float4 final_reduce(const float4* partials, uint32_t n, float4 init) {
     float4 v = init;
-    for (uint32_t i = threadIdx.x; i < n; i += kBlock) v = OP == 0 ? add4(v, partials[i]) : coef4(v, partials[i]);
+    uint32_t i = threadIdx.x;
+    for (; i + 7 * kBlock < n; i += 8 * kBlock) {
+        float4 t[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) t[k] = partials[i + k * kBlock];
+#pragma unroll
+        for (int k = 0; k < 8; k++) v = OP == 0 ? add4(v, t[k]) : coef4(v, t[k]);
+    }
+    for (; i < n; i += kBlock) v = OP == 0 ? add4(v, partials[i]) : coef4(v, partials[i]);
     return tree256<OP>(v);
 }
 __device__ __forceinline__ uint32_t groups_of(uint32_t n) { return (n + kBlock - 1) / kBlock; }
@@ -402,17 +544,8 @@ __global__ void __launch_bounds__(kBlock) k_em_prepare(EmDev D) {
     const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (i < D.E) {
-        int p[3], w;
-        edge_decode(D, i, p, &w);
-        const float m = mass(D, i);
-        float b = m * D.dt * D.emf[i] - m * (D.as[i] - D.asp[i]) + adjoint<2, true>(D, p, w) -
-                  adjoint<4, false>(D, p, w) - gauge<4>(D, i, p, w);
-        float r = b;
-        if (D.pf > 0.0f) r -= adjoint<0, false>(D, p, w) + gauge<0>(D, i, p, w) + m * D.x[i];
-        if (on_boundary(D, p, w)) {
-            r = 0.0f;
-            b = 0.0f;
-        }
+        const float2 br = EM_BY_AXIS(prepare_edge, D, i);
+        float b = br.x, r = br.y;
         const float physical_l1 = fabsf(b);
         const float scale = residual_scale(D);
         b /= scale;
@@ -470,10 +603,7 @@ __global__ void __launch_bounds__(kBlock) k_em_apply(EmDev D) {
             result += (c - D.p[i - zs]) + (c - D.p[i + zs]);
             q = result;
         } else {
-            int p[3], w;
-            edge_decode(D, i, p, &w);
-            q = adjoint<1, false>(D, p, w) + gauge<1>(D, i, p, w) + mass(D, i) * D.p[i];
-            if (on_boundary(D, p, w)) q = D.p[i];
+            q = EM_BY_AXIS(apply_edge, D, i);
         }
         D.w[i] = q;
         dot = D.p[i] * q;
@@ -528,13 +658,7 @@ __global__ void __launch_bounds__(kBlock) k_em_true_residual(EmDev D) {
     const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (i < D.E) {
-        int p[3], w;
-        edge_decode(D, i, p, &w);
-        const float m = mass(D, i);
-        float r = m * D.dt * D.emf[i] - m * (D.x[i] + (D.as[i] - D.asp[i])) + adjoint<2, true>(D, p, w) -
-                  adjoint<4, false>(D, p, w) - gauge<4>(D, i, p, w) - adjoint<0, false>(D, p, w) -
-                  gauge<0>(D, i, p, w);
-        if (on_boundary(D, p, w)) r = 0.0f;
+        float r = EM_BY_AXIS(true_residual_edge, D, i);
         r /= residual_scale(D);
         const float d = diagonal(D, i);
         D.r[i] = r;
