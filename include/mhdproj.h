@@ -326,6 +326,29 @@ int mhdproj_fluid_step(mhdproj_ctx *ctx, float *u, float *v, float *w, const flo
 int mhdproj_export_fields(const mhdproj_grid *grid, const float *cells, const char *directory, uint64_t step,
                           double time_s, const float origin_m[3], int moving_interface, const char *forcing_kind);
 
+/* Fluid mobility and cell phase lanes: the `phase` and `surface` passes of
+ * src/fluid/phase.wgsl:10-31 as FluidState::update_cells runs them
+ * (src/fluid/mod.rs:713-852).  Device arrays, n = nx*ny*nz cells:
+ *   materials   material id per cell; liquid_material = FluidConfig::material_id
+ *   thermal     the thermal phase's liquid fraction, read at thermal[i*thermal_stride]
+ *               (16 with the reference's thermal packet offset to state.y); NULL: none
+ *   interface   NULL runs `phase`; else (a, y) at interface[i*interface_stride + 0/1]
+ *               (4 for the reference's vec4 interface field)
+ *   mask        0/1 mobility per cell, updated in place
+ *   cells       16-float FluidCell records: `phase` writes reserved.y (float 13),
+ *               `surface` writes reserved = (1, f, a, y) (floats 12-15)
+ *   flags_device one u32 of device scratch
+ * *changed: bit 0 some cell's mobility changed (the caller relabels the
+ * topology, as update_cells does), bit 1 an interface fraction was outside
+ * [-1e-5, 1+1e-5] or not finite, which also returns MHDPROJ_ERR_INVALID with
+ * the reference's message (mhdproj_classify_last_error()).  Allocates nothing;
+ * synchronises `stream`. */
+int mhdproj_classify_cells(const mhdproj_grid *grid, const uint32_t *materials, uint32_t liquid_material,
+                           const float *thermal, uint32_t thermal_stride, const float *interface,
+                           uint32_t interface_stride, uint32_t *mask, float *cells, uint32_t *flags_device,
+                           uint32_t *changed, void *stream);
+const char *mhdproj_classify_last_error(void);
+
 /* Host utilities, mirroring src/fluid/multigrid.rs:25-65 and src/fluid/mod.rs:1447-1493. */
 /* Aggregation hierarchy: halve (ceil) until every dimension is <= 4.  Returns
  * 0 and the level count / coarse-cell total, or MHDPROJ_ERR_INVALID for zero,
@@ -415,6 +438,12 @@ int mhdproj_em_set_materials(mhdproj_em_ctx *ctx, const uint32_t *materials, con
                              uint32_t count, float conductivity_range[2]);
 /* Motional EMF per edge (device, E floats; NULL clears it). */
 int mhdproj_em_set_motional_emf(mhdproj_em_ctx *ctx, const float *emf);
+/* The motional EMF of EmState::set_velocity (src/em/mod.rs:757-834,
+ * motion.wgsl): per edge the conductivity-weighted u x B of the four cells
+ * around it, from the fluid's 16-float cell records (velocity floats 0-2,
+ * mobile where float 12 > 0.5; device, cells x 16) and the B of the last
+ * accepted EM step, with the conductivities of the last material update. */
+int mhdproj_em_set_motion(mhdproj_em_ctx *ctx, const float *fluid_cells);
 /* Overwrites the accepted reaction potential (device, E floats). */
 int mhdproj_em_set_reaction(mhdproj_em_ctx *ctx, const float *a);
 /* One step to time_s (initial != 0: the source-only solve EmState::new and

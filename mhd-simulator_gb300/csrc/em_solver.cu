@@ -815,6 +815,39 @@ __global__ void k_em_pack_work(EmDev D, float4* out) {
     if (i < D.E) out[i] = make_float4(D.x[i], D.r[i], D.p[i], D.w[i]);
 }
 
+// motion (src/em/motion.wgsl:8-26): the conductivity-weighted u x B of the
+// (up to) four cells around each edge, projected on the edge; fluid cells
+// are FluidCell records (velocity at floats 0-2, mobile where float 12 >
+// 0.5), B is this context's last cell result.
+__global__ void __launch_bounds__(kBlock) k_em_motion(EmDev D, const float* __restrict__ fluid) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= D.E) return;
+    int p[3], w;
+    edge_decode(D, i, p, &w);
+    const int a = (w + 1) % 3, b = (w + 2) % 3;
+    const uint32_t d[3] = {D.n[0], D.n[1], D.n[2]};
+    float weighted = 0.0f, sigma = 0.0f;
+    for (int u = 0; u < 2; u++)
+        for (int v = 0; v < 2; v++) {
+            int q[3] = {p[0], p[1], p[2]};
+            q[a] -= u;
+            q[b] -= v;
+            if (valid3(q, d)) {
+                const uint32_t c = (uint32_t)q[0] + D.n[0] * ((uint32_t)q[1] + D.n[1] * (uint32_t)q[2]);
+                const float sc = D.sig_c[c];
+                sigma += sc;
+                const float* f = fluid + (size_t)c * 16;
+                if (f[12] > 0.5f) {
+                    const float4 B = D.results[4 * (size_t)c];
+                    const float cr = w == 0 ? f[1] * B.z - f[2] * B.y : w == 1 ? f[2] * B.x - f[0] * B.z
+                                                                                 : f[0] * B.y - f[1] * B.x;
+                    weighted += sc * cr;
+                }
+            }
+        }
+    D.emf[i] = weighted / fmx(sigma, 1e-30f);
+}
+
 __global__ void k_em_pack_coefficients(EmDev D, float4* out) {
     const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     if (i < D.E) out[i] = make_float4(D.sig[i], D.diag[i], (float)D.flags[i], D.emf[i]);
@@ -1143,6 +1176,16 @@ int mhdproj_em_set_motional_emf(mhdproj_em_ctx* ctx, const float* emf) {
     if (!ctx) return MHDPROJ_ERR_INVALID;
     if (emf) EK(cudaMemcpyAsync(ctx->D.emf, emf, (size_t)ctx->D.E * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     else EK(cudaMemsetAsync(ctx->D.emf, 0, (size_t)ctx->D.E * 4, ctx->stream));
+    return em_wait(ctx);
+}
+
+// EmState::set_velocity (src/em/mod.rs:757-834): the lagged motional EMF
+// from the fluid's cell records and the B of the last accepted step.
+int mhdproj_em_set_motion(mhdproj_em_ctx* ctx, const float* fluid_cells) {
+    if (!ctx || !fluid_cells) return MHDPROJ_ERR_INVALID;
+    if (!ctx->materials) return em_fail(ctx, MHDPROJ_ERR_STATE, "set the EM materials first");
+    EM_LAUNCH(k_em_motion, ctx->D.E, ctx->D, fluid_cells);
+    EK(cudaGetLastError());
     return em_wait(ctx);
 }
 

@@ -157,6 +157,10 @@ def load():
                                                          C.POINTER(Diagnostics)]
     L.mhdproj_export_fields.argtypes = [C.POINTER(Grid), _vp, C.c_char_p, C.c_uint64, C.c_double,
                                         C.POINTER(C.c_float * 3), C.c_int, C.c_char_p]
+    L.mhdproj_classify_cells.argtypes = [C.POINTER(Grid), _vp, C.c_uint32, _vp, C.c_uint32, _vp, C.c_uint32, _vp,
+                                         _vp, _vp, C.POINTER(C.c_uint32), _vp]
+    L.mhdproj_classify_last_error.argtypes = []
+    L.mhdproj_classify_last_error.restype = C.c_char_p
     L.mhdproj_em_create.argtypes = [C.POINTER(EmConfig), C.POINTER(_vp)]
     L.mhdproj_em_destroy.argtypes = [_vp]
     L.mhdproj_em_last_error.argtypes = [_vp]
@@ -166,6 +170,7 @@ def load():
     L.mhdproj_em_set_materials.argtypes = [_vp, _vp, _vp, C.c_uint32, C.POINTER(C.c_float * 2)]
     L.mhdproj_em_set_motional_emf.argtypes = [_vp, _vp]
     L.mhdproj_em_set_reaction.argtypes = [_vp, _vp]
+    L.mhdproj_em_set_motion.argtypes = [_vp, _vp]
     L.mhdproj_em_advance.argtypes = [_vp, C.c_double, C.c_int, _vp, C.POINTER(EmDiagnostics)]
     L.mhdproj_em_copy.argtypes = [_vp, C.c_int, _vp]
     L.mhdproj_em_apply_operator.argtypes = [_vp, _vp, _vp, C.c_int]
@@ -181,8 +186,9 @@ EXPORTED = [
     "mhdproj_apply_preconditioner", "mhdproj_copy_coefficients", "mhdproj_copy_potential", "mhdproj_copy_topology",
     "mhdproj_hierarchy", "mhdproj_anchors", "mhdproj_profile_kernels", "mhdproj_divergence_noalloc",
     "mhdproj_kernel_launches", "mhdproj_fields", "mhdproj_fluid_step", "mhdproj_export_fields",
+    "mhdproj_classify_cells", "mhdproj_classify_last_error",
     "mhdproj_em_create", "mhdproj_em_destroy", "mhdproj_em_last_error", "mhdproj_em_set_stream", "mhdproj_em_sizes",
-    "mhdproj_em_set_materials", "mhdproj_em_set_motional_emf", "mhdproj_em_set_reaction", "mhdproj_em_advance",
+    "mhdproj_em_set_materials", "mhdproj_em_set_motional_emf", "mhdproj_em_set_motion", "mhdproj_em_set_reaction", "mhdproj_em_advance",
     "mhdproj_em_copy", "mhdproj_em_apply_operator", "mhdproj_em_kernel_launches",
 ]
 
@@ -215,6 +221,29 @@ def export_fields(dims, h, cells, directory, step=0, time_s=0.0, origin_m=(0.0, 
                                  C.byref(o), int(bool(moving_interface)), forcing_kind.encode())
     if rc:
         raise ProjectionError(rc, L.mhdproj_last_error(None).decode())
+
+
+def classify_cells(dims, materials, liquid_material, mask, cells, thermal=None, thermal_stride=1, interface=None,
+                   interface_stride=2, stream=None):
+    """The phase/surface passes of FluidState::update_cells
+    (src/fluid/phase.wgsl:10-31) on CUDA tensors: updates the 0/1 mobility
+    ``mask`` (int32/uint32 storage, one per cell) and the FluidCell
+    ``cells`` records (16 floats per cell) in place; returns the changed
+    flags (bit 0: some cell's mobility changed).  Raises ProjectionError with
+    the reference's message for an interface fraction out of [0, 1]."""
+    import torch
+
+    L = load()
+    g = Grid(int(dims[0]), int(dims[1]), int(dims[2]), 1.0, 0, 0)
+    scratch = torch.zeros(1, dtype=torch.int32, device=mask.device)
+    changed = C.c_uint32()
+    s = torch.cuda.current_stream() if stream is None else stream
+    rc = L.mhdproj_classify_cells(C.byref(g), _ptr(materials), int(liquid_material), _ptr(thermal),
+                                  int(thermal_stride), _ptr(interface), int(interface_stride), _ptr(mask),
+                                  _ptr(cells), _ptr(scratch), C.byref(changed), C.c_void_p(s.cuda_stream))
+    if rc:
+        raise ProjectionError(rc, L.mhdproj_classify_last_error().decode())
+    return int(changed.value)
 
 
 def hierarchy(dims4):
@@ -575,6 +604,12 @@ class EmInduction:
     def set_reaction(self, a):
         self._order()
         self._check(self._lib.mhdproj_em_set_reaction(self._ctx, _ptr(a.contiguous())))
+
+    def set_motion(self, fluid_cells):
+        """EmState::set_velocity: the motional EMF from the fluid's
+        (cells, 16) FluidCell records and this state's last B."""
+        self._order()
+        self._check(self._lib.mhdproj_em_set_motion(self._ctx, _ptr(fluid_cells.contiguous())))
 
     def advance(self, time_s, initial=False, applied=None):
         """One step to ``time_s``; returns :class:`EmDiagnostics`."""

@@ -25,7 +25,8 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler"
 EXACT = {"reference_kernels.cu", "step_kernels.cu", "em_solver.cu"}
 
 SOURCES = ["context.cu", "gb300_kernels.cu", "fine_kernels.cu", "fused_kernels.cu", "mg_kernels.cu", "reference_kernels.cu", "noalloc.cu",
-           "topology_kernels.cu", "step_kernels.cu", "export_fields.cu", "em_solver.cu"]
+           "topology_kernels.cu", "step_kernels.cu", "export_fields.cu", "em_solver.cu",
+           "classify.cu"]
 HOST_SOURCES = ["topology.cpp"]
 
 

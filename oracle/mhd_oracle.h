@@ -209,6 +209,13 @@ int onat_chain_adjoint(const onat_grid *g, const float *alpha, const uint8_t *so
                        const double *uk, const double *vk, const double *wk, float dt, int steps,
                        double rtol, double *gfu, double *gfv, double *gfw);
 
+/* phase / surface passes (src/fluid/phase.wgsl:10-31): mobility mask and
+ * FluidCell.reserved lanes; returns the changed flags (bit 0 mobility, bit 1
+ * an interface fraction out of range). interface == NULL: the phase pass. */
+uint32_t oref_classify_cells(uint32_t n, const uint32_t *materials, uint32_t liquid, const float *thermal,
+                             uint32_t thermal_stride, const float *interface, uint32_t interface_stride,
+                             uint32_t *mask, float *cells);
+
 /* ---- oem_*: the implicit EM induction solve (oracle_em.c) ----
  * FP32 restatement of the reference's edge-element A-formulation step:
  * src/em/induction.wgsl (coefficients, Jacobi-preconditioned CG with
@@ -230,6 +237,8 @@ void oem_sizes(const OEm *s, uint32_t out[8]);
 int oem_set_materials(OEm *s, const uint32_t *materials, const float *props, uint32_t n_props, float check[4]);
 /* Motional EMF per edge (NULL: zero), as set_velocity leaves it. */
 void oem_set_motional(OEm *s, const float *emf);
+/* Motional EMF from fluid cell records (set_velocity, motion.wgsl). */
+void oem_set_motion(OEm *s, const float *fluid_cells);
 /* Overwrite the accepted reaction potential (edges). */
 void oem_set_reaction(OEm *s, const float *a);
 /* which: 0 work (E x 4), 1 previous (E), 2 source (2E x 4), 3 cell results

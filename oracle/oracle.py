@@ -147,6 +147,9 @@ def lib():
                                          C.c_int, C.c_double, _f64p, _f64p, _f64p, C.POINTER(C.c_double)]
         L.onat_chain_adjoint.argtypes = [g, _f32p, _u8p, _f64p, _f64p, _f64p, C.c_float, C.c_int, C.c_double,
                                          _f64p, _f64p, _f64p]
+        L.oref_classify_cells.argtypes = [C.c_uint32, _u32p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
+                                          C.c_uint32, _u32p, _f32p]
+        L.oref_classify_cells.restype = C.c_uint32
         L.oem_new.argtypes = [C.POINTER(C.c_uint32), C.c_float, C.POINTER(C.c_float), C.c_double, C.c_float,
                               C.c_uint32, C.c_int]
         L.oem_new.restype = C.c_void_p
@@ -156,6 +159,7 @@ def lib():
         L.oem_set_materials.restype = C.c_int
         L.oem_set_motional.argtypes = [C.c_void_p, C.c_void_p]
         L.oem_set_reaction.argtypes = [C.c_void_p, _f32p]
+        L.oem_set_motion.argtypes = [C.c_void_p, _f32p]
         L.oem_get.argtypes = [C.c_void_p, C.c_int, _f32p]
         L.oem_apply_operator.argtypes = [C.c_void_p, _f32p, _f32p, C.c_int]
         L.oem_advance.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_void_p, _f32p, _f32p]
@@ -391,6 +395,18 @@ def chain_adjoint(g, alpha, solid, uk, vk, wk, dt, steps, rtol=1e-13):
     return st, (gu, gv, gw)
 
 
+def classify_cells(materials, liquid_material, mask, cells, thermal=None, thermal_stride=1, interface=None,
+                   interface_stride=2):
+    """phase/surface passes in place on `mask` (uint32) and `cells` (n x 16
+    float32); returns the changed flags."""
+    m = np.ascontiguousarray(materials, np.uint32).reshape(-1)
+    th = None if thermal is None else np.ascontiguousarray(thermal, np.float32).reshape(-1)
+    it = None if interface is None else np.ascontiguousarray(interface, np.float32).reshape(-1)
+    return int(lib().oref_classify_cells(m.size, m, int(liquid_material), None if th is None else th.ctypes.data,
+                                         int(thermal_stride), None if it is None else it.ctypes.data,
+                                         int(interface_stride), mask, cells.reshape(-1)))
+
+
 class EmSolve:
     """The EM induction step restated in FP32 (oracle_em.c): one instance per
     grid, mirroring EmState (src/em/mod.rs) without its source summation."""
@@ -435,6 +451,9 @@ class EmSolve:
 
     def set_reaction(self, a):
         lib().oem_set_reaction(self._p, np.ascontiguousarray(a, np.float32))
+
+    def set_motion(self, fluid_cells):
+        lib().oem_set_motion(self._p, np.ascontiguousarray(fluid_cells, np.float32).reshape(-1))
 
     def work(self):
         out = np.zeros((self.edges, 4), np.float32)

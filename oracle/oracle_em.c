@@ -657,6 +657,35 @@ int oem_set_materials(OEm *s, const uint32_t *materials, const float *props, uin
 void oem_set_motional(OEm *s, const float *emf) {
     for (uint32_t i = 0; i < s->edges[3]; i++) s->source[i + s->edges[3]].x = emf ? emf[i] : 0.0f;
 }
+/* motion (src/em/motion.wgsl:8-26): fluid cell records (16 floats: velocity
+   0-2, mobile where float 12 > 0.5) and this state's last B. */
+void oem_set_motion(OEm *s, const float *fluid) {
+    uint32_t E = s->edges[3];
+    for (uint32_t i = 0; i < E; i++) {
+        int p[3], w;
+        edge_decode(s, i, p, &w);
+        int a = (w + 1) % 3, b = (w + 2) % 3;
+        float weighted = 0.0f, sigma = 0.0f;
+        for (int u = 0; u < 2; u++)
+            for (int v = 0; v < 2; v++) {
+                int q[3] = {p[0], p[1], p[2]};
+                q[a] -= u;
+                q[b] -= v;
+                if (!valid3(q, s->dims)) continue;
+                uint32_t c = (uint32_t)q[0] + s->dims[0] * ((uint32_t)q[1] + s->dims[1] * (uint32_t)q[2]);
+                float sc = cell_sigma(s, q);
+                sigma += sc;
+                const float *f = fluid + (size_t)c * 16;
+                if (f[12] > 0.5f) {
+                    f4 B = s->results[4 * (size_t)c];
+                    float cr[3] = {f[1] * B.z - f[2] * B.y, f[2] * B.x - f[0] * B.z, f[0] * B.y - f[1] * B.x};
+                    weighted += sc * cr[w];
+                }
+            }
+        s->source[i + E].x = weighted / maxf(sigma, 1e-30f);
+    }
+}
+
 void oem_set_reaction(OEm *s, const float *a) {
     for (uint32_t i = 0; i < s->edges[3]; i++) s->work[i].x = a[i];
 }

@@ -1801,3 +1801,47 @@ int oref_diffuse_surface_stress(const oref_params *params, const uint32_t *mask,
     free(S.mu); free(S.t4); free(S.t2); free(S.y0); free(S.f0);
     return 0;
 }
+
+/* ---- phase / surface classification (src/fluid/phase.wgsl:10-31) ----
+ * The mobility mask and FluidCell.reserved lanes from the material ids, the
+ * thermal phase (stride in floats; state.y of the reference's 16-float
+ * packet) and the interface field (a, y at floats 0 and 1 of each record).
+ * interface == NULL runs the `phase` pass, else the `surface` pass.
+ * Returns the changed flags: bit 0 mobility changed, bit 1 a fraction
+ * outside [-1e-5, 1+1e-5] or not finite (src/surface.rs:12). */
+uint32_t oref_classify_cells(uint32_t n, const uint32_t *materials, uint32_t liquid, const float *thermal,
+                             uint32_t thermal_stride, const float *interface, uint32_t interface_stride,
+                             uint32_t *mask, float *cells) {
+    uint32_t changed = 0;
+    const float eps = 1e-5f;
+    for (uint32_t i = 0; i < n; i++) {
+        int mobile;
+        if (!interface) {
+            float fraction = 0.0f;
+            if (materials[i] == liquid) fraction = thermal[(size_t)i * thermal_stride];
+            mobile = fraction > 1e-6f;
+            cells[(size_t)i * 16 + 13] = fraction;
+        } else {
+            float a = interface[(size_t)i * interface_stride];
+            if (!(a >= -eps && a <= 1.0f + eps)) {
+                changed |= 2u;
+                continue;
+            }
+            float f = 1.0f;
+            if (thermal && a > 0.0f) f = thermal[(size_t)i * thermal_stride];
+            int wall = materials[i] != 0u && materials[i] != liquid;
+            mobile = !wall && !(a > 0.0f && f <= 1e-6f);
+            float *r = cells + (size_t)i * 16 + 12;
+            r[0] = 1.0f;
+            r[1] = f;
+            r[2] = a;
+            r[3] = interface[(size_t)i * interface_stride + 1];
+        }
+        int old = mask[i] != 0u;
+        if (mobile != old) {
+            mask[i] = mobile ? 1u : 0u;
+            changed |= 1u;
+        }
+    }
+    return changed;
+}

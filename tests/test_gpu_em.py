@@ -261,3 +261,23 @@ def test_bad_material_id_is_rejected(gpu):
     with pytest.raises(mhdproj.ProjectionError):
         mhdproj.EmInduction((0, 8, 8), 1e-3)
     em.close()
+
+
+def test_motional_emf_from_fluid_cells_bit_exact(gpu):
+    """EmState::set_velocity: the motional EMF from FluidCell records and the
+    last B (motion.wgsl), then a step driven by it."""
+    import mhdproj
+
+    pair, applied = _driven_pair(gpu, mhdproj, 16)
+    pair.set_materials()
+    pair.step(0.0, initial=True, applied=applied(0.0), label="initial")
+    pair.step(1e-5, applied=applied(1e-5), label="step 0")
+    rng = np.random.default_rng(21)
+    fluid = rng.standard_normal((pair.cpu.cells, 16)).astype(np.float32)
+    fluid[:, 12] = (rng.random(pair.cpu.cells) < 0.6).astype(np.float32)
+    pair.cpu.set_motion(fluid)
+    pair.gpu.set_motion(pair.dev(fluid))
+    E = pair.cpu.edges
+    _assert_bits(pair.gpu.copy("coefficients").cpu().numpy()[:, 3], pair.cpu.source()[E:, 0], "motional EMF")
+    pair.step(2e-5, applied=applied(2e-5), label="with motion")
+    pair.close()

@@ -190,3 +190,32 @@ def test_tiny_source_uses_power_of_two_scaling():
     assert np.linalg.norm(x1 - x0) <= 1e-4 * np.linalg.norm(x0)
     base.close()
     tiny.close()
+
+
+def test_motional_emf_of_rigid_motion():
+    """motion.wgsl on a uniform conductor moving rigidly through the uniform
+    applied field: every edge carries (v x B) along its axis."""
+    n, h = 8, 1e-3
+    origin = (-4e-3,) * 3
+    s = O.EmSolve((n, n, n), h, origin=origin)
+    s.set_materials(np.full(n ** 3, 6, np.uint32), _props())
+    b = (np.float32(0.01), np.float32(-0.02), np.float32(0.03))
+    assert s.advance(0.0, initial=True, applied=_uniform_applied(s, h, origin, b))[0] == s.OK
+    v = np.array([0.5, -0.25, 1.0], np.float32)
+    fluid = np.zeros((s.cells, 16), np.float32)
+    fluid[:, :3] = v
+    fluid[:, 12] = 1.0
+    s.set_motion(fluid)
+    emf = s.source()[s.edges:, 0]
+    bb = s.results()[:, :3].mean(0)
+    vxb = np.cross(v.astype(np.float64), bb.astype(np.float64))
+    off = 0
+    for axis in range(3):
+        cnt = s.edge_counts[axis]
+        np.testing.assert_allclose(emf[off:off + cnt], vxb[axis], rtol=1e-4, atol=1e-9)
+        off += cnt
+    # immobile cells contribute conductivity but no EMF
+    fluid[:, 12] = 0.0
+    s.set_motion(fluid)
+    assert not s.source()[s.edges:, 0].any()
+    s.close()
