@@ -370,10 +370,10 @@ uint32_t mhdproj_anchors(uint32_t *mask, const uint32_t dims[3], uint32_t period
  * B, J, the Lorentz force J x B and Joule heat per cell, and commits or rolls
  * back.  The applied potential A_s of coils and magnets is an input (the
  * reference's source pass, src/em/source.wgsl, is not built); so is the
- * motional EMF (src/em/motion.wgsl).  Not built either: the nodal
- * preconditioner that the reference switches to after 1024 Jacobi
- * iterations when max_iterations exceeds 1024 (reported as
- * MHDPROJ_ERR_UNSUPPORTED with the state restored), and body integrals.
+ * motional EMF (src/em/motion.wgsl, or mhdproj_em_set_motion from the fluid's
+ * cell records).  The nodal gradient correction (src/em/nodal.wgsl) takes
+ * over after nodal_switch_after Jacobi iterations as in the reference.  Not
+ * built: the per-body force integrals.
  * ------------------------------------------------------------------------- */
 typedef struct mhdproj_em_ctx mhdproj_em_ctx;
 
@@ -390,6 +390,8 @@ typedef struct {
     float relative_tolerance;   /* EmConfig::relative_tolerance */
     uint32_t max_iterations;    /* EmConfig::max_iterations */
     int32_t mode;               /* mhdproj_em_mode */
+    uint32_t nodal_switch_after;/* Jacobi iterations before the nodal gradient correction takes over
+                                   (1024 in the reference, src/em/mod.rs:892; 0 = from the first pass) */
 } mhdproj_em_config;
 
 /* Diagnostics (src/em/mod.rs:33-46) and the solver's status record. */

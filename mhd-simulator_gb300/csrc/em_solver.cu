@@ -27,11 +27,11 @@
 // reductions accumulate their partials with a stride of 256 before the tree,
 // so results are bit-identical to the FP32 restatement of the same shader.
 //
-// Not built (the caller supplies what they produce): the coil/magnet source
-// summation (src/em/source.wgsl, src/em/sources.rs), the nodal
-// preconditioner that advance_to switches to after 1024 Jacobi iterations
-// when max_iterations exceeds 1024 (src/em/nodal.rs; reported as
-// MHDPROJ_ERR_UNSUPPORTED at that point), and the per-body force integrals.
+// Also here: the nodal gradient correction advance_to switches to after 1024
+// Jacobi iterations (src/em/nodal.wgsl) and the motional EMF
+// (src/em/motion.wgsl).  Not built (the caller supplies what they produce):
+// the coil/magnet source summation (src/em/source.wgsl, src/em/sources.rs)
+// and the per-body force integrals.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -51,12 +51,12 @@ namespace {
 
 constexpr int kBlock = 256;
 constexpr uint32_t kBatch = 32;        // iterations between status reads (mod.rs:952)
-constexpr uint32_t kNodalSwitch = 1024;  // mod.rs:892
 
 struct EmDev {
     uint32_t n[3], cells;
     uint32_t e[3], E;
     uint32_t initial;  // control.y: the applied-field solve has no mass term
+    uint32_t nodal;    // control.w: the nodal gradient correction is active
     float pf;          // origin.w: increment prediction factor
     float dt, mu0, h, tol2;
     // edges
@@ -66,6 +66,7 @@ struct EmDev {
     // cells and faces
     float *sig_c, *mu_c;
     float* nu[3];
+    float* nv;  // (nx+1)(ny+1)(nz+1) nodal corrections
     float4* partials;
     float4* scalars;  // [0] (rz, rr, bb, threshold) [1] (alpha, beta, iterations, status) [2..5] fields [6].x scale
     float4* results;  // cells x 4: (B,|B|) (J,|J|) (F, heat) (applied B, |applied B|)
@@ -645,11 +646,11 @@ __global__ void __launch_bounds__(kBlock) k_em_beta_reduce(EmDev D) {
         if (fabsf(sum.x) > 3e38f || fabsf(sum.y) > 3e38f) D.scalars[1].w = 2.0f;
     }
 }
-// update_search, Jacobi branch (induction.wgsl:214)
+// update_search (induction.wgsl:214): z = r/d, or the nodal z left in w
 __global__ void __launch_bounds__(kBlock) k_em_update_search(EmDev D) {
     const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
     if (i < D.E && active(D)) {
-        const float z = D.r[i] / D.w[i];
+        const float z = D.nodal ? D.w[i] : D.r[i] / D.w[i];
         D.p[i] = z + D.scalars[1].y * D.p[i];
     }
 }
@@ -674,6 +675,74 @@ __global__ void __launch_bounds__(kBlock) k_em_restart_reduce(EmDev D) {
         D.scalars[0].x = sum.x;
         D.scalars[0].y = sum.y;
         D.scalars[1].w = sum.y <= D.scalars[0].w ? 1.0f : 0.0f;
+    }
+}
+
+// ------------------------------------------------------------ nodal correction
+// The additive gradient-space Jacobi correction of src/em/nodal.wgsl: a value
+// per interior node from the edge residuals, then z = r/d + nv(lower node)
+// - nv(upper node) on every edge.
+__device__ __forceinline__ float cached_air_node(const EmDev& D, int x, int y, int z) {
+    if (x <= 0 || y <= 0 || z <= 0 || x >= (int)D.n[0] || y >= (int)D.n[1] || z >= (int)D.n[2]) return 0.0f;
+    const uint32_t i = (uint32_t)x + D.n[0] * ((uint32_t)y + (D.n[1] + 1) * (uint32_t)z);  // the x-edge at the node
+    return (D.flags[i] & 1) ? 1.0f : 0.0f;
+}
+template <int A>
+__device__ __forceinline__ void nodal_axis(const EmDev& D, int x, int y, int z, float& rhs, float& diag) {
+    int lx = x, ly = y, lz = z, ux = x, uy = y, uz = z;
+    bump<A>(lx, ly, lz, -1);
+    bump<A>(ux, uy, uz, 1);
+    const uint32_t dx = D.n[0] + (A != 0), dy = D.n[1] + (A != 1);
+    const uint32_t off = A == 0 ? 0u : A == 1 ? D.e[0] : D.e[0] + D.e[1];
+    const uint32_t out = off + (uint32_t)x + dx * ((uint32_t)y + dy * (uint32_t)z);
+    const uint32_t inc = off + (uint32_t)lx + dx * ((uint32_t)ly + dy * (uint32_t)lz);
+    rhs += D.r[out] - D.r[inc];
+    diag += mass(D, out) + mass(D, inc) + cached_air_node(D, lx, ly, lz) + cached_air_node(D, ux, uy, uz);
+}
+template <bool INITIAL>
+__global__ void __launch_bounds__(kBlock) k_em_nodal_build(EmDev D, uint32_t nodes) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= nodes || (!INITIAL && !active(D))) return;
+    const uint32_t d0 = D.n[0] + 1, d1 = D.n[1] + 1;
+    const int x = (int)(i % d0), y = (int)((i / d0) % d1), z = (int)(i / (d0 * d1));
+    float value = 0.0f;
+    if (x > 0 && y > 0 && z > 0 && x < (int)D.n[0] && y < (int)D.n[1] && z < (int)D.n[2]) {
+        float rhs = 0.0f, diag = 36.0f * cached_air_node(D, x, y, z);
+        nodal_axis<0>(D, x, y, z, rhs, diag);
+        nodal_axis<1>(D, x, y, z, rhs, diag);
+        nodal_axis<2>(D, x, y, z, rhs, diag);
+        value = rhs / fmx(diag, 1e-30f);
+    }
+    D.nv[i] = value;
+}
+template <int W>
+__device__ __forceinline__ float nodal_z_edge(const EmDev& D, uint32_t i, uint32_t q) {
+    int x, y, z;
+    decode_s<W>(D, q, x, y, z);
+    const uint32_t d0 = D.n[0] + 1, d1 = D.n[1] + 1;
+    const uint32_t lo = (uint32_t)x + d0 * ((uint32_t)y + d1 * (uint32_t)z);
+    bump<W>(x, y, z, 1);
+    const uint32_t up = (uint32_t)x + d0 * ((uint32_t)y + d1 * (uint32_t)z);
+    return D.r[i] / diagonal(D, i) + D.nv[lo] - D.nv[up];
+}
+// nodal_initial / nodal_update: only the x and y lanes of the partials are
+// written (the update only while the solve is active).
+template <bool INITIAL>
+__global__ void __launch_bounds__(kBlock) k_em_nodal(EmDev D) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const bool on = INITIAL || active(D);
+    if (i < D.E && on) {
+        const float r = D.r[i];
+        const float z = EM_BY_AXIS(nodal_z_edge, D, i);
+        if (INITIAL) D.p[i] = z;
+        D.w[i] = z;
+        v = make_float4(r * z, r * r, 0.0f, 0.0f);
+    }
+    const float4 t = tree256<0>(v);
+    if (threadIdx.x == 0 && on) {
+        D.partials[blockIdx.x].x = t.x;
+        D.partials[blockIdx.x].y = t.y;
     }
 }
 
@@ -870,6 +939,7 @@ struct mhdproj_em_ctx {
     uint32_t props_cap = 0;
     cudaGraphExec_t batch = nullptr;  // kBatch CG iterations
     uint32_t batch_initial = 0;       // the step constants the batch graph was captured with
+    uint32_t batch_nodal = 0;
     float batch_dt = 0.0f;
     bool materials = false;
     double time_s = 0.0, last_dt = 0.0;
@@ -948,18 +1018,35 @@ static bool status_finite(const float4* sc) {
         if (!std::isfinite(v[k])) return false;
     return true;
 }
+static uint32_t em_nodes(const EmDev& D) { return (D.n[0] + 1) * (D.n[1] + 1) * (D.n[2] + 1); }
+// append_nodal (src/em/mod.rs:639-659)
+static void em_append_nodal(mhdproj_em_ctx* ctx, bool initial) {
+    const EmDev& D = ctx->D;
+    if (!D.nodal) return;
+    if (initial) {
+        EM_LAUNCH(k_em_nodal_build<true>, em_nodes(D), D, em_nodes(D));
+        EM_LAUNCH(k_em_nodal<true>, D.E, D);
+    } else {
+        EM_LAUNCH(k_em_nodal_build<false>, em_nodes(D), D, em_nodes(D));
+        EM_LAUNCH(k_em_nodal<false>, D.E, D);
+    }
+}
 static void em_iteration(mhdproj_em_ctx* ctx) {
     const EmDev& D = ctx->D;
     EM_LAUNCH(k_em_apply<true>, D.E, D);
     EM_SINGLE(k_em_alpha_reduce, D);
     EM_LAUNCH(k_em_update_residual, D.E, D);
+    em_append_nodal(ctx, false);
     EM_SINGLE(k_em_beta_reduce, D);
     EM_LAUNCH(k_em_update_search, D.E, D);
 }
 // The iteration kernels take EmDev by value, so the graph holds the step
-// constants they read (initial, dt); it is captured again when they change.
+// constants they read (initial, dt, nodal mode); it is captured again when
+// they change.
 static int em_build_batch(mhdproj_em_ctx* ctx) {
-    if (ctx->batch && ctx->batch_initial == ctx->D.initial && ctx->batch_dt == ctx->D.dt) return 0;
+    if (ctx->batch && ctx->batch_initial == ctx->D.initial && ctx->batch_dt == ctx->D.dt &&
+        ctx->batch_nodal == ctx->D.nodal)
+        return 0;
     if (ctx->batch) {
         cudaGraphExecDestroy(ctx->batch);
         ctx->batch = nullptr;
@@ -976,15 +1063,18 @@ static int em_build_batch(mhdproj_em_ctx* ctx) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return em_fail(ctx, MHDPROJ_ERR_CUDA, "batch instantiate: %s", cudaGetErrorString(e));
     ctx->batch_initial = ctx->D.initial;
+    ctx->batch_nodal = ctx->D.nodal;
     ctx->batch_dt = ctx->D.dt;
     return 0;
 }
 static void em_prepare(mhdproj_em_ctx* ctx) {
     EM_LAUNCH(k_em_prepare, ctx->D.E, ctx->D);
+    em_append_nodal(ctx, true);
     EM_SINGLE(k_em_initial_reduce, ctx->D);
 }
 static void em_restart(mhdproj_em_ctx* ctx) {
     EM_LAUNCH(k_em_true_residual, ctx->D.E, ctx->D);
+    em_append_nodal(ctx, true);
     EM_SINGLE(k_em_restart_reduce, ctx->D);
 }
 
@@ -1056,7 +1146,7 @@ int mhdproj_em_create(const mhdproj_em_config* cfg, mhdproj_em_ctx** out) {
     ctx->own_stream = true;
     const size_t E = D.E, C = D.cells;
     const size_t groups = std::max(em_groups(D.E), em_groups(D.cells));
-    cudaError_t es[32];
+    cudaError_t es[40];
     int ne = 0;
     es[ne++] = cudaEventCreateWithFlags(&ctx->ev, cudaEventDisableTiming);
     es[ne++] = cudaEventCreate(&ctx->t0);
@@ -1078,6 +1168,7 @@ int mhdproj_em_create(const mhdproj_em_config* cfg, mhdproj_em_ctx** out) {
         uint64_t f = (x + (a == 0)) * (y + (a == 1)) * (z + (a == 2));
         es[ne++] = em_alloc(ctx, &D.nu[a], f * 4);
     }
+    es[ne++] = em_alloc(ctx, &D.nv, (x + 1) * (y + 1) * (z + 1) * 4);
     es[ne++] = em_alloc(ctx, &D.partials, (4 * groups + 4) * sizeof(float4));
     es[ne++] = em_alloc(ctx, &D.scalars, 8 * sizeof(float4));
     es[ne++] = em_alloc(ctx, &D.results, 4 * C * sizeof(float4));
@@ -1259,7 +1350,11 @@ int mhdproj_em_advance(mhdproj_em_ctx* ctx, double time_s, int initial, const fl
     D.pf = pf;
     D.dt = (float)ctx->cfg.dt_s;
     D.tol2 = ctx->cfg.relative_tolerance * ctx->cfg.relative_tolerance;
-    const bool allow_nodal = !initial && ctx->cfg.mode == MHDPROJ_EM_INDUCTION && ctx->cfg.max_iterations > kNodalSwitch;
+    const uint32_t switch_after = ctx->cfg.nodal_switch_after;
+    const bool allow_nodal = !initial && ctx->cfg.mode == MHDPROJ_EM_INDUCTION && ctx->cfg.max_iterations > switch_after;
+    // each step starts in Jacobi mode; a zero switch point starts in nodal
+    // mode (src/em/mod.rs:897-903)
+    D.nodal = (allow_nodal && switch_after == 0) ? 1u : 0u;
     EK(cudaEventRecord(ctx->t0, ctx->stream));
     EM_LAUNCH(k_em_sources, D.E, D, applied);
     EM_LAUNCH(k_em_begin_step, D.E, D);
@@ -1292,15 +1387,14 @@ int mhdproj_em_advance(mhdproj_em_ctx* ctx, double time_s, int initial, const fl
             }
             EK(cudaGetLastError());
             if ((rc = em_read_status(ctx))) return rc;
-            if (allow_nodal && ctx->h_sc[1].w == 0.0f && status_finite(ctx->h_sc) && its() >= kNodalSwitch &&
-                its() < cap) {
-                EM_LAUNCH(k_em_rollback, D.E, D);
-                ctx->can_predict = false;
-                if ((rc = em_wait(ctx))) return rc;
-                return em_fail(ctx, MHDPROJ_ERR_UNSUPPORTED,
-                               "EM solve reached %u Jacobi iterations; the nodal preconditioner the reference "
-                               "switches to here is not built (state restored)",
-                               its());
+            // switch to the nodal correction at a true-residual restart
+            // (src/em/mod.rs:966-990); the batch graph is captured again
+            if (allow_nodal && !D.nodal && ctx->h_sc[1].w == 0.0f && status_finite(ctx->h_sc) &&
+                its() >= switch_after && its() < cap) {
+                D.nodal = 1;
+                em_restart(ctx);
+                if ((rc = em_read_status(ctx))) return rc;
+                if ((rc = em_build_batch(ctx))) return rc;
             }
         }
         if (ctx->h_sc[1].w != 1.0f) break;

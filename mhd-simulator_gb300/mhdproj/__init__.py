@@ -83,7 +83,7 @@ class StepParams(C.Structure):
 class EmConfig(C.Structure):
     _fields_ = [("nx", C.c_uint32), ("ny", C.c_uint32), ("nz", C.c_uint32), ("cell_m", C.c_float),
                 ("origin_m", C.c_float * 3), ("dt_s", C.c_double), ("relative_tolerance", C.c_float),
-                ("max_iterations", C.c_uint32), ("mode", C.c_int32)]
+                ("max_iterations", C.c_uint32), ("mode", C.c_int32), ("nodal_switch_after", C.c_uint32)]
 
 
 class EmDiagnostics(C.Structure):
@@ -537,13 +537,14 @@ class EmInduction:
     """
 
     def __init__(self, dims, cell_m, dt_s=1e-5, relative_tolerance=1e-5, max_iterations=1000,
-                 origin_m=(0.0, 0.0, 0.0), mode="induction", stream=None):
+                 origin_m=(0.0, 0.0, 0.0), mode="induction", nodal_switch_after=1024, stream=None):
         import torch
 
         self._torch = torch
         L = load()
         cfg = EmConfig(int(dims[0]), int(dims[1]), int(dims[2]), float(cell_m), (C.c_float * 3)(*origin_m),
-                       float(dt_s), float(relative_tolerance), int(max_iterations), EM_MODES[mode])
+                       float(dt_s), float(relative_tolerance), int(max_iterations), EM_MODES[mode],
+                       int(nodal_switch_after))
         h_ = C.c_void_p()
         rc = L.mhdproj_em_create(C.byref(cfg), C.byref(h_))
         if rc:

@@ -223,7 +223,7 @@ uint32_t oref_classify_cells(uint32_t n, const uint32_t *materials, uint32_t liq
  * EmState::advance_to (src/em/mod.rs:863-1090).  Edges are numbered x-edges,
  * y-edges, z-edges, each block x-fastest (src/em/common.wgsl:3-6). */
 typedef struct OEm OEm;
-enum { OEM_OK = 0, OEM_NOT_CONVERGED = 1, OEM_NONFINITE = 2, OEM_NODAL_REQUIRED = 3 };
+enum { OEM_OK = 0, OEM_NOT_CONVERGED = 1, OEM_NONFINITE = 2 };
 /* vacuum != 0 is the applied-field mode (every cell reads as air). */
 OEm *oem_new(const uint32_t dims[3], float h, const float origin[3], double dt_s, float rel_tol, uint32_t max_it,
              int vacuum);
@@ -237,6 +237,9 @@ void oem_sizes(const OEm *s, uint32_t out[8]);
 int oem_set_materials(OEm *s, const uint32_t *materials, const float *props, uint32_t n_props, float check[4]);
 /* Motional EMF per edge (NULL: zero), as set_velocity leaves it. */
 void oem_set_motional(OEm *s, const float *emf);
+/* Iterations before the solve switches to the nodal correction (1024 in the
+ * reference; 0 = from the first pass, the reference's test setting). */
+void oem_set_nodal_switch(OEm *s, uint32_t after);
 /* Motional EMF from fluid cell records (set_velocity, motion.wgsl). */
 void oem_set_motion(OEm *s, const float *fluid_cells);
 /* Overwrite the accepted reaction potential (edges). */

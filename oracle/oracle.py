@@ -160,6 +160,7 @@ def lib():
         L.oem_set_motional.argtypes = [C.c_void_p, C.c_void_p]
         L.oem_set_reaction.argtypes = [C.c_void_p, _f32p]
         L.oem_set_motion.argtypes = [C.c_void_p, _f32p]
+        L.oem_set_nodal_switch.argtypes = [C.c_void_p, C.c_uint32]
         L.oem_get.argtypes = [C.c_void_p, C.c_int, _f32p]
         L.oem_apply_operator.argtypes = [C.c_void_p, _f32p, _f32p, C.c_int]
         L.oem_advance.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_void_p, _f32p, _f32p]
@@ -411,9 +412,10 @@ class EmSolve:
     """The EM induction step restated in FP32 (oracle_em.c): one instance per
     grid, mirroring EmState (src/em/mod.rs) without its source summation."""
 
-    OK, NOT_CONVERGED, NONFINITE, NODAL_REQUIRED = 0, 1, 2, 3
+    OK, NOT_CONVERGED, NONFINITE = 0, 1, 2
 
-    def __init__(self, dims, h, dt=1e-5, rel_tol=1e-5, max_iterations=1000, origin=(0.0, 0.0, 0.0), vacuum=False):
+    def __init__(self, dims, h, dt=1e-5, rel_tol=1e-5, max_iterations=1000, origin=(0.0, 0.0, 0.0), vacuum=False,
+                 nodal_switch_after=1024):
         L = lib()
         d = (C.c_uint32 * 3)(*dims)
         o = (C.c_float * 3)(*origin)
@@ -426,6 +428,7 @@ class EmSolve:
         self.cells = int(sz[3])
         self.edge_counts = tuple(int(v) for v in sz[4:7])
         self.edges = int(sz[7])
+        L.oem_set_nodal_switch(self._p, int(nodal_switch_after))
 
     def close(self):
         if self._p:

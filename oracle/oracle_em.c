@@ -30,11 +30,13 @@
  *   work[i]       = (reaction increment x, r, p, A p or diagonal)
  * mix(e1, e2, t) is e1*(1-t) + e2*t and length(v) is sqrt((x*x + y*y) + z*z).
  *
- * Out of scope, as in the library: the nodal preconditioner that the
- * reference enables after 1024 iterations (advance_to reports
- * OEM_NODAL_REQUIRED where the switch would occur), the coil and magnet
- * source summation (the caller supplies the applied potential) and the
- * per-body force integrals.
+ *   src/em/nodal.wgsl            the additive nodal gradient correction the
+ *                                solve switches to after 1024 iterations
+ *   src/em/motion.wgsl:8-26      the motional EMF
+ *
+ * Out of scope, as in the library: the coil and magnet source summation
+ * (the caller supplies the applied potential) and the per-body force
+ * integrals.
  */
 #include <math.h>
 #include <stdint.h>
@@ -59,6 +61,8 @@ struct OEm {
     float rel_tol;
     uint32_t max_it;
     int can_predict;
+    uint32_t nodal_after; /* iterations before the nodal switch (1024 in the reference) */
+    float *nodal;         /* (nx+1)(ny+1)(nz+1) nodal corrections */
 };
 
 static f4 F4(float x, float y, float z, float w) { f4 r = {x, y, z, w}; return r; }
@@ -450,6 +454,86 @@ static void restart_reduce(OEm *s) {
     s->scalars[1].w = sum.y <= s->scalars[0].w ? 1.0f : 0.0f;
 }
 
+/* ---- nodal gradient-space correction (src/em/nodal.wgsl) ---- */
+static uint32_t nodal_count(const OEm *s) { return (s->dims[0] + 1) * (s->dims[1] + 1) * (s->dims[2] + 1); }
+static float cached_air_node(const OEm *s, const int p[3]) {
+    for (int k = 0; k < 3; k++)
+        if (p[k] <= 0 || p[k] >= (int)s->dims[k]) return 0.0f;
+    return s->source[edge_index(s, 0, p) + s->edges[3]].y;
+}
+static float nodal_value(const OEm *s, uint32_t i) {
+    uint32_t d0 = s->dims[0] + 1, d1 = s->dims[1] + 1;
+    int p[3] = {(int)(i % d0), (int)((i / d0) % d1), (int)(i / (d0 * d1))};
+    for (int k = 0; k < 3; k++)
+        if (p[k] <= 0 || p[k] >= (int)s->dims[k]) return 0.0f;
+    float rhs = 0.0f, diag = 36.0f * cached_air_node(s, p);
+    for (int a = 0; a < 3; a++) {
+        int lower[3] = {p[0], p[1], p[2]}, upper[3] = {p[0], p[1], p[2]};
+        lower[a] -= 1;
+        upper[a] += 1;
+        uint32_t out = edge_index(s, a, p), inc = edge_index(s, a, lower);
+        rhs += s->work[out].y - s->work[inc].y;
+        diag += mass(s, out) + mass(s, inc) + cached_air_node(s, lower) + cached_air_node(s, upper);
+    }
+    return rhs / maxf(diag, 1e-30f);
+}
+static void nodal_build(OEm *s, int initial) {
+    if (!initial && s->scalars[1].w != 0.0f) return;
+    uint32_t n = nodal_count(s);
+#pragma omp parallel for schedule(static)
+    for (uint32_t i = 0; i < n; i++) s->nodal[i] = nodal_value(s, i);
+}
+static float nodal_z(const OEm *s, uint32_t i) {
+    int p[3], w;
+    edge_decode(s, i, p, &w);
+    uint32_t d0 = s->dims[0] + 1, d1 = s->dims[1] + 1;
+    uint32_t lo = (uint32_t)p[0] + d0 * ((uint32_t)p[1] + d1 * (uint32_t)p[2]);
+    p[w] += 1;
+    uint32_t up = (uint32_t)p[0] + d0 * ((uint32_t)p[1] + d1 * (uint32_t)p[2]);
+    return s->work[i].y / diagonal(s, i) + s->nodal[lo] - s->nodal[up];
+}
+static int g_nodal_initial = 0;
+static f4 k_nodal(OEm *s, uint32_t i) {
+    f4 v = F4(0, 0, 0, 0);
+    if (g_nodal_initial) {
+        float r = s->work[i].y, z = nodal_z(s, i);
+        s->work[i].z = z;
+        s->work[i].w = z;
+        v = F4(r * z, r * r, 0.0f, 0.0f);
+    } else if (s->scalars[1].w == 0.0f) {
+        float r = s->work[i].y, z = nodal_z(s, i);
+        s->work[i].w = z;
+        v = F4(r * z, r * r, 0.0f, 0.0f);
+    }
+    return v;
+}
+/* nodal_initial / nodal_update: only the x and y lanes of the partials are
+   written (the update only while the solve is active). */
+static void nodal_pass(OEm *s, int initial) {
+    uint32_t n = s->edges[3], ng = groups_of(n);
+    int write = initial || s->scalars[1].w == 0.0f;
+    g_nodal_initial = initial;
+#pragma omp parallel for schedule(static)
+    for (uint32_t g = 0; g < ng; g++) {
+        f4 lane[256];
+        for (uint32_t l = 0; l < 256; l++) {
+            uint32_t i = g * 256 + l;
+            lane[l] = i < n ? k_nodal(s, i) : F4(0, 0, 0, 0);
+        }
+        f4 t = tree(lane, RED_SUM);
+        if (write) {
+            s->partials[g].x = t.x;
+            s->partials[g].y = t.y;
+        }
+    }
+}
+/* append_nodal (src/em/mod.rs:639-659) */
+static void append_nodal(OEm *s, int initial) {
+    if (s->control[3] != 1) return;
+    nodal_build(s, initial);
+    nodal_pass(s, initial);
+}
+
 static void begin_step(OEm *s) {
     s->scalars[6].x = 1.0f;
 #pragma omp parallel for schedule(static)
@@ -620,7 +704,10 @@ OEm *oem_new(const uint32_t dims[3], float h, const float origin[3], double dt_s
     s->partials = (f4 *)calloc(4 * ng + 4, sizeof(f4));
     s->results = (f4 *)calloc(4 * C + 4, sizeof(f4));
     s->checkpoint = (f4 *)calloc(4 * C + 4, sizeof(f4));
-    if (!s->materials || !s->source || !s->work || !s->previous || !s->partials || !s->results || !s->checkpoint) {
+    s->nodal = (float *)calloc((size_t)(x + 1) * (y + 1) * (z + 1), 4);
+    s->nodal_after = 1024;
+    if (!s->materials || !s->source || !s->work || !s->previous || !s->partials || !s->results || !s->checkpoint ||
+        !s->nodal) {
         oem_free(s);
         return NULL;
     }
@@ -630,7 +717,7 @@ OEm *oem_new(const uint32_t dims[3], float h, const float origin[3], double dt_s
 void oem_free(OEm *s) {
     if (!s) return;
     free(s->materials); free(s->props); free(s->source); free(s->work); free(s->previous);
-    free(s->partials); free(s->results); free(s->checkpoint);
+    free(s->partials); free(s->results); free(s->checkpoint); free(s->nodal);
     free(s);
 }
 
@@ -719,12 +806,16 @@ static int status_finite(const f4 *sc) {
 }
 static void solve_prepare(OEm *s) {
     edge_pass(s, k_prepare, F4(0, 0, 0, 0), RED_SUM, 1);
+    append_nodal(s, 1);
     initial_reduce(s);
 }
 static void restart(OEm *s) {
     edge_pass(s, k_true_residual, F4(0, 0, 0, 0), RED_SUM, 1);
+    append_nodal(s, 1);
     restart_reduce(s);
 }
+
+void oem_set_nodal_switch(OEm *s, uint32_t after) { s->nodal_after = after; }
 
 /* EmState::advance_to (src/em/mod.rs:863-1090) for one step to `time_s`.
    `applied` (E floats) is the applied potential at that time, or NULL when it
@@ -741,7 +832,10 @@ int oem_advance(OEm *s, double time_s, int initial, const float *applied, float 
     s->origin[3] = pf;
     s->physical[0] = (float)s->dt_s;
     s->physical[3] = s->rel_tol * s->rel_tol;
-    int allow_nodal = !initial && s->control[2] == 0 && s->max_it > 1024;
+    int allow_nodal = !initial && s->control[2] == 0 && s->max_it > s->nodal_after;
+    /* update_sources leaves control.w = 0; a zero switch point starts in
+       nodal mode (src/em/mod.rs:897-903) */
+    s->control[3] = (allow_nodal && s->nodal_after == 0) ? 1u : 0u;
     /* update_sources: the source pass shifts the history (source.wgsl:16-17);
        an unchanged field keeps a zero history delta (hold_source). */
     for (uint32_t i = 0; i < E; i++) {
@@ -769,15 +863,16 @@ int oem_advance(OEm *s, double time_s, int initial, const float *applied, float 
                 edge_pass(s, k_apply, F4(0, 0, 0, 0), RED_SUM, 1);
                 alpha_reduce(s);
                 edge_pass(s, k_update_residual, F4(0, 0, 0, 0), RED_SUM, 1);
+                append_nodal(s, 0);
                 beta_reduce(s);
                 update_search(s);
             }
-            if (allow_nodal && s->scalars[1].w == 0.0f && status_finite(s->scalars) &&
-                (uint32_t)s->scalars[1].z >= 1024 && (uint32_t)s->scalars[1].z < s->max_it) {
-                rollback(s);
-                s->can_predict = 0;
-                memcpy(status_out, s->scalars, 32);
-                return OEM_NODAL_REQUIRED;
+            /* switch to the nodal correction at a true-residual restart
+               (src/em/mod.rs:966-990) */
+            if (allow_nodal && s->control[3] == 0 && s->scalars[1].w == 0.0f && status_finite(s->scalars) &&
+                (uint32_t)s->scalars[1].z >= s->nodal_after && (uint32_t)s->scalars[1].z < s->max_it) {
+                s->control[3] = 1;
+                restart(s);
             }
         }
         if (s->scalars[1].w != 1.0f) break;

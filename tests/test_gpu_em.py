@@ -12,7 +12,9 @@ reductions take their 256-stride path), a non-cubic grid with partial cells
 power-of-two residual rescale of a tiny source, the applied-field (vacuum)
 mode, the homogeneous-conductor eigenmode of src/em/tests.rs:272-333 against
 its backward-Euler decay, the air-stencil operator check of
-tests.rs:665-738, a failing solve's rollback and a bad material id.
+tests.rs:665-738, the nodal gradient correction (from the first pass and
+switched in mid-solve), the motional EMF from fluid cell records, a failing
+solve's rollback and a bad material id.
 """
 import math
 
@@ -42,12 +44,12 @@ class Pair:
     """The same EM problem in the library and in the oracle."""
 
     def __init__(self, torch, mhdproj, dims, h, materials, props, dt=1e-5, tol=1e-5, max_it=1000,
-                 origin=(0.0, 0.0, 0.0), mode="induction"):
+                 origin=(0.0, 0.0, 0.0), mode="induction", nodal_switch_after=1024):
         self.torch = torch
         self.gpu = mhdproj.EmInduction(dims, h, dt_s=dt, relative_tolerance=tol, max_iterations=max_it,
-                                       origin_m=origin, mode=mode)
+                                       origin_m=origin, mode=mode, nodal_switch_after=nodal_switch_after)
         self.cpu = O.EmSolve(dims, h, dt=dt, rel_tol=tol, max_iterations=max_it, origin=origin,
-                             vacuum=(mode == "applied"))
+                             vacuum=(mode == "applied"), nodal_switch_after=nodal_switch_after)
         assert self.gpu.edges == self.cpu.edges and self.gpu.cells == self.cpu.cells
         self.m = np.ascontiguousarray(materials, np.uint32)
         self.props = np.ascontiguousarray(props, np.float32)
@@ -94,11 +96,12 @@ class Pair:
         self.cpu.close()
 
 
-def _driven_pair(torch, mhdproj, n, sigma_scale=40.0, scale=1.0, max_it=1000):
+def _driven_pair(torch, mhdproj, n, sigma_scale=40.0, scale=1.0, max_it=1000, nodal_switch_after=1024):
     h = 1e-3
     origin = (-0.5 * n * h,) * 3
     pair = Pair(torch, mhdproj, (n, n, n), h, _ring(n, inner=0.19 * n, outer=0.38 * n, z0=n // 3, z1=n - n // 3),
-                _props(SIGMA_316 * sigma_scale, 1.0), max_it=max_it, origin=origin)
+                _props(SIGMA_316 * sigma_scale, 1.0), max_it=max_it, origin=origin,
+                nodal_switch_after=nodal_switch_after)
     b = (np.float32(0.0), np.float32(0.0), np.float32(0.02))
     applied = lambda t: _uniform_applied(pair.cpu, h, origin, b, scale=scale * math.sin(2 * math.pi * 1e3 * t))
     return pair, applied
@@ -280,4 +283,21 @@ def test_motional_emf_from_fluid_cells_bit_exact(gpu):
     E = pair.cpu.edges
     _assert_bits(pair.gpu.copy("coefficients").cpu().numpy()[:, 3], pair.cpu.source()[E:, 0], "motional EMF")
     pair.step(2e-5, applied=applied(2e-5), label="with motion")
+    pair.close()
+
+
+@pytest.mark.parametrize("n,after", [(16, 0), (32, 16)])
+def test_nodal_correction_bit_exact(gpu, n, after):
+    """The nodal gradient correction from the first pass, and switched in
+    after the first 32-iteration batch at a true-residual restart."""
+    import mhdproj
+
+    pair, applied = _driven_pair(gpu, mhdproj, n, nodal_switch_after=after)
+    pair.set_materials()
+    pair.step(0.0, initial=True, applied=applied(0.0), label="initial")
+    t = 0.0
+    for k in range(3):
+        t += 1e-5
+        d, st, _ = pair.step(t, applied=applied(t), label=f"nodal step {k}")
+        assert st[7] == 1.0
     pair.close()

@@ -219,3 +219,28 @@ def test_motional_emf_of_rigid_motion():
     s.set_motion(fluid)
     assert not s.source()[s.edges:, 0].any()
     s.close()
+
+
+@pytest.mark.parametrize("n,after", [(16, 0), (32, 16)])
+def test_nodal_correction_solves_the_same_system(n, after):
+    """The nodal gradient correction (src/em/nodal.wgsl) from the first pass
+    (the reference's test setting nodal_switch_after = 0) and after a
+    mid-solve switch at a true-residual restart (src/em/mod.rs:966-990)
+    converge to the Jacobi solution within the solve tolerance."""
+    from mhdproj import synth
+
+    c = synth.em_ring(n)
+    out = {}
+    for sw in (1024, after):
+        s = O.EmSolve(c["dims"], c["h"], dt=c["dt"], origin=c["origin"], max_iterations=1000,
+                      nodal_switch_after=sw)
+        s.set_materials(c["materials"], c["properties"])
+        assert s.advance(0.0, initial=True, applied=c["applied"](0.0))[0] == s.OK
+        for k in (1, 2):
+            rc, st, _ = s.advance(k * c["dt"], applied=c["applied"](k * c["dt"]))
+            assert rc == s.OK and st[7] == 1.0
+            if sw == after and after > 0:
+                assert st[6] > 32  # the solve ran past the switch point and continued
+        out[sw] = s.reaction().astype(np.float64)
+        s.close()
+    assert np.linalg.norm(out[after] - out[1024]) <= 1e-4 * np.linalg.norm(out[1024])
