@@ -365,6 +365,23 @@ def run_ours(args):
                 "relative_residual": ds[-1].relative_residual, "max_J": ds[-1].maxima[1],
                 "kernel_launches_per_step": launches / steps}
 
+    def em_sources_leg(n, segments, reps=5):
+        """The source pass (src/em/source.wgsl): a wire loop of `segments`
+        straight elements summed at every edge of an n^3 grid, timed on the
+        EM stream.  About 60 flops, two logarithms and three square roots
+        per edge-element interaction."""
+        c = synth.em_ring(n)
+        em = mhdproj.EmInduction(c["dims"], c["h"], dt_s=c["dt"], origin_m=c["origin"])
+        el = synth.em_loop_elements(0.3 * n * c["h"], 100.0, segments, core=c["h"])
+        em.evaluate_sources(el)
+        ms_s, _ = timed(em, reps, lambda e: e.evaluate_sources(el))
+        edges = em.edges
+        em.close()
+        sec = ms_s / reps * 1e-3
+        return {"workload": f"{segments} wire segments at the {edges} edges of {n}^3 cells",
+                "ms": ms_s / reps, "interactions_per_s": edges * segments / sec,
+                "approx_tflops": 60.0 * edges * segments / sec / 1e12}
+
     def em_cpu_leg(n, warm=1):
         """The oracle's FP32 restatement of the same EM step on the host cores
         (OpenMP over edge groups), one timed step after `warm` steps."""
@@ -381,14 +398,20 @@ def run_ours(args):
         t0 = time.perf_counter()
         rc, st, _ = s.advance((warm + 1) * c["dt"], applied=a)
         sec = time.perf_counter() - t0
+        el = synth.em_loop_elements(0.3 * n * c["h"], 100.0, 256, core=c["h"])
+        t0 = time.perf_counter()
+        s.evaluate_sources(el)
+        src_sec = time.perf_counter() - t0
+        edges = s.edges
         s.close()
         return {"steps_per_s": 1.0 / sec, "seconds_per_step": sec, "iterations": int(st[6]), "ok": rc == 0,
+                "source_pass_interactions_per_s": edges * 256 / src_sec,
                 "cores": os.cpu_count() or 1, "kind": "port",
                 "sample": f"oracle/oracle_em.c on em_ring {n}^3, step {warm + 1} of the driven sequence"}
 
     pr = make(args.precision)
     if args.em:
-        out_e = {"em_step128": em_leg(128, 5), "em_step64": em_leg(64, 5)}
+        out_e = {"em_step128": em_leg(128, 5), "em_step64": em_leg(64, 5), "em_sources": em_sources_leg(128, 1024)}
         if rank == 0:
             print(json.dumps(out_e))
         pr.close()
@@ -569,6 +592,7 @@ def run_ours(args):
             if rank == 0 and world == 1:
                 e64["cpu_baseline"] = em_cpu_leg(64)
             line["em_step64"] = e64
+            line["em_sources"] = em_sources_leg(128, 1024)
         except mhdproj.ProjectionError as exc:
             line["em_step"] = {"unavailable": str(exc)}
         # CPU baseline: bounded sample of the reference algorithm on the host cores

@@ -368,10 +368,11 @@ uint32_t mhdproj_anchors(uint32_t *mask, const uint32_t dims[3], uint32_t period
  * (src/em/common.wgsl:3-6).  A step solves the backward-Euler curl-curl
  * system for the reaction potential with Jacobi-preconditioned CG, computes
  * B, J, the Lorentz force J x B and Joule heat per cell, and commits or rolls
- * back.  The applied potential A_s of coils and magnets is an input (the
- * reference's source pass, src/em/source.wgsl, is not built); so is the
- * motional EMF (src/em/motion.wgsl, or mhdproj_em_set_motion from the fluid's
- * cell records).  The nodal gradient correction (src/em/nodal.wgsl) takes
+ * back.  The applied potential A_s of coils and magnets is an input, which
+ * mhdproj_em_evaluate_sources computes from the source elements (the
+ * reference's source pass, src/em/source.wgsl); so is the motional EMF
+ * (src/em/motion.wgsl, or mhdproj_em_set_motion from the fluid's cell
+ * records).  The nodal gradient correction (src/em/nodal.wgsl) takes
  * over after nodal_switch_after Jacobi iterations as in the reference.  Not
  * built: the per-body force integrals.
  * ------------------------------------------------------------------------- */
@@ -440,6 +441,18 @@ int mhdproj_em_set_materials(mhdproj_em_ctx *ctx, const uint32_t *materials, con
                              uint32_t count, float conductivity_range[2]);
 /* Motional EMF per edge (device, E floats; NULL clears it). */
 int mhdproj_em_set_motional_emf(mhdproj_em_ctx *ctx, const float *emf);
+/* The source pass (src/em/source.wgsl): the applied potential A_s at every
+ * edge midpoint of `count` source elements as EmConfig::elements builds them
+ * (src/em/sources.rs:280-338), 12 floats each (a, b, c as vec4; host
+ * memory).  c.y selects the kind: < 0.5 a wire segment from a to b with core
+ * radius c.x carrying c.z amperes; < 1.5 a surface-current element at a with
+ * moment b scaled by c.z, softening c.x; otherwise a uniform field b tesla
+ * scaled by c.z.  Elements with c.z == 0 contribute nothing.  Summed in
+ * batches of 32 elements as the reference's passes are.  Writes E floats to
+ * `applied` (device), ready for mhdproj_em_advance.  Fails with the
+ * reference's messages for more than 1e6 elements, non-finite values, or
+ * more than 5e10 edge-element pairs. */
+int mhdproj_em_evaluate_sources(mhdproj_em_ctx *ctx, const float *elements, uint32_t count, float *applied);
 /* The motional EMF of EmState::set_velocity (src/em/mod.rs:757-834,
  * motion.wgsl): per edge the conductivity-weighted u x B of the four cells
  * around it, from the fluid's 16-float cell records (velocity floats 0-2,

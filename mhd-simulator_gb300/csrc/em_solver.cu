@@ -28,10 +28,11 @@
 // so results are bit-identical to the FP32 restatement of the same shader.
 //
 // Also here: the nodal gradient correction advance_to switches to after 1024
-// Jacobi iterations (src/em/nodal.wgsl) and the motional EMF
-// (src/em/motion.wgsl).  Not built (the caller supplies what they produce):
-// the coil/magnet source summation (src/em/source.wgsl, src/em/sources.rs)
-// and the per-body force integrals.
+// Jacobi iterations (src/em/nodal.wgsl), the motional EMF
+// (src/em/motion.wgsl) and the source pass that sums the applied potential
+// of wire, surface-current and uniform-field elements (src/em/source.wgsl).
+// Not built: building the elements from the model (src/em/sources.rs, host
+// code the caller keeps) and the per-body force integrals.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -59,6 +60,7 @@ struct EmDev {
     uint32_t nodal;    // control.w: the nodal gradient correction is active
     float pf;          // origin.w: increment prediction factor
     float dt, mu0, h, tol2;
+    float origin[3];
     // edges
     float *as, *asp, *sig, *diag, *emf;
     uint8_t* flags;  // bit 0: lower node gauged, bit 1: upper node gauged, bit 2: air stencil
@@ -877,6 +879,100 @@ __global__ void __launch_bounds__(kBlock) k_em_field_reduce(EmDev D) {
     }
 }
 
+// ------------------------------------------------------------ sources
+// The source pass (src/em/source.wgsl:5-17): the applied potential of the
+// source elements at every edge midpoint.  Elements arrive in tiles of 32 --
+// the reference's batch per pass, whose vector sum is added to the running
+// value -- staged in shared memory with the per-element segment direction
+// and length; each thread owns one edge.  Kinds (c.y): wire segment a->b
+// with core radius c.x and current c.z; surface-current element at a with
+// moment b scaled by c.z, softening c.x; uniform field b scaled by c.z.
+// Compute-bound: about 60 flops, two logarithms and three square roots per
+// wire interaction.
+__device__ __forceinline__ float ash(float x) {
+    const float sg = x > 0.0f ? 1.0f : x < 0.0f ? -1.0f : 0.0f;
+    return sg * logf(fabsf(x) + sqrtf(x * x + 1.0f));
+}
+constexpr int kTile = 32;
+__global__ void __launch_bounds__(kBlock) k_em_source_eval(EmDev D, const float* __restrict__ el, uint32_t count,
+                                                            float* __restrict__ out) {
+    __shared__ float tile[kTile][14];
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    int w = 0;
+    float p[3] = {0.0f, 0.0f, 0.0f};
+    if (i < D.E) {
+        int e[3];
+        edge_decode(D, i, e, &w);
+        float pe[3] = {(float)e[0], (float)e[1], (float)e[2]};
+        pe[w] += 0.5f;
+        p[0] = D.origin[0] + pe[0] * D.h;
+        p[1] = D.origin[1] + pe[1] * D.h;
+        p[2] = D.origin[2] + pe[2] * D.h;
+    }
+    float acc = 0.0f;
+    const uint32_t nb = count == 0 ? 1u : (count + kTile - 1) / kTile;
+    for (uint32_t bi = 0; bi < nb; bi++) {
+        __syncthreads();
+        if (threadIdx.x < kTile) {
+            const uint32_t j = bi * kTile + threadIdx.x;
+            float* t = tile[threadIdx.x];
+            if (j < count) {
+                const float* q = el + 12 * (size_t)j;
+                t[0] = q[0];
+                t[1] = q[1];
+                t[2] = q[2];
+                t[3] = q[4];
+                t[4] = q[5];
+                t[5] = q[6];
+                t[6] = q[8];
+                t[7] = q[9];
+                t[8] = q[10];
+                if (q[9] < 0.5f) {
+                    const float d0 = q[4] - q[0], d1 = q[5] - q[1], d2 = q[6] - q[2];
+                    const float len = sqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+                    t[9] = d0 / len;
+                    t[10] = d1 / len;
+                    t[11] = d2 / len;
+                    t[12] = len;
+                }
+            } else {
+                t[8] = 0.0f;  // no contribution
+            }
+        }
+        __syncthreads();
+        if (i < D.E) {
+            const uint32_t left = count - bi * kTile;
+            const uint32_t end = count == 0 ? 0u : (left < (uint32_t)kTile ? left : (uint32_t)kTile);
+            float a = 0.0f;
+            for (uint32_t k = 0; k < end; k++) {
+                const float* t = tile[k];
+                const float cz = t[8];
+                if (cz == 0.0f) continue;
+                const float r0 = p[0] - t[0], r1 = p[1] - t[1], r2 = p[2] - t[2];
+                const float kind = t[7];
+                if (kind < 0.5f) {
+                    const float u0 = t[9], u1 = t[10], u2 = t[11], len = t[12];
+                    const float tt = r0 * u0 + r1 * u1 + r2 * u2;
+                    const float q0 = r0 - u0 * tt, q1 = r1 - u1 * tt, q2 = r2 - u2 * tt;
+                    const float radius = sqrtf(q0 * q0 + q1 * q1 + q2 * q2 + t[6] * t[6]);
+                    const float uw = w == 0 ? u0 : w == 1 ? u1 : u2;
+                    a += uw * (1e-7f * cz * (ash(tt / radius) - ash((tt - len) / radius)));
+                } else if (kind < 1.5f) {
+                    const float bw = w == 0 ? t[3] : w == 1 ? t[4] : t[5];
+                    a += bw * (1e-7f * cz * (1.0f / sqrtf(r0 * r0 + r1 * r1 + r2 * r2 + t[6] * t[6])));
+                } else {
+                    const float b0 = t[3], b1 = t[4], b2 = t[5];
+                    const float cw = w == 0 ? b1 * p[2] - b2 * p[1] : w == 1 ? b2 * p[0] - b0 * p[2]
+                                                                      : b0 * p[1] - b1 * p[0];
+                    a += 0.5f * cz * cw;
+                }
+            }
+            acc = bi == 0 ? a : acc + a;
+        }
+    }
+    if (i < D.E) out[i] = acc;
+}
+
 // Interleaves the planar work vectors into the reference's vec4 record
 // (x, r, p, w) for inspection.
 __global__ void k_em_pack_work(EmDev D, float4* out) {
@@ -937,6 +1033,8 @@ struct mhdproj_em_ctx {
     float4* checkpoint = nullptr;
     float* d_props = nullptr;
     uint32_t props_cap = 0;
+    float* d_elements = nullptr;
+    uint32_t elements_cap = 0;
     cudaGraphExec_t batch = nullptr;  // kBatch CG iterations
     uint32_t batch_initial = 0;       // the step constants the batch graph was captured with
     uint32_t batch_nodal = 0;
@@ -1133,6 +1231,7 @@ int mhdproj_em_create(const mhdproj_em_config* cfg, mhdproj_em_ctx** out) {
     D.h = cfg->cell_m;
     D.tol2 = 1e-10f;
     D.vacuum = cfg->mode == MHDPROJ_EM_APPLIED ? 1u : 0u;
+    for (int k = 0; k < 3; k++) D.origin[k] = cfg->origin_m[k];
     auto bail = [&](int code) {
         mhdproj_em_destroy(ctx);
         return code;
@@ -1267,6 +1366,31 @@ int mhdproj_em_set_motional_emf(mhdproj_em_ctx* ctx, const float* emf) {
     if (!ctx) return MHDPROJ_ERR_INVALID;
     if (emf) EK(cudaMemcpyAsync(ctx->D.emf, emf, (size_t)ctx->D.E * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     else EK(cudaMemsetAsync(ctx->D.emf, 0, (size_t)ctx->D.E * 4, ctx->stream));
+    return em_wait(ctx);
+}
+
+// The source pass over host-side elements (12 floats each), into `applied`
+// (device, one float per edge).
+int mhdproj_em_evaluate_sources(mhdproj_em_ctx* ctx, const float* elements, uint32_t count, float* applied) {
+    if (!ctx || !applied || (count && !elements)) return MHDPROJ_ERR_INVALID;
+    if (count > 1000000u)  // src/em/sources.rs:330-336
+        return em_fail(ctx, MHDPROJ_ERR_INVALID, "Source discretization is too large or has nonfinite values");
+    for (size_t k = 0; k < 12 * (size_t)count; k++)
+        if (!std::isfinite(elements[k]))
+            return em_fail(ctx, MHDPROJ_ERR_INVALID, "Source discretization is too large or has nonfinite values");
+    if ((uint64_t)ctx->D.E * count > 50000000000ull)  // src/em/mod.rs:208-210
+        return em_fail(ctx, MHDPROJ_ERR_INVALID,
+                       "Direct source summation exceeds the work budget for this grid; reduce source refinement/"
+                       "segment count or increase cell spacing");
+    if (count > ctx->elements_cap) {
+        float* p = nullptr;
+        EK(em_alloc(ctx, &p, (size_t)count * 48));
+        ctx->d_elements = p;
+        ctx->elements_cap = count;
+    }
+    if (count) EK(cudaMemcpyAsync(ctx->d_elements, elements, (size_t)count * 48, cudaMemcpyHostToDevice, ctx->stream));
+    EM_LAUNCH(k_em_source_eval, ctx->D.E, ctx->D, ctx->d_elements, count, applied);
+    EK(cudaGetLastError());
     return em_wait(ctx);
 }
 

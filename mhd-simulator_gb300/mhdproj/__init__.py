@@ -171,6 +171,7 @@ def load():
     L.mhdproj_em_set_motional_emf.argtypes = [_vp, _vp]
     L.mhdproj_em_set_reaction.argtypes = [_vp, _vp]
     L.mhdproj_em_set_motion.argtypes = [_vp, _vp]
+    L.mhdproj_em_evaluate_sources.argtypes = [_vp, _vp, C.c_uint32, _vp]
     L.mhdproj_em_advance.argtypes = [_vp, C.c_double, C.c_int, _vp, C.POINTER(EmDiagnostics)]
     L.mhdproj_em_copy.argtypes = [_vp, C.c_int, _vp]
     L.mhdproj_em_apply_operator.argtypes = [_vp, _vp, _vp, C.c_int]
@@ -188,7 +189,7 @@ EXPORTED = [
     "mhdproj_kernel_launches", "mhdproj_fields", "mhdproj_fluid_step", "mhdproj_export_fields",
     "mhdproj_classify_cells", "mhdproj_classify_last_error",
     "mhdproj_em_create", "mhdproj_em_destroy", "mhdproj_em_last_error", "mhdproj_em_set_stream", "mhdproj_em_sizes",
-    "mhdproj_em_set_materials", "mhdproj_em_set_motional_emf", "mhdproj_em_set_motion", "mhdproj_em_set_reaction", "mhdproj_em_advance",
+    "mhdproj_em_set_materials", "mhdproj_em_set_motional_emf", "mhdproj_em_set_motion", "mhdproj_em_evaluate_sources", "mhdproj_em_set_reaction", "mhdproj_em_advance",
     "mhdproj_em_copy", "mhdproj_em_apply_operator", "mhdproj_em_kernel_launches",
 ]
 
@@ -605,6 +606,16 @@ class EmInduction:
     def set_reaction(self, a):
         self._order()
         self._check(self._lib.mhdproj_em_set_reaction(self._ctx, _ptr(a.contiguous())))
+
+    def evaluate_sources(self, elements):
+        """The applied potential (edges) of source elements, an (n, 12)
+        float32 array on the host (EmConfig::elements records)."""
+        el = np.ascontiguousarray(elements, np.float32).reshape(-1, 12)
+        out = self._torch.empty(self.edges, dtype=self._torch.float32, device="cuda")
+        self._order()
+        self._check(self._lib.mhdproj_em_evaluate_sources(self._ctx, _host_ptr(el) if el.size else None, el.shape[0],
+                                                          _ptr(out)))
+        return out
 
     def set_motion(self, fluid_cells):
         """EmState::set_velocity: the motional EMF from the fluid's

@@ -240,3 +240,59 @@ def em_ring(n: int) -> dict:
     applied = lambda t: (base * np.float32(np.sin(2 * np.pi * 1e3 * t))).astype(np.float32)
     return dict(dims=(n, n, n), h=h, origin=origin, materials=m.reshape(-1), properties=props, dt=1e-5,
                 applied=applied)
+
+
+def em_loop_elements(radius, current, segments, centre=(0.0, 0.0, 0.0), core=0.0):
+    """A closed polygonal wire loop in the plane z = centre[2]: `segments`
+    straight elements (EmConfig::elements records, 12 float32 each)."""
+    ang = 2.0 * np.pi * np.arange(segments + 1) / segments
+    pts = np.stack([centre[0] + radius * np.cos(ang), centre[1] + radius * np.sin(ang),
+                    np.full(segments + 1, centre[2])], 1)
+    el = np.zeros((segments, 12), np.float32)
+    el[:, 0:3] = pts[:-1]
+    el[:, 4:7] = pts[1:]
+    el[:, 8] = core
+    el[:, 9] = 0.0
+    el[:, 10] = current
+    return el
+
+
+def em_magnet_block_elements(half_x, half_y, half_z, magnetization, divisions, smoothing=0.0):
+    """Surface-current elements of a uniformly magnetised block centred at the
+    origin (M along z): each side face is split into divisions^2 squares of
+    two triangles; element = (centroid, M x outward area vector, smoothing),
+    as EmConfig::elements builds magnet bodies."""
+    m = np.array([0.0, 0.0, magnetization])
+    out = []
+    faces = []
+    for sx in (-1.0, 1.0):   # x = +-half_x, outward normal along x
+        faces.append((np.array([sx * half_x, 0, 0]), np.array([0, 1.0, 0]) * half_y, np.array([0, 0, 1.0]) * half_z,
+                      np.array([sx, 0, 0])))
+    for sy in (-1.0, 1.0):
+        faces.append((np.array([0, sy * half_y, 0]), np.array([1.0, 0, 0]) * half_x, np.array([0, 0, 1.0]) * half_z,
+                      np.array([0, sy, 0])))
+    for c, du, dv, n in faces:
+        for i in range(divisions):
+            for j in range(divisions):
+                u0, u1 = -1 + 2 * i / divisions, -1 + 2 * (i + 1) / divisions
+                v0, v1 = -1 + 2 * j / divisions, -1 + 2 * (j + 1) / divisions
+                q = [c + du * u0 + dv * v0, c + du * u1 + dv * v0, c + du * u1 + dv * v1, c + du * u0 + dv * v1]
+                for tri in ((q[0], q[1], q[2]), (q[0], q[2], q[3])):
+                    a, b, cc = tri
+                    area = np.cross(b - a, cc - a) * 0.5
+                    if np.dot(area, n) < 0:
+                        area = -area
+                    e = np.zeros(12)
+                    e[0:3] = (a + b + cc) / 3.0
+                    e[4:7] = np.cross(m, area)
+                    e[8], e[9], e[10] = smoothing, 1.0, 1.0
+                    out.append(e)
+    return np.array(out, np.float32)
+
+
+def em_uniform_element(b, scale=1.0):
+    e = np.zeros((1, 12), np.float32)
+    e[0, 4:7] = b
+    e[0, 9] = 2.0
+    e[0, 10] = scale
+    return e

@@ -240,6 +240,9 @@ void oem_set_motional(OEm *s, const float *emf);
 /* Iterations before the solve switches to the nodal correction (1024 in the
  * reference; 0 = from the first pass, the reference's test setting). */
 void oem_set_nodal_switch(OEm *s, uint32_t after);
+/* Applied potential of source elements (12 floats each) at the edges
+ * (the source pass, source.wgsl); out: E floats. */
+void oem_evaluate_sources(const OEm *s, const float *elements, uint32_t count, float *out);
 /* Motional EMF from fluid cell records (set_velocity, motion.wgsl). */
 void oem_set_motion(OEm *s, const float *fluid_cells);
 /* Overwrite the accepted reaction potential (edges). */

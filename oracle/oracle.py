@@ -161,6 +161,7 @@ def lib():
         L.oem_set_reaction.argtypes = [C.c_void_p, _f32p]
         L.oem_set_motion.argtypes = [C.c_void_p, _f32p]
         L.oem_set_nodal_switch.argtypes = [C.c_void_p, C.c_uint32]
+        L.oem_evaluate_sources.argtypes = [C.c_void_p, _f32p, C.c_uint32, _f32p]
         L.oem_get.argtypes = [C.c_void_p, C.c_int, _f32p]
         L.oem_apply_operator.argtypes = [C.c_void_p, _f32p, _f32p, C.c_int]
         L.oem_advance.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_void_p, _f32p, _f32p]
@@ -454,6 +455,13 @@ class EmSolve:
 
     def set_reaction(self, a):
         lib().oem_set_reaction(self._p, np.ascontiguousarray(a, np.float32))
+
+    def evaluate_sources(self, elements):
+        el = np.ascontiguousarray(elements, np.float32).reshape(-1, 12)
+        out = np.zeros(self.edges, np.float32)
+        lib().oem_evaluate_sources(self._p, el.reshape(-1) if el.size else np.zeros(12, np.float32), el.shape[0],
+                                   out)
+        return out
 
     def set_motion(self, fluid_cells):
         lib().oem_set_motion(self._p, np.ascontiguousarray(fluid_cells, np.float32).reshape(-1))

@@ -34,9 +34,10 @@
  *                                solve switches to after 1024 iterations
  *   src/em/motion.wgsl:8-26      the motional EMF
  *
- * Out of scope, as in the library: the coil and magnet source summation
- * (the caller supplies the applied potential) and the per-body force
- * integrals.
+ *   src/em/source.wgsl:5-17      the applied potential of source elements
+ *
+ * Out of scope, as in the library: building the source elements from the
+ * model (src/em/sources.rs) and the per-body force integrals.
  */
 #include <math.h>
 #include <stdint.h>
@@ -744,6 +745,59 @@ int oem_set_materials(OEm *s, const uint32_t *materials, const float *props, uin
 void oem_set_motional(OEm *s, const float *emf) {
     for (uint32_t i = 0; i < s->edges[3]; i++) s->source[i + s->edges[3]].x = emf ? emf[i] : 0.0f;
 }
+/* source pass (src/em/source.wgsl:5-17): the applied potential of the
+   source elements at every edge midpoint, summed in batches of 32 elements
+   (one pass each in the reference) whose per-batch vector is added to the
+   running value.  Element = 12 floats (a, b, c as vec4): c.y < 0.5 a wire
+   segment a->b with core radius c.x and current c.z; c.y < 1.5 a surface
+   current element at a with moment b scaled by c.z and softening c.x;
+   otherwise a uniform field b scaled by c.z.  ash(x) = sign(x) log(|x| +
+   sqrt(x^2 + 1)); inverseSqrt(x) = 1/sqrtf(x). */
+static float ash(float x) {
+    float sg = x > 0.0f ? 1.0f : x < 0.0f ? -1.0f : 0.0f;
+    return sg * logf(fabsf(x) + sqrtf(x * x + 1.0f));
+}
+void oem_evaluate_sources(const OEm *s, const float *el, uint32_t count, float *out) {
+    uint32_t E = s->edges[3];
+#pragma omp parallel for schedule(static)
+    for (uint32_t i = 0; i < E; i++) {
+        int e[3], w;
+        edge_decode(s, i, e, &w);
+        float pe[3] = {(float)e[0], (float)e[1], (float)e[2]};
+        pe[w] += 0.5f;
+        float p[3];
+        for (int k = 0; k < 3; k++) p[k] = s->origin[k] + pe[k] * s->physical[2];
+        float acc = 0.0f;
+        uint32_t nb = count == 0 ? 1 : (count + 31) / 32;
+        for (uint32_t bi = 0; bi < nb; bi++) {
+            uint32_t begin = bi * 32, end = begin + 32 < count ? begin + 32 : count;
+            float a = 0.0f;
+            for (uint32_t j = begin; j < end; j++) {
+                const float *q = el + 12 * (size_t)j;
+                const float *A = q, *B = q + 4, *Cc = q + 8;
+                if (Cc[2] == 0.0f) continue;
+                float r[3] = {p[0] - A[0], p[1] - A[1], p[2] - A[2]};
+                if (Cc[1] < 0.5f) {
+                    float d[3] = {B[0] - A[0], B[1] - A[1], B[2] - A[2]};
+                    float len = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                    float u[3] = {d[0] / len, d[1] / len, d[2] / len};
+                    float t = r[0] * u[0] + r[1] * u[1] + r[2] * u[2];
+                    float pp[3] = {r[0] - u[0] * t, r[1] - u[1] * t, r[2] - u[2] * t};
+                    float radius = sqrtf(pp[0] * pp[0] + pp[1] * pp[1] + pp[2] * pp[2] + Cc[0] * Cc[0]);
+                    a += u[w] * (1e-7f * Cc[2] * (ash(t / radius) - ash((t - len) / radius)));
+                } else if (Cc[1] < 1.5f) {
+                    a += B[w] * (1e-7f * Cc[2] * (1.0f / sqrtf(r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + Cc[0] * Cc[0])));
+                } else {
+                    float cr[3] = {B[1] * p[2] - B[2] * p[1], B[2] * p[0] - B[0] * p[2], B[0] * p[1] - B[1] * p[0]};
+                    a += 0.5f * Cc[2] * cr[w];
+                }
+            }
+            acc = bi == 0 ? a : acc + a;
+        }
+        out[i] = acc;
+    }
+}
+
 /* motion (src/em/motion.wgsl:8-26): fluid cell records (16 floats: velocity
    0-2, mobile where float 12 > 0.5) and this state's last B. */
 void oem_set_motion(OEm *s, const float *fluid) {

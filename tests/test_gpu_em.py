@@ -301,3 +301,37 @@ def test_nodal_correction_bit_exact(gpu, n, after):
         d, st, _ = pair.step(t, applied=applied(t), label=f"nodal step {k}")
         assert st[7] == 1.0
     pair.close()
+
+
+def test_source_pass_against_oracle(gpu):
+    """mhdproj_em_evaluate_sources (source.wgsl) against the oracle: the
+    surface-current and uniform kinds use no logarithm and match bit for bit;
+    wire segments call CUDA's logf, so they are held to a relative L2 error of
+    1e-5 and a max error of 1e-5 of the largest value.  The GPU potential
+    then drives a bit-exact step on both sides."""
+    import mhdproj
+    from mhdproj import synth
+
+    n, h = 20, 0.5e-3
+    origin = (-0.5 * n * h,) * 3
+    pair = Pair(gpu, mhdproj, (n, n, n), h, _ring(n, inner=3.0, outer=6.0, z0=7, z1=13),
+                _props(SIGMA_316 * 40, 1.0), origin=origin)
+    pair.set_materials()
+    block = synth.em_magnet_block_elements(1.5e-3, 1.0e-3, 1.0e-3, 5e5, 5, smoothing=1e-4)
+    uni = synth.em_uniform_element((0.01, -0.02, 0.03), 0.5)
+    dead = synth.em_uniform_element((1.0, 1.0, 1.0), 0.0)
+    exact = np.concatenate([block, dead, uni, block[:7]])
+    _assert_bits(pair.gpu.evaluate_sources(exact).cpu().numpy(), pair.cpu.evaluate_sources(exact),
+                 "surface-current and uniform sources")
+    loop = synth.em_loop_elements(3.5e-3, 50.0, 45, centre=(0.0, 0.0, 1e-3), core=2e-4)
+    wires = np.concatenate([loop, exact[:40], loop[:13]])
+    g = pair.gpu.evaluate_sources(wires).cpu().numpy().astype(np.float64)
+    c = pair.cpu.evaluate_sources(wires).astype(np.float64)
+    assert np.linalg.norm(g - c) <= 1e-5 * np.linalg.norm(c)
+    assert np.abs(g - c).max() <= 1e-5 * np.abs(c).max()
+    empty = pair.gpu.evaluate_sources(np.zeros((0, 12), np.float32)).cpu().numpy()
+    assert not empty.any()
+    a = g.astype(np.float32)
+    pair.step(0.0, initial=True, applied=a * np.float32(0.0), label="initial")
+    pair.step(1e-5, applied=a, label="driven by the GPU source pass")
+    pair.close()

@@ -244,3 +244,70 @@ def test_nodal_correction_solves_the_same_system(n, after):
         out[sw] = s.reaction().astype(np.float64)
         s.close()
     assert np.linalg.norm(out[after] - out[1024]) <= 1e-4 * np.linalg.norm(out[1024])
+
+
+def _applied_b_at(s, elements, cell):
+    """Applied-field solve in vacuum: the cell's applied B (results lanes 12-14)."""
+    a = s.evaluate_sources(elements)
+    rc, _, _ = s.advance(0.0, initial=True, applied=a)
+    assert rc == s.OK
+    n = s.dims
+    return s.results().reshape(n[2], n[1], n[0], 16)[cell[2], cell[1], cell[0], 12:15].astype(np.float64), a
+
+
+def test_source_pass_wire_loop_centre_field():
+    """src/em/tests.rs:51-176 (loop field against the analytic value): the
+    centre field of an N-gon loop, mu0 I N tan(pi/N) / (2 pi R)."""
+    from mhdproj import synth
+
+    n, h = 33, 0.5e-3
+    origin = (-0.5 * n * h,) * 3
+    s = O.EmSolve((n, n, n), h, origin=origin, vacuum=True)
+    s.set_materials(np.zeros(n ** 3, np.uint32), _props())
+    R, current, segs = 4e-3, 100.0, 96
+    b, _ = _applied_b_at(s, synth.em_loop_elements(R, current, segs), (16, 16, 16))
+    want = MU0 * current * segs * math.tan(math.pi / segs) / (2 * math.pi * R)
+    assert abs(b[2] - want) < 0.01 * want, (b, want)
+    assert abs(b[0]) < 1e-3 * want and abs(b[1]) < 1e-3 * want
+    s.close()
+
+
+def test_source_pass_magnet_block_axis_field():
+    """src/em/tests.rs:201-238 (magnetised CAD prism against the analytic axis
+    field): B_z above a block magnetised along z."""
+    from mhdproj import synth
+
+    n, h = 33, 0.5e-3
+    origin = (-0.5 * n * h,) * 3
+    s = O.EmSolve((n, n, n), h, origin=origin, vacuum=True)
+    s.set_materials(np.zeros(n ** 3, np.uint32), _props())
+    ax, ay, az, M = 3e-3, 2e-3, 2e-3, 8e5
+    el = synth.em_magnet_block_elements(ax, ay, az, M, 12)
+    k = 16 + 10                    # cell centre at z = 5 mm, 3 mm above the top face
+    b, _ = _applied_b_at(s, el, (16, 16, k))
+    z = origin[2] + (k + 0.5) * h
+    f = lambda d: math.atan(ax * ay / (d * math.sqrt(ax * ax + ay * ay + d * d)))
+    want = MU0 * M / math.pi * (f(z - az) - f(z + az))
+    assert abs(b[2] - want) < 0.01 * abs(want), (b, want)
+    s.close()
+
+
+def test_source_pass_uniform_element_and_batches():
+    """The uniform kind reproduces B x r / 2; zero-amplitude elements add
+    nothing; 70 elements sum in three passes of up to 32."""
+    from mhdproj import synth
+
+    n, h = 8, 1e-3
+    origin = (-4e-3,) * 3
+    s = O.EmSolve((n, n, n), h, origin=origin)
+    bvec = (np.float32(0.003), np.float32(-0.004), np.float32(0.005))
+    a = s.evaluate_sources(synth.em_uniform_element(bvec))
+    np.testing.assert_allclose(a, _uniform_applied(s, h, origin, bvec), rtol=1e-6, atol=1e-12)
+    assert not s.evaluate_sources(np.zeros((0, 12), np.float32)).any()
+    dead = synth.em_uniform_element(bvec, 0.0)
+    np.testing.assert_array_equal(s.evaluate_sources(np.concatenate([dead] * 5)), 0.0)
+    loop = synth.em_loop_elements(2e-3, 10.0, 70)
+    whole = s.evaluate_sources(loop).astype(np.float64)
+    parts = sum(s.evaluate_sources(loop[i:i + 32]).astype(np.float64) for i in range(0, 70, 32))
+    np.testing.assert_allclose(whole, parts, rtol=1e-5, atol=1e-12)
+    s.close()
