@@ -373,8 +373,8 @@ uint32_t mhdproj_anchors(uint32_t *mask, const uint32_t dims[3], uint32_t period
  * reference's source pass, src/em/source.wgsl); so is the motional EMF
  * (src/em/motion.wgsl, or mhdproj_em_set_motion from the fluid's cell
  * records).  The nodal gradient correction (src/em/nodal.wgsl) takes
- * over after nodal_switch_after Jacobi iterations as in the reference.  Not
- * built: the per-body force integrals.
+ * over after nodal_switch_after Jacobi iterations as in the reference.
+ * mhdproj_em_body_forces gives the per-body integrals.
  * ------------------------------------------------------------------------- */
 typedef struct mhdproj_em_ctx mhdproj_em_ctx;
 
@@ -441,6 +441,11 @@ int mhdproj_em_set_materials(mhdproj_em_ctx *ctx, const uint32_t *materials, con
                              uint32_t count, float conductivity_range[2]);
 /* Motional EMF per edge (device, E floats; NULL clears it). */
 int mhdproj_em_set_motional_emf(mhdproj_em_ctx *ctx, const float *emf);
+/* Per-body force (N, xyz) and Joule power (W) of the last accepted step
+ * (body-stats.wgsl, src/em/mod.rs:1036-1069): body z holds the cells with
+ * bit z of masks[i] set (device, one u32 per cell; 1 <= bodies <= 32).
+ * totals: 4 floats per body, host memory. */
+int mhdproj_em_body_forces(mhdproj_em_ctx *ctx, const uint32_t *masks, uint32_t bodies, float *totals);
 /* The source pass (src/em/source.wgsl): the applied potential A_s at every
  * edge midpoint of `count` source elements as EmConfig::elements builds them
  * (src/em/sources.rs:280-338), 12 floats each (a, b, c as vec4; host

@@ -31,8 +31,9 @@
 // Jacobi iterations (src/em/nodal.wgsl), the motional EMF
 // (src/em/motion.wgsl) and the source pass that sums the applied potential
 // of wire, surface-current and uniform-field elements (src/em/source.wgsl).
-// Not built: building the elements from the model (src/em/sources.rs, host
-// code the caller keeps) and the per-body force integrals.
+// Also the per-body force integrals (src/em/body-stats.wgsl).  Not built:
+// building the elements from the model (src/em/sources.rs, host code the
+// caller keeps).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -879,6 +880,30 @@ __global__ void __launch_bounds__(kBlock) k_em_field_reduce(EmDev D) {
     }
 }
 
+// ------------------------------------------------------------ body integrals
+// body-stats.wgsl: per body z (blockIdx.z) the 256-cell group sums of
+// ((fq * h) * h) * h over the cells with bit z set, then one block per body
+// reduces its groups.
+__global__ void __launch_bounds__(kBlock) k_em_body_collect(EmDev D, const uint32_t* __restrict__ masks,
+                                                             float4* __restrict__ part) {
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    const uint32_t z = blockIdx.z;
+    float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (i < D.cells && (masks[i] & (1u << z))) {
+        const float4 q = D.results[4 * (size_t)i + 2];
+        const float h = D.h;
+        v = make_float4(q.x * h * h * h, q.y * h * h * h, q.z * h * h * h, q.w * h * h * h);
+    }
+    const float4 t = tree256<0>(v);
+    if (threadIdx.x == 0) part[(size_t)z * gridDim.x + blockIdx.x] = t;
+}
+__global__ void __launch_bounds__(kBlock) k_em_body_reduce(EmDev D, const float4* __restrict__ part,
+                                                            float4* __restrict__ totals) {
+    const uint32_t n = groups_of(D.cells);
+    const float4 t = final_reduce<0>(part + (size_t)blockIdx.z * n, n, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    if (threadIdx.x == 0) totals[blockIdx.z] = t;
+}
+
 // ------------------------------------------------------------ sources
 // The source pass (src/em/source.wgsl:5-17): the applied potential of the
 // source elements at every edge midpoint.  Elements arrive in tiles of 32 --
@@ -1035,6 +1060,9 @@ struct mhdproj_em_ctx {
     uint32_t props_cap = 0;
     float* d_elements = nullptr;
     uint32_t elements_cap = 0;
+    float4* d_body = nullptr;  // body partials and totals
+    uint32_t body_cap = 0;
+    float* h_body = nullptr;   // pinned totals
     cudaGraphExec_t batch = nullptr;  // kBatch CG iterations
     uint32_t batch_initial = 0;       // the step constants the batch graph was captured with
     uint32_t batch_nodal = 0;
@@ -1189,6 +1217,7 @@ void mhdproj_em_destroy(mhdproj_em_ctx* ctx) {
     for (void* p : ctx->allocs) cudaFree(p);
     if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
     if (ctx->h_err) cudaFreeHost(ctx->h_err);
+    if (ctx->h_body) cudaFreeHost(ctx->h_body);
     if (ctx->ev) cudaEventDestroy(ctx->ev);
     if (ctx->t0) cudaEventDestroy(ctx->t0);
     if (ctx->t1) cudaEventDestroy(ctx->t1);
@@ -1367,6 +1396,33 @@ int mhdproj_em_set_motional_emf(mhdproj_em_ctx* ctx, const float* emf) {
     if (emf) EK(cudaMemcpyAsync(ctx->D.emf, emf, (size_t)ctx->D.E * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     else EK(cudaMemsetAsync(ctx->D.emf, 0, (size_t)ctx->D.E * 4, ctx->stream));
     return em_wait(ctx);
+}
+
+// Per-body force and power of the last accepted step (body-stats.wgsl).
+int mhdproj_em_body_forces(mhdproj_em_ctx* ctx, const uint32_t* masks, uint32_t bodies, float* totals) {
+    if (!ctx || !masks || !totals || bodies == 0 || bodies > 32)
+        return em_fail(ctx, MHDPROJ_ERR_INVALID, "body masks hold 1..32 bodies");
+    const EmDev& D = ctx->D;
+    const uint32_t ng = em_groups(D.cells);
+    if (bodies > ctx->body_cap) {
+        float4* p = nullptr;
+        EK(em_alloc(ctx, &p, ((size_t)bodies * ng + bodies) * sizeof(float4)));
+        ctx->d_body = p;
+        if (ctx->h_body) cudaFreeHost(ctx->h_body);
+        ctx->h_body = nullptr;
+        EK(cudaMallocHost(&ctx->h_body, (size_t)bodies * 16));
+        ctx->body_cap = bodies;
+    }
+    float4* totals_d = ctx->d_body + (size_t)bodies * ng;
+    k_em_body_collect<<<dim3(ng, 1, bodies), kBlock, 0, ctx->stream>>>(D, masks, ctx->d_body);
+    k_em_body_reduce<<<dim3(1, 1, bodies), kBlock, 0, ctx->stream>>>(D, ctx->d_body, totals_d);
+    ctx->launches += 2;
+    EK(cudaGetLastError());
+    EK(cudaMemcpyAsync(ctx->h_body, totals_d, (size_t)bodies * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    int rc = em_wait(ctx);
+    if (rc) return rc;
+    memcpy(totals, ctx->h_body, (size_t)bodies * 16);
+    return 0;
 }
 
 // The source pass over host-side elements (12 floats each), into `applied`

@@ -172,6 +172,7 @@ def load():
     L.mhdproj_em_set_reaction.argtypes = [_vp, _vp]
     L.mhdproj_em_set_motion.argtypes = [_vp, _vp]
     L.mhdproj_em_evaluate_sources.argtypes = [_vp, _vp, C.c_uint32, _vp]
+    L.mhdproj_em_body_forces.argtypes = [_vp, _vp, C.c_uint32, _vp]
     L.mhdproj_em_advance.argtypes = [_vp, C.c_double, C.c_int, _vp, C.POINTER(EmDiagnostics)]
     L.mhdproj_em_copy.argtypes = [_vp, C.c_int, _vp]
     L.mhdproj_em_apply_operator.argtypes = [_vp, _vp, _vp, C.c_int]
@@ -189,7 +190,7 @@ EXPORTED = [
     "mhdproj_kernel_launches", "mhdproj_fields", "mhdproj_fluid_step", "mhdproj_export_fields",
     "mhdproj_classify_cells", "mhdproj_classify_last_error",
     "mhdproj_em_create", "mhdproj_em_destroy", "mhdproj_em_last_error", "mhdproj_em_set_stream", "mhdproj_em_sizes",
-    "mhdproj_em_set_materials", "mhdproj_em_set_motional_emf", "mhdproj_em_set_motion", "mhdproj_em_evaluate_sources", "mhdproj_em_set_reaction", "mhdproj_em_advance",
+    "mhdproj_em_set_materials", "mhdproj_em_set_motional_emf", "mhdproj_em_set_motion", "mhdproj_em_evaluate_sources", "mhdproj_em_body_forces", "mhdproj_em_set_reaction", "mhdproj_em_advance",
     "mhdproj_em_copy", "mhdproj_em_apply_operator", "mhdproj_em_kernel_launches",
 ]
 
@@ -615,6 +616,15 @@ class EmInduction:
         self._order()
         self._check(self._lib.mhdproj_em_evaluate_sources(self._ctx, _host_ptr(el) if el.size else None, el.shape[0],
                                                           _ptr(out)))
+        return out
+
+    def body_forces(self, masks, bodies):
+        """(bodies, 4) float32: force xyz (N) and Joule power (W) of the last
+        step for the cells with bit z of ``masks`` (int32 CUDA tensor)."""
+        out = np.zeros((bodies, 4), np.float32)
+        self._order()
+        self._check(self._lib.mhdproj_em_body_forces(self._ctx, _ptr(masks.contiguous()), int(bodies),
+                                                     _host_ptr(out)))
         return out
 
     def set_motion(self, fluid_cells):

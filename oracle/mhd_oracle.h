@@ -243,6 +243,9 @@ void oem_set_nodal_switch(OEm *s, uint32_t after);
 /* Applied potential of source elements (12 floats each) at the edges
  * (the source pass, source.wgsl); out: E floats. */
 void oem_evaluate_sources(const OEm *s, const float *elements, uint32_t count, float *out);
+/* Per-body force (N) and Joule power (W) from the last cell results; body z
+ * holds the cells with bit z of masks[i] (body-stats.wgsl). totals: 4/body. */
+void oem_body_forces(const OEm *s, const uint32_t *masks, uint32_t bodies, float *totals);
 /* Motional EMF from fluid cell records (set_velocity, motion.wgsl). */
 void oem_set_motion(OEm *s, const float *fluid_cells);
 /* Overwrite the accepted reaction potential (edges). */

@@ -162,6 +162,7 @@ def lib():
         L.oem_set_motion.argtypes = [C.c_void_p, _f32p]
         L.oem_set_nodal_switch.argtypes = [C.c_void_p, C.c_uint32]
         L.oem_evaluate_sources.argtypes = [C.c_void_p, _f32p, C.c_uint32, _f32p]
+        L.oem_body_forces.argtypes = [C.c_void_p, _u32p, C.c_uint32, _f32p]
         L.oem_get.argtypes = [C.c_void_p, C.c_int, _f32p]
         L.oem_apply_operator.argtypes = [C.c_void_p, _f32p, _f32p, C.c_int]
         L.oem_advance.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_void_p, _f32p, _f32p]
@@ -461,6 +462,11 @@ class EmSolve:
         out = np.zeros(self.edges, np.float32)
         lib().oem_evaluate_sources(self._p, el.reshape(-1) if el.size else np.zeros(12, np.float32), el.shape[0],
                                    out)
+        return out
+
+    def body_forces(self, masks, bodies):
+        out = np.zeros((bodies, 4), np.float32)
+        lib().oem_body_forces(self._p, np.ascontiguousarray(masks, np.uint32).reshape(-1), bodies, out.reshape(-1))
         return out
 
     def set_motion(self, fluid_cells):

@@ -36,8 +36,10 @@
  *
  *   src/em/source.wgsl:5-17      the applied potential of source elements
  *
+ *   src/em/body-stats.wgsl       per-body force and power integrals
+ *
  * Out of scope, as in the library: building the source elements from the
- * model (src/em/sources.rs) and the per-body force integrals.
+ * model (src/em/sources.rs).
  */
 #include <math.h>
 #include <stdint.h>
@@ -745,6 +747,36 @@ int oem_set_materials(OEm *s, const uint32_t *materials, const float *props, uin
 void oem_set_motional(OEm *s, const float *emf) {
     for (uint32_t i = 0; i < s->edges[3]; i++) s->source[i + s->edges[3]].x = emf ? emf[i] : 0.0f;
 }
+/* body integrals (src/em/body-stats.wgsl): for each body z (< 32) the force
+   and Joule power, sum over the cells with bit z of masks[i] of
+   ((fq * h) * h) * h, as 256-cell group trees and a 256-stride final pass. */
+void oem_body_forces(const OEm *s, const uint32_t *masks, uint32_t bodies, float *totals) {
+    uint32_t n = s->dims[3], ng = groups_of(n);
+    float h = s->physical[2];
+    f4 *part = (f4 *)calloc((size_t)ng + 1, sizeof(f4));
+    for (uint32_t z = 0; z < bodies; z++) {
+        for (uint32_t g = 0; g < ng; g++) {
+            f4 lane[256];
+            for (uint32_t l = 0; l < 256; l++) {
+                uint32_t i = g * 256 + l;
+                f4 v = F4(0, 0, 0, 0);
+                if (i < n && (masks[i] & (1u << z))) {
+                    f4 q = s->results[4 * (size_t)i + 2];
+                    v = F4(q.x * h * h * h, q.y * h * h * h, q.z * h * h * h, q.w * h * h * h);
+                }
+                lane[l] = v;
+            }
+            part[g] = tree(lane, RED_SUM);
+        }
+        f4 t = final_reduce(part, ng, 1, F4(0, 0, 0, 0), RED_SUM);
+        totals[4 * z + 0] = t.x;
+        totals[4 * z + 1] = t.y;
+        totals[4 * z + 2] = t.z;
+        totals[4 * z + 3] = t.w;
+    }
+    free(part);
+}
+
 /* source pass (src/em/source.wgsl:5-17): the applied potential of the
    source elements at every edge midpoint, summed in batches of 32 elements
    (one pass each in the reference) whose per-batch vector is added to the

@@ -335,3 +335,20 @@ def test_source_pass_against_oracle(gpu):
     pair.step(0.0, initial=True, applied=a * np.float32(0.0), label="initial")
     pair.step(1e-5, applied=a, label="driven by the GPU source pass")
     pair.close()
+
+
+def test_body_forces_bit_exact(gpu):
+    """mhdproj_em_body_forces (body-stats.wgsl) for three overlapping bodies."""
+    import mhdproj
+
+    pair, applied = _driven_pair(gpu, mhdproj, 32)
+    pair.set_materials()
+    pair.step(0.0, initial=True, applied=applied(0.0), label="initial")
+    pair.step(1e-5, applied=applied(1e-5), label="step")
+    rng = np.random.default_rng(17)
+    masks = rng.integers(0, 8, pair.cpu.cells).astype(np.uint32)
+    got = pair.gpu.body_forces(gpu.from_numpy(masks.view(np.int32)).cuda(), 3)
+    _assert_bits(got, pair.cpu.body_forces(masks, 3), "body force and power")
+    with pytest.raises(mhdproj.ProjectionError):
+        pair.gpu.body_forces(gpu.from_numpy(masks.view(np.int32)).cuda(), 33)
+    pair.close()

@@ -311,3 +311,21 @@ def test_source_pass_uniform_element_and_batches():
     parts = sum(s.evaluate_sources(loop[i:i + 32]).astype(np.float64) for i in range(0, 70, 32))
     np.testing.assert_allclose(whole, parts, rtol=1e-5, atol=1e-12)
     s.close()
+
+
+def test_body_forces_partition_the_totals():
+    """body-stats.wgsl: bodies that partition the grid sum to the step's
+    total force and Joule power (field statistics 4-7)."""
+    s, applied = _driven()
+    assert s.advance(0.0, initial=True, applied=applied(0.0))[0] == s.OK
+    rc, _, stats = s.advance(1e-5, applied=applied(1e-5))
+    assert rc == s.OK
+    n = s.dims[0]
+    x = np.arange(s.cells) % n
+    masks = np.where(x < n // 2, 1, 2).astype(np.uint32)
+    masks[::7] |= 4                       # a third body overlapping the others
+    tot = s.body_forces(masks, 3).astype(np.float64)
+    both = tot[0] + tot[1]
+    np.testing.assert_allclose(both, stats[4:8].astype(np.float64), rtol=1e-5, atol=1e-6 * np.abs(stats[4:8]).max())
+    assert tot[1, 3] > 0 and tot[0, 3] > 0     # heat in both halves of the ring
+    s.close()
