@@ -441,6 +441,12 @@ int mhdproj_em_set_materials(mhdproj_em_ctx *ctx, const uint32_t *materials, con
                              uint32_t count, float conductivity_range[2]);
 /* Motional EMF per edge (device, E floats; NULL clears it). */
 int mhdproj_em_set_motional_emf(mhdproj_em_ctx *ctx, const float *emf);
+/* The energy ledger of the last committed step (EmState::energy_step,
+ * src/em/mod.rs:1106-1133, energy.wgsl), joules: out = (magnetic, change of
+ * magnetic, backward-Euler loss, Joule heat, mechanical work, external work,
+ * balance error = external - the other four).  At time 0 only the magnetic
+ * energy is reported. */
+int mhdproj_em_energy(mhdproj_em_ctx *ctx, double out[7]);
 /* Per-body force (N, xyz) and Joule power (W) of the last accepted step
  * (body-stats.wgsl, src/em/mod.rs:1036-1069): body z holds the cells with
  * bit z of masks[i] set (device, one u32 per cell; 1 <= bodies <= 32).

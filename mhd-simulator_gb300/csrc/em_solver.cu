@@ -31,7 +31,8 @@
 // Jacobi iterations (src/em/nodal.wgsl), the motional EMF
 // (src/em/motion.wgsl) and the source pass that sums the applied potential
 // of wire, surface-current and uniform-field elements (src/em/source.wgsl).
-// Also the per-body force integrals (src/em/body-stats.wgsl).  Not built:
+// Also the per-body force integrals (src/em/body-stats.wgsl) and the energy
+// ledger (src/em/energy.wgsl).  Not built:
 // building the elements from the model (src/em/sources.rs, host code the
 // caller keeps).
 #include <cuda_runtime.h>
@@ -880,6 +881,112 @@ __global__ void __launch_bounds__(kBlock) k_em_field_reduce(EmDev D) {
     }
 }
 
+// ------------------------------------------------------------ energy ledger
+// energy.wgsl after a committed step.  kind 0: new total potential
+// (reaction + applied), 1: the previous total, 3: its increment, 2: applied.
+template <int KIND>
+__device__ __forceinline__ float en_a(const EmDev& D, int axis, const int p[3]) {
+    uint32_t d[3];
+    edge_dims(D, axis, d);
+    if (!valid3(p, d)) return 0.0f;
+    const uint32_t i = edge_offset(D, axis) + (uint32_t)p[0] + d[0] * ((uint32_t)p[1] + d[1] * (uint32_t)p[2]);
+    if (KIND == 0) return D.x[i] + D.as[i];
+    if (KIND == 1) return D.prev[i] + D.asp[i];
+    if (KIND == 3) return (D.x[i] - D.prev[i]) + (D.as[i] - D.asp[i]);
+    return D.as[i];
+}
+template <int KIND>
+__device__ __forceinline__ float en_curl(const EmDev& D, int axis, const int p[3]) {
+    uint32_t fi;
+    if (!face_valid(D, axis, p, &fi)) return 0.0f;
+    const int a = (axis + 1) % 3, b = (axis + 2) % 3;
+    int qa[3] = {p[0], p[1], p[2]}, qb[3] = {p[0], p[1], p[2]};
+    qa[a] += 1;
+    qb[b] += 1;
+    return en_a<KIND>(D, b, qa) - en_a<KIND>(D, b, p) - en_a<KIND>(D, a, qb) + en_a<KIND>(D, a, p);
+}
+template <int KIND, bool WEIGHTED>
+__device__ __forceinline__ float en_face(const EmDev& D, int axis, const int p[3]) {
+    uint32_t fi;
+    if (!face_valid(D, axis, p, &fi)) return 0.0f;
+    return en_curl<KIND>(D, axis, p) * (WEIGHTED ? D.nu[axis][fi] : 1.0f);
+}
+template <int KIND, bool WEIGHTED>
+__device__ __forceinline__ float en_adjoint(const EmDev& D, const int p[3], int w) {
+    const int a = (w + 1) % 3, b = (w + 2) % 3;
+    int qa[3] = {p[0], p[1], p[2]}, qb[3] = {p[0], p[1], p[2]};
+    qa[a] -= 1;
+    qb[b] -= 1;
+    return en_face<KIND, WEIGHTED>(D, b, p) - en_face<KIND, WEIGHTED>(D, b, qa) -
+           en_face<KIND, WEIGHTED>(D, a, p) + en_face<KIND, WEIGHTED>(D, a, qb);
+}
+__global__ void __launch_bounds__(kBlock) k_em_energy_collect(EmDev D, float4* __restrict__ part) {
+    __shared__ float4 ra[kBlock], rb[kBlock];
+    const uint32_t i = blockIdx.x * kBlock + threadIdx.x;
+    const float h = D.h, dt = D.dt, mu0 = D.mu0, volume = h * h * h;
+    float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = a;
+    if (i < D.E) {
+        int p[3], w;
+        edge_decode(D, i, p, &w);
+        const float delta = (D.x[i] - D.prev[i]) + (D.as[i] - D.asp[i]);
+        const float motion = D.emf[i];
+        const float ee = -delta / dt + motion;
+        const float j = D.sig[i] * ee;
+        a.w = dt * volume * j * ee;
+        b.x = -dt * volume * j * motion;
+        float drive = on_boundary(D, p, w) ? en_adjoint<0, true>(D, p, w) : en_adjoint<2, false>(D, p, w);
+        b.y = h / mu0 * delta * drive;
+    }
+    const uint32_t fx = (D.n[0] + 1) * D.n[1] * D.n[2], fy = D.n[0] * (D.n[1] + 1) * D.n[2],
+                   fz = D.n[0] * D.n[1] * (D.n[2] + 1);
+    if (i < fx + fy + fz) {
+        int axis = 0;
+        uint32_t q = i;
+        if (q >= fx) {
+            q -= fx;
+            axis = 1;
+            if (q >= fy) {
+                q -= fy;
+                axis = 2;
+            }
+        }
+        uint32_t d[3] = {D.n[0], D.n[1], D.n[2]};
+        d[axis] += 1;
+        const int p[3] = {(int)(q % d[0]), (int)((q / d[0]) % d[1]), (int)(q / (d[0] * d[1]))};
+        const float now = en_curl<0>(D, axis, p), old = en_curl<1>(D, axis, p), dl = en_curl<3>(D, axis, p);
+        const float scale = h / (2.0f * mu0) * D.nu[axis][q];
+        a.x = scale * now * now;
+        a.y = scale * dl * (now + old);
+        a.z = scale * dl * dl;
+    }
+    const int l = threadIdx.x;
+    ra[l] = a;
+    rb[l] = b;
+    __syncthreads();
+    for (int st = kBlock / 2; st > 0; st >>= 1) {
+        if (l < st) {
+            ra[l] = add4(ra[l], ra[l + st]);
+            rb[l] = add4(rb[l], rb[l + st]);
+        }
+        __syncthreads();
+    }
+    if (l == 0) {
+        part[blockIdx.x] = ra[0];
+        part[gridDim.x + blockIdx.x] = rb[0];
+    }
+}
+__global__ void __launch_bounds__(kBlock) k_em_energy_reduce(EmDev D, const float4* __restrict__ part,
+                                                              float4* __restrict__ out) {
+    const uint32_t n = groups_of(D.E);
+    const float4 a = final_reduce<0>(part, n, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    __syncthreads();
+    const float4 b = final_reduce<0>(part + n, n, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    if (threadIdx.x == 0) {
+        out[0] = a;
+        out[1] = b;
+    }
+}
+
 // ------------------------------------------------------------ body integrals
 // body-stats.wgsl: per body z (blockIdx.z) the 256-cell group sums of
 // ((fq * h) * h) * h over the cells with bit z set, then one block per body
@@ -1060,6 +1167,7 @@ struct mhdproj_em_ctx {
     uint32_t props_cap = 0;
     float* d_elements = nullptr;
     uint32_t elements_cap = 0;
+    float4* d_energy = nullptr;  // energy partials and result
     float4* d_body = nullptr;  // body partials and totals
     uint32_t body_cap = 0;
     float* h_body = nullptr;   // pinned totals
@@ -1396,6 +1504,39 @@ int mhdproj_em_set_motional_emf(mhdproj_em_ctx* ctx, const float* emf) {
     if (emf) EK(cudaMemcpyAsync(ctx->D.emf, emf, (size_t)ctx->D.E * 4, cudaMemcpyDeviceToDevice, ctx->stream));
     else EK(cudaMemsetAsync(ctx->D.emf, 0, (size_t)ctx->D.E * 4, ctx->stream));
     return em_wait(ctx);
+}
+
+// EmState::energy_step (src/em/mod.rs:1106-1133): the energy ledger of the
+// last committed step.
+int mhdproj_em_energy(mhdproj_em_ctx* ctx, double out[7]) {
+    if (!ctx || !out) return MHDPROJ_ERR_INVALID;
+    if (!ctx->materials) return em_fail(ctx, MHDPROJ_ERR_STATE, "set the EM materials first");
+    const EmDev& D = ctx->D;
+    const uint32_t ng = em_groups(D.E);
+    if (!ctx->d_energy) {
+        float4* p = nullptr;
+        EK(em_alloc(ctx, &p, (2 * (size_t)ng + 2) * sizeof(float4)));
+        ctx->d_energy = p;
+    }
+    float4* res = ctx->d_energy + 2 * (size_t)ng;
+    k_em_energy_collect<<<ng, kBlock, 0, ctx->stream>>>(D, ctx->d_energy);
+    k_em_energy_reduce<<<1, kBlock, 0, ctx->stream>>>(D, ctx->d_energy, res);
+    ctx->launches += 2;
+    EK(cudaGetLastError());
+    EK(cudaMemcpyAsync(ctx->h_sc + 6, res, 2 * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+    int rc = em_wait(ctx);
+    if (rc) return rc;
+    const float* v = &ctx->h_sc[6].x;
+    for (int k = 0; k < 8; k++)
+        if (!std::isfinite(v[k])) return em_fail(ctx, MHDPROJ_ERR_NONFINITE, "Nonfinite EM energy integral");
+    for (int k = 0; k < 6; k++) out[k] = v[k];
+    out[6] = 0.0;
+    if (ctx->time_s == 0.0) {
+        for (int k = 1; k < 7; k++) out[k] = 0.0;
+        return 0;
+    }
+    out[6] = out[5] - out[1] - out[2] - out[3] - out[4];
+    return 0;
 }
 
 // Per-body force and power of the last accepted step (body-stats.wgsl).

@@ -173,6 +173,7 @@ def load():
     L.mhdproj_em_set_motion.argtypes = [_vp, _vp]
     L.mhdproj_em_evaluate_sources.argtypes = [_vp, _vp, C.c_uint32, _vp]
     L.mhdproj_em_body_forces.argtypes = [_vp, _vp, C.c_uint32, _vp]
+    L.mhdproj_em_energy.argtypes = [_vp, _vp]
     L.mhdproj_em_advance.argtypes = [_vp, C.c_double, C.c_int, _vp, C.POINTER(EmDiagnostics)]
     L.mhdproj_em_copy.argtypes = [_vp, C.c_int, _vp]
     L.mhdproj_em_apply_operator.argtypes = [_vp, _vp, _vp, C.c_int]
@@ -190,7 +191,7 @@ EXPORTED = [
     "mhdproj_kernel_launches", "mhdproj_fields", "mhdproj_fluid_step", "mhdproj_export_fields",
     "mhdproj_classify_cells", "mhdproj_classify_last_error",
     "mhdproj_em_create", "mhdproj_em_destroy", "mhdproj_em_last_error", "mhdproj_em_set_stream", "mhdproj_em_sizes",
-    "mhdproj_em_set_materials", "mhdproj_em_set_motional_emf", "mhdproj_em_set_motion", "mhdproj_em_evaluate_sources", "mhdproj_em_body_forces", "mhdproj_em_set_reaction", "mhdproj_em_advance",
+    "mhdproj_em_set_materials", "mhdproj_em_set_motional_emf", "mhdproj_em_set_motion", "mhdproj_em_evaluate_sources", "mhdproj_em_body_forces", "mhdproj_em_energy", "mhdproj_em_set_reaction", "mhdproj_em_advance",
     "mhdproj_em_copy", "mhdproj_em_apply_operator", "mhdproj_em_kernel_launches",
 ]
 
@@ -617,6 +618,16 @@ class EmInduction:
         self._check(self._lib.mhdproj_em_evaluate_sources(self._ctx, _host_ptr(el) if el.size else None, el.shape[0],
                                                           _ptr(out)))
         return out
+
+    ENERGY_KEYS = ("magnetic_j", "delta_magnetic_j", "backward_euler_j", "joule_j", "mechanical_j", "external_j",
+                   "balance_error_j")
+
+    def energy(self):
+        """EmState::energy_step: the energy ledger of the last step (J)."""
+        out = np.zeros(7, np.float64)
+        self._order()
+        self._check(self._lib.mhdproj_em_energy(self._ctx, _host_ptr(out)))
+        return dict(zip(self.ENERGY_KEYS, out.tolist()))
 
     def body_forces(self, masks, bodies):
         """(bodies, 4) float32: force xyz (N) and Joule power (W) of the last

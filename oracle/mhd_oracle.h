@@ -243,6 +243,10 @@ void oem_set_nodal_switch(OEm *s, uint32_t after);
 /* Applied potential of source elements (12 floats each) at the edges
  * (the source pass, source.wgsl); out: E floats. */
 void oem_evaluate_sources(const OEm *s, const float *elements, uint32_t count, float *out);
+/* Energy ledger of the last committed step (energy.wgsl): magnetic, delta
+ * magnetic, backward-Euler loss, Joule, mechanical, external, balance (J).
+ * Returns -1 for a non-finite integral. */
+int oem_energy(OEm *s, double out[7]);
 /* Per-body force (N) and Joule power (W) from the last cell results; body z
  * holds the cells with bit z of masks[i] (body-stats.wgsl). totals: 4/body. */
 void oem_body_forces(const OEm *s, const uint32_t *masks, uint32_t bodies, float *totals);

@@ -163,6 +163,8 @@ def lib():
         L.oem_set_nodal_switch.argtypes = [C.c_void_p, C.c_uint32]
         L.oem_evaluate_sources.argtypes = [C.c_void_p, _f32p, C.c_uint32, _f32p]
         L.oem_body_forces.argtypes = [C.c_void_p, _u32p, C.c_uint32, _f32p]
+        L.oem_energy.argtypes = [C.c_void_p, _f64p]
+        L.oem_energy.restype = C.c_int
         L.oem_get.argtypes = [C.c_void_p, C.c_int, _f32p]
         L.oem_apply_operator.argtypes = [C.c_void_p, _f32p, _f32p, C.c_int]
         L.oem_advance.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_void_p, _f32p, _f32p]
@@ -463,6 +465,15 @@ class EmSolve:
         lib().oem_evaluate_sources(self._p, el.reshape(-1) if el.size else np.zeros(12, np.float32), el.shape[0],
                                    out)
         return out
+
+    ENERGY_KEYS = ("magnetic_j", "delta_magnetic_j", "backward_euler_j", "joule_j", "mechanical_j", "external_j",
+                   "balance_error_j")
+
+    def energy(self):
+        out = np.zeros(7, np.float64)
+        if lib().oem_energy(self._p, out) != 0:
+            raise ValueError("Nonfinite EM energy integral")
+        return dict(zip(self.ENERGY_KEYS, out.tolist()))
 
     def body_forces(self, masks, bodies):
         out = np.zeros((bodies, 4), np.float32)

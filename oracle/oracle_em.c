@@ -37,6 +37,7 @@
  *   src/em/source.wgsl:5-17      the applied potential of source elements
  *
  *   src/em/body-stats.wgsl       per-body force and power integrals
+ *   src/em/energy.wgsl           the energy ledger of a committed step
  *
  * Out of scope, as in the library: building the source elements from the
  * model (src/em/sources.rs).
@@ -747,6 +748,118 @@ int oem_set_materials(OEm *s, const uint32_t *materials, const float *props, uin
 void oem_set_motional(OEm *s, const float *emf) {
     for (uint32_t i = 0; i < s->edges[3]; i++) s->source[i + s->edges[3]].x = emf ? emf[i] : 0.0f;
 }
+/* energy ledger (src/em/energy.wgsl, EmState::energy_step mod.rs:1106-1133),
+   after a step is committed.  kind 0: new total potential (reaction +
+   applied), 1: previous total, 3: its increment, 2: applied potential. */
+static float en_a(const OEm *s, int axis, const int p[3], int kind) {
+    uint32_t d[3];
+    edge_dims(s, axis, d);
+    if (!valid3(p, d)) return 0.0f;
+    uint32_t i = edge_index(s, axis, p);
+    if (kind == 0) return s->work[i].x + s->source[i].x;
+    if (kind == 1) return s->previous[i] + s->source[i].y;
+    if (kind == 3) return (s->work[i].x - s->previous[i]) + (s->source[i].x - s->source[i].y);
+    return s->source[i].x;
+}
+static float en_curl(const OEm *s, int axis, const int p[3], int kind) {
+    uint32_t d[3];
+    face_dims(s, axis, d);
+    if (!valid3(p, d)) return 0.0f;
+    int a = (axis + 1) % 3, b = (axis + 2) % 3;
+    int qa[3] = {p[0], p[1], p[2]}, qb[3] = {p[0], p[1], p[2]};
+    qa[a] += 1;
+    qb[b] += 1;
+    return en_a(s, b, qa, kind) - en_a(s, b, p, kind) - en_a(s, a, qb, kind) + en_a(s, a, p, kind);
+}
+static float en_face(OEm *s, int axis, const int p[3], int kind, int weighted) {
+    uint32_t d[3];
+    face_dims(s, axis, d);
+    if (!valid3(p, d)) return 0.0f;
+    return en_curl(s, axis, p, kind) * (weighted ? nu_face(s, axis, p) : 1.0f);
+}
+static float en_adjoint(OEm *s, const int p[3], int w, int kind, int weighted) {
+    int a = (w + 1) % 3, b = (w + 2) % 3;
+    int qa[3] = {p[0], p[1], p[2]}, qb[3] = {p[0], p[1], p[2]};
+    qa[a] -= 1;
+    qb[b] -= 1;
+    return en_face(s, b, p, kind, weighted) - en_face(s, b, qa, kind, weighted) - en_face(s, a, p, kind, weighted) +
+           en_face(s, a, qb, kind, weighted);
+}
+static void energy_item(OEm *s, uint32_t i, f4 *A, f4 *B) {
+    float h = s->physical[2], dt = s->physical[0], mu0 = s->physical[1], volume = h * h * h;
+    uint32_t E = s->edges[3];
+    f4 a = F4(0, 0, 0, 0), b = F4(0, 0, 0, 0);
+    if (i < E) {
+        int p[3], w;
+        edge_decode(s, i, p, &w);
+        float delta = (s->work[i].x - s->previous[i]) + (s->source[i].x - s->source[i].y);
+        float motion = s->source[i + E].x;
+        float ee = -delta / dt + motion;
+        float j = s->source[i].z * ee;
+        a.w = dt * volume * j * ee;
+        b.x = -dt * volume * j * motion;
+        float drive = en_adjoint(s, p, w, 2, 0);
+        if (boundary(s, p, w)) drive = en_adjoint(s, p, w, 0, 1);
+        b.y = h / mu0 * delta * drive;
+    }
+    uint32_t nx = s->dims[0], ny = s->dims[1], nz = s->dims[2];
+    uint32_t fx = (nx + 1) * ny * nz, fy = nx * (ny + 1) * nz, fz = nx * ny * (nz + 1);
+    if (i < fx + fy + fz) {
+        int axis = 0;
+        uint32_t q = i;
+        if (q >= fx) {
+            q -= fx;
+            axis = 1;
+            if (q >= fy) {
+                q -= fy;
+                axis = 2;
+            }
+        }
+        uint32_t d[3];
+        face_dims(s, axis, d);
+        int p[3] = {(int)(q % d[0]), (int)((q / d[0]) % d[1]), (int)(q / (d[0] * d[1]))};
+        float now = en_curl(s, axis, p, 0), old = en_curl(s, axis, p, 1), dl = en_curl(s, axis, p, 3);
+        float scale = h / (2.0f * mu0) * nu_face(s, axis, p);
+        a.x = scale * now * now;
+        a.y = scale * dl * (now + old);
+        a.z = scale * dl * dl;
+    }
+    *A = a;
+    *B = b;
+}
+/* out: magnetic, delta magnetic, backward-Euler loss, Joule, mechanical,
+   external work, balance error (J); returns -1 for a non-finite integral. */
+int oem_energy(OEm *s, double out[7]) {
+    uint32_t n = s->edges[3], ng = groups_of(n);
+    f4 *pa = (f4 *)calloc(2 * (size_t)ng + 2, sizeof(f4));
+#pragma omp parallel for schedule(static)
+    for (uint32_t g = 0; g < ng; g++) {
+        f4 la[256], lb[256];
+        for (uint32_t l = 0; l < 256; l++) energy_item(s, g * 256 + l, &la[l], &lb[l]);
+        for (int st = 128; st > 0; st /= 2)
+            for (int l = 0; l < st; l++) {
+                la[l] = add4(la[l], la[l + st]);
+                lb[l] = add4(lb[l], lb[l + st]);
+            }
+        pa[g] = la[0];
+        pa[ng + g] = lb[0];
+    }
+    f4 A = final_reduce(pa, ng, 1, F4(0, 0, 0, 0), RED_SUM);
+    f4 B = final_reduce(pa + ng, ng, 1, F4(0, 0, 0, 0), RED_SUM);
+    free(pa);
+    float v[8] = {A.x, A.y, A.z, A.w, B.x, B.y, B.z, B.w};
+    for (int k = 0; k < 8; k++)
+        if (!isfinite(v[k])) return -1;
+    for (int k = 0; k < 6; k++) out[k] = v[k];
+    out[6] = 0.0;
+    if (s->time_s == 0.0) {
+        for (int k = 1; k < 7; k++) out[k] = 0.0;
+        return 0;
+    }
+    out[6] = out[5] - out[1] - out[2] - out[3] - out[4];
+    return 0;
+}
+
 /* body integrals (src/em/body-stats.wgsl): for each body z (< 32) the force
    and Joule power, sum over the cells with bit z of masks[i] of
    ((fq * h) * h) * h, as 256-cell group trees and a 256-stride final pass. */

@@ -352,3 +352,27 @@ def test_body_forces_bit_exact(gpu):
     with pytest.raises(mhdproj.ProjectionError):
         pair.gpu.body_forces(gpu.from_numpy(masks.view(np.int32)).cuda(), 33)
     pair.close()
+
+
+def test_energy_ledger_bit_exact(gpu):
+    """mhdproj_em_energy (energy.wgsl) equals the oracle's ledger bit for bit
+    after each driven step, and the ledger closes (src/em/tests.rs:633-663)."""
+    import mhdproj
+
+    n, h = 20, 0.8e-3
+    origin = (-8e-3,) * 3
+    pair = Pair(gpu, mhdproj, (n, n, n), h, _ring(n, inner=3.0, outer=7.0, z0=7, z1=13), _props(), origin=origin)
+    pair.set_materials()
+    b = (np.float32(0.0), np.float32(0.0), np.float32(0.01))
+    applied = lambda t: _uniform_applied(pair.cpu, h, origin, b, scale=math.sin(2 * math.pi * 1e3 * t))
+    pair.step(0.0, initial=True, applied=applied(0.0), label="initial")
+    assert pair.gpu.energy() == pair.cpu.energy()
+    t = 0.0
+    for k in range(3):
+        t += 1e-5
+        pair.step(t, applied=applied(t), label=f"step {k}")
+        g, c = pair.gpu.energy(), pair.cpu.energy()
+        assert g == c, (g, c)
+        scale = abs(g["external_j"]) + abs(g["delta_magnetic_j"]) + g["joule_j"] + g["backward_euler_j"]
+        assert abs(g["balance_error_j"]) / scale < 1e-4
+    pair.close()

@@ -329,3 +329,30 @@ def test_body_forces_partition_the_totals():
     np.testing.assert_allclose(both, stats[4:8].astype(np.float64), rtol=1e-5, atol=1e-6 * np.abs(stats[4:8]).max())
     assert tot[1, 3] > 0 and tot[0, 3] > 0     # heat in both halves of the ring
     s.close()
+
+
+def test_driven_energy_balance():
+    """src/em/tests.rs:633-663: under a sinusoidal uniform drive the ledger
+    closes -- external work = change of magnetic energy + backward-Euler
+    loss + Joule heat + mechanical work, to 1e-4 of its scale -- and the
+    Joule term equals the step's power x dt to 1e-5."""
+    n, h = 20, 0.8e-3
+    origin = (-8e-3,) * 3
+    s = O.EmSolve((n, n, n), h, origin=origin)
+    s.set_materials(_ring(n, inner=3.0, outer=7.0, z0=7, z1=13), _props())
+    b = (np.float32(0.0), np.float32(0.0), np.float32(0.01))
+    applied = lambda t: _uniform_applied(s, h, origin, b, scale=math.sin(2 * math.pi * 1e3 * t))
+    assert s.advance(0.0, initial=True, applied=applied(0.0))[0] == s.OK
+    e0 = s.energy()
+    assert e0["delta_magnetic_j"] == 0.0 and e0["balance_error_j"] == 0.0   # time 0: magnetic energy only
+    t = 0.0
+    for _ in range(5):
+        t += 1e-5
+        rc, _, stats = s.advance(t, applied=applied(t))
+        assert rc == s.OK
+        e = s.energy()
+        scale = abs(e["external_j"]) + abs(e["delta_magnetic_j"]) + e["joule_j"] + e["backward_euler_j"]
+        assert e["joule_j"] > 0 and e["external_j"] > 0 and e["backward_euler_j"] > 0, e
+        assert abs(e["balance_error_j"]) / scale < 1e-4, e
+        assert abs(e["joule_j"] / (float(stats[7]) * 1e-5) - 1.0) < 1e-5, (e, stats[7])
+    s.close()
