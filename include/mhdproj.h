@@ -44,8 +44,7 @@ typedef enum {
     MHDPROJ_ERR_NO_PROGRESS = 5,    /* "Fluid pressure iteration made no progress" */
     MHDPROJ_ERR_STATE = 6,          /* call order (e.g. project before set_coefficients) */
     MHDPROJ_ERR_OUT_OF_MEMORY = 7,  /* workspace does not fit */
-    MHDPROJ_ERR_TIMEOUT = 8,        /* a bounded host wait on the device expired */
-    MHDPROJ_ERR_UNSUPPORTED = 9     /* a reference branch this library does not build */
+    MHDPROJ_ERR_TIMEOUT = 8         /* a bounded host wait on the device expired */
 } mhdproj_status;
 
 typedef enum {

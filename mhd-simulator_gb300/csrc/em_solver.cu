@@ -150,46 +150,6 @@ __device__ __forceinline__ float curl_face(const EmDev& D, int axis, const int p
     qb[b] += 1;
     return a_edge<KIND>(D, b, qa) - a_edge<KIND>(D, b, p) - a_edge<KIND>(D, a, qb) + a_edge<KIND>(D, a, p);
 }
-template <int KIND, bool CONTRAST>
-__device__ __forceinline__ float face_term(const EmDev& D, int axis, const int p[3]) {
-    uint32_t fi;
-    if (!face_valid(D, axis, p, &fi)) return 0.0f;
-    float nu = D.nu[axis][fi];
-    if (CONTRAST) nu = 1.0f - nu;
-    return nu * curl_face<KIND>(D, axis, p);
-}
-// Inlined like every helper here: no device function receives the address of
-// the kernel's parameter block.
-template <int KIND, bool CONTRAST>
-__device__ __forceinline__ float adjoint(const EmDev& D, const int p[3], int w) {
-    const int a = (w + 1) % 3, b = (w + 2) % 3;
-    int qa[3] = {p[0], p[1], p[2]}, qb[3] = {p[0], p[1], p[2]};
-    qa[a] -= 1;
-    qb[b] -= 1;
-    return face_term<KIND, CONTRAST>(D, b, p) - face_term<KIND, CONTRAST>(D, b, qa) -
-           face_term<KIND, CONTRAST>(D, a, p) + face_term<KIND, CONTRAST>(D, a, qb);
-}
-template <int KIND>
-__device__ __forceinline__ float node_div(const EmDev& D, const int p[3]) {
-    float value = 0.0f;
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        int q[3] = {p[0], p[1], p[2]};
-        q[a] -= 1;
-        value += a_edge<KIND>(D, a, p) - a_edge<KIND>(D, a, q);
-    }
-    return value;
-}
-template <int KIND>
-__device__ __forceinline__ float gauge(const EmDev& D, uint32_t i, const int p[3], int w) {
-    const uint8_t f = D.flags[i];
-    int upper[3] = {p[0], p[1], p[2]};
-    upper[w] += 1;
-    float value = 0.0f;
-    if (f & 1) value += node_div<KIND>(D, p);
-    if (f & 2) value -= node_div<KIND>(D, upper);
-    return value;
-}
 __device__ __forceinline__ float mass(const EmDev& D, uint32_t i) {
     if (D.initial) return 0.0f;
     return D.mu0 * D.sig[i] * D.h * D.h / D.dt;
@@ -201,11 +161,13 @@ __device__ __forceinline__ float residual_scale(const EmDev& D) {
 }
 __device__ __forceinline__ bool active(const EmDev& D) { return D.scalars[1].w == 0.0f; }
 
-// ---- the same operator with the edge axis fixed at compile time ----
-// adjoint_s/gauge_s repeat adjoint()/gauge() term for term and in the same
-// order; with the axis a template parameter every neighbour offset is a
-// constant, positions stay in registers (the runtime-axis form keeps small
-// position arrays in local memory) and each array is read directly.
+// ---- the curl-curl + gauge operator, edge axis fixed at compile time ----
+// adjoint_s is the shader's adjoint (induction.wgsl:57-63: the transposed
+// curl of nu-weighted face curls) and gauge_s its gauge (:75-80: nodal
+// divergences at gauged end nodes), term for term in the shader's order.
+// With the axis a template parameter every neighbour offset is a constant
+// and positions stay in registers (a runtime axis keeps small position
+// arrays in local memory); each kind of potential is read from its array.
 template <int K>
 __device__ __forceinline__ void bump(int& x, int& y, int& z, int s) {
     if (K == 0) x += s;

@@ -36,7 +36,6 @@ STATUS = {
     6: "call order",
     7: "out of memory",
     8: "timeout",
-    9: "unsupported",
 }
 
 
