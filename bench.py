@@ -574,8 +574,8 @@ def run_ours(args):
             pref.close()
         except mhdproj.ProjectionError as exc:
             line["reference_algorithm_gpu"] = {"unavailable": str(exc)}
-        # BASELINE configs 4 (128^3 adjoint chain, K = 8, checkpoints every 4)
-        # and 5 (512x256x256 column, K = 4): forward, gradient, projection
+        # the 128^3 adjoint chain (K = 8 steps, checkpoints every 4) and the
+        # 512x256x256 liquid column (K = 4): forward, gradient, projection
         # throughput and device memory
         line["adjoint128_chain"] = chain_leg("adjoint128", 1.0, 8, 4, 3)
         line["column512"] = chain_leg("column512", 1.0, 4, 4, 3)

@@ -9,7 +9,7 @@
  * :1447-1493) and the pressure written by `fields` (p = rho_l * phi / dt,
  * src/fluid/solver.wgsl:269-270).  The reference's method is private Rust on
  * wgpu buffers; this header is the FFI boundary a Rust crate would bind
- * instead (see INTEGRATION.md).
+ * instead.
  *
  * Conventions
  *  - Cells are indexed x-fastest: i = x + nx*(y + ny*z) (src/simulation.rs:319-323).
