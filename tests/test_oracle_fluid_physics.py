@@ -10,7 +10,9 @@ viscosity 1 Pa s (src/fluid/tests.rs:8-57).
   - plane Poiseuille flow at 8 and 16 cells across converges to
     u(y) = g y (H - y) / (2 nu) with errors 2.130% and 0.526% -- the
     values the reference publishes (docs/FLUIDS.md:54), reproduced here to
-    the printed digits -- and a second-order rate (src/fluid/tests.rs:118-160).
+    the printed digits -- and a second-order rate (src/fluid/tests.rs:118-160);
+  - a periodic sinusoidal shear decays by the exact discrete viscous factor
+    in velocity and kinetic energy (src/fluid/tests.rs:280-322).
 """
 import math
 
@@ -89,3 +91,29 @@ def test_poiseuille_channel_matches_published_errors(oracle_lib):
         errors.append(rel)
         assert round(100.0 * rel, 3) == pytest.approx(100.0 * published, abs=1e-9), rel
     assert errors[1] < 0.015 and errors[1] < 0.45 * errors[0]
+
+
+def test_viscous_shear_matches_discrete_decay(oracle_lib):
+    """src/fluid/tests.rs:280-322: a periodic sinusoidal shear u_x(y) on the
+    16-cell channel decays over 20 steps by the exact discrete factor
+    (1 - 4 nu dt / h^2 sin^2(pi/16))^20: the probe value within 2e-5 and
+    the kinetic energy ratio within 2e-5 of the factor squared."""
+    n, dt = 16, 3e-5
+    dims, prm, comps, mask = _channel(oracle_lib, n, dt, 7)
+    y = np.arange(n, dtype=np.float32)
+    prof = np.sin(np.float32(2 * np.pi) * (y + np.float32(0.5)) / np.float32(16.0)).astype(np.float32)
+    u = np.broadcast_to(prof[None, :, None], (4, n, 5)).astype(np.float32).copy()
+    vel = R.soa_to_records(dims, u, np.zeros((4, n + 1, 4), np.float32), np.zeros((5, n, 4), np.float32))
+    cells = prm.dims[3]
+    occ = np.ones(cells, np.float32)
+    zero3 = np.zeros(3, np.float32)
+    ke = lambda v: float(oracle_lib.fields(prm, mask, occ, np.zeros((cells, 4), np.float32), v, zero3)[1][3])
+    e0 = ke(vel)
+    vel, _, _ = _steps(oracle_lib, prm, comps, mask, vel, (0.0, 0.0, 0.0), 20)
+    h = float(np.float32(0.008 / n))
+    factor = (1.0 - 4.0 * 1e-3 * dt / h ** 2 * math.sin(math.pi / 16) ** 2) ** 20
+    got = R.records_to_soa(dims, vel)[0]
+    expected = math.sin(2 * math.pi * 5.5 / 16) * factor
+    cell = 0.5 * (float(got[1, 5, 1]) + float(got[1, 5, 2]))
+    assert abs(cell - expected) < 2e-5, (cell, expected)
+    assert abs(ke(vel) / e0 - factor * factor) < 2e-5
