@@ -12,7 +12,10 @@ viscosity 1 Pa s (src/fluid/tests.rs:8-57).
     values the reference publishes (docs/FLUIDS.md:54), reproduced here to
     the printed digits -- and a second-order rate (src/fluid/tests.rs:118-160);
   - a periodic sinusoidal shear decays by the exact discrete viscous factor
-    in velocity and kinetic energy (src/fluid/tests.rs:280-322).
+    in velocity and kinetic energy (src/fluid/tests.rs:280-322);
+  - a stratified thermal phase, classified by the `phase` pass, stays at
+    hydrostatic rest under the phase-drag weighted projection with the
+    expected fluid mass, for Jacobi and multigrid (src/fluid/tests.rs:336-391).
 """
 import math
 
@@ -117,3 +120,50 @@ def test_viscous_shear_matches_discrete_decay(oracle_lib):
     cell = 0.5 * (float(got[1, 5, 1]) + float(got[1, 5, 2]))
     assert abs(cell - expected) < 2e-5, (cell, expected)
     assert abs(ke(vel) / e0 - factor * factor) < 2e-5
+
+
+@pytest.mark.parametrize("multigrid", [0, 1])
+def test_thermal_phase_topology_and_weighted_projection_preserve_rest(oracle_lib, multigrid):
+    """src/fluid/tests.rs:336-391: a stratified thermal phase (solid below
+    y = 4, liquid fraction rising 0.25 -> 1 above) classified by the `phase`
+    pass halves the fluid cells; five gravity steps with the phase-drag
+    weighted projection keep the fluid at rest (speed < 5e-6 m/s, RMS
+    divergence < 5e-5 /s) with the fluid mass equal to sum(fraction) rho h^3;
+    a fully solid phase then leaves no fluid cells."""
+    n = 8
+    dims = (4, n, 4)
+    cells = 16 * n
+    y = (np.arange(cells) // 4) % n
+    frac = np.where(y < 4, 0.0, 0.25 + 0.75 * (y - 4) / np.float32(3.0)).astype(np.float32)
+    materials = np.full(cells, 3, np.uint32)
+    mask01 = np.ones(cells, np.uint32)
+    rec = np.zeros((cells, 16), np.float32)
+    flags = oracle_lib.classify_cells(materials, 3, mask01, rec, thermal=frac)
+    assert flags & 1 and int(mask01.sum()) == cells // 2
+    comps, mask = oracle_lib.anchors(mask01, dims, 5)
+    h = float(np.float32(0.001))
+    prm = oracle_lib.make_params(dims, h, 1e-4, 1000.0, 1000.0, False, 5, 1e-5, 1e-5, int(mask01.sum()), True, 1e6)
+    prm.physical[2] = 1e-3
+    prm.flags[1] = 1
+    occ = np.ones(cells, np.float32)
+    phase = rec[:, 13].copy()
+    vel = np.zeros((prm.faces[3], 4), np.float32)
+    old = np.zeros(cells, np.float32)
+    g = np.array([0.0, -9.81, 0.0], np.float32)
+    for _ in range(5):
+        pred = oracle_lib.predict(prm, mask, vel)
+        visc = oracle_lib.viscous(prm, mask, occ, pred, g, phase=phase)
+        res, vel, work, _ = oracle_lib.ref_project(prm, mask, comps, occ, visc, warm_start=True, old_pressure=old,
+                                                   phase=phase, force_mg=multigrid)
+        assert res.status == 0
+        old = work[:, 0].copy()
+    _, sc = oracle_lib.fields(prm, mask, occ, work, vel, g, reserved=rec[:, 12:16].copy(), cells=False)
+    fluid = int(mask01.sum())
+    assert sc[0] < 5e-6
+    assert math.sqrt(sc[2] / fluid) < 5e-5
+    mass = 1000.0 * float(sc[9]) * h ** 3
+    expected = float(frac.sum(dtype=np.float32)) * 1000.0 * h ** 3
+    assert abs(mass / expected - 1.0) < 1e-5
+    # the whole grid solidifies: no fluid cells remain
+    flags = oracle_lib.classify_cells(materials, 3, mask01, rec, thermal=np.zeros(cells, np.float32))
+    assert flags & 1 and int(mask01.sum()) == 0
