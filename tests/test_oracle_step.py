@@ -3,7 +3,10 @@ fields/diagnostics of src/fluid/solver.wgsl:127-163, :256-291) against
 analytic answers: no advection copies the open faces, a uniform periodic
 flow is advected onto itself, a fluid at rest gains dt * g on every open face,
 a uniform flow's diagnostics are its speed, zero divergence and its kinetic
-energy, and solid walls close their faces."""
+energy, and solid walls close their faces; the moving-interface stress
+diffusion keeps uniform and linear shear flows, builds the capillary force of
+a planar interface, and its damped RKC2 stages converge to the exact shear
+decay as the step is refined (src/fluid/viscosity_tests.rs:516-597)."""
 import numpy as np
 
 import refcases as R
@@ -194,3 +197,41 @@ def test_stress_diffusion_keeps_linear_shear_flow(oracle_lib):
     uo = R.records_to_soa(dims, out)[0]
     np.testing.assert_allclose(uo[:, 1:ny - 1, :], u[:, 1:ny - 1, :], rtol=1e-5, atol=1e-9)
     assert np.all(np.abs(uo[:, 0, :]) < np.abs(u[:, 0, :]))  # the walls slow the outer rows
+
+
+def test_stabilized_stress_diffusion_matches_shear_decay_and_time_refines(oracle_lib):
+    """src/fluid/viscosity_tests.rs:516-597: a periodic shear u_x = cos(2 pi
+    (y + 1/2)/n) in a 32 x 32 x 4 box of a liquid with nu = 1 m^2/s, diffused
+    by the damped RKC2 stages over 0.016 s in 1, 2, 4 and 8 ticks: the error
+    to exp(-lambda t) falls by more than 1/0.3 per refinement and ends below
+    1%, and no v or w appears."""
+    import math
+
+    n = 32
+    dims = (n, n, 4)
+    cells = n * n * 4
+    h = float(np.float32(1.0 / n))
+    lam = 4.0 * n * n * math.sin(math.pi / n) ** 2
+    exact = math.exp(-lam * 0.016)
+    mask = np.ones(cells, np.uint32)
+    occ = np.ones(cells, np.float32)
+    u = np.cos(2 * np.pi * (np.arange(n)[None, :, None] + 0.5) / n).astype(np.float32) * np.ones((4, 1, n + 1),
+                                                                                                np.float32)
+    init = R.soa_to_records(dims, u.astype(np.float32), np.zeros((4, n + 1, n), np.float32),
+                            np.zeros((5, n, n), np.float32))
+    errors = []
+    for ticks in (1, 2, 4, 8):
+        dt = 0.016 / ticks
+        p = oracle_lib.make_params(dims, h, dt, 1.0, 1.2, True, 7, 1e-5, 1e-5, cells, False, 1e6)
+        p.physical[2] = 1.0
+        field = init.copy()
+        for _ in range(ticks):
+            st, sub, _, field = oracle_lib.diffuse_surface_stress(p, mask, occ, field, field, 1.8e-5, dt)
+            assert st == 0 and sub > 1
+        gu, gv, gw = R.records_to_soa(dims, field)
+        ref = u.astype(np.float64)
+        err = math.sqrt(((gu[:, :, :n] - exact * ref[:, :, :n]) ** 2).sum() / (ref[:, :, :n] ** 2).sum())
+        assert np.abs(gv).max() < 1e-6 and np.abs(gw).max() < 1e-6
+        errors.append(err)
+    assert all(b < 0.3 * a for a, b in zip(errors, errors[1:])), errors
+    assert errors[-1] < 0.01
