@@ -286,3 +286,43 @@ def test_stabilized_variable_density_stress_dissipates_and_conserves_momentum(or
     assert after[0] < before[0]
     for a in range(3):
         assert abs(after[1][a] - before[1][a]) / before[2] < 2e-6, a
+
+
+def test_ambient_viscosity_matches_discrete_shear_decay_with_subcycling(oracle_lib):
+    """src/fluid/viscosity_tests.rs:249-338: a periodic shear in pure air
+    (1 kg/m^3, 0.1 Pa s) over 20 steps of 0.01 s of the moving-interface
+    step (stress diffusion by Euler substeps, viscous with zero surface
+    tension, projection) decays by prod (1 - lambda dt / k)^k over the
+    substep counts k, to 2e-5."""
+    import math
+
+    n = 16
+    dims = (n, n, n)
+    cells = n ** 3
+    h = float(np.float32(1.0 / n))
+    dt = 0.01
+    mask = np.ones(cells, np.uint32)
+    comps, mask_enc = oracle_lib.anchors(mask, dims, 7)
+    occ = np.zeros(cells, np.float32)
+    p = oracle_lib.make_params(dims, h, dt, 8400.0, 1.0, True, 7, 1e-5, 1e-5, cells, False, 1e6)
+    p.physical[2] = 0.0
+    prof = (np.float32(0.1) * np.sin(np.float32(2 * np.pi) * (np.arange(n, dtype=np.float32) + np.float32(0.5))
+                                       / np.float32(n))).astype(np.float32)
+    u0 = (prof[None, :, None] * np.ones((n, 1, n + 1), np.float32)).astype(np.float32)
+    vel = R.soa_to_records(dims, u0, np.zeros((n, n + 1, n), np.float32), np.zeros((n + 1, n, n), np.float32))
+    zero3 = np.zeros(3, np.float32)
+    old = np.zeros(cells, np.float32)
+    decay = 1.0
+    lam = 4.0 * 0.1 * math.sin(math.pi / n) ** 2 / h ** 2
+    for _ in range(20):
+        pred = oracle_lib.predict(p, mask_enc, vel)
+        st, k, _, pred = oracle_lib.diffuse_surface_stress(p, mask_enc, occ, pred, vel, 0.1, dt)
+        assert st == 0 and k > 1
+        visc = oracle_lib.viscous_surface(p, mask_enc, occ, pred, zero3, sigma=0.0)
+        res, vel, work, _ = oracle_lib.ref_project(p, mask_enc, comps, occ, visc, warm_start=True, old_pressure=old)
+        assert res.status == 0
+        old = work[:, 0].copy()
+        decay *= (1.0 - lam * dt / k) ** k
+    got = R.records_to_soa(dims, vel)[0][:, :, :n].astype(np.float64)
+    want = u0[:, :, :n].astype(np.float64) * decay
+    assert math.sqrt(((got - want) ** 2).sum() / (want ** 2).sum()) < 2e-5
