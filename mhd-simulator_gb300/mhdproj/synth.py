@@ -296,3 +296,26 @@ def em_uniform_element(b, scale=1.0):
     e[0, 9] = 2.0
     e[0, 10] = scale
     return e
+
+
+def em_sphere_materials(cells, h, origin, radius, material=2, sub=4):
+    """Material ids of a sphere of `radius` centred at the origin on a cells^3
+    grid whose low corner is at `origin` (all axes): cells fully inside carry
+    `material`; cut cells carry the partial-cell encoding (bit 31, fraction
+    in bits 8..30 from sub^3 point samples, material in bits 0..7)."""
+    g = (np.arange(sub) + 0.5) / sub
+    c = np.arange(cells)
+    z, y, x = np.meshgrid(c, c, c, indexing="ij")
+    frac = np.zeros((cells,) * 3)
+    for a in g:
+        for b in g:
+            for d in g:
+                px, py, pz = origin + (x + a) * h, origin + (y + b) * h, origin + (z + d) * h
+                frac += (px * px + py * py + pz * pz) <= radius * radius
+    frac /= sub ** 3
+    m = np.zeros(frac.shape, np.uint32)
+    m[frac >= 1.0] = material
+    cut = (frac > 0.0) & (frac < 1.0)
+    q = np.round(frac[cut] * 8388607).astype(np.uint32)
+    m[cut] = np.uint32(0x80000000) | (q << np.uint32(8)) | np.uint32(material)
+    return m.reshape(-1)
