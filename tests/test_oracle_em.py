@@ -404,3 +404,24 @@ def test_rotating_sphere_torque_and_motional_energy_balance():
         assert abs(torque * omega / power + 1.0) < 3e-3
         s.close()
     assert errors[1] < 0.025 and errors[1] < errors[0], errors
+
+
+def test_permeability_contrast_matches_sphere_polarization():
+    """src/em/tests.rs:239-270: a linear magnetic sphere (mu_r = 2, R = 3 mm,
+    non-conducting) in a uniform 1 mT field: the initial solve's B at the
+    centre is 3 mu_r / (mu_r + 2) B0 within 7%, and no current flows."""
+    from mhdproj import synth
+
+    h, cells, origin = 0.5e-3, 40, -10e-3
+    s = O.EmSolve((cells,) * 3, h, max_iterations=3000, origin=(origin,) * 3)
+    props = np.zeros((7, 2), np.float32)
+    props[:, 1] = 1.0
+    props[6] = (0.0, 2.0)
+    s.set_materials(synth.em_sphere_materials(cells, h, origin, 3e-3, material=6), props)
+    rc, st, stats = s.advance(0.0, initial=True, applied=s.evaluate_sources(synth.em_uniform_element((0, 0, 1e-3))))
+    assert rc == s.OK
+    b = s.results().reshape(cells, cells, cells, 16)[20, 20, 20, :3]
+    expected = 1e-3 * 3 * 2 / (2 + 2)
+    assert abs(b[2] / expected - 1.0) < 0.07, b
+    assert stats[1] == 0.0
+    s.close()
