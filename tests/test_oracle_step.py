@@ -326,3 +326,41 @@ def test_ambient_viscosity_matches_discrete_shear_decay_with_subcycling(oracle_l
     got = R.records_to_soa(dims, vel)[0][:, :, :n].astype(np.float64)
     want = u0[:, :, :n].astype(np.float64) * decay
     assert math.sqrt(((got - want) ** 2).sum() / (want ** 2).sum()) < 2e-5
+
+
+def test_closed_wall_stress_is_symmetric_and_dissipative(oracle_lib):
+    """src/fluid/viscosity_tests.rs:121-248: one stress-diffusion pass of a
+    variable-viscosity two-phase fluid (liquid 1 Pa s, air 0.1 Pa s, equal
+    densities, liquid fraction 0.25..0.75) in a closed 8^3 box, with and
+    without an internal voxel block and step: the viscous power <u, L u> is
+    negative, the kinetic energy falls, and <u1, L u2> = <u2, L u1> to 2e-5."""
+    n = 8
+    dims = (n, n, n)
+    cells = n ** 3
+    i = np.arange(cells)
+    occ = (0.25 + 0.5 * np.sin(i.astype(np.float32) * np.float32(0.37)) ** 2).astype(np.float32)
+    x, y, z = i % n, (i // n) % n, i // (n * n)
+    dt = 1e-4
+    p = oracle_lib.make_params(dims, float(np.float32(1.0 / n)), dt, 1.0, 1.0, True, 0, 1e-5, 1e-5, cells, False, 1e6)
+    p.physical[2] = 1.0
+    nf = p.faces[3]
+    for internal in (False, True):
+        blocked = (((3 <= x) & (x <= 5) & (3 <= y) & (y <= 5) & (3 <= z) & (z <= 5)) | ((x >= 5) & (y >= 1) & (z >= 4)))
+        m01 = (~blocked if internal else np.ones(cells, bool)).astype(np.uint32)
+        _, mask = oracle_lib.anchors(m01, dims, 0)
+        fields = []
+        for seed in (7.0, 19.0):
+            k = np.arange(nf, dtype=np.float32) + np.float32(seed)
+            raw = np.stack([np.sin(k * np.float32(0.391)), np.cos(k * np.float32(0.717)),
+                            np.sin(k * np.float32(0.923)), np.zeros(nf, np.float32)], 1).astype(np.float32)
+            u = oracle_lib.predict(p, mask, raw)            # closes the faces that are not open
+            st, sub, _, out = oracle_lib.diffuse_surface_stress(p, mask, occ, u, u, 0.1, dt)
+            assert st == 0 and sub == 1
+            u64 = u[:, :3].astype(np.float64)
+            lu = (out[:, :3].astype(np.float64) - u64) / dt
+            assert (u64 * lu).sum() < 0.0
+            assert (out[:, :3].astype(np.float64) ** 2).sum() < (u64 ** 2).sum()
+            fields.append((u64, lu))
+        xy = (fields[0][0] * fields[1][1]).sum()
+        yx = (fields[1][0] * fields[0][1]).sum()
+        assert abs(xy - yx) / max(abs(xy), abs(yx)) < 2e-5, (internal, xy, yx)
