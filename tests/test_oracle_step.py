@@ -364,3 +364,53 @@ def test_closed_wall_stress_is_symmetric_and_dissipative(oracle_lib):
         xy = (fields[0][0] * fields[1][1]).sum()
         yx = (fields[1][0] * fields[0][1]).sum()
         assert abs(xy - yx) / max(abs(xy), abs(yx)) < 2e-5, (internal, xy, yx)
+
+
+def test_manufactured_variable_viscosity_symmetric_stress_refines(oracle_lib):
+    """src/fluid/viscosity_tests.rs:7-120: the symmetric stress of a
+    viscosity mu = 0.5 + 0.25 cos(2 pi x) (the liquid fraction mixes 1 Pa s
+    with inviscid air) applied once to a periodic manufactured field
+    u = (2 sin(kx) cos(2ky), -cos(kx) sin(2ky)): the discrete (u' - u)/dt
+    approaches div(mu (grad u + grad u^T)) with an L2 error below 2% at
+    n = 32 and a refinement ratio below 0.3."""
+    import math
+
+    errors = []
+    for n in (16, 32):
+        nz = 4
+        dims = (n, n, nz)
+        cells = n * n * nz
+        h = float(np.float32(1.0 / n))
+        dt = float(np.float32(0.01) * np.float32(h) * np.float32(h))
+        i = np.arange(cells)
+        occ = (0.5 + 0.25 * np.cos(2 * np.pi * ((i % n) + 0.5) / n)).astype(np.float32)
+        p = oracle_lib.make_params(dims, h, dt, 1.0, 1.0, True, 7, 1e-5, 1e-5, cells, False, 1e6)
+        p.physical[2] = 1.0
+        f0, f1 = n + 1, n + 1
+        nf = p.faces[3]
+        q = np.arange(nf)
+        x, y = (q % f0).astype(np.float64), ((q // f0) % f1).astype(np.float64)
+        k = 2 * np.pi / n
+        raw = np.zeros((nf, 4), np.float32)
+        raw[:, 0] = 2 * np.sin(k * x) * np.cos(2 * k * (y + 0.5))
+        raw[:, 1] = -np.cos(k * (x + 0.5)) * np.sin(2 * k * y)
+        _, mask = oracle_lib.anchors(np.ones(cells, np.uint32), dims, 7)
+        u = oracle_lib.predict(p, mask, raw)
+        st, sub, _, out = oracle_lib.diffuse_surface_stress(p, mask, occ, u, u, 0.0, dt)
+        assert st == 0 and sub == 1
+        err = norm = 0.0
+        K = 2 * np.pi
+        z3, y3, x3 = np.meshgrid(np.arange(nz), np.arange(n), np.arange(n), indexing="ij")
+        idx = (x3 + f0 * (y3 + f1 * z3)).reshape(-1)
+        for axis in (0, 1):
+            xx = (x3.reshape(-1) + (0.0 if axis == 0 else 0.5)) / n
+            yy = (y3.reshape(-1) + (0.0 if axis == 1 else 0.5)) / n
+            sx, cx, sy, cy = np.sin(K * xx), np.cos(K * xx), np.sin(2 * K * yy), np.cos(2 * K * yy)
+            mu, mux = 0.5 + 0.25 * cx, -0.25 * K * sx
+            exact = (-10 * mu * K * K * sx * cy + 4 * K * mux * cx * cy) if axis == 0 else \
+                (5 * mu * K * K * cx * sy - 3 * K * mux * sx * sy)
+            actual = (out[idx, axis].astype(np.float64) - u[idx, axis].astype(np.float64)) / dt
+            err += ((actual - exact) ** 2).sum()
+            norm += (exact ** 2).sum()
+        errors.append(math.sqrt(err / norm))
+    assert errors[1] < 0.02 and errors[1] < 0.3 * errors[0], errors
