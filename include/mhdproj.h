@@ -424,6 +424,10 @@ typedef enum {
 } mhdproj_em_array;
 
 int mhdproj_em_create(const mhdproj_em_config *config, mhdproj_em_ctx **out);
+/* Takes dt_s, relative_tolerance, max_iterations and nodal_switch_after from
+ * `config` for the following steps (the EmConfig fields the reference lets a
+ * caller change); the grid, origin and mode stay as created. */
+int mhdproj_em_update_config(mhdproj_em_ctx *ctx, const mhdproj_em_config *config);
 void mhdproj_em_destroy(mhdproj_em_ctx *ctx);
 const char *mhdproj_em_last_error(const mhdproj_em_ctx *ctx);
 int mhdproj_em_set_stream(mhdproj_em_ctx *ctx, void *stream);

@@ -1390,6 +1390,22 @@ int mhdproj_em_create(const mhdproj_em_config* cfg, mhdproj_em_ctx** out) {
     return 0;
 }
 
+// The EmConfig fields a caller may change between steps (dt_s,
+// relative_tolerance, max_iterations) and the nodal switch point; the grid,
+// origin and mode are fixed at creation.
+int mhdproj_em_update_config(mhdproj_em_ctx* ctx, const mhdproj_em_config* cfg) {
+    if (!ctx || !cfg) return MHDPROJ_ERR_INVALID;
+    if (!(cfg->dt_s > 0.0) || !std::isfinite(cfg->dt_s))
+        return em_fail(ctx, MHDPROJ_ERR_INVALID, "EM time step must be positive and finite");
+    if (!(cfg->relative_tolerance > 0.0f) || cfg->max_iterations == 0)
+        return em_fail(ctx, MHDPROJ_ERR_INVALID, "EM tolerance and iteration cap must be positive");
+    ctx->cfg.dt_s = cfg->dt_s;
+    ctx->cfg.relative_tolerance = cfg->relative_tolerance;
+    ctx->cfg.max_iterations = cfg->max_iterations;
+    ctx->cfg.nodal_switch_after = cfg->nodal_switch_after;
+    return 0;
+}
+
 int mhdproj_em_set_stream(mhdproj_em_ctx* ctx, void* stream) {
     if (!ctx) return MHDPROJ_ERR_INVALID;
     EK(cudaStreamSynchronize(ctx->stream));

@@ -162,6 +162,7 @@ def load():
     L.mhdproj_classify_last_error.restype = C.c_char_p
     L.mhdproj_em_create.argtypes = [C.POINTER(EmConfig), C.POINTER(_vp)]
     L.mhdproj_em_destroy.argtypes = [_vp]
+    L.mhdproj_em_update_config.argtypes = [_vp, C.POINTER(EmConfig)]
     L.mhdproj_em_last_error.argtypes = [_vp]
     L.mhdproj_em_last_error.restype = C.c_char_p
     L.mhdproj_em_set_stream.argtypes = [_vp, _vp]
@@ -189,7 +190,7 @@ EXPORTED = [
     "mhdproj_hierarchy", "mhdproj_anchors", "mhdproj_profile_kernels", "mhdproj_divergence_noalloc",
     "mhdproj_kernel_launches", "mhdproj_fields", "mhdproj_fluid_step", "mhdproj_export_fields",
     "mhdproj_classify_cells", "mhdproj_classify_last_error",
-    "mhdproj_em_create", "mhdproj_em_destroy", "mhdproj_em_last_error", "mhdproj_em_set_stream", "mhdproj_em_sizes",
+    "mhdproj_em_create", "mhdproj_em_update_config", "mhdproj_em_destroy", "mhdproj_em_last_error", "mhdproj_em_set_stream", "mhdproj_em_sizes",
     "mhdproj_em_set_materials", "mhdproj_em_set_motional_emf", "mhdproj_em_set_motion", "mhdproj_em_evaluate_sources", "mhdproj_em_body_forces", "mhdproj_em_energy", "mhdproj_em_set_reaction", "mhdproj_em_advance",
     "mhdproj_em_copy", "mhdproj_em_apply_operator", "mhdproj_em_kernel_launches",
 ]
@@ -575,6 +576,20 @@ class EmInduction:
     def _check(self, rc):
         if rc:
             raise ProjectionError(rc, self._lib.mhdproj_em_last_error(self._ctx).decode())
+
+    def update_config(self, dt_s=None, relative_tolerance=None, max_iterations=None, nodal_switch_after=None):
+        """Changes the EmConfig fields the reference lets a caller change."""
+        c = self.config
+        if dt_s is not None:
+            c.dt_s = float(dt_s)
+        if relative_tolerance is not None:
+            c.relative_tolerance = float(relative_tolerance)
+        if max_iterations is not None:
+            c.max_iterations = int(max_iterations)
+        if nodal_switch_after is not None:
+            c.nodal_switch_after = int(nodal_switch_after)
+        self._check(self._lib.mhdproj_em_update_config(self._ctx, C.byref(c)))
+        self.dt_s = float(c.dt_s)
 
     def close(self):
         if getattr(self, "_ctx", None):

@@ -240,6 +240,15 @@ void oem_set_motional(OEm *s, const float *emf);
 /* Iterations before the solve switches to the nodal correction (1024 in the
  * reference; 0 = from the first pass, the reference's test setting). */
 void oem_set_nodal_switch(OEm *s, uint32_t after);
+/* The mutable EmConfig fields (dt_s, relative_tolerance, max_iterations). */
+void oem_update_config(OEm *s, double dt_s, float rel_tol, uint32_t max_it);
+/* The reference's test switch predict_increments, its prediction_diagnostic
+ * (factor, initial relative residual, fallback flag) and (time, last dt). */
+void oem_set_predict(OEm *s, int on);
+/* Overwrite the previous accepted potential (the tests' poisoned history). */
+void oem_set_previous(OEm *s, const float *a);
+void oem_prediction(const OEm *s, float out[3]);
+void oem_time(const OEm *s, double out[2]);
 /* Applied potential of source elements (12 floats each) at the edges
  * (the source pass, source.wgsl); out: E floats. */
 void oem_evaluate_sources(const OEm *s, const float *elements, uint32_t count, float *out);

@@ -161,6 +161,11 @@ def lib():
         L.oem_set_reaction.argtypes = [C.c_void_p, _f32p]
         L.oem_set_motion.argtypes = [C.c_void_p, _f32p]
         L.oem_set_nodal_switch.argtypes = [C.c_void_p, C.c_uint32]
+        L.oem_update_config.argtypes = [C.c_void_p, C.c_double, C.c_float, C.c_uint32]
+        L.oem_set_predict.argtypes = [C.c_void_p, C.c_int]
+        L.oem_set_previous.argtypes = [C.c_void_p, _f32p]
+        L.oem_prediction.argtypes = [C.c_void_p, _f32p]
+        L.oem_time.argtypes = [C.c_void_p, _f64p]
         L.oem_evaluate_sources.argtypes = [C.c_void_p, _f32p, C.c_uint32, _f32p]
         L.oem_body_forces.argtypes = [C.c_void_p, _u32p, C.c_uint32, _f32p]
         L.oem_energy.argtypes = [C.c_void_p, _f64p]
@@ -458,6 +463,25 @@ class EmSolve:
 
     def set_reaction(self, a):
         lib().oem_set_reaction(self._p, np.ascontiguousarray(a, np.float32))
+
+    def update_config(self, dt, rel_tol, max_iterations):
+        lib().oem_update_config(self._p, float(dt), float(rel_tol), int(max_iterations))
+
+    def set_previous(self, a):
+        lib().oem_set_previous(self._p, np.ascontiguousarray(a, np.float32))
+
+    def set_predict(self, on):
+        lib().oem_set_predict(self._p, int(bool(on)))
+
+    def prediction(self):
+        out = np.zeros(3, np.float32)
+        lib().oem_prediction(self._p, out)
+        return out
+
+    def time(self):
+        out = np.zeros(2, np.float64)
+        lib().oem_time(self._p, out)
+        return float(out[0]), float(out[1])
 
     def evaluate_sources(self, elements):
         el = np.ascontiguousarray(elements, np.float32).reshape(-1, 12)

@@ -67,6 +67,8 @@ struct OEm {
     int can_predict;
     uint32_t nodal_after; /* iterations before the nodal switch (1024 in the reference) */
     float *nodal;         /* (nx+1)(ny+1)(nz+1) nodal corrections */
+    int no_predict;       /* the reference's test switch predict_increments = false */
+    float prediction[3];  /* its prediction_diagnostic: factor, initial residual, fallback */
 };
 
 static f4 F4(float x, float y, float z, float w) { f4 r = {x, y, z, w}; return r; }
@@ -1015,6 +1017,18 @@ static void restart(OEm *s) {
 }
 
 void oem_set_nodal_switch(OEm *s, uint32_t after) { s->nodal_after = after; }
+void oem_update_config(OEm *s, double dt_s, float rel_tol, uint32_t max_it) {
+    s->dt_s = dt_s;
+    s->rel_tol = rel_tol;
+    s->max_it = max_it;
+}
+void oem_set_predict(OEm *s, int on) { s->no_predict = !on; }
+void oem_set_previous(OEm *s, const float *a) { memcpy(s->previous, a, (size_t)s->edges[3] * 4); }
+void oem_prediction(const OEm *s, float out[3]) { memcpy(out, s->prediction, sizeof s->prediction); }
+void oem_time(const OEm *s, double out[2]) {
+    out[0] = s->time_s;
+    out[1] = s->last_dt;
+}
 
 /* EmState::advance_to (src/em/mod.rs:863-1090) for one step to `time_s`.
    `applied` (E floats) is the applied potential at that time, or NULL when it
@@ -1024,7 +1038,7 @@ int oem_advance(OEm *s, double time_s, int initial, const float *applied, float 
     uint32_t E = s->edges[3];
     s->control[1] = initial ? 1u : 0u;
     float pf = 0.0f;
-    if (!initial && s->can_predict && s->last_dt > 0.0) {
+    if (!s->no_predict && !initial && s->can_predict && s->last_dt > 0.0) {
         float ratio = (float)((time_s - s->time_s) / s->last_dt);
         pf = (isfinite(ratio) && ratio > 0.0f) ? ratio : 0.0f;
     }
@@ -1049,7 +1063,11 @@ int oem_advance(OEm *s, double time_s, int initial, const float *applied, float 
     begin_step(s);
     solve_prepare(s);
     if (s->scalars[1].x != 0.0f) solve_prepare(s);
+    s->prediction[0] = pf;
+    s->prediction[1] = sqrtf(s->scalars[0].y / maxf(s->scalars[0].z, 1e-38f));
+    s->prediction[2] = 0.0f;
     if (pf > 0.0f && (!status_finite(s->scalars) || s->scalars[0].y > s->scalars[0].z)) {
+        s->prediction[2] = 1.0f;
         s->origin[3] = 0.0f;
         zero_guess(s);
         solve_prepare(s);

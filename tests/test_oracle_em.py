@@ -505,3 +505,101 @@ def test_sources_superpose_in_applied_mode():
     summed = sum(probe(p) for p in parts)
     assert np.linalg.norm(total - summed) < np.linalg.norm(summed) * 2e-4 + 1e-7, (total, summed)
     s.close()
+
+
+def _prediction_pair():
+    """src/em/prediction_tests.rs:93-128: two equal states in a 16 mm box
+    with a conductor, driven by B_z = 1 mT sin(2 pi 2 kHz t)."""
+    n, h, origin = 16, 1e-3, (-8e-3,) * 3
+    states = []
+    for _ in range(2):
+        s = O.EmSolve((n,) * 3, h, origin=origin, max_iterations=2000)
+        s.set_materials(_ring(n), _props())
+        states.append(s)
+    b = (np.float32(0.0), np.float32(0.0), np.float32(1e-3))
+    applied = lambda t: _uniform_applied(states[0], h, origin, b, scale=math.sin(2 * math.pi * 2000.0 * t))
+    for s in states:
+        assert s.advance(0.0, initial=True, applied=applied(0.0))[0] == s.OK
+    return states[0], states[1], applied
+
+
+def _compare_fields(a, b, tol=2e-4):
+    ra, rb = a.results().astype(np.float64), b.results().astype(np.float64)
+    for lanes in ((0, 1, 2, 3), (4, 5, 6, 7), (8, 9, 10), (11,)):
+        x, y = ra[:, lanes], rb[:, lanes]
+        assert math.sqrt(((x - y) ** 2).sum() / max((x ** 2).sum(), 1e-38)) < tol, lanes
+
+
+def test_prediction_bad_history_falls_back_to_identical_zero_guess_fields():
+    """prediction_tests.rs:169-189: poisoned history (1e-3 or 1e20 on every
+    edge) trips the guard and the step equals the unpredicted one bit for bit."""
+    for poison in (1e-3, 1e20):
+        original, predicted, applied = _prediction_pair()
+        original.set_predict(False)
+        predicted.set_predict(False)
+        t = 0.0
+        for _ in range(2):
+            t += 1e-5
+            original.advance(t, applied=applied(t))
+            predicted.advance(t, applied=applied(t))
+        np.testing.assert_array_equal(original.results().view(np.uint32), predicted.results().view(np.uint32))
+        predicted.set_predict(True)
+        predicted.set_previous(np.full(predicted.edges, np.float32(poison)))
+        t += 1e-5
+        original.advance(t, applied=applied(t))
+        predicted.advance(t, applied=applied(t))
+        assert predicted.prediction()[2] == 1.0
+        np.testing.assert_array_equal(original.results().view(np.uint32), predicted.results().view(np.uint32))
+        original.close()
+        predicted.close()
+
+
+def test_prediction_tracks_timestep_changes():
+    """prediction_tests.rs:190-211: the prediction factor follows
+    dt / previous dt (to 1e-6), every solve meets its tolerance, and the fields
+    stay within 2e-4 of the unpredicted run's."""
+    original, predicted, applied = _prediction_pair()
+    original.set_predict(False)
+    prev, t = 0.0, 0.0
+    for dt in (1e-5, 1e-5, 0.5e-5, 0.5e-5, 2e-5, 1e-5):
+        for s in (original, predicted):
+            s.update_config(dt, 1e-5, 2000)
+        t += dt
+        assert original.advance(t, applied=applied(t))[0] == O.EmSolve.OK
+        rc, st, _ = predicted.advance(t, applied=applied(t))
+        assert rc == O.EmSolve.OK
+        expected = dt / prev if prev > 0 else 0.0
+        assert abs(float(predicted.prediction()[0]) - expected) < 1e-6
+        assert math.sqrt(st[1] / max(st[2], 1e-38)) <= 1e-5
+        _compare_fields(original, predicted)
+        prev = dt
+    original.close()
+    predicted.close()
+
+
+def test_prediction_failure_restores_fields_and_retry_uses_valid_history():
+    """prediction_tests.rs:212-236: a predicted step capped at one iteration
+    fails, leaves time, the step history and the fields as they were, and the
+    retry matches the unpredicted run."""
+    original, predicted, applied = _prediction_pair()
+    original.set_predict(False)
+    t = 0.0
+    for _ in range(2):
+        t += 1e-5
+        original.advance(t, applied=applied(t))
+        predicted.advance(t, applied=applied(t))
+    predicted.update_config(1e-5, 1e-5, 1)
+    accepted = predicted.results().copy()
+    before = predicted.time()
+    rc, _, _ = predicted.advance(t + 1e-5, applied=applied(t + 1e-5))
+    assert rc == O.EmSolve.NOT_CONVERGED
+    assert predicted.time() == before
+    np.testing.assert_array_equal(predicted.results().view(np.uint32), accepted.view(np.uint32))
+    predicted.update_config(1e-5, 1e-5, 2000)
+    t += 1e-5
+    assert original.advance(t, applied=applied(t))[0] == O.EmSolve.OK
+    assert predicted.advance(t, applied=applied(t))[0] == O.EmSolve.OK
+    assert original.time() == predicted.time()
+    _compare_fields(original, predicted)
+    original.close()
+    predicted.close()
