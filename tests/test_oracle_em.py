@@ -603,3 +603,35 @@ def test_prediction_failure_restores_fields_and_retry_uses_valid_history():
     _compare_fields(original, predicted)
     original.close()
     predicted.close()
+
+
+def test_weak_drive_preserves_linear_fields_and_quadratic_force_heat():
+    """prediction_tests.rs:237-321: the same drive at amplitudes 1 and 1e-8
+    (tolerance 1e-4, nodal correction from the first pass, so the weak case
+    runs on the power-of-two residual scale): every step meets the physical
+    bound r^2 <= tol^2 b^2 + 1e-38 after undoing the scale, and B, J and the
+    applied B scale by 1e-8 while force and heat scale by 1e-16, to 2e-4."""
+    n, h, origin = 16, 1e-3, (-8e-3,) * 3
+    results = []
+    for amplitude in (1.0, 1e-8):
+        s = O.EmSolve((n,) * 3, h, origin=origin, rel_tol=1e-4, max_iterations=4000)
+        s.set_materials(_ring(n), _props())
+        b = (np.float32(0.0), np.float32(0.0), np.float32(1e-3))
+        applied = lambda t: _uniform_applied(s, h, origin, b, scale=amplitude * math.sin(2 * math.pi * 2000.0 * t))
+        assert s.advance(0.0, initial=True, applied=applied(0.0))[0] == s.OK
+        O.lib().oem_set_nodal_switch(s._p, 0)
+        t = 0.0
+        for _ in range(4):
+            t += 1e-5
+            rc, st, _ = s.advance(t, applied=applied(t))
+            assert rc == s.OK
+            sc = s.scalars()
+            scale = float(sc[24]) if sc[24] > 0 else 1.0
+            r2, b2 = float(st[1]) * scale ** 2, float(st[2]) * scale ** 2
+            assert r2 <= (b2 * 1e-8 + 1e-38) * 1.00001
+        results.append(s.results().astype(np.float64))
+        s.close()
+    ref, weak = results
+    for lanes, k in (((0, 1, 2), 1e-8), ((4, 5, 6), 1e-8), ((8, 9, 10), 1e-16), ((11,), 1e-16), ((12, 13, 14), 1e-8)):
+        x, y = ref[:, lanes], weak[:, lanes] / k
+        assert math.sqrt(((x - y) ** 2).sum() / max((x ** 2).sum(), 1e-300)) < 2e-4, lanes
