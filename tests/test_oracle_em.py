@@ -635,3 +635,55 @@ def test_weak_drive_preserves_linear_fields_and_quadratic_force_heat():
     for lanes, k in (((0, 1, 2), 1e-8), ((4, 5, 6), 1e-8), ((8, 9, 10), 1e-16), ((11,), 1e-16), ((12, 13, 14), 1e-8)):
         x, y = ref[:, lanes], weak[:, lanes] / k
         assert math.sqrt(((x - y) ** 2).sum() / max((x ** 2).sum(), 1e-300)) < 2e-4, lanes
+
+
+def test_held_sources_match_recomputation():
+    """prediction_tests.rs:323-430: two square loops (a tabulated current with
+    a plateau, and -4 A) plus a uniform field.  A state that holds the
+    applied potential while the currents are unchanged (hold_source) stays bit
+    for bit equal to one that recomputes it every step -- also around a
+    failed step, after which the held state recomputes."""
+    from mhdproj import synth
+
+    n, h, origin = 16, 1e-3, (-8e-3,) * 3
+
+    def square(z, current):
+        pts = np.array([[-5, -5, z], [5, -5, z], [5, 5, z], [-5, 5, z], [-5, -5, z]], np.float64) * 1e-3
+        el = np.zeros((4, 12), np.float32)
+        el[:, 0:3], el[:, 4:7], el[:, 8], el[:, 10] = pts[:-1], pts[1:], 2e-4, current
+        return el
+
+    table = lambda t: float(np.interp(t, [0.0, 1e-5, 3e-5, 4e-5], [0.0, 10.0, 10.0, 0.0]))
+    elements = lambda t: np.concatenate([square(-2.0, table(t)), square(2.0, -4.0),
+                                         synth.em_uniform_element((0.0, 0.0, 1e-3))])
+    states = []
+    for _ in range(2):
+        s = O.EmSolve((n,) * 3, h, origin=origin, max_iterations=4000)
+        s.set_materials(_ring(n), _props())
+        s.set_predict(False)
+        assert s.advance(0.0, initial=True, applied=s.evaluate_sources(elements(0.0)))[0] == s.OK
+        states.append(s)
+    reference, cached = states
+    valid, last = True, table(0.0)
+    reused = []
+    for tick in range(1, 6):
+        t = tick / 1e5
+        assert reference.advance(t, applied=reference.evaluate_sources(elements(t)))[0] == O.EmSolve.OK
+        if tick == 4:
+            before, when = cached.results().copy(), cached.time()
+            cached.update_config(1e-5, 1e-5, 1)
+            rc, _, _ = cached.advance(t, applied=cached.evaluate_sources(elements(t)))
+            assert rc == O.EmSolve.NOT_CONVERGED and cached.time() == when
+            np.testing.assert_array_equal(cached.results().view(np.uint32), before.view(np.uint32))
+            cached.update_config(1e-5, 1e-5, 4000)
+            valid = False
+        hold = valid and table(t) == last
+        reused.append(hold)
+        rc, _, _ = cached.advance(t, applied=None if hold else cached.evaluate_sources(elements(t)))
+        assert rc == O.EmSolve.OK
+        valid, last = True, table(t)
+        assert cached.time() == reference.time()
+        np.testing.assert_array_equal(cached.results().view(np.uint32), reference.results().view(np.uint32))
+    assert reused == [False, True, True, False, True]
+    reference.close()
+    cached.close()
