@@ -245,6 +245,8 @@ void oem_update_config(OEm *s, double dt_s, float rel_tol, uint32_t max_it);
 /* The reference's test switch predict_increments, its prediction_diagnostic
  * (factor, initial relative residual, fallback flag) and (time, last dt). */
 void oem_set_predict(OEm *s, int on);
+/* The nodal-corrected preconditioner applied to a residual (edges). */
+void oem_apply_nodal(OEm *s, const float *r, float *out);
 /* Overwrite the previous accepted potential (the tests' poisoned history). */
 void oem_set_previous(OEm *s, const float *a);
 void oem_prediction(const OEm *s, float out[3]);

@@ -164,6 +164,7 @@ def lib():
         L.oem_update_config.argtypes = [C.c_void_p, C.c_double, C.c_float, C.c_uint32]
         L.oem_set_predict.argtypes = [C.c_void_p, C.c_int]
         L.oem_set_previous.argtypes = [C.c_void_p, _f32p]
+        L.oem_apply_nodal.argtypes = [C.c_void_p, _f32p, _f32p]
         L.oem_prediction.argtypes = [C.c_void_p, _f32p]
         L.oem_time.argtypes = [C.c_void_p, _f64p]
         L.oem_evaluate_sources.argtypes = [C.c_void_p, _f32p, C.c_uint32, _f32p]
@@ -466,6 +467,11 @@ class EmSolve:
 
     def update_config(self, dt, rel_tol, max_iterations):
         lib().oem_update_config(self._p, float(dt), float(rel_tol), int(max_iterations))
+
+    def apply_nodal(self, r):
+        out = np.zeros(self.edges, np.float32)
+        lib().oem_apply_nodal(self._p, np.ascontiguousarray(r, np.float32), out)
+        return out
 
     def set_previous(self, a):
         lib().oem_set_previous(self._p, np.ascontiguousarray(a, np.float32))

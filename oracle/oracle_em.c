@@ -1023,6 +1023,18 @@ void oem_update_config(OEm *s, double dt_s, float rel_tol, uint32_t max_it) {
     s->max_it = max_it;
 }
 void oem_set_predict(OEm *s, int on) { s->no_predict = !on; }
+/* B r with the nodal correction (append_nodal's initial passes on a
+   residual r in work.y): out = the preconditioned residual it leaves in
+   work.w.  Uses the mass terms of the last step. */
+void oem_apply_nodal(OEm *s, const float *r, float *out) {
+    uint32_t E = s->edges[3];
+    for (uint32_t i = 0; i < E; i++) s->work[i] = F4(0.0f, r[i], 0.0f, 0.0f);
+    uint32_t saved = s->control[3];
+    s->control[3] = 1;
+    append_nodal(s, 1);
+    s->control[3] = saved;
+    for (uint32_t i = 0; i < E; i++) out[i] = s->work[i].w;
+}
 void oem_set_previous(OEm *s, const float *a) { memcpy(s->previous, a, (size_t)s->edges[3] * 4); }
 void oem_prediction(const OEm *s, float out[3]) { memcpy(out, s->prediction, sizeof s->prediction); }
 void oem_time(const OEm *s, double out[2]) {

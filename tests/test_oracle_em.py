@@ -687,3 +687,83 @@ def test_held_sources_match_recomputation():
     assert reused == [False, True, True, False, True]
     reference.close()
     cached.close()
+
+
+def _nodal_pair(after=0):
+    reference, corrected, applied = _prediction_pair()
+    for s in (reference, corrected):
+        s.set_predict(False)
+    O.lib().oem_set_nodal_switch(corrected._p, after)
+    return reference, corrected, applied
+
+
+def test_nodal_correction_matches_original_fields():
+    """prediction_tests.rs:430-441: with the nodal correction from the first
+    pass the fields stay within 2e-4 of the Jacobi run's for four steps."""
+    reference, corrected, applied = _nodal_pair(0)
+    t = 0.0
+    for _ in range(4):
+        t += 1e-5
+        assert reference.advance(t, applied=applied(t))[0] == O.EmSolve.OK
+        assert corrected.advance(t, applied=applied(t))[0] == O.EmSolve.OK
+        _compare_fields(reference, corrected)
+    reference.close()
+    corrected.close()
+
+
+def test_nodal_correction_is_symmetric_positive():
+    """prediction_tests.rs:443-473: the nodal-corrected preconditioner is
+    symmetric (normalised defect below 2e-6) and positive."""
+    _, state, applied = _nodal_pair(0)
+    assert state.advance(1e-5, applied=applied(1e-5))[0] == O.EmSolve.OK
+    i = np.arange(state.edges)
+    r = (((i * 17) % 31).astype(np.float32) - 15.0) / 16.0
+    s = (((i * 29) % 37).astype(np.float32) - 18.0) / 19.0
+    br, bs = state.apply_nodal(r).astype(np.float64), state.apply_nodal(s).astype(np.float64)
+    rbr, sbs = float(r @ br), float(s @ bs)
+    assert rbr > 0 and sbs > 0
+    assert abs(float(r @ bs) - float(s @ br)) / math.sqrt(rbr * sbs) < 2e-6
+
+
+def test_nodal_correction_timestep_changes_and_failure():
+    """prediction_tests.rs:475-515 (without the reference's allocation
+    failure): switched to the nodal correction after one iteration, the
+    solves follow timestep changes within 2e-4 of the Jacobi fields, a step
+    capped at one iteration fails leaving time and fields unchanged, and the
+    retry matches."""
+    reference, corrected, applied = _nodal_pair(1)
+    corrected.set_predict(True)
+    t = 0.0
+    for dt in (1e-5, 0.5e-5, 2e-5):
+        for s in (reference, corrected):
+            s.update_config(dt, 1e-5, 2000)
+        t += dt
+        assert reference.advance(t, applied=applied(t))[0] == O.EmSolve.OK
+        rc, st, _ = corrected.advance(t, applied=applied(t))
+        assert rc == O.EmSolve.OK and 32 < st[6] <= 2000   # past the first batch: switched
+        _compare_fields(reference, corrected)
+    accepted, when = corrected.results().copy(), corrected.time()
+    corrected.update_config(2e-5, 1e-5, 1)
+    assert corrected.advance(t + 2e-5, applied=applied(t + 2e-5))[0] == O.EmSolve.NOT_CONVERGED
+    assert corrected.time() == when
+    np.testing.assert_array_equal(corrected.results().view(np.uint32), accepted.view(np.uint32))
+    corrected.update_config(2e-5, 1e-5, 2000)
+    t += 2e-5
+    assert reference.advance(t, applied=applied(t))[0] == O.EmSolve.OK
+    assert corrected.advance(t, applied=applied(t))[0] == O.EmSolve.OK
+    _compare_fields(reference, corrected)
+
+
+def test_nodal_fallback_keeps_short_solves_identical():
+    """prediction_tests.rs:517-532: with the switch at 1024 iterations, short
+    solves never switch and stay bit for bit equal to plain Jacobi, with the
+    same iteration counts."""
+    reference, corrected, applied = _nodal_pair(1024)
+    O.lib().oem_update_config(corrected._p, 1e-5, 1e-5, 2000)
+    t = 0.0
+    for _ in range(4):
+        t += 1e-5
+        _, sa, _ = reference.advance(t, applied=applied(t))
+        _, sb, _ = corrected.advance(t, applied=applied(t))
+        assert sa[6] == sb[6]
+        np.testing.assert_array_equal(reference.results().view(np.uint32), corrected.results().view(np.uint32))
