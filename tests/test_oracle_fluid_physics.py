@@ -15,7 +15,9 @@ viscosity 1 Pa s (src/fluid/tests.rs:8-57).
     in velocity and kinetic energy (src/fluid/tests.rs:280-322);
   - a stratified thermal phase, classified by the `phase` pass, stays at
     hydrostatic rest under the phase-drag weighted projection with the
-    expected fluid mass, for Jacobi and multigrid (src/fluid/tests.rs:336-391).
+    expected fluid mass, for Jacobi and multigrid (src/fluid/tests.rs:336-391);
+  - a uniform EM force accelerates the fluid by f / rho in one step
+    (src/fluid/tests.rs:198-278).
 """
 import math
 
@@ -167,3 +169,26 @@ def test_thermal_phase_topology_and_weighted_projection_preserve_rest(oracle_lib
     # the whole grid solidifies: no fluid cells remain
     flags = oracle_lib.classify_cells(materials, 3, mask01, rec, thermal=np.zeros(cells, np.float32))
     assert flags & 1 and int(mask01.sum()) == 0
+
+
+def test_em_force_accelerates_velocity(oracle_lib):
+    """src/fluid/tests.rs:198-278: a uniform EM force of 1000 N/m^3 along x on
+    the periodic 8-cell channel (rho = 1000) accelerates the fluid by 1 m/s^2:
+    after one 1e-4 s step u_x = 1e-4 m/s within 1e-8, and the cell records
+    carry the force."""
+    dims, prm, comps, mask = _channel(oracle_lib, 8, 1e-4, 7)
+    cells = prm.dims[3]
+    em = np.zeros((cells, 4), np.float32)
+    em[:, 0] = 1000.0
+    occ = np.ones(cells, np.float32)
+    zero3 = np.zeros(3, np.float32)
+    vel = np.zeros((prm.faces[3], 4), np.float32)
+    pred = oracle_lib.predict(prm, mask, vel)
+    visc = oracle_lib.viscous(prm, mask, occ, pred, zero3, em=em)
+    res, vel, work, _ = oracle_lib.ref_project(prm, mask, comps, occ, visc, warm_start=True,
+                                               old_pressure=np.zeros(cells, np.float32))
+    assert res.status == 0
+    u = R.records_to_soa(dims, vel)[0]
+    assert abs(float(u[2, 4, 2]) - 1e-4) < 1e-8
+    rec, _ = oracle_lib.fields(prm, mask, occ, work, vel, zero3, em=em)
+    assert np.all(rec[:, 8] == 1000.0)
