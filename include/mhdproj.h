@@ -234,10 +234,13 @@ int mhdproj_kernel_launches(mhdproj_ctx *ctx, uint64_t *count);
  * on the host.  The reduction scratch is a fixed 96 KiB array in the library's
  * device image (kept by every GPU that loads the library until exit), so an
  * x-y plane may hold at most 4096 tiles of 32x8 cells (nx*ny up to about one
- * million); larger planes return MHDPROJ_ERR_INVALID with a message from
- * mhdproj_last_error(NULL).  All calls on a device share the array: calls
- * that overlap on the GPU race.  The first call on each device looks up the
- * array's device address; make it before any stream capture. */
+ * million); larger planes, and grids whose face arrays reach 2^31 elements,
+ * return MHDPROJ_ERR_INVALID with a message from mhdproj_last_error(NULL).
+ * grid->periodic is honoured: on a periodic axis the high face of the last
+ * cell is read at face 0.  All calls on a device share the array: calls that
+ * overlap on the GPU race.  The first call on each device looks up the
+ * array's device address.  Every call waits on the host for its result, so
+ * it cannot be made on a stream that is being captured into a CUDA graph. */
 int mhdproj_divergence_noalloc(const mhdproj_grid *grid, const uint8_t *solid, const float *u, const float *v,
                                const float *w, double *out, void *stream);
 

@@ -101,6 +101,35 @@ __device__ __forceinline__ float outlet_conductance(float a, float rho_l, float 
     return __fmul_rn(2.0f, __fdiv_rn(rho_l, rho_of(a, rho_l, rho_air)));
 }
 
+// Face mobility of the GB300 solver (mobility, src/fluid/solver.wgsl:43-51):
+// beta = rho_l / mean face density with two phases, 1 with one phase
+// (SurfaceConfig disabled); with a thermal phase field, divided by
+// 1 + dt * drag where drag = rate (1 - f)^2 / (f^3 + 1e-3) and f is the
+// smaller phase fraction of the two cells.  Same operation order as the
+// reference and the oracle, no fused multiply-adds.
+struct Mobility {
+    float rho_l, rho_air;
+    int single;          // one phase: beta = 1
+    const float* phase;  // thermal phase fraction per cell, or nullptr (no drag)
+    float drag_rate, dt;
+};
+__device__ __forceinline__ float mobility_of(const Mobility& m, float aL, float aR, long long iL, long long iR) {
+    float b = m.single ? 1.0f : beta_of(aL, aR, m.rho_l, m.rho_air);
+    if (m.phase) {
+        const float f = fminf(__ldg(m.phase + iL), __ldg(m.phase + iR));
+        const float om = __fsub_rn(1.0f, f);
+        const float drag = __fdiv_rn(__fmul_rn(__fmul_rn(m.drag_rate, om), om),
+                                     __fadd_rn(__fmul_rn(__fmul_rn(f, f), f), 1e-3f));
+        b = __fdiv_rn(b, __fadd_rn(1.0f, __fmul_rn(m.dt, drag)));
+    }
+    return b;
+}
+// Dirichlet outlet: conductance 2 beta to p = 0 half a cell above the cell
+// (beta of the cell with itself; 2 rho_l / rho with two phases).
+__device__ __forceinline__ float outlet_mobility(const Mobility& m, float a, long long i) {
+    return __fmul_rn(2.0f, mobility_of(m, a, a, i, i));
+}
+
 // ------------------------------------------------------ storage types
 struct CoefF32 { using store = float4; };
 struct CoefF16 { using store = uint2; };

@@ -60,6 +60,10 @@ struct mhdproj_ctx {
     void* coef_lo = nullptr;
     float* gtop = nullptr;
     float rho_l = 0.f, rho_air = 0.f;
+    // thermal phase drag of the GB300 mobility (mhdproj_set_phase_drag)
+    float* phase = nullptr;
+    bool drag = false;
+    float drag_rate = 0.f, drag_dt = 0.f;
     // solver state
     // double-FP32 pairs: right-hand side, potential, adjoint potential
     float *b_hi = nullptr, *b_lo = nullptr, *phi_hi = nullptr, *phi_lo = nullptr;
@@ -166,6 +170,12 @@ static Fields fields(mhdproj_ctx* c) {
     F.h = c->grid.h;
     F.rho_l = c->rho_l;
     F.rho_air = c->rho_air;
+    F.mob.rho_l = c->rho_l;
+    F.mob.rho_air = c->rho_air;
+    F.mob.single = c->opt.two_phase == 0;
+    F.mob.phase = c->drag ? c->phase : nullptr;
+    F.mob.drag_rate = c->drag_rate;
+    F.mob.dt = c->drag_dt;
     F.n_active = c->n_active;
     return F;
 }
@@ -501,6 +511,8 @@ static int update_topology(mhdproj_ctx* ctx, const uint8_t* solid, bool* changed
     return 0;
 }
 
+static int rebuild_coefficients(mhdproj_ctx* ctx);
+
 extern "C" int mhdproj_set_coefficients(mhdproj_ctx* ctx, const float* alpha, const uint8_t* solid, float rho_liquid,
                                         float rho_air) {
     if (!ctx || !alpha || !solid) return ctx ? fail(ctx, MHDPROJ_ERR_INVALID, "alpha and solid must not be NULL") : MHDPROJ_ERR_INVALID;
@@ -518,6 +530,12 @@ extern "C" int mhdproj_set_coefficients(mhdproj_ctx* ctx, const float* alpha, co
         return 0;
     }
     CK(cudaMemcpyAsync(ctx->alpha, alpha, ctx->n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    return rebuild_coefficients(ctx);
+}
+
+// GB300 solver: the coefficient cache, smoother records and multigrid
+// hierarchy from the stored liquid fraction, densities and phase drag.
+static int rebuild_coefficients(mhdproj_ctx* ctx) {
     Fields F = fields(ctx);
     launch_coefficients(ctx->L, F, ctx->stream);
     ctx->launches += 1;
@@ -538,8 +556,20 @@ extern "C" int mhdproj_set_coefficients(mhdproj_ctx* ctx, const float* alpha, co
 
 extern "C" int mhdproj_set_phase_drag(mhdproj_ctx* ctx, const float* phase, float drag_rate, float dt) {
     if (!ctx) return MHDPROJ_ERR_INVALID;
-    if (!ctx->ref) return fail(ctx, MHDPROJ_ERR_INVALID, "phase drag is a reference-solver mobility term");
-    return ref_set_phase_drag(ctx->ref, phase, drag_rate, dt, ctx->err);
+    if (ctx->ref) return ref_set_phase_drag(ctx->ref, phase, drag_rate, dt, ctx->err);
+    if (!phase) {
+        ctx->drag = false;
+    } else {
+        if (!(drag_rate > 0.0f) || !(dt > 0.0f) || !std::isfinite(drag_rate) || !std::isfinite(dt))
+            return fail(ctx, MHDPROJ_ERR_INVALID, "Invalid fluid timestep, initial condition or solver limits/tolerances");
+        if (!ctx->phase) CK(dalloc(ctx, &ctx->phase, ctx->n * 4));
+        CK(cudaMemcpyAsync(ctx->phase, phase, ctx->n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+        ctx->drag = true;
+        ctx->drag_rate = drag_rate;
+        ctx->drag_dt = dt;
+    }
+    // the mobility changed: rebuild the cache if coefficients are set
+    return ctx->have_coef ? rebuild_coefficients(ctx) : 0;
 }
 
 // ------------------------------------------------------------- solver
@@ -761,9 +791,19 @@ static void begin_scalars(mhdproj_ctx* ctx) {
     launch_init_scalars(ctx->sc, tol2, abs_floor, 1e-10, (int)ctx->opt.max_iterations, ctx->stream);
 }
 
+// The phase-drag mobility depends on dt; a call with another dt is refused
+// (the reference rebuilds its coefficients with the step's dt).
+static int check_drag_dt(mhdproj_ctx* ctx, float dt) {
+    if (ctx->drag && dt != ctx->drag_dt)
+        return fail(ctx, MHDPROJ_ERR_INVALID,
+                    "the phase-drag mobility was set for a different dt; call mhdproj_set_phase_drag again");
+    return 0;
+}
+
 static int project_gb300(mhdproj_ctx* ctx, const float* us, const float* vs, const float* ws, float* uo, float* vo,
                          float* wo, float* po, float dt, int warm, mhdproj_stats* st) {
     if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients before projecting");
+    if (int rc = check_drag_dt(ctx, dt)) return rc;
     CK(cudaEventRecord(ctx->ev_a, ctx->stream));
     begin_scalars(ctx);
     Fields F = fields(ctx);
@@ -921,6 +961,7 @@ extern "C" int mhdproj_project_vjp(mhdproj_ctx* ctx, const float* gux, const flo
     if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients before the adjoint");
     if (!gux || !guy || !guz || !ogx || !ogy || !ogz) return fail(ctx, MHDPROJ_ERR_INVALID, "face arrays must not be NULL");
     if (!(dt > 0.f)) return fail(ctx, MHDPROJ_ERR_INVALID, "dt must be positive");
+    if (int rc = check_drag_dt(ctx, dt)) return rc;
     CK(cudaEventRecord(ctx->ev_a, ctx->stream));
     mhdproj_stats local{};
     int rc = vjp_gb300(ctx, gux, guy, guz, gp, dt, ogx, ogy, ogz, &local);
@@ -963,6 +1004,7 @@ extern "C" int mhdproj_chain_forward(mhdproj_ctx* ctx, const float* u0x, const f
     if (ctx->ref) return fail(ctx, MHDPROJ_ERR_INVALID, "the chained adjoint is part of the GB300 solver");
     if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients before the chain");
     if (steps < 1 || checkpoint_every < 1 || !(dt > 0.f)) return fail(ctx, MHDPROJ_ERR_INVALID, "steps, checkpoint_every and dt must be positive");
+    if (int rc = check_drag_dt(ctx, dt)) return rc;
     int rc = chain_alloc(ctx);
     if (rc) return rc;
     const long long m[3] = {ctx->nfx, ctx->nfy, ctx->nfz};
@@ -1193,6 +1235,10 @@ static StepView step_view(mhdproj_ctx* ctx, const float* u, const float* v, cons
         sv.two_phase = ctx->rho_air != ctx->rho_l;
         sv.rho_l = ctx->rho_l;
         sv.rho_air = ctx->rho_air;
+        if (ctx->drag) {
+            sv.phase = ctx->phase;
+            sv.drag_rate = ctx->drag_rate;
+        }
     }
     return sv;
 }
@@ -1425,6 +1471,9 @@ extern "C" int mhdproj_fluid_step(mhdproj_ctx* ctx, float* u, float* v, float* w
     if (ctx->ref && base.phase && dt != ref_export(ctx->ref).drag_dt)
         return fail(ctx, MHDPROJ_ERR_INVALID,
                     "the phase-drag mobility was set for a different dt; call mhdproj_set_phase_drag again");
+    if (!ctx->ref) {
+        if (int rc = check_drag_dt(ctx, dt)) return rc;
+    }
     int rc = step_buffers(ctx);
     if (rc) return rc;
     float* const vel[3] = {u, v, w};

@@ -71,8 +71,8 @@ __global__ void k_set_sigma(Scalars* sc, float sigma) {
 
 // ------------------------------------------------------- coefficients
 __global__ void __launch_bounds__(TILE_THREADS) k_coefficients(Grid3 g, int outlet, const float* __restrict__ alpha,
-                                                               const uint8_t* __restrict__ cls, float rho_l,
-                                                               float rho_air, float4* __restrict__ coef,
+                                                               const uint8_t* __restrict__ cls, Mobility mob,
+                                                               float4* __restrict__ coef,
                                                                void* __restrict__ lo, int lo_kind,
                                                                float* __restrict__ gtop) {
     TILE_BEGIN(g) {
@@ -93,15 +93,15 @@ __global__ void __launch_bounds__(TILE_THREADS) k_coefficients(Grid3 g, int outl
             an[k] = order[k] >= 0 ? alpha[order[k]] : 0.0f;
         }
         if (ci == 1) {
-            if (cn[0] == 1) c.x = beta_of(an[0], ai, rho_l, rho_air);
-            if (cn[2] == 1) c.y = beta_of(an[2], ai, rho_l, rho_air);
-            if (cn[4] == 1) c.z = beta_of(an[4], ai, rho_l, rho_air);
+            if (cn[0] == 1) c.x = mobility_of(mob, an[0], ai, order[0], i);
+            if (cn[2] == 1) c.y = mobility_of(mob, an[2], ai, order[2], i);
+            if (cn[4] == 1) c.z = mobility_of(mob, an[4], ai, order[4], i);
             float r = 0.0f;
 #pragma unroll
             for (int k = 0; k < 6; k++)
-                if (cn[k] == 2) r = __fadd_rn(r, beta_of(ai, an[k], rho_l, rho_air));
+                if (cn[k] == 2) r = __fadd_rn(r, mobility_of(mob, ai, an[k], i, order[k]));
             if (outlet && z == g.nz - 1) {
-                const float gt = outlet_conductance(ai, rho_l, rho_air);
+                const float gt = outlet_mobility(mob, ai, i);
                 r = __fadd_rn(r, gt);
                 gtop[x + g.nx * y] = gt;
             }
@@ -556,7 +556,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_scale(Grid3 g, const float* __
 __device__ __forceinline__ float grad_term(float bt, df pi, df pj, float inv_h) {
     return __fmul_rn(__fmul_rn(bt, df_to_f(df_sub(pi, pj))), inv_h);
 }
-__global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, float h, float rho_l, float rho_air,
+__global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, float h, Mobility mob,
                                                           float p_scale, const uint8_t* __restrict__ cls,
                                                           const float* __restrict__ alpha,
                                                           const float* __restrict__ gtop,
@@ -587,7 +587,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, f
             const int f = x + (nx + 1) * (y + ny * z);
             float out = 0.0f;
             if (nb.xm >= 0 && ci != 0 && cxm != 0)
-                out = uin - grad_term(beta_of(axm, ai, rho_l, rho_air), pi, pxm, inv_h);
+                out = uin - grad_term(mobility_of(mob, axm, ai, nb.xm, i), pi, pxm, inv_h);
             uo[f] = out;
             if (x == 0 && (g.periodic & 1)) uo[nx + (nx + 1) * (y + ny * z)] = out;
             if (x == nx - 1 && !(g.periodic & 1)) uo[nx + (nx + 1) * (y + ny * z)] = 0.0f;
@@ -596,7 +596,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, f
             const int f = x + nx * (y + (ny + 1) * z);
             float out = 0.0f;
             if (nb.ym >= 0 && ci != 0 && cym != 0)
-                out = vin - grad_term(beta_of(aym, ai, rho_l, rho_air), pi, pym, inv_h);
+                out = vin - grad_term(mobility_of(mob, aym, ai, nb.ym, i), pi, pym, inv_h);
             vo[f] = out;
             if (y == 0 && (g.periodic & 2)) vo[x + nx * (ny + (ny + 1) * z)] = out;
             if (y == ny - 1 && !(g.periodic & 2)) vo[x + nx * (ny + (ny + 1) * z)] = 0.0f;
@@ -605,7 +605,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, f
             const int f = x + nx * (y + ny * z);
             float out = 0.0f;
             if (nb.zm >= 0 && ci != 0 && czm != 0)
-                out = win - grad_term(beta_of(azm, ai, rho_l, rho_air), pi, pzm, inv_h);
+                out = win - grad_term(mobility_of(mob, azm, ai, nb.zm, i), pi, pzm, inv_h);
             wo[f] = out;
             const int ft = x + nx * (y + ny * nz);
             if (z == 0 && (g.periodic & 4)) wo[ft] = out;
@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_divergence(Grid3 g, float h, c
 // g_phi = d u / d phi ^T g_u + rho_l/dt g_p on active cells (the transposed
 // gradient), a double-FP32 right-hand side; ||b||^2.  Gradients of a periodic
 // duplicate face are folded into the canonical face.
-__global__ void __launch_bounds__(TILE_THREADS) k_adj_rhs(Grid3 g, int outlet, float h, float rho_l, float rho_air,
+__global__ void __launch_bounds__(TILE_THREADS) k_adj_rhs(Grid3 g, int outlet, float h, Mobility mob,
                                                           float p_scale, const uint8_t* __restrict__ cls,
                                                           const float* __restrict__ alpha,
                                                           const float* __restrict__ gtop,
@@ -703,35 +703,35 @@ __global__ void __launch_bounds__(TILE_THREADS) k_adj_rhs(Grid3 g, int outlet, f
             if (nb.xm >= 0 && cls[nb.xm] != 0) {
                 float gf = gu[x + (nx + 1) * (y + ny * z)];
                 if (x == 0) gf += gu[nx + (nx + 1) * (y + ny * z)];
-                s = df_add(s, two_prod(-beta_of(alpha[nb.xm], ai, rho_l, rho_air) * inv_h, gf));
+                s = df_add(s, two_prod(-mobility_of(mob, alpha[nb.xm], ai, nb.xm, i) * inv_h, gf));
             }
             if (nb.xp >= 0 && cls[nb.xp] != 0) {
                 const int hx = x + 1 == nx ? 0 : x + 1;
                 float gf = gu[hx + (nx + 1) * (y + ny * z)];
                 if (hx == 0) gf += gu[nx + (nx + 1) * (y + ny * z)];
-                s = df_add(s, two_prod(beta_of(ai, alpha[nb.xp], rho_l, rho_air) * inv_h, gf));
+                s = df_add(s, two_prod(mobility_of(mob, ai, alpha[nb.xp], i, nb.xp) * inv_h, gf));
             }
             if (nb.ym >= 0 && cls[nb.ym] != 0) {
                 float gf = gv[x + nx * (y + (ny + 1) * z)];
                 if (y == 0) gf += gv[x + nx * (ny + (ny + 1) * z)];
-                s = df_add(s, two_prod(-beta_of(alpha[nb.ym], ai, rho_l, rho_air) * inv_h, gf));
+                s = df_add(s, two_prod(-mobility_of(mob, alpha[nb.ym], ai, nb.ym, i) * inv_h, gf));
             }
             if (nb.yp >= 0 && cls[nb.yp] != 0) {
                 const int hy = y + 1 == ny ? 0 : y + 1;
                 float gf = gv[x + nx * (hy + (ny + 1) * z)];
                 if (hy == 0) gf += gv[x + nx * (ny + (ny + 1) * z)];
-                s = df_add(s, two_prod(beta_of(ai, alpha[nb.yp], rho_l, rho_air) * inv_h, gf));
+                s = df_add(s, two_prod(mobility_of(mob, ai, alpha[nb.yp], i, nb.yp) * inv_h, gf));
             }
             if (nb.zm >= 0 && cls[nb.zm] != 0) {
                 float gf = gw[x + nx * (y + ny * z)];
                 if (z == 0) gf += gw[x + nx * (y + ny * nz)];
-                s = df_add(s, two_prod(-beta_of(alpha[nb.zm], ai, rho_l, rho_air) * inv_h, gf));
+                s = df_add(s, two_prod(-mobility_of(mob, alpha[nb.zm], ai, nb.zm, i) * inv_h, gf));
             }
             if (nb.zp >= 0 && cls[nb.zp] != 0) {
                 const int hz = z + 1 == nz ? 0 : z + 1;
                 float gf = gw[x + nx * (y + ny * hz)];
                 if (hz == 0) gf += gw[x + nx * (y + ny * nz)];
-                s = df_add(s, two_prod(beta_of(ai, alpha[nb.zp], rho_l, rho_air) * inv_h, gf));
+                s = df_add(s, two_prod(mobility_of(mob, ai, alpha[nb.zp], i, nb.zp) * inv_h, gf));
             } else if (nb.zp < 0 && outlet && z == nz - 1) {
                 s = df_add(s, two_prod(gtop[x + nx * y] * inv_h, gw[x + nx * (y + ny * nz)]));
             }
@@ -942,7 +942,7 @@ Launch tile_launch(int nx, int ny, int nz, int periodic, int target_blocks) {
 }
 
 void launch_coefficients(const Launch& L, const Fields& F, cudaStream_t s) {
-    k_coefficients<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.alpha, F.cls, F.rho_l, F.rho_air, F.coef, F.coef_lo,
+    k_coefficients<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.alpha, F.cls, F.mob, F.coef, F.coef_lo,
                                               F.coef_lo_kind, F.gtop);
 }
 void launch_init_scalars(Scalars* sc, double tol2, double abs_floor, double inner_floor2, int max_total,
@@ -1004,7 +1004,7 @@ void launch_correct(const Launch& L, const Fields& F, const float* ph, const flo
                     const float* vs, const float* ws, float* uo, float* vo, float* wo, float* po, float dt,
                     cudaStream_t s) {
     const float p_scale = (float)((double)F.rho_l / (double)dt);
-    k_correct<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.h, F.rho_l, F.rho_air, p_scale, F.cls, F.alpha, F.gtop, ph,
+    k_correct<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.h, F.mob, p_scale, F.cls, F.alpha, F.gtop, ph,
                                          pl, us, vs, ws, uo, vo, wo, po);
 }
 void launch_divergence(const Launch& L, const Fields& F, const float* u, const float* v, const float* w,
@@ -1020,7 +1020,7 @@ void launch_scale(const Launch& L, const float* in, float* out, float scale, con
 void launch_adj_rhs(const Launch& L, const Fields& F, const float* gu, const float* gv, const float* gw,
                     const float* gp, float dt, cudaStream_t s) {
     const float p_scale = (float)((double)F.rho_l / (double)dt);
-    k_adj_rhs<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.h, F.rho_l, F.rho_air, p_scale, F.cls, F.alpha, F.gtop, gu,
+    k_adj_rhs<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.h, F.mob, p_scale, F.cls, F.alpha, F.gtop, gu,
                                          gv, gw, gp, F.b_hi, F.b_lo, F.sc, F.partials, L.nblocks);
 }
 void launch_adj_correct(const Launch& L, const Fields& F, const float* psi_hi, const float* psi_lo, const float* gu,

@@ -28,6 +28,7 @@ struct Fields {
     double* partials;
     int outlet;
     float h, rho_l, rho_air;
+    Mobility mob;  // face mobility (densities, one-phase flag, thermal drag)
     long long n_active;
 };
 

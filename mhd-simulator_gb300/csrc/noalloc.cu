@@ -13,10 +13,13 @@
 // rejected.  The array is shared by every call on a device and keeps the
 // previous call's contents; each call clears the completion counter first.
 // Calls that overlap on the GPU (two streams at once) race on the array.
-// The first call on a device looks up the array's device address; make that
-// first call before any stream capture.
+// The first call on a device looks up the array's device address.  Every call
+// waits for its result on the host, so none may be made on a stream that is
+// being captured into a CUDA graph.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <climits>
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -52,7 +55,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_divergence_static(Grid3 g, flo
     __shared__ double sh[8 * 2];
     __shared__ double shm[8];
     __shared__ bool last;
-    const int nx = g.nx, ny = g.ny;
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
     const float inv_h = 1.0f / h;
     const int x = blockIdx.x * TX + threadIdx.x;
     const int y = blockIdx.y * TY + threadIdx.y;
@@ -65,9 +68,13 @@ __global__ void __launch_bounds__(TILE_THREADS) k_divergence_static(Grid3 g, flo
             const int i = x + nx * (y + ny * z);
             if (solid[i]) continue;
             cnt += 1.0;
-            df d = two_sum(u[x + 1 + (nx + 1) * (y + ny * z)], -u[x + (nx + 1) * (y + ny * z)]);
-            d = df_add(d, two_sum(v[x + nx * (y + 1 + (ny + 1) * z)], -v[x + nx * (y + (ny + 1) * z)]));
-            d = df_add(d, two_sum(w[x + nx * (y + ny * (z + 1))], -w[x + nx * (y + ny * z)]));
+            // on a periodic axis the high face of the last cell is face 0
+            const int xh = (x + 1 == nx && (g.periodic & 1u)) ? 0 : x + 1;
+            const int yh = (y + 1 == ny && (g.periodic & 2u)) ? 0 : y + 1;
+            const int zh = (z + 1 == nz && (g.periodic & 4u)) ? 0 : z + 1;
+            df d = two_sum(u[xh + (nx + 1) * (y + ny * z)], -u[x + (nx + 1) * (y + ny * z)]);
+            d = df_add(d, two_sum(v[x + nx * (yh + (ny + 1) * z)], -v[x + nx * (y + (ny + 1) * z)]));
+            d = df_add(d, two_sum(w[x + nx * (y + ny * zh)], -w[x + nx * (y + ny * z)]));
             const float dv = df_to_f(d) * inv_h;
             mx = fmaxf(mx, fabsf(dv));
             acc.add_prod(dv, dv);
@@ -142,8 +149,15 @@ extern "C" int mhdproj_divergence_noalloc(const mhdproj_grid* grid, const uint8_
         set_global_error("mhdproj_divergence_noalloc: invalid grid");
         return MHDPROJ_ERR_INVALID;
     }
-    const long long tiles = (long long)((grid->nx + TX - 1) / TX) * ((grid->ny + TY - 1) / TY);
-    if (tiles > NOALLOC_MAX_BLOCKS || (long long)(grid->nx + 1) * grid->ny * (grid->nz + 1) >= (1ll << 31)) {
+    // every index is a 32-bit int in the kernel: each array must stay below 2^31 elements
+    const long long nx = grid->nx, ny = grid->ny, nz = grid->nz;
+    const long long largest = std::max(std::max((nx + 1) * ny * nz, nx * (ny + 1) * nz), nx * ny * (nz + 1));
+    if (nx > INT_MAX || ny > INT_MAX || nz > INT_MAX || largest >= (1ll << 31)) {
+        set_global_error("mhdproj_divergence_noalloc: a face array of 2^31 or more elements is not supported");
+        return MHDPROJ_ERR_INVALID;
+    }
+    const long long tiles = ((nx + TX - 1) / TX) * ((ny + TY - 1) / TY);
+    if (tiles > NOALLOC_MAX_BLOCKS) {
         set_global_error("mhdproj_divergence_noalloc: an x-y plane of more than 4096 tiles of 32x8 cells "
                          "exceeds the fixed scratch (nx*ny up to about 1M cells)");
         return MHDPROJ_ERR_INVALID;

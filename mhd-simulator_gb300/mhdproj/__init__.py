@@ -196,13 +196,22 @@ EXPORTED = [
 ]
 
 
-def divergence_noalloc(dims, h, solid, u, v, w, stream=None):
+def divergence_noalloc(dims, h, solid, u, v, w, stream=None, periodic=0):
     """Max and RMS divergence (1/s) of a face field over non-solid cells, with
-    no device allocation (mhdproj_divergence_noalloc)."""
+    no device allocation (mhdproj_divergence_noalloc).  periodic: bit a set
+    reads the high face of the last cell on axis a at face 0."""
     import torch
 
     L = load()
-    g = Grid(int(dims[0]), int(dims[1]), int(dims[2]), float(h), 0, 0)
+    nx, ny, nz = (int(d) for d in dims)
+    want = (("solid", solid, (nz, ny, nx), torch.uint8), ("u", u, (nz, ny, nx + 1), torch.float32),
+            ("v", v, (nz, ny + 1, nx), torch.float32), ("w", w, (nz + 1, ny, nx), torch.float32))
+    for name, a, shape, dtype in want:
+        if not (a.is_cuda and a.is_contiguous()) or a.dtype != dtype or a.numel() != shape[0] * shape[1] * shape[2]:
+            raise ValueError(f"divergence_noalloc: {name} must be a contiguous CUDA {dtype} tensor of shape {shape}")
+        if a.dim() == 3 and tuple(a.shape) != shape:
+            raise ValueError(f"divergence_noalloc: {name} has shape {tuple(a.shape)}, expected {shape}")
+    g = Grid(nx, ny, nz, float(h), int(periodic), 0)
     out = (C.c_double * 2)()
     s = stream if stream is not None else torch.cuda.current_stream()
     s.synchronize()
@@ -327,6 +336,9 @@ class PressureProjection:
         self.stream = stream
         self._check(L.mhdproj_set_stream(self._ctx, C.c_void_p(stream.cuda_stream)))
         self.solver = solver
+        self.device = torch.device("cuda", torch.cuda.current_device())
+        # bumped by every coefficient change; the autograd pair checks it
+        self.coefficient_generation = 0
 
     # ------------------------------------------------------------ helpers
     def _order(self):
@@ -360,10 +372,12 @@ class PressureProjection:
     # ---------------------------------------------------------- interface
     def set_coefficients(self, alpha, solid, rho_liquid, rho_air):
         self._order()
+        self.coefficient_generation += 1
         self._check(self._lib.mhdproj_set_coefficients(self._ctx, _ptr(alpha), _ptr(solid), rho_liquid, rho_air))
 
     def set_phase_drag(self, phase, drag_rate, dt):
         self._order()
+        self.coefficient_generation += 1
         self._check(self._lib.mhdproj_set_phase_drag(self._ctx, _ptr(phase), drag_rate, dt))
 
     def project(self, u_star, dt, warm_start=False, out=None, pressure=True):
@@ -433,14 +447,14 @@ class PressureProjection:
     def coefficients(self):
         self._order()
         torch = self._torch
-        c = torch.empty(self.cell_shape() + (4,), dtype=torch.float32, device="cuda")
+        c = torch.empty(self.cell_shape() + (4,), dtype=torch.float32, device=self.device)
         self._check(self._lib.mhdproj_copy_coefficients(self._ctx, _ptr(c)))
         return c
 
     def potential(self):
         self._order()
         torch = self._torch
-        phi = torch.empty(self.cell_shape(), dtype=torch.float64, device="cuda")
+        phi = torch.empty(self.cell_shape(), dtype=torch.float64, device=self.device)
         self._check(self._lib.mhdproj_copy_potential(self._ctx, _ptr(phi)))
         return phi
 
@@ -502,7 +516,13 @@ class PressureProjection:
 
 def autograd_projection():
     """torch.autograd.Function pair over forward projection and its VJP:
-    ``ProjectFn.apply(proj, dt, u, v, w) -> (u', v', w', p)``."""
+    ``ProjectFn.apply(proj, dt, u, v, w) -> (u', v', w', p)``.
+
+    The projection is linear in (u, v, w) for fixed coefficients, so the
+    backward pass needs only the coefficients the forward pass used.  It
+    refuses (RuntimeError) when the context's coefficients changed between
+    forward and backward, instead of returning the VJP of another operator.
+    Missing output gradients are zeros on the projection's device."""
     import torch
 
     class ProjectFn(torch.autograd.Function):
@@ -511,14 +531,20 @@ def autograd_projection():
             (uo, vo, wo), p, _ = proj.project((u.contiguous(), v.contiguous(), w.contiguous()), dt)
             ctx.proj = proj
             ctx.dt = dt
+            ctx.generation = proj.coefficient_generation
             return uo, vo, wo, p
 
         @staticmethod
         def backward(ctx, gu, gv, gw, gp):
+            proj = ctx.proj
+            if proj.coefficient_generation != ctx.generation:
+                raise RuntimeError("the projection's coefficients changed between forward and backward; "
+                                   "the VJP would belong to another operator")
             grads = [g.contiguous() if g is not None else None for g in (gu, gv, gw)]
-            shapes = ctx.proj.face_shapes()
-            grads = [g if g is not None else torch.zeros(s, device="cuda") for g, s in zip(grads, shapes)]
-            (a, b, c), _ = ctx.proj.vjp(tuple(grads), gp.contiguous() if gp is not None else None, ctx.dt)
+            shapes = proj.face_shapes()
+            grads = [g if g is not None else torch.zeros(s, dtype=torch.float32, device=proj.device)
+                     for g, s in zip(grads, shapes)]
+            (a, b, c), _ = proj.vjp(tuple(grads), gp.contiguous() if gp is not None else None, ctx.dt)
             return None, None, a, b, c
 
     return ProjectFn

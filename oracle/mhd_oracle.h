@@ -162,6 +162,9 @@ typedef struct {
     int32_t outlet;        /* 1: Dirichlet p=0 on the top z-face */
     float h;
     float rho_liquid, rho_air;
+    int32_t single;        /* one phase: face mobility 1 (SurfaceConfig disabled) */
+    float drag_rate, dt;   /* thermal phase drag (with phase) */
+    const float *phase;    /* thermal phase fraction per cell, or NULL: no drag */
 } onat_grid;
 
 /* Cell classes: 0 solid, 1 active fluid, 2 pinned gauge cell.  Components that

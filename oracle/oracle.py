@@ -59,6 +59,10 @@ class OnatGrid(C.Structure):
         ("h", C.c_float),
         ("rho_liquid", C.c_float),
         ("rho_air", C.c_float),
+        ("single", C.c_int32),
+        ("drag_rate", C.c_float),
+        ("dt", C.c_float),
+        ("phase", C.c_void_p),
     ]
 
 
@@ -313,8 +317,15 @@ def fields(params, mask, occupancy, work, velocity, acceleration, em=None, reser
 
 
 # -------------------------------------------------------------------- native
-def grid(nx, ny, nz, h, rho_liquid, rho_air, periodic=0, outlet=True):
-    return OnatGrid(nx, ny, nz, periodic, int(outlet), h, rho_liquid, rho_air)
+def grid(nx, ny, nz, h, rho_liquid, rho_air, periodic=0, outlet=True, single=False, phase=None, drag_rate=0.0,
+         dt=0.0):
+    """The FP64 oracle's problem description.  single: one phase (mobility 1);
+    phase (cells, float32) with drag_rate and dt: thermal phase drag."""
+    ph = None if phase is None else np.ascontiguousarray(phase, dtype=np.float32).reshape(-1)
+    g = OnatGrid(nx, ny, nz, periodic, int(outlet), h, rho_liquid, rho_air, int(bool(single)), drag_rate, dt,
+                 None if ph is None else ph.ctypes.data)
+    g._phase = ph  # keeps the array alive while the grid is used
+    return g
 
 
 def classify(g, solid):

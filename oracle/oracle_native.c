@@ -75,8 +75,19 @@ uint32_t onat_classify(const onat_grid *g, const uint8_t *solid, uint8_t *cls) {
 
 /* ------------------------------------------------------- coefficients */
 static inline float nrho(const onat_grid *g, float a) { return g->rho_air * (1.0f - a) + g->rho_liquid * a; }
-static inline float nbeta(const onat_grid *g, float a, float b) {
-    return g->rho_liquid / (0.5f * (nrho(g, a) + nrho(g, b)));
+/* mobility() of src/fluid/solver.wgsl:43-51 for the face between cells L and
+ * R: rho_l / mean face density (1 with one phase), divided by 1 + dt * drag
+ * with drag = rate (1 - f)^2 / (f^3 + 1e-3), f the smaller thermal phase
+ * fraction of the two cells, when a phase field is set.  FP32 in the
+ * reference's operation order (built without contraction). */
+static inline float nbeta(const onat_grid *g, const float *alpha, uint64_t L, uint64_t R) {
+    float b = g->single ? 1.0f : g->rho_liquid / (0.5f * (nrho(g, alpha[L]) + nrho(g, alpha[R])));
+    if (g->phase) {
+        float f = fminf(g->phase[L], g->phase[R]);
+        float drag = g->drag_rate * (1.0f - f) * (1.0f - f) / (f * f * f + 1e-3f);
+        b = b / (1.0f + g->dt * drag);
+    }
+    return b;
 }
 void onat_coefficients(const onat_grid *g, const float *alpha, const uint8_t *cls, float *coef, float *gtop) {
     const uint32_t d[3] = {g->nx, g->ny, g->nz};
@@ -90,16 +101,16 @@ void onat_coefficients(const onat_grid *g, const float *alpha, const uint8_t *cl
         if (cls[i] == 1) {
             for (int a = 0; a < 3; a++) {
                 int64_t l = nbr(d, g->periodic, x, y, z, a, -1);
-                if (l >= 0 && cls[l] == 1) c[a] = nbeta(g, alpha[l], alpha[i]);
+                if (l >= 0 && cls[l] == 1) c[a] = nbeta(g, alpha, (uint64_t)l, i);
             }
             float r = 0.0f;
             for (int a = 0; a < 3; a++)
                 for (int dir = -1; dir <= 1; dir += 2) {
                     int64_t j = nbr(d, g->periodic, x, y, z, a, dir);
-                    if (j >= 0 && cls[j] == 2) r += nbeta(g, alpha[i], alpha[j]);
+                    if (j >= 0 && cls[j] == 2) r += nbeta(g, alpha, i, (uint64_t)j);
                 }
             if (outlet_on(g) && z == d[2] - 1) {
-                float gt = 2.0f * (g->rho_liquid / nrho(g, alpha[i]));
+                float gt = 2.0f * nbeta(g, alpha, i, i);
                 r += gt;
                 gtop[x + (uint64_t)d[0] * y] = gt;
             }
@@ -460,7 +471,7 @@ static void correct_d(const onat_grid *g, const float *alpha, const uint8_t *cls
                     uint64_t L = xl + (uint64_t)nx * (y + (uint64_t)ny * z), R = xr + (uint64_t)nx * (y + (uint64_t)ny * z);
                     if (cls[L] != 0 && cls[R] != 0) {
                         uint64_t fc = xr + (uint64_t)(nx + 1) * (y + (uint64_t)ny * z);
-                        out = (double)us[fc] - (double)nbeta(g, alpha[L], alpha[R]) * (phi[R] - phi[L]) / h;
+                        out = (double)us[fc] - (double)nbeta(g, alpha, L, R) * (phi[R] - phi[L]) / h;
                     }
                 }
                 u[f] = out;
@@ -482,7 +493,7 @@ static void correct_d(const onat_grid *g, const float *alpha, const uint8_t *cls
                     uint64_t L = x + (uint64_t)nx * (yl + (uint64_t)ny * z), R = x + (uint64_t)nx * (yr + (uint64_t)ny * z);
                     if (cls[L] != 0 && cls[R] != 0) {
                         uint64_t fc = x + (uint64_t)nx * (yr + (uint64_t)(ny + 1) * z);
-                        out = (double)vs[fc] - (double)nbeta(g, alpha[L], alpha[R]) * (phi[R] - phi[L]) / h;
+                        out = (double)vs[fc] - (double)nbeta(g, alpha, L, R) * (phi[R] - phi[L]) / h;
                     }
                 }
                 v[f] = out;
@@ -508,7 +519,7 @@ static void correct_d(const onat_grid *g, const float *alpha, const uint8_t *cls
                         uint64_t L = x + (uint64_t)nx * (y + (uint64_t)ny * zl), R = x + (uint64_t)nx * (y + (uint64_t)ny * zr);
                         if (cls[L] != 0 && cls[R] != 0) {
                             uint64_t fc = x + (uint64_t)nx * (y + (uint64_t)ny * zr);
-                            out = (double)ws[fc] - (double)nbeta(g, alpha[L], alpha[R]) * (phi[R] - phi[L]) / h;
+                            out = (double)ws[fc] - (double)nbeta(g, alpha, L, R) * (phi[R] - phi[L]) / h;
                         }
                     }
                 }
@@ -633,7 +644,7 @@ static int face_info(const onat_grid *g, const float *alpha, const uint8_t *cls,
     o->fc = cc[0] + F[0] * (cc[1] + F[1] * cc[2]);
     o->L = (int64_t)L;
     o->R = (int64_t)R;
-    o->beta = nbeta(g, alpha[L], alpha[R]);
+    o->beta = nbeta(g, alpha, L, R);
     return 1;
 }
 

@@ -8,14 +8,17 @@ the golden values are the literal expectations its tests assert:
   * gauge anchors on tiny masks: src/fluid/tests.rs,
     pressure_failure_rolls_back_and_disconnected_components_get_gauges
   * acceptance tolerances of the analytic projection tests.
-Run: python tests/golden/make_known_answers.py [reference root]
+Run: python tests/golden/make_known_answers.py <reference root>
+(or set MHD_REFERENCE_ROOT to the reference checkout).
 """
 import json
 import os
 import re
 import sys
 
-ROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MHD_REFERENCE_ROOT")
+if not ROOT:
+    sys.exit("usage: make_known_answers.py <reference root>  (or set MHD_REFERENCE_ROOT)")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 

@@ -1,0 +1,161 @@
+"""The GB300 solver against the reference's projection, through the C ABI.
+
+The GB300 solver (red-black Gauss-Seidel multigrid CG with FP16/BF16/FP32
+levels and FP64 refinement) is run with the reference's own closed
+boundaries (MHDPROJ_BOUNDARY_REFERENCE_CLOSED) on the reference's fixtures
+and on closed jets, and compared with the oracle's FP32 restatement of the
+reference projection (FluidState::project, src/fluid/mod.rs:1015-1115, with
+`correct`, src/fluid/solver.wgsl:245-250) on the same inputs:
+  * face velocities: L2 difference within 2e-4 of the candidate field's
+    norm, the reference's own acceptance measure and bound
+    (src/fluid/multigrid/tests.rs:330-465);
+  * pressure p = rho_l phi / dt in the reference's gauge (each component's
+    root cell at zero; the GB300 solver pins the same cell) within 2e-4.
+The reference restatement runs at 3e-6, close to its FP32 floor on the jets;
+the GB300 solver at 1e-8.  The thermal phase-drag mobility
+(solver.wgsl:46-50) is checked the same way, plus bit-exact coefficients
+against the FP64 oracle's and a projection against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+import refcases as R
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    ("cosine16_one_phase", lambda: R.cosine_case()),
+    ("walls17x13x9", lambda: R.wall_case((17, 13, 9), (0, 0, 0), True, False)),
+    ("walls16x12x8_periodic_xy", lambda: R.wall_case((16, 12, 8), (1, 1, 0), True, True)),
+    ("walls16x12x8_periodic_z", lambda: R.wall_case((16, 12, 8), (0, 0, 1), True, False)),
+    ("jet32_closed", lambda: R.jet_case("jet128", 0.25)),
+    ("jet64_closed", lambda: R.jet_case("jet64", 1.0)),
+    ("jet96_closed", lambda: R.jet_case("jet128", 0.75)),
+]
+
+
+_REFERENCE = {}
+
+
+def _reference(oracle_lib, name, c, **kw):
+    """The restated reference projection of a case (computed once per case)."""
+    key = (name, tuple(sorted(kw)))
+    if key not in _REFERENCE:
+        _REFERENCE[key] = R.run_oracle(oracle_lib, c, max_iterations=4000, **kw)
+    return _REFERENCE[key]
+
+
+def _t(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _gb300(mhdproj, torch, c, precision, rel_tol=1e-8, phase=None, drag_rate=1e6):
+    per = [bool(c["periodic"] & (1 << a)) for a in range(3)]
+    pr = mhdproj.PressureProjection(c["dims"], c["h"], periodic=per, outlet=False, solver="gb300",
+                                    precision=precision, rel_tol=rel_tol, two_phase=c["two_phase"])
+    if phase is not None:
+        pr.set_phase_drag(_t(torch, phase), drag_rate, c["dt"])
+    pr.set_coefficients(_t(torch, c["alpha"]), _t(torch, c["solid"]), c["rho_liquid"], c["rho_air"])
+    (u, v, w), p, st = pr.project(tuple(_t(torch, c[k]) for k in "uvw"), c["dt"])
+    torch.cuda.synchronize()
+    return pr, dict(u=u.cpu().numpy(), v=v.cpu().numpy(), w=w.cpu().numpy(), p=p.cpu().numpy(), stats=st)
+
+
+def _velocity_error(got, want, c):
+    num = sum(float(((np.asarray(got[k], np.float64) - np.asarray(want[k], np.float64)) ** 2).sum()) for k in "uvw")
+    den = sum(float((np.asarray(c[k], np.float64) ** 2).sum()) for k in "uvw")
+    return float(np.sqrt(num / den))
+
+
+def _pressure_error(got, want, mask):
+    fl = mask != 0
+    a = np.asarray(got, np.float64).reshape(-1)[fl]
+    b = np.asarray(want, np.float64).reshape(-1)[fl]
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.mark.parametrize("precision", ["fp16", "bf16", "fp32"])
+@pytest.mark.parametrize("name,factory", CASES, ids=[n for n, _ in CASES])
+def test_gb300_projection_equals_the_references(gpu, oracle_lib, name, factory, precision):
+    import mhdproj
+
+    torch = gpu
+    c = dict(factory(), rel_tol=3e-6, abs_div_tol=0.0)
+    ref = _reference(oracle_lib, name, c)
+    assert ref["result"].status == 0
+    pr, got = _gb300(mhdproj, torch, c, precision)
+    assert got["stats"].true_relative_residual <= 1e-8
+    assert _velocity_error(got, ref, c) < 2e-4
+    assert _pressure_error(got["p"], ref["p"], ref["mask"]) < 2e-4
+    pr.close()
+
+
+def _phase(c, seed=4):
+    rng = np.random.default_rng(seed)
+    f = rng.random(np.asarray(c["alpha"]).shape).astype(np.float32)
+    f[f > 0.6] = 1.0
+    return f
+
+
+DRAG_CASES = [
+    ("walls17x13x9", lambda: R.wall_case((17, 13, 9), (0, 0, 0), True, False)),
+    ("walls16x12x8_periodic_xy", lambda: R.wall_case((16, 12, 8), (1, 1, 0), True, True)),
+    ("walls16x12x8_periodic_z", lambda: R.wall_case((16, 12, 8), (0, 0, 1), True, False)),
+]
+
+
+@pytest.mark.parametrize("name,factory", DRAG_CASES, ids=[n for n, _ in DRAG_CASES])
+def test_phase_drag_coefficients_bit_exact(gpu, oracle_lib, name, factory):
+    """GB300 coefficients with the thermal drag equal the FP64 oracle's bit
+    for bit; set_phase_drag after set_coefficients rebuilds them, and
+    clearing the drag restores the plain mobilities."""
+    import mhdproj
+
+    torch = gpu
+    c = factory()
+    f = _phase(c)
+    nx, ny, nz = c["dims"]
+    per = [bool(c["periodic"] & (1 << a)) for a in range(3)]
+    pr = mhdproj.PressureProjection(c["dims"], c["h"], periodic=per, outlet=False, precision="fp16",
+                                    two_phase=c["two_phase"])
+    pr.set_coefficients(_t(torch, c["alpha"]), _t(torch, c["solid"]), c["rho_liquid"], c["rho_air"])
+    plain = pr.coefficients().cpu().numpy().reshape(-1, 4).copy()
+    pr.set_phase_drag(_t(torch, f), 1e6, c["dt"])
+    got = pr.coefficients().cpu().numpy().reshape(-1, 4)
+    g = oracle_lib.grid(nx, ny, nz, c["h"], c["rho_liquid"], c["rho_air"], c["periodic"], outlet=False,
+                        single=not c["two_phase"], phase=f, drag_rate=1e6, dt=c["dt"])
+    _, cls = oracle_lib.classify(g, c["solid"])
+    want, _ = oracle_lib.coefficients(g, c["alpha"], cls)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert np.any(got[:, :3] < plain[:, :3])
+    pr.set_phase_drag(None, 0.0, 0.0)
+    again = pr.coefficients().cpu().numpy().reshape(-1, 4)
+    assert np.array_equal(again.view(np.uint32), plain.view(np.uint32))
+
+
+@pytest.mark.parametrize("precision", ["fp16", "fp32"])
+@pytest.mark.parametrize("name,factory", DRAG_CASES, ids=[n for n, _ in DRAG_CASES])
+def test_phase_drag_projection(gpu, oracle_lib, name, factory, precision):
+    """The GB300 projection with phase drag against the restated reference
+    projection with the same drag, and against the FP64 oracle; a projection
+    with another dt is refused, as the reference solver refuses it."""
+    import mhdproj
+
+    torch = gpu
+    c = dict(factory(), rel_tol=3e-6, abs_div_tol=0.0)
+    f = _phase(c)
+    ref = _reference(oracle_lib, name, c, phase=f, drag_rate=1e6)
+    assert ref["result"].status == 0
+    pr, got = _gb300(mhdproj, torch, c, precision, phase=f)
+    assert got["stats"].true_relative_residual <= 1e-8
+    assert _velocity_error(got, ref, c) < 2e-4
+    assert _pressure_error(got["p"], ref["p"], ref["mask"]) < 2e-4
+    nx, ny, nz = c["dims"]
+    g = oracle_lib.grid(nx, ny, nz, c["h"], c["rho_liquid"], c["rho_air"], c["periodic"], outlet=False,
+                        single=not c["two_phase"], phase=f, drag_rate=1e6, dt=c["dt"])
+    nat = oracle_lib.project(g, c["alpha"], c["solid"], c["u"], c["v"], c["w"], c["dt"], 1e-13)
+    for k in "uvw":
+        a, b = got[k].reshape(-1).astype(np.float64), nat[k]
+        assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(b) + 1e-7 * np.linalg.norm(c[k])
+    with pytest.raises(mhdproj.ProjectionError, match="different dt"):
+        pr.project(tuple(_t(torch, c[k]) for k in "uvw"), 2.0 * c["dt"])
