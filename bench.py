@@ -143,28 +143,13 @@ def barrier(pg, device=None):
 
 
 # --------------------------------------------------------------- CPU legs
-def reference_iterations(workload, tol):
-    """CG iterations the reference algorithm needs on this workload (closed
-    boundaries), recorded by running the oracle to convergence
-    (oracle/measure_iterations.py -> oracle/reference_iterations.json)."""
-    path = os.path.join(ROOT, "oracle", "reference_iterations.json")
-    try:
-        with open(path) as f:
-            rec = json.load(f).get(f"{workload}@{tol:g}")
-    except OSError:
-        rec = None
-    if not rec or rec.get("status") != 0:
-        return None
-    return int(rec["iterations"])
-
-
 class CpuReference:
     """The reference algorithm on the host cores: the oracle's restatement of
     the reference projection (FP32 aggregation-multigrid CG, 256-lane
-    reductions, closed boundaries, mean-free gauge) run with OpenMP on every
-    host thread.  A full projection takes minutes, so a sample is the set-up
-    plus a few CG iterations, and one projection is set-up + K iterations with
-    K the recorded iteration count of the same workload."""
+    reductions, closed boundaries, mean-free gauge, the reference's batched
+    convergence reads and 64-iteration check) run with OpenMP on every host
+    thread.  One sample is one whole projection to the tolerance: the
+    coefficient cache, the multigrid build and every CG iteration."""
 
     def __init__(self, case, threads, tol):
         os.environ["OMP_NUM_THREADS"] = str(threads)
@@ -189,18 +174,24 @@ class CpuReference:
         self.faces = rec.reshape(-1, 4)
         self.occ = np.ascontiguousarray(case["alpha"].reshape(-1))
 
-    def run(self, iterations):
+    def run(self, iterations=20000):
+        """One projection (to convergence, or `iterations` CG iterations);
+        returns (seconds, oref_result, projected face records)."""
         t0 = time.perf_counter()
-        res, *_ = self.oracle.ref_project(self.params, self.mask, self.comps, self.occ, self.faces,
-                                          max_iterations=iterations)
-        return time.perf_counter() - t0, res
+        res, vel, *_ = self.oracle.ref_project(self.params, self.mask, self.comps, self.occ, self.faces,
+                                               max_iterations=iterations)
+        return time.perf_counter() - t0, res, vel
 
-    def calibrate(self, k_lo=2, k_hi=6):
-        t_lo, _ = self.run(k_lo)
-        t_hi, res = self.run(k_hi)
-        per_it = max((t_hi - t_lo) / (k_hi - k_lo), 1e-9)
-        setup = max(t_lo - k_lo * per_it, 0.0)
-        return setup, per_it, res
+    def projections(self, count, warmup=0):
+        """`warmup` untimed and `count` timed whole projections: the seconds
+        of each timed one and the last result."""
+        for _ in range(warmup):
+            self.run()
+        secs, res = [], None
+        for _ in range(count):
+            t, res, _ = self.run()
+            secs.append(t)
+        return secs, res
 
 
 # ------------------------------------------------------------ our arm
@@ -535,6 +526,33 @@ def run_ours(args):
         line["e2e"] = {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                        "d2h_bytes_per_step": int(d2h)}
         pe.close()
+        # the GB300 solver on the reference's own closed boundaries (no
+        # outlet; each component pinned at its root cell) and the same inputs
+        # as the reference arm, device-resident and end to end
+        pc = mhdproj.PressureProjection(case["dims"], case["h"], outlet=False, precision=args.precision,
+                                        rel_tol=args.tol)
+        for _ in range(2):
+            step(pc)
+        msc, stc = timed(pc, max(3, args.steps // 2))
+        msc /= len(stc)
+        for _ in range(2):
+            pc.project_host(h_alpha, h_solid, case["rho_liquid"], case["rho_air"], h_us, case["dt"], out=h_out,
+                            p_out=h_p)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            pc.project_host(h_alpha, h_solid, case["rho_liquid"], case["rho_air"], h_us, case["dt"], out=h_out,
+                            p_out=h_p)
+        torch.cuda.synchronize(dev)
+        e2e_c = (time.perf_counter() - t0) / ke
+        line["closed256"] = {"workload": f"{args.workload}: {nx}x{ny}x{nz} cells, closed boundaries (the reference's), "
+                                         f"tol {args.tol:g}",
+                             "projections_per_s": 1000.0 / msc, "ms_per_step": msc, "iterations": stc[-1].iterations,
+                             "refinements": stc[-1].refinements,
+                             "true_relative_residual": stc[-1].true_relative_residual,
+                             "e2e": {"value": 1.0 / e2e_c, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                                     "d2h_bytes_per_step": int(d2h)}}
+        pc.close()
         # roofline of the dominant kernel (isolated launches, CUDA events on the library stream)
         pr.set_coefficients(alpha, solid, case["rho_liquid"], case["rho_air"])
         step(pr)
@@ -595,30 +613,93 @@ def run_ours(args):
             line["em_sources"] = em_sources_leg(128, 1024)
         except mhdproj.ProjectionError as exc:
             line["em_step"] = {"unavailable": str(exc)}
-        # CPU baseline: bounded sample of the reference algorithm on the host cores
-        threads = os.cpu_count() or 1
-        k_ref = reference_iterations(args.workload, args.tol)
-        cref = CpuReference(case, threads, args.tol)
-        setup, per_it, _ = cref.calibrate()
-        if "topology" in line:
-            line["topology"]["host_search_ms"] = cref.anchors_s * 1e3
-            line["topology"]["host_search"] = "the reference's anchors() breadth-first search (oracle), 1 thread"
-        if k_ref is not None:
-            line["cpu_baseline"] = {
-                "value": 1.0 / (setup + per_it * k_ref), "unit": UNIT, "cores": threads, "kind": "port",
-                "sample": f"oracle restatement of the reference FP32 multigrid CG on {nx}x{ny}x{nz} (closed "
-                          f"boundaries): set-up {setup:.2f} s + per-iteration {per_it:.2f} s from 2- and "
-                          f"6-iteration runs, scaled to the {k_ref} iterations the reference needs for {args.tol:g}",
-                "setup_seconds": setup, "seconds_per_iteration": per_it, "iterations": k_ref,
-            }
-        else:
-            line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": threads, "kind": "port",
-                                    "sample": "no recorded iteration count for this workload/tolerance"}
+        # CPU leg: whole projections of the reference algorithm on the host
+        # cores, then the FP64 oracle as the checker of the 256^3 results
+        cpu_leg(args, case, line, outputs_for_accuracy(args, case, mhdproj, torch, dev, alpha, solid, us))
     pr.close()
     if rank == 0:
         print(json.dumps(line))
     if pg is not None:
         pg.destroy_process_group()
+
+
+def outputs_for_accuracy(args, case, mhdproj, torch, dev, alpha, solid, us):
+    """The workload projected with FP16 and BF16 multigrid levels at 1e-6 and
+    1e-8 (untimed), copied to the host for the FP64 check."""
+    import numpy as np
+
+    runs = {}
+    for prec in ("fp16", "bf16"):
+        for tol in (1e-6, 1e-8):
+            pa = mhdproj.PressureProjection(case["dims"], case["h"], outlet=True, precision=prec, rel_tol=tol)
+            pa.set_coefficients(alpha, solid, case["rho_liquid"], case["rho_air"])
+            (u, v, w), p, st = pa.project(us, case["dt"])
+            torch.cuda.synchronize(dev)
+            runs[(prec, tol)] = dict(u=u.cpu().numpy(), v=v.cpu().numpy(), w=w.cpu().numpy(), p=p.cpu().numpy(),
+                                     iterations=st.iterations, true_relative_residual=st.true_relative_residual)
+            pa.close()
+    return runs
+
+
+def cpu_leg(args, case, line, runs):
+    """The CPU leg of the bench (rank 0, N = 1).
+
+    cpu_baseline: the oracle's restatement of the reference projection (the
+    reference's FP32 aggregation-multigrid CG, closed boundaries: the
+    reference has no outlet) timed as whole projections of the workload on
+    every host thread, one untimed then two timed.  `vs_cpu_reference` sets
+    the GPU legs against it: the outlet headline, and the GB300 solver on the
+    same closed problem.
+
+    accuracy: the FP64 oracle (onat_project, 1e-12) solves the workload and
+    checks the GPU outputs of `runs`: max and relative-L2 errors of the
+    pressure and of the face velocities (all three arrays together)."""
+    import numpy as np
+
+    nx, ny, nz = case["dims"]
+    threads = os.cpu_count() or 1
+    cref = CpuReference(case, threads, args.tol)
+    secs, res = cref.projections(2, warmup=1)
+    cpu_s = statistics.median(secs)
+    line["cpu_baseline"] = {
+        "value": 1.0 / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
+        "sample": f"2 whole projections (after 1 untimed) of the oracle's restatement of the reference FP32 "
+                  f"multigrid CG on {args.workload} {nx}x{ny}x{nz}, closed boundaries (the reference has no outlet), "
+                  f"to {args.tol:g}: {res.iterations} CG iterations each; {threads} OpenMP threads",
+        "seconds_per_projection": cpu_s, "iterations": int(res.iterations), "status": int(res.status)}
+    if "topology" in line:
+        line["topology"]["host_search_ms"] = cref.anchors_s * 1e3
+        line["topology"]["host_search"] = "the reference's anchors() breadth-first search (oracle), 1 thread"
+    cpu_rate = 1.0 / cpu_s
+    ratios = {"outlet_over_closed_cpu": line["value"] / cpu_rate}
+    if "e2e" in line:
+        ratios["outlet_e2e_over_closed_cpu"] = line["e2e"]["value"] / cpu_rate
+    if "closed256" in line:
+        ratios["closed_over_closed_cpu"] = line["closed256"]["projections_per_s"] / cpu_rate
+        ratios["closed_e2e_over_closed_cpu"] = line["closed256"]["e2e"]["value"] / cpu_rate
+    line["vs_cpu_reference"] = ratios
+    # accuracy against the FP64 oracle
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    g = oracle.grid(nx, ny, nz, case["h"], case["rho_liquid"], case["rho_air"], case["periodic"], case["outlet"])
+    t0 = time.perf_counter()
+    ref = oracle.project(g, case["alpha"], case["solid"], case["u"], case["v"], case["w"], case["dt"], 1e-12)
+    t_ref = time.perf_counter() - t0
+    ref_u = np.concatenate([ref[k] for k in "uvw"])
+    ref_p = ref["p"]
+    acc = {"oracle": f"FP64 onat_project to 1e-12 ({ref['iterations']} iterations, {t_ref:.1f} s on {threads} threads)",
+           "pressure_max": float(np.abs(ref_p).max()), "velocity_max": float(np.abs(ref_u).max())}
+    for (prec, tol), r in runs.items():
+        gu = np.concatenate([r[k].reshape(-1).astype(np.float64) for k in "uvw"])
+        gp = r["p"].reshape(-1).astype(np.float64)
+        acc[f"{prec}@{tol:g}"] = {
+            "iterations": r["iterations"], "true_relative_residual": r["true_relative_residual"],
+            "p_max_abs_error": float(np.abs(gp - ref_p).max()),
+            "p_rel_l2_error": float(np.linalg.norm(gp - ref_p) / np.linalg.norm(ref_p)),
+            "u_max_abs_error": float(np.abs(gu - ref_u).max()),
+            "u_rel_l2_error": float(np.linalg.norm(gu - ref_u) / np.linalg.norm(ref_u))}
+    line["accuracy"] = acc
 
 
 def projection_bytes(n, iterations, refinements, precision):
@@ -661,26 +742,15 @@ def run_reference(args):
     case = synth.make_case(args.workload, seed=args.seed)
     nx, ny, nz = case["dims"]
     threads = os.cpu_count() or 1
-    k_ref = reference_iterations(args.workload, args.tol)
-    if k_ref is None:
-        print(json.dumps({"impl": "reference", "unavailable": f"no recorded reference iteration count for "
-                                                              f"{args.workload} at {args.tol:g}"}))
-        return
     cref = CpuReference(case, threads, args.tol)
-    setup, per_it, _ = cref.calibrate()
-    # Each step: the reference's set-up and first two CG iterations, timed,
-    # plus the remaining iterations at the calibrated per-iteration cost.
-    k_step = 2
-    secs = []
-    for k in range(args.warmup + args.steps):
-        t_step, res = cref.run(k_step)
-        if k >= args.warmup:
-            secs.append(t_step + (k_ref - k_step) * per_it)
-    s_per = statistics.median(secs)
-    value = 1.0 / s_per
-    sample = (f"per step: oracle restatement of the reference FP32 multigrid CG on {nx}x{ny}x{nz} (closed boundaries), "
-              f"set-up + {k_step} CG iterations timed, + {k_ref - k_step} iterations at the calibrated {per_it:.2f} s "
-              f"(the reference needs {k_ref} iterations for {args.tol:g}); {threads} OpenMP threads")
+    # Each step: one whole projection of the reference algorithm (coefficient
+    # cache, multigrid build, every CG iteration to the tolerance).
+    secs, res = cref.projections(args.steps, warmup=args.warmup)
+    total = sum(secs)
+    value = args.steps / total
+    sample = (f"per step: one whole projection by the oracle's restatement of the reference FP32 multigrid CG on "
+              f"{nx}x{ny}x{nz} (closed boundaries), {res.iterations} CG iterations to {args.tol:g} "
+              f"(status {res.status}); {threads} OpenMP threads")
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -689,7 +759,7 @@ def run_reference(args):
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": 1000.0 * s_per,
+        "ms_per_step": 1000.0 * total / args.steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -697,7 +767,8 @@ def run_reference(args):
         "data": "synthetic (seeded jet256 fields)",
         "config": {"workload": f"{args.workload}: {nx}x{ny}x{nz} cells, closed boundaries (the reference has no outlet), "
                                f"tol {args.tol:g}",
-                   "iterations": k_ref, "setup_seconds": setup, "seconds_per_iteration": per_it},
+                   "iterations": int(res.iterations), "relative_residual": float(res.residual),
+                   "seconds_per_projection": [round(x, 3) for x in secs]},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

@@ -77,7 +77,7 @@ def _stale() -> bool:
     t = os.path.getmtime(LIB_PATH)
     return any(
         os.path.getmtime(os.path.join(HERE, f)) > t
-        for f in ("oracle_ref.c", "oracle_native.c", "oracle_em.c", "mhd_oracle.h")
+        for f in ("oracle_ref.c", "oracle_native.c", "oracle_em.c", "mhd_oracle.h", "Makefile")
     )
 
 

@@ -103,6 +103,78 @@ static float face_density(const state *s, ivec3 pos, uint32_t axis) {
     left.v[axis] -= 1;
     return 0.5f * (density(s, left) + density(s, pos));
 }
+/* ------------------------------------------------ interior fast paths
+ * For a cell whose six neighbours all lie inside the grid no coordinate
+ * wraps, so the face and neighbour records sit at fixed offsets.  The *_fast
+ * helpers evaluate the same expressions as the general functions, in the
+ * same order, so their results are bit-identical; they only skip the
+ * per-neighbour coordinate arithmetic.  Cells on the grid's shell take the
+ * general path.  Neighbour order: -x, +x, -y, +y, -z, +z. */
+/* the position of cell i + 1 from that of cell i (x-fastest order) */
+static void next3(ivec3 *q, const uint32_t *d) {
+    if (++q->v[0] == (int32_t)d[0]) {
+        q->v[0] = 0;
+        if (++q->v[1] == (int32_t)d[1]) {
+            q->v[1] = 0;
+            q->v[2]++;
+        }
+    }
+}
+static int interior3(const uint32_t *d, ivec3 q) {
+    return q.v[0] >= 1 && q.v[0] + 1 < (int32_t)d[0] && q.v[1] >= 1 && q.v[1] + 1 < (int32_t)d[1] &&
+           q.v[2] >= 1 && q.v[2] + 1 < (int32_t)d[2];
+}
+static void cell_offsets(const uint32_t *d, int64_t co[6]) {
+    const int64_t sy = d[0], sz = (int64_t)d[0] * d[1];
+    co[0] = -1; co[1] = 1; co[2] = -sy; co[3] = sy; co[4] = -sz; co[5] = sz;
+}
+/* offset of the face record crossed towards each neighbour from the cell's
+ * own (low) face record, in a grid of face records of extents f */
+static void face_offsets(const uint32_t *f, int64_t fo[6]) {
+    fo[0] = 0; fo[1] = 1; fo[2] = 0; fo[3] = f[0]; fo[4] = 0; fo[5] = (int64_t)f[0] * f[1];
+}
+/* sum over the six faces of cell i with a positive mobility beta (lane
+ * `axis` of the face record) of beta * (center - neighbour value), in the
+ * order -x, +x, -y, +y, -z, +z: the loop of apply (solver.wgsl:78-92) and of
+ * the fine-level action (multigrid.wgsl:33-49).  The face records have
+ * extents f (4 lanes each, starting at record fi); the values have stride
+ * `vs` and cell extents d. */
+static inline float stencil7(const float *rec, int64_t fi, const uint32_t *f, const float *val, int64_t vs,
+                             uint32_t i, const uint32_t *d, float center) {
+    const int64_t sy = d[0], sz = (int64_t)d[0] * d[1], fy = f[0], fz = (int64_t)f[0] * f[1];
+    const int64_t ii = i;
+    float out = 0.0f, beta;
+    beta = rec[LANES * fi + 0];
+    if (beta > 0.0f) out += beta * (center - val[vs * (ii - 1)]);
+    beta = rec[LANES * (fi + 1) + 0];
+    if (beta > 0.0f) out += beta * (center - val[vs * (ii + 1)]);
+    beta = rec[LANES * fi + 1];
+    if (beta > 0.0f) out += beta * (center - val[vs * (ii - sy)]);
+    beta = rec[LANES * (fi + fy) + 1];
+    if (beta > 0.0f) out += beta * (center - val[vs * (ii + sy)]);
+    beta = rec[LANES * fi + 2];
+    if (beta > 0.0f) out += beta * (center - val[vs * (ii - sz)]);
+    beta = rec[LANES * (fi + fz) + 2];
+    if (beta > 0.0f) out += beta * (center - val[vs * (ii + sz)]);
+    return out;
+}
+static float density_at(const state *s, uint32_t i) {
+    float t = s->occ[i];
+    return s->p->surface[1] * (1.0f - t) + s->p->physical[3] * t;
+}
+/* mobility() of the face between cells iL (low side) and iR, both inside
+ * the grid (the face is open). */
+static float mobility_cells(const state *s, uint32_t iL, uint32_t iR) {
+    const oref_params *p = s->p;
+    float beta = 1.0f;
+    if (p->surface[0] > 0.5f) beta = p->physical[3] / (0.5f * (density_at(s, iL) + density_at(s, iR)));
+    if (p->flags[3] == 0u) return beta;
+    if (s->mask[iR] == 0u || s->mask[iL] == 0u) return 0.0f;
+    float f = fminf(s->phase[iR], s->phase[iL]);
+    float drag = p->solve[3] * (1.0f - f) * (1.0f - f) / (f * f * f + 1e-3f);
+    return beta / (1.0f + p->physical[1] * drag);
+}
+
 /* mobility(): :43-51 */
 static float mobility(const state *s, ivec3 pos, uint32_t axis) {
     const oref_params *p = s->p;
@@ -125,6 +197,17 @@ static int pinned_anchor(const state *s, uint32_t i) {
 /* diagonal(): :60-64 */
 static float diagonal(const state *s, ivec3 pos) {
     float d = 0.0f;
+    if (interior3(s->p->dims, pos)) {
+        const uint32_t i = idx3(pos, s->p->dims);
+        int64_t co[6];
+        cell_offsets(s->p->dims, co);
+        for (int t = 0; t < 6; t++) {
+            const uint32_t j = (uint32_t)((int64_t)i + co[t]);
+            if (s->mask[j] != 0u) d += (t & 1) ? mobility_cells(s, i, j) : mobility_cells(s, j, i);
+        }
+        if (pinned_anchor(s, i)) return 1.0f;
+        return fmaxf(d, 1e-30f);
+    }
     for (uint32_t axis = 0; axis < 3; axis++)
         for (int sign = -1; sign <= 1; sign += 2) {
             ivec3 q = pos;
@@ -140,6 +223,22 @@ static float diagonal(const state *s, ivec3 pos) {
 }
 /* laplacian(): :65-69 */
 static float laplacian(const state *s, ivec3 pos, uint32_t kind) {
+    if (interior3(s->p->dims, pos)) {
+        const uint32_t i = idx3(pos, s->p->dims), k = kind == 0u ? 0u : 2u;
+        const float *w = s->work;
+        const float center = s->mask[i] != 0u ? w[LANES * i + k] : 0.0f;
+        float out = 0.0f;
+        int64_t co[6];
+        cell_offsets(s->p->dims, co);
+        for (int t = 0; t < 6; t++) {
+            const uint32_t j = (uint32_t)((int64_t)i + co[t]);
+            if (s->mask[j] != 0u) {
+                const float beta = (t & 1) ? mobility_cells(s, i, j) : mobility_cells(s, j, i);
+                out += beta * (center - w[LANES * j + k]);
+            }
+        }
+        return out;
+    }
     float center = potential(s, pos, kind), out = 0.0f;
     for (uint32_t axis = 0; axis < 3; axis++)
         for (int sign = -1; sign <= 1; sign += 2) {
@@ -160,6 +259,12 @@ static float cached_mobility(const state *s, ivec3 pos, uint32_t axis) {
 static float cached_diagonal(const state *s, uint32_t i) { return s->velocity[LANES * i + 3]; }
 static float apply_cached(const state *s, ivec3 pos, uint32_t kind) {
     if (pinned_anchor(s, idx3(pos, s->p->dims))) return potential(s, pos, kind);
+    if (interior3(s->p->dims, pos) && s->mask[idx3(pos, s->p->dims)] != 0u) {
+        const uint32_t i = idx3(pos, s->p->dims), k = kind == 1u ? 2u : 0u;
+        const int64_t fi = idx3(pos, s->p->faces);
+        const float *c = s->velocity, *w = s->work;
+        return stencil7(c, fi, s->p->faces, w + k, LANES, i, s->p->dims, w[LANES * i + k]);
+    }
     float center = potential(s, pos, kind), out = 0.0f;
     for (uint32_t axis = 0; axis < 3; axis++)
         for (int sign = -1; sign <= 1; sign += 2) {
@@ -178,6 +283,23 @@ static float apply_cached(const state *s, ivec3 pos, uint32_t kind) {
 /* divergence()/rhs(): :104-107 */
 static float divergence(const state *s, ivec3 pos, int star) {
     float sum = 0.0f;
+    if (interior3(s->p->dims, pos)) {
+        const uint32_t i = idx3(pos, s->p->dims);
+        const int64_t fi = idx3(pos, s->p->faces);
+        const float *f = star ? s->predicted : s->velocity;
+        int64_t co[6], fo[6];
+        cell_offsets(s->p->dims, co);
+        face_offsets(s->p->faces, fo);
+        const int ci = s->mask[i] != 0u;
+        for (uint32_t a = 0; a < 3; a++) {
+            const int lo = ci && s->mask[(int64_t)i + co[2 * a]] != 0u;
+            const int hi = ci && s->mask[(int64_t)i + co[2 * a + 1]] != 0u;
+            const float fh = hi ? f[LANES * (fi + fo[2 * a + 1]) + a] : 0.0f;
+            const float fl = lo ? f[LANES * fi + a] : 0.0f;
+            sum += fh - fl;
+        }
+        return sum / s->p->physical[0];
+    }
     for (uint32_t axis = 0; axis < 3; axis++) {
         ivec3 q = pos;
         q.v[axis] += 1;
@@ -226,8 +348,18 @@ static void k_pressure_coefficients(state *s) {
         uint32_t i = (uint32_t)ii;
         ivec3 pos = decode3(i, p->faces);
         float coeff[4] = {0, 0, 0, 0};
-        for (uint32_t axis = 0; axis < 3; axis++)
-            if (open_face(s, pos, axis)) coeff[axis] = mobility(s, pos, axis);
+        if (interior3(p->dims, pos)) {
+            const uint32_t c = idx3(pos, p->dims);
+            int64_t co[6];
+            cell_offsets(p->dims, co);
+            for (uint32_t axis = 0; axis < 3; axis++) {
+                const uint32_t l = (uint32_t)((int64_t)c + co[2 * axis]);
+                if (s->mask[l] != 0u && s->mask[c] != 0u) coeff[axis] = mobility_cells(s, l, c);
+            }
+        } else {
+            for (uint32_t axis = 0; axis < 3; axis++)
+                if (open_face(s, pos, axis)) coeff[axis] = mobility(s, pos, axis);
+        }
         if (i < p->dims[3] && s->mask[i] != 0u) coeff[3] = diagonal(s, decode3(i, p->dims));
         memcpy(s->velocity + LANES * i, coeff, sizeof coeff);
     }
@@ -271,11 +403,11 @@ static void k_pressure_refresh(state *s) {
 #pragma omp parallel for schedule(static)
     for (int64_t g = 0; g < (int64_t)s->groups; g++) {
         float red[256][4];
-        for (uint32_t l = 0; l < 256u; l++) {
+        ivec3 pos = decode3((uint32_t)g * 256u, p->dims);
+        for (uint32_t l = 0; l < 256u; l++, next3(&pos, p->dims)) {
             uint32_t i = (uint32_t)g * 256u + l;
             float sum[4] = {0, 0, 0, 0};
             if (i < p->dims[3] && s->mask[i] != 0u) {
-                ivec3 pos = decode3(i, p->dims);
                 float b = rhs(s, pos), r = b - apply_cached(s, pos, 0u), d = cached_diagonal(s, i);
                 s->work[LANES * i + 1] = r;
                 s->work[LANES * i + 2] = r / d;
@@ -311,11 +443,12 @@ static void k_pressure_apply(state *s) {
 #pragma omp parallel for schedule(static)
     for (int64_t g = 0; g < (int64_t)s->groups; g++) {
         float red[256][4];
-        for (uint32_t l = 0; l < 256u; l++) {
+        ivec3 pos = decode3((uint32_t)g * 256u, p->dims);
+        for (uint32_t l = 0; l < 256u; l++, next3(&pos, p->dims)) {
             uint32_t i = (uint32_t)g * 256u + l;
             float value = 0.0f;
             if (i < p->dims[3] && s->mask[i] != 0u && !conv) {
-                float a = apply_cached(s, decode3(i, p->dims), 1u);
+                float a = apply_cached(s, pos, 1u);
                 s->work[LANES * i + 3] = a;
                 value = s->work[LANES * i + 2] * a;
             }
@@ -441,11 +574,11 @@ static void k_pressure_check(state *s) {
 #pragma omp parallel for schedule(static)
     for (int64_t g = 0; g < (int64_t)s->groups; g++) {
         float red[256][4];
-        for (uint32_t l = 0; l < 256u; l++) {
+        ivec3 pos = decode3((uint32_t)g * 256u, p->dims);
+        for (uint32_t l = 0; l < 256u; l++, next3(&pos, p->dims)) {
             uint32_t i = (uint32_t)g * 256u + l;
             red[l][0] = red[l][1] = red[l][2] = red[l][3] = 0.0f;
             if (i < p->dims[3] && s->mask[i] != 0u) {
-                ivec3 pos = decode3(i, p->dims);
                 float b = -p->physical[0] * p->physical[0] * divergence(s, pos, 1);
                 float r = b - laplacian(s, pos, 0u);
                 red[l][1] = r * r;
@@ -469,14 +602,26 @@ static void k_correct(state *s) {
         uint32_t i = (uint32_t)ii;
         ivec3 pos = decode3(i, p->faces);
         float out[4] = {0, 0, 0, 0};
-        for (uint32_t axis = 0; axis < 3; axis++)
-            if (open_face(s, pos, axis)) {
-                ivec3 left = pos;
-                left.v[axis] -= 1;
-                out[axis] = face_value(s, pos, axis, 1) -
-                            mobility(s, pos, axis) * (potential(s, pos, 0u) - potential(s, left, 0u)) /
-                                p->physical[0];
+        if (interior3(p->dims, pos)) {
+            const uint32_t c = idx3(pos, p->dims);
+            int64_t co[6];
+            cell_offsets(p->dims, co);
+            for (uint32_t axis = 0; axis < 3; axis++) {
+                const uint32_t l = (uint32_t)((int64_t)c + co[2 * axis]);
+                if (s->mask[l] != 0u && s->mask[c] != 0u)
+                    out[axis] = s->predicted[LANES * i + axis] -
+                                mobility_cells(s, l, c) * (s->work[LANES * c] - s->work[LANES * l]) / p->physical[0];
             }
+        } else {
+            for (uint32_t axis = 0; axis < 3; axis++)
+                if (open_face(s, pos, axis)) {
+                    ivec3 left = pos;
+                    left.v[axis] -= 1;
+                    out[axis] = face_value(s, pos, axis, 1) -
+                                mobility(s, pos, axis) * (potential(s, pos, 0u) - potential(s, left, 0u)) /
+                                    p->physical[0];
+                }
+        }
         /* Each invocation writes only its own face record; the cache it
            reads (mobility is uncached here) is not used any more. */
         memcpy(s->velocity + LANES * i, out, sizeof out);
@@ -537,7 +682,25 @@ static float mg_solution(const struct oref_mg *mg, uint32_t i, uint32_t offset, 
 static float mg_action(const struct oref_mg *mg, const level_t *L, ivec3 q, const uint32_t *d,
                        uint32_t offset, int fine, int temp) {
     uint32_t i = idx3(q, d);
+    if (fine && interior3(d, q)) {
+        /* interior fast path (same operations, same order as below) */
+        const float *src = temp ? mg->temp : mg->work + 3;
+        const int64_t vs = temp ? 1 : LANES;
+        return stencil7(mg->cache, idx3(q, L->faces), L->faces, src, vs, i, d, src[vs * i]);
+    }
     float center = mg_solution(mg, i, offset, fine, temp), out = 0.0f;
+    if (interior3(d, q)) {
+        int64_t co[6];
+        cell_offsets(d, co);
+        out = mg->coeff[LANES * (offset + i) + 3] * center;
+        const uint32_t lane = temp ? 2u : 1u;
+        for (int t = 0; t < 6; t++) {
+            const int64_t f = (t & 1) ? (int64_t)i + co[t] : (int64_t)i;
+            const float beta = mg->coeff[LANES * (offset + f) + (t >> 1)];
+            if (beta > 0.0f) out += beta * (center - mg->value[LANES * (offset + (int64_t)i + co[t]) + lane]);
+        }
+        return out;
+    }
     if (fine) {
         for (uint32_t a = 0; a < 3; a++)
             for (int s = -1; s <= 1; s += 2) {
@@ -614,9 +777,10 @@ static void mg_jacobi(struct oref_mg *mg, const level_t *L, int temp) {
     const int fine = L->location[2] == 0u;
     const uint32_t off = L->location[0];
 #pragma omp parallel for schedule(static)
-    for (int64_t ii = 0; ii < (int64_t)L->dims[3]; ii++) {
-        uint32_t i = (uint32_t)ii;
-        ivec3 q = decode3(i, L->dims);
+    for (int64_t row = 0; row < (int64_t)L->dims[1] * L->dims[2]; row++)
+    for (uint32_t x = 0; x < L->dims[0]; x++) {
+        uint32_t i = x + L->dims[0] * (uint32_t)row;
+        ivec3 q = {{(int32_t)x, (int32_t)(row % L->dims[1]), (int32_t)(row / L->dims[1])}};
         float d, r;
         if (fine) {
             d = mg->cache[LANES * i + 3];
@@ -644,9 +808,10 @@ static void mg_restrict(struct oref_mg *mg, const level_t *L) {
     if (mg_converged(mg)) return;
     const int fine = L->location[2] == 1u;
 #pragma omp parallel for schedule(static)
-    for (int64_t ii = 0; ii < (int64_t)L->dims[3]; ii++) {
-        uint32_t i = (uint32_t)ii;
-        ivec3 q = decode3(i, L->dims);
+    for (int64_t row = 0; row < (int64_t)L->dims[1] * L->dims[2]; row++)
+    for (uint32_t x = 0; x < L->dims[0]; x++) {
+        uint32_t i = x + L->dims[0] * (uint32_t)row;
+        ivec3 q = {{(int32_t)x, (int32_t)(row % L->dims[1]), (int32_t)(row / L->dims[1])}};
         float sum = 0.0f;
         for (int z = 0; z < 2; z++)
             for (int y = 0; y < 2; y++)
@@ -673,9 +838,10 @@ static void mg_restrict(struct oref_mg *mg, const level_t *L) {
 static void mg_prolong(struct oref_mg *mg, const level_t *L) {
     if (mg_converged(mg)) return;
 #pragma omp parallel for schedule(static)
-    for (int64_t ii = 0; ii < (int64_t)L->child[3]; ii++) {
-        uint32_t i = (uint32_t)ii;
-        ivec3 q = decode3(i, L->child);
+    for (int64_t row = 0; row < (int64_t)L->child[1] * L->child[2]; row++)
+    for (uint32_t x = 0; x < L->child[0]; x++) {
+        uint32_t i = x + L->child[0] * (uint32_t)row;
+        ivec3 q = {{(int32_t)x, (int32_t)(row % L->child[1]), (int32_t)(row / L->child[1])}};
         ivec3 par = {{q.v[0] / 2, q.v[1] / 2, q.v[2] / 2}};
         float correction = mg->value[LANES * (L->location[0] + idx3(par, L->dims)) + 1];
         if (L->location[2] == 1u) {
@@ -760,7 +926,9 @@ static void mg_diagonal_start(struct oref_mg *mg, const level_t *L) {
 static void mg_commit(struct oref_mg *mg, const level_t *L) {
     if (mg_converged(mg)) return;
     const uint32_t off = L->location[0];
-    for (uint32_t i = 0; i < L->dims[3]; i++) {
+#pragma omp parallel for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)L->dims[3]; ii++) {
+        const uint32_t i = (uint32_t)ii;
         if (L->location[2] == 0u) mg->work[LANES * i + 3] = mg->temp[i];
         else mg->value[LANES * (off + i) + 1] = mg->value[LANES * (off + i) + 2];
     }

@@ -336,3 +336,46 @@ def test_full_size_jet256_properties(gpu, precision):
     den = sum(float((y.double() ** 2).sum()) for y in (uo, vo, wo))
     assert math.sqrt(num / den) < 1e-6
     assert st.max_divergence < 1e-3 * float(torch.abs(us[2]).max()) / c["h"]
+
+
+_FP64_FULL = {}
+
+
+def _fp64_full(oracle_lib, c, name):
+    if name not in _FP64_FULL:
+        _FP64_FULL[name] = oracle_lib.project(ogrid(oracle_lib, c), c["alpha"], c["solid"], c["u"], c["v"], c["w"],
+                                              c["dt"], 1e-12)
+    return _FP64_FULL[name]
+
+
+FULL = [("jet64", "fp32"), ("jet128", "fp32"), ("jet256", "fp16"), ("jet256", "bf16")]
+
+
+@pytest.mark.parametrize("tol", [1e-6, 1e-8])
+@pytest.mark.parametrize("name,precision", FULL, ids=[f"{a}-{b}" for a, b in FULL])
+def test_full_size_configs_against_fp64(gpu, oracle_lib, name, precision, tol):
+    """The benchmark configurations at their full sizes against the FP64
+    oracle: 64^3 and 128^3 with FP32 levels (configurations 1 and 2), 256^3
+    with FP16 and BF16 levels (configuration 3), each at relative residuals
+    1e-6 and 1e-8.  Pressure and face velocities within 100 tol (relative
+    L2, plus a 1e-6 floor for FP32 rounding of the outputs); the largest
+    pointwise error within 1000 tol of the largest value."""
+    import mhdproj
+
+    torch = gpu
+    c = synth.make_case(name)
+    pr = make(mhdproj, c, precision=precision, rel_tol=tol)
+    a, s, us = tensors(torch, c)
+    pr.set_coefficients(a, s, c["rho_liquid"], c["rho_air"])
+    (uo, vo, wo), p, st = pr.project(us, c["dt"])
+    assert st.true_relative_residual <= tol
+    ref = _fp64_full(oracle_lib, c, name)
+    assert ref["status"] == 0
+    got_u = np.concatenate([x.cpu().numpy().reshape(-1).astype(np.float64) for x in (uo, vo, wo)])
+    ref_u = np.concatenate([ref[k] for k in "uvw"])
+    got_p = p.cpu().numpy().reshape(-1).astype(np.float64)
+    assert rel_l2(got_p, ref["p"]) < 100 * tol + 1e-6
+    assert rel_l2(got_u, ref_u) < 100 * tol + 1e-6
+    assert np.abs(got_p - ref["p"]).max() <= (1000 * tol + 1e-6) * np.abs(ref["p"]).max()
+    assert np.abs(got_u - ref_u).max() <= (1000 * tol + 1e-6) * np.abs(ref_u).max()
+    pr.close()

@@ -10,7 +10,11 @@ reference projection (FluidState::project, src/fluid/mod.rs:1015-1115, with
     norm, the reference's own acceptance measure and bound
     (src/fluid/multigrid/tests.rs:330-465);
   * pressure p = rho_l phi / dt in the reference's gauge (each component's
-    root cell at zero; the GB300 solver pins the same cell) within 2e-4.
+    root cell at zero; the GB300 solver pins the same cell) within 2e-4, or,
+    where the reference's FP32 solve is itself further than that from the
+    exact discrete pressure (the FP64 oracle), within that distance: the
+    GB300 result sits at the FP64 solution (1e-5) and the reference's own
+    solve error is all that separates the two.
 The reference restatement runs at 3e-6, close to its FP32 floor on the jets;
 the GB300 solver at 1e-8.  The thermal phase-drag mobility
 (solver.wgsl:46-50) is checked the same way, plus bit-exact coefficients
@@ -43,6 +47,28 @@ def _reference(oracle_lib, name, c, **kw):
     if key not in _REFERENCE:
         _REFERENCE[key] = R.run_oracle(oracle_lib, c, max_iterations=4000, **kw)
     return _REFERENCE[key]
+
+
+_FP64 = {}
+
+
+def _fp64(oracle_lib, name, c, phase=None, drag_rate=1e6):
+    """The FP64 oracle's projection of a case on closed boundaries (cached)."""
+    key = (name, phase is not None)
+    if key not in _FP64:
+        nx, ny, nz = c["dims"]
+        g = oracle_lib.grid(nx, ny, nz, c["h"], c["rho_liquid"], c["rho_air"], c["periodic"], outlet=False,
+                            single=not c["two_phase"], phase=phase, drag_rate=drag_rate if phase is not None else 0.0,
+                            dt=c["dt"] if phase is not None else 0.0)
+        _FP64[key] = oracle_lib.project(g, c["alpha"], c["solid"], c["u"], c["v"], c["w"], c["dt"], 1e-13)
+    return _FP64[key]
+
+
+def _check_pressure(got, ref, exact):
+    mask = ref["mask"]
+    own = _pressure_error(ref["p"], exact["p"], mask)  # the reference's own solve error
+    assert _pressure_error(got["p"], exact["p"], mask) < 1e-5
+    assert _pressure_error(got["p"], ref["p"], mask) <= max(2e-4, 1.05 * own + 1e-6)
 
 
 def _t(torch, a):
@@ -86,7 +112,7 @@ def test_gb300_projection_equals_the_references(gpu, oracle_lib, name, factory, 
     pr, got = _gb300(mhdproj, torch, c, precision)
     assert got["stats"].true_relative_residual <= 1e-8
     assert _velocity_error(got, ref, c) < 2e-4
-    assert _pressure_error(got["p"], ref["p"], ref["mask"]) < 2e-4
+    _check_pressure(got, ref, _fp64(oracle_lib, name, c))
     pr.close()
 
 
@@ -149,11 +175,8 @@ def test_phase_drag_projection(gpu, oracle_lib, name, factory, precision):
     pr, got = _gb300(mhdproj, torch, c, precision, phase=f)
     assert got["stats"].true_relative_residual <= 1e-8
     assert _velocity_error(got, ref, c) < 2e-4
-    assert _pressure_error(got["p"], ref["p"], ref["mask"]) < 2e-4
-    nx, ny, nz = c["dims"]
-    g = oracle_lib.grid(nx, ny, nz, c["h"], c["rho_liquid"], c["rho_air"], c["periodic"], outlet=False,
-                        single=not c["two_phase"], phase=f, drag_rate=1e6, dt=c["dt"])
-    nat = oracle_lib.project(g, c["alpha"], c["solid"], c["u"], c["v"], c["w"], c["dt"], 1e-13)
+    nat = _fp64(oracle_lib, name, c, phase=f)
+    _check_pressure(got, ref, nat)
     for k in "uvw":
         a, b = got[k].reshape(-1).astype(np.float64), nat[k]
         assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(b) + 1e-7 * np.linalg.norm(c[k])
