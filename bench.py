@@ -531,27 +531,30 @@ def run_ours(args):
         # as the reference arm, device-resident and end to end
         pc = mhdproj.PressureProjection(case["dims"], case["h"], outlet=False, precision=args.precision,
                                         rel_tol=args.tol)
-        for _ in range(2):
-            step(pc)
-        msc, stc = timed(pc, max(3, args.steps // 2))
-        msc /= len(stc)
-        for _ in range(2):
-            pc.project_host(h_alpha, h_solid, case["rho_liquid"], case["rho_air"], h_us, case["dt"], out=h_out,
-                            p_out=h_p)
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        for _ in range(ke):
-            pc.project_host(h_alpha, h_solid, case["rho_liquid"], case["rho_air"], h_us, case["dt"], out=h_out,
-                            p_out=h_p)
-        torch.cuda.synchronize(dev)
-        e2e_c = (time.perf_counter() - t0) / ke
-        line["closed256"] = {"workload": f"{args.workload}: {nx}x{ny}x{nz} cells, closed boundaries (the reference's), "
-                                         f"tol {args.tol:g}",
-                             "projections_per_s": 1000.0 / msc, "ms_per_step": msc, "iterations": stc[-1].iterations,
-                             "refinements": stc[-1].refinements,
-                             "true_relative_residual": stc[-1].true_relative_residual,
-                             "e2e": {"value": 1.0 / e2e_c, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                                     "d2h_bytes_per_step": int(d2h)}}
+        try:
+            for _ in range(2):
+                step(pc)
+            msc, stc = timed(pc, max(3, args.steps // 2))
+            msc /= len(stc)
+            for _ in range(2):
+                pc.project_host(h_alpha, h_solid, case["rho_liquid"], case["rho_air"], h_us, case["dt"], out=h_out,
+                                p_out=h_p)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            for _ in range(ke):
+                pc.project_host(h_alpha, h_solid, case["rho_liquid"], case["rho_air"], h_us, case["dt"], out=h_out,
+                                p_out=h_p)
+            torch.cuda.synchronize(dev)
+            e2e_c = (time.perf_counter() - t0) / ke
+            line["closed256"] = {"workload": f"{args.workload}: {nx}x{ny}x{nz} cells, closed boundaries (the "
+                                             f"reference's), tol {args.tol:g}",
+                                 "projections_per_s": 1000.0 / msc, "ms_per_step": msc,
+                                 "iterations": stc[-1].iterations, "refinements": stc[-1].refinements,
+                                 "true_relative_residual": stc[-1].true_relative_residual,
+                                 "e2e": {"value": 1.0 / e2e_c, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                                         "d2h_bytes_per_step": int(d2h)}}
+        except mhdproj.ProjectionError as exc:
+            line["closed256"] = {"unavailable": str(exc)}
         pc.close()
         # roofline of the dominant kernel (isolated launches, CUDA events on the library stream)
         pr.set_coefficients(alpha, solid, case["rho_liquid"], case["rho_air"])
@@ -674,7 +677,7 @@ def cpu_leg(args, case, line, runs):
     ratios = {"outlet_over_closed_cpu": line["value"] / cpu_rate}
     if "e2e" in line:
         ratios["outlet_e2e_over_closed_cpu"] = line["e2e"]["value"] / cpu_rate
-    if "closed256" in line:
+    if "projections_per_s" in line.get("closed256", {}):
         ratios["closed_over_closed_cpu"] = line["closed256"]["projections_per_s"] / cpu_rate
         ratios["closed_e2e_over_closed_cpu"] = line["closed256"]["e2e"]["value"] / cpu_rate
     line["vs_cpu_reference"] = ratios

@@ -95,7 +95,9 @@ typedef struct {
     uint32_t max_iterations;/* FluidConfig::max_iterations (all refinement passes) */
     int32_t max_refinements;/* GB300 solver: FP64 refinement passes (>= 1) */
     int32_t two_phase;      /* reference solver: SurfaceConfig::enabled (density from the liquid fraction) */
-    int32_t gauge;          /* reference solver: -1 automatic, 0 pinned cells, 1 mean-free if connected */
+    int32_t gauge;          /* -1 automatic, 0 pinned cells, 1 mean-free if connected.  Both solvers take the
+                               mean-free gauge for one closed component (GB300: the result is zero at the
+                               component's first cell; the adjoint needs gauge 0 or an outlet) */
     int32_t compute_divergence; /* fill max/RMS divergence of the projected velocity in the stats */
 } mhdproj_options;
 
@@ -139,10 +141,14 @@ int mhdproj_set_stream(mhdproj_ctx *ctx, void *stream);
 int mhdproj_set_coefficients(mhdproj_ctx *ctx, const float *alpha, const uint8_t *solid, float rho_liquid,
                              float rho_air);
 
-/* Reference solver only: the thermal phase-fraction drag of mobility()
- * (solver.wgsl:46-50), beta / (1 + dt * rate (1-f)^2 / (f^3 + 1e-3)) with f the
- * smaller phase fraction (FluidCell.reserved.y) of the two cells.  Pass
- * phase = NULL to disable.  Takes effect at the next mhdproj_set_coefficients. */
+/* The thermal phase-fraction drag of mobility() (solver.wgsl:46-50),
+ * beta / (1 + dt * rate (1-f)^2 / (f^3 + 1e-3)) with f the smaller phase
+ * fraction (FluidCell.reserved.y) of the two cells; phase is a device array of
+ * one FP32 per cell, copied by the call.  Pass phase = NULL to disable.  The
+ * reference solver applies it at the next mhdproj_set_coefficients; the GB300
+ * solver rebuilds its coefficients at once if they are set.  A projection,
+ * adjoint or chain with another dt is refused, as the reference rebuilds its
+ * coefficients with the step's dt. */
 int mhdproj_set_phase_drag(mhdproj_ctx *ctx, const float *phase, float drag_rate, float dt);
 
 /* FluidState::project + correct (src/fluid/mod.rs:1015-1115, solver.wgsl:245-250):

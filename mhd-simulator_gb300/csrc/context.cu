@@ -53,6 +53,9 @@ struct mhdproj_ctx {
     TopoCounts* d_topo = nullptr;
     TopoCounts* h_topo = nullptr;
     uint32_t components = 0, pinned = 0;
+    // one component without an outlet: mean-free pressure, gauge at its root
+    bool meanfree = false;
+    long long root = -1;
     long long n_active = 0;
     bool have_topology = false, have_coef = false;
     float* alpha = nullptr;
@@ -225,6 +228,7 @@ static int build_levels(mhdproj_ctx* ctx) {
     P.precision = ctx->opt.precision;
     P.sc = ctx->sc;
     P.prolong = 2.0f;
+    P.pin_coarse = -1;
     P.staged = ctx->staged;
     int d[3] = {(int)ctx->grid.nx, (int)ctx->grid.ny, (int)ctx->grid.nz};
     const int per = (int)ctx->grid.periodic;
@@ -469,6 +473,16 @@ __global__ void k_compare_u8(const uint8_t* a, const uint8_t* b, long long n, in
     if (__syncthreads_or(diff) && threadIdx.x == 0) atomicOr(flag, 1);
 }
 
+// Mean-free gauge: the single gauge cell (class 2) becomes an active cell;
+// its index is recorded.
+__global__ void k_unpin(uint8_t* cls, long long n, int* root) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        if (cls[i] == 2) {
+            cls[i] = 1;
+            *root = (int)i;
+        }
+}
+
 static int update_topology(mhdproj_ctx* ctx, const uint8_t* solid, bool* changed) {
     *changed = !ctx->have_topology;
     if (ctx->have_topology) {
@@ -505,7 +519,36 @@ static int update_topology(mhdproj_ctx* ctx, const uint8_t* solid, bool* changed
         ref_set_topology_device(ctx->ref, ctx->components, (uint32_t)t.fluid);
     } else {
         ctx->pinned = (uint32_t)t.pinned;
-        ctx->n_active = (long long)(t.fluid - t.pinned);
+        ctx->meanfree = false;
+        ctx->root = -1;
+        ctx->mg.pin_coarse = -1;
+        // One component that needs a gauge: mean-free pressure, as
+        // configure_pressure_projection chooses for one connected component
+        // (src/fluid/mod.rs:978-1002).  The operator is singular with the
+        // constant null space; its root cell (the reference's anchor) fixes
+        // the gauge of the result, and the coarsest multigrid solve pins the
+        // coarsest cell that holds it.  A single pinned cell would leave a
+        // near-null mode of eigenvalue ~1/N that FP16/BF16 level rounding
+        // cannot resolve.
+        if (t.components == 1 && t.pinned == 1 && ctx->opt.gauge != 0) {
+            k_unpin<<<152 * 4, 256, 0, ctx->stream>>>(ctx->d_cls, ctx->n, ctx->d_flag);
+            ctx->launches += 1;
+            CK(cudaGetLastError());
+            CK(cudaMemcpyAsync(ctx->h_flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            rc = wait_stream(ctx);
+            if (rc) return rc;
+            ctx->meanfree = true;
+            ctx->pinned = 0;
+            ctx->root = *ctx->h_flag;
+            if (ctx->use_mg) {
+                const int L = ctx->mg.nlevels - 1;
+                const long long nx = ctx->grid.nx, ny = ctx->grid.ny;
+                const long long x = ctx->root % nx, y = (ctx->root / nx) % ny, z = ctx->root / (nx * ny);
+                const Grid3& c = ctx->mg.lv[L].L.g;
+                ctx->mg.pin_coarse = (int)((x >> L) + c.nx * ((y >> L) + c.ny * (z >> L)));
+            }
+        }
+        ctx->n_active = (long long)(t.fluid - ctx->pinned);
     }
     ctx->have_topology = true;
     return 0;
@@ -791,12 +834,40 @@ static void begin_scalars(mhdproj_ctx* ctx) {
     launch_init_scalars(ctx->sc, tol2, abs_floor, 1e-10, (int)ctx->opt.max_iterations, ctx->stream);
 }
 
+static const char* const MEANFREE_ADJOINT =
+    "the adjoint needs an outlet or pinned gauges; this domain is one closed component (mean-free pressure): "
+    "create the context with mhdproj_options.gauge = 0";
+
 // The phase-drag mobility depends on dt; a call with another dt is refused
 // (the reference rebuilds its coefficients with the step's dt).
 static int check_drag_dt(mhdproj_ctx* ctx, float dt) {
     if (ctx->drag && dt != ctx->drag_dt)
         return fail(ctx, MHDPROJ_ERR_INVALID,
                     "the phase-drag mobility was set for a different dt; call mhdproj_set_phase_drag again");
+    return 0;
+}
+
+// Mean-free gauge: the potential is defined up to a constant; take the one
+// that is zero at the root cell (the reference's pressure of the mean-free
+// mode, p = rho_l (phi - phi_anchor) / dt, src/fluid/solver.wgsl:269-270).
+// The root itself is left alone while the others read it, then zeroed.
+__global__ void k_shift_gauge(Grid3 g, const uint8_t* __restrict__ cls, float* __restrict__ hi,
+                              float* __restrict__ lo, long long root) {
+    const df pr = {hi[root], lo[root]};
+    const long long n = g.n();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        if (i == root || cls[i] == 0) continue;
+        const df d = df_sub(df{hi[i], lo[i]}, pr);
+        hi[i] = d.hi;
+        lo[i] = d.lo;
+    }
+}
+static int shift_gauge(mhdproj_ctx* ctx) {
+    k_shift_gauge<<<152 * 8, 256, 0, ctx->stream>>>(ctx->L.g, ctx->d_cls, ctx->phi_hi, ctx->phi_lo, ctx->root);
+    ctx->launches += 1;
+    CK(cudaGetLastError());
+    CK(cudaMemsetAsync(ctx->phi_hi + ctx->root, 0, sizeof(float), ctx->stream));
+    CK(cudaMemsetAsync(ctx->phi_lo + ctx->root, 0, sizeof(float), ctx->stream));
     return 0;
 }
 
@@ -817,6 +888,10 @@ static int project_gb300(mhdproj_ctx* ctx, const float* us, const float* vs, con
     mhdproj_stats local{};
     int rc = solve(ctx, ctx->phi_hi, ctx->phi_lo, &local, from_zero);
     if (rc) return rc;
+    if (ctx->meanfree) {
+        rc = shift_gauge(ctx);
+        if (rc) return rc;
+    }
     launch_correct(ctx->L, F, ctx->phi_hi, ctx->phi_lo, us, vs, ws, uo, vo, wo, po, dt, ctx->stream);
     ctx->launches += 1;
     if (ctx->opt.compute_divergence) {
@@ -962,6 +1037,7 @@ extern "C" int mhdproj_project_vjp(mhdproj_ctx* ctx, const float* gux, const flo
     if (!gux || !guy || !guz || !ogx || !ogy || !ogz) return fail(ctx, MHDPROJ_ERR_INVALID, "face arrays must not be NULL");
     if (!(dt > 0.f)) return fail(ctx, MHDPROJ_ERR_INVALID, "dt must be positive");
     if (int rc = check_drag_dt(ctx, dt)) return rc;
+    if (ctx->meanfree) return fail(ctx, MHDPROJ_ERR_INVALID, MEANFREE_ADJOINT);
     CK(cudaEventRecord(ctx->ev_a, ctx->stream));
     mhdproj_stats local{};
     int rc = vjp_gb300(ctx, gux, guy, guz, gp, dt, ogx, ogy, ogz, &local);
@@ -1005,6 +1081,7 @@ extern "C" int mhdproj_chain_forward(mhdproj_ctx* ctx, const float* u0x, const f
     if (!ctx->have_coef) return fail(ctx, MHDPROJ_ERR_STATE, "call mhdproj_set_coefficients before the chain");
     if (steps < 1 || checkpoint_every < 1 || !(dt > 0.f)) return fail(ctx, MHDPROJ_ERR_INVALID, "steps, checkpoint_every and dt must be positive");
     if (int rc = check_drag_dt(ctx, dt)) return rc;
+    if (ctx->meanfree) return fail(ctx, MHDPROJ_ERR_INVALID, MEANFREE_ADJOINT);
     int rc = chain_alloc(ctx);
     if (rc) return rc;
     const long long m[3] = {ctx->nfx, ctx->nfy, ctx->nfz};

@@ -137,6 +137,7 @@ struct MGPlan {
     BottomPlan bottom;
     float4* bottom_img;  // the bottom sub-cycle's shared-memory image (bottom.img_floats floats)
     float* e0;         // fine-level pre-smoothed correction of the fused passes
+    int pin_coarse;    // mean-free gauge: the coarsest cell held at zero in the coarsest solve (-1: none)
 };
 void mg_build(const MGPlan& P, cudaStream_t s);
 // single fine-level stages, for measurement

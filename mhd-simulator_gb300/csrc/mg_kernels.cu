@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(TILE_THREADS) k_mg_build(Grid3 gf, Grid3 gc, c
 // Spreading the columns over blocks spreads the FP64 work over SMs; each
 // block's factorisation is the same computation, so the columns agree.
 __global__ void __launch_bounds__(256) k_coarse_invert(Grid3 g, const float4* __restrict__ coef,
-                                                       float* __restrict__ ainv) {
+                                                       float* __restrict__ ainv, int pin) {
     extern __shared__ double A[];  // m x m, then y/x vectors
     const int m = g.nx * g.ny * g.nz;
     const int t = threadIdx.x, nt = blockDim.x;
@@ -374,7 +374,7 @@ __global__ void __launch_bounds__(256) k_coarse_invert(Grid3 g, const float4* __
             }
         }
         A[t * m + t] += d;
-        active[t] = d > 0.0;
+        active[t] = d > 0.0 && t != pin;  // a pinned cell (mean-free gauge) is held at zero
     }
     __syncthreads();
     if (t < m && !active[t]) {
@@ -859,7 +859,7 @@ void mg_build(const MGPlan& P, cudaStream_t s) {
     }
     const MGLevel& K = P.lv[P.nlevels - 1];
     const size_t smem = ((size_t)P.m * P.m + P.m) * sizeof(double);
-    k_coarse_invert<<<P.m, 256, smem, s>>>(K.L.g, K.coef32, P.ainv);
+    k_coarse_invert<<<P.m, 256, smem, s>>>(K.L.g, K.coef32, P.ainv, P.pin_coarse);
     if (P.bottom_from > 0 && P.bottom_img) {
         if (P.precision == 1) k_bottom_image<1><<<1, BOTTOM_THREADS, P.bottom_smem, s>>>(P.bottom, P.bottom_img);
         else if (P.precision == 2) k_bottom_image<2><<<1, BOTTOM_THREADS, P.bottom_smem, s>>>(P.bottom, P.bottom_img);

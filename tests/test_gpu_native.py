@@ -63,20 +63,27 @@ def test_coefficients_bit_exact(gpu, oracle_lib, name, scale):
     assert np.array_equal(m.astype(np.uint8), cls)
 
 
-def test_coefficients_bit_exact_periodic_pinned(gpu, oracle_lib):
+@pytest.mark.parametrize("gauge", [0, -1], ids=["pinned", "mean_free"])
+def test_coefficients_bit_exact_periodic_closed(gpu, oracle_lib, gauge):
+    """One closed component: pinned at its root with gauge 0; by default the
+    mean-free gauge, with no pinned cell and so no reactions."""
     import mhdproj
 
     torch = gpu
     c = periodic_case()
-    pr = make(mhdproj, c)
+    pr = make(mhdproj, c, gauge=gauge)
     a, s, _ = tensors(torch, c)
     pr.set_coefficients(a, s, c["rho_liquid"], c["rho_air"])
     g = ogrid(oracle_lib, c)
     pinned, cls = oracle_lib.classify(g, c["solid"])
-    assert pinned >= 1
+    assert pinned == 1
+    if gauge != 0:
+        cls[cls == 2] = 1
     coef, _ = oracle_lib.coefficients(g, c["alpha"], cls)
     got = pr.coefficients().cpu().numpy().reshape(-1, 4)
     assert np.array_equal(got.view(np.uint32), coef.view(np.uint32))
+    m, _ = pr.topology()
+    assert np.array_equal(m.astype(np.uint8), cls)
 
 
 @pytest.mark.parametrize("name,scale", CASES)
@@ -126,19 +133,23 @@ def test_projection_matches_fp64_oracle(gpu, oracle_lib, precision, name, scale,
     assert st.rms_divergence <= max(10 * tol, 1e-6) * div0
 
 
+@pytest.mark.parametrize("gauge", [0, -1], ids=["pinned", "mean_free"])
 @pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16"])
-def test_projection_pinned_periodic(gpu, oracle_lib, precision):
+def test_projection_periodic_closed(gpu, oracle_lib, precision, gauge):
+    """Velocities do not depend on the gauge; the pressure of either gauge is
+    zero at the component's root, like the FP64 oracle's."""
     import mhdproj
 
     torch = gpu
     c = periodic_case()
-    pr = make(mhdproj, c, precision=precision, rel_tol=1e-8)
+    pr = make(mhdproj, c, precision=precision, rel_tol=1e-8, gauge=gauge)
     a, s, us = tensors(torch, c)
     pr.set_coefficients(a, s, c["rho_liquid"], c["rho_air"])
     (uo, vo, wo), p, st = pr.project(us, c["dt"])
     assert st.true_relative_residual <= 1e-8
     ref = oracle_lib.project(ogrid(oracle_lib, c), c["alpha"], c["solid"], c["u"], c["v"], c["w"], c["dt"], 1e-13)
     assert rel_l2(uo.cpu().numpy(), ref["u"]) < 1e-5
+    assert rel_l2(p.cpu().numpy(), ref["p"]) < 1e-5
 
 
 @pytest.mark.parametrize("precision", ["fp32", "fp16", "bf16"])
@@ -379,3 +390,20 @@ def test_full_size_configs_against_fp64(gpu, oracle_lib, name, precision, tol):
     assert np.abs(got_p - ref["p"]).max() <= (1000 * tol + 1e-6) * np.abs(ref["p"]).max()
     assert np.abs(got_u - ref_u).max() <= (1000 * tol + 1e-6) * np.abs(ref_u).max()
     pr.close()
+
+
+def test_mean_free_gauge_refuses_the_adjoint(gpu):
+    """One closed component takes the mean-free gauge; the adjoint is defined
+    for outlets and pinned gauges and says so."""
+    import mhdproj
+
+    torch = gpu
+    c = periodic_case()
+    pr = make(mhdproj, c, precision="fp16", rel_tol=1e-6)
+    a, s, us = tensors(torch, c)
+    pr.set_coefficients(a, s, c["rho_liquid"], c["rho_air"])
+    with pytest.raises(mhdproj.ProjectionError, match="gauge = 0"):
+        pr.vjp(us, None, c["dt"])
+    pinned = make(mhdproj, c, precision="fp16", rel_tol=1e-6, gauge=0)
+    pinned.set_coefficients(a, s, c["rho_liquid"], c["rho_air"])
+    pinned.vjp(us, None, c["dt"])
