@@ -47,6 +47,7 @@ struct Scalars {
     int total_iterations;
     int nonfinite;      // a reduction produced NaN/Inf
     int breakdown;      // p.Ap <= 0
+    int stalled;        // a bounded device-side wait ran out (the solve stops)
     unsigned int ticket[12];
 };
 

@@ -200,7 +200,10 @@ static int wait_stream(mhdproj_ctx* ctx, double timeout_s = 600.0) {
 }
 static int read_scalars(mhdproj_ctx* ctx) {
     CK(cudaMemcpyAsync(ctx->h_sc, ctx->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, ctx->stream));
-    return wait_stream(ctx);
+    const int rc = wait_stream(ctx);
+    if (rc == 0 && ctx->h_sc->stalled)
+        return fail(ctx, MHDPROJ_ERR_TIMEOUT, "a bounded wait for staged data inside a smoothing pass expired");
+    return rc;
 }
 
 // ------------------------------------------------------------ options

@@ -164,6 +164,18 @@ void launch_search_spmv(const Launch& L, const float4* coef, const float* z, con
 void launch_accumulate_pipelined(const Launch& L, float* x_hi, float* x_lo, const float* x, const float* p0,
                                  const float* p1, const Scalars* sc, cudaStream_t s);
 cudaError_t mg_prepare_attributes();
+// The same two passes with TMA-staged planes (tma_fused.cu), for grids without
+// periodic axes whose rows are whole 16-byte multiples; they return false, and
+// launch nothing, where they do not apply (the cp.async passes then run).
+// fine: level 0 (FP32 vectors, the level-precision coarse residual);
+// otherwise a coarse level in the level precision.
+cudaError_t tma_prepare_attributes();
+bool tma_fused_enabled();
+bool tma_pre(int ck, bool fine, bool update, const Grid3& g, const Grid3& gc, const void* sm, const void* rin,
+             const float* q, float* r_out, void* e, void* rc, Scalars* sc, double* partials, cudaStream_t s);
+bool tma_post(int ck, bool fine, const Grid3& g, const Grid3& gc, const void* sm, const void* e, const void* ec,
+              const void* r, void* out, const void* accum, float w, Scalars* sc, double* partials, long long n_active,
+              cudaStream_t s);
 
 // ---- connected components of the non-solid cells (topology_kernels.cu)
 struct TopoCounts {

@@ -1,0 +1,733 @@
+// tma_fused.cu -- the fused multigrid smoothing passes with planes staged by
+// the Tensor Memory Accelerator.
+//
+// k_pre_tma and k_post_tma do the work of k_presmooth_restrict and
+// k_prolong_postsmooth (fused_kernels.cu) with the same per-cell arithmetic
+// in the same order, so every vector they write is bit-identical; the
+// difference is how planes reach shared memory and how work is spread over
+// the threads:
+//
+//  * One elected thread issues, per plane, one cp.async.bulk.tensor copy of
+//    each input: the smoother records (a 4-D box over the split rows: half-row
+//    columns, even/odd half, y, z), the level vectors (3-D boxes of 80 x RH
+//    cells starting at x0-8, so the first coordinate stays 16-byte aligned
+//    for FP32 and FP16 data) and, for the post-smoothing pass, the coarse
+//    correction (48 x CRH coarse cells from x0/2-8).  The copies of a plane
+//    complete on one mbarrier; two mbarriers alternate between planes.  Cells
+//    outside the grid arrive as zeros (the copy's out-of-bounds fill), which
+//    is the closed wall the cp.async zero fill stood for.  No thread computes
+//    a global address for a halo load, which removes most of the integer
+//    work of the cp.async kernels.
+//  * 384 threads (224 with FP32 records) take one task each in every stage
+//    (360 red/prolongation quads, 324 black quads, 256 tile quads), instead
+//    of two rounds of 256 threads.
+//
+// Only grids without periodic axes take these kernels (a copy box cannot
+// wrap around an axis); the cp.async kernels serve the others.  Every wait
+// on an mbarrier is bounded: when it runs out the block stops issuing
+// copies, marks the solve as stalled and converged (the host reports a
+// timeout), and finishes its loop without waiting again.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <mutex>
+
+#include "kernels.h"
+#include "fused_common.cuh"
+
+namespace mhdproj {
+
+namespace {
+using namespace staged;
+using namespace fused;
+
+template <int CK>
+struct TGeo {
+    static constexpr int FTY = CK == 0 ? 8 : 16;       // tile rows
+    static constexpr int RH = FTY + 4;                 // staged rows y0-2 .. y0+FTY+1
+    static constexpr int NRED = RH * NQ;               // red / prolongation quads
+    static constexpr int NBLK = (FTY + 2) * NQ;        // black quads, rows y0-1 .. y0+FTY
+    static constexpr int NOWN = QX * FTY;              // tile quads
+    static constexpr int NT = (NRED + 31) / 32 * 32;   // threads: one red task each
+    static constexpr int VW = 80;                      // staged vector row: x0-8 .. x0+71
+    static constexpr int VX = 4;                       // column of x0-4 in a staged vector row
+    static constexpr int CRH = FTY / 2 + 2;            // coarse rows y0/2-1 .. y0/2+FTY/2
+    static constexpr int CW = 48;                      // coarse columns x0/2-8 .. x0/2+39
+    static_assert(NBLK <= NT && NOWN <= NT, "one task per thread");
+};
+constexpr int TMA_MIN_BLOCKS = 2;
+constexpr int WAIT_LIMIT = 1 << 22;
+
+// ------------------------------------------------------------- PTX wrappers
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_barrier_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+// Orders this thread's (and, after a barrier, the block's) generic-proxy
+// accesses of shared memory before the copies it issues next.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for the phase of the given parity; false when it ran out.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity) {
+    for (int i = 0; i < WAIT_LIMIT; i++)
+        if (mbar_try_wait(b, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_3d(void* dst, const CUtensorMap* tm, int x, int y, int z, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tma_4d(void* dst, const CUtensorMap* tm, int x, int h, int y, int z,
+                                       unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];\n" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x), "r"(h), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+template <class T, int N>
+constexpr int padded128() {  // elements of N T rounded up to 128 bytes
+    return (int)(((N * sizeof(T) + 127) / 128) * 128 / sizeof(T));
+}
+
+// Shared memory of the pre-smoothing pass.  Ring slots: records and the
+// correction of planes zA-2 .. zA+1 (4), the copied residual and q of planes
+// zA, zA+1 (2).
+template <int CK, class VT, bool UPDATE>
+struct PreTmaSm {
+    using CT = typename CoefStore<CK>::T;
+    using G = TGeo<CK>;
+    alignas(128) CT c[4][G::RH][RW];
+    alignas(128) VT rv[2][G::RH][G::VW];
+    alignas(128) float qv[UPDATE ? 2 : 1][UPDATE ? G::RH : 1][G::VW];
+    alignas(16) float er[4][G::RH][RW];
+    float2 ypart[G::FTY][QX];
+    unsigned long long bar[2];
+    int abort_;
+};
+// Shared memory of the post-smoothing pass: records and the smoothed
+// correction of planes zA-2 .. zA+1, the copied pre-smoothed correction and
+// right-hand side of planes zA, zA+1, and the coarse correction of the two
+// coarse planes they fall in.
+template <int CK, class VT, class VTc>
+struct PostTmaSm {
+    using CT = typename CoefStore<CK>::T;
+    using G = TGeo<CK>;
+    static constexpr int ECS = padded128<VTc, G::CRH * G::CW>();
+    alignas(128) CT c[4][G::RH][RW];
+    alignas(128) VT ev[2][G::RH][G::VW];
+    alignas(128) VT rv[2][G::RH][G::VW];
+    alignas(128) VTc ec[2][ECS];
+    alignas(16) float ep[4][G::RH][RW];
+    unsigned long long bar[2];
+    int abort_;
+};
+template <class SM>
+__device__ __forceinline__ SM& aligned_smem(unsigned char* raw) {
+    return *reinterpret_cast<SM*>(raw + ((128u - (smem_u32(raw) & 127u)) & 127u));
+}
+
+// ------------------------------------------------------ pre-smoothing pass
+// See k_presmooth_restrict for the algebra; rin and q arrive through tm_r
+// and tm_q, the records through tm_rec.
+template <int CK, class VT, class VTc, bool UPDATE, bool FINE>
+__global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
+    k_pre_tma(const __grid_constant__ CUtensorMap tm_rec, const __grid_constant__ CUtensorMap tm_r,
+              const __grid_constant__ CUtensorMap tm_q, Grid3 g, Grid3 gc, float* __restrict__ r_out,
+              VT* __restrict__ e, VTc* __restrict__ rc, Scalars* sc, double* partials, int nblocks) {
+    if (sc->converged) return;
+    using CT = typename CoefStore<CK>::T;
+    using G = TGeo<CK>;
+    using SM = PreTmaSm<CK, VT, UPDATE>;
+    using R4 = typename Raw4<VT>::T;
+    constexpr int FTY = G::FTY, NT = G::NT, RH = G::RH, VW = G::VW;
+    constexpr unsigned BYTES = RH * RW * sizeof(CT) + RH * VW * sizeof(VT) + (UPDATE ? RH * VW * 4 : 0);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    SM& S = aligned_smem<SM>(smem_raw);
+    __shared__ double sh[NT / 32];
+    const int t = threadIdx.x;
+    const float sigma = FINE ? sc->sigma : 1.0f;
+    const float alpha = UPDATE ? sc->alpha_f : 0.0f;
+    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * FTY;
+    const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
+    const int zs = z0 - 2, nsteps = z1 - z0 + 4;  // planes zs .. z1+1
+    const long long sxy = (long long)g.nx * g.ny;
+    int last_issued = 0;
+    auto issue = [&](int k) {  // thread 0: the copies of plane zs + k
+        const int zz = zs + k;
+        unsigned long long* b = &S.bar[k & 1];
+        fence_proxy_async();
+        mbar_expect_tx(b, BYTES);
+        tma_4d(&S.c[k & 3][0][0], &tm_rec, 2 * x0 - 8, 0, y0 - 2, zz, b);
+        tma_3d(&S.rv[k & 1][0][0], &tm_r, x0 - 8, y0 - 2, zz, b);
+        if (UPDATE) tma_3d(&S.qv[k & 1][0][0], &tm_q, x0 - 8, y0 - 2, zz, b);
+        last_issued = k;
+    };
+    if (t == 0) {
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        S.abort_ = 0;
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (t == 0) issue(0);
+
+    // red task: quad r_q of staged row r_row
+    const bool has_red = t < G::NRED;
+    const int r_row = t / NQ, r_q = t - (t / NQ) * NQ;
+    const int r_o = r_row * RW + 2 * r_q;          // split offset of the quad's even half
+    const int r_v = r_row * VW + G::VX + 4 * r_q;  // its cells in a copied vector row
+    const int r_gx = x0 - XO + 4 * r_q, r_gy = y0 - 2 + r_row;
+    const int r_par = r_gy & 1;
+    const int r_own = (has_red && r_row >= 2 && r_row < FTY + 2 && r_q >= 1 && r_q <= QX && r_gx < g.nx && r_gy < g.ny)
+                          ? r_gx + g.nx * r_gy
+                          : -1;
+    // black task: quad b_q of staged row b_row (1 .. FTY+2)
+    const bool has_blk = t < G::NBLK;
+    const int b_row = t / NQ + 1, b_q = t - (t / NQ) * NQ;
+    const int b_o = b_row * RW + 2 * b_q;
+    const int b_par = (y0 - 2 + b_row) & 1;
+    // tile task: the own quad
+    const bool has_own = t < G::NOWN;
+    const int tx = t % QX, ty = t / QX;
+    const int ox = x0 + 4 * tx, oy = y0 + ty;
+    const bool own_inside = has_own && ox < g.nx && oy < g.ny;
+    const int oo = (ty + 2) * RW + 2 * (tx + 1);
+    const long long og = ox + (long long)g.nx * oy;
+
+    float rr_thread = 0.f;
+    float2 part = make_float2(0.f, 0.f);
+    int rc_z = -1;
+    auto flush_rc = [&]() {
+        if (rc_z >= 0 && own_inside && !(ty & 1)) {
+            const float2 a = S.ypart[ty][tx], b = S.ypart[ty + 1][tx];
+            st2<VTc>(rc + (ox >> 1) + (long long)gc.nx * ((oy >> 1) + (long long)gc.ny * rc_z),
+                     make_float2(0.25f * (a.x + b.x), 0.25f * (a.y + b.y)));
+        }
+        rc_z = -1;
+    };
+    auto step = [&](auto ph, int k) {
+        constexpr int P = decltype(ph)::value;  // k & 3; zs is even, so plane zA has parity P & 1
+        const int zA = zs + k;
+        __syncthreads();
+        const bool aborted = S.abort_ != 0;
+        if (t == 0 && k + 1 < nsteps && !aborted) issue(k + 1);
+        flush_rc();
+        if (!aborted && !mbar_wait(&S.bar[P & 1], P >> 1)) {
+            S.abort_ = 1;
+            sc->stalled = 1;
+            sc->converged = 1;
+        }
+        // ---- red stage: plane zA over the 2-halo rows
+        if (has_red) {
+            const CT* C = &S.c[P][0][0];
+            float* ER = &S.er[P][0][0];
+            float4 rn = cvt4r<VT>(*reinterpret_cast<const R4*>(&S.rv[P & 1][0][0] + r_v));
+            if (UPDATE) {
+                const float4 qq = *reinterpret_cast<const float4*>(&S.qv[P & 1][0][0] + r_v);
+                rn = make_float4(fmaf(-alpha, qq.x, rn.x), fmaf(-alpha, qq.y, rn.y), fmaf(-alpha, qq.z, rn.z),
+                                 fmaf(-alpha, qq.w, rn.w));
+            }
+            const int p = r_par ^ (P & 1);
+            float4 d0, d1;
+            rec2<CK>(C + r_o + p * HW, &d0, &d1);
+            const float2 rr = p ? make_float2(rn.y, rn.w) : make_float2(rn.x, rn.z);  // red cells
+            const float2 rb = p ? make_float2(rn.x, rn.z) : make_float2(rn.y, rn.w);  // black cells
+            const float2 ev = divide2(make_float2(sigma * rr.x, sigma * rr.y), make_float2(d0.w, d1.w));
+            *reinterpret_cast<float2*>(ER + r_o + p * HW) = ev;
+            *reinterpret_cast<float2*>(ER + r_o + (1 - p) * HW) = make_float2(sigma * rb.x, sigma * rb.y);
+            if (UPDATE && r_own >= 0 && zA >= z0 && zA < z1) {
+                *reinterpret_cast<float4*>(r_out + sxy * zA + r_own) = rn;
+                rr_thread = fmaf(rn.x, rn.x, fmaf(rn.y, rn.y, fmaf(rn.z, rn.z, fmaf(rn.w, rn.w, rr_thread))));
+            }
+        }
+        __syncthreads();
+        // ---- black stage: plane zA-1 over the 1-halo rows, in place
+        if (has_blk && zA - 1 >= z0 - 1) {
+            const CT* C = &S.c[(P + 3) & 3][0][0];
+            const CT* CN = &S.c[P][0][0];
+            float* E = &S.er[(P + 3) & 3][0][0];
+            const float* EM = &S.er[(P + 2) & 3][0][0];
+            const float* EP = &S.er[P][0][0];
+            const int h = b_par ^ (P & 1);  // black half of the row at plane zA-1
+            const int o = b_o + h * HW;
+            float2 d;
+            const float2 s = gs_sum2<CK>(C, CN, E, EM, EP, o, h, *reinterpret_cast<const float2*>(E + o), &d);
+            *reinterpret_cast<float2*>(E + o) = divide2(s, d);
+        }
+        __syncthreads();
+        // ---- correction out and restriction: plane zA-2 over the tile
+        const int zC = zA - 2;
+        if (has_own && zC >= z0 && zC < z1) {
+            const CT* C = &S.c[(P + 2) & 3][0][0];
+            const CT* CN = &S.c[(P + 3) & 3][0][0];
+            const float* E = &S.er[(P + 2) & 3][0][0];
+            const float* EM = &S.er[(P + 1) & 3][0][0];
+            const float* EP = &S.er[(P + 3) & 3][0][0];
+            const int p = (oy & 1) ^ (P & 1);  // red half of the own quad
+            float2 d;
+            const float2 s = gs_sum2<CK>(C, CN, E, EM, EP, oo + p * HW, p, make_float2(0.f, 0.f), &d);
+            part.x += s.x;
+            part.y += s.y;
+            if (own_inside) {
+                const float2 ev = *reinterpret_cast<const float2*>(E + oo);
+                const float2 od = *reinterpret_cast<const float2*>(E + oo + HW);
+                st4<VT>(e + (og + sxy * zC), make_float4(ev.x, od.x, ev.y, od.y));
+            }
+            if ((zC & 1) || zC + 1 == z1) {
+                // the row pair sum is formed after the next barrier
+                S.ypart[ty][tx] = part;
+                rc_z = zC >> 1;
+                part = make_float2(0.f, 0.f);
+            }
+        }
+    };
+    for (int k = 0;;) {
+        step(Phase<0>{}, k);
+        if (++k >= nsteps) break;
+        step(Phase<1>{}, k);
+        if (++k >= nsteps) break;
+        step(Phase<2>{}, k);
+        if (++k >= nsteps) break;
+        step(Phase<3>{}, k);
+        if (++k >= nsteps) break;
+    }
+    __syncthreads();
+    flush_rc();
+    if (t == 0 && S.abort_) (void)mbar_wait(&S.bar[last_issued & 1], (last_issued >> 1) & 1);
+    if (UPDATE) {
+        double v1[1] = {(double)rr_thread};
+        block_sum<1>(v1, sh);
+        if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[8])) {
+            double tot[1];
+            finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[8]);
+            if (t == 0 && !sc->stalled) {
+                const double rr = tot[0];
+                sc->rr = rr;
+                sc->iterations += 1;
+                sc->total_iterations += 1;
+                if (!isfinite(rr)) {
+                    sc->nonfinite = 1;
+                    sc->converged = 1;
+                } else if (rr <= sc->rr_target || sc->total_iterations >= sc->max_total) {
+                    sc->converged = 1;
+                }
+            }
+        }
+    }
+}
+
+// ----------------------------------------------------- post-smoothing pass
+// See k_prolong_postsmooth; e, r and the coarse correction arrive through
+// tm_e, tm_r and tm_ec, the records through tm_rec.
+template <int CK, class VT, class VTc, bool DOT, bool FINE>
+__global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
+    k_post_tma(const __grid_constant__ CUtensorMap tm_rec, const __grid_constant__ CUtensorMap tm_e,
+               const __grid_constant__ CUtensorMap tm_r, const __grid_constant__ CUtensorMap tm_ec, Grid3 g,
+               VT* __restrict__ out, const VT* __restrict__ accum, float w, Scalars* sc, double* partials,
+               int nblocks, long long n_active) {
+    if (sc->converged) return;
+    using CT = typename CoefStore<CK>::T;
+    using G = TGeo<CK>;
+    using SM = PostTmaSm<CK, VT, VTc>;
+    using R4 = typename Raw4<VT>::T;
+    using C2 = typename Raw2<VTc>::T;
+    constexpr int FTY = G::FTY, NT = G::NT, RH = G::RH, VW = G::VW;
+    constexpr unsigned BYTES = RH * RW * sizeof(CT) + 2 * RH * VW * sizeof(VT);
+    constexpr unsigned EC_BYTES = G::CRH * G::CW * sizeof(VTc);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    SM& S = aligned_smem<SM>(smem_raw);
+    __shared__ double sh[NT / 32];
+    const int t = threadIdx.x;
+    const float sigma = FINE ? sc->sigma : 1.0f;
+    const float is = FINE ? sc->inv_sigma : 1.0f;
+    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * FTY;
+    const int z0 = blockIdx.z * g.zper, z1 = min(g.nz, z0 + g.zper);
+    const int zs = z0 - 2, nsteps = z1 - z0 + 4;
+    const long long sxy = (long long)g.nx * g.ny;
+    int last_issued = 0;
+    auto issue = [&](int k) {  // thread 0: the copies of plane zs + k (and its coarse plane when it starts one)
+        const int zz = zs + k;
+        unsigned long long* b = &S.bar[k & 1];
+        fence_proxy_async();
+        mbar_expect_tx(b, BYTES + ((k & 1) ? 0u : EC_BYTES));
+        tma_4d(&S.c[k & 3][0][0], &tm_rec, 2 * x0 - 8, 0, y0 - 2, zz, b);
+        tma_3d(&S.ev[k & 1][0][0], &tm_e, x0 - 8, y0 - 2, zz, b);
+        tma_3d(&S.rv[k & 1][0][0], &tm_r, x0 - 8, y0 - 2, zz, b);
+        if (!(k & 1)) tma_3d(&S.ec[(k >> 1) & 1][0], &tm_ec, (x0 >> 1) - 8, (y0 >> 1) - 1, zz >> 1, b);
+        last_issued = k;
+    };
+    if (t == 0) {
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        S.abort_ = 0;
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (t == 0) issue(0);
+
+    const bool has_red = t < G::NRED;
+    const int r_row = t / NQ, r_q = t - (t / NQ) * NQ;
+    const int r_o = r_row * RW + 2 * r_q;
+    const int r_v = r_row * VW + G::VX + 4 * r_q;
+    const int r_c = (r_row >> 1) * G::CW + 6 + 2 * r_q;  // the quad's two coarse parents
+    const int r_gx = x0 - XO + 4 * r_q, r_gy = y0 - 2 + r_row;
+    const int r_par = r_gy & 1;
+    const bool r_inside = r_gx >= 0 && r_gx < g.nx && r_gy >= 0 && r_gy < g.ny;
+    const bool has_blk = t < G::NBLK;
+    const int b_row = t / NQ + 1, b_q = t - (t / NQ) * NQ;
+    const int b_o = b_row * RW + 2 * b_q;
+    const int b_par = (y0 - 2 + b_row) & 1;
+    const bool has_own = t < G::NOWN;
+    const int tx = t % QX, ty = t / QX;
+    const int ox = x0 + 4 * tx, oy = y0 + ty;
+    const bool own_inside = has_own && ox < g.nx && oy < g.ny;
+    const int oo = (ty + 2) * RW + 2 * (tx + 1);
+    const int ov = (ty + 2) * VW + G::VX + 4 * (tx + 1);
+    const long long og = ox + (long long)g.nx * oy;
+    Acc acc;
+    R4 rq_own[4];  // own quad's right-hand side of planes zA-3 .. zA (slot zA & 3)
+
+    auto step = [&](auto ph, int k) {
+        constexpr int P = decltype(ph)::value;
+        const int zA = zs + k;
+        __syncthreads();
+        const bool aborted = S.abort_ != 0;
+        if (t == 0 && k + 1 < nsteps && !aborted) issue(k + 1);
+        if (!aborted && !mbar_wait(&S.bar[P & 1], P >> 1)) {
+            S.abort_ = 1;
+            sc->stalled = 1;
+            sc->converged = 1;
+        }
+        if (has_own) rq_own[P] = *reinterpret_cast<const R4*>(&S.rv[P & 1][0][0] + ov);
+        // ---- prolongation: plane zA over the 2-halo rows
+        if (has_red) {
+            float* EP = &S.ep[P][0][0];
+            float4 ev = make_float4(0.f, 0.f, 0.f, 0.f), rq = ev;
+            float2 cv = make_float2(0.f, 0.f);
+            if (r_inside && zA >= 0 && zA < g.nz) {
+                ev = cvt4r<VT>(*reinterpret_cast<const R4*>(&S.ev[P & 1][0][0] + r_v));
+                rq = cvt4r<VT>(*reinterpret_cast<const R4*>(&S.rv[P & 1][0][0] + r_v));
+                cv = cvt2(*reinterpret_cast<const C2*>(&S.ec[P >> 1][0] + r_c));
+            }
+            const int p = r_par ^ (P & 1);
+            const float2 er = p ? make_float2(ev.y, ev.w) : make_float2(ev.x, ev.z);
+            const float2 rb = p ? make_float2(rq.x, rq.z) : make_float2(rq.y, rq.w);
+            *reinterpret_cast<float2*>(EP + r_o + p * HW) = make_float2(fmaf(w, cv.x, er.x), fmaf(w, cv.y, er.y));
+            *reinterpret_cast<float2*>(EP + r_o + (1 - p) * HW) = make_float2(sigma * rb.x, sigma * rb.y);
+        }
+        __syncthreads();
+        // ---- black half-step: plane zA-1 over the 1-halo rows, in place
+        if (has_blk && zA - 1 >= z0 - 1) {
+            const CT* C = &S.c[(P + 3) & 3][0][0];
+            const CT* CN = &S.c[P][0][0];
+            float* E = &S.ep[(P + 3) & 3][0][0];
+            const float* EM = &S.ep[(P + 2) & 3][0][0];
+            const float* EP = &S.ep[P][0][0];
+            const int h = b_par ^ (P & 1);
+            const int o = b_o + h * HW;
+            float2 d;
+            const float2 s = gs_sum2<CK>(C, CN, E, EM, EP, o, h, *reinterpret_cast<const float2*>(E + o), &d);
+            *reinterpret_cast<float2*>(E + o) = divide2(s, d);
+        }
+        __syncthreads();
+        // ---- red half-step: plane zA-2 over the tile, out = z
+        const int zC = zA - 2;
+        if (has_own && zC >= z0 && zC < z1) {
+            const CT* C = &S.c[(P + 2) & 3][0][0];
+            const CT* CN = &S.c[(P + 3) & 3][0][0];
+            const float* E = &S.ep[(P + 2) & 3][0][0];
+            const float* EM = &S.ep[(P + 1) & 3][0][0];
+            const float* EP = &S.ep[(P + 3) & 3][0][0];
+            const int p = (oy & 1) ^ (P & 1);
+            const float4 rv = cvt4r<VT>(rq_own[(P + 2) & 3]);
+            const float2 rr = p ? make_float2(rv.y, rv.w) : make_float2(rv.x, rv.z);
+            float2 d;
+            const float2 s = gs_sum2<CK>(C, CN, E, EM, EP, oo + p * HW, p, make_float2(sigma * rr.x, sigma * rr.y), &d);
+            const float2 zr = divide2(s, d);
+            const float2 zb = *reinterpret_cast<const float2*>(E + oo + (1 - p) * HW);
+            float4 zv = p ? make_float4(zb.x, zr.x, zb.y, zr.y) : make_float4(zr.x, zb.x, zr.y, zb.y);
+            if (own_inside) {
+                if (accum) {  // out = accum + z (second W-cycle visit)
+                    const float4 a = cvt4r<VT>(*reinterpret_cast<const R4*>(accum + og + sxy * zC));
+                    zv = make_float4(a.x + zv.x, a.y + zv.y, a.z + zv.z, a.w + zv.w);
+                }
+                st4<VT>(out + og + sxy * zC, zv);
+                if (DOT) {
+                    acc.add_prod(rv.x, zv.x * is);
+                    acc.add_prod(rv.y, zv.y * is);
+                    acc.add_prod(rv.z, zv.z * is);
+                    acc.add_prod(rv.w, zv.w * is);
+                }
+            }
+        }
+    };
+    for (int k = 0;;) {
+        step(Phase<0>{}, k);
+        if (++k >= nsteps) break;
+        step(Phase<1>{}, k);
+        if (++k >= nsteps) break;
+        step(Phase<2>{}, k);
+        if (++k >= nsteps) break;
+        step(Phase<3>{}, k);
+        if (++k >= nsteps) break;
+    }
+    if (t == 0 && S.abort_) (void)mbar_wait(&S.bar[last_issued & 1], (last_issued >> 1) & 1);
+    if (DOT) {
+        double v1[1] = {acc.total()};
+        block_sum<1>(v1, sh);
+        if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[9])) {
+            double tot[1];
+            finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[9]);
+            if (t == 0 && !sc->stalled) {
+                const double rz = tot[0];
+                if (!isfinite(rz)) {
+                    sc->nonfinite = 1;
+                    sc->converged = 1;
+                } else if (!(rz > 0.0)) {
+                    sc->breakdown = 1;
+                    sc->converged = 1;
+                } else if (sc->first) {
+                    sc->rz = rz;
+                    sc->beta = 0.0;
+                    sc->beta_f = 0.0f;
+                } else {
+                    sc->beta = rz / sc->rz;
+                    sc->beta_f = (float)sc->beta;
+                    sc->rz = rz;
+                }
+                sc->inv_sigma_z = sc->inv_sigma;
+                set_sigma_from(sc, sc->rr, n_active);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ host
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+bool g_tma_enabled = false;
+int g_sms = 0;
+int g_occ[3][2][2] = {};  // [records precision][coarse level][pre / post]: resident blocks per SM
+
+bool encoder() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        else
+            (void)cudaGetLastError();
+    });
+    return g_encode != nullptr;
+}
+
+// 3-D map of a level vector (x-fastest cells, element size 4 or 2 bytes),
+// box w x rows x 1.
+bool vec_map(CUtensorMap* m, const void* base, int esize, const Grid3& g, int w, int rows) {
+    const cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.nx * esize, (cuuint64_t)g.nx * g.ny * esize};
+    const cuuint32_t box[3] = {(cuuint32_t)w, (cuuint32_t)rows, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return g_encode(m, esize == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3,
+                    const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+// 4-D map of the split-row smoother records: (4 values x nx/2 records of a
+// half row, even/odd half, y, z), box 144 values x 2 halves x rows x 1.
+bool rec_map(CUtensorMap* m, const void* base, int ck, const Grid3& g, int rows) {
+    const int esize = ck == 0 ? 4 : 2;
+    const cuuint64_t half = (cuuint64_t)2 * g.nx;  // values per half row
+    const cuuint64_t dims[4] = {half, 2, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
+    const cuuint64_t strides[3] = {half * esize, 2 * half * esize, 2 * half * esize * g.ny};
+    const cuuint32_t box[4] = {(cuuint32_t)(2 * RW), 2, (cuuint32_t)rows, 1};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    return g_encode(m, esize == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 4,
+                    const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// z runs as in fused_launch: even runs that fill whole waves of resident
+// blocks, each run computing two planes below and above it.
+Launch tma_launch(const Grid3& g0, int fty, int nt, int occ) {
+    Launch P;
+    P.g = g0;
+    P.block = dim3(nt, 1, 1);
+    const int gx = (g0.nx + PX - 1) / PX, gy = (g0.ny + fty - 1) / fty, nz = g0.nz;
+    const int tiles = gx * gy;
+    const int cap = (g_sms > 0 ? g_sms : 152) * (occ > 0 ? occ : 1);
+    int best_zper = nz + (nz & 1), best_zc = 1;
+    double best = -1.0;
+    for (int zc = 1; zc <= nz; zc++) {
+        int zper = (nz + zc - 1) / zc;
+        if (zper & 1) zper++;
+        if (zper < 2 && zc > 1) break;
+        const int zcr = (nz + zper - 1) / zper;
+        const long long blocks = (long long)tiles * zcr;
+        if (blocks > MAX_REDUCE_BLOCKS) break;
+        const double waves = (double)blocks / cap;
+        const double score = waves / std::ceil(waves) * ((double)zper / (zper + 4));
+        if (score > best) {
+            best = score;
+            best_zper = zper;
+            best_zc = zcr;
+        }
+    }
+    P.grid = dim3(gx, gy, best_zc);
+    P.g.zper = best_zper;
+    P.nblocks = tiles * best_zc;
+    return P;
+}
+
+template <int CK, class VT, class VTc, bool UPDATE, bool FINE>
+bool pre_tma(const Grid3& g, const Grid3& gc, const void* sm, const void* rin, const float* q, float* r_out, void* e,
+             void* rc, Scalars* sc, double* partials, cudaStream_t s) {
+    using G = TGeo<CK>;
+    if (!aligned16(sm) || !aligned16(rin) || (UPDATE && !aligned16(q))) return false;
+    CUtensorMap tm_rec, tm_r, tm_q;
+    if (!rec_map(&tm_rec, sm, CK, g, G::RH)) return false;
+    if (!vec_map(&tm_r, rin, (int)sizeof(VT), g, G::VW, G::RH)) return false;
+    if (UPDATE) {
+        if (!vec_map(&tm_q, q, 4, g, G::VW, G::RH)) return false;
+    } else {
+        tm_q = tm_r;
+    }
+    const Launch P = tma_launch(g, G::FTY, G::NT, g_occ[CK][FINE ? 0 : 1][0]);
+    k_pre_tma<CK, VT, VTc, UPDATE, FINE><<<P.grid, P.block, sizeof(PreTmaSm<CK, VT, UPDATE>) + 128, s>>>(
+        tm_rec, tm_r, tm_q, P.g, gc, r_out, (VT*)e, (VTc*)rc, sc, partials, P.nblocks);
+    return true;
+}
+template <int CK, class VT, class VTc, bool DOT, bool FINE>
+bool post_tma(const Grid3& g, const Grid3& gc, const void* sm, const void* e, const void* ec, const void* r, void* out,
+              const void* accum, float w, Scalars* sc, double* partials, long long n_active, cudaStream_t s) {
+    using G = TGeo<CK>;
+    if (!aligned16(sm) || !aligned16(e) || !aligned16(r) || !aligned16(ec)) return false;
+    if ((gc.nx * (int)sizeof(VTc)) % 16) return false;
+    CUtensorMap tm_rec, tm_e, tm_r, tm_ec;
+    if (!rec_map(&tm_rec, sm, CK, g, G::RH)) return false;
+    if (!vec_map(&tm_e, e, (int)sizeof(VT), g, G::VW, G::RH)) return false;
+    if (!vec_map(&tm_r, r, (int)sizeof(VT), g, G::VW, G::RH)) return false;
+    if (!vec_map(&tm_ec, ec, (int)sizeof(VTc), gc, G::CW, G::CRH)) return false;
+    const Launch P = tma_launch(g, G::FTY, G::NT, g_occ[CK][FINE ? 0 : 1][1]);
+    k_post_tma<CK, VT, VTc, DOT, FINE><<<P.grid, P.block, sizeof(PostTmaSm<CK, VT, VTc>) + 128, s>>>(
+        tm_rec, tm_e, tm_r, tm_ec, P.g, (VT*)out, (const VT*)accum, w, sc, partials, P.nblocks, n_active);
+    return true;
+}
+
+template <class F>
+cudaError_t prep(F* fn, size_t bytes, int threads, int* occ) {
+    cudaError_t e = cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess && occ) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, (const void*)fn, threads, bytes);
+    return e;
+}
+template <int CK, class VT, class VTc>
+cudaError_t prep_level(bool fine) {
+    using G = TGeo<CK>;
+    cudaError_t e = cudaSuccess;
+    const size_t pre_u = sizeof(PreTmaSm<CK, VT, true>) + 128, pre_n = sizeof(PreTmaSm<CK, VT, false>) + 128;
+    const size_t post = sizeof(PostTmaSm<CK, VT, VTc>) + 128;
+    if (fine) {
+        if (e == cudaSuccess) e = prep(k_pre_tma<CK, VT, VTc, true, true>, pre_u, G::NT, &g_occ[CK][0][0]);
+        if (e == cudaSuccess) e = prep(k_pre_tma<CK, VT, VTc, false, true>, pre_n, G::NT, nullptr);
+        if (e == cudaSuccess) e = prep(k_post_tma<CK, VT, VTc, true, true>, post, G::NT, &g_occ[CK][0][1]);
+    } else {
+        if (e == cudaSuccess) e = prep(k_pre_tma<CK, VT, VTc, false, false>, pre_n, G::NT, &g_occ[CK][1][0]);
+        if (e == cudaSuccess) e = prep(k_post_tma<CK, VT, VTc, false, false>, post, G::NT, &g_occ[CK][1][1]);
+    }
+    return e;
+}
+}  // namespace
+
+bool tma_fused_enabled() { return g_tma_enabled; }
+
+cudaError_t tma_prepare_attributes() {
+    const char* ev = getenv("MHDPROJ_TMA");
+    g_tma_enabled = !(ev && ev[0] == '0') && encoder();
+    if (!g_tma_enabled) return cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = prep_level<0, float, float>(true);
+    if (e == cudaSuccess) e = prep_level<1, float, __half>(true);
+    if (e == cudaSuccess) e = prep_level<2, float, __nv_bfloat16>(true);
+    if (e == cudaSuccess) e = prep_level<0, float, float>(false);
+    if (e == cudaSuccess) e = prep_level<1, __half, __half>(false);
+    if (e == cudaSuccess) e = prep_level<2, __nv_bfloat16, __nv_bfloat16>(false);
+    return e;
+}
+
+static bool tma_grid_ok(const Grid3& g, int vt_bytes) {
+    return g_tma_enabled && g.periodic == 0 && g.nx % 4 == 0 && (g.nx * vt_bytes) % 16 == 0;
+}
+
+bool tma_pre(int ck, bool fine, bool update, const Grid3& g, const Grid3& gc, const void* sm, const void* rin,
+             const float* q, float* r_out, void* e, void* rc, Scalars* sc, double* partials, cudaStream_t s) {
+    const int vt = fine || ck == 0 ? 4 : 2;
+    if (!tma_grid_ok(g, vt)) return false;
+    if (fine) {
+        if (ck == 1)
+            return update ? pre_tma<1, float, __half, true, true>(g, gc, sm, rin, q, r_out, e, rc, sc, partials, s)
+                          : pre_tma<1, float, __half, false, true>(g, gc, sm, rin, q, r_out, e, rc, sc, partials, s);
+        if (ck == 2)
+            return update
+                       ? pre_tma<2, float, __nv_bfloat16, true, true>(g, gc, sm, rin, q, r_out, e, rc, sc, partials, s)
+                       : pre_tma<2, float, __nv_bfloat16, false, true>(g, gc, sm, rin, q, r_out, e, rc, sc, partials, s);
+        return update ? pre_tma<0, float, float, true, true>(g, gc, sm, rin, q, r_out, e, rc, sc, partials, s)
+                      : pre_tma<0, float, float, false, true>(g, gc, sm, rin, q, r_out, e, rc, sc, partials, s);
+    }
+    if (ck == 1) return pre_tma<1, __half, __half, false, false>(g, gc, sm, rin, q, r_out, e, rc, sc, partials, s);
+    if (ck == 2)
+        return pre_tma<2, __nv_bfloat16, __nv_bfloat16, false, false>(g, gc, sm, rin, q, r_out, e, rc, sc, partials, s);
+    return pre_tma<0, float, float, false, false>(g, gc, sm, rin, q, r_out, e, rc, sc, partials, s);
+}
+
+bool tma_post(int ck, bool fine, const Grid3& g, const Grid3& gc, const void* sm, const void* e, const void* ec,
+              const void* r, void* out, const void* accum, float w, Scalars* sc, double* partials, long long n_active,
+              cudaStream_t s) {
+    const int vt = fine || ck == 0 ? 4 : 2;
+    if (!tma_grid_ok(g, vt)) return false;
+    if (fine) {
+        if (ck == 1)
+            return post_tma<1, float, __half, true, true>(g, gc, sm, e, ec, r, out, accum, w, sc, partials, n_active, s);
+        if (ck == 2)
+            return post_tma<2, float, __nv_bfloat16, true, true>(g, gc, sm, e, ec, r, out, accum, w, sc, partials,
+                                                                 n_active, s);
+        return post_tma<0, float, float, true, true>(g, gc, sm, e, ec, r, out, accum, w, sc, partials, n_active, s);
+    }
+    if (ck == 1)
+        return post_tma<1, __half, __half, false, false>(g, gc, sm, e, ec, r, out, accum, w, sc, partials, n_active, s);
+    if (ck == 2)
+        return post_tma<2, __nv_bfloat16, __nv_bfloat16, false, false>(g, gc, sm, e, ec, r, out, accum, w, sc,
+                                                                       partials, n_active, s);
+    return post_tma<0, float, float, false, false>(g, gc, sm, e, ec, r, out, accum, w, sc, partials, n_active, s);
+}
+
+}  // namespace mhdproj

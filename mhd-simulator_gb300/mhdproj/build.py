@@ -24,7 +24,7 @@ NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler"
 # exactly: no fused multiply-adds.
 EXACT = {"reference_kernels.cu", "step_kernels.cu", "em_solver.cu"}
 
-SOURCES = ["context.cu", "gb300_kernels.cu", "fine_kernels.cu", "fused_kernels.cu", "mg_kernels.cu", "reference_kernels.cu", "noalloc.cu",
+SOURCES = ["context.cu", "gb300_kernels.cu", "fine_kernels.cu", "fused_kernels.cu", "tma_fused.cu", "mg_kernels.cu", "reference_kernels.cu", "noalloc.cu",
            "topology_kernels.cu", "step_kernels.cu", "export_fields.cu", "em_solver.cu",
            "classify.cu"]
 HOST_SOURCES = ["topology.cpp"]
