@@ -7,21 +7,27 @@
 // difference is how planes reach shared memory and how work is spread over
 // the threads:
 //
-//  * One elected thread issues, per plane, one cp.async.bulk.tensor copy of
-//    each input: the smoother records (a 4-D box over the split rows: half-row
-//    columns, even/odd half, y, z), the level vectors (3-D boxes of 80 x RH
-//    cells starting at x0-8, so the first coordinate stays 16-byte aligned
-//    for FP32 and FP16 data) and, for the post-smoothing pass, the coarse
-//    correction (48 x CRH coarse cells from x0/2-8).  The copies of a plane
-//    complete on one mbarrier; two mbarriers alternate between planes.  Cells
-//    outside the grid arrive as zeros (the copy's out-of-bounds fill), which
-//    is the closed wall the cp.async zero fill stood for.  No thread computes
-//    a global address for a halo load, which removes most of the integer
-//    work of the cp.async kernels.
-//  * 384 threads (224 with FP32 records) take one task each in every stage
-//    (360 red/prolongation quads, 324 black quads, 256 tile quads), instead
-//    of two rounds of 256 threads.
-//
+//  * One thread with no other task issues, per plane, one
+//    cp.async.bulk.tensor copy of each input: the smoother records (a 4-D box
+//    over the split rows: half-row columns, even/odd half, y, z), the level
+//    vectors (3-D boxes of RH rows from x0-4 for FP32 and from x0-8 for
+//    2-byte values, so the first coordinate stays 16-byte aligned) and, for
+//    the post-smoothing pass, the coarse correction (48 x CRH coarse cells
+//    from x0/2-8).  The copies of a plane complete on one mbarrier; two
+//    mbarriers alternate between planes.  Cells outside the grid arrive as
+//    zeros (the copy's out-of-bounds fill), which is the closed wall the
+//    cp.async zero fill stood for.  No thread computes a global address for a
+//    halo load, which removes most of the integer work of the cp.async
+//    kernels.
+//  * 384 threads (224 with FP32 records) take at most one task in every
+//    stage (360 red/prolongation quads, 324 black quads, 256 tile quads).
+//    The 16 interior quads of a staged row go to one half-warp, so its
+//    shared-memory accesses are contiguous; the halo quads of all rows follow.
+//  * Records and corrections sit in five-slot rings (planes zA-3 .. zA+1), so
+//    a step needs two barriers instead of three: warps that finish the tile
+//    stage of plane zA-2 go on to the next plane's red stage while others
+//    are still busy.
+
 // Only grids without periodic axes take these kernels (a copy box cannot
 // wrap around an axis); the cp.async kernels serve the others.  Every wait
 // on an mbarrier is bounded: when it runs out the block stops issuing
@@ -49,14 +55,22 @@ struct TGeo {
     static constexpr int FTY = CK == 0 ? 8 : 16;       // tile rows
     static constexpr int RH = FTY + 4;                 // staged rows y0-2 .. y0+FTY+1
     static constexpr int NRED = RH * NQ;               // red / prolongation quads
-    static constexpr int NBLK = (FTY + 2) * NQ;        // black quads, rows y0-1 .. y0+FTY
+    static constexpr int NBR = FTY + 2;                // black rows y0-1 .. y0+FTY
+    static constexpr int NBLK = NBR * NQ;              // black quads
     static constexpr int NOWN = QX * FTY;              // tile quads
-    static constexpr int NT = (NRED + 31) / 32 * 32;   // threads: one red task each
-    static constexpr int VW = 80;                      // staged vector row: x0-8 .. x0+71
-    static constexpr int VX = 4;                       // column of x0-4 in a staged vector row
+    static constexpr int NT = (NRED + 32) / 32 * 32;   // threads: one red task each, and a spare issuing thread
     static constexpr int CRH = FTY / 2 + 2;            // coarse rows y0/2-1 .. y0/2+FTY/2
     static constexpr int CW = 48;                      // coarse columns x0/2-8 .. x0/2+39
-    static_assert(NBLK <= NT && NOWN <= NT, "one task per thread");
+    static constexpr int NS = 5;                       // ring slots of records and corrections: zA-3 .. zA+1
+    static_assert(NBLK <= NT && NOWN <= NT && NRED < NT, "one task per thread");
+};
+// Staged rows of a level vector: x0-4 .. x0+67 for FP32 (the first
+// coordinate x0-4 is 16-byte aligned), x0-8 .. x0+71 for 2-byte values.
+template <class VT>
+struct VGeo {
+    static constexpr int XS = sizeof(VT) == 4 ? 4 : 8;  // row starts at x0 - XS
+    static constexpr int VW = sizeof(VT) == 4 ? 72 : 80;
+    static constexpr int VX = XS - XO;                 // column of x0-4 in a staged row
 };
 constexpr int TMA_MIN_BLOCKS = 2;
 constexpr int WAIT_LIMIT = 1 << 22;
@@ -113,35 +127,37 @@ constexpr int padded128() {  // elements of N T rounded up to 128 bytes
     return (int)(((N * sizeof(T) + 127) / 128) * 128 / sizeof(T));
 }
 
-// Shared memory of the pre-smoothing pass.  Ring slots: records and the
-// correction of planes zA-2 .. zA+1 (4), the copied residual and q of planes
-// zA, zA+1 (2).
+// Shared memory of the pre-smoothing pass: records and corrections of planes
+// zA-3 .. zA+1 (five slots), the copied residual and q of planes zA, zA+1.
 template <int CK, class VT, bool UPDATE>
 struct PreTmaSm {
     using CT = typename CoefStore<CK>::T;
     using G = TGeo<CK>;
-    alignas(128) CT c[4][G::RH][RW];
-    alignas(128) VT rv[2][G::RH][G::VW];
-    alignas(128) float qv[UPDATE ? 2 : 1][UPDATE ? G::RH : 1][G::VW];
-    alignas(16) float er[4][G::RH][RW];
+    using V = VGeo<VT>;
+    using VQ = VGeo<float>;
+    alignas(128) CT c[G::NS][G::RH][RW];
+    alignas(128) VT rv[2][G::RH][V::VW];
+    alignas(128) float qv[UPDATE ? 2 : 1][UPDATE ? G::RH : 1][VQ::VW];
+    alignas(16) float er[G::NS][G::RH][RW];
     float2 ypart[G::FTY][QX];
     unsigned long long bar[2];
     int abort_;
 };
-// Shared memory of the post-smoothing pass: records and the smoothed
-// correction of planes zA-2 .. zA+1, the copied pre-smoothed correction and
-// right-hand side of planes zA, zA+1, and the coarse correction of the two
-// coarse planes they fall in.
+// Shared memory of the post-smoothing pass: records and smoothed corrections
+// of planes zA-3 .. zA+1, the copied pre-smoothed correction and right-hand
+// side of planes zA, zA+1, and the coarse correction of the two coarse
+// planes they fall in.
 template <int CK, class VT, class VTc>
 struct PostTmaSm {
     using CT = typename CoefStore<CK>::T;
     using G = TGeo<CK>;
+    using V = VGeo<VT>;
     static constexpr int ECS = padded128<VTc, G::CRH * G::CW>();
-    alignas(128) CT c[4][G::RH][RW];
-    alignas(128) VT ev[2][G::RH][G::VW];
-    alignas(128) VT rv[2][G::RH][G::VW];
+    alignas(128) CT c[G::NS][G::RH][RW];
+    alignas(128) VT ev[2][G::RH][V::VW];
+    alignas(128) VT rv[2][G::RH][V::VW];
     alignas(128) VTc ec[2][ECS];
-    alignas(16) float ep[4][G::RH][RW];
+    alignas(16) float ep[G::NS][G::RH][RW];
     unsigned long long bar[2];
     int abort_;
 };
@@ -150,9 +166,27 @@ __device__ __forceinline__ SM& aligned_smem(unsigned char* raw) {
     return *reinterpret_cast<SM*>(raw + ((128u - (smem_u32(raw) & 127u)) & 127u));
 }
 
+// Task of thread t in a stage over `rows` staged rows starting at row0: the
+// 16 interior quads (1 .. 16) of a row go to one half-warp, so its
+// shared-memory accesses are contiguous and free of bank conflicts; the two
+// halo quads of each row (0 and 17) follow as tasks rows*16 .. rows*18-1.
+__device__ __forceinline__ void stage_task(int t, int rows, int row0, int* row, int* q) {
+    if (t < rows * 16) {
+        *row = row0 + (t >> 4);
+        *q = 1 + (t & 15);
+    } else {
+        const int e = t - rows * 16;
+        *row = row0 + (e >> 1);
+        *q = (e & 1) ? NQ - 1 : 0;
+    }
+}
+
 // ------------------------------------------------------ pre-smoothing pass
 // See k_presmooth_restrict for the algebra; rin and q arrive through tm_r
-// and tm_q, the records through tm_rec.
+// and tm_q, the records through tm_rec.  A step handles the red stage of
+// plane zA, the black stage of zA-1 and the tile stage of zA-2 with two
+// barriers: the five-slot rings let the next step's copies and red stage
+// start while other warps still finish the tile stage.
 template <int CK, class VT, class VTc, bool UPDATE, bool FINE>
 __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
     k_pre_tma(const __grid_constant__ CUtensorMap tm_rec, const __grid_constant__ CUtensorMap tm_r,
@@ -161,14 +195,18 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
     if (sc->converged) return;
     using CT = typename CoefStore<CK>::T;
     using G = TGeo<CK>;
+    using V = VGeo<VT>;
+    using VQ = VGeo<float>;
     using SM = PreTmaSm<CK, VT, UPDATE>;
     using R4 = typename Raw4<VT>::T;
-    constexpr int FTY = G::FTY, NT = G::NT, RH = G::RH, VW = G::VW;
-    constexpr unsigned BYTES = RH * RW * sizeof(CT) + RH * VW * sizeof(VT) + (UPDATE ? RH * VW * 4 : 0);
+    constexpr int FTY = G::FTY, NT = G::NT, RH = G::RH, NS = G::NS, SL = RH * RW;
+    constexpr unsigned BYTES =
+        RH * RW * sizeof(CT) + RH * V::VW * sizeof(VT) + (UPDATE ? RH * VQ::VW * 4 : 0);
     extern __shared__ __align__(128) unsigned char smem_raw[];
     SM& S = aligned_smem<SM>(smem_raw);
     __shared__ double sh[NT / 32];
     const int t = threadIdx.x;
+    constexpr int ISSUER = NT - 1;  // no task in any stage
     const float sigma = FINE ? sc->sigma : 1.0f;
     const float alpha = UPDATE ? sc->alpha_f : 0.0f;
     const int x0 = blockIdx.x * PX, y0 = blockIdx.y * FTY;
@@ -176,38 +214,41 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
     const int zs = z0 - 2, nsteps = z1 - z0 + 4;  // planes zs .. z1+1
     const long long sxy = (long long)g.nx * g.ny;
     int last_issued = 0;
-    auto issue = [&](int k) {  // thread 0: the copies of plane zs + k
+    auto issue = [&](int k, int off) {  // the copies of plane zs + k
         const int zz = zs + k;
         unsigned long long* b = &S.bar[k & 1];
         fence_proxy_async();
         mbar_expect_tx(b, BYTES);
-        tma_4d(&S.c[k & 3][0][0], &tm_rec, 2 * x0 - 8, 0, y0 - 2, zz, b);
-        tma_3d(&S.rv[k & 1][0][0], &tm_r, x0 - 8, y0 - 2, zz, b);
-        if (UPDATE) tma_3d(&S.qv[k & 1][0][0], &tm_q, x0 - 8, y0 - 2, zz, b);
+        tma_4d(&S.c[0][0][0] + off, &tm_rec, 2 * x0 - 8, 0, y0 - 2, zz, b);
+        tma_3d(&S.rv[k & 1][0][0], &tm_r, x0 - V::XS, y0 - 2, zz, b);
+        if (UPDATE) tma_3d(&S.qv[k & 1][0][0], &tm_q, x0 - VQ::XS, y0 - 2, zz, b);
         last_issued = k;
     };
-    if (t == 0) {
+    if (t == ISSUER) {
         mbar_init(&S.bar[0], 1);
         mbar_init(&S.bar[1], 1);
         S.abort_ = 0;
         fence_barrier_init();
     }
     __syncthreads();
-    if (t == 0) issue(0);
+    if (t == ISSUER) issue(0, 0);
 
-    // red task: quad r_q of staged row r_row
+    // red task
+    int r_row, r_q;
+    stage_task(t, RH, 0, &r_row, &r_q);
     const bool has_red = t < G::NRED;
-    const int r_row = t / NQ, r_q = t - (t / NQ) * NQ;
-    const int r_o = r_row * RW + 2 * r_q;          // split offset of the quad's even half
-    const int r_v = r_row * VW + G::VX + 4 * r_q;  // its cells in a copied vector row
+    const int r_o = r_row * RW + 2 * r_q;             // split offset of the quad's even half
+    const int r_v = r_row * V::VW + V::VX + 4 * r_q;  // its cells in a copied vector row
+    const int r_qv = r_row * VQ::VW + VQ::VX + 4 * r_q;
     const int r_gx = x0 - XO + 4 * r_q, r_gy = y0 - 2 + r_row;
     const int r_par = r_gy & 1;
     const int r_own = (has_red && r_row >= 2 && r_row < FTY + 2 && r_q >= 1 && r_q <= QX && r_gx < g.nx && r_gy < g.ny)
                           ? r_gx + g.nx * r_gy
                           : -1;
-    // black task: quad b_q of staged row b_row (1 .. FTY+2)
+    // black task
+    int b_row, b_q;
+    stage_task(t, G::NBR, 1, &b_row, &b_q);
     const bool has_blk = t < G::NBLK;
-    const int b_row = t / NQ + 1, b_q = t - (t / NQ) * NQ;
     const int b_o = b_row * RW + 2 * b_q;
     const int b_par = (y0 - 2 + b_row) & 1;
     // tile task: the own quad
@@ -218,6 +259,8 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
     const int oo = (ty + 2) * RW + 2 * (tx + 1);
     const long long og = ox + (long long)g.nx * oy;
 
+    const CT* c0 = &S.c[0][0][0];
+    float* e0 = &S.er[0][0][0];
     float rr_thread = 0.f;
     float2 part = make_float2(0.f, 0.f);
     int rc_z = -1;
@@ -229,13 +272,13 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
         }
         rc_z = -1;
     };
+    // element offsets of the ring slots of planes zA, zA-1, zA-2, zA-3
+    int o0 = 0, o1 = (NS - 1) * SL, o2 = (NS - 2) * SL, o3 = (NS - 3) * SL;
     auto step = [&](auto ph, int k) {
         constexpr int P = decltype(ph)::value;  // k & 3; zs is even, so plane zA has parity P & 1
         const int zA = zs + k;
-        __syncthreads();
-        const bool aborted = S.abort_ != 0;
-        if (t == 0 && k + 1 < nsteps && !aborted) issue(k + 1);
-        flush_rc();
+        const bool aborted = *reinterpret_cast<volatile int*>(&S.abort_) != 0;
+        if (t == ISSUER && k + 1 < nsteps && !aborted) issue(k + 1, o0 == (NS - 1) * SL ? 0 : o0 + SL);
         if (!aborted && !mbar_wait(&S.bar[P & 1], P >> 1)) {
             S.abort_ = 1;
             sc->stalled = 1;
@@ -243,11 +286,11 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
         }
         // ---- red stage: plane zA over the 2-halo rows
         if (has_red) {
-            const CT* C = &S.c[P][0][0];
-            float* ER = &S.er[P][0][0];
+            const CT* C = c0 + o0;
+            float* ER = e0 + o0;
             float4 rn = cvt4r<VT>(*reinterpret_cast<const R4*>(&S.rv[P & 1][0][0] + r_v));
             if (UPDATE) {
-                const float4 qq = *reinterpret_cast<const float4*>(&S.qv[P & 1][0][0] + r_v);
+                const float4 qq = *reinterpret_cast<const float4*>(&S.qv[P & 1][0][0] + r_qv);
                 rn = make_float4(fmaf(-alpha, qq.x, rn.x), fmaf(-alpha, qq.y, rn.y), fmaf(-alpha, qq.z, rn.z),
                                  fmaf(-alpha, qq.w, rn.w));
             }
@@ -265,13 +308,14 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
             }
         }
         __syncthreads();
+        flush_rc();
         // ---- black stage: plane zA-1 over the 1-halo rows, in place
         if (has_blk && zA - 1 >= z0 - 1) {
-            const CT* C = &S.c[(P + 3) & 3][0][0];
-            const CT* CN = &S.c[P][0][0];
-            float* E = &S.er[(P + 3) & 3][0][0];
-            const float* EM = &S.er[(P + 2) & 3][0][0];
-            const float* EP = &S.er[P][0][0];
+            const CT* C = c0 + o1;
+            const CT* CN = c0 + o0;
+            float* E = e0 + o1;
+            const float* EM = e0 + o2;
+            const float* EP = e0 + o0;
             const int h = b_par ^ (P & 1);  // black half of the row at plane zA-1
             const int o = b_o + h * HW;
             float2 d;
@@ -282,11 +326,11 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
         // ---- correction out and restriction: plane zA-2 over the tile
         const int zC = zA - 2;
         if (has_own && zC >= z0 && zC < z1) {
-            const CT* C = &S.c[(P + 2) & 3][0][0];
-            const CT* CN = &S.c[(P + 3) & 3][0][0];
-            const float* E = &S.er[(P + 2) & 3][0][0];
-            const float* EM = &S.er[(P + 1) & 3][0][0];
-            const float* EP = &S.er[(P + 3) & 3][0][0];
+            const CT* C = c0 + o2;
+            const CT* CN = c0 + o1;
+            const float* E = e0 + o2;
+            const float* EM = e0 + o3;
+            const float* EP = e0 + o1;
             const int p = (oy & 1) ^ (P & 1);  // red half of the own quad
             float2 d;
             const float2 s = gs_sum2<CK>(C, CN, E, EM, EP, oo + p * HW, p, make_float2(0.f, 0.f), &d);
@@ -298,26 +342,36 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
                 st4<VT>(e + (og + sxy * zC), make_float4(ev.x, od.x, ev.y, od.y));
             }
             if ((zC & 1) || zC + 1 == z1) {
-                // the row pair sum is formed after the next barrier
+                // the row pair sum is formed after the next step's first barrier
                 S.ypart[ty][tx] = part;
                 rc_z = zC >> 1;
                 part = make_float2(0.f, 0.f);
             }
         }
     };
+    auto advance = [&]() {
+        o3 = o2;
+        o2 = o1;
+        o1 = o0;
+        o0 = o0 == (NS - 1) * SL ? 0 : o0 + SL;
+    };
     for (int k = 0;;) {
         step(Phase<0>{}, k);
+        advance();
         if (++k >= nsteps) break;
         step(Phase<1>{}, k);
+        advance();
         if (++k >= nsteps) break;
         step(Phase<2>{}, k);
+        advance();
         if (++k >= nsteps) break;
         step(Phase<3>{}, k);
+        advance();
         if (++k >= nsteps) break;
     }
     __syncthreads();
     flush_rc();
-    if (t == 0 && S.abort_) (void)mbar_wait(&S.bar[last_issued & 1], (last_issued >> 1) & 1);
+    if (t == ISSUER && S.abort_) (void)mbar_wait(&S.bar[last_issued & 1], (last_issued >> 1) & 1);
     if (UPDATE) {
         double v1[1] = {(double)rr_thread};
         block_sum<1>(v1, sh);
@@ -342,7 +396,8 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
 
 // ----------------------------------------------------- post-smoothing pass
 // See k_prolong_postsmooth; e, r and the coarse correction arrive through
-// tm_e, tm_r and tm_ec, the records through tm_rec.
+// tm_e, tm_r and tm_ec, the records through tm_rec.  Step structure as in
+// k_pre_tma.
 template <int CK, class VT, class VTc, bool DOT, bool FINE>
 __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
     k_post_tma(const __grid_constant__ CUtensorMap tm_rec, const __grid_constant__ CUtensorMap tm_e,
@@ -352,16 +407,18 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
     if (sc->converged) return;
     using CT = typename CoefStore<CK>::T;
     using G = TGeo<CK>;
+    using V = VGeo<VT>;
     using SM = PostTmaSm<CK, VT, VTc>;
     using R4 = typename Raw4<VT>::T;
     using C2 = typename Raw2<VTc>::T;
-    constexpr int FTY = G::FTY, NT = G::NT, RH = G::RH, VW = G::VW;
-    constexpr unsigned BYTES = RH * RW * sizeof(CT) + 2 * RH * VW * sizeof(VT);
+    constexpr int FTY = G::FTY, NT = G::NT, RH = G::RH, NS = G::NS, SL = RH * RW;
+    constexpr unsigned BYTES = RH * RW * sizeof(CT) + 2 * RH * V::VW * sizeof(VT);
     constexpr unsigned EC_BYTES = G::CRH * G::CW * sizeof(VTc);
     extern __shared__ __align__(128) unsigned char smem_raw[];
     SM& S = aligned_smem<SM>(smem_raw);
     __shared__ double sh[NT / 32];
     const int t = threadIdx.x;
+    constexpr int ISSUER = NT - 1;
     const float sigma = FINE ? sc->sigma : 1.0f;
     const float is = FINE ? sc->inv_sigma : 1.0f;
     const int x0 = blockIdx.x * PX, y0 = blockIdx.y * FTY;
@@ -369,36 +426,38 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
     const int zs = z0 - 2, nsteps = z1 - z0 + 4;
     const long long sxy = (long long)g.nx * g.ny;
     int last_issued = 0;
-    auto issue = [&](int k) {  // thread 0: the copies of plane zs + k (and its coarse plane when it starts one)
+    auto issue = [&](int k, int off) {  // the copies of plane zs + k (and its coarse plane when it starts one)
         const int zz = zs + k;
         unsigned long long* b = &S.bar[k & 1];
         fence_proxy_async();
         mbar_expect_tx(b, BYTES + ((k & 1) ? 0u : EC_BYTES));
-        tma_4d(&S.c[k & 3][0][0], &tm_rec, 2 * x0 - 8, 0, y0 - 2, zz, b);
-        tma_3d(&S.ev[k & 1][0][0], &tm_e, x0 - 8, y0 - 2, zz, b);
-        tma_3d(&S.rv[k & 1][0][0], &tm_r, x0 - 8, y0 - 2, zz, b);
+        tma_4d(&S.c[0][0][0] + off, &tm_rec, 2 * x0 - 8, 0, y0 - 2, zz, b);
+        tma_3d(&S.ev[k & 1][0][0], &tm_e, x0 - V::XS, y0 - 2, zz, b);
+        tma_3d(&S.rv[k & 1][0][0], &tm_r, x0 - V::XS, y0 - 2, zz, b);
         if (!(k & 1)) tma_3d(&S.ec[(k >> 1) & 1][0], &tm_ec, (x0 >> 1) - 8, (y0 >> 1) - 1, zz >> 1, b);
         last_issued = k;
     };
-    if (t == 0) {
+    if (t == ISSUER) {
         mbar_init(&S.bar[0], 1);
         mbar_init(&S.bar[1], 1);
         S.abort_ = 0;
         fence_barrier_init();
     }
     __syncthreads();
-    if (t == 0) issue(0);
+    if (t == ISSUER) issue(0, 0);
 
+    int r_row, r_q;
+    stage_task(t, RH, 0, &r_row, &r_q);
     const bool has_red = t < G::NRED;
-    const int r_row = t / NQ, r_q = t - (t / NQ) * NQ;
     const int r_o = r_row * RW + 2 * r_q;
-    const int r_v = r_row * VW + G::VX + 4 * r_q;
+    const int r_v = r_row * V::VW + V::VX + 4 * r_q;
     const int r_c = (r_row >> 1) * G::CW + 6 + 2 * r_q;  // the quad's two coarse parents
     const int r_gx = x0 - XO + 4 * r_q, r_gy = y0 - 2 + r_row;
     const int r_par = r_gy & 1;
     const bool r_inside = r_gx >= 0 && r_gx < g.nx && r_gy >= 0 && r_gy < g.ny;
+    int b_row, b_q;
+    stage_task(t, G::NBR, 1, &b_row, &b_q);
     const bool has_blk = t < G::NBLK;
-    const int b_row = t / NQ + 1, b_q = t - (t / NQ) * NQ;
     const int b_o = b_row * RW + 2 * b_q;
     const int b_par = (y0 - 2 + b_row) & 1;
     const bool has_own = t < G::NOWN;
@@ -406,17 +465,19 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
     const int ox = x0 + 4 * tx, oy = y0 + ty;
     const bool own_inside = has_own && ox < g.nx && oy < g.ny;
     const int oo = (ty + 2) * RW + 2 * (tx + 1);
-    const int ov = (ty + 2) * VW + G::VX + 4 * (tx + 1);
+    const int ov = (ty + 2) * V::VW + V::VX + 4 * (tx + 1);
     const long long og = ox + (long long)g.nx * oy;
+    const CT* c0 = &S.c[0][0][0];
+    float* e0 = &S.ep[0][0][0];
     Acc acc;
     R4 rq_own[4];  // own quad's right-hand side of planes zA-3 .. zA (slot zA & 3)
 
+    int o0 = 0, o1 = (NS - 1) * SL, o2 = (NS - 2) * SL, o3 = (NS - 3) * SL;
     auto step = [&](auto ph, int k) {
         constexpr int P = decltype(ph)::value;
         const int zA = zs + k;
-        __syncthreads();
-        const bool aborted = S.abort_ != 0;
-        if (t == 0 && k + 1 < nsteps && !aborted) issue(k + 1);
+        const bool aborted = *reinterpret_cast<volatile int*>(&S.abort_) != 0;
+        if (t == ISSUER && k + 1 < nsteps && !aborted) issue(k + 1, o0 == (NS - 1) * SL ? 0 : o0 + SL);
         if (!aborted && !mbar_wait(&S.bar[P & 1], P >> 1)) {
             S.abort_ = 1;
             sc->stalled = 1;
@@ -425,7 +486,7 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
         if (has_own) rq_own[P] = *reinterpret_cast<const R4*>(&S.rv[P & 1][0][0] + ov);
         // ---- prolongation: plane zA over the 2-halo rows
         if (has_red) {
-            float* EP = &S.ep[P][0][0];
+            float* EP = e0 + o0;
             float4 ev = make_float4(0.f, 0.f, 0.f, 0.f), rq = ev;
             float2 cv = make_float2(0.f, 0.f);
             if (r_inside && zA >= 0 && zA < g.nz) {
@@ -442,11 +503,11 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
         __syncthreads();
         // ---- black half-step: plane zA-1 over the 1-halo rows, in place
         if (has_blk && zA - 1 >= z0 - 1) {
-            const CT* C = &S.c[(P + 3) & 3][0][0];
-            const CT* CN = &S.c[P][0][0];
-            float* E = &S.ep[(P + 3) & 3][0][0];
-            const float* EM = &S.ep[(P + 2) & 3][0][0];
-            const float* EP = &S.ep[P][0][0];
+            const CT* C = c0 + o1;
+            const CT* CN = c0 + o0;
+            float* E = e0 + o1;
+            const float* EM = e0 + o2;
+            const float* EP = e0 + o0;
             const int h = b_par ^ (P & 1);
             const int o = b_o + h * HW;
             float2 d;
@@ -457,11 +518,11 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
         // ---- red half-step: plane zA-2 over the tile, out = z
         const int zC = zA - 2;
         if (has_own && zC >= z0 && zC < z1) {
-            const CT* C = &S.c[(P + 2) & 3][0][0];
-            const CT* CN = &S.c[(P + 3) & 3][0][0];
-            const float* E = &S.ep[(P + 2) & 3][0][0];
-            const float* EM = &S.ep[(P + 1) & 3][0][0];
-            const float* EP = &S.ep[(P + 3) & 3][0][0];
+            const CT* C = c0 + o2;
+            const CT* CN = c0 + o1;
+            const float* E = e0 + o2;
+            const float* EM = e0 + o3;
+            const float* EP = e0 + o1;
             const int p = (oy & 1) ^ (P & 1);
             const float4 rv = cvt4r<VT>(rq_own[(P + 2) & 3]);
             const float2 rr = p ? make_float2(rv.y, rv.w) : make_float2(rv.x, rv.z);
@@ -485,17 +546,28 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
             }
         }
     };
+    auto advance = [&]() {
+        o3 = o2;
+        o2 = o1;
+        o1 = o0;
+        o0 = o0 == (NS - 1) * SL ? 0 : o0 + SL;
+    };
     for (int k = 0;;) {
         step(Phase<0>{}, k);
+        advance();
         if (++k >= nsteps) break;
         step(Phase<1>{}, k);
+        advance();
         if (++k >= nsteps) break;
         step(Phase<2>{}, k);
+        advance();
         if (++k >= nsteps) break;
         step(Phase<3>{}, k);
+        advance();
         if (++k >= nsteps) break;
     }
-    if (t == 0 && S.abort_) (void)mbar_wait(&S.bar[last_issued & 1], (last_issued >> 1) & 1);
+    __syncthreads();
+    if (t == ISSUER && S.abort_) (void)mbar_wait(&S.bar[last_issued & 1], (last_issued >> 1) & 1);
     if (DOT) {
         double v1[1] = {acc.total()};
         block_sum<1>(v1, sh);
@@ -614,9 +686,9 @@ bool pre_tma(const Grid3& g, const Grid3& gc, const void* sm, const void* rin, c
     if (!aligned16(sm) || !aligned16(rin) || (UPDATE && !aligned16(q))) return false;
     CUtensorMap tm_rec, tm_r, tm_q;
     if (!rec_map(&tm_rec, sm, CK, g, G::RH)) return false;
-    if (!vec_map(&tm_r, rin, (int)sizeof(VT), g, G::VW, G::RH)) return false;
+    if (!vec_map(&tm_r, rin, (int)sizeof(VT), g, VGeo<VT>::VW, G::RH)) return false;
     if (UPDATE) {
-        if (!vec_map(&tm_q, q, 4, g, G::VW, G::RH)) return false;
+        if (!vec_map(&tm_q, q, 4, g, VGeo<float>::VW, G::RH)) return false;
     } else {
         tm_q = tm_r;
     }
@@ -633,8 +705,8 @@ bool post_tma(const Grid3& g, const Grid3& gc, const void* sm, const void* e, co
     if ((gc.nx * (int)sizeof(VTc)) % 16) return false;
     CUtensorMap tm_rec, tm_e, tm_r, tm_ec;
     if (!rec_map(&tm_rec, sm, CK, g, G::RH)) return false;
-    if (!vec_map(&tm_e, e, (int)sizeof(VT), g, G::VW, G::RH)) return false;
-    if (!vec_map(&tm_r, r, (int)sizeof(VT), g, G::VW, G::RH)) return false;
+    if (!vec_map(&tm_e, e, (int)sizeof(VT), g, VGeo<VT>::VW, G::RH)) return false;
+    if (!vec_map(&tm_r, r, (int)sizeof(VT), g, VGeo<VT>::VW, G::RH)) return false;
     if (!vec_map(&tm_ec, ec, (int)sizeof(VTc), gc, G::CW, G::CRH)) return false;
     const Launch P = tma_launch(g, G::FTY, G::NT, g_occ[CK][FINE ? 0 : 1][1]);
     k_post_tma<CK, VT, VTc, DOT, FINE><<<P.grid, P.block, sizeof(PostTmaSm<CK, VT, VTc>) + 128, s>>>(
