@@ -53,7 +53,8 @@ void launch_divergence(const Launch& L, const Fields& F, const float* u, const f
                        cudaStream_t s);
 void launch_apply(const Launch& L, const Fields& F, const float* x, float* y, cudaStream_t s);
 void launch_set_sigma(Scalars* sc, float sigma, cudaStream_t s);
-void launch_profile_reset(Scalars* sc, cudaStream_t s);
+// no_stop: also disable the stop test, so repeated launches keep running
+void launch_profile_reset(Scalars* sc, cudaStream_t s, bool no_stop = false);
 void launch_scale(const Launch& L, const float* in, float* out, float scale, const Scalars* sc, cudaStream_t s);
 // adjoint and chain
 void launch_adj_rhs(const Launch& L, const Fields& F, const float* gu, const float* gv, const float* gw,
