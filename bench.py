@@ -503,6 +503,8 @@ def run_ours(args):
         msf, _ = timed(pr, 3, fwd_only)
         msa, sta = timed(pr, 3, vjp_step)
         line["adjoint_over_forward"] = msa / msf
+        line["adjoint"] = {"iterations": sta[-1].iterations, "refinements": sta[-1].refinements,
+                           "ms": msa / 3, "forward_ms": msf / 3}
         # end to end through the C ABI with host buffers (pinned)
         pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
         h_alpha, h_solid = pin(case["alpha"]), pin(case["solid"])
@@ -567,8 +569,16 @@ def run_ours(args):
                             "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
                             "traffic": measured_traffic(args.workload, args.precision, best["name"]),
                             "algorithmic_bytes_per_launch": best["bytes"]}
-        line["kernels"] = [{"name": k["name"], "us": k["ms"] * 1e3, "GBps": k["bytes"] / (k["ms"] * 1e-3) / 1e9,
+        line["kernels"] = [{"name": k["name"], "us": k["ms"] * 1e3,
+                            "GBps": k["bytes"] / (k["ms"] * 1e-3) / 1e9 if k["bytes"] > 0 and k["ms"] > 0 else None,
                             "per_iteration": k["per_iteration"]} for k in prof]
+        # share of a projection spent below the finest level: one coarse-grid
+        # correction per CG iteration plus one per refinement pass start
+        crs = next((k for k in prof if k["name"] == "coarse_levels"), None)
+        if crs is not None:
+            cycles = its[-1] + sts[-1].refinements + 1
+            line["coarse_levels"] = {"us_per_vcycle": crs["ms"] * 1e3, "vcycles": cycles,
+                                     "share_of_step": crs["ms"] * cycles / ms_per}
         # gauge/topology labelling of the solid mask on the GPU (union-find,
         # four kernels), run when the mask changes
         topo = next((k for k in prof if k["name"] == "topology"), None)

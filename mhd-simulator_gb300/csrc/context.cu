@@ -1694,6 +1694,8 @@ static void profile_launch(mhdproj_ctx* ctx, int kind, int r, const Fields& F, c
             break;
         case 11: mg_fused_pre(ctx->mg, ctx->r, ctx->q, ctx->r1, ctx->partials, s); break;
         case 12: mg_fused_post(ctx->mg, ctx->r1, ctx->partials, ctx->n_active, s); break;
+        case 13: mg_fused_coarse(ctx->mg, ctx->partials, ctx->n_active, s); break;
+        case 14: mg_bottom_cycle(ctx->mg, s); break;
     }
 }
 
@@ -1751,6 +1753,11 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
         {"step_viscous", 3.0 * (16.0 + mask_bytes), 0, 21},
         // faces 12 + mask + potential 4 (+ liquid fraction 4) -> reductions
         {"step_fields", 20.0 + mask_bytes, 0, 22},
+        // the coarse-grid correction of one V-cycle (every level below the
+        // finest, W-cycle visits and bottom sub-cycle included) and one bottom
+        // sub-cycle launch: latency-bound, no byte model
+        {"coarse_levels", 0.0, 0, 13},
+        {"bottom_subcycle", 0.0, 0, 14},
     };
     const Item* items = ctx->pipelined ? pipelined : classic;
     const int n_items = ctx->pipelined ? (int)(sizeof pipelined / sizeof pipelined[0])
@@ -1761,6 +1768,7 @@ extern "C" int mhdproj_profile_kernels(mhdproj_ctx* ctx, int reps, mhdproj_kerne
         if (k >= max_out) break;
         if (!ctx->use_mg && (it.kind >= 2 && it.kind <= 4)) continue;
         if (it.kind >= 20 && it.kind <= 22 && !ctx->step_ran) continue;
+        if (it.kind == 14 && ctx->mg.bottom_from <= 0) continue;
         launch_set_sigma(ctx->sc, 1.0f, s);  // clears the converged flag
         if (it.kind >= 10) launch_profile_reset(ctx->sc, s);
         // Timed as `reps` launches inside one CUDA graph, each after a small

@@ -789,6 +789,15 @@ void mg_smoother_records(const MGPlan& P, cudaStream_t s) {
     else records_impl<0>(P, s);
 }
 
+// The coarse-grid correction of one V-cycle (level 1 and below), for
+// measurement.
+void mg_fused_coarse(const MGPlan& P, double* partials, long long n_active, cudaStream_t s) {
+    if (P.fused_levels < 1 || P.nlevels < 2) return;
+    if (P.precision == 1) (void)fused_solve_level<1, __half>(P, 1, partials, n_active, s);
+    else if (P.precision == 2) (void)fused_solve_level<2, __nv_bfloat16>(P, 1, partials, n_active, s);
+    else (void)fused_solve_level<0, float>(P, 1, partials, n_active, s);
+}
+
 // Single passes, for measurement.
 void mg_fused_pre(const MGPlan& P, const float* r_in, const float* q, float* r_out, double* partials,
                   cudaStream_t s) {

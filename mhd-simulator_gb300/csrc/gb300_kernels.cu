@@ -23,6 +23,27 @@ namespace mhdproj {
     const int z0 = blockIdx.z * (G).zper;                  \
     const int z1 = min((G).nz, z0 + (G).zper);             \
     for (int z = z0; z < z1; z++)
+// A thread's (x, y) column and z run, for kernels that walk the run two
+// planes at a time: both planes' loads are issued before either plane's
+// arithmetic (the one-pass set-up kernels are bound by memory latency).
+#define TILE_COLUMN(G)                                     \
+    const int x = blockIdx.x * TX + threadIdx.x;           \
+    const int y = blockIdx.y * TY + threadIdx.y;           \
+    const bool in_xy = x < (G).nx && y < (G).ny;           \
+    const int z0 = blockIdx.z * (G).zper;                  \
+    const int z1 = min((G).nz, z0 + (G).zper)
+// Runs load(z) -> In and finish(z, In) over the column's planes in pairs.
+template <class Load, class Finish>
+__device__ __forceinline__ void walk_pairs(int z0, int z1, Load load, Finish finish) {
+    int z = z0;
+    for (; z + 1 < z1; z += 2) {
+        const auto a = load(z);
+        const auto b = load(z + 1);
+        finish(z, a);
+        finish(z + 1, b);
+    }
+    if (z < z1) finish(z, load(z));
+}
 
 __device__ __forceinline__ int cell_index(const Grid3& g, int x, int y, int z) { return x + g.nx * (y + g.ny * z); }
 
@@ -130,28 +151,45 @@ __global__ void __launch_bounds__(TILE_THREADS) k_rhs(Grid3 g, int outlet, float
     __shared__ double sh[8 * 1];
     Acc acc;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    TILE_BEGIN(g) {
-        if (!in_xy) continue;
+    TILE_COLUMN(g);
+    struct In {
+        float ulo, uhi, vlo, vhi, wlo, whi;
+        uint8_t ci, cxm, cxp, cym, cyp, czm, czp;
+        bool zp_in;  // the cell above exists (not the top of a closed z axis)
+    };
+    // every load of a cell first (face indices are always valid)
+    auto load = [&](int z) {
+        In L;
         const int i = cell_index(g, x, y, z);
-        df bi = {0.0f, 0.0f};
-        // every load first (face indices are always valid), then the sums
         const Nbr nb = neighbours(g, x, y, z);
-        const uint8_t ci = cls[i];
-        const uint8_t cxm = nb.xm >= 0 ? cls[nb.xm] : 0, cxp = nb.xp >= 0 ? cls[nb.xp] : 0;
-        const uint8_t cym = nb.ym >= 0 ? cls[nb.ym] : 0, cyp = nb.yp >= 0 ? cls[nb.yp] : 0;
-        const uint8_t czm = nb.zm >= 0 ? cls[nb.zm] : 0, czp = nb.zp >= 0 ? cls[nb.zp] : 0;
+        L.ci = cls[i];
+        L.cxm = nb.xm >= 0 ? cls[nb.xm] : 0;
+        L.cxp = nb.xp >= 0 ? cls[nb.xp] : 0;
+        L.cym = nb.ym >= 0 ? cls[nb.ym] : 0;
+        L.cyp = nb.yp >= 0 ? cls[nb.yp] : 0;
+        L.czm = nb.zm >= 0 ? cls[nb.zm] : 0;
+        L.czp = nb.zp >= 0 ? cls[nb.zp] : 0;
+        L.zp_in = nb.zp >= 0;
         const int hx = (x + 1 == nx && (g.periodic & 1)) ? 0 : x + 1;
         const int hy = (y + 1 == ny && (g.periodic & 2)) ? 0 : y + 1;
         const int hz = (z + 1 == nz && (g.periodic & 4)) ? 0 : z + 1;
-        const float ulo = u[x + (nx + 1) * (y + ny * z)], uhi = u[hx + (nx + 1) * (y + ny * z)];
-        const float vlo = v[x + nx * (y + (ny + 1) * z)], vhi = v[x + nx * (hy + (ny + 1) * z)];
-        const float wlo = w[x + nx * (y + ny * z)], whi = w[x + nx * (y + ny * hz)];
-        if (ci == 1) {
+        L.ulo = u[x + (nx + 1) * (y + ny * z)];
+        L.uhi = u[hx + (nx + 1) * (y + ny * z)];
+        L.vlo = v[x + nx * (y + (ny + 1) * z)];
+        L.vhi = v[x + nx * (hy + (ny + 1) * z)];
+        L.wlo = w[x + nx * (y + ny * z)];
+        L.whi = w[x + nx * (y + ny * hz)];
+        return L;
+    };
+    auto finish = [&](int z, const In& L) {
+        const int i = cell_index(g, x, y, z);
+        df bi = {0.0f, 0.0f};
+        if (L.ci == 1) {
             df sum = {0.0f, 0.0f};
-            sum = df_add(sum, two_sum(cxp != 0 ? uhi : 0.0f, -(cxm != 0 ? ulo : 0.0f)));
-            sum = df_add(sum, two_sum(cyp != 0 ? vhi : 0.0f, -(cym != 0 ? vlo : 0.0f)));
-            const bool hopen = (nb.zp >= 0 && czp != 0) || (nb.zp < 0 && outlet && z + 1 == nz);
-            sum = df_add(sum, two_sum(hopen ? whi : 0.0f, -(czm != 0 ? wlo : 0.0f)));
+            sum = df_add(sum, two_sum(L.cxp != 0 ? L.uhi : 0.0f, -(L.cxm != 0 ? L.ulo : 0.0f)));
+            sum = df_add(sum, two_sum(L.cyp != 0 ? L.vhi : 0.0f, -(L.cym != 0 ? L.vlo : 0.0f)));
+            const bool hopen = (L.zp_in && L.czp != 0) || (!L.zp_in && outlet && z + 1 == nz);
+            sum = df_add(sum, two_sum(hopen ? L.whi : 0.0f, -(L.czm != 0 ? L.wlo : 0.0f)));
             bi = df_mul_f(sum, -h);
         }
         b_hi[i] = bi.hi;
@@ -161,7 +199,8 @@ __global__ void __launch_bounds__(TILE_THREADS) k_rhs(Grid3 g, int outlet, float
             r[i] = df_to_f(bi);
             xs[i] = 0.0f;
         }
-    }
+    };
+    if (in_xy) walk_pairs(z0, z1, load, finish);
     double v1[1] = {acc.total()};
     block_sum<1>(v1, sh);
     if (store_partials_is_last<1>(v1, partials, nblocks, &sc->ticket[0])) {
@@ -567,27 +606,45 @@ __global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, f
                                                           float* __restrict__ po) {
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const float inv_h = 1.0f / h;
-    TILE_BEGIN(g) {
-        if (!in_xy) continue;
+    TILE_COLUMN(g);
+    struct In {
+        df pi, pxm, pym, pzm;
+        float ai, axm, aym, azm, uin, vin, win;
+        int xm, ym, zm;  // low neighbours or -1
+        uint8_t ci, cxm, cym, czm;
+    };
+    // every load of a cell first (guarded by the coordinates only)
+    auto load = [&](int z) {
+        In L;
         const int i = cell_index(g, x, y, z);
         const Nbr nb = neighbours(g, x, y, z);
-        // every load first (guarded by the coordinates only), then the faces
-        const uint8_t ci = cls[i];
-        const df pi = {ph[i], pl[i]};
-        const float ai = alpha[i];
-        const uint8_t cxm = nb.xm >= 0 ? cls[nb.xm] : 0, cym = nb.ym >= 0 ? cls[nb.ym] : 0;
-        const uint8_t czm = nb.zm >= 0 ? cls[nb.zm] : 0;
-        const float axm = nb.xm >= 0 ? alpha[nb.xm] : 0.f, aym = nb.ym >= 0 ? alpha[nb.ym] : 0.f;
-        const float azm = nb.zm >= 0 ? alpha[nb.zm] : 0.f;
-        const df pxm = nb.xm >= 0 ? df{ph[nb.xm], pl[nb.xm]} : pi, pym = nb.ym >= 0 ? df{ph[nb.ym], pl[nb.ym]} : pi;
-        const df pzm = nb.zm >= 0 ? df{ph[nb.zm], pl[nb.zm]} : pi;
-        const float uin = us[x + (nx + 1) * (y + ny * z)], vin = vs[x + nx * (y + (ny + 1) * z)];
-        const float win = ws[x + nx * (y + ny * z)];
+        L.xm = nb.xm;
+        L.ym = nb.ym;
+        L.zm = nb.zm;
+        L.ci = cls[i];
+        L.pi = {ph[i], pl[i]};
+        L.ai = alpha[i];
+        L.cxm = nb.xm >= 0 ? cls[nb.xm] : 0;
+        L.cym = nb.ym >= 0 ? cls[nb.ym] : 0;
+        L.czm = nb.zm >= 0 ? cls[nb.zm] : 0;
+        L.axm = nb.xm >= 0 ? alpha[nb.xm] : 0.f;
+        L.aym = nb.ym >= 0 ? alpha[nb.ym] : 0.f;
+        L.azm = nb.zm >= 0 ? alpha[nb.zm] : 0.f;
+        L.pxm = nb.xm >= 0 ? df{ph[nb.xm], pl[nb.xm]} : L.pi;
+        L.pym = nb.ym >= 0 ? df{ph[nb.ym], pl[nb.ym]} : L.pi;
+        L.pzm = nb.zm >= 0 ? df{ph[nb.zm], pl[nb.zm]} : L.pi;
+        L.uin = us[x + (nx + 1) * (y + ny * z)];
+        L.vin = vs[x + nx * (y + (ny + 1) * z)];
+        L.win = ws[x + nx * (y + ny * z)];
+        return L;
+    };
+    auto finish = [&](int z, const In& L) {
+        const int i = cell_index(g, x, y, z);
         {
             const int f = x + (nx + 1) * (y + ny * z);
             float out = 0.0f;
-            if (nb.xm >= 0 && ci != 0 && cxm != 0)
-                out = uin - grad_term(mobility_of(mob, axm, ai, nb.xm, i), pi, pxm, inv_h);
+            if (L.xm >= 0 && L.ci != 0 && L.cxm != 0)
+                out = L.uin - grad_term(mobility_of(mob, L.axm, L.ai, L.xm, i), L.pi, L.pxm, inv_h);
             uo[f] = out;
             if (x == 0 && (g.periodic & 1)) uo[nx + (nx + 1) * (y + ny * z)] = out;
             if (x == nx - 1 && !(g.periodic & 1)) uo[nx + (nx + 1) * (y + ny * z)] = 0.0f;
@@ -595,8 +652,8 @@ __global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, f
         {
             const int f = x + nx * (y + (ny + 1) * z);
             float out = 0.0f;
-            if (nb.ym >= 0 && ci != 0 && cym != 0)
-                out = vin - grad_term(mobility_of(mob, aym, ai, nb.ym, i), pi, pym, inv_h);
+            if (L.ym >= 0 && L.ci != 0 && L.cym != 0)
+                out = L.vin - grad_term(mobility_of(mob, L.aym, L.ai, L.ym, i), L.pi, L.pym, inv_h);
             vo[f] = out;
             if (y == 0 && (g.periodic & 2)) vo[x + nx * (ny + (ny + 1) * z)] = out;
             if (y == ny - 1 && !(g.periodic & 2)) vo[x + nx * (ny + (ny + 1) * z)] = 0.0f;
@@ -604,19 +661,20 @@ __global__ void __launch_bounds__(TILE_THREADS) k_correct(Grid3 g, int outlet, f
         {
             const int f = x + nx * (y + ny * z);
             float out = 0.0f;
-            if (nb.zm >= 0 && ci != 0 && czm != 0)
-                out = win - grad_term(mobility_of(mob, azm, ai, nb.zm, i), pi, pzm, inv_h);
+            if (L.zm >= 0 && L.ci != 0 && L.czm != 0)
+                out = L.win - grad_term(mobility_of(mob, L.azm, L.ai, L.zm, i), L.pi, L.pzm, inv_h);
             wo[f] = out;
             const int ft = x + nx * (y + ny * nz);
             if (z == 0 && (g.periodic & 4)) wo[ft] = out;
             if (z == nz - 1 && !(g.periodic & 4)) {
                 float top = 0.0f;
-                if (outlet && ci != 0) top = ws[ft] + __fmul_rn(__fmul_rn(gtop[x + nx * y], df_to_f(pi)), inv_h);
+                if (outlet && L.ci != 0) top = ws[ft] + __fmul_rn(__fmul_rn(gtop[x + nx * y], df_to_f(L.pi)), inv_h);
                 wo[ft] = top;
             }
         }
-        if (po) po[i] = ci != 0 ? __fmul_rn(p_scale, df_to_f(pi)) : 0.0f;
-    }
+        if (po) po[i] = L.ci != 0 ? __fmul_rn(p_scale, df_to_f(L.pi)) : 0.0f;
+    };
+    if (in_xy) walk_pairs(z0, z1, load, finish);
 }
 
 // max |div u| and sum div^2 over active cells of a face field.

@@ -158,6 +158,8 @@ void mg_vcycle_fused(const MGPlan& P, const float* r_in, const float* q, float* 
                      long long n_active, cudaStream_t s);
 void mg_fused_pre(const MGPlan& P, const float* r_in, const float* q, float* r_out, double* partials, cudaStream_t s);
 void mg_fused_post(const MGPlan& P, const float* r, double* partials, long long n_active, cudaStream_t s);
+void mg_fused_coarse(const MGPlan& P, double* partials, long long n_active, cudaStream_t s);
+void mg_bottom_cycle(const MGPlan& P, cudaStream_t s);
 // Smoother records of the fused levels, after every coefficient change.
 void mg_smoother_records(const MGPlan& P, cudaStream_t s);
 void launch_search_spmv(const Launch& L, const float4* coef, const float* z, const float* p_old, float* p_new,

@@ -445,35 +445,92 @@ __global__ void __launch_bounds__(256) k_coarse_invert(Grid3 g, const float4* __
 // per cell, so the sub-cycle stays a fixed symmetric operator).
 constexpr int BOTTOM_THREADS = 1024;
 
+// Cell lists of the bottom sub-cycle: per level the red cells, then the
+// black ones, each colour in index order.  On a grid without periodic axes a
+// list entry is a flat word: the cell index (bits 0-12), which of its six
+// neighbours exist (bits 13-18: x-, x+, y-, y+, z-, z+) and its parent cell
+// on the next level (bits 19-31), so the loops decode no coordinates and
+// test no wrap-around.  With a periodic axis an entry holds the packed
+// coordinates x | y << 10 | z << 20 and the loops take the wrap-aware path.
+constexpr unsigned BW_XM = 1u << 13, BW_XP = 1u << 14, BW_YM = 1u << 15, BW_YP = 1u << 16, BW_ZM = 1u << 17,
+                   BW_ZP = 1u << 18;
+__device__ __forceinline__ int bw_index(unsigned w) { return (int)(w & 0x1fffu); }
+__device__ __forceinline__ int bw_parent(unsigned w) { return (int)(w >> 19); }
+
+// Exclusive prefix sum of one count per thread over the block (blockDim.x a
+// multiple of 32, at most 1024).
+__device__ int block_exclusive_scan(int v, int* warp_tot) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int s = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, s, o);
+        if (lane >= o) s += u;
+    }
+    if (lane == 31) warp_tot[wid] = s;
+    __syncthreads();
+    if (wid == 0) {
+        int w = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += u;
+        }
+        warp_tot[lane] = w;  // inclusive totals of warps 0 .. lane
+    }
+    __syncthreads();
+    const int r = (wid ? warp_tot[wid - 1] : 0) + s - v;
+    __syncthreads();  // warp_tot is reused by the next call
+    return r;
+}
+
 // The shared-memory image of the bottom sub-cycle that depends only on the
 // coefficients, built once per coefficient set: per level the records with
-// the diagonal in place of the reaction (k_smooth's sum order) and the cells'
-// packed coordinates (x | y << 10 | z << 20) listed red first, so loops run
-// over the cells of one colour without index arithmetic; then the coarsest
-// inverse.  Every launch of k_bottom_vcycle copies it in with 16-byte
-// cp.async.
+// the diagonal in place of the reaction (k_smooth's sum order) and the cell
+// list; then the coarsest inverse.  Every launch of k_bottom_vcycle copies it
+// in with 16-byte cp.async.
 template <int CK>
 __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_image(BottomPlan B, float4* __restrict__ img) {
     extern __shared__ float4 bsm4[];
     float* bsm = reinterpret_cast<float*>(bsm4);
     const int t = threadIdx.x, nt = blockDim.x;
     auto nb = [](int c, int n, bool per) { return wrap_or_neg(c, n, per); };
-    __shared__ int fill[8][2];
-    if (t < 16) fill[t >> 1][t & 1] = 0;
-    __syncthreads();
-    // Per level: coefficient records, and the cells' packed coordinates
-    // (x | y << 10 | z << 20) listed red first, so loops run over the cells
-    // of one colour without index arithmetic.
+    __shared__ int warp_tot[32];
     for (int l = 0; l < B.nl; l++) {
         const BottomLevel& L = B.lv[l];
+        const Grid3& g = L.g;
         float4* c = bsm4 + L.coff;
-        int* cells = reinterpret_cast<int*>(bsm + L.xoff);
-        for (int i = t; i < L.n; i += nt) {
-            c[i] = ldc<CK>(L.coef, i);
-            const int x = i % L.g.nx, y = (i / L.g.nx) % L.g.ny, z = i / (L.g.nx * L.g.ny);
-            const int col = (x + y + z) & 1;
-            const int k = atomicAdd(&fill[l][col], 1);
-            cells[col ? L.nred + k : k] = x | (y << 10) | (z << 20);
+        unsigned* cells = reinterpret_cast<unsigned*>(bsm + L.xoff);
+        for (int i = t; i < L.n; i += nt) c[i] = ldc<CK>(L.coef, i);
+        // thread t lists the cells of one contiguous chunk; a scan of the red
+        // counts gives each cell its place in the colour-ordered list
+        const int chunk = (L.n + nt - 1) / nt;
+        const int i0 = min(L.n, t * chunk), i1 = min(L.n, i0 + chunk);
+        int red = 0;
+        for (int i = i0; i < i1; i++) {
+            const int x = i % g.nx, y = (i / g.nx) % g.ny, z = i / (g.nx * g.ny);
+            red += ((x + y + z) & 1) == 0;
+        }
+        int rk = block_exclusive_scan(red, warp_tot);  // red cells before i0
+        const bool flat = g.periodic == 0;
+        const Grid3 gc = l + 1 < B.nl ? B.lv[l + 1].g : g;
+        for (int i = i0; i < i1; i++) {
+            const int x = i % g.nx, y = (i / g.nx) % g.ny, z = i / (g.nx * g.ny);
+            unsigned w;
+            if (flat) {
+                w = (unsigned)i;
+                if (x > 0) w |= BW_XM;
+                if (x + 1 < g.nx) w |= BW_XP;
+                if (y > 0) w |= BW_YM;
+                if (y + 1 < g.ny) w |= BW_YP;
+                if (z > 0) w |= BW_ZM;
+                if (z + 1 < g.nz) w |= BW_ZP;
+                if (l + 1 < B.nl) w |= (unsigned)((x >> 1) + gc.nx * ((y >> 1) + gc.ny * (z >> 1))) << 19;
+            } else {
+                w = (unsigned)(x | (y << 10) | (z << 20));
+            }
+            if (((x + y + z) & 1) == 0) cells[rk++] = w;
+            else cells[L.nred + (i - rk)] = w;  // i - rk black cells precede i
         }
     }
     __syncthreads();
@@ -524,7 +581,8 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
     staged::cp_wait<0>();
     __syncthreads();
     auto nb = [](int c, int n, bool per) { return wrap_or_neg(c, n, per); };
-    // sum of beta * e over the six neighbours (k_smooth order) and the diagonal
+    // sum of beta * e over the six neighbours (k_smooth order) and the
+    // diagonal; wrap-aware, for levels with a periodic axis
     auto stencil = [&](const BottomLevel& L, const float4* c, const float* e, int x, int y, int z, int i, float acc,
                        float* d) {
         const Grid3& g = L.g;
@@ -546,19 +604,42 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
         acc = fmaf(bzh, zp >= 0 ? e[i + (zp - z) * sz] : 0.f, acc);
         return acc;
     };
+    // the same sums for a flat list word: fixed strides, neighbour bits
+    auto stencil_flat = [&](const float4* c, const float* e, unsigned w, int sy, int sz, float acc, float* d) {
+        const int i = bw_index(w);
+        const float4 cc = c[i];
+        const float bxh = (w & BW_XP) ? c[i + 1].x : 0.f;
+        const float byh = (w & BW_YP) ? c[i + sy].y : 0.f;
+        const float bzh = (w & BW_ZP) ? c[i + sz].z : 0.f;
+        *d = cc.w;
+        acc = fmaf(cc.x, (w & BW_XM) ? e[i - 1] : 0.f, acc);
+        acc = fmaf(bxh, (w & BW_XP) ? e[i + 1] : 0.f, acc);
+        acc = fmaf(cc.y, (w & BW_YM) ? e[i - sy] : 0.f, acc);
+        acc = fmaf(byh, (w & BW_YP) ? e[i + sy] : 0.f, acc);
+        acc = fmaf(cc.z, (w & BW_ZM) ? e[i - sz] : 0.f, acc);
+        acc = fmaf(bzh, (w & BW_ZP) ? e[i + sz] : 0.f, acc);
+        return acc;
+    };
     auto half_step = [&](int l, int color, bool zero) {
         const BottomLevel& L = B.lv[l];
         const Grid3& g = L.g;
         const float4* c = bsm4 + L.coff;
-        const int* cells = reinterpret_cast<const int*>(bsm + L.xoff);
+        const unsigned* cells = reinterpret_cast<const unsigned*>(bsm + L.xoff);
         const float* r = bsm + L.off;
         float* e = bsm + L.off + L.n;
         float* tmp = bsm + L.off + 2 * L.n;
+        const bool flat = g.periodic == 0;
         if (zero) {  // from zero: red cells r / d, black cells 0
 #pragma unroll 4
             for (int k = t; k < L.n; k += nt) {
-                const int cc = cells[k], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
-                const int i = x + g.nx * (y + g.ny * z);
+                const unsigned cc = cells[k];
+                int i;
+                if (flat) {
+                    i = bw_index(cc);
+                } else {
+                    const int x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+                    i = x + g.nx * (y + g.ny * z);
+                }
                 float val = 0.f;
                 if (k < L.nred) {
                     const float d = c[i].w;
@@ -570,9 +651,22 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
             return;
         }
         const int k0 = color ? L.nred : 0, k1 = color ? L.n : L.nred;
+        if (flat) {  // never odd: odd extents only matter on periodic axes
+            const int sy = g.nx, sz = g.nx * g.ny;
+#pragma unroll 2
+            for (int k = k0 + t; k < k1; k += nt) {
+                const unsigned w = cells[k];
+                float d;
+                const float acc = stencil_flat(c, e, w, sy, sz, r[bw_index(w)], &d);
+                e[bw_index(w)] = d > 0.f ? __fdividef(acc, d) : 0.f;
+            }
+            __syncthreads();
+            return;
+        }
 #pragma unroll 2
         for (int k = k0 + t; k < k1; k += nt) {
-            const int cc = cells[k], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+            const unsigned cc = cells[k];
+            const int x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
             const int i = x + g.nx * (y + g.ny * z);
             float d;
             const float acc = stencil(L, c, e, x, y, z, i, r[i], &d);
@@ -583,7 +677,8 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
         __syncthreads();
         if (L.odd) {
             for (int k = k0 + t; k < k1; k += nt) {
-                const int cc = cells[k], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+                const unsigned cc = cells[k];
+                const int x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
                 const int i = x + g.nx * (y + g.ny * z);
                 e[i] = tmp[i];
             }
@@ -602,20 +697,31 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
         const float* r = bsm + F.off;
         const float* e = bsm + F.off + F.n;
         float* rc = bsm + C.off;
-        const int* ccells = reinterpret_cast<const int*>(bsm + C.xoff);
+        const unsigned* ccells = reinterpret_cast<const unsigned*>(bsm + C.xoff);
         if (!F.odd) {
             float* rs = bsm + F.off + 2 * F.n;
-            const int* cells = reinterpret_cast<const int*>(bsm + F.xoff);
+            const unsigned* cells = reinterpret_cast<const unsigned*>(bsm + F.xoff);
+            if (g.periodic == 0) {
+                const int sy = g.nx, sz = g.nx * g.ny;
 #pragma unroll 2
-            for (int k = t; k < F.nred; k += nt) {
-                const int cc = cells[k], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
-                const int i = x + g.nx * (y + g.ny * z);
-                float d;
-                rs[i] = stencil(F, c, e, x, y, z, i, 0.f, &d);
+                for (int k = t; k < F.nred; k += nt) {
+                    const unsigned w = cells[k];
+                    float d;
+                    rs[bw_index(w)] = stencil_flat(c, e, w, sy, sz, 0.f, &d);
+                }
+            } else {
+#pragma unroll 2
+                for (int k = t; k < F.nred; k += nt) {
+                    const unsigned cc = cells[k];
+                    const int x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+                    const int i = x + g.nx * (y + g.ny * z);
+                    float d;
+                    rs[i] = stencil(F, c, e, x, y, z, i, 0.f, &d);
+                }
             }
             __syncthreads();
-            for (int k = t; k < C.n; k += nt) {
-                const int cq = ccells[k], X = cq & 1023, Y = (cq >> 10) & 1023, Z = cq >> 20;
+            for (int K = t; K < C.n; K += nt) {
+                const int X = K % gc.nx, Y = (K / gc.nx) % gc.ny, Z = K / (gc.nx * gc.ny);
                 float part = 0.f;
                 for (int dz = 0; dz < 2; dz++)
                     for (int dy = 0; dy < 2; dy++)
@@ -624,13 +730,14 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
                             if (x >= g.nx || y >= g.ny || z >= g.nz || ((x + y + z) & 1)) continue;
                             part += rs[x + g.nx * (y + g.ny * z)];
                         }
-                rc[X + gc.nx * (Y + gc.ny * Z)] = 0.25f * part;
+                rc[K] = 0.25f * part;
             }
             __syncthreads();
             return;
         }
         for (int k = t; k < C.n; k += nt) {
-            const int cq = ccells[k], X = cq & 1023, Y = (cq >> 10) & 1023, Z = cq >> 20;
+            const unsigned cq = ccells[k];
+            const int X = cq & 1023, Y = (cq >> 10) & 1023, Z = cq >> 20;
             float part = 0.f;
             for (int dz = 0; dz < 2; dz++)
                 for (int dy = 0; dy < 2; dy++)
@@ -651,11 +758,20 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
         const Grid3 &g = F.g, &gc = C.g;
         float* e = bsm + F.off + F.n;
         const float* ec = bsm + C.off + C.n;
-        const int* cells = reinterpret_cast<const int*>(bsm + F.xoff);
-        for (int k = t; k < F.n; k += nt) {
-            const int cc = cells[k], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
-            const int i = x + g.nx * (y + g.ny * z);
-            e[i] = fmaf(B.w, ec[(x >> 1) + gc.nx * ((y >> 1) + gc.ny * (z >> 1))], e[i]);
+        const unsigned* cells = reinterpret_cast<const unsigned*>(bsm + F.xoff);
+        if (g.periodic == 0) {
+            for (int k = t; k < F.n; k += nt) {
+                const unsigned w = cells[k];
+                const int i = bw_index(w);
+                e[i] = fmaf(B.w, ec[bw_parent(w)], e[i]);
+            }
+        } else {
+            for (int k = t; k < F.n; k += nt) {
+                const unsigned cc = cells[k];
+                const int x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+                const int i = x + g.nx * (y + g.ny * z);
+                e[i] = fmaf(B.w, ec[(x >> 1) + gc.nx * ((y >> 1) + gc.ny * (z >> 1))], e[i]);
+            }
         }
         __syncthreads();
     };
@@ -690,24 +806,39 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
             const BottomLevel& L = B.lv[l];
             const Grid3& g = L.g;
             const float4* c = bsm4 + L.coff;
-            const int* cells = reinterpret_cast<const int*>(bsm + L.xoff);
+            const unsigned* cells = reinterpret_cast<const unsigned*>(bsm + L.xoff);
             float* r = bsm + L.off;
             const float* e = bsm + L.off + L.n;
             float* es = bsm + L.off + 3 * L.n;
+            const bool flat = g.periodic == 0;
+            const int sy = g.nx, sz = g.nx * g.ny;
             float rn[4];  // each thread's cells, at most 4096 / 1024
             int cnt = 0;
             for (int q = t; q < L.n; q += nt) {
-                const int cc = cells[q], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
-                const int i = x + g.nx * (y + g.ny * z);
-                float d;
-                const float nsum = stencil(L, c, e, x, y, z, i, 0.f, &d);
+                const unsigned cc = cells[q];
+                float d, nsum;
+                int i;
+                if (flat) {
+                    i = bw_index(cc);
+                    nsum = stencil_flat(c, e, cc, sy, sz, 0.f, &d);
+                } else {
+                    const int x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+                    i = x + g.nx * (y + g.ny * z);
+                    nsum = stencil(L, c, e, x, y, z, i, 0.f, &d);
+                }
                 rn[cnt++] = r[i] - (d * e[i] - nsum);
             }
             __syncthreads();
             cnt = 0;
             for (int q = t; q < L.n; q += nt) {
-                const int cc = cells[q], x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
-                const int i = x + g.nx * (y + g.ny * z);
+                const unsigned cc = cells[q];
+                int i;
+                if (flat) {
+                    i = bw_index(cc);
+                } else {
+                    const int x = cc & 1023, y = (cc >> 10) & 1023, z = cc >> 20;
+                    i = x + g.nx * (y + g.ny * z);
+                }
                 r[i] = rn[cnt++];
                 es[i] = e[i];
             }
@@ -812,6 +943,16 @@ void mg_vcycle_from(const MGPlan& P, int l0, cudaStream_t s) {
 }
 
 void mg_vcycle(const MGPlan& P, cudaStream_t s) { mg_vcycle_from(P, 0, s); }
+
+// One launch of the bottom sub-cycle on its current right-hand side, for
+// measurement.
+void mg_bottom_cycle(const MGPlan& P, cudaStream_t s) {
+    if (P.bottom_from <= 0) return;
+    if (P.precision == 1) k_bottom_vcycle<1, __half><<<1, BOTTOM_THREADS, P.bottom_smem, s>>>(P.bottom, P.sc);
+    else if (P.precision == 2)
+        k_bottom_vcycle<2, __nv_bfloat16><<<1, BOTTOM_THREADS, P.bottom_smem, s>>>(P.bottom, P.sc);
+    else k_bottom_vcycle<0, float><<<1, BOTTOM_THREADS, P.bottom_smem, s>>>(P.bottom, P.sc);
+}
 
 template <int CK, class VT>
 static void fine_restrict_impl(const MGPlan& P, cudaStream_t s) {
