@@ -62,6 +62,7 @@ struct TGeo {
     static constexpr int CRH = FTY / 2 + 2;            // coarse rows y0/2-1 .. y0/2+FTY/2
     static constexpr int CW = 48;                      // coarse columns x0/2-8 .. x0/2+39
     static constexpr int NS = 5;                       // ring slots of records and corrections: zA-3 .. zA+1
+    static constexpr int NP = 6;                       // planes of a run of two with its halo (whole-run passes)
     static_assert(NBLK <= NT && NOWN <= NT && NRED < NT, "one task per thread");
 };
 // Staged rows of a level vector: x0-4 .. x0+67 for FP32 (the first
@@ -598,6 +599,297 @@ __global__ void __launch_bounds__(TGeo<CK>::NT, TMA_MIN_BLOCKS)
     }
 }
 
+// ------------------------------------------------- whole-run coarse passes
+// On a coarse level whose runs of two planes fill at most one wave of one
+// block per SM (the 64^3 and 32^3 levels below a 256^3 or 128^3 grid), a
+// z-marching pass is six plane steps of three dependent stages each, and the
+// stages' latency, not bandwidth, sets its time.  These kernels do the same
+// work with each stage over every plane of the run at once: the red (or
+// prolongation) stage over planes z0-2 .. z1+1, the black half-step over
+// z0-1 .. z1, the restriction (or last red half-step) over z0 .. z1-1, with a
+// barrier between stages.  Every plane's copies are issued when the block
+// starts, each plane on its own mbarrier.  The per-cell arithmetic and its
+// order are those of k_pre_tma / k_post_tma on coarse levels, so every
+// vector written is bit-identical.
+template <int CK, class VT>
+struct PreRunSm {
+    using CT = typename CoefStore<CK>::T;
+    using G = TGeo<CK>;
+    using V = VGeo<VT>;
+    alignas(128) CT c[G::NP][G::RH][RW];
+    alignas(128) VT rv[G::NP][G::RH][V::VW];
+    alignas(16) float er[G::NP][G::RH][RW];
+    float2 ypart[G::FTY][QX];
+    unsigned long long bar[G::NP];
+    int abort_;
+};
+template <int CK, class VT, class VTc>
+struct PostRunSm {
+    using CT = typename CoefStore<CK>::T;
+    using G = TGeo<CK>;
+    using V = VGeo<VT>;
+    static constexpr int ECS = padded128<VTc, G::CRH * G::CW>();
+    alignas(128) CT c[G::NP][G::RH][RW];
+    alignas(128) VT ev[G::NP][G::RH][V::VW];
+    alignas(128) VT rv[G::NP][G::RH][V::VW];
+    alignas(128) VTc ec[G::NP / 2][ECS];
+    alignas(16) float ep[G::NP][G::RH][RW];
+    unsigned long long bar[G::NP];
+    int abort_;
+};
+
+// Issue the copies of planes zs .. zs+np-1 (thread ISSUER) and wait for all of
+// them (every thread, bounded); false when a wait ran out.
+template <class SM, class IssueFn>
+__device__ __forceinline__ bool run_copies(SM& S, int np, int issuer, IssueFn issue_plane) {
+    const int t = threadIdx.x;
+    if (t == issuer) {
+        for (int k = 0; k < (int)(sizeof(S.bar) / sizeof(S.bar[0])); k++) mbar_init(&S.bar[k], 1);
+        S.abort_ = 0;
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (t == issuer)
+        for (int k = 0; k < np; k++) issue_plane(k, &S.bar[k]);
+    bool ok = true;
+    for (int k = 0; k < np && ok; k++) ok = mbar_wait(&S.bar[k], 0);
+    return ok;
+}
+// After a timed-out wait: the issuing thread waits (bounded) for every copy
+// it issued before the block exits.
+template <class SM>
+__device__ __forceinline__ void run_drain(SM& S, int np, int issuer) {
+    if (threadIdx.x == issuer && S.abort_)
+        for (int k = 0; k < np; k++) (void)mbar_wait(&S.bar[k], 0);
+}
+
+template <int CK, class VT, class VTc>
+__global__ void __launch_bounds__(TGeo<CK>::NT, 1)
+    k_pre_run(const __grid_constant__ CUtensorMap tm_rec, const __grid_constant__ CUtensorMap tm_r, Grid3 g,
+              Grid3 gc, VT* __restrict__ e, VTc* __restrict__ rc, Scalars* sc) {
+    if (sc->converged) return;
+    using CT = typename CoefStore<CK>::T;
+    using G = TGeo<CK>;
+    using V = VGeo<VT>;
+    using SM = PreRunSm<CK, VT>;
+    using R4 = typename Raw4<VT>::T;
+    constexpr int FTY = G::FTY, NT = G::NT, RH = G::RH, NP = G::NP, SL = RH * RW;
+    constexpr unsigned BYTES = RH * RW * sizeof(CT) + RH * V::VW * sizeof(VT);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    SM& S = aligned_smem<SM>(smem_raw);
+    const int t = threadIdx.x;
+    constexpr int ISSUER = NT - 1;
+    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * FTY;
+    const int z0 = blockIdx.z * 2, z1 = min(g.nz, z0 + 2);
+    const int zs = z0 - 2, np = z1 - z0 + 4;  // planes zs .. z1+1; zs is even
+    const long long sxy = (long long)g.nx * g.ny;
+    const bool ok = run_copies(S, np, ISSUER, [&](int k, unsigned long long* b) {
+        fence_proxy_async();
+        mbar_expect_tx(b, BYTES);
+        tma_4d(&S.c[k][0][0], &tm_rec, 2 * x0 - 8, 0, y0 - 2, zs + k, b);
+        tma_3d(&S.rv[k][0][0], &tm_r, x0 - V::XS, y0 - 2, zs + k, b);
+    });
+    if (!ok) {
+        S.abort_ = 1;
+        sc->stalled = 1;
+        sc->converged = 1;
+    }
+    const CT* c0 = &S.c[0][0][0];
+    float* e0 = &S.er[0][0][0];
+    // ---- red stage, planes 0 .. np-1 over the 2-halo rows
+    if (ok && t < G::NRED) {
+        int row, q;
+        stage_task(t, RH, 0, &row, &q);
+        const int o = row * RW + 2 * q, vo = row * V::VW + V::VX + 4 * q;
+        const int par = (y0 - 2 + row) & 1;
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            if (k >= np) break;
+            const float4 rn = cvt4r<VT>(*reinterpret_cast<const R4*>(&S.rv[k][0][0] + vo));
+            const int p = par ^ (k & 1);
+            float4 d0, d1;
+            rec2<CK>(c0 + k * SL + o + p * HW, &d0, &d1);
+            const float2 rr = p ? make_float2(rn.y, rn.w) : make_float2(rn.x, rn.z);
+            const float2 rb = p ? make_float2(rn.x, rn.z) : make_float2(rn.y, rn.w);
+            const float2 ev = divide2(make_float2(1.0f * rr.x, 1.0f * rr.y), make_float2(d0.w, d1.w));
+            *reinterpret_cast<float2*>(e0 + k * SL + o + p * HW) = ev;
+            *reinterpret_cast<float2*>(e0 + k * SL + o + (1 - p) * HW) = make_float2(1.0f * rb.x, 1.0f * rb.y);
+        }
+    }
+    __syncthreads();
+    // ---- black half-step, planes 1 .. np-2 over the 1-halo rows, in place
+    if (ok && t < G::NBLK) {
+        int row, q;
+        stage_task(t, G::NBR, 1, &row, &q);
+        const int ob = row * RW + 2 * q;
+        const int par = (y0 - 2 + row) & 1;
+#pragma unroll
+        for (int k = 1; k < NP - 1; k++) {
+            if (k > np - 2) break;
+            const int h = par ^ ((k + 1) & 1);
+            const int o = ob + h * HW;
+            float* E = e0 + k * SL;
+            float2 d;
+            const float2 s = gs_sum2<CK>(c0 + k * SL, c0 + (k + 1) * SL, E, E - SL, E + SL, o, h,
+                                         *reinterpret_cast<const float2*>(E + o), &d);
+            *reinterpret_cast<float2*>(E + o) = divide2(s, d);
+        }
+    }
+    __syncthreads();
+    // ---- correction out and restriction, planes 2 .. np-3 over the tile
+    const bool has_own = t < G::NOWN;
+    const int tx = t % QX, ty = t / QX;
+    const int ox = x0 + 4 * tx, oy = y0 + ty;
+    const bool own_inside = has_own && ox < g.nx && oy < g.ny;
+    const int oo = (ty + 2) * RW + 2 * (tx + 1);
+    const long long og = ox + (long long)g.nx * oy;
+    if (ok && has_own) {
+        float2 part = make_float2(0.f, 0.f);
+        for (int k = 2; k < np - 2; k++) {
+            const int zC = zs + k;
+            const float* E = e0 + k * SL;
+            const int p = (oy & 1) ^ (k & 1);
+            float2 d;
+            const float2 s = gs_sum2<CK>(c0 + k * SL, c0 + (k + 1) * SL, E, E - SL, E + SL, oo + p * HW, p,
+                                         make_float2(0.f, 0.f), &d);
+            part.x += s.x;
+            part.y += s.y;
+            if (own_inside) {
+                const float2 ev = *reinterpret_cast<const float2*>(E + oo);
+                const float2 od = *reinterpret_cast<const float2*>(E + oo + HW);
+                st4<VT>(e + (og + sxy * zC), make_float4(ev.x, od.x, ev.y, od.y));
+            }
+        }
+        S.ypart[ty][tx] = part;
+    }
+    __syncthreads();
+    if (ok && own_inside && !(ty & 1)) {
+        const float2 a = S.ypart[ty][tx], b = S.ypart[ty + 1][tx];
+        st2<VTc>(rc + (ox >> 1) + (long long)gc.nx * ((oy >> 1) + (long long)gc.ny * (z0 >> 1)),
+                 make_float2(0.25f * (a.x + b.x), 0.25f * (a.y + b.y)));
+    }
+    run_drain(S, np, ISSUER);
+}
+
+template <int CK, class VT, class VTc>
+__global__ void __launch_bounds__(TGeo<CK>::NT, 1)
+    k_post_run(const __grid_constant__ CUtensorMap tm_rec, const __grid_constant__ CUtensorMap tm_e,
+               const __grid_constant__ CUtensorMap tm_r, const __grid_constant__ CUtensorMap tm_ec, Grid3 g,
+               VT* __restrict__ out, const VT* __restrict__ accum, float w, Scalars* sc) {
+    if (sc->converged) return;
+    using CT = typename CoefStore<CK>::T;
+    using G = TGeo<CK>;
+    using V = VGeo<VT>;
+    using SM = PostRunSm<CK, VT, VTc>;
+    using R4 = typename Raw4<VT>::T;
+    using C2 = typename Raw2<VTc>::T;
+    constexpr int FTY = G::FTY, NT = G::NT, RH = G::RH, NP = G::NP, SL = RH * RW;
+    constexpr unsigned BYTES = RH * RW * sizeof(CT) + 2 * RH * V::VW * sizeof(VT);
+    constexpr unsigned EC_BYTES = G::CRH * G::CW * sizeof(VTc);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    SM& S = aligned_smem<SM>(smem_raw);
+    const int t = threadIdx.x;
+    constexpr int ISSUER = NT - 1;
+    const int x0 = blockIdx.x * PX, y0 = blockIdx.y * FTY;
+    const int z0 = blockIdx.z * 2, z1 = min(g.nz, z0 + 2);
+    const int zs = z0 - 2, np = z1 - z0 + 4;
+    const long long sxy = (long long)g.nx * g.ny;
+    const bool ok = run_copies(S, np, ISSUER, [&](int k, unsigned long long* b) {
+        const int zz = zs + k;
+        fence_proxy_async();
+        mbar_expect_tx(b, BYTES + ((k & 1) ? 0u : EC_BYTES));
+        tma_4d(&S.c[k][0][0], &tm_rec, 2 * x0 - 8, 0, y0 - 2, zz, b);
+        tma_3d(&S.ev[k][0][0], &tm_e, x0 - V::XS, y0 - 2, zz, b);
+        tma_3d(&S.rv[k][0][0], &tm_r, x0 - V::XS, y0 - 2, zz, b);
+        if (!(k & 1)) tma_3d(&S.ec[k >> 1][0], &tm_ec, (x0 >> 1) - 8, (y0 >> 1) - 1, zz >> 1, b);
+    });
+    if (!ok) {
+        S.abort_ = 1;
+        sc->stalled = 1;
+        sc->converged = 1;
+    }
+    const CT* c0 = &S.c[0][0][0];
+    float* e0 = &S.ep[0][0][0];
+    // ---- prolongation, planes 0 .. np-1 over the 2-halo rows
+    if (ok && t < G::NRED) {
+        int row, q;
+        stage_task(t, RH, 0, &row, &q);
+        const int o = row * RW + 2 * q, vo = row * V::VW + V::VX + 4 * q;
+        const int co = (row >> 1) * G::CW + 6 + 2 * q;  // the quad's two coarse parents
+        const int gx = x0 - XO + 4 * q, gy = y0 - 2 + row;
+        const int par = gy & 1;
+        const bool inside = gx >= 0 && gx < g.nx && gy >= 0 && gy < g.ny;
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            if (k >= np) break;
+            const int zA = zs + k;
+            float4 ev = make_float4(0.f, 0.f, 0.f, 0.f), rq = ev;
+            float2 cv = make_float2(0.f, 0.f);
+            if (inside && zA >= 0 && zA < g.nz) {
+                ev = cvt4r<VT>(*reinterpret_cast<const R4*>(&S.ev[k][0][0] + vo));
+                rq = cvt4r<VT>(*reinterpret_cast<const R4*>(&S.rv[k][0][0] + vo));
+                cv = cvt2(*reinterpret_cast<const C2*>(&S.ec[k >> 1][0] + co));
+            }
+            const int p = par ^ (k & 1);
+            const float2 er = p ? make_float2(ev.y, ev.w) : make_float2(ev.x, ev.z);
+            const float2 rb = p ? make_float2(rq.x, rq.z) : make_float2(rq.y, rq.w);
+            float* EP = e0 + k * SL;
+            *reinterpret_cast<float2*>(EP + o + p * HW) = make_float2(fmaf(w, cv.x, er.x), fmaf(w, cv.y, er.y));
+            *reinterpret_cast<float2*>(EP + o + (1 - p) * HW) = make_float2(1.0f * rb.x, 1.0f * rb.y);
+        }
+    }
+    __syncthreads();
+    // ---- black half-step, planes 1 .. np-2 over the 1-halo rows, in place
+    if (ok && t < G::NBLK) {
+        int row, q;
+        stage_task(t, G::NBR, 1, &row, &q);
+        const int ob = row * RW + 2 * q;
+        const int par = (y0 - 2 + row) & 1;
+#pragma unroll
+        for (int k = 1; k < NP - 1; k++) {
+            if (k > np - 2) break;
+            const int h = par ^ ((k + 1) & 1);
+            const int o = ob + h * HW;
+            float* E = e0 + k * SL;
+            float2 d;
+            const float2 s = gs_sum2<CK>(c0 + k * SL, c0 + (k + 1) * SL, E, E - SL, E + SL, o, h,
+                                         *reinterpret_cast<const float2*>(E + o), &d);
+            *reinterpret_cast<float2*>(E + o) = divide2(s, d);
+        }
+    }
+    __syncthreads();
+    // ---- red half-step, planes 2 .. np-3 over the tile, out = z
+    if (ok && t < G::NOWN) {
+        const int tx = t % QX, ty = t / QX;
+        const int ox = x0 + 4 * tx, oy = y0 + ty;
+        const bool own_inside = ox < g.nx && oy < g.ny;
+        const int oo = (ty + 2) * RW + 2 * (tx + 1);
+        const int ov = (ty + 2) * V::VW + V::VX + 4 * (tx + 1);
+        const long long og = ox + (long long)g.nx * oy;
+        for (int k = 2; k < np - 2; k++) {
+            const int zC = zs + k;
+            const float* E = e0 + k * SL;
+            const int p = (oy & 1) ^ (k & 1);
+            const float4 rv = cvt4r<VT>(*reinterpret_cast<const R4*>(&S.rv[k][0][0] + ov));
+            const float2 rr = p ? make_float2(rv.y, rv.w) : make_float2(rv.x, rv.z);
+            float2 d;
+            const float2 s = gs_sum2<CK>(c0 + k * SL, c0 + (k + 1) * SL, E, E - SL, E + SL, oo + p * HW, p,
+                                         make_float2(1.0f * rr.x, 1.0f * rr.y), &d);
+            const float2 zr = divide2(s, d);
+            const float2 zb = *reinterpret_cast<const float2*>(E + oo + (1 - p) * HW);
+            float4 zv = p ? make_float4(zb.x, zr.x, zb.y, zr.y) : make_float4(zr.x, zb.x, zr.y, zb.y);
+            if (own_inside) {
+                if (accum) {  // out = accum + z (second W-cycle visit)
+                    const float4 a = cvt4r<VT>(*reinterpret_cast<const R4*>(accum + og + sxy * zC));
+                    zv = make_float4(a.x + zv.x, a.y + zv.y, a.z + zv.z, a.w + zv.w);
+                }
+                st4<VT>(out + og + sxy * zC, zv);
+            }
+        }
+    }
+    run_drain(S, np, ISSUER);
+}
+
 // ------------------------------------------------------------------ host
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 bool g_tma_enabled = false;
@@ -714,6 +1006,42 @@ bool post_tma(const Grid3& g, const Grid3& gc, const void* sm, const void* e, co
     return true;
 }
 
+// Coarse levels whose runs of two planes fill at most one wave of one block
+// per SM take the whole-run passes.
+bool whole_runs(const Grid3& g, int fty) {
+    const long long tiles = (long long)((g.nx + PX - 1) / PX) * ((g.ny + fty - 1) / fty);
+    return tiles * ((g.nz + 1) / 2) <= (g_sms > 0 ? g_sms : 152);
+}
+template <int CK, class VT, class VTc>
+bool pre_run(const Grid3& g, const Grid3& gc, const void* sm, const void* rin, void* e, void* rc, Scalars* sc,
+             cudaStream_t s) {
+    using G = TGeo<CK>;
+    if (!aligned16(sm) || !aligned16(rin)) return false;
+    CUtensorMap tm_rec, tm_r;
+    if (!rec_map(&tm_rec, sm, CK, g, G::RH)) return false;
+    if (!vec_map(&tm_r, rin, (int)sizeof(VT), g, VGeo<VT>::VW, G::RH)) return false;
+    const dim3 grid((g.nx + PX - 1) / PX, (g.ny + G::FTY - 1) / G::FTY, (g.nz + 1) / 2);
+    k_pre_run<CK, VT, VTc><<<grid, G::NT, sizeof(PreRunSm<CK, VT>) + 128, s>>>(tm_rec, tm_r, g, gc, (VT*)e,
+                                                                              (VTc*)rc, sc);
+    return true;
+}
+template <int CK, class VT, class VTc>
+bool post_run(const Grid3& g, const Grid3& gc, const void* sm, const void* e, const void* ec, const void* r, void* out,
+              const void* accum, float w, Scalars* sc, cudaStream_t s) {
+    using G = TGeo<CK>;
+    if (!aligned16(sm) || !aligned16(e) || !aligned16(r) || !aligned16(ec)) return false;
+    if ((gc.nx * (int)sizeof(VTc)) % 16) return false;
+    CUtensorMap tm_rec, tm_e, tm_r, tm_ec;
+    if (!rec_map(&tm_rec, sm, CK, g, G::RH)) return false;
+    if (!vec_map(&tm_e, e, (int)sizeof(VT), g, VGeo<VT>::VW, G::RH)) return false;
+    if (!vec_map(&tm_r, r, (int)sizeof(VT), g, VGeo<VT>::VW, G::RH)) return false;
+    if (!vec_map(&tm_ec, ec, (int)sizeof(VTc), gc, G::CW, G::CRH)) return false;
+    const dim3 grid((g.nx + PX - 1) / PX, (g.ny + G::FTY - 1) / G::FTY, (g.nz + 1) / 2);
+    k_post_run<CK, VT, VTc><<<grid, G::NT, sizeof(PostRunSm<CK, VT, VTc>) + 128, s>>>(
+        tm_rec, tm_e, tm_r, tm_ec, g, (VT*)out, (const VT*)accum, w, sc);
+    return true;
+}
+
 template <class F>
 cudaError_t prep(F* fn, size_t bytes, int threads, int* occ) {
     cudaError_t e = cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -733,6 +1061,9 @@ cudaError_t prep_level(bool fine) {
     } else {
         if (e == cudaSuccess) e = prep(k_pre_tma<CK, VT, VTc, false, false>, pre_n, G::NT, &g_occ[CK][1][0]);
         if (e == cudaSuccess) e = prep(k_post_tma<CK, VT, VTc, false, false>, post, G::NT, &g_occ[CK][1][1]);
+        if (e == cudaSuccess) e = prep(k_pre_run<CK, VT, VTc>, sizeof(PreRunSm<CK, VT>) + 128, G::NT, nullptr);
+        if (e == cudaSuccess)
+            e = prep(k_post_run<CK, VT, VTc>, sizeof(PostRunSm<CK, VT, VTc>) + 128, G::NT, nullptr);
     }
     return e;
 }
@@ -775,6 +1106,11 @@ bool tma_pre(int ck, bool fine, bool update, const Grid3& g, const Grid3& gc, co
         return update ? pre_tma<0, float, float, true, true>(g, gc, sm, rin, q, r_out, e, rc, sc, partials, s)
                       : pre_tma<0, float, float, false, true>(g, gc, sm, rin, q, r_out, e, rc, sc, partials, s);
     }
+    if (whole_runs(g, ck == 0 ? TGeo<0>::FTY : TGeo<1>::FTY)) {
+        if (ck == 1) return pre_run<1, __half, __half>(g, gc, sm, rin, e, rc, sc, s);
+        if (ck == 2) return pre_run<2, __nv_bfloat16, __nv_bfloat16>(g, gc, sm, rin, e, rc, sc, s);
+        return pre_run<0, float, float>(g, gc, sm, rin, e, rc, sc, s);
+    }
     if (ck == 1) return pre_tma<1, __half, __half, false, false>(g, gc, sm, rin, q, r_out, e, rc, sc, partials, s);
     if (ck == 2)
         return pre_tma<2, __nv_bfloat16, __nv_bfloat16, false, false>(g, gc, sm, rin, q, r_out, e, rc, sc, partials, s);
@@ -793,6 +1129,11 @@ bool tma_post(int ck, bool fine, const Grid3& g, const Grid3& gc, const void* sm
             return post_tma<2, float, __nv_bfloat16, true, true>(g, gc, sm, e, ec, r, out, accum, w, sc, partials,
                                                                  n_active, s);
         return post_tma<0, float, float, true, true>(g, gc, sm, e, ec, r, out, accum, w, sc, partials, n_active, s);
+    }
+    if (whole_runs(g, ck == 0 ? TGeo<0>::FTY : TGeo<1>::FTY)) {
+        if (ck == 1) return post_run<1, __half, __half>(g, gc, sm, e, ec, r, out, accum, w, sc, s);
+        if (ck == 2) return post_run<2, __nv_bfloat16, __nv_bfloat16>(g, gc, sm, e, ec, r, out, accum, w, sc, s);
+        return post_run<0, float, float>(g, gc, sm, e, ec, r, out, accum, w, sc, s);
     }
     if (ck == 1)
         return post_tma<1, __half, __half, false, false>(g, gc, sm, e, ec, r, out, accum, w, sc, partials, n_active, s);
