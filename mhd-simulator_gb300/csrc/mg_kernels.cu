@@ -455,6 +455,14 @@ constexpr int BOTTOM_THREADS = 1024;
 constexpr unsigned BW_XM = 1u << 13, BW_XP = 1u << 14, BW_YM = 1u << 15, BW_YP = 1u << 16, BW_ZM = 1u << 17,
                    BW_ZP = 1u << 18;
 __device__ __forceinline__ int bw_index(unsigned w) { return (int)(w & 0x1fffu); }
+// A level's records in shared memory, one array per lane (beta_x, beta_y,
+// beta_z of the low faces, diagonal): the cells of one colour sit two apart,
+// so a float4 record per cell made each neighbour-face load an eight-way bank
+// conflict; with separate arrays it is two-way.
+struct RecSoA {
+    float *bx, *by, *bz, *d;
+    __device__ __forceinline__ RecSoA(float* base, int n) : bx(base), by(base + n), bz(base + 2 * n), d(base + 3 * n) {}
+};
 __device__ __forceinline__ int bw_parent(unsigned w) { return (int)(w >> 19); }
 
 // Exclusive prefix sum of one count per thread over the block (blockDim.x a
@@ -499,9 +507,15 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_image(BottomPlan B, f
     for (int l = 0; l < B.nl; l++) {
         const BottomLevel& L = B.lv[l];
         const Grid3& g = L.g;
-        float4* c = bsm4 + L.coff;
+        const RecSoA c(bsm + 4 * L.coff, L.n);
         unsigned* cells = reinterpret_cast<unsigned*>(bsm + L.xoff);
-        for (int i = t; i < L.n; i += nt) c[i] = ldc<CK>(L.coef, i);
+        for (int i = t; i < L.n; i += nt) {
+            const float4 v = ldc<CK>(L.coef, i);
+            c.bx[i] = v.x;
+            c.by[i] = v.y;
+            c.bz[i] = v.z;
+            c.d[i] = v.w;
+        }
         // thread t lists the cells of one contiguous chunk; a scan of the red
         // counts gives each cell its place in the colour-ordered list
         const int chunk = (L.n + nt - 1) / nt;
@@ -538,25 +552,24 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_image(BottomPlan B, f
     for (int l = 0; l < B.nl; l++) {
         const BottomLevel& L = B.lv[l];
         const Grid3& g = L.g;
-        float4* c = bsm4 + L.coff;
+        const RecSoA c(bsm + 4 * L.coff, L.n);
         float* dtmp = bsm + L.off + 2 * L.n;  // scratch until the cycle starts
         const bool px = g.periodic & 1, py = g.periodic & 2, pz = g.periodic & 4;
         for (int i = t; i < L.n; i += nt) {
             const int x = i % g.nx, y = (i / g.nx) % g.ny, z = i / (g.nx * g.ny);
             const int xp = nb(x + 1, g.nx, px), yp = nb(y + 1, g.ny, py), zp = nb(z + 1, g.nz, pz);
-            const float4 cc = c[i];
-            const float bxh = xp >= 0 ? c[i + (xp - x)].x : 0.f;
-            const float byh = yp >= 0 ? c[i + (yp - y) * g.nx].y : 0.f;
-            const float bzh = zp >= 0 ? c[i + (zp - z) * g.nx * g.ny].z : 0.f;
-            dtmp[i] = ((cc.x + bxh) + (cc.y + byh)) + ((cc.z + bzh) + cc.w);
+            const float bxh = xp >= 0 ? c.bx[i + (xp - x)] : 0.f;
+            const float byh = yp >= 0 ? c.by[i + (yp - y) * g.nx] : 0.f;
+            const float bzh = zp >= 0 ? c.bz[i + (zp - z) * g.nx * g.ny] : 0.f;
+            dtmp[i] = ((c.bx[i] + bxh) + (c.by[i] + byh)) + ((c.bz[i] + bzh) + c.d[i]);
         }
     }
     __syncthreads();
     for (int l = 0; l < B.nl; l++) {
         const BottomLevel& L = B.lv[l];
-        float4* c = bsm4 + L.coff;
+        const RecSoA c(bsm + 4 * L.coff, L.n);
         const float* dtmp = bsm + L.off + 2 * L.n;
-        for (int i = t; i < L.n; i += nt) c[i].w = dtmp[i];
+        for (int i = t; i < L.n; i += nt) c.d[i] = dtmp[i];
     }
     __syncthreads();
     for (int i = t; i < B.m * B.m; i += nt) bsm[B.aoff + i] = B.ainv[i];
@@ -583,7 +596,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
     auto nb = [](int c, int n, bool per) { return wrap_or_neg(c, n, per); };
     // sum of beta * e over the six neighbours (k_smooth order) and the
     // diagonal; wrap-aware, for levels with a periodic axis
-    auto stencil = [&](const BottomLevel& L, const float4* c, const float* e, int x, int y, int z, int i, float acc,
+    auto stencil = [&](const BottomLevel& L, const RecSoA& c, const float* e, int x, int y, int z, int i, float acc,
                        float* d) {
         const Grid3& g = L.g;
         const bool px = g.periodic & 1, py = g.periodic & 2, pz = g.periodic & 4;
@@ -591,39 +604,37 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
         const int xm = nb(x - 1, g.nx, px), xp = nb(x + 1, g.nx, px);
         const int ym = nb(y - 1, g.ny, py), yp = nb(y + 1, g.ny, py);
         const int zm = nb(z - 1, g.nz, pz), zp = nb(z + 1, g.nz, pz);
-        const float4 cc = c[i];
-        const float bxh = xp >= 0 ? c[i + (xp - x)].x : 0.f;
-        const float byh = yp >= 0 ? c[i + (yp - y) * sy].y : 0.f;
-        const float bzh = zp >= 0 ? c[i + (zp - z) * sz].z : 0.f;
-        *d = cc.w;
-        acc = fmaf(cc.x, xm >= 0 ? e[i + (xm - x)] : 0.f, acc);
+        const float bxh = xp >= 0 ? c.bx[i + (xp - x)] : 0.f;
+        const float byh = yp >= 0 ? c.by[i + (yp - y) * sy] : 0.f;
+        const float bzh = zp >= 0 ? c.bz[i + (zp - z) * sz] : 0.f;
+        *d = c.d[i];
+        acc = fmaf(c.bx[i], xm >= 0 ? e[i + (xm - x)] : 0.f, acc);
         acc = fmaf(bxh, xp >= 0 ? e[i + (xp - x)] : 0.f, acc);
-        acc = fmaf(cc.y, ym >= 0 ? e[i + (ym - y) * sy] : 0.f, acc);
+        acc = fmaf(c.by[i], ym >= 0 ? e[i + (ym - y) * sy] : 0.f, acc);
         acc = fmaf(byh, yp >= 0 ? e[i + (yp - y) * sy] : 0.f, acc);
-        acc = fmaf(cc.z, zm >= 0 ? e[i + (zm - z) * sz] : 0.f, acc);
+        acc = fmaf(c.bz[i], zm >= 0 ? e[i + (zm - z) * sz] : 0.f, acc);
         acc = fmaf(bzh, zp >= 0 ? e[i + (zp - z) * sz] : 0.f, acc);
         return acc;
     };
     // the same sums for a flat list word: fixed strides, neighbour bits
-    auto stencil_flat = [&](const float4* c, const float* e, unsigned w, int sy, int sz, float acc, float* d) {
+    auto stencil_flat = [&](const RecSoA& c, const float* e, unsigned w, int sy, int sz, float acc, float* d) {
         const int i = bw_index(w);
-        const float4 cc = c[i];
-        const float bxh = (w & BW_XP) ? c[i + 1].x : 0.f;
-        const float byh = (w & BW_YP) ? c[i + sy].y : 0.f;
-        const float bzh = (w & BW_ZP) ? c[i + sz].z : 0.f;
-        *d = cc.w;
-        acc = fmaf(cc.x, (w & BW_XM) ? e[i - 1] : 0.f, acc);
+        const float bxh = (w & BW_XP) ? c.bx[i + 1] : 0.f;
+        const float byh = (w & BW_YP) ? c.by[i + sy] : 0.f;
+        const float bzh = (w & BW_ZP) ? c.bz[i + sz] : 0.f;
+        *d = c.d[i];
+        acc = fmaf(c.bx[i], (w & BW_XM) ? e[i - 1] : 0.f, acc);
         acc = fmaf(bxh, (w & BW_XP) ? e[i + 1] : 0.f, acc);
-        acc = fmaf(cc.y, (w & BW_YM) ? e[i - sy] : 0.f, acc);
+        acc = fmaf(c.by[i], (w & BW_YM) ? e[i - sy] : 0.f, acc);
         acc = fmaf(byh, (w & BW_YP) ? e[i + sy] : 0.f, acc);
-        acc = fmaf(cc.z, (w & BW_ZM) ? e[i - sz] : 0.f, acc);
+        acc = fmaf(c.bz[i], (w & BW_ZM) ? e[i - sz] : 0.f, acc);
         acc = fmaf(bzh, (w & BW_ZP) ? e[i + sz] : 0.f, acc);
         return acc;
     };
     auto half_step = [&](int l, int color, bool zero) {
         const BottomLevel& L = B.lv[l];
         const Grid3& g = L.g;
-        const float4* c = bsm4 + L.coff;
+        const RecSoA c(bsm + 4 * L.coff, L.n);
         const unsigned* cells = reinterpret_cast<const unsigned*>(bsm + L.xoff);
         const float* r = bsm + L.off;
         float* e = bsm + L.off + L.n;
@@ -642,7 +653,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
                 }
                 float val = 0.f;
                 if (k < L.nred) {
-                    const float d = c[i].w;
+                    const float d = c.d[i];
                     if (d > 0.f) val = __fdividef(r[i], d);
                 }
                 e[i] = val;
@@ -693,7 +704,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
     auto restrict_to = [&](int l) {  // level l -> l+1
         const BottomLevel &F = B.lv[l], &C = B.lv[l + 1];
         const Grid3 &g = F.g, &gc = C.g;
-        const float4* c = bsm4 + F.coff;
+        const RecSoA c(bsm + 4 * F.coff, F.n);
         const float* r = bsm + F.off;
         const float* e = bsm + F.off + F.n;
         float* rc = bsm + C.off;
@@ -805,7 +816,7 @@ __global__ void __launch_bounds__(BOTTOM_THREADS) k_bottom_vcycle(BottomPlan B, 
         } else if (op == BOP_SAVE_RESID) {
             const BottomLevel& L = B.lv[l];
             const Grid3& g = L.g;
-            const float4* c = bsm4 + L.coff;
+            const RecSoA c(bsm + 4 * L.coff, L.n);
             const unsigned* cells = reinterpret_cast<const unsigned*>(bsm + L.xoff);
             float* r = bsm + L.off;
             const float* e = bsm + L.off + L.n;
