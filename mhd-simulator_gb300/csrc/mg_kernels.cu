@@ -342,13 +342,15 @@ __global__ void __launch_bounds__(TILE_THREADS) k_mg_build(Grid3 gf, Grid3 gc, c
 // block's factorisation is the same computation, so the columns agree.
 __global__ void __launch_bounds__(256) k_coarse_invert(Grid3 g, const float4* __restrict__ coef,
                                                        float* __restrict__ ainv, int pin) {
-    extern __shared__ double A[];  // m x m, then y/x vectors
-    const int m = g.nx * g.ny * g.nz;
+    // m x m with rows padded to m + 1 doubles (a column of 16 rows spans the
+    // shared-memory banks instead of hitting one), then the y/x vector
+    extern __shared__ double A[];
+    const int m = g.nx * g.ny * g.nz, lda = m + 1;
     const int t = threadIdx.x, nt = blockDim.x;
     const int b = blockIdx.x;
     __shared__ int active[64];
-    double* v = A + m * m;  // right-hand side / solution
-    for (int k = t; k < m * m; k += nt) A[k] = 0.0;
+    double* v = A + m * lda;  // right-hand side / solution
+    for (int k = t; k < m * lda; k += nt) A[k] = 0.0;
     __syncthreads();
     if (t < m) {
         const int x = t % g.nx, y = (t / g.nx) % g.ny, z = t / (g.nx * g.ny);
@@ -362,24 +364,24 @@ __global__ void __launch_bounds__(256) k_coarse_invert(Grid3 g, const float4* __
             const int lp = wrap_or_neg(p3[a] + 1, n3[a], g.periodic & (1 << a));
             if (lm >= 0 && lowb[a] != 0.0f) {
                 d += lowb[a];
-                A[t * m + (t + (lm - p3[a]) * stride)] -= lowb[a];
+                A[t * lda + (t + (lm - p3[a]) * stride)] -= lowb[a];
             }
             if (lp >= 0) {
                 const int j = t + (lp - p3[a]) * stride;
                 const float bh = (a == 0 ? coef[j].x : (a == 1 ? coef[j].y : coef[j].z));
                 if (bh != 0.0f) {
                     d += bh;
-                    A[t * m + j] -= bh;
+                    A[t * lda + j] -= bh;
                 }
             }
         }
-        A[t * m + t] += d;
+        A[t * lda + t] += d;
         active[t] = d > 0.0 && t != pin;  // a pinned cell (mean-free gauge) is held at zero
     }
     __syncthreads();
     if (t < m && !active[t]) {
-        for (int k = 0; k < m; k++) A[t * m + k] = A[k * m + t] = 0.0;
-        A[t * m + t] = 1.0;
+        for (int k = 0; k < m; k++) A[t * lda + k] = A[k * lda + t] = 0.0;
+        A[t * lda + t] = 1.0;
     }
     __syncthreads();
     // Cholesky, lower triangle in place (a non-positive pivot is treated as
@@ -391,7 +393,7 @@ __global__ void __launch_bounds__(256) k_coarse_invert(Grid3 g, const float4* __
     const int tx = t & 15, ty = t >> 4;
     for (int j = 0; j < m; j++) {
         if (t == 0) {
-            const double piv = A[j * m + j];
+            const double piv = A[j * lda + j];
             double r = 0.0;
             if (piv > 1e-30 && piv < 1e30) {
                 r = (double)rsqrtf((float)piv);
@@ -400,15 +402,15 @@ __global__ void __launch_bounds__(256) k_coarse_invert(Grid3 g, const float4* __
             } else if (piv > 1e-300) {
                 r = 1.0 / sqrt(piv);
             }
-            A[j * m + j] = piv * r;  // L_jj (0 for an empty row)
+            A[j * lda + j] = piv * r;  // L_jj (0 for an empty row)
             rsq[j] = r;
         }
         __syncthreads();
         const double rj = rsq[j];
-        for (int i = j + 1 + t; i < m; i += nt) A[i * m + j] *= rj;
+        for (int i = j + 1 + t; i < m; i += nt) A[i * lda + j] *= rj;
         __syncthreads();
         for (int i = j + 1 + ty; i < m; i += 16)
-            for (int k = j + 1 + tx; k <= i; k += 16) A[i * m + k] -= A[i * m + j] * A[k * m + j];
+            for (int k = j + 1 + tx; k <= i; k += 16) A[i * lda + k] -= A[i * lda + j] * A[k * lda + j];
         __syncthreads();
     }
     // L y = e_b, then L^T x = y, column-oriented: thread i keeps v[i]; step j
@@ -419,14 +421,14 @@ __global__ void __launch_bounds__(256) k_coarse_invert(Grid3 g, const float4* __
         const double yj = v[j] * rsq[j];
         __syncthreads();
         if (t == j) v[j] = yj;
-        else if (t > j && t < m) v[t] -= A[t * m + j] * yj;
+        else if (t > j && t < m) v[t] -= A[t * lda + j] * yj;
         __syncthreads();
     }
     for (int j = m - 1; j >= 0; j--) {
         const double xj = v[j] * rsq[j];
         __syncthreads();
         if (t == j) v[j] = xj;
-        else if (t < j) v[t] -= A[j * m + t] * xj;
+        else if (t < j) v[t] -= A[j * lda + t] * xj;
         __syncthreads();
     }
     __syncthreads();
@@ -1010,7 +1012,7 @@ void mg_build(const MGPlan& P, cudaStream_t s) {
             k_mg_build<0><<<C.L.grid, C.L.block, 0, s>>>(F.L.g, C.L.g, F.coef32, C.coef32, nullptr);
     }
     const MGLevel& K = P.lv[P.nlevels - 1];
-    const size_t smem = ((size_t)P.m * P.m + P.m) * sizeof(double);
+    const size_t smem = ((size_t)P.m * (P.m + 1) + P.m) * sizeof(double);
     k_coarse_invert<<<P.m, 256, smem, s>>>(K.L.g, K.coef32, P.ainv, P.pin_coarse);
     if (P.bottom_from > 0 && P.bottom_img) {
         if (P.precision == 1) k_bottom_image<1><<<1, BOTTOM_THREADS, P.bottom_smem, s>>>(P.bottom, P.bottom_img);
@@ -1020,7 +1022,7 @@ void mg_build(const MGPlan& P, cudaStream_t s) {
 }
 
 cudaError_t mg_prepare_attributes() {
-    cudaError_t e = cudaFuncSetAttribute(k_coarse_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, (64 * 64 + 64) * 8);
+    cudaError_t e = cudaFuncSetAttribute(k_coarse_invert, cudaFuncAttributeMaxDynamicSharedMemorySize, (64 * 65 + 64) * 8);
     const int bmax = (int)BOTTOM_SMEM_MAX;
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bottom_vcycle<0, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, bmax);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_bottom_vcycle<1, __half>, cudaFuncAttributeMaxDynamicSharedMemorySize, bmax);
