@@ -297,6 +297,17 @@ def run_ours(args):
         bwd(pc)
         ms_f, st_f = timed(pc, reps, fwd)
         ms_b, _ = timed(pc, reps, bwd)
+        # the objective summed over every state of the chain: its backward
+        # pass recomputes each checkpoint segment's states from the checkpoint
+        pc.chain_set_objective("summed")
+        fwd(pc)
+        bwd(pc)
+        ms_fs, _ = timed(pc, reps, fwd)
+        ms_bs, st_bs = timed(pc, reps, bwd)
+        pc.chain_set_objective("final")
+        summed = {"forward_ms": ms_fs / reps, "backward_ms": ms_bs / reps, "backward_over_forward": ms_bs / ms_fs,
+                  "recomputed_steps": steps - (steps + every - 1) // every,
+                  "backward_iterations": st_bs[-1].iterations}
         # a single projection of the same workload for projections/s
         us_c = (ta(c["u"]), ta(c["v"]), ta(c["w"]))
         out_c = tuple(torch.empty_like(x) for x in us_c)
@@ -315,7 +326,7 @@ def run_ours(args):
                 "forward_ms": ms_f / reps, "backward_ms": ms_b / reps, "backward_over_forward": ms_b / ms_f,
                 "projections_per_s": 1000.0 * reps / ms_p, "projection_ms": ms_p / reps,
                 "iterations": st_p[-1].iterations, "true_relative_residual": st_p[-1].true_relative_residual,
-                "device_memory_gb": used / 1e9}
+                "device_memory_gb": used / 1e9, "summed_objective": summed}
 
     def em_leg(n, steps, warm=2):
         """EmState::step on the driven-ring workload (synth.em_ring): the

@@ -189,6 +189,18 @@ int mhdproj_chain_forward(mhdproj_ctx *ctx, const float *u0_x, const float *u0_y
 int mhdproj_chain_backward(mhdproj_ctx *ctx, float *grad_f_x, float *grad_f_y, float *grad_f_z,
                            mhdproj_stats *stats);
 
+/* Objective of the chain for the following mhdproj_chain_forward/backward
+ * calls (resets the differentiable chain).  MHDPROJ_CHAIN_FINAL_OUTLET (the
+ * default): J = sum of w^2 over the outlet faces of the final state; its
+ * adjoint needs no forward state.  MHDPROJ_CHAIN_SUMMED_OUTLET: J = that sum
+ * over the states after every step; the backward pass recomputes each
+ * checkpoint segment's states from its checkpoint (at most
+ * checkpoint_every - 1 forward projections per segment) and keeps a copy of
+ * the force from the forward call.  The reference has no adjoint: this
+ * extends the benchmark spec's outlet-plane objective. */
+enum { MHDPROJ_CHAIN_FINAL_OUTLET = 0, MHDPROJ_CHAIN_SUMMED_OUTLET = 1 };
+int mhdproj_chain_set_objective(mhdproj_ctx *ctx, int kind);
+
 /* Probes used by the tests.  y = A x with the solver's operator (reference:
  * apply() of solver.wgsl:78-92 on the cached coefficients, pinned cells as
  * identity rows); z = M r with the solver's preconditioner (reference: the

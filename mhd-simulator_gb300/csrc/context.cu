@@ -101,6 +101,12 @@ struct mhdproj_ctx {
     int c_steps = 0, c_every = 0;
     float c_dt = 0.f;
     bool c_ready = false;
+    // objective 1 (summed over the chain's states): the force and a working
+    // state kept for the backward pass, and the states of one checkpoint
+    // segment recomputed there
+    int c_objective = 0;
+    float *c_force[3] = {nullptr, nullptr, nullptr}, *c_work[3] = {nullptr, nullptr, nullptr};
+    std::vector<float*> c_segment;
     // fluid step and fields: rollback copies, predicted and viscous velocity,
     // reduction partials, and the last fields pass's CFL inputs
     float *st_prev[3] = {nullptr, nullptr, nullptr}, *st_pred[3] = {nullptr, nullptr, nullptr};
@@ -442,6 +448,7 @@ extern "C" void mhdproj_destroy(mhdproj_ctx* ctx) {
     if (ctx->ref) ref_destroy(ctx->ref);
     for (void* p : ctx->allocs) cudaFree(p);
     for (float* p : ctx->c_checkpoints) cudaFree(p);
+    for (float* p : ctx->c_segment) cudaFree(p);
     if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
     if (ctx->h_flag) cudaFreeHost(ctx->h_flag);
     if (ctx->h_topo) cudaFreeHost(ctx->h_topo);
@@ -1075,6 +1082,39 @@ static int chain_alloc(mhdproj_ctx* ctx) {
     return 0;
 }
 
+// One chain step on the state `cur` in place: u* = u + dt f / rho_face into
+// c_star, then the projection of u* back into `cur`.
+static int chain_step(mhdproj_ctx* ctx, float* const cur[3], const float* fx, const float* fy, const float* fz,
+                      float dt, mhdproj_stats* total) {
+    cudaStream_t s = ctx->stream;
+    Fields F = fields(ctx);
+    launch_add_force(ctx->L, F, cur[0], cur[1], cur[2], fx, fy, fz, dt, ctx->c_star[0], ctx->c_star[1],
+                     ctx->c_star[2], s);
+    mhdproj_stats one{};
+    begin_scalars(ctx);
+    launch_rhs(ctx->L, F, ctx->c_star[0], ctx->c_star[1], ctx->c_star[2], s);
+    CK(cudaMemsetAsync(ctx->phi_hi, 0, ctx->n * 4, s));
+    CK(cudaMemsetAsync(ctx->phi_lo, 0, ctx->n * 4, s));
+    int rc = solve(ctx, ctx->phi_hi, ctx->phi_lo, &one);
+    if (rc) return rc;
+    launch_correct(ctx->L, F, ctx->phi_hi, ctx->phi_lo, ctx->c_star[0], ctx->c_star[1], ctx->c_star[2], cur[0], cur[1],
+                   cur[2], nullptr, dt, s);
+    total->iterations += one.iterations;
+    total->refinements += one.refinements;
+    total->true_relative_residual = std::max(total->true_relative_residual, one.true_relative_residual);
+    return 0;
+}
+
+extern "C" int mhdproj_chain_set_objective(mhdproj_ctx* ctx, int kind) {
+    if (!ctx) return MHDPROJ_ERR_INVALID;
+    if (ctx->ref) return fail(ctx, MHDPROJ_ERR_INVALID, "the chained adjoint is part of the GB300 solver");
+    if (kind != MHDPROJ_CHAIN_FINAL_OUTLET && kind != MHDPROJ_CHAIN_SUMMED_OUTLET)
+        return fail(ctx, MHDPROJ_ERR_INVALID, "unknown chain objective (0: final outlet plane, 1: summed over the steps)");
+    ctx->c_objective = kind;
+    ctx->c_steps = 0;  // a chain run under the other objective is not differentiated
+    return 0;
+}
+
 extern "C" int mhdproj_chain_forward(mhdproj_ctx* ctx, const float* u0x, const float* u0y, const float* u0z,
                                      const float* fx, const float* fy, const float* fz, float dt, int steps,
                                      int checkpoint_every, float* ufx, float* ufy, float* ufz, double* objective,
@@ -1087,6 +1127,7 @@ extern "C" int mhdproj_chain_forward(mhdproj_ctx* ctx, const float* u0x, const f
     if (ctx->meanfree) return fail(ctx, MHDPROJ_ERR_INVALID, MEANFREE_ADJOINT);
     int rc = chain_alloc(ctx);
     if (rc) return rc;
+    ctx->c_steps = 0;  // differentiable again once this chain has finished
     const long long m[3] = {ctx->nfx, ctx->nfy, ctx->nfz};
     const float* u0[3] = {u0x, u0y, u0z};
     cudaStream_t s = ctx->stream;
@@ -1099,6 +1140,18 @@ extern "C" int mhdproj_chain_forward(mhdproj_ctx* ctx, const float* u0x, const f
         CK(cudaMalloc(&p, m[a] * 4));
         ctx->c_checkpoints.push_back(p);
     }
+    const bool summed = ctx->c_objective == MHDPROJ_CHAIN_SUMMED_OUTLET;
+    if (summed) {
+        // the backward pass recomputes states from the checkpoints with this force
+        for (int a = 0; a < 3; a++)
+            if (!ctx->c_force[a]) {
+                CK(dalloc(ctx, &ctx->c_force[a], m[a] * 4));
+                CK(dalloc(ctx, &ctx->c_work[a], m[a] * 4));
+            }
+        const float* f[3] = {fx, fy, fz};
+        for (int a = 0; a < 3; a++) CK(cudaMemcpyAsync(ctx->c_force[a], f[a], m[a] * 4, cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemsetAsync(reinterpret_cast<char*>(ctx->sc) + offsetof(Scalars, objective), 0, sizeof(double), s));
+    }
     CK(cudaEventRecord(ctx->ev_a, s));
     Fields F = fields(ctx);
     mhdproj_stats total{};
@@ -1108,22 +1161,12 @@ extern "C" int mhdproj_chain_forward(mhdproj_ctx* ctx, const float* u0x, const f
             for (int a = 0; a < 3; a++)
                 CK(cudaMemcpyAsync(ctx->c_checkpoints[3 * c + a], ctx->c_cur[a], m[a] * 4, cudaMemcpyDeviceToDevice, s));
         }
-        launch_add_force(ctx->L, F, ctx->c_cur[0], ctx->c_cur[1], ctx->c_cur[2], fx, fy, fz, dt, ctx->c_star[0],
-                         ctx->c_star[1], ctx->c_star[2], s);
-        mhdproj_stats one{};
-        begin_scalars(ctx);
-        launch_rhs(ctx->L, F, ctx->c_star[0], ctx->c_star[1], ctx->c_star[2], s);
-        CK(cudaMemsetAsync(ctx->phi_hi, 0, ctx->n * 4, s));
-        CK(cudaMemsetAsync(ctx->phi_lo, 0, ctx->n * 4, s));
-        rc = solve(ctx, ctx->phi_hi, ctx->phi_lo, &one);
+        rc = chain_step(ctx, ctx->c_cur, fx, fy, fz, dt, &total);
         if (rc) return rc;
-        launch_correct(ctx->L, F, ctx->phi_hi, ctx->phi_lo, ctx->c_star[0], ctx->c_star[1], ctx->c_star[2], ctx->c_cur[0],
-                       ctx->c_cur[1], ctx->c_cur[2], nullptr, dt, s);
-        total.iterations += one.iterations;
-        total.refinements += one.refinements;
-        total.true_relative_residual = std::max(total.true_relative_residual, one.true_relative_residual);
+        // objective 1: the outlet term of every state after a step
+        if (summed) launch_outlet_objective(ctx->L, F, ctx->c_cur[2], nullptr, s, true);
     }
-    launch_outlet_objective(ctx->L, F, ctx->c_cur[2], nullptr, s);
+    if (!summed) launch_outlet_objective(ctx->L, F, ctx->c_cur[2], nullptr, s);
     CK(cudaGetLastError());
     CK(cudaEventRecord(ctx->ev_b, s));
     rc = read_scalars(ctx);
@@ -1163,7 +1206,9 @@ extern "C" int mhdproj_chain_backward(mhdproj_ctx* ctx, float* gfx, float* gfy, 
     mhdproj_stats total{};
     float* lam[3] = {ctx->c_lam[0], ctx->c_lam[1], ctx->c_lam[2]};
     float* nxt[3] = {ctx->c_lam2[0], ctx->c_lam2[1], ctx->c_lam2[2]};
-    for (int k = ctx->c_steps - 1; k >= 0; k--) {
+    // lambda <- P^T lambda (the VJP of step k's projection) and dJ/df +=
+    // dt / rho_face times it
+    auto adjoint_step = [&]() -> int {
         mhdproj_stats one{};
         int rc = vjp_gb300(ctx, lam[0], lam[1], lam[2], nullptr, ctx->c_dt, nxt[0], nxt[1], nxt[2], &one);
         if (rc) return rc;
@@ -1174,6 +1219,45 @@ extern "C" int mhdproj_chain_backward(mhdproj_ctx* ctx, float* gfx, float* gfy, 
         total.iterations += one.iterations;
         total.refinements += one.refinements;
         total.true_relative_residual = std::max(total.true_relative_residual, one.true_relative_residual);
+        return 0;
+    };
+    if (ctx->c_objective != MHDPROJ_CHAIN_SUMMED_OUTLET) {
+        // J depends on the final state only: the adjoint steps need no
+        // forward state (the projection's VJP does not depend on it)
+        for (int k = ctx->c_steps - 1; k >= 0; k--)
+            if (int rc = adjoint_step()) return rc;
+    } else {
+        // J sums the outlet term of every state u_1 .. u_K, so step k's
+        // adjoint adds 2 w_k on the outlet faces: the states of each
+        // checkpoint segment are recomputed from its checkpoint (at most
+        // checkpoint_every - 1 forward steps per segment), last segment first
+        const int K = ctx->c_steps, every = ctx->c_every;
+        const int nck = (K + every - 1) / every;
+        while ((int)ctx->c_segment.size() < 3 * (every - 1)) {
+            float* p = nullptr;
+            const int a = (int)ctx->c_segment.size() % 3;
+            CK(cudaMalloc(&p, m[a] * 4));
+            ctx->c_segment.push_back(p);
+        }
+        const float* fo[3] = {ctx->c_force[0], ctx->c_force[1], ctx->c_force[2]};
+        for (int j = nck - 1; j >= 0; j--) {
+            const int s0 = j * every, e0 = std::min(K, s0 + every);
+            for (int a = 0; a < 3; a++)
+                CK(cudaMemcpyAsync(ctx->c_work[a], ctx->c_checkpoints[3 * j + a], m[a] * 4, cudaMemcpyDeviceToDevice, s));
+            for (int k = s0; k + 1 < e0; k++) {  // u_{k+1} into segment slot k - s0
+                if (int rc = chain_step(ctx, ctx->c_work, fo[0], fo[1], fo[2], ctx->c_dt, &total)) return rc;
+                for (int a = 0; a < 3; a++)
+                    CK(cudaMemcpyAsync(ctx->c_segment[3 * (k - s0) + a], ctx->c_work[a], m[a] * 4,
+                                       cudaMemcpyDeviceToDevice, s));
+            }
+            for (int k = e0 - 1; k >= s0; k--) {
+                if (int rc = adjoint_step()) return rc;
+                if (k >= 1 && ctx->outlet) {
+                    const float* wk = k == s0 ? ctx->c_checkpoints[3 * j + 2] : ctx->c_segment[3 * (k - s0 - 1) + 2];
+                    launch_outlet_objective(ctx->L, F, wk, lam[2], s, false, true);
+                }
+            }
+        }
     }
     float* out[3] = {gfx, gfy, gfz};
     for (int a = 0; a < 3; a++) k_d2f<<<152 * 4, 256, 0, s>>>(ctx->c_grad[a], out[a], m[a]);

@@ -951,10 +951,12 @@ __global__ void __launch_bounds__(TILE_THREADS) k_force_grad(Grid3 g, int outlet
         }
     }
 }
-// J = sum over outlet faces of w^2 (into sc->objective); seed_w = 2 w there.
+// J = sum over outlet faces of w^2 (into sc->objective, or added to it when
+// `accumulate`); seed_w = 2 w there (added to seed_w when `add_seed`).
 __global__ void __launch_bounds__(TILE_THREADS) k_outlet_objective(Grid3 g, const float* __restrict__ w,
                                                                    float* __restrict__ seed_w, Scalars* sc,
-                                                                   double* partials, int nblocks) {
+                                                                   double* partials, int nblocks, int accumulate,
+                                                                   int add_seed) {
     __shared__ double sh[8 * 1];
     double acc[1] = {0.0};
     const int x = blockIdx.x * TX + threadIdx.x;
@@ -963,13 +965,13 @@ __global__ void __launch_bounds__(TILE_THREADS) k_outlet_objective(Grid3 g, cons
         const int ft = x + g.nx * (y + g.ny * g.nz);
         const double wz = w[ft];
         acc[0] = wz * wz;
-        if (seed_w) seed_w[ft] = (float)(2.0 * wz);
+        if (seed_w) seed_w[ft] = add_seed ? seed_w[ft] + (float)(2.0 * wz) : (float)(2.0 * wz);
     }
     block_sum<1>(acc, sh);
     if (store_partials_is_last<1>(acc, partials, nblocks, &sc->ticket[6])) {
         double tot[1];
         finish_partials<1>(tot, partials, nblocks, sh, &sc->ticket[6]);
-        if (threadIdx.x == 0 && threadIdx.y == 0) sc->objective = tot[0];
+        if (threadIdx.x == 0 && threadIdx.y == 0) sc->objective = accumulate ? sc->objective + tot[0] : tot[0];
     }
 }
 
@@ -1100,9 +1102,11 @@ void launch_force_grad(const Launch& L, const Fields& F, const float* lu, const 
     k_force_grad<<<L.grid, L.block, 0, s>>>(L.g, F.outlet, F.rho_l, F.rho_air, F.cls, F.alpha, lu, lv, lw, dt, gu, gv,
                                             gw);
 }
-void launch_outlet_objective(const Launch& L, const Fields& F, const float* w, float* seed_w, cudaStream_t s) {
+void launch_outlet_objective(const Launch& L, const Fields& F, const float* w, float* seed_w, cudaStream_t s,
+                             bool accumulate, bool add_seed) {
     dim3 grid(L.grid.x, L.grid.y, 1);
-    k_outlet_objective<<<grid, L.block, 0, s>>>(L.g, w, seed_w, F.sc, F.partials, (int)(grid.x * grid.y));
+    k_outlet_objective<<<grid, L.block, 0, s>>>(L.g, w, seed_w, F.sc, F.partials, (int)(grid.x * grid.y),
+                                                accumulate ? 1 : 0, add_seed ? 1 : 0);
 }
 
 }  // namespace mhdproj

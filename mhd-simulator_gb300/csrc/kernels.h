@@ -66,7 +66,10 @@ void launch_add_force(const Launch& L, const Fields& F, const float* u, const fl
                       cudaStream_t s);
 void launch_force_grad(const Launch& L, const Fields& F, const float* lu, const float* lv, const float* lw, float dt,
                        double* gu, double* gv, double* gw, cudaStream_t s);
-void launch_outlet_objective(const Launch& L, const Fields& F, const float* w, float* seed_w, cudaStream_t s);
+// J = sum of w^2 over the outlet faces into the scalars (added to them when
+// `accumulate`); seed_w = 2 w on those faces (added when `add_seed`).
+void launch_outlet_objective(const Launch& L, const Fields& F, const float* w, float* seed_w, cudaStream_t s,
+                             bool accumulate = false, bool add_seed = false);
 
 // ---- finest-level kernels with shared-memory plane staging (fine_kernels.cu)
 void launch_spmv_staged(const Launch& L, const Fields& F, cudaStream_t s);

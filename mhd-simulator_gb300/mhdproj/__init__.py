@@ -139,6 +139,7 @@ def load():
     L.mhdproj_chain_forward.argtypes = [_vp] + [_vp] * 6 + [C.c_float, C.c_int, C.c_int] + [_vp] * 3 + [
         C.POINTER(C.c_double), C.POINTER(Stats)]
     L.mhdproj_chain_backward.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(Stats)]
+    L.mhdproj_chain_set_objective.argtypes = [_vp, C.c_int]
     L.mhdproj_apply_operator.argtypes = [_vp, _vp, _vp]
     L.mhdproj_apply_preconditioner.argtypes = [_vp, _vp, _vp]
     L.mhdproj_copy_coefficients.argtypes = [_vp, _vp]
@@ -185,7 +186,8 @@ def load():
 EXPORTED = [
     "mhdproj_default_options", "mhdproj_create", "mhdproj_destroy", "mhdproj_last_error", "mhdproj_set_stream",
     "mhdproj_set_coefficients", "mhdproj_set_phase_drag", "mhdproj_project", "mhdproj_project_host",
-    "mhdproj_project_vjp", "mhdproj_chain_forward", "mhdproj_chain_backward", "mhdproj_apply_operator",
+    "mhdproj_project_vjp", "mhdproj_chain_forward", "mhdproj_chain_backward", "mhdproj_chain_set_objective",
+    "mhdproj_apply_operator",
     "mhdproj_apply_preconditioner", "mhdproj_copy_coefficients", "mhdproj_copy_potential", "mhdproj_copy_topology",
     "mhdproj_hierarchy", "mhdproj_anchors", "mhdproj_profile_kernels", "mhdproj_divergence_noalloc",
     "mhdproj_kernel_launches", "mhdproj_fields", "mhdproj_fluid_step", "mhdproj_export_fields",
@@ -423,6 +425,16 @@ class PressureProjection:
                                                     steps, checkpoint_every, *[_ptr(t) for t in uf], C.byref(J),
                                                     C.byref(st)))
         return uf, J.value, st
+
+    CHAIN_OBJECTIVES = {"final": 0, "summed": 1}
+
+    def chain_set_objective(self, kind):
+        """'final': J = sum of w^2 over the outlet faces of the final state
+        (the default); 'summed': that sum over the states after every step,
+        whose backward pass recomputes the states between checkpoints."""
+        if kind not in self.CHAIN_OBJECTIVES:
+            raise ValueError(f"chain objective must be one of {sorted(self.CHAIN_OBJECTIVES)}")
+        self._check(self._lib.mhdproj_chain_set_objective(self._ctx, self.CHAIN_OBJECTIVES[kind]))
 
     def chain_backward(self, like):
         self._order()

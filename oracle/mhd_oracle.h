@@ -211,6 +211,11 @@ int onat_chain_forward(const onat_grid *g, const float *alpha, const uint8_t *so
 int onat_chain_adjoint(const onat_grid *g, const float *alpha, const uint8_t *solid,
                        const double *uk, const double *vk, const double *wk, float dt, int steps,
                        double rtol, double *gfu, double *gfv, double *gfw);
+/* The same chain with J = sum over the states u_1 .. u_K of the outlet term
+ * (all states kept in FP64); dJ/df into gf* when they are not NULL. */
+int onat_chain_summed(const onat_grid *g, const float *alpha, const uint8_t *solid, const float *u0,
+                      const float *v0, const float *w0, const float *fu, const float *fv, const float *fw, float dt,
+                      int steps, double rtol, double *objective, double *gfu, double *gfv, double *gfw);
 
 /* phase / surface passes (src/fluid/phase.wgsl:10-31): mobility mask and
  * FluidCell.reserved lanes; returns the changed flags (bit 0 mobility, bit 1

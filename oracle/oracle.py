@@ -151,6 +151,8 @@ def lib():
                                          C.c_int, C.c_double, _f64p, _f64p, _f64p, C.POINTER(C.c_double)]
         L.onat_chain_adjoint.argtypes = [g, _f32p, _u8p, _f64p, _f64p, _f64p, C.c_float, C.c_int, C.c_double,
                                          _f64p, _f64p, _f64p]
+        L.onat_chain_summed.argtypes = [g, _f32p, _u8p, _f32p, _f32p, _f32p, _f32p, _f32p, _f32p, C.c_float, C.c_int,
+                                        C.c_double, C.POINTER(C.c_double), C.c_void_p, C.c_void_p, C.c_void_p]
         L.oref_classify_cells.argtypes = [C.c_uint32, _u32p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
                                           C.c_uint32, _u32p, _f32p]
         L.oref_classify_cells.restype = C.c_uint32
@@ -415,6 +417,20 @@ def chain_adjoint(g, alpha, solid, uk, vk, wk, dt, steps, rtol=1e-13):
     st = lib().onat_chain_adjoint(C.byref(g), f(alpha), np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1),
                                   d(uk), d(vk), d(wk), dt, steps, rtol, gu, gv, gw)
     return st, (gu, gv, gw)
+
+
+def chain_summed(g, alpha, solid, u0, v0, w0, fu, fv, fw, dt, steps, gradient=True, rtol=1e-13):
+    """The chain with J summed over the states after every step (FP64):
+    returns (status, J, (gu, gv, gw) or None)."""
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+    su, sv, sw = face_shapes(g)
+    grads = [np.zeros(int(np.prod(s))) for s in (su, sv, sw)] if gradient else None
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p) if a is not None else None
+    J = C.c_double()
+    st = lib().onat_chain_summed(C.byref(g), f(alpha), np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1),
+                                 f(u0), f(v0), f(w0), f(fu), f(fv), f(fw), dt, steps, rtol, C.byref(J),
+                                 *([ptr(x) for x in grads] if grads else [None, None, None]))
+    return st, J.value, (tuple(grads) if grads else None)
 
 
 def classify_cells(materials, liquid_material, mask, cells, thermal=None, thermal_stride=1, interface=None,

@@ -800,3 +800,78 @@ int onat_chain_adjoint(const onat_grid *g, const float *alpha, const uint8_t *so
     release(&P);
     return st;
 }
+
+/* Summed outlet objective: every state after a step contributes, so the
+ * adjoint of step k adds 2 w_k on the outlet faces to lambda before the VJP
+ * of step k-1.  Test oracle for the GPU chain's checkpoint recompute. */
+int onat_chain_summed(const onat_grid *g, const float *alpha, const uint8_t *solid, const float *u0,
+                      const float *v0, const float *w0, const float *fu, const float *fv, const float *fw, float dt,
+                      int steps, double rtol, double *objective, double *gfu, double *gfv, double *gfw) {
+    const uint64_t m[3] = {faces_of(g, 0), faces_of(g, 1), faces_of(g, 2)};
+    const uint64_t n = (uint64_t)g->nx * g->ny * g->nz;
+    const uint64_t top = (uint64_t)g->nx * g->ny * g->nz;  /* first outlet w face */
+    const uint64_t plane = (uint64_t)g->nx * g->ny;
+    prepared P;
+    prepare(g, alpha, solid, &P);
+    /* states[k][a]: u_k, k = 0 .. steps */
+    double **states = (double **)malloc((size_t)(steps + 1) * 3 * sizeof(double *));
+    const float *init[3] = {u0, v0, w0}, *force[3] = {fu, fv, fw};
+    double *star[3];
+    for (int a = 0; a < 3; a++) {
+        states[a] = to_double(init[a], m[a]);
+        star[a] = (double *)malloc(m[a] * sizeof(double));
+    }
+    double *phi = (double *)malloc(n * sizeof(double));
+    int st = 0;
+    double J = 0.0;
+    for (int k = 0; k < steps; k++) {
+        double **cur = states + 3 * k, **nx_ = states + 3 * (k + 1);
+        for (int a = 0; a < 3; a++) {
+            nx_[a] = (double *)malloc(m[a] * sizeof(double));
+            memcpy(star[a], cur[a], m[a] * sizeof(double));
+            for (uint64_t f = 0; f < m[a]; f++) {
+                oface o;
+                if (!face_info(g, alpha, P.cls, P.gtop, a, f, &o) || o.duplicate) continue;
+                star[a][o.fc] = cur[a][o.fc] + (double)dt * (double)force[a][o.fc] / face_density_of(g, alpha, &o);
+            }
+        }
+        int it;
+        double rel;
+        st |= project_d(g, alpha, solid, star[0], star[1], star[2], dt, rtol, phi, nx_[0], nx_[1], nx_[2], NULL, &it,
+                        &rel);
+        if (outlet_on(g))
+            for (uint64_t f = 0; f < plane; f++) J += nx_[2][top + f] * nx_[2][top + f];
+    }
+    *objective = J;
+    if (gfu && gfv && gfw) {
+        double *lam[3], *nxt[3], *gf[3] = {gfu, gfv, gfw};
+        for (int a = 0; a < 3; a++) {
+            lam[a] = (double *)calloc(m[a], sizeof(double));
+            nxt[a] = (double *)calloc(m[a], sizeof(double));
+            memset(gf[a], 0, m[a] * sizeof(double));
+        }
+        if (outlet_on(g))
+            for (uint64_t f = 0; f < plane; f++) lam[2][top + f] = 2.0 * states[3 * steps + 2][top + f];
+        for (int k = steps - 1; k >= 0; k--) {
+            st |= onat_project_vjp(g, alpha, solid, lam[0], lam[1], lam[2], NULL, dt, rtol, nxt[0], nxt[1], nxt[2]);
+            for (int a = 0; a < 3; a++) {
+                memcpy(lam[a], nxt[a], m[a] * sizeof(double));
+                for (uint64_t f = 0; f < m[a]; f++) {
+                    oface o;
+                    if (!face_info(g, alpha, P.cls, P.gtop, a, f, &o) || o.duplicate) continue;
+                    gf[a][o.fc] += (double)dt / face_density_of(g, alpha, &o) * lam[a][o.fc];
+                }
+            }
+            if (k >= 1 && outlet_on(g))
+                for (uint64_t f = 0; f < plane; f++) lam[2][top + f] += 2.0 * states[3 * k + 2][top + f];
+        }
+        for (int a = 0; a < 3; a++) { free(lam[a]); free(nxt[a]); }
+    }
+    for (int k = 0; k <= steps; k++)
+        for (int a = 0; a < 3; a++) free(states[3 * k + a]);
+    free(states);
+    for (int a = 0; a < 3; a++) free(star[a]);
+    free(phi);
+    release(&P);
+    return st;
+}

@@ -276,6 +276,61 @@ def test_chain_gradient_full_size_16_directions(gpu):
     assert worst < 1e-4, worst
 
 
+def test_chain_summed_objective_recomputes_from_checkpoints(gpu, oracle_lib):
+    """The chain objective summed over the states after every step.  Its
+    backward pass needs every forward state, so it recomputes each checkpoint
+    segment's states from its checkpoint (8 steps, checkpoints every 3: a
+    ragged last segment).  J and dJ/df match the FP64 oracle, the gradient
+    matches central differences of the oracle's summed chain, the backward
+    pass runs the recomputed projections on top of the adjoint solves, and
+    switching back restores the final-state objective."""
+    import mhdproj
+
+    torch = gpu
+    c = synth.make_case("adjoint128", scale=0.25)
+    pr = make(mhdproj, c, precision="fp16", rel_tol=1e-9)
+    a, s, us = tensors(torch, c)
+    pr.set_coefficients(a, s, c["rho_liquid"], c["rho_air"])
+    f = tuple(torch.from_numpy(x).cuda() for x in (c["fu"], c["fv"], c["fw"]))
+    steps, every = c["steps"], 3
+    g = ogrid(oracle_lib, c)
+    args = (g, c["alpha"], c["solid"], c["u"], c["v"], c["w"])
+    _, _, st_f = pr.chain_forward(us, f, c["dt"], steps, every)
+    _, st_fb = pr.chain_backward(us)
+    pr.chain_set_objective("summed")
+    with pytest.raises(mhdproj.ProjectionError):
+        pr.chain_backward(us)  # a new objective needs a new forward chain
+    _, J, st = pr.chain_forward(us, f, c["dt"], steps, every)
+    grad, st2 = pr.chain_backward(us)
+    _, Jo, go = oracle_lib.chain_summed(*args, c["fu"], c["fv"], c["fw"], c["dt"], steps)
+    assert abs(J - Jo) <= 1e-5 * abs(Jo)
+    for x, y in zip(grad, go):
+        assert rel_l2(x.cpu().numpy(), y) < 1e-4
+    # steps - checkpoints forward projections recomputed on top of the adjoint solves
+    assert st2.iterations > st_fb.iterations
+    rng = np.random.default_rng(23)
+    fo = (c["fu"], c["fv"], c["fw"])
+    fn = math.sqrt(sum(float((x.astype(np.float64) ** 2).sum()) for x in fo))
+    for _ in range(2):
+        d = [rng.standard_normal(x.shape) for x in fo]
+        dn = math.sqrt(sum(float((x ** 2).sum()) for x in d))
+        eps = 1e-3 * fn / dn
+        fp = [(x + eps * y).astype(np.float32) for x, y in zip(fo, d)]
+        fm = [(x - eps * y).astype(np.float32) for x, y in zip(fo, d)]
+        _, Jp, _ = oracle_lib.chain_summed(*args, *fp, c["dt"], steps, gradient=False)
+        _, Jm, _ = oracle_lib.chain_summed(*args, *fm, c["dt"], steps, gradient=False)
+        fd = (Jp - Jm) / (2 * eps)
+        ad = sum(float((x.cpu().numpy().astype(np.float64) * y).sum()) for x, y in zip(grad, d))
+        assert abs(fd - ad) <= 1e-4 * abs(fd)
+    pr.chain_set_objective("final")
+    _, J2, _ = pr.chain_forward(us, f, c["dt"], steps, every)
+    _, Jo2, _ = oracle_lib.chain_forward(*args, c["fu"], c["fv"], c["fw"], c["dt"], steps)
+    assert abs(J2 - Jo2) <= 1e-5 * abs(Jo2)
+    with pytest.raises(ValueError):
+        pr.chain_set_objective("mean")
+    pr.close()
+
+
 def test_failures_leave_outputs_untouched(gpu):
     import mhdproj
 

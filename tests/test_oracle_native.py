@@ -89,3 +89,33 @@ def test_chain_adjoint_matches_central_differences(oracle_lib):
         fd = (Jp - Jm) / (2 * eps)
         ad = sum(float(np.dot(gg, dd.reshape(-1))) for gg, dd in zip(grad, d))
         assert abs(fd - ad) <= 1e-4 * abs(ad)
+
+
+def test_summed_chain_adjoint_matches_central_differences(oracle_lib):
+    """The chain objective summed over the states after every step: for one
+    step it is the final-state objective, and its adjoint (which adds 2 w_k on
+    the outlet faces after each step's VJP) matches central differences."""
+    c = synth.make_case("adjoint128", scale=0.125)
+    g = grid_of(oracle_lib, c)
+    args = (g, c["alpha"], c["solid"], c["u"], c["v"], c["w"])
+    f = [c["fu"], c["fv"], c["fw"]]
+    _, J1, _ = oracle_lib.chain_forward(*args, *f, c["dt"], 1)
+    _, S1, _ = oracle_lib.chain_summed(*args, *f, c["dt"], 1, gradient=False)
+    assert S1 == pytest.approx(J1, rel=1e-14)
+    steps = 3
+    st, J, grad = oracle_lib.chain_summed(*args, *f, c["dt"], steps)
+    _, Jf, _ = oracle_lib.chain_forward(*args, *f, c["dt"], steps)
+    assert st == 0 and J > Jf
+    rng = np.random.default_rng(6)
+    fn = np.sqrt(sum(float((x.astype(np.float64) ** 2).sum()) for x in f))
+    for _ in range(2):
+        d = [rng.standard_normal(x.shape) for x in f]
+        dn = np.sqrt(sum(float((x ** 2).sum()) for x in d))
+        eps = 1e-3 * fn / dn
+        fp = [(x + eps * y).astype(np.float32) for x, y in zip(f, d)]
+        fm = [(x - eps * y).astype(np.float32) for x, y in zip(f, d)]
+        _, Jp, _ = oracle_lib.chain_summed(*args, *fp, c["dt"], steps, gradient=False)
+        _, Jm, _ = oracle_lib.chain_summed(*args, *fm, c["dt"], steps, gradient=False)
+        fd = (Jp - Jm) / (2 * eps)
+        ad = sum(float(np.dot(gg, dd.reshape(-1))) for gg, dd in zip(grad, d))
+        assert abs(fd - ad) <= 1e-4 * abs(ad)
