@@ -357,11 +357,15 @@ __global__ void __launch_bounds__(TILE_THREADS) k_search_spmv(Grid3 g, const flo
             }
         }
     }
+    // q stage: thread tx takes cells x0+tx and x0+tx+32 of row ty, so every
+    // shared-memory read of a warp is unit-stride (adjacent cell pairs made
+    // the float4 records two-way and their neighbour-face lanes eight-way
+    // bank conflicts)
     Acc acc;
-    const int ox = x0 + 2 * tx, oy = y0 + ty;
-    const bool own_inside = ox < g.nx && oy < g.ny;
-    const int oo = (ty + 1) * SW + 4 + 2 * tx, co = ty * CW + 2 * tx;
-    const long long og = ox + (long long)g.nx * oy;
+    const int oy = y0 + ty;
+    const bool own_row = oy < g.ny;
+    const int oo = (ty + 1) * SW + 4 + tx, co = ty * CW + tx;
+    const long long og = x0 + tx + (long long)g.nx * oy;
     auto step = [&](auto ph, int zA) {
         constexpr int P = decltype(ph)::value;
         fetch(zA + 1, (P + 1) & 1, (P + 1) & 3);
@@ -399,16 +403,16 @@ __global__ void __launch_bounds__(TILE_THREADS) k_search_spmv(Grid3 g, const flo
         }
         __syncthreads();
         const int z = zA - 1;
-        if (z >= z0 && z < z1 && own_inside) {
+        if (z >= z0 && z < z1 && own_row) {
             const float* Pc = &S.pn[(P + 3) & 3][0][0];
             const float* PM = &S.pn[(P + 2) & 3][0][0];
             const float* PP = &S.pn[P][0][0];
             const float4* C = &S.c[(P + 3) & 3][0][0];
             const float4* CN = &S.c[P][0][0];
-            float qv[2];
 #pragma unroll
             for (int k = 0; k < 2; k++) {
-                const int o = oo + k, c = co + k;
+                if (x0 + tx + 32 * k >= g.nx) break;
+                const int o = oo + 32 * k, c = co + 32 * k;
                 const float4 cc = C[c];
                 const float bxh = C[c + 1].x, byh = C[c + CW].y, bzh = CN[c].z;
                 const float pc = Pc[o];
@@ -419,10 +423,9 @@ __global__ void __launch_bounds__(TILE_THREADS) k_search_spmv(Grid3 g, const flo
                 v = fmaf(byh, pc - Pc[o + SW], v);
                 v = fmaf(cc.z, pc - PM[o], v);
                 v = fmaf(bzh, pc - PP[o], v);
-                qv[k] = v;
+                q[og + 32 * k + sxy * z] = v;
                 acc.add_prod(pc, v);
             }
-            *reinterpret_cast<float2*>(q + og + sxy * z) = make_float2(qv[0], qv[1]);
         }
         __syncthreads();
     };
