@@ -93,3 +93,15 @@ def test_em_create_without_gpu_fails_loudly(lib):
         pytest.skip("a GPU is present")
     with pytest.raises(Exception):
         mhdproj.EmInduction((8, 8, 8), 1e-3)
+
+
+def test_chain_objective_names_match_the_header():
+    """The Python objective names map to the header's MHDPROJ_CHAIN_* values."""
+    import mhdproj
+
+    with open(os.path.join(ROOT, "include", "mhdproj.h")) as f:
+        text = f.read()
+    values = {m.group(1): int(m.group(2)) for m in re.finditer(r"MHDPROJ_CHAIN_(\w+) = (\d+)", text)}
+    assert values == {"FINAL_OUTLET": 0, "SUMMED_OUTLET": 1}
+    names = mhdproj.PressureProjection.CHAIN_OBJECTIVES
+    assert names["final"] == values["FINAL_OUTLET"] and names["summed"] == values["SUMMED_OUTLET"]
