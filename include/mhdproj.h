@@ -196,8 +196,8 @@ int mhdproj_chain_backward(mhdproj_ctx *ctx, float *grad_f_x, float *grad_f_y, f
  * over the states after every step; the backward pass recomputes each
  * checkpoint segment's states from its checkpoint (at most
  * checkpoint_every - 1 forward projections per segment) and keeps a copy of
- * the force from the forward call.  The reference has no adjoint: this
- * extends the benchmark spec's outlet-plane objective. */
+ * the force from the forward call.  The reference has no adjoint: both
+ * objectives are additions of this library. */
 enum { MHDPROJ_CHAIN_FINAL_OUTLET = 0, MHDPROJ_CHAIN_SUMMED_OUTLET = 1 };
 int mhdproj_chain_set_objective(mhdproj_ctx *ctx, int kind);
 
